@@ -1,0 +1,103 @@
+#pragma once
+/*
+ * GB300 extensions to the LibRPA C API.
+ *
+ * Everything here is additive: none of it exists in LibRPA, and a caller that
+ * uses only librpa.h keeps the reference's behaviour.  Knobs that LibRPA does
+ * not have (precision mode, block screening, learned screening) live in
+ * LibrpaGB300Options instead of LibrpaOptions, whose layout is frozen by the
+ * Fortran binding.
+ */
+#include "librpa_handler.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* chi0 contraction precision */
+#define LIBRPA_GB300_CHI0_FP64 0      /* plain FP64 SIMT kernels (reference-precision GPU path) */
+#define LIBRPA_GB300_CHI0_BF16X3 1    /* 3-term BF16 split products on tcgen05, FP32 accumulate in TMEM */
+#define LIBRPA_GB300_CHI0_FP32 2      /* FP32 SIMT kernels (diagnostic middle ground) */
+
+/* E_c kernel path */
+#define LIBRPA_GB300_EC_LU_FP64 0     /* Pi = V chi0 in FP64, FP64 LU, sum log(+-u_ii) (LibRPA form) */
+#define LIBRPA_GB300_EC_CHOL 1        /* L^H chi0 L split-precision GEMMs, FP64 Cholesky */
+
+/* block screening of chi0 contributions */
+#define LIBRPA_GB300_SCREEN_OFF 0
+#define LIBRPA_GB300_SCREEN_THRESHOLD 1   /* drop (I,J,R) blocks whose bound is below the threshold */
+#define LIBRPA_GB300_SCREEN_MLP 2         /* learned predictor + random audit, threshold as judge */
+
+typedef struct
+{
+    int chi0_precision;      /* LIBRPA_GB300_CHI0_*   (default BF16X3) */
+    int ec_path;             /* LIBRPA_GB300_EC_*     (default CHOL)   */
+    int screen_mode;         /* LIBRPA_GB300_SCREEN_* (default OFF)    */
+    double screen_threshold; /* block-norm threshold for screening (default 1e-6) */
+    double audit_fraction;   /* share of skipped blocks computed exactly (default 0.02) */
+    unsigned long long seed; /* audit sampling seed */
+    int use_cuda_graph;      /* capture the per-tau launch sequence once and replay it (default 1) */
+    int keep_chi0;           /* keep chi0(q, omega) on the device for librpa_gb300_get_chi0_block */
+    int device;              /* CUDA device ordinal (default 0) */
+    int reuse_device_inputs; /* keep the staged inputs on the device between calls while no
+                                librpa_set_* call changed them (default 1); 0 re-uploads every call */
+} LibrpaGB300Options;
+
+/* Timing and work counters of the last librpa_get_rpa_correlation_energy call. */
+typedef struct
+{
+    double t_total;        /* wall seconds of the whole call */
+    double t_grids;        /* minimax grid set-up (host) */
+    double t_upload;       /* host -> device staging of the dataset */
+    double t_gf;           /* G(R, +-tau) build (device) */
+    double t_chi0;         /* chi0(R, tau) contraction (device) */
+    double t_ftct;         /* R->q Fourier and tau->omega cosine transform (device) */
+    double t_ec;           /* Pi / log-det / trace (device) */
+    double chi0_flops;     /* FLOPs executed by the chi0 contraction kernels (useful work, split terms not counted) */
+    double chi0_flops_libri; /* FLOPs the LibRI loop order would spend on the same blocks */
+    double ec_flops;       /* FLOPs of the E_c stage */
+    double gf_flops;       /* FLOPs of the G build */
+    double ftct_bytes;     /* algorithmic bytes of the FT/CT kernels */
+    long long n_launches;  /* kernels launched by this library during the call */
+    long long blocks_total;     /* (I<=J, R) chi0 blocks in the problem */
+    long long blocks_computed;  /* blocks actually contracted */
+    long long blocks_audited;   /* skipped-by-predictor blocks computed for the audit */
+    double audit_max_dropped;   /* largest block norm among audited skipped blocks */
+    double dt_chi0_kernel_ms;   /* CUDA-event time of the dominant chi0 kernel, summed over launches */
+    long long n_chi0_kernel;    /* launches of the dominant chi0 kernel */
+    double h2d_bytes;           /* host -> device bytes staged by this call (0 when the cache was reused) */
+    double d2h_bytes;           /* device -> host bytes of results */
+} LibrpaGB300Stats;
+
+/* Set defaults. */
+void librpa_gb300_init_options(LibrpaGB300Options *o);
+/* Attach options to a handler (copied). */
+void librpa_gb300_set_options(LibrpaHandler *h, const LibrpaGB300Options *o);
+/* Counters of the last RPA call on this handler. */
+void librpa_gb300_get_stats(LibrpaHandler *h, LibrpaGB300Stats *s);
+
+/* Last error recorded on this handler (h may be NULL for the process-wide
+ * last error); empty string when none.  Errors never escape as C++ exceptions. */
+const char *librpa_get_last_error(LibrpaHandler *h);
+/* 0 when the last call on h succeeded. */
+int librpa_get_last_error_code(LibrpaHandler *h);
+
+/* Minimax grids without a handler (host only, no GPU needed).  Arrays of
+ * length n (tau, tau_w, omega, omega_w) and n*n (row-major cos_t2f[w][t],
+ * cos_f2t[t][w], sin_t2f[w][t]).  Returns 0 on success. */
+int librpa_gb300_minimax_grid(int n, double emin, double emax, double regularization,
+                              double *tau, double *tau_w, double *omega, double *omega_w,
+                              double *cos_t2f, double *cos_f2t, double *sin_t2f,
+                              double *duality_error);
+
+/* After a call with keep_chi0 = 1: copy chi0(q_ibz, omega) block (I<=J) to the
+ * caller as two row-major n_mu x n_nu arrays.  Returns 0 on success. */
+int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq_ibz, int I, int J,
+                                double *re, double *im);
+
+/* Number of CUDA devices visible (0 when there is no GPU). */
+int librpa_gb300_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,869 @@
+// C ABI of the GB300 RPA library: the LibRPA entry points of librpa.h with
+// the same names, arguments and copy semantics, plus the additive GB300
+// extensions of librpa_gb300.h.  No C++ exception crosses this boundary:
+// every entry catches, records the message on the handler (and process-wide),
+// and returns NaN / a nonzero status / nothing, as its signature allows.
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/librpa.h"
+#include "common.h"
+#include "dataset.h"
+#include "minimax.h"
+
+namespace {
+
+using gb::cplx;
+using gb::Dataset;
+
+std::mutex g_mu;
+std::vector<std::unique_ptr<Dataset>> g_instances(1);  // slot 0 is a sentinel (instance_manager.cpp:15-57)
+std::string g_last_error;
+int g_last_code = 0;
+
+Dataset *get_ds(LibrpaHandler *h)
+{
+    if (!h) GB_FAIL("null handler");
+    const int id = h->instance_id_;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (id <= 0 || id >= static_cast<int>(g_instances.size()) || !g_instances[id]) GB_FAIL("invalid handler");
+    return g_instances[id].get();
+}
+
+void record_error(LibrpaHandler *h, const std::string &msg)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_last_error = msg;
+        g_last_code = 1;
+    }
+    if (h)
+    {
+        const int id = h->instance_id_;
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (id > 0 && id < static_cast<int>(g_instances.size()) && g_instances[id])
+        {
+            g_instances[id]->last_error = msg;
+            g_instances[id]->last_error_code = 1;
+        }
+    }
+    std::fprintf(stderr, "librpa_gb300 error: %s\n", msg.c_str());
+}
+
+void clear_error(Dataset *ds)
+{
+    ds->last_error.clear();
+    ds->last_error_code = 0;
+}
+
+template <typename F>
+void guarded(LibrpaHandler *h, F &&f)
+{
+    try
+    {
+        f();
+    }
+    catch (const std::exception &e)
+    {
+        record_error(h, e.what());
+    }
+    catch (...)
+    {
+        record_error(h, "unknown error");
+    }
+}
+
+// MeanField::get_E_min_max / get_band_gap (meanfield.cpp:151-197) on the stored data.
+void e_min_max(const Dataset &ds, double &emin, double &emax)
+{
+    double lb = std::numeric_limits<double>::max(), ub = std::numeric_limits<double>::min();
+    double homo = -1e6, lumo = 1e6;
+    const int nk = ds.n_kpts, nb = ds.n_states;
+    for (int s = 0; s < ds.n_spins; ++s)
+    {
+        for (int k = 0; k < nk; ++k)
+        {
+            lb = std::min(lb, ds.ekb[(static_cast<size_t>(s) * nk + k) * nb]);
+            ub = std::max(ub, ds.ekb[(static_cast<size_t>(s) * nk + k) * nb + nb - 1]);
+        }
+        const double midpoint = 1.0 / (ds.n_spins * nk * ds.n_spinor);
+        for (int k = 0; k < nk; ++k)
+        {
+            int hl = -1;
+            for (int n = 0; n < nb; ++n)
+                if (ds.wg[(static_cast<size_t>(s) * nk + k) * nb + n] >= midpoint) hl = n;
+            GB_REQUIRE(hl + 1 < nb, "no unoccupied state: cannot define the band gap");
+            lumo = std::min(lumo, ds.ekb[(static_cast<size_t>(s) * nk + k) * nb + hl + 1]);
+            if (hl != -1) homo = std::max(homo, ds.ekb[(static_cast<size_t>(s) * nk + k) * nb + hl]);
+        }
+    }
+    emin = lumo - homo;
+    emax = ub - lb;
+}
+
+gb::TimeFreqGrids make_grids(const Dataset &ds, const LibrpaOptions &o)
+{
+    // TFGrids::generate (timefreq.cpp:117-154): the Gauss-Legendre / Chebyshev cases
+    // fall through to the minimax branch in LibRPA, so they produce minimax grids too.
+    switch (o.tfgrids_type)
+    {
+    case GaussLegendre:
+    case GaussChebyshevI:
+    case GaussChebyshevII:
+    case Minimax:
+    {
+        double emin_mf = 0, emax_mf = 0;
+        if (o.minimax_emin <= 0 || o.minimax_emax <= 0)
+        {
+            GB_REQUIRE(ds.occ_set, "occupations/eigenvalues needed for the minimax energy window");
+            e_min_max(ds, emin_mf, emax_mf);
+        }
+        const double emax = o.minimax_emax > 0 ? o.minimax_emax : emax_mf;
+        const double emin = o.minimax_emin > 0 ? o.minimax_emin : emin_mf;
+        return gb::minimax_grids(o.nfreq, emin, emax, o.minimax_regulation);
+    }
+    case EvenSpaced_TF:
+    {
+        // generate_evenspaced_tf (timefreq.cpp:173-191): uniform nodes, diagonal "transform"
+        GB_REQUIRE(o.tfgrids_freq_min > 0 && o.tfgrids_time_min > 0, "emin/tmin must be positive");
+        gb::TimeFreqGrids g;
+        const int n = o.nfreq;
+        g.n = n;
+        g.tau.resize(n);
+        g.tau_w.resize(n);
+        g.omega.resize(n);
+        g.omega_w.resize(n);
+        g.cos_t2f.assign(static_cast<size_t>(n) * n, 0.0);
+        g.cos_f2t.assign(static_cast<size_t>(n) * n, 0.0);
+        g.sin_t2f.assign(static_cast<size_t>(n) * n, 0.0);
+        const double w = 1.0 / n;
+        for (int i = 0; i < n; ++i)
+        {
+            g.omega[i] = o.tfgrids_freq_min + o.tfgrids_freq_interval * i;
+            g.omega_w[i] = w;
+            g.tau[i] = o.tfgrids_time_min + o.tfgrids_time_interval * i;
+            g.tau_w[i] = w;
+            g.cos_t2f[i * n + i] = w;
+            g.sin_t2f[i * n + i] = w;
+            g.cos_f2t[i * n + i] = 1.0 / w;
+        }
+        return g;
+    }
+    case EvenSpaced:
+        GB_FAIL("even-spaced frequency grids have no time grid: the conventional chi0 method is not part of this build");
+    default:
+        GB_FAIL("requested time-frequency grid is not implemented");
+    }
+}
+
+const char *kBuildInfo =
+    "librpa-gb300 1.0.0: space-time RPA correlation energy on NVIDIA GB300 (sm_103a), "
+    "C++17 host + hand-written CUDA kernels; built " __DATE__ " " __TIME__;
+
+void set_wfc_impl(Dataset *ds, int ispin, int isoc, int ik, int nstates_local, int nbasis_local,
+                  const double *re, const double *im, const double *ri)
+{
+    GB_REQUIRE(ds->n_spins > 0, "call librpa_set_scf_dimension first");
+    GB_REQUIRE(ispin >= 0 && ispin < ds->n_spins && ik >= 0 && ik < ds->n_kpts, "spin or k index out of range");
+    GB_REQUIRE(nstates_local == ds->n_states && nbasis_local == ds->n_ao,
+               "distributed (local) eigenvector blocks are not supported: pass all states and basis functions");
+    const size_t n = static_cast<size_t>(ds->n_states) * ds->n_ao;
+    const size_t base = ((static_cast<size_t>(ispin) * ds->n_spinor + isoc) * ds->n_kpts + ik) * n;
+    for (size_t i = 0; i < n; ++i)
+        ds->wfc[base + i] = ri ? cplx(ri[2 * i], ri[2 * i + 1]) : cplx(re[i], im[i]);
+    ds->wfc_set[(static_cast<size_t>(ispin) * ds->n_spinor + isoc) * ds->n_kpts + ik] = 1;
+}
+
+void add_vq_block(Dataset *ds, int ik, int I, int J, int nmu, int nnu, const double *re, const double *im,
+                  double thr)
+{
+    // input.cpp:556-581: keep the block if max |Re V| >= threshold
+    double mx = 0.0;
+    const size_t n = static_cast<size_t>(nmu) * nnu;
+    for (size_t t = 0; t < n; ++t) mx = std::max(mx, std::fabs(re[t]));
+    if (!(mx >= thr)) return;
+    std::array<int, 3> key{ik, I, J};
+    auto it = ds->vq_index.find(key);
+    if (it != ds->vq_index.end() && ds->vq_blocks[it->second].nmu == nmu && ds->vq_blocks[it->second].nnu == nnu)
+    {
+        const size_t off = ds->vq_blocks[it->second].offset;
+        for (size_t t = 0; t < n; ++t) ds->vq_blob[off + t] = cplx(re[t], im[t]);
+        return;
+    }
+    gb::VqBlock b{ik, I, J, nmu, nnu, ds->vq_blob.size()};
+    for (size_t t = 0; t < n; ++t) ds->vq_blob.emplace_back(re[t], im[t]);
+    ds->vq_index[key] = ds->vq_blocks.size();
+    ds->vq_blocks.push_back(b);
+}
+
+// Redistribute 2D-block Coulomb input into atom-pair blocks (Dataset::redistribute_coulomb_blacs2ap).
+void merge_vq_2d(Dataset *ds)
+{
+    if (ds->vq_2d.empty()) return;
+    const int nat = static_cast<int>(ds->nabf_at.size());
+    GB_REQUIRE(nat > 0, "auxiliary basis needed to use 2D-block Coulomb input");
+    std::vector<int> off(nat + 1, 0);
+    for (int I = 0; I < nat; ++I) off[I + 1] = off[I] + ds->nabf_at[I];
+    const int N = off[nat];
+    std::map<int, std::vector<cplx>> full;
+    for (const auto &b : ds->vq_2d)
+    {
+        auto &M = full[b.ik];
+        if (M.empty()) M.assign(static_cast<size_t>(N) * N, cplx(0, 0));
+        const int nr = b.mu_end - b.mu_begin, ncl = b.nu_end - b.nu_begin;
+        for (int r = 0; r < nr; ++r)
+            for (int c = 0; c < ncl; ++c)
+                M[static_cast<size_t>(b.mu_begin + r) * N + b.nu_begin + c] = b.data[static_cast<size_t>(r) * ncl + c];
+    }
+    for (auto &kv : full)
+        for (int I = 0; I < nat; ++I)
+            for (int J = I; J < nat; ++J)
+            {
+                const int nmu = ds->nabf_at[I], nnu = ds->nabf_at[J];
+                std::vector<double> re(static_cast<size_t>(nmu) * nnu), im(re.size());
+                for (int a = 0; a < nmu; ++a)
+                    for (int b = 0; b < nnu; ++b)
+                    {
+                        const cplx v = kv.second[static_cast<size_t>(off[I] + a) * N + off[J] + b];
+                        re[static_cast<size_t>(a) * nnu + b] = v.real();
+                        im[static_cast<size_t>(a) * nnu + b] = v.imag();
+                    }
+                add_vq_block(ds, kv.first, I, J, nmu, nnu, re.data(), im.data(), -1.0);
+            }
+    ds->vq_2d.clear();
+}
+
+} // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ global
+const char *librpa_get_build_info(void) { return kBuildInfo; }
+int librpa_get_major_version(void) { return 1; }
+int librpa_get_minor_version(void) { return 0; }
+int librpa_get_patch_version(void) { return 0; }
+void librpa_init_global(LibrpaSwitch, const char *, LibrpaSwitch) {}
+void librpa_finalize_global(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (auto &p : g_instances)
+        if (p) gb::release_kept(*p);
+}
+
+void librpa_print_profile(void)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (size_t i = 1; i < g_instances.size(); ++i)
+    {
+        if (!g_instances[i]) continue;
+        const auto &s = g_instances[i]->stats;
+        std::printf("librpa_gb300 profile (handler %zu)\n", i);
+        std::printf("  total %.6f s | grids %.6f | upload %.6f | G %.6f | chi0 %.6f | FT+CT %.6f | E_c %.6f\n",
+                    s.t_total, s.t_grids, s.t_upload, s.t_gf, s.t_chi0, s.t_ftct, s.t_ec);
+        std::printf("  chi0 FLOP %.4e (LibRI order %.4e) | E_c FLOP %.4e | launches %lld\n", s.chi0_flops,
+                    s.chi0_flops_libri, s.ec_flops, s.n_launches);
+    }
+}
+
+void librpa_test(void)
+{
+    guarded(nullptr, [&] {
+        const auto g = gb::minimax_grids(16, 0.25, 25.0, 0.0);
+        std::printf("librpa_gb300 self-test: minimax(16) duality error %.3e, CUDA devices %d\n",
+                    g.cosft_duality_error, gb::device_count());
+    });
+}
+
+// ------------------------------------------------------------------ options
+void librpa_init_options(LibrpaOptions *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    librpa_set_output_dir(o, ".");
+    o->parallel_routing = AUTO;
+    o->output_level = LIBRPA_VERBOSE_INFO;
+    o->vq_threshold = 0.0;
+    o->use_kpara_scf_eigvec = LIBRPA_SWITCH_OFF;
+    o->tfgrids_type = TFGRID_UNSET;
+    o->nfreq = 6;
+    o->tfgrids_freq_min = 0.005;
+    o->tfgrids_freq_interval = 0.0;
+    o->tfgrids_freq_max = 1000.0;
+    o->tfgrids_time_min = 0.005;
+    o->tfgrids_time_interval = 0.0;
+    o->minimax_emin = -1.0;
+    o->minimax_emax = -1.0;
+    o->minimax_regulation = 0.0;
+    o->use_fullcoul_eps = LIBRPA_SWITCH_ON;
+    o->use_fullcoul_exx = LIBRPA_SWITCH_OFF;
+    o->use_fullcoul_wc = LIBRPA_SWITCH_OFF;
+    o->n_bands_chi0 = -1;
+    o->n_bands_sigc = -1;
+    o->gf_threshold = 0.0;
+    o->use_scalapack_ecrpa = LIBRPA_SWITCH_ON;
+    o->use_shrink_abfs = LIBRPA_SWITCH_OFF;
+    o->use_shrink_chi = LIBRPA_SWITCH_OFF;
+    o->n_params_anacon = -1;
+    o->use_scalapack_gw_wc = LIBRPA_SWITCH_ON;
+    o->use_cholesky_gw_wc = LIBRPA_SWITCH_OFF;
+    o->replace_w_head = LIBRPA_SWITCH_OFF;
+    o->option_dielect_func = 0;
+    o->use_2d_dielectric = LIBRPA_SWITCH_OFF;
+    o->sqrt_coulomb_threshold = 0.0;
+    o->load_sigc_from_file = LIBRPA_SWITCH_OFF;
+    o->libri_chi0_threshold_C = 0.0;
+    o->libri_chi0_threshold_G = 0.0;
+    o->libri_exx_threshold_C = 0.0;
+    o->libri_exx_threshold_D = 0.0;
+    o->libri_exx_threshold_V = 0.0;
+    o->libri_g0w0_threshold_C = 0.0;
+    o->libri_g0w0_threshold_G = 0.0;
+    o->libri_g0w0_threshold_Wc = 0.0;
+    o->output_gw_sigc_mat = LIBRPA_SWITCH_OFF;
+    o->output_gw_sigc_mat_rt = LIBRPA_SWITCH_OFF;
+    o->output_gw_sigc_mat_rf = LIBRPA_SWITCH_OFF;
+    o->option_output_Wc_Rf_mat = 0;
+}
+
+void librpa_set_output_dir(LibrpaOptions *o, const char *dir)
+{
+    if (!o || !dir) return;
+    std::string s(dir);
+    if (s.empty() || s.back() != '/') s += '/';
+    std::strncpy(o->output_dir, s.c_str(), LIBRPA_MAX_STRLEN - 1);
+    o->output_dir[LIBRPA_MAX_STRLEN - 1] = '\0';
+}
+
+// ------------------------------------------------------------------ handler
+LibrpaHandler *librpa_create_handler(MPI_Comm)
+{
+    try
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_instances.push_back(std::make_unique<Dataset>());
+        const int id = static_cast<int>(g_instances.size()) - 1;
+        librpa_gb300_init_options(&g_instances[id]->gbopt);
+        return new LibrpaHandler{id};
+    }
+    catch (const std::exception &e)
+    {
+        record_error(nullptr, e.what());
+        return nullptr;
+    }
+}
+
+void librpa_destroy_handler(LibrpaHandler *h)
+{
+    if (!h) return;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        const int id = h->instance_id_;
+        if (id > 0 && id < static_cast<int>(g_instances.size()) && g_instances[id])
+        {
+            gb::release_kept(*g_instances[id]);
+            g_instances[id].reset();
+        }
+    }
+    delete h;
+}
+
+// ------------------------------------------------------------------ input
+void librpa_set_scf_dimension(LibrpaHandler *h, int nspins, int nkpts, int nstates, int nbasis, int nspinor)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(nspins > 0 && nkpts > 0 && nstates > 0 && nbasis > 0 && (nspinor == 1 || nspinor == 2),
+                   "invalid mean-field dimensions");
+        ds->n_spins = nspins;
+        ds->n_kpts = nkpts;
+        ds->n_states = nstates;
+        ds->n_ao = nbasis;
+        ds->n_spinor = nspinor;
+        ds->wg.assign(static_cast<size_t>(nspins) * nkpts * nstates, 0.0);
+        ds->ekb.assign(ds->wg.size(), 0.0);
+        ds->wfc.assign(static_cast<size_t>(nspins) * nspinor * nkpts * nstates * nbasis, cplx(0, 0));
+        ds->wfc_set.assign(static_cast<size_t>(nspins) * nspinor * nkpts, 0);
+        ds->occ_set = false;
+        clear_error(ds);
+    });
+}
+
+void librpa_set_wg_ekb_efermi(LibrpaHandler *h, int nspins, int nkpts, int nstates, const double *wg,
+                              const double *ekb, double efermi)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(nspins == ds->n_spins && nkpts == ds->n_kpts && nstates == ds->n_states,
+                   "dimensions differ from librpa_set_scf_dimension");
+        const size_t n = static_cast<size_t>(nspins) * nkpts * nstates;
+        for (size_t i = 0; i < n; ++i)
+        {
+            ds->wg[i] = wg[i] / nkpts;  // input.cpp:82
+            ds->ekb[i] = ekb[i];
+        }
+        ds->efermi = efermi;
+        ds->occ_set = true;
+    });
+}
+
+void librpa_set_wfc(LibrpaHandler *h, int ispin, int ik, int ns_loc, int nb_loc, const double *re, const double *im)
+{
+    guarded(h, [&] { Dataset *ds = get_ds(h); ds->generation++; set_wfc_impl(ds, ispin, 0, ik, ns_loc, nb_loc, re, im, nullptr); });
+}
+
+void librpa_set_wfc_spinor(LibrpaHandler *h, int ik, int ns_loc, int nb_loc, const double *ur, const double *ui,
+                           const double *dr, const double *di)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(ds->n_spinor == 2, "spinor wfc set requires n_spinor initialized to 2");
+        set_wfc_impl(ds, 0, 0, ik, ns_loc, nb_loc, ur, ui, nullptr);
+        set_wfc_impl(ds, 0, 1, ik, ns_loc, nb_loc, dr, di, nullptr);
+    });
+}
+
+void librpa_set_wfc_packed(LibrpaHandler *h, int ispin, int ik, int ns_loc, int nb_loc, const double *ri)
+{
+    guarded(h, [&] { Dataset *ds = get_ds(h); ds->generation++; set_wfc_impl(ds, ispin, 0, ik, ns_loc, nb_loc, nullptr, nullptr, ri); });
+}
+
+void librpa_set_wfc_spinor_packed(LibrpaHandler *h, int ik, int ns_loc, int nb_loc, const double *u, const double *d)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(ds->n_spinor == 2, "spinor wfc set requires n_spinor initialized to 2");
+        set_wfc_impl(ds, 0, 0, ik, ns_loc, nb_loc, nullptr, nullptr, u);
+        set_wfc_impl(ds, 0, 1, ik, ns_loc, nb_loc, nullptr, nullptr, d);
+    });
+}
+
+void librpa_set_ao_basis_wfc(LibrpaHandler *h, int natoms, const size_t *nbs)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(natoms > 0, "natoms must be positive");
+        ds->nao_at.assign(nbs, nbs + natoms);
+    });
+}
+
+void librpa_set_ao_basis_aux(LibrpaHandler *h, int natoms, const size_t *nbs)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(natoms > 0, "natoms must be positive");
+        ds->nabf_at.assign(nbs, nbs + natoms);
+    });
+}
+
+void librpa_set_latvec_and_G(LibrpaHandler *h, const double lat[9], const double G[9])
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        for (int i = 0; i < 9; ++i)
+        {
+            ds->latvec[i] = lat[i];
+            ds->recvec[i] = G[i] / (2.0 * M_PI);  // pbc.cpp:76
+        }
+        ds->latt_set = true;
+    });
+}
+
+void librpa_set_atoms(LibrpaHandler *h, int natoms, const int *types, const double *pos)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        ds->types.assign(types, types + natoms);
+        ds->positions.assign(pos, pos + 3 * natoms);
+    });
+}
+
+void librpa_set_kgrids_kvec(LibrpaHandler *h, int nk1, int nk2, int nk3, const double *kvecs)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(nk1 > 0 && nk2 > 0 && nk3 > 0, "k grid must be positive");
+        ds->period[0] = nk1;
+        ds->period[1] = nk2;
+        ds->period[2] = nk3;
+        const int nk = nk1 * nk2 * nk3;
+        ds->klist.resize(3ull * nk);
+        ds->kfrac.resize(3ull * nk);
+        for (int k = 0; k < nk; ++k)
+        {
+            double kv[3];
+            for (int d = 0; d < 3; ++d) kv[d] = kvecs[3 * k + d] / (2.0 * M_PI);
+            for (int d = 0; d < 3; ++d) ds->klist[3 * k + d] = kv[d];
+            // kfrac = latvec * kvec with -0 cleanup (pbc.cpp:96-100)
+            for (int a = 0; a < 3; ++a)
+            {
+                double f = ds->latvec[3 * a] * kv[0] + ds->latvec[3 * a + 1] * kv[1] + ds->latvec[3 * a + 2] * kv[2];
+                if (std::fabs(f) < 1e-8) f = 0.0;
+                ds->kfrac[3 * k + a] = f;
+            }
+        }
+        ds->ibz_map.resize(nk);
+        for (int k = 0; k < nk; ++k) ds->ibz_map[k] = k;
+    });
+}
+
+void librpa_set_ibz_mapping(LibrpaHandler *h, int nkpts, const int *map)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(nkpts == ds->period[0] * ds->period[1] * ds->period[2],
+                   "irk_point_id_mapping size not equal to n_k_points");
+        for (int k = 0; k < nkpts; ++k) GB_REQUIRE(map[k] >= 0 && map[k] < nkpts, "IBZ mapping index out of range");
+        ds->ibz_map.assign(map, map + nkpts);
+    });
+}
+
+void librpa_set_lri_coeff(LibrpaHandler *h, LibrpaParallelRouting, int I, int J, int ni, int nj, int nmu,
+                          const int R[3], const double *Cs)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        // input.cpp:497-500
+        GB_REQUIRE(!ds->nao_at.empty(), "wave function basis not set, call (librpa_)set_ao_basis_wfc first");
+        GB_REQUIRE(!ds->nabf_at.empty(), "auxiliary basis not set, call (librpa_)set_ao_basis_aux first");
+        GB_REQUIRE(I >= 0 && J >= 0 && I < static_cast<int>(ds->nao_at.size()) && J < static_cast<int>(ds->nao_at.size()),
+                   "atom index out of range");
+        GB_REQUIRE(ds->nabf_at[I] == nmu && ds->nao_at[I] == ni && ds->nao_at[J] == nj, "RI block dimensions inconsistent");
+        const size_t n = static_cast<size_t>(ni) * nj * nmu;
+        std::array<int, 5> key{I, J, R[0], R[1], R[2]};
+        auto it = ds->cs_index.find(key);
+        if (it != ds->cs_index.end())
+        {
+            std::memcpy(&ds->cs_blob[ds->cs_blocks[it->second].offset], Cs, n * sizeof(double));
+            return;
+        }
+        gb::CsBlock b{I, J, {R[0], R[1], R[2]}, ni, nj, nmu, ds->cs_blob.size()};
+        ds->cs_blob.insert(ds->cs_blob.end(), Cs, Cs + n);
+        ds->cs_index[key] = ds->cs_blocks.size();
+        ds->cs_blocks.push_back(b);
+    });
+}
+
+void librpa_set_aux_bare_coulomb_k_atom_pair(LibrpaHandler *h, int ik, int I, int J, int nmu, int nnu,
+                                             const double *re, const double *im, double thr)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(ik >= 0 && ik < static_cast<int>(ds->ibz_map.size()) || ds->klist.empty(), "k index out of range");
+        add_vq_block(ds, ik, I, J, nmu, nnu, re, im, thr);
+    });
+}
+
+void librpa_set_aux_cut_coulomb_k_atom_pair(LibrpaHandler *h, int, int, int, int nmu, int nnu, const double *re,
+                                            const double *im, double)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(nmu) * nnu;
+        for (size_t t = 0; t < n; ++t) ds->vq_cut_blob.emplace_back(re[t], im[t]);
+        ds->n_vq_cut_blocks++;
+    });
+}
+
+void librpa_set_aux_bare_coulomb_k_2d_block(LibrpaHandler *h, int ik, int mb, int me, int nb_, int ne,
+                                            const double *re, const double *im)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const int nr = me - mb, ncl = ne - nb_;
+        if (nr < 1 || ncl < 1) return;
+        gb::Vq2DBlock b{ik, mb, me, nb_, ne, {}};
+        b.data.resize(static_cast<size_t>(nr) * ncl);
+        for (size_t t = 0; t < b.data.size(); ++t) b.data[t] = cplx(re[t], im[t]);
+        ds->vq_2d.push_back(std::move(b));
+    });
+}
+
+void librpa_set_aux_cut_coulomb_k_2d_block(LibrpaHandler *h, int, int mb, int me, int nb_, int ne, const double *re,
+                                           const double *im)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(std::max(0, me - mb)) * std::max(0, ne - nb_);
+        for (size_t t = 0; t < n; ++t) ds->vq_cut_blob.emplace_back(re[t], im[t]);
+    });
+}
+
+void librpa_set_dielect_func_imagfreq(LibrpaHandler *h, int nfreq, const double *om, const double *eps)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        ds->dielect_omega.assign(om, om + nfreq);
+        ds->dielect_eps.assign(eps, eps + nfreq);
+    });
+}
+
+void librpa_set_band_kvec(LibrpaHandler *h, int n, const double *kf)
+{
+    guarded(h, [&] { Dataset *ds = get_ds(h); ds->generation++; ds->band_kfrac.assign(kf, kf + 3 * n); });
+}
+
+void librpa_set_band_occ_eigval(LibrpaHandler *h, int ns, int nk, int nst, const double *occ, const double *eig)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(ns) * nk * nst;
+        ds->band_occ.assign(occ, occ + n);
+        ds->band_eig.assign(eig, eig + n);
+    });
+}
+
+void librpa_set_wfc_band(LibrpaHandler *h, int, int, int nst, int nbas, const double *re, const double *im)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(nst) * nbas;
+        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(re[t], im[t]);
+    });
+}
+
+void librpa_set_wfc_band_spinor(LibrpaHandler *h, int, int nst, int nbas, const double *ur, const double *ui,
+                                const double *dr, const double *di)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(nst) * nbas;
+        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(ur[t], ui[t]);
+        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(dr[t], di[t]);
+    });
+}
+
+void librpa_set_wfc_band_packed(LibrpaHandler *h, int, int, int nst, int nbas, const double *ri)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(nst) * nbas;
+        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(ri[2 * t], ri[2 * t + 1]);
+    });
+}
+
+void librpa_set_wfc_band_spinor_packed(LibrpaHandler *h, int, int nst, int nbas, const double *u, const double *d)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        const size_t n = static_cast<size_t>(nst) * nbas;
+        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(u[2 * t], u[2 * t + 1]);
+        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(d[2 * t], d[2 * t + 1]);
+    });
+}
+
+void librpa_reset_band_data(LibrpaHandler *h)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        ds->band_kfrac.clear();
+        ds->band_occ.clear();
+        ds->band_eig.clear();
+        ds->band_wfc.clear();
+    });
+}
+
+// ------------------------------------------------------------------ compute
+void librpa_get_imaginary_frequency_grids(LibrpaHandler *h, const LibrpaOptions *p_opts, double *omegas,
+                                          double *weights)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(p_opts, "null options");
+        const auto g = make_grids(*ds, *p_opts);
+        std::memcpy(omegas, g.omega.data(), sizeof(double) * g.n);
+        std::memcpy(weights, g.omega_w.data(), sizeof(double) * g.n);
+    });
+}
+
+double librpa_get_rpa_correlation_energy(LibrpaHandler *h, const LibrpaOptions *p_opts, int n_ibz_kpoints,
+                                         double *re, double *im)
+{
+    double out = std::numeric_limits<double>::quiet_NaN();
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts, "null options");
+        const LibrpaOptions &o = *p_opts;
+        // compute_rpa.cpp:50-64: distributed eigenvectors need the k-parallel switch
+        for (unsigned char f : ds->wfc_set)
+            if (!f && o.use_kpara_scf_eigvec != LIBRPA_SWITCH_ON)
+                GB_FAIL("inconsistent input: eigenvectors missing for some k while use_kpara_scf_eigvec is off");
+        switch (o.parallel_routing)
+        {
+        case AUTO: case RTAU: case ATOMPAIR: case LIBRI: break;
+        default: GB_FAIL("invalid parallel routing");
+        }
+        GB_REQUIRE(!o.use_shrink_abfs, "use_shrink_abfs is not supported by the GPU RPA path");
+        if (ds->klist.empty())
+        {
+            // Gamma-only default lattice (PeriodicBoundaryData constructor, pbc.cpp:16-32)
+            ds->klist.assign(3, 0.0);
+            ds->kfrac.assign(3, 0.0);
+            ds->ibz_map.assign(1, 0);
+        }
+        merge_vq_2d(ds);
+        std::memset(&ds->stats, 0, sizeof(ds->stats));
+        const double t0 = gb::wall_seconds();
+        const auto g = make_grids(*ds, o);
+        ds->stats.t_grids = gb::wall_seconds() - t0;
+        GB_REQUIRE(!g.tau.empty(), "time grids required for the space-time method");
+        const auto res = gb::run_rpa_gpu(*ds, o, g, o.n_bands_chi0);
+        ds->stats.t_total += ds->stats.t_grids;
+        if (static_cast<int>(res.per_q.size()) != n_ibz_kpoints)
+            std::fprintf(stderr, "WARNING: parsed n_ibz_kpoints is not consistent with generated CorrEne object: %d != %zu\n",
+                         n_ibz_kpoints, res.per_q.size());
+        const int ncopy = std::min<int>(n_ibz_kpoints, static_cast<int>(res.per_q.size()));
+        for (int q = 0; q < ncopy; ++q)
+        {
+            if (re) re[q] = res.per_q[q].real();
+            if (im) im[q] = res.per_q[q].imag();
+        }
+        out = res.ec.real();
+    });
+    return out;
+}
+
+#define GB_UNSUPPORTED(name)                                                                        \
+    guarded(h, [&] { GB_FAIL(std::string(name) + " is outside the RPA path of this GB300 build"); })
+
+void librpa_build_exx(LibrpaHandler *h, const LibrpaOptions *) { GB_UNSUPPORTED("librpa_build_exx"); }
+void librpa_get_exx_pot_kgrid(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
+                              double *)
+{
+    GB_UNSUPPORTED("librpa_get_exx_pot_kgrid");
+}
+void librpa_get_exx_pot_band_k(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
+                               double *)
+{
+    GB_UNSUPPORTED("librpa_get_exx_pot_band_k");
+}
+void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *) { GB_UNSUPPORTED("librpa_build_g0w0_sigma"); }
+void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
+                                const double *, const double *, double *, double *)
+{
+    GB_UNSUPPORTED("librpa_get_g0w0_sigc_kgrid");
+}
+void librpa_get_g0w0_sigc_band_k(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
+                                 const double *, const double *, double *, double *)
+{
+    GB_UNSUPPORTED("librpa_get_g0w0_sigc_band_k");
+}
+
+// ------------------------------------------------------------------ GB300 extensions
+void librpa_gb300_init_options(LibrpaGB300Options *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->chi0_precision = LIBRPA_GB300_CHI0_BF16X3;
+    o->ec_path = LIBRPA_GB300_EC_CHOL;
+    o->screen_mode = LIBRPA_GB300_SCREEN_OFF;
+    o->screen_threshold = 1e-6;
+    o->audit_fraction = 0.02;
+    o->seed = 12345ULL;
+    o->use_cuda_graph = 1;
+    o->keep_chi0 = 0;
+    o->device = 0;
+    o->reuse_device_inputs = 1;
+}
+
+void librpa_gb300_set_options(LibrpaHandler *h, const LibrpaGB300Options *o)
+{
+    guarded(h, [&] {
+        GB_REQUIRE(o, "null options");
+        get_ds(h)->gbopt = *o;
+    });
+}
+
+void librpa_gb300_get_stats(LibrpaHandler *h, LibrpaGB300Stats *s)
+{
+    guarded(h, [&] {
+        GB_REQUIRE(s, "null stats");
+        *s = get_ds(h)->stats;
+    });
+}
+
+const char *librpa_get_last_error(LibrpaHandler *h)
+{
+    if (!h) return g_last_error.c_str();
+    try
+    {
+        return get_ds(h)->last_error.c_str();
+    }
+    catch (...)
+    {
+        return g_last_error.c_str();
+    }
+}
+
+int librpa_get_last_error_code(LibrpaHandler *h)
+{
+    if (!h) return g_last_code;
+    try
+    {
+        return get_ds(h)->last_error_code;
+    }
+    catch (...)
+    {
+        return 1;
+    }
+}
+
+int librpa_gb300_minimax_grid(int n, double emin, double emax, double reg, double *tau, double *tau_w,
+                              double *omega, double *omega_w, double *cos_t2f, double *cos_f2t, double *sin_t2f,
+                              double *dual)
+{
+    int rc = 1;
+    guarded(nullptr, [&] {
+        const auto g = gb::minimax_grids(n, emin, emax, reg);
+        auto cp = [](double *dst, const std::vector<double> &v) {
+            if (dst) std::memcpy(dst, v.data(), v.size() * sizeof(double));
+        };
+        cp(tau, g.tau);
+        cp(tau_w, g.tau_w);
+        cp(omega, g.omega);
+        cp(omega_w, g.omega_w);
+        cp(cos_t2f, g.cos_t2f);
+        cp(cos_f2t, g.cos_f2t);
+        cp(sin_t2f, g.sin_t2f);
+        if (dual) *dual = g.cosft_duality_error;
+        rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq, int I, int J, double *re, double *im)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ds->kept_chi0, "no chi0 kept: run with LibrpaGB300Options.keep_chi0 = 1");
+        const int nat = static_cast<int>(ds->nabf_at.size());
+        GB_REQUIRE(I >= 0 && I <= J && J < nat, "need 0 <= I <= J < n_atoms");
+        GB_REQUIRE(ifreq >= 0 && ifreq < ds->kept_nfreq && iq >= 0 && iq < ds->kept_nq, "frequency or q index out of range");
+        int p = 0;
+        for (int a = 0; a < I; ++a) p += nat - a;
+        p += J - I;
+        const size_t nel = static_cast<size_t>(ds->nabf_at[I]) * ds->nabf_at[J];
+        std::vector<cplx> buf(nel);
+        const size_t off = (static_cast<size_t>(ifreq) * ds->kept_nq + iq) * ds->kept_pair_elems + ds->kept_pair_offset[p];
+        GB_CUDA(cudaMemcpy(buf.data(), static_cast<cplx *>(ds->kept_chi0) + off, nel * sizeof(cplx), cudaMemcpyDeviceToHost));
+        for (size_t t = 0; t < nel; ++t)
+        {
+            re[t] = buf[t].real();
+            im[t] = buf[t].imag();
+        }
+        rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_device_count(void) { return gb::device_count(); }
+
+} // extern "C"

@@ -1,0 +1,120 @@
+// Host-side dataset held by one handler: a copy of everything the librpa_set_*
+// calls pass in (the caller keeps ownership of its buffers, as in LibRPA's
+// src/api/input.cpp).  The GPU engine stages it to the device per call.
+#pragma once
+
+#include <array>
+#include <complex>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/librpa_gb300.h"
+#include "../../include/librpa_options.h"
+
+namespace gb {
+
+using cplx = std::complex<double>;
+
+struct CsBlock
+{
+    int I, J, R[3], ni, nj, nmu;
+    size_t offset;  // into Dataset::cs_blob, (ni*nj) x nmu row-major
+};
+
+struct VqBlock
+{
+    int ik, I, J, nmu, nnu;
+    size_t offset;  // into Dataset::vq_blob, nmu x nnu row-major complex
+};
+
+struct Vq2DBlock
+{
+    int ik, mu_begin, mu_end, nu_begin, nu_end;
+    std::vector<cplx> data;  // row-major
+};
+
+struct Dataset
+{
+    // mean field (MeanField, src/core/meanfield.h)
+    int n_spins = 0, n_kpts = 0, n_states = 0, n_ao = 0, n_spinor = 1;
+    std::vector<double> wg;    // [s][k][n], already scaled by 1/n_kpts (input.cpp:82)
+    std::vector<double> ekb;   // [s][k][n]
+    double efermi = 0.0;
+    bool occ_set = false;
+    std::vector<cplx> wfc;     // [s][spinor][k][n][ao]
+    std::vector<unsigned char> wfc_set;  // [s][spinor][k]
+
+    // bases (AtomicBasis)
+    std::vector<int> nao_at, nabf_at;
+
+    // lattice / k mesh (PeriodicBoundaryData, src/core/pbc.cpp)
+    bool latt_set = false;
+    double latvec[9] = {1e5, 0, 0, 0, 1e5, 0, 0, 0, 1e5};  // rows a1, a2, a3 (Bohr)
+    double recvec[9] = {1e-5, 0, 0, 0, 1e-5, 0, 0, 0, 1e-5};
+    int period[3] = {1, 1, 1};
+    std::vector<double> klist;  // [k][3] Cartesian / 2pi
+    std::vector<double> kfrac;  // [k][3]
+    std::vector<int> ibz_map{0};
+    std::vector<int> types;
+    std::vector<double> positions;
+
+    // RI coefficients (Cs_LRI) and Coulomb matrices
+    std::vector<double> cs_blob;
+    std::vector<CsBlock> cs_blocks;
+    std::map<std::array<int, 5>, size_t> cs_index;  // (I,J,R) -> index into cs_blocks
+    std::vector<cplx> vq_blob;
+    std::vector<VqBlock> vq_blocks;
+    std::map<std::array<int, 3>, size_t> vq_index;   // (ik,I,J) -> index
+    std::vector<Vq2DBlock> vq_2d;
+    std::vector<cplx> vq_cut_blob;                   // truncated Coulomb (stored, unused by RPA)
+    size_t n_vq_cut_blocks = 0;
+
+    // GW-side inputs that the RPA path does not use (kept so the setters behave)
+    std::vector<double> dielect_omega, dielect_eps;
+    std::vector<double> band_kfrac, band_occ, band_eig;
+    std::vector<cplx> band_wfc;
+
+    // GB300 extensions
+    LibrpaGB300Options gbopt{};
+    LibrpaGB300Stats stats{};
+    int last_error_code = 0;
+    std::string last_error;
+
+    // Device copies of the inputs, reused by later calls while no setter ran
+    // (generation unchanged) and LibrpaGB300Options.reuse_device_inputs is set.
+    unsigned long long generation = 1;
+    std::shared_ptr<void> dev_cache;
+
+    // chi0(q, omega) kept on the device after a call (keep_chi0)
+    void *kept_chi0 = nullptr;  // device buffer owned via engine helpers
+    size_t kept_chi0_bytes = 0;
+    std::vector<size_t> kept_pair_offset;  // per upper pair (I<=J) element offset
+    size_t kept_pair_elems = 0;
+    int kept_nfreq = 0, kept_nq = 0;
+
+    int n_atoms() const
+    {
+        int n = static_cast<int>(nabf_at.size());
+        if (static_cast<int>(nao_at.size()) > n) n = static_cast<int>(nao_at.size());
+        if (static_cast<int>(types.size()) > n) n = static_cast<int>(types.size());
+        return n;
+    }
+};
+
+struct RpaResult
+{
+    cplx ec{0.0, 0.0};
+    std::vector<cplx> per_q;  // per IBZ k-point, order of first appearance
+};
+
+struct TimeFreqGrids;
+
+// GPU pipeline (engine.cu).  Throws gb::Error on failure.
+RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &grids,
+                      int nbands_g);
+void release_kept(Dataset &ds);
+int device_count();
+
+} // namespace gb

@@ -1,0 +1,581 @@
+// GPU pipeline of librpa_get_rpa_correlation_energy.
+//
+// Per imaginary time tau (and spin):
+//   1. s(+-tau) weights, A_k = Psi^T diag(s) conj(Psi), G(R,+-tau) = sgn Re sum_k e^{-i2pi k.R} A_k
+//      (chi0.cpp:303-426)
+//   2. supercell G and X(+-) = C * G_super(+-)      (first contraction of LRI::cal_loop3)
+//   3. chi0(R,tau) upper atom-pair blocks = two G+/G- passes of the a1b1_a2b2 and
+//      a1b2_a2b1 contractions (RPA.hpp:104-137, LRI-cal_loop3.hpp:902-1032)
+//   4. chi0(q,w) += 2/n_s gamma(w,tau) e^{i2pi q.R} chi0(R,tau)   (chi0.cpp:507-596)
+// then per IBZ q: Pi = V chi0(q,w), tr Pi, ln det(I - Pi) and
+//   E_c = sum_{q,w} w_w w_q / 2pi [ln det(I - Pi) + tr Pi]   (epsilon.cpp:270-558, :43-268)
+//
+// HBM layout (row-major everywhere):
+//   C      [(I, mu, i)][(cell, K, k)]          rows_c x n_sup
+//   G(+-)  [sign][cell][i][j]                  2 x n_c x n_ao x n_ao
+//   Gs     [sign][(cK,k)][(cL,l)]              2 x n_sup x n_sup
+//   X(+-)  [sign][(I, mu, i)][(cL, L, l)]      2 x rows_c x n_sup
+//   chi0R  [pair I<=J][cell][mu][nu]           one tau at a time
+//   chi0q  [w][q_ibz][pair][mu][nu] complex    accumulated over tau
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
+#include <numeric>
+
+#include "chi0_fast.h"
+#include "common.h"
+#include "dataset.h"
+#include "kernels.h"
+#include "minimax.h"
+
+namespace gb {
+
+namespace {
+
+int centred_mod(int i, int n)
+{
+    int r = i % n;  // C semantics, like LibRI's Array_Operator::operator%
+    r = (r + 3 * n / 2) % n;
+    return r - n / 2;
+}
+
+struct Cells
+{
+    std::vector<std::array<int, 3>> R;
+    std::map<std::array<int, 3>, int> index;
+    int period[3];
+    int find(int x, int y, int z) const
+    {
+        std::array<int, 3> k{centred_mod(x, period[0]), centred_mod(y, period[1]), centred_mod(z, period[2])};
+        auto it = index.find(k);
+        return it == index.end() ? -1 : it->second;
+    }
+};
+
+Cells make_cells(const int period[3])
+{
+    Cells c;
+    for (int d = 0; d < 3; ++d) c.period[d] = period[d];
+    // construct_R_grid (pbc.cpp:178-190): x outer, z inner, centred range
+    for (int x = -(period[0]) / 2; x <= (period[0] - 1) / 2; ++x)
+        for (int y = -(period[1]) / 2; y <= (period[1] - 1) / 2; ++y)
+            for (int z = -(period[2]) / 2; z <= (period[2] - 1) / 2; ++z)
+            {
+                c.index[{x, y, z}] = static_cast<int>(c.R.size());
+                c.R.push_back({x, y, z});
+            }
+    return c;
+}
+
+template <typename T>
+DevBuf<T> to_dev(const std::vector<T> &h, cudaStream_t st)
+{
+    DevBuf<T> d(h.size());
+    d.upload(h.data(), h.size(), st);
+    return d;
+}
+
+struct EventTimer
+{
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventTimer()
+    {
+        GB_CUDA(cudaEventCreate(&a));
+        GB_CUDA(cudaEventCreate(&b));
+    }
+    ~EventTimer()
+    {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+    void start(cudaStream_t s) { GB_CUDA(cudaEventRecord(a, s)); }
+    void stop(cudaStream_t s) { GB_CUDA(cudaEventRecord(b, s)); }
+    double ms()
+    {
+        GB_CUDA(cudaEventSynchronize(b));
+        float t = 0;
+        GB_CUDA(cudaEventElapsedTime(&t, a, b));
+        return t;
+    }
+};
+
+} // namespace
+
+int device_count()
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+void release_kept(Dataset &ds)
+{
+    if (ds.kept_chi0) cudaFree(ds.kept_chi0);
+    ds.kept_chi0 = nullptr;
+    ds.kept_chi0_bytes = 0;
+}
+
+RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf, int nbands_g)
+{
+    const double t_begin = wall_seconds();
+    LibrpaGB300Stats &S = ds.stats;
+    const LibrpaGB300Options &go = ds.gbopt;
+    const int ndev = device_count();
+    GB_REQUIRE(ndev > 0, "no CUDA device visible: the GB300 RPA path has no CPU fallback");
+    GB_CUDA(cudaSetDevice(go.device));
+
+    // ------------------------------------------------------------ host-side tables
+    const int n_at = ds.n_atoms();
+    GB_REQUIRE(n_at > 0, "number of atoms unknown: set atoms or bases first");
+    GB_REQUIRE(static_cast<int>(ds.nao_at.size()) == n_at && static_cast<int>(ds.nabf_at.size()) == n_at,
+               "wave-function and auxiliary bases must be set for every atom");
+    GB_REQUIRE(ds.n_spinor == 1, "spinor (SOC) wave functions are not supported by the GPU RPA path");
+    const int nk = ds.n_kpts, nb = ds.n_states, nao = ds.n_ao, ns = ds.n_spins;
+    GB_REQUIRE(nk > 0 && nb > 0 && nao > 0 && ns > 0, "mean-field dimensions not set");
+    GB_REQUIRE(ds.occ_set, "occupations/eigenvalues not set");
+    for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some (spin, k)");
+    std::vector<int> ao_off(n_at), abf_off(n_at + 1, 0);
+    std::vector<long long> rowc_off(n_at);
+    int tot_ao = 0, max_nao = 0, max_nabf = 0;
+    long long rows_c = 0;
+    for (int I = 0; I < n_at; ++I)
+    {
+        ao_off[I] = tot_ao;
+        tot_ao += ds.nao_at[I];
+        abf_off[I + 1] = abf_off[I] + ds.nabf_at[I];
+        rowc_off[I] = rows_c;
+        rows_c += static_cast<long long>(ds.nabf_at[I]) * ds.nao_at[I];
+        max_nao = std::max(max_nao, ds.nao_at[I]);
+        max_nabf = std::max(max_nabf, ds.nabf_at[I]);
+    }
+    GB_REQUIRE(tot_ao == nao, "sum of per-atom NAOs differs from the mean-field basis size");
+    const int N = abf_off[n_at];
+    const Cells cells = make_cells(ds.period);
+    const int nc = static_cast<int>(cells.R.size());
+    GB_REQUIRE(nc == nk, "number of BvK cells must equal the number of k points");
+    std::vector<int> cdiff(static_cast<size_t>(nc) * nc), cneg(nc);
+    for (int a = 0; a < nc; ++a)
+    {
+        for (int b = 0; b < nc; ++b)
+            cdiff[a * nc + b] = cells.find(cells.R[a][0] - cells.R[b][0], cells.R[a][1] - cells.R[b][1],
+                                           cells.R[a][2] - cells.R[b][2]);
+        cneg[a] = cells.find(-cells.R[a][0], -cells.R[a][1], -cells.R[a][2]);
+    }
+    const long long n_sup = static_cast<long long>(nc) * nao;
+
+    // G phases: theta = 2pi kfrac_k . R_c  (kphase = e^{-i theta}, chi0.cpp:379-380)
+    std::vector<double> gcos(static_cast<size_t>(nk) * nc), gsin(static_cast<size_t>(nk) * nc);
+    for (int k = 0; k < nk; ++k)
+        for (int c = 0; c < nc; ++c)
+        {
+            const double th = 2.0 * M_PI *
+                              (ds.kfrac[3 * k] * cells.R[c][0] + ds.kfrac[3 * k + 1] * cells.R[c][1] +
+                               ds.kfrac[3 * k + 2] * cells.R[c][2]);
+            gcos[k * nc + c] = std::cos(th);
+            gsin[k * nc + c] = std::sin(th);
+        }
+    // IBZ list (pbc.cpp:110-153): representatives in order of first appearance, weight count/nk
+    std::vector<int> ibz_rep;
+    std::vector<double> ibz_w;
+    {
+        std::map<int, int> seen;
+        for (int k = 0; k < nk; ++k)
+        {
+            const int r = ds.ibz_map[k];
+            auto it = seen.find(r);
+            if (it == seen.end())
+            {
+                seen[r] = static_cast<int>(ibz_rep.size());
+                ibz_rep.push_back(r);
+                ibz_w.push_back(1.0 / nk);
+            }
+            else
+                ibz_w[it->second] += 1.0 / nk;
+        }
+    }
+    const int nq = static_cast<int>(ibz_rep.size());
+    // FT phases: 2pi q.(R latvec) with q = k_cart / 2pi  (chi0.cpp:582)
+    std::vector<double> qcos(static_cast<size_t>(nq) * nc), qsin(static_cast<size_t>(nq) * nc);
+    for (int q = 0; q < nq; ++q)
+        for (int c = 0; c < nc; ++c)
+        {
+            double Rc[3] = {0, 0, 0};
+            for (int d = 0; d < 3; ++d)
+                for (int a = 0; a < 3; ++a) Rc[d] += cells.R[c][a] * ds.latvec[a * 3 + d];
+            const double *qv = &ds.klist[3 * ibz_rep[q]];
+            const double arg = (qv[0] * Rc[0] + qv[1] * Rc[1] + qv[2] * Rc[2]) * 2.0 * M_PI;
+            qcos[q * nc + c] = std::cos(arg);
+            qsin[q * nc + c] = std::sin(arg);
+        }
+
+    // upper atom pairs
+    std::vector<int> pI, pJ, pair_of(static_cast<size_t>(n_at) * n_at, -1);
+    std::vector<long long> r_off, e_off;
+    long long r_tot = 0, e_tot = 0;
+    for (int I = 0; I < n_at; ++I)
+        for (int J = I; J < n_at; ++J)
+        {
+            pair_of[I * n_at + J] = static_cast<int>(pI.size());
+            pI.push_back(I);
+            pJ.push_back(J);
+            r_off.push_back(r_tot);
+            e_off.push_back(e_tot);
+            const long long el = static_cast<long long>(ds.nabf_at[I]) * ds.nabf_at[J];
+            r_tot += el * nc;
+            e_tot += el;
+        }
+    const int n_pairs = static_cast<int>(pI.size());
+    std::vector<int> atom_of(N);
+    for (int I = 0; I < n_at; ++I)
+        for (int a = abf_off[I]; a < abf_off[I + 1]; ++a) atom_of[a] = I;
+
+    // RI blocks -> (I, J, cell) table; LibRI skips keys outside the BvK cell list
+    const double thr_c = opts.libri_chi0_threshold_C;
+    std::vector<long long> cs_off;
+    std::vector<int> cs_meta;
+    for (const CsBlock &b : ds.cs_blocks)
+    {
+        GB_REQUIRE(b.I >= 0 && b.I < n_at && b.J >= 0 && b.J < n_at, "RI block atom index out of range");
+        GB_REQUIRE(b.ni == ds.nao_at[b.I] && b.nj == ds.nao_at[b.J] && b.nmu == ds.nabf_at[b.I],
+                   "RI block dimensions inconsistent with the bases");
+        const int c = cells.index.count({b.R[0], b.R[1], b.R[2]}) ? cells.index.at({b.R[0], b.R[1], b.R[2]}) : -1;
+        if (c < 0) continue;
+        if (thr_c > 0)
+        {
+            double mx = 0.0;
+            const size_t n = static_cast<size_t>(b.ni) * b.nj * b.nmu;
+            for (size_t t = 0; t < n; ++t) mx = std::max(mx, std::fabs(ds.cs_blob[b.offset + t]));
+            if (mx < thr_c) continue;
+        }
+        cs_off.push_back(static_cast<long long>(b.offset));
+        cs_meta.insert(cs_meta.end(), {b.I, b.J, c, 0});
+    }
+
+    // Coulomb blocks per IBZ q (upper pairs)
+    std::vector<std::vector<int>> vq_of_q(nq);
+    for (size_t bi = 0; bi < ds.vq_blocks.size(); ++bi)
+    {
+        const VqBlock &b = ds.vq_blocks[bi];
+        for (int q = 0; q < nq; ++q)
+            if (ibz_rep[q] == b.ik && b.I <= b.J) vq_of_q[q].push_back(static_cast<int>(bi));
+    }
+
+    // ------------------------------------------------------------ device staging
+    cudaStream_t st;
+    GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct StreamGuard
+    {
+        cudaStream_t s;
+        ~StreamGuard() { cudaStreamDestroy(s); }
+    } sg{st};
+    long long launches = 0;
+    const double t_up0 = wall_seconds();
+    auto d_ao_off = to_dev(ao_off, st);
+    auto d_nao = to_dev(ds.nao_at, st);
+    auto d_nabf = to_dev(ds.nabf_at, st);
+    auto d_rowc = to_dev(rowc_off, st);
+    auto d_cdiff = to_dev(cdiff, st);
+    auto d_cneg = to_dev(cneg, st);
+    auto d_gcos = to_dev(gcos, st);
+    auto d_gsin = to_dev(gsin, st);
+    auto d_qcos = to_dev(qcos, st);
+    auto d_qsin = to_dev(qsin, st);
+    auto d_pI = to_dev(pI, st);
+    auto d_pJ = to_dev(pJ, st);
+    auto d_roff = to_dev(r_off, st);
+    auto d_eoff = to_dev(e_off, st);
+    auto d_pair_of = to_dev(pair_of, st);
+    auto d_atom_of = to_dev(atom_of, st);
+    std::vector<int> abf_off_n(abf_off.begin(), abf_off.end() - 1);
+    auto d_abf_off = to_dev(abf_off_n, st);
+    // Inputs staged once per input generation (reused while no setter ran).
+    struct DeviceInputs
+    {
+        unsigned long long generation = 0;
+        int precision = -1;
+        DevBuf<double> ekb, wg, C;
+        DevBuf<cuDoubleComplex> psi, vblob;
+        long long rows_c = 0, n_sup = 0;
+    };
+    std::shared_ptr<DeviceInputs> din = std::static_pointer_cast<DeviceInputs>(ds.dev_cache);
+    const bool reuse = go.reuse_device_inputs && din && din->generation == ds.generation &&
+                       din->rows_c == rows_c && din->n_sup == n_sup;
+    double h2d = 0.0;
+    if (!reuse)
+    {
+        ds.dev_cache.reset();
+        din = std::make_shared<DeviceInputs>();
+        din->generation = ds.generation;
+        din->rows_c = rows_c;
+        din->n_sup = n_sup;
+        din->ekb.alloc(ds.ekb.size());
+        din->wg.alloc(ds.wg.size());
+        din->ekb.upload(ds.ekb.data(), ds.ekb.size(), st);
+        din->wg.upload(ds.wg.data(), ds.wg.size(), st);
+        din->psi.alloc(ds.wfc.size());
+        din->psi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()), ds.wfc.size(), st);
+        din->vblob.alloc(ds.vq_blob.size());
+        din->vblob.upload(reinterpret_cast<const cuDoubleComplex *>(ds.vq_blob.data()), ds.vq_blob.size(), st);
+        DevBuf<double> d_csblob(ds.cs_blob.size());
+        d_csblob.upload(ds.cs_blob.data(), ds.cs_blob.size(), st);
+        auto d_csoff = to_dev(cs_off, st);
+        auto d_csmeta = to_dev(cs_meta, st);
+        h2d = 8.0 * (ds.ekb.size() + ds.wg.size() + ds.cs_blob.size()) + 16.0 * (ds.wfc.size() + ds.vq_blob.size());
+        din->C.alloc(static_cast<size_t>(rows_c) * n_sup);
+        din->C.zero(st);
+        Geom gs;
+        gs.n_at = n_at;
+        gs.n_c = nc;
+        gs.n_ao = nao;
+        gs.n_sup = static_cast<int>(n_sup);
+        gs.ao_off = d_ao_off.get();
+        gs.nao = d_nao.get();
+        gs.nabf = d_nabf.get();
+        gs.rowc_off = d_rowc.get();
+        launch_cs_scatter(d_csblob.get(), d_csoff.get(), d_csmeta.get(), static_cast<int>(cs_off.size()), gs,
+                          din->C.get(), st);
+        ++launches;
+        GB_CUDA(cudaStreamSynchronize(st));
+        if (go.reuse_device_inputs) ds.dev_cache = din;
+    }
+    S.h2d_bytes = h2d;
+    DevBuf<double> &d_ekb = din->ekb, &d_wg = din->wg;
+    DevBuf<cuDoubleComplex> &d_psi = din->psi;
+
+    Geom g;
+    g.n_at = n_at;
+    g.n_c = nc;
+    g.n_ao = nao;
+    g.n_sup = static_cast<int>(n_sup);
+    g.max_nao = max_nao;
+    g.max_nabf = max_nabf;
+    g.rows_c = rows_c;
+    g.ao_off = d_ao_off.get();
+    g.nao = d_nao.get();
+    g.nabf = d_nabf.get();
+    g.rowc_off = d_rowc.get();
+    g.cdiff = d_cdiff.get();
+    g.cneg = d_cneg.get();
+    Pairs pr;
+    pr.n_pairs = n_pairs;
+    pr.I = d_pI.get();
+    pr.J = d_pJ.get();
+    pr.r_off = d_roff.get();
+    pr.e_off = d_eoff.get();
+    pr.e_total = e_tot;
+
+    DevBuf<double> &d_C = din->C;
+    GB_CUDA(cudaStreamSynchronize(st));
+    S.t_upload = wall_seconds() - t_up0;
+
+    // ------------------------------------------------------------ tau loop
+    const int nw = tf.n;
+    DevBuf<double> d_s(2ull * nk * nb);
+    DevBuf<cuDoubleComplex> d_A(2ull * nk * nao * nao);
+    DevBuf<double> d_G(2ull * nc * nao * nao);
+    DevBuf<double> d_Gs(2ull * n_sup * n_sup);
+    DevBuf<double> d_X(2ull * rows_c * n_sup);
+    DevBuf<double> d_chi0R(static_cast<size_t>(r_tot));
+    DevBuf<cuDoubleComplex> d_chi0q(static_cast<size_t>(nw) * nq * e_tot);
+    d_chi0q.zero(st);
+    DevBuf<double> d_gamma(static_cast<size_t>(nw));
+
+    const int prec = go.chi0_precision;
+    std::unique_ptr<Chi0Fast> fast;
+    if (prec != LIBRPA_GB300_CHI0_FP64) fast = std::make_unique<Chi0Fast>(prec, g, pr, d_C.get(), st);
+
+    EventTimer ev_gf, ev_x, ev_chi, ev_ft;
+    double t_gf = 0, t_chi = 0, t_ft = 0;
+    double flops_chi = 0.0, flops_libri = 0.0;
+    S.dt_chi0_kernel_ms = 0.0;
+    S.n_chi0_kernel = 0;
+    const double fac = 2.0 / ns;
+    for (int it = 0; it < nw; ++it)
+    {
+        const double tau = tf.tau[it];
+        std::vector<double> gam(nw);
+        for (int w = 0; w < nw; ++w) gam[w] = tf.cos_t2f[static_cast<size_t>(w) * nw + it];
+        d_gamma.upload(gam.data(), nw, st);
+        for (int is = 0; is < ns; ++is)
+        {
+            ev_gf.start(st);
+            launch_tau_scale(d_ekb.get() + static_cast<size_t>(is) * nk * nb, d_wg.get() + static_cast<size_t>(is) * nk * nb,
+                             nk, nb, ds.efermi, tau, ns, nbands_g, d_s.get(), st);
+            launch_gk_build(d_psi.get() + static_cast<size_t>(is) * nk * nb * nao, d_s.get(), nk, nb, nao, d_A.get(), st);
+            launch_phase_sum(d_A.get(), d_gcos.get(), d_gsin.get(), nk, nc, nao, d_G.get(), st);
+            launch_gsuper(d_G.get(), g, d_Gs.get(), st);
+            launches += 4;
+            ev_gf.stop(st);
+            t_gf += ev_gf.ms();
+            ev_chi.start(st);
+            const double *Gp = d_G.get(), *Gm = d_G.get() + static_cast<size_t>(nc) * nao * nao;
+            if (prec == LIBRPA_GB300_CHI0_FP64)
+            {
+                launch_dgemm(static_cast<int>(rows_c), static_cast<int>(n_sup), static_cast<int>(n_sup), d_C.get(), n_sup, 0,
+                             d_Gs.get(), n_sup, n_sup * n_sup, d_X.get(), n_sup, rows_c * n_sup, 2, 1.0, 0.0, st);
+                ev_x.start(st);
+                launch_chi0_fp64(d_X.get(), d_X.get() + rows_c * n_sup, d_C.get(), Gp, Gm, g, pr, d_chi0R.get(), st);
+                ev_x.stop(st);
+                launches += 2;
+            }
+            else
+            {
+                ev_x.start(st);
+                launches += fast->run(d_Gs.get(), Gp, Gm, d_chi0R.get(), st);
+                ev_x.stop(st);
+            }
+            ev_chi.stop(st);
+            t_chi += ev_chi.ms();
+            S.dt_chi0_kernel_ms += ev_x.ms();
+            S.n_chi0_kernel += 1;
+            ev_ft.start(st);
+            launch_ftct(d_chi0R.get(), g, pr, d_qcos.get(), d_qsin.get(), nq, d_gamma.get(), nw, fac, d_chi0q.get(), st);
+            ++launches;
+            ev_ft.stop(st);
+            t_ft += ev_ft.ms();
+        }
+    }
+    // FLOP counts per tau and spin.
+    //  ours: X GEMMs 2 * 2 rows_c n_sup^2; per upper (pair, cell) and pass:
+    //        E = g^T X (2 bI aI aJ n_sup), T1 (2 bI bJ aJ n_sup), T2 (2 bI bJ aI aJ)
+    //  LibRI (all ordered pairs, both passes), LRI-cal_loop3.hpp:902-1032:
+    //   a1b1_a2b2: sum_I 2 bI aI n_sup^2 + sum_{I,J} nc (2 aJ bI aI + 2 bI bJ aJ) n_sup
+    //   a1b2_a2b1: sum_{I,J} nc (2 bJ aJ aI n_sup + 2 aJ aI bI n_sup + 2 bI bJ aJ aI)
+    {
+        double per = 2.0 * 2.0 * static_cast<double>(rows_c) * n_sup * n_sup;
+        for (int p = 0; p < n_pairs; ++p)
+        {
+            const double aI = ds.nao_at[pI[p]], aJ = ds.nao_at[pJ[p]], bI = ds.nabf_at[pI[p]], bJ = ds.nabf_at[pJ[p]];
+            per += nc * 2.0 * (2.0 * bI * aI * aJ * n_sup + 2.0 * bI * bJ * aJ * n_sup + 2.0 * bI * bJ * aI * aJ);
+        }
+        double lib = 0.0;
+        for (int I = 0; I < n_at; ++I)
+        {
+            const double aI = ds.nao_at[I], bI = ds.nabf_at[I];
+            lib += 2.0 * bI * aI * static_cast<double>(n_sup) * n_sup;
+            for (int J = 0; J < n_at; ++J)
+            {
+                const double aJ = ds.nao_at[J], bJ = ds.nabf_at[J];
+                lib += nc * (2.0 * aJ * bI * aI + 2.0 * bI * bJ * aJ) * n_sup;
+                lib += nc * (2.0 * bJ * aJ * aI * n_sup + 2.0 * aJ * aI * bI * n_sup + 2.0 * bI * bJ * aJ * aI);
+            }
+        }
+        flops_chi = per * nw * ns;
+        flops_libri = 2.0 * lib * nw * ns;
+    }
+    S.t_gf = t_gf * 1e-3;
+    S.t_chi0 = t_chi * 1e-3;
+    S.t_ftct = t_ft * 1e-3;
+    S.chi0_flops = flops_chi;
+    S.chi0_flops_libri = flops_libri;
+    S.gf_flops = static_cast<double>(nw) * ns * 2.0 * (8.0 * nk * nao * nao * nb + 4.0 * nc * nk * nao * nao);
+    S.ftct_bytes = static_cast<double>(nw) * ns * (8.0 * r_tot + 2.0 * 16.0 * nw * nq * e_tot);
+    d_X.release();
+    d_Gs.release();
+    fast.reset();
+
+    // ------------------------------------------------------------ E_c
+    EventTimer ev_ec;
+    ev_ec.start(st);
+    const bool gamma_only = (nk == 1);
+    RpaResult res;
+    res.per_q.assign(nq, cplx(0, 0));
+    const long long NN = static_cast<long long>(N) * N;
+    double ec_flops = 0.0;
+    for (int q = 0; q < nq; ++q)
+    {
+        // V(q) full: blocks of this q inside the staged Coulomb blob
+        std::vector<long long> voff;
+        std::vector<int> vIJ;
+        for (int bi : vq_of_q[q])
+        {
+            const VqBlock &b = ds.vq_blocks[bi];
+            GB_REQUIRE(b.nmu == ds.nabf_at[b.I] && b.nnu == ds.nabf_at[b.J], "Coulomb block dimensions inconsistent");
+            voff.push_back(static_cast<long long>(b.offset));
+            vIJ.push_back(b.I);
+            vIJ.push_back(b.J);
+        }
+        auto d_voff = to_dev(voff, st);
+        auto d_vIJ = to_dev(vIJ, st);
+        const cuDoubleComplex *vbase = din->vblob.get();
+        std::vector<double> tr_h(gamma_only ? nw : 2 * nw), ld_h(gamma_only ? nw : 2 * nw);
+        if (gamma_only)
+        {
+            DevBuf<double> V(NN), X(NN * nw), P(NN * nw), tr(nw), ld(nw);
+            V.zero(st);
+            launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
+                              d_nabf.get(), N, true, nullptr, V.get(), st);
+            launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot, nw, N,
+                                 d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at, d_eoff.get(), true,
+                                 nullptr, X.get(), NN, st);
+            launch_dgemm(N, N, N, V.get(), N, 0, X.get(), N, NN, P.get(), N, NN, nw, 1.0, 0.0, st);
+            launch_trace_and_negate_r(P.get(), N, nw, tr.get(), st);
+            launch_lu_logdet_r(P.get(), N, nw, ld.get(), st);
+            launches += 5;
+            tr.download(tr_h.data(), nw, st);
+            ld.download(ld_h.data(), nw, st);
+            GB_CUDA(cudaStreamSynchronize(st));
+            for (int w = 0; w < nw; ++w)
+            {
+                const cplx v = cplx(tr_h[w] + ld_h[w], 0.0) * tf.omega_w[w] * ibz_w[q] / (2.0 * M_PI);
+                res.per_q[q] += v;
+            }
+            ec_flops += nw * (2.0 * N * N * N + 2.0 * N * N * N / 3.0);
+        }
+        else
+        {
+            DevBuf<cuDoubleComplex> V(NN), X(NN * nw), P(NN * nw), tr(nw), ld(nw);
+            V.zero(st);
+            launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
+                              d_nabf.get(), N, false, V.get(), nullptr, st);
+            launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot, nw, N,
+                                 d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at, d_eoff.get(), false,
+                                 X.get(), nullptr, NN, st);
+            launch_zgemm(N, N, N, V.get(), N, 0, X.get(), N, NN, P.get(), N, NN, nw, st);
+            launch_trace_and_negate_c(P.get(), N, nw, tr.get(), st);
+            launch_lu_logdet_c(P.get(), N, nw, ld.get(), st);
+            launches += 5;
+            tr.download(reinterpret_cast<cuDoubleComplex *>(tr_h.data()), nw, st);
+            ld.download(reinterpret_cast<cuDoubleComplex *>(ld_h.data()), nw, st);
+            GB_CUDA(cudaStreamSynchronize(st));
+            for (int w = 0; w < nw; ++w)
+            {
+                const cplx v = (cplx(tr_h[2 * w], tr_h[2 * w + 1]) + cplx(ld_h[2 * w], ld_h[2 * w + 1])) *
+                               tf.omega_w[w] * ibz_w[q] / (2.0 * M_PI);
+                res.per_q[q] += v;
+            }
+            ec_flops += nw * (8.0 * N * N * N + 8.0 * N * N * N / 3.0);
+        }
+    }
+    ev_ec.stop(st);
+    S.t_ec = ev_ec.ms() * 1e-3;
+    S.ec_flops = ec_flops;
+    for (const cplx &v : res.per_q) res.ec += v;
+
+    // keep chi0(q, w) for inspection
+    release_kept(ds);
+    if (go.keep_chi0)
+    {
+        ds.kept_chi0_bytes = d_chi0q.bytes();
+        GB_CUDA(cudaMalloc(&ds.kept_chi0, ds.kept_chi0_bytes));
+        GB_CUDA(cudaMemcpyAsync(ds.kept_chi0, d_chi0q.get(), ds.kept_chi0_bytes, cudaMemcpyDeviceToDevice, st));
+        ds.kept_pair_offset.assign(e_off.begin(), e_off.end());
+        ds.kept_pair_elems = static_cast<size_t>(e_tot);
+        ds.kept_nfreq = nw;
+        ds.kept_nq = nq;
+    }
+    GB_CUDA(cudaStreamSynchronize(st));
+    S.n_launches = launches;
+    S.d2h_bytes = 16.0 * 2 * nw * nq;
+    S.blocks_total = static_cast<long long>(n_pairs) * nc;
+    S.blocks_computed = S.blocks_total;
+    S.t_total = wall_seconds() - t_begin;
+    return res;
+}
+
+} // namespace gb

@@ -1,0 +1,144 @@
+"""Oracle (test infrastructure only): reader for LibRPA's FHI-aims dataset export.
+
+Follows the driver readers of the reference (driver/read_data.cpp):
+  band_out          read_scf_occ_eigenvalues   :32-140
+  stru_out          read_stru                  :1814-1867
+  bz_sampling_out   read_bz_sampling           :1869-1916
+  basis_out         read_basis                 :1976-2011
+  KS_eigenvector_*  handle_KS_file             :184-284  (order: ao, spinor, band, spin)
+  Cs_data_* (bin)   handle_Cs_file_binary      :690-747  (keep if max|C| >= cs_threshold, default 1e-6)
+  coulomb_mat_*     handle_Vq_row_file (bin)   :1472-1577 (upper atom blocks)
+Only the unformatted-binary Cs/V variants are handled (the regression datasets use them).
+"""
+from __future__ import annotations
+
+import glob
+import os
+import struct
+
+import numpy as np
+
+from .rpa_oracle import RPAInput
+
+
+def _tokens(path):
+    with open(path) as f:
+        return f.read().split()
+
+
+def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
+    d = d.rstrip("/") + "/"
+    t = _tokens(d + "band_out")
+    nk, ns, nb, nao = int(t[0]), int(t[1]), int(t[2]), int(t[3])
+    efermi = float(t[4])
+    p = 5
+    wg = np.zeros((ns, nk, nb))
+    ekb = np.zeros((ns, nk, nb))
+    for _ in range(nk):
+        for _s in range(ns):
+            k = int(t[p]) - 1
+            s = int(t[p + 1]) - 1
+            p += 2
+            for n in range(nb):
+                wg[s, k, n] = float(t[p + 1])
+                ekb[s, k, n] = float(t[p + 2])
+                p += 4
+
+    t = _tokens(d + "stru_out")
+    lat = np.array([float(x) for x in t[0:9]]).reshape(3, 3)
+    nat = int(t[18])
+    pos = np.zeros((nat, 3))
+    types = []
+    p = 19
+    for a in range(nat):
+        pos[a] = [float(x) for x in t[p:p + 3]]
+        types.append(int(t[p + 3]) - 1)
+        p += 4
+
+    if os.path.exists(d + "bz_sampling_out"):
+        t = _tokens(d + "bz_sampling_out")
+        period = (int(t[0]), int(t[1]), int(t[2]))
+        nkf = int(t[3])
+        p = 5
+        kv = np.zeros((nkf, 3))
+        ibz = np.zeros(nkf, int)
+        for i in range(nkf):
+            kv[i] = [float(x) for x in t[p + 5:p + 8]]
+            ibz[i] = int(t[p + 9]) - 1
+            p += 10
+    else:
+        t = _tokens(d + "stru_out")
+        p = 19 + 4 * nat
+        period = (int(t[p]), int(t[p + 1]), int(t[p + 2]))
+        p += 3
+        nkf = period[0] * period[1] * period[2]
+        kv = np.array([float(x) for x in t[p:p + 3 * nkf]]).reshape(nkf, 3)
+        p += 3 * nkf
+        ibz = np.array([int(x) - 1 for x in t[p:p + nkf]])
+
+    t = _tokens(d + "basis_out")
+    ntypes = int(t[0])
+    p = 4
+    mw, ma = {}, {}
+    for _ in range(ntypes):
+        ty = int(t[p]) - 1
+        mw[ty] = int(t[p + 1])
+        ma[ty] = int(t[p + 2])
+        p += 3
+    nao_at = [mw[types[a]] for a in range(nat)]
+    nabf_at = [ma[types[a]] for a in range(nat)]
+
+    wfc = np.zeros((ns, nk, nb, nao), complex)
+    for fn in sorted(glob.glob(d + "KS_eigenvector*")):
+        t = _tokens(fn)
+        p = 0
+        while p < len(t):
+            ik = int(t[p]) - 1
+            p += 1
+            if p >= len(t):
+                break
+            for iw in range(nao):
+                for ib in range(nb):
+                    for s in range(ns):
+                        wfc[s, ik, ib, iw] = complex(float(t[p]), float(t[p + 1]))
+                        p += 2
+
+    Cs = {}
+    for fn in sorted(glob.glob(d + "Cs_data*")):
+        raw = open(fn, "rb").read()
+        natom, ncell, nblk = struct.unpack_from("<3i", raw, 0)
+        off = 12
+        for _ in range(nblk):
+            I, J, r1, r2, r3, ni, nj, nmu = struct.unpack_from("<8i", raw, off)
+            off += 32
+            cnt = ni * nj * nmu
+            m = np.frombuffer(raw, "<f8", cnt, off).reshape(ni * nj, nmu).copy()
+            off += 8 * cnt
+            if np.abs(m).max() >= cs_threshold:
+                Cs[(I - 1, J - 1, (r1, r2, r3))] = m
+
+    aoff = np.concatenate([[0], np.cumsum(nabf_at)]).astype(int)
+    Vq = {}
+    for fn in sorted(glob.glob(d + "coulomb_mat*")):
+        raw = open(fn, "rb").read()
+        _nirk, nloc = struct.unpack_from("<2i", raw, 0)
+        off = 8
+        full = {}
+        for _ in range(nloc):
+            nbb, br, er, bc, ec, iq = struct.unpack_from("<6i", raw, off)
+            off += 24
+            off += 8  # q weight
+            br, er, bc, ec, iq = br - 1, er - 1, bc - 1, ec - 1, iq - 1
+            nr, nc = er - br + 1, ec - bc + 1
+            blk = np.frombuffer(raw, "<c16", nr * nc, off).reshape(nr, nc)
+            off += 16 * nr * nc
+            M = full.setdefault(iq, np.zeros((nbb, nbb), complex))
+            M[br:er + 1, bc:ec + 1] = blk
+        for iq, M in full.items():
+            for I in range(nat):
+                for J in range(I, nat):
+                    Vq[(iq, I, J)] = M[aoff[I]:aoff[I + 1], aoff[J]:aoff[J + 1]].copy()
+
+    return RPAInput(n_spins=ns, n_kpts=nk, n_bands=nb, n_ao=nao, wg=wg, ekb=ekb, efermi=efermi,
+                    wfc=wfc, latvec=lat, period=period, kvecs=kv, ibz_map=ibz,
+                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos)

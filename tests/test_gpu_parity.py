@@ -1,0 +1,82 @@
+"""GPU path vs the oracle through the C ABI (needs a GB300)."""
+import numpy as np
+import pytest
+
+import librpa_gb300 as L
+from conftest import load_h2o, oracle_input
+from librpa_gb300 import synthetic as sy
+from oracle.rpa_oracle import Options as OOpts, rpa_correlation_energy
+
+pytestmark = pytest.mark.gpu
+
+MEV_PER_ATOM = 3.674932e-6  # 0.1 meV in Hartree
+
+
+def _opts(s):
+    return L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                     minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
+
+
+def run_gpu(s, prec, keep=False, ec_path=L.EC_LU_FP64):
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=prec, keep_chi0=int(keep), ec_path=ec_path))
+    ec, perq = h.get_rpa_correlation_energy(_opts(s), L.n_ibz(s))
+    return h, ec, perq
+
+
+def run_oracle(s):
+    return rpa_correlation_energy(oracle_input(s), OOpts(nfreq=s.nfreq, minimax_emin=s.minimax_emin,
+                                                         minimax_emax=s.minimax_emax))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(lib):
+    if lib.librpa_gb300_device_count() == 0:
+        pytest.fail("no CUDA device visible for a gpu-marked test")
+
+
+def test_h2o_regression_fp64():
+    """H2O regression dataset: GPU FP64 path vs the reference's printed E_c and the oracle."""
+    s = load_h2o()
+    h, ec, perq = run_gpu(s, L.CHI0_FP64)
+    o = run_oracle(s)
+    assert abs(ec - s.ec_reference) < 5e-9
+    assert abs(ec - o["ec"].real) < 1e-11
+    assert abs(perq[0] - o["per_q"][0]) < 1e-11
+    st = h.stats()
+    assert st["n_launches"] > 0 and st["chi0_flops"] > 0
+
+
+@pytest.mark.parametrize("period,nao,nabf,nocc", [((2, 1, 1), [3, 5], [7, 10], 2), ((3, 1, 1), [4, 2], [6, 9], 2),
+                                                  ((2, 2, 1), [3, 3], [5, 5], 1), ((1, 1, 1), [2, 4, 3], [4, 6, 5], 3),
+                                                  ((3, 2, 1), [5, 4], [12, 9], 3)])
+def test_small_periodic_fp64_vs_oracle(period, nao, nabf, nocc):
+    s = sy.small_periodic(n_atoms=len(nao), nao=nao, nabf=nabf, period=period, nocc=nocc, seed=21)
+    h, ec, perq = run_gpu(s, L.CHI0_FP64, keep=True)
+    o = run_oracle(s)
+    assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
+    np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
+    # chi0(q, w) blocks
+    for iw in (0, s.nfreq // 2, s.nfreq - 1):
+        for iq in range(L.n_ibz(s)):
+            for (I, J), ref in o["chi0q"][iw][iq].items():
+                got = h.get_chi0_block(iw, iq, I, J, s.nabf[I], s.nabf[J])
+                np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
+
+
+def test_fcc2_k222_fp64_vs_oracle():
+    s = sy.fcc2_k222()
+    h, ec, perq = run_gpu(s, L.CHI0_FP64)
+    o = run_oracle(s)
+    assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
+    np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("prec", [L.CHI0_FP32])
+def test_reduced_precision_within_tolerance(prec):
+    """Reduced-precision chi0 paths stay within 0.1 meV/atom of the FP64 GPU path."""
+    s = sy.fcc2_k222()
+    _, e64, _ = run_gpu(s, L.CHI0_FP64)
+    _, e, _ = run_gpu(s, prec)
+    assert abs(e - e64) <= MEV_PER_ATOM * len(s.nao)
