@@ -98,6 +98,11 @@ int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq_ibz, int I, 
 /* Number of CUDA devices visible (0 when there is no GPU). */
 int librpa_gb300_device_count(void);
 
+/* Diagnostic: a random M x N x K product through the tcgen05 split-precision GEMM
+ * (pieces = 2: 3 BF16 products; 3: 6 BF16 products) compared on the device with the FP64
+ * CUDA-core GEMM.  Returns max|diff| / max|ref| (NaN on error). */
+double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces);
+
 #ifdef __cplusplus
 }
 #endif

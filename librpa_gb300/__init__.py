@@ -129,7 +129,7 @@ EXPORTS = [
     "librpa_get_g0w0_sigc_kgrid", "librpa_get_g0w0_sigc_band_k",
     "librpa_gb300_init_options", "librpa_gb300_set_options", "librpa_gb300_get_stats",
     "librpa_get_last_error", "librpa_get_last_error_code", "librpa_gb300_minimax_grid",
-    "librpa_gb300_get_chi0_block", "librpa_gb300_device_count",
+    "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
 ]
 
 _lib = None
@@ -179,6 +179,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_minimax_grid": (i, [i, d, d, d, _dp, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(d)]),
         "librpa_gb300_get_chi0_block": (i, [vp, i, i, i, i, _dp, _dp]),
         "librpa_gb300_device_count": (i, []),
+        "librpa_gb300_selftest_tc_gemm": (d, [i, i, i, i, i]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -17,6 +17,7 @@
 #include "common.h"
 #include "dataset.h"
 #include "minimax.h"
+#include "tc_gemm.h"
 
 namespace {
 
@@ -865,5 +866,15 @@ int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq, int I, int 
 }
 
 int librpa_gb300_device_count(void) { return gb::device_count(); }
+
+double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces)
+{
+    double r = std::numeric_limits<double>::quiet_NaN();
+    guarded(nullptr, [&] {
+        GB_REQUIRE(gb::device_count() > 0, "no CUDA device visible");
+        r = gb::tc_gemm_selftest(M, N, K, seed, pieces);
+    });
+    return r;
+}
 
 } // extern "C"

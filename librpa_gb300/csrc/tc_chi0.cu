@@ -1,0 +1,663 @@
+// Tensor-core chi0 path (BF16 split products on tcgen05, FP32 accumulation).
+//
+// Per (tau, spin), with the algebra of k_chi0_simt.cu:
+//  1. X(+-) = C * G_super(+-): one batched split-precision GEMM (k_tc_gemm.cu); the B operand
+//     G_super^T is built and split directly from G(R).
+//  2. T1 (fused, this file): for each upper atom pair (I, J) and a tile of 128 rows
+//     (cell cJ, mu), accumulate in TMEM
+//        D[(cJ,mu)][nu] = sum_{pass} sum_{j, K'} E[(cJ,mu)][j, K'] * C^J[nu][j, K']
+//        E[(cJ,mu)][j, K'] = sum_i Ga[cJ]_{ij} X_b^I[mu i][shift_cJ(K')]
+//     where K' runs over the supercell orbitals (cell R', atom L, orbital l) of C^J's own
+//     frame and shift_cJ maps R' -> R' + R_cJ (the T1 term with R_L = R' + R_J).
+//     Sixteen producer warps form E in FP32 on the CUDA cores, split it into BF16 pieces and
+//     write the 128 x 64 A tile of each pipeline stage into swizzled shared memory; one lane
+//     streams the matching C^J tile (64 K-elements per row, pre-arranged in HBM) with TMA and
+//     one lane issues the tcgen05.mma terms.  K order: pass, 16-column chunk, group of 4 j.
+//  3. T2 (small, CUDA cores): D += sum_{i,j} X_b^I[mu i; (cJ,J) j] X_a^J[nu j; (-cJ,I) i].
+// Every wait is bounded (tc_common.cuh) and failures surface through a device error flag.
+#include <cstdlib>
+#include <vector>
+
+#include "../../include/librpa_gb300.h"
+#include "tc_common.cuh"
+#include "tc_gemm.h"
+
+namespace gb {
+
+namespace {
+
+using namespace tc;
+
+constexpr int NS = 3;            // BF16 pieces per operand (hi, mid, lo): 6 MMA terms
+constexpr int T1_BM = 128;       // rows (cJ, mu) per CTA
+constexpr int CW = 8;            // supercell columns per chunk
+constexpr int JG = 8;            // j per pipeline stage (JG * CW = 64 = K per stage)
+constexpr int T1_STAGES = 2;
+constexpr int T1_NMAX = 128;     // max N tile (ABFs of one atom, padded to 16)
+constexpr int PRODUCERS = 512;   // warps 0-15: E tiles (4 threads per row, 2 columns each)
+constexpr int DRAIN_WARP0 = 16;  // warps 16-19: accumulator drain + epilogue
+constexpr int CTRL_WARP = 20;    // warp 20: TMA + MMA issue
+constexpr int T1_THREADS = 21 * 32;
+constexpr int A_TILE = T1_BM * 64 * 2;       // bytes per A piece
+constexpr int T1_MAXA = 32;                  // max NAOs per atom (G buffer row stride)
+constexpr int T1_SMEM_MAX = 227 * 1024;
+// Shared memory: T1_STAGES x [NS A pieces | NS B pieces of b_tile bytes] | G blocks | barriers.
+// b_tile = NT_max * 128 rounded up to 1024; G blocks hold maxcj cells x RA x T1_MAXA floats.
+
+struct T1Work
+{
+    int pair, tile;
+};
+
+constexpr int T1_MAXSPEC = 8;    // distinct (NAO, ABF) species with their own B maps
+
+// C^J B-operand maps, one rank-3 map per (species, piece): dims {ktot, nabf, atoms of the species}.
+struct T1Maps
+{
+    CUtensorMap m[T1_MAXSPEC][3];
+    long long ktot[T1_MAXSPEC];
+};
+
+struct T1Args
+{
+    Geom g;
+    Pairs pr;
+    const float *X;          // [2][rows_c][n_sup]: sign 0 = X(+), sign 1 = X(-)
+    long long xsign;         // rows_c * n_sup
+    const double *G;         // [2][n_c][n_ao][n_ao]
+    const int *cadd;         // [n_c*n_c] cadd[a*n_c+b] = cell of R_a + R_b
+    const T1Work *work;
+    const int *spec;           // [n_at] species of each atom
+    const int *spec_idx;       // [n_at] index of the atom inside its species
+    const int *aJpad;          // NAOs of each atom rounded up to JG
+    int nkc;                   // number of CW-wide chunks of the supercell axis
+    int b_tile;                // bytes per B piece (1024-aligned)
+    int maxcj;                 // distinct cells a 128-row tile can span
+    double *out;               // chi0R
+    int *err;
+};
+
+__device__ __forceinline__ void named_bar_sync(int id, int n)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b)
+{
+    return static_cast<uint32_t>(__bfloat16_as_ushort(a)) | (static_cast<uint32_t>(__bfloat16_as_ushort(b)) << 16);
+}
+
+// RA: register blocking over the NAOs i of atom I (16 or 32); NTC: accumulator columns
+// held by the drain warps (64 or 128).
+template <int RA, int NTC>
+__global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__ T1Args a,
+                                                        const __grid_constant__ T1Maps maps)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int stage_bytes = NS * (A_TILE + a.b_tile);
+    const int g_floats = a.maxcj * RA * T1_MAXA;
+    float *gsm = reinterpret_cast<float *>(smem + T1_STAGES * stage_bytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(gsm + g_floats);
+    uint64_t *empty = full + T1_STAGES;
+    uint64_t *accf = empty + T1_STAGES;
+    uint64_t *acce = accf + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acce + 2);
+
+    const Geom &g = a.g;
+    const T1Work w = a.work[blockIdx.x];
+    const int I = a.pr.I[w.pair], J = a.pr.J[w.pair];
+    const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
+    const int njg = a.aJpad[J] / JG;
+    const int NT = (bJ + 15) / 16 * 16;
+    const uint32_t tcols = NTC;          // columns per accumulator
+    const int nc = g.n_c, nao = g.n_ao;
+    const long long nsup = g.n_sup;
+    const int row0 = w.tile * T1_BM;
+    const int cj_min = row0 / bI;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int total_stages = 2 * a.nkc * njg;
+
+    if (threadIdx.x == 0)
+    {
+        for (int s = 0; s < T1_STAGES; ++s)
+        {
+            mbar_init(&full[s], PRODUCERS + 1);
+            mbar_init(&empty[s], 1);
+        }
+        for (int i = 0; i < 2; ++i)
+        {
+            mbar_init(&accf[i], 1);
+            mbar_init(&acce[i], 128);
+        }
+        fence_barrier_init();
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, 4 * tcols);
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (threadIdx.x < PRODUCERS)
+    {
+        // ---------------- producers: E tiles
+        const int t = threadIdx.x;
+        const int r = t >> 2;           // row in tile
+        const int cg = t & 3;           // 2-column group inside the 8-column chunk
+        const int rg = row0 + r;
+        const bool valid = rg < nc * bI;
+        const int cJ = valid ? rg / bI : 0;
+        const int mu = valid ? rg % bI : 0;
+        const int cjl = valid ? cJ - cj_min : 0;
+        const long long xrow = g.rowc_off[I] + static_cast<long long>(mu) * aI;
+        bool ok = true;
+        int st_count = 0;
+        for (int pass = 0; pass < 2 && ok; ++pass)
+        {
+            // Ga blocks of this pass for the tile's cells, FP32 in shared memory
+            named_bar_sync(1, PRODUCERS);
+            const int ncj = min(a.maxcj, (min(row0 + T1_BM, nc * bI) - 1) / bI - cj_min + 1);
+            const double *Ga = a.G + static_cast<size_t>(pass) * nc * nao * nao;
+            for (int e = t; e < ncj * RA * T1_MAXA; e += PRODUCERS)
+            {
+                const int cl = e / (RA * T1_MAXA), ij = e % (RA * T1_MAXA);
+                const int i = ij / T1_MAXA, j = ij % T1_MAXA;
+                float v = 0.0f;
+                if (i < aI && j < aJ)
+                    v = static_cast<float>(Ga[(static_cast<size_t>(cj_min + cl) * nao + g.ao_off[I] + i) * nao +
+                                              g.ao_off[J] + j]);
+                gsm[e] = v;
+            }
+            named_bar_sync(1, PRODUCERS);
+            const float *Xb = a.X + (pass == 0 ? a.xsign : 0);  // pass 0: Ga = G+, X_b from G-
+            const float *gr = gsm + cjl * RA * T1_MAXA;
+            for (int kc = 0; kc < a.nkc && ok; ++kc)
+            {
+                float xr[RA][2];
+                int srcc[2];
+#pragma unroll
+                for (int q = 0; q < 2; ++q)
+                {
+                    const long long col = static_cast<long long>(kc) * CW + cg * 2 + q;
+                    if (col < nsup && valid)
+                    {
+                        const int cp = static_cast<int>(col / nao), ao = static_cast<int>(col % nao);
+                        srcc[q] = a.cadd[cp * nc + cJ] * nao + ao;
+                    }
+                    else
+                        srcc[q] = -1;
+                }
+#pragma unroll
+                for (int i = 0; i < RA; ++i)
+                {
+#pragma unroll
+                    for (int q = 0; q < 2; ++q)
+                        xr[i][q] = (i < aI && srcc[q] >= 0) ? Xb[(xrow + i) * nsup + srcc[q]] : 0.0f;
+                }
+                for (int jg = 0; jg < njg; ++jg, ++st_count)
+                {
+                    const int s = st_count % T1_STAGES, rr = st_count / T1_STAGES;
+                    if (!mbar_wait(&empty[s], (rr & 1) ^ 1))
+                    {
+                        atomicExch(a.err, 201);
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *stg = smem + s * stage_bytes;
+#pragma unroll
+                    for (int jl = 0; jl < JG; ++jl)
+                    {
+                        const int j = jg * JG + jl;  // zero G columns beyond aJ give zero E
+                        float e0 = 0.f, e1 = 0.f;
+#pragma unroll
+                        for (int i = 0; i < RA; ++i)
+                        {
+                            const float gij = gr[i * T1_MAXA + j];
+                            e0 = fmaf(gij, xr[i][0], e0);
+                            e1 = fmaf(gij, xr[i][1], e1);
+                        }
+                        const __nv_bfloat16 h0 = __float2bfloat16_rn(e0), h1 = __float2bfloat16_rn(e1);
+                        const float r0 = e0 - __bfloat162float(h0), r1 = e1 - __bfloat162float(h1);
+                        const __nv_bfloat16 m0 = __float2bfloat16_rn(r0), m1 = __float2bfloat16_rn(r1);
+                        const __nv_bfloat16 l0 = __float2bfloat16_rn(r0 - __bfloat162float(m0));
+                        const __nv_bfloat16 l1 = __float2bfloat16_rn(r1 - __bfloat162float(m1));
+                        const uint32_t off = sw128_offset(r, jl * CW + cg * 2);
+                        *reinterpret_cast<uint32_t *>(stg + off) = pack_bf16(h0, h1);
+                        *reinterpret_cast<uint32_t *>(stg + A_TILE + off) = pack_bf16(m0, m1);
+                        *reinterpret_cast<uint32_t *>(stg + 2 * A_TILE + off) = pack_bf16(l0, l1);
+                    }
+                    fence_proxy_async_smem();
+                    mbar_arrive(&full[s]);
+                }
+            }
+        }
+    }
+    else if (warp == CTRL_WARP)
+    {
+        if (lane == 0)
+        {
+            // ---------------- TMA for C^J tiles and MMA issue
+            const uint32_t idesc = idesc_bf16_f32(T1_BM, NT);
+            const uint32_t bbytes = static_cast<uint32_t>(NT) * 64 * 2;
+            const int sp = a.spec[J], zj = a.spec_idx[J];
+            const long long ktot = maps.ktot[sp];
+            for (int st = 0; st < total_stages; ++st)
+            {
+                const int s = st % T1_STAGES, rr = st / T1_STAGES;
+                const int ab = st & 1;
+                if (!mbar_wait(&empty[s], (rr & 1) ^ 1))
+                {
+                    atomicExch(a.err, 202);
+                    break;
+                }
+                const int rem = st % (a.nkc * njg);
+                const int x = rem * 64;  // K offset (kc * njg + jg) * 64
+                if (x < 0 || static_cast<long long>(x) + 64 > ktot || (x & 7) != 0)
+                {
+                    atomicExch(a.err, 205);  // coordinate outside the C^J operand: skip the copy
+                    break;
+                }
+                unsigned char *stg = smem + s * stage_bytes;
+                mbar_arrive_expect_tx(&full[s], NS * bbytes);
+#pragma unroll
+                for (int p = 0; p < NS; ++p)
+                    tma_load_3d(stg + NS * A_TILE + p * a.b_tile, &maps.m[sp][p], x, 0, zj, &full[s]);
+                if (!mbar_wait(&full[s], rr & 1) || !mbar_wait(&acce[ab], ((st >> 1) & 1) ^ 1))
+                {
+                    atomicExch(a.err, 203);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t t_hh = tmem + ab * 2 * tcols, t_x = t_hh + tcols;
+                uint64_t da[NS], db[NS];
+#pragma unroll
+                for (int p = 0; p < NS; ++p)
+                {
+                    da[p] = smem_desc_sw128(stg + p * A_TILE);
+                    db[p] = smem_desc_sw128(stg + NS * A_TILE + p * a.b_tile);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                {
+                    const uint64_t dk = static_cast<uint64_t>(k * 32 >> 4);
+                    // cross terms (smallest first) into t_x, hi*hi into t_hh; both restart each stage
+                    mma_bf16(t_x, da[2] + dk, db[0] + dk, idesc, k != 0);
+                    mma_bf16(t_x, da[0] + dk, db[2] + dk, idesc, 1);
+                    mma_bf16(t_x, da[1] + dk, db[1] + dk, idesc, 1);
+                    mma_bf16(t_x, da[1] + dk, db[0] + dk, idesc, 1);
+                    mma_bf16(t_x, da[0] + dk, db[1] + dk, idesc, 1);
+                    mma_bf16(t_hh, da[0] + dk, db[0] + dk, idesc, k != 0);
+                }
+                mma_commit(&empty[s]);
+                mma_commit(&accf[ab]);
+            }
+        }
+        __syncwarp();
+    }
+    else
+    {
+        // ---------------- drain warps: per-stage accumulator pairs -> FP32 registers -> chi0R
+        const int wq = warp - DRAIN_WARP0;
+        const uint32_t lane_base = static_cast<uint32_t>(wq * 32) << 16;
+        float acc[NTC];
+#pragma unroll
+        for (int c = 0; c < NTC; ++c) acc[c] = 0.0f;
+        bool ok = true;
+        for (int st = 0; st < total_stages; ++st)
+        {
+            const int ab = st & 1;
+            if (!mbar_wait(&accf[ab], (st >> 1) & 1))
+            {
+                atomicExch(a.err, 204);
+                ok = false;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t t_hh = tmem + ab * 2 * tcols, t_x = t_hh + tcols;
+#pragma unroll
+            for (int c0 = 0; c0 < NTC; c0 += 16)
+            {
+                if (c0 < NT)
+                {
+                    float v[16];
+                    tmem_ld16(t_x + lane_base + c0, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+                    tmem_ld16(t_hh + lane_base + c0, v);
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&acce[ab]);
+        }
+        const int r = wq * 32 + lane;
+        const int rg = row0 + r;
+        if (ok && rg < nc * bI)
+        {
+            const int cJ = rg / bI, mu = rg % bI;
+            double *orow = a.out + a.pr.r_off[w.pair] + (static_cast<long long>(cJ) * bI + mu) * bJ;
+#pragma unroll
+            for (int c = 0; c < NTC; ++c)
+                if (c < bJ) orow[c] = static_cast<double>(acc[c]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, 4 * tcols);
+}
+
+// T2 for one (pair, cJ): out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i]
+__global__ void __launch_bounds__(256) k_t2(const float *__restrict__ X, long long xsign, Geom g, Pairs pr,
+                                           double *__restrict__ out)
+{
+    __shared__ float s1[128 * 32];
+    __shared__ float s2[128 * 32];
+    const int p = blockIdx.x / g.n_c, cJ = blockIdx.x % g.n_c;
+    const int I = pr.I[p], J = pr.J[p];
+    const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
+    const long long nsup = g.n_sup;
+    const long long colJ = static_cast<long long>(cJ) * g.n_ao + g.ao_off[J];
+    const long long colI = static_cast<long long>(g.cneg[cJ]) * g.n_ao + g.ao_off[I];
+    double *o = out + pr.r_off[p] + static_cast<long long>(cJ) * bI * bJ;
+    const int nel = bI * bJ;
+    for (int e0 = 0; e0 < nel; e0 += 8 * 256)
+    {
+        float acc[8];
+        for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+        for (int pass = 0; pass < 2; ++pass)
+        {
+            const float *Xb = X + (pass == 0 ? xsign : 0);
+            const float *Xa = X + (pass == 0 ? 0 : xsign);
+            for (int i = 0; i < aI; ++i)
+            {
+                __syncthreads();
+                for (int t = threadIdx.x; t < bI * aJ; t += blockDim.x)
+                {
+                    const int mu = t / aJ, j = t % aJ;
+                    s1[mu * 32 + j] = Xb[(g.rowc_off[I] + static_cast<long long>(mu) * aI + i) * nsup + colJ + j];
+                }
+                for (int t = threadIdx.x; t < bJ * aJ; t += blockDim.x)
+                {
+                    const int nu = t / aJ, j = t % aJ;
+                    s2[nu * 32 + j] = Xa[(g.rowc_off[J] + static_cast<long long>(nu) * aJ + j) * nsup + colI + i];
+                }
+                __syncthreads();
+                for (int q = 0; q < 8; ++q)
+                {
+                    const int e = e0 + threadIdx.x + q * 256;
+                    if (e < nel)
+                    {
+                        const int mu = e / bJ, nu = e % bJ;
+                        float v = 0.f;
+                        for (int j = 0; j < aJ; ++j) v = fmaf(s1[mu * 32 + j], s2[nu * 32 + j], v);
+                        acc[q] += v;
+                    }
+                }
+            }
+        }
+        for (int q = 0; q < 8; ++q)
+        {
+            const int e = e0 + threadIdx.x + q * 256;
+            if (e < nel) o[e] += static_cast<double>(acc[q]);
+        }
+    }
+}
+
+// B operand of X = C * Gs: row n = (cL, l), column k = (cK, k'):  Gs^T[n][k] = G[cdiff(cL,cK)][k'][l]
+__global__ void k_gsT_split(const double *__restrict__ G, Geom g, long long kpad, __nv_bfloat16 *__restrict__ p0,
+                            __nv_bfloat16 *__restrict__ p1, __nv_bfloat16 *__restrict__ p2)
+{
+    const long long nsup = g.n_sup;
+    const int sign = blockIdx.y;
+    const long long n_el = nsup * kpad;
+    const int nao = g.n_ao, nc = g.n_c;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n_el;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long n = t / kpad, k = t % kpad;
+        double x = 0.0;
+        if (k < nsup)
+        {
+            const int cL = static_cast<int>(n / nao), l = static_cast<int>(n % nao);
+            const int cK = static_cast<int>(k / nao), kk = static_cast<int>(k % nao);
+            const int c = g.cdiff[cL * nc + cK];
+            x = G[((static_cast<size_t>(sign) * nc + c) * nao + kk) * nao + l];
+        }
+        const __nv_bfloat16 h = __double2bfloat16(x);
+        const double r1 = x - static_cast<double>(__bfloat162float(h));
+        const __nv_bfloat16 m = __double2bfloat16(r1);
+        const __nv_bfloat16 l = __double2bfloat16(r1 - static_cast<double>(__bfloat162float(m)));
+        p0[sign * n_el + t] = h;
+        p1[sign * n_el + t] = m;
+        p2[sign * n_el + t] = l;
+    }
+}
+
+// T1 B-operand layout of atom J: row nu, K index ((kc * aJpad + j) * CW + col) for
+// C^J[nu][j][kc*CW + col] (zero beyond the atom's NAOs and the supercell width).
+__global__ void k_cb_layout(const double *__restrict__ C, Geom g, int J, int ajp, int nkc, long long ktot,
+                            __nv_bfloat16 *__restrict__ p0, __nv_bfloat16 *__restrict__ p1,
+                            __nv_bfloat16 *__restrict__ p2)
+{
+    const int aJ = g.nao[J], bJ = g.nabf[J];
+    const long long n = static_cast<long long>(bJ) * ktot;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const int nu = static_cast<int>(t / ktot);
+        const long long k = t % ktot;
+        const long long kc = k / (static_cast<long long>(ajp) * CW);
+        const int rem = static_cast<int>(k % (static_cast<long long>(ajp) * CW));
+        const int j = rem / CW, col = rem % CW;
+        const long long c = kc * CW + col;
+        double x = 0.0;
+        if (j < aJ && c < g.n_sup) x = C[(g.rowc_off[J] + static_cast<long long>(nu) * aJ + j) * g.n_sup + c];
+        const __nv_bfloat16 h = __double2bfloat16(x);
+        const double r1 = x - static_cast<double>(__bfloat162float(h));
+        const __nv_bfloat16 m = __double2bfloat16(r1);
+        const __nv_bfloat16 l = __double2bfloat16(r1 - static_cast<double>(__bfloat162float(m)));
+        p0[t] = h;
+        p1[t] = m;
+        p2[t] = l;
+    }
+}
+
+} // namespace
+
+struct TcChi0::Impl
+{
+    Geom g;
+    Pairs pr;
+    long long kpad = 0;
+    int nkc = 0;
+    bool t1_simt = false;
+    SplitStore csplit, gs;
+    DevBuf<float> X, Gf, Cf;
+    DevBuf<int> err, cadd, ajpad;
+    DevBuf<T1Work> work;
+    int n_work = 0;
+    std::vector<SplitStore> cb;  // per species: C^J of its atoms, stacked
+    T1Maps maps{};
+    DevBuf<int> spec, spec_idx;
+    int b_tile = 0, maxcj = 0, smem = 0, ra = 16, ntc = 64;
+};
+
+namespace {
+using T1Fn = void (*)(T1Args, T1Maps);
+T1Fn t1_kernel(int ra, int ntc)
+{
+    if (ra == 16) return ntc == 64 ? k_t1_tc<16, 64> : k_t1_tc<16, 128>;
+    return ntc == 64 ? k_t1_tc<32, 64> : k_t1_tc<32, 128>;
+}
+} // namespace
+
+TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st) : impl_(std::make_unique<Impl>())
+{
+    Impl &m = *impl_;
+    m.g = g;
+    m.pr = pr;
+    const long long nsup = g.n_sup;
+    m.kpad = (nsup + 63) / 64 * 64;
+    m.nkc = static_cast<int>((nsup + CW - 1) / CW);
+    const char *env = std::getenv("LIBRPA_GB300_T1");
+    m.t1_simt = env && std::string(env) == "simt";
+    GB_REQUIRE(g.max_nao <= T1_MAXA, "the tensor-core chi0 kernel supports up to 32 NAOs per atom");
+    GB_REQUIRE(g.max_nabf <= T1_NMAX, "the tensor-core chi0 kernel supports up to 128 ABFs per atom");
+    m.csplit.alloc(NS, static_cast<size_t>(g.rows_c) * m.kpad);
+    split_rows_f64(C, nsup, g.rows_c, static_cast<int>(nsup), static_cast<int>(m.kpad), m.csplit.bufs(), st);
+    m.gs.alloc(NS, 2ull * nsup * m.kpad);
+    m.X.alloc(2ull * g.rows_c * nsup);
+    m.err.alloc(1);
+    m.err.zero(st);
+    // host copies of the small tables (Geom holds device pointers)
+    std::vector<int> nao(g.n_at), nabf(g.n_at), cdiff(static_cast<size_t>(g.n_c) * g.n_c);
+    GB_CUDA(cudaMemcpyAsync(nao.data(), g.nao, sizeof(int) * g.n_at, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(nabf.data(), g.nabf, sizeof(int) * g.n_at, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(cdiff.data(), g.cdiff, sizeof(int) * cdiff.size(), cudaMemcpyDeviceToHost, st));
+    std::vector<int> hI(pr.n_pairs), hJ(pr.n_pairs);
+    GB_CUDA(cudaMemcpyAsync(hI.data(), pr.I, sizeof(int) * pr.n_pairs, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaMemcpyAsync(hJ.data(), pr.J, sizeof(int) * pr.n_pairs, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    // cadd[a][b] = cell of R_a + R_b: the unique c with cdiff[c][b] == a
+    std::vector<int> cadd(cdiff.size(), -1);
+    for (int c = 0; c < g.n_c; ++c)
+        for (int b = 0; b < g.n_c; ++b) cadd[cdiff[c * g.n_c + b] * g.n_c + b] = c;
+    m.cadd.alloc(cadd.size());
+    m.cadd.upload(cadd.data(), cadd.size(), st);
+    if (m.t1_simt)
+    {
+        m.Cf.alloc(static_cast<size_t>(g.rows_c) * nsup);
+        launch_d2f(C, m.Cf.get(), g.rows_c * nsup, st);
+        m.Gf.alloc(2ull * g.n_c * g.n_ao * g.n_ao);
+        return;
+    }
+    // T1 B operands grouped by species (same NAO and ABF counts) and their TMA maps
+    std::vector<int> ajp(g.n_at), spec(g.n_at), spec_idx(g.n_at);
+    std::vector<std::pair<int, int>> species;
+    std::vector<int> spec_count;
+    for (int J = 0; J < g.n_at; ++J)
+    {
+        ajp[J] = (nao[J] + JG - 1) / JG * JG;
+        const std::pair<int, int> key{nao[J], nabf[J]};
+        int sp = -1;
+        for (size_t k = 0; k < species.size(); ++k)
+            if (species[k] == key) sp = static_cast<int>(k);
+        if (sp < 0)
+        {
+            sp = static_cast<int>(species.size());
+            species.push_back(key);
+            spec_count.push_back(0);
+        }
+        GB_REQUIRE(sp < T1_MAXSPEC, "the tensor-core chi0 kernel supports up to 8 atom species");
+        spec[J] = sp;
+        spec_idx[J] = spec_count[sp]++;
+    }
+    m.cb.resize(species.size());
+    for (size_t sp = 0; sp < species.size(); ++sp)
+    {
+        const int na = species[sp].first, nb = species[sp].second;
+        const int ap = (na + JG - 1) / JG * JG;
+        const long long ktot = static_cast<long long>(m.nkc) * ap * CW;
+        const long long per_atom = static_cast<long long>(nb) * ktot;
+        m.cb[sp].alloc(NS, static_cast<size_t>(per_atom) * spec_count[sp]);
+        const SplitBufs b = m.cb[sp].bufs();
+        for (int J = 0; J < g.n_at; ++J)
+        {
+            if (spec[J] != static_cast<int>(sp)) continue;
+            const long long o = per_atom * spec_idx[J];
+            k_cb_layout<<<static_cast<unsigned>(std::min<long long>((per_atom + 255) / 256, 152LL * 16)), 256, 0, st>>>(
+                C, g, J, ap, m.nkc, ktot, b.p[0] + o, b.p[1] + o, b.p[2] + o);
+            GB_LAUNCH_CHECK();
+        }
+        const int NT = (nb + 15) / 16 * 16;
+        for (int p = 0; p < NS; ++p)
+            make_tmap_bf16(&m.maps.m[sp][p], b.p[p], ktot, nb, spec_count[sp], ktot, per_atom, 64, NT);
+        m.maps.ktot[sp] = ktot;
+    }
+    m.ajpad.alloc(ajp.size());
+    m.ajpad.upload(ajp.data(), ajp.size(), st);
+    m.spec.alloc(spec.size());
+    m.spec.upload(spec.data(), spec.size(), st);
+    m.spec_idx.alloc(spec_idx.size());
+    m.spec_idx.upload(spec_idx.data(), spec_idx.size(), st);
+    std::vector<T1Work> work;
+    for (int p = 0; p < pr.n_pairs; ++p)
+    {
+        const int rows = g.n_c * nabf[hI[p]];
+        for (int t = 0; t * T1_BM < rows; ++t) work.push_back({p, t});
+    }
+    m.n_work = static_cast<int>(work.size());
+    m.work.alloc(work.size());
+    m.work.upload(work.data(), work.size(), st);
+    int ntmax = 16, minb = 1 << 30;
+    for (int J = 0; J < g.n_at; ++J)
+    {
+        ntmax = std::max(ntmax, (nabf[J] + 15) / 16 * 16);
+        minb = std::min(minb, nabf[J]);
+    }
+    m.b_tile = (ntmax * 128 + 1023) / 1024 * 1024;
+    m.maxcj = (T1_BM + minb - 1) / minb + 1;
+    m.ra = g.max_nao <= 16 ? 16 : 32;
+    m.ntc = ntmax <= 64 ? 64 : 128;
+    m.smem = T1_STAGES * NS * (A_TILE + m.b_tile) + m.maxcj * m.ra * T1_MAXA * 4 + 1024 + 256;
+    GB_REQUIRE(m.smem <= T1_SMEM_MAX, "chi0 tile does not fit shared memory (too many cells per tile or too many ABFs)");
+    GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc), cudaFuncAttributeMaxDynamicSharedMemorySize, m.smem));
+    GB_CUDA(cudaStreamSynchronize(st));
+}
+
+TcChi0::~TcChi0() = default;
+
+int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t st)
+{
+    (void)Gs;
+    Impl &m = *impl_;
+    const Geom &g = m.g;
+    const long long nsup = g.n_sup;
+    dim3 grid(static_cast<unsigned>(std::min<long long>((nsup * m.kpad + 255) / 256, 152LL * 32)), 2);
+    const SplitBufs gb = m.gs.bufs();
+    k_gsT_split<<<grid, 256, 0, st>>>(G, g, m.kpad, gb.p[0], gb.p[1], gb.p[2]);
+    GB_LAUNCH_CHECK();
+    tc_gemm_split(m.csplit.mat(g.rows_c, m.kpad, 0), m.gs.mat(nsup, m.kpad, nsup * m.kpad), static_cast<int>(g.rows_c),
+                  static_cast<int>(nsup), static_cast<int>(nsup), 2, m.X.get(), nsup, g.rows_c * nsup, false,
+                  m.err.get(), st);
+    int launches = 2;
+    if (m.t1_simt)
+    {
+        const long long ng = static_cast<long long>(g.n_c) * g.n_ao * g.n_ao;
+        launch_d2f(G, m.Gf.get(), 2 * ng, st);
+        launch_chi0_fp32(m.X.get(), m.X.get() + g.rows_c * nsup, m.Cf.get(), m.Gf.get(), m.Gf.get() + ng, g, m.pr,
+                         chi0R, st);
+        launches += 2;
+    }
+    else
+    {
+        T1Args a;
+        a.g = g;
+        a.pr = m.pr;
+        a.X = m.X.get();
+        a.xsign = g.rows_c * nsup;
+        a.G = G;
+        a.cadd = m.cadd.get();
+        a.work = m.work.get();
+        a.spec = m.spec.get();
+        a.spec_idx = m.spec_idx.get();
+        a.aJpad = m.ajpad.get();
+        a.nkc = m.nkc;
+        a.b_tile = m.b_tile;
+        a.maxcj = m.maxcj;
+        a.out = chi0R;
+        a.err = m.err.get();
+        t1_kernel(m.ra, m.ntc)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
+        GB_LAUNCH_CHECK();
+        k_t2<<<m.pr.n_pairs * g.n_c, 256, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, chi0R);
+        GB_LAUNCH_CHECK();
+        launches += 2;
+    }
+    int herr = 0;
+    m.err.download(&herr, 1, st);
+    GB_CUDA(cudaStreamSynchronize(st));
+    GB_REQUIRE(herr == 0, "tensor-core chi0 kernel reported wait timeout code " + std::to_string(herr));
+    return launches;
+}
+
+} // namespace gb

@@ -1,6 +1,10 @@
-// tcgen05 (5th-generation tensor core) chi0 path: BF16 3-term split products,
-// FP32 accumulation in TMEM, operands staged to shared memory by TMA.
+// tcgen05 (5th-generation tensor core) building blocks: BF16 hi/lo split
+// operands, TMA descriptors, the split-precision GEMM, and the chi0 path built
+// on them.
 #pragma once
+
+#include <cuda.h>
+#include <cuda_bf16.h>
 
 #include <memory>
 
@@ -8,6 +12,62 @@
 #include "kernels.h"
 
 namespace gb {
+
+// A K-major operand held as ns = 2 (hi, lo) or ns = 3 (hi, mid, lo) BF16 pieces:
+// rows x kpad (kpad a multiple of 64), batch_stride elements between batch entries
+// (0: the same matrix for every batch entry).
+struct SplitMat
+{
+    int ns;
+    const __nv_bfloat16 *p[3];
+    long long rows;
+    long long kpad;
+    long long batch_stride;
+};
+
+struct SplitBufs
+{
+    int ns;
+    __nv_bfloat16 *p[3];
+};
+
+// Owning storage for the pieces of one split operand.
+struct SplitStore
+{
+    int ns = 0;
+    DevBuf<__nv_bfloat16> piece[3];
+    SplitStore() = default;
+    SplitStore(int n, size_t elems) { alloc(n, elems); }
+    void alloc(int n, size_t elems)
+    {
+        ns = n;
+        for (int i = 0; i < 3; ++i)
+            if (i < n) piece[i].alloc(elems);
+            else piece[i].release();
+    }
+    SplitBufs bufs() const { return {ns, {piece[0].get(), piece[1].get(), ns == 3 ? piece[2].get() : nullptr}}; }
+    SplitMat mat(long long rows, long long kpad, long long batch_stride) const
+    {
+        return {ns, {piece[0].get(), piece[1].get(), ns == 3 ? piece[2].get() : nullptr}, rows, kpad, batch_stride};
+    }
+};
+
+void make_tmap_bf16(CUtensorMap *map, const void *base, long long inner, long long rows, long long batch,
+                    long long row_stride_elems, long long batch_stride_elems, int box_inner, int box_rows);
+// split of row-major [rows][cols] into [rows][kpad] pieces (zero padded)
+void split_rows_f64(const double *src, long long lds, long long rows, int cols, int kpad, const SplitBufs &o,
+                    cudaStream_t st);
+void split_rows_f32(const float *src, long long lds, long long rows, int cols, int kpad, const SplitBufs &o,
+                    cudaStream_t st);
+// split of the transpose: src [K][N] row-major -> dst [N][kpad]
+void split_transpose_f64(const double *src, long long lds, int K, int N, int kpad, const SplitBufs &o,
+                         cudaStream_t st);
+// D[b] (+)= A[b] * B[b]^T from BF16 split pieces (ns = 2: 3 products, ns = 3: 6 products),
+// FP32 TMEM accumulation.
+void tc_gemm_split(const SplitMat &A, const SplitMat &B, int M, int N, int K, int batch, float *D, long long ldd,
+                   long long sD, bool accumulate, int *err, cudaStream_t st);
+// Random M x N x K product vs the FP64 SIMT GEMM on the device; returns max |diff| / max |ref|.
+double tc_gemm_selftest(int M, int N, int K, int seed, int ns);
 
 class TcChi0
 {

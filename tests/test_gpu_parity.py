@@ -73,7 +73,7 @@ def test_fcc2_k222_fp64_vs_oracle():
     np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
 
 
-@pytest.mark.parametrize("prec", [L.CHI0_FP32])
+@pytest.mark.parametrize("prec", [L.CHI0_FP32, L.CHI0_BF16X3])
 def test_reduced_precision_within_tolerance(prec):
     """Reduced-precision chi0 paths stay within 0.1 meV/atom of the FP64 GPU path."""
     s = sy.fcc2_k222()
