@@ -1,0 +1,359 @@
+// E_c stage on the tensor cores + FP64 Cholesky.
+//
+// LibRPA evaluates, per IBZ q and frequency w (epsilon.cpp:414-536),
+//   e(q,w) = ln det(I - V chi0) + tr(V chi0)
+// with an LU of I - V chi0.  With V = L L^H (V is Hermitian positive definite),
+//   det(I - V chi0) = det(I - L^H chi0 L)
+// and M' = I - L^H chi0 L is Hermitian positive definite (chi0 is negative semidefinite),
+// so ln det comes from an FP64 Cholesky: ln det M' = 2 sum log L'_ii.  The two N^3
+// products L^H chi0 L run on tcgen05 with 3-piece BF16 operands; complex matrices use
+// the real embedding [[Re, -Im], [Im, Re]].  tr(V chi0) = sum_ij V_ij conj(chi0_ij) in FP64.
+#include <cuComplex.h>
+
+#include <vector>
+
+#include "chol.h"
+#include "common.h"
+#include "ec_tc.h"
+#include "kernels.h"
+#include "tc_gemm.h"
+
+namespace gb {
+
+namespace {
+
+__device__ __forceinline__ void split3(double x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l)
+{
+    h = __double2bfloat16(x);
+    const double r1 = x - static_cast<double>(__bfloat162float(h));
+    m = __double2bfloat16(r1);
+    l = __double2bfloat16(r1 - static_cast<double>(__bfloat162float(m)));
+}
+
+// A operand (2M x kpad) of the embedding of X (M x K complex): rows r < M: [Re X, -Im X],
+// rows M + r: [Im X, Re X].  X(r,k) = src[r][k], or conj(src[k][r]) when ctrans.
+__global__ void k_embed_A(const cuDoubleComplex *__restrict__ src, long long sstride, int M, int K, int kpad,
+                          bool ctrans, __nv_bfloat16 *__restrict__ p0, __nv_bfloat16 *__restrict__ p1,
+                          __nv_bfloat16 *__restrict__ p2, long long ostride)
+{
+    const int b = blockIdx.y;
+    const cuDoubleComplex *S = src + b * sstride;
+    const long long n = 2LL * M * kpad;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const int row = static_cast<int>(t / kpad), col = static_cast<int>(t % kpad);
+        double x = 0.0;
+        if (col < 2 * K)
+        {
+            const int r = row < M ? row : row - M;
+            const int k = col < K ? col : col - K;
+            cuDoubleComplex v = ctrans ? S[static_cast<long long>(k) * M + r] : S[static_cast<long long>(r) * K + k];
+            if (ctrans) v.y = -v.y;
+            const bool top = row < M, left = col < K;
+            x = top ? (left ? v.x : -v.y) : (left ? v.y : v.x);
+        }
+        __nv_bfloat16 h, m, l;
+        split3(x, h, m, l);
+        const long long o = b * ostride + t;
+        p0[o] = h;
+        p1[o] = m;
+        p2[o] = l;
+    }
+}
+
+// B operand (N x kpad, K-major) of the embedding [Re Y; Im Y] of Y (K x N complex): row n = [Re Y(:,n), Im Y(:,n)].
+__global__ void k_embed_Bt(const cuDoubleComplex *__restrict__ Y, int K, int N, int kpad,
+                           __nv_bfloat16 *__restrict__ p0, __nv_bfloat16 *__restrict__ p1,
+                           __nv_bfloat16 *__restrict__ p2)
+{
+    const long long n = static_cast<long long>(N) * kpad;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const int row = static_cast<int>(t / kpad), col = static_cast<int>(t % kpad);
+        double x = 0.0;
+        if (col < 2 * K)
+        {
+            const int k = col < K ? col : col - K;
+            const cuDoubleComplex v = Y[static_cast<long long>(k) * N + row];
+            x = col < K ? v.x : v.y;
+        }
+        __nv_bfloat16 h, m, l;
+        split3(x, h, m, l);
+        p0[t] = h;
+        p1[t] = m;
+        p2[t] = l;
+    }
+}
+
+// K-major B operand of a row-major FP32 matrix S (K x N): row n = S(:, n) (batched).
+__global__ void k_split_T_f32(const float *__restrict__ S, long long sstride, int K, int N, int kpad,
+                              __nv_bfloat16 *__restrict__ p0, __nv_bfloat16 *__restrict__ p1,
+                              __nv_bfloat16 *__restrict__ p2, long long ostride)
+{
+    __shared__ float tile[32][33];
+    const int b = blockIdx.z;
+    const float *Sb = S + b * sstride;
+    const int k0 = blockIdx.x * 32, n0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+    {
+        const int k = k0 + i, n = n0 + threadIdx.x;
+        tile[i][threadIdx.x] = (k < K && n < N) ? Sb[static_cast<long long>(k) * N + n] : 0.0f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y)
+    {
+        const int n = n0 + i, k = k0 + threadIdx.x;
+        if (n < N && k < kpad)
+        {
+            __nv_bfloat16 h, m, l;
+            split3(static_cast<double>(tile[threadIdx.x][i]), h, m, l);
+            const long long o = b * ostride + static_cast<long long>(n) * kpad + k;
+            p0[o] = h;
+            p1[o] = m;
+            p2[o] = l;
+        }
+    }
+}
+
+// M'[b] = I - (Mstack real part + i imag part), Mstack = [Re; Im] (2N x N FP32)
+__global__ void k_form_mprime_c(const float *__restrict__ Ms, int N, cuDoubleComplex *__restrict__ Mp)
+{
+    const int b = blockIdx.y;
+    const long long nn = static_cast<long long>(N) * N;
+    const float *S = Ms + b * 2 * nn;
+    cuDoubleComplex *O = Mp + b * nn;
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const bool d = (e / N) == (e % N);
+        O[e] = make_cuDoubleComplex((d ? 1.0 : 0.0) - static_cast<double>(S[e]), -static_cast<double>(S[nn + e]));
+    }
+}
+
+__global__ void k_form_mprime_r(const float *__restrict__ Ms, int N, double *__restrict__ Mp)
+{
+    const int b = blockIdx.y;
+    const long long nn = static_cast<long long>(N) * N;
+    const float *S = Ms + b * nn;
+    double *O = Mp + b * nn;
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const bool d = (e / N) == (e % N);
+        O[e] = (d ? 1.0 : 0.0) - static_cast<double>(S[e]);
+    }
+}
+
+// tr(V X[b]) = sum_ij V_ij X_ji (full matrices), FP64, one CTA per batch entry
+__global__ void k_trace_prod_c(const cuDoubleComplex *__restrict__ V, const cuDoubleComplex *__restrict__ X, int N,
+                               cuDoubleComplex *__restrict__ out)
+{
+    __shared__ double rr[256], ri[256];
+    const long long nn = static_cast<long long>(N) * N;
+    const cuDoubleComplex *Xb = X + blockIdx.x * nn;
+    double ar = 0.0, ai = 0.0;
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x)
+    {
+        const long long i = e / N, j = e % N;
+        const cuDoubleComplex v = V[e], x = Xb[j * N + i];
+        ar += v.x * x.x - v.y * x.y;
+        ai += v.x * x.y + v.y * x.x;
+    }
+    rr[threadIdx.x] = ar;
+    ri[threadIdx.x] = ai;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1)
+    {
+        if (threadIdx.x < s)
+        {
+            rr[threadIdx.x] += rr[threadIdx.x + s];
+            ri[threadIdx.x] += ri[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = make_cuDoubleComplex(rr[0], ri[0]);
+}
+
+__global__ void k_trace_prod_r(const double *__restrict__ V, const double *__restrict__ X, int N,
+                               double *__restrict__ out)
+{
+    __shared__ double rr[256];
+    const long long nn = static_cast<long long>(N) * N;
+    const double *Xb = X + blockIdx.x * nn;
+    double a = 0.0;
+    for (long long e = threadIdx.x; e < nn; e += blockDim.x)
+    {
+        const long long i = e / N, j = e % N;
+        a += V[e] * Xb[j * N + i];
+    }
+    rr[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1)
+    {
+        if (threadIdx.x < s) rr[threadIdx.x] += rr[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = rr[0];
+}
+
+unsigned blocks_for(long long n) { return static_cast<unsigned>(std::min<long long>((n + 255) / 256, 152LL * 16)); }
+
+} // namespace
+
+struct EcChol::Impl
+{
+    int N = 0, nw = 0;
+    bool cplx = true;
+    long long kpad = 0;
+    DevBuf<int> err, bad;
+    // per-q
+    SplitStore Bl, Al;            // L as B^T and L^H (or L^T) as A
+    DevBuf<double> diagV;
+    // per-(q, w) batch
+    SplitStore A1, B2;
+    DevBuf<float> Tst, Mst;
+    DevBuf<double> diag, logdet;
+    DevBuf<cuDoubleComplex> Mpc, trc;
+    DevBuf<double> Mpr, trr;
+};
+
+EcChol::EcChol(int N, int nw, bool complex_path) : impl_(std::make_unique<Impl>())
+{
+    Impl &m = *impl_;
+    m.N = N;
+    m.nw = nw;
+    m.cplx = complex_path;
+    const int kdim = complex_path ? 2 * N : N;
+    m.kpad = (kdim + 63) / 64 * 64;
+    const long long rowsA = kdim;  // rows of the A operands
+    m.err.alloc(1);
+    m.bad.alloc(nw);
+    m.Bl.alloc(3, static_cast<size_t>(N) * m.kpad);
+    m.Al.alloc(3, static_cast<size_t>(rowsA) * m.kpad);
+    m.diagV.alloc(N);
+    m.A1.alloc(3, static_cast<size_t>(nw) * rowsA * m.kpad);
+    m.B2.alloc(3, static_cast<size_t>(nw) * N * m.kpad);
+    m.Tst.alloc(static_cast<size_t>(nw) * rowsA * N);
+    m.Mst.alloc(static_cast<size_t>(nw) * rowsA * N);
+    m.diag.alloc(static_cast<size_t>(nw) * N);
+    m.logdet.alloc(nw);
+    if (complex_path)
+    {
+        m.Mpc.alloc(static_cast<size_t>(nw) * N * N);
+        m.trc.alloc(nw);
+    }
+    else
+    {
+        m.Mpr.alloc(static_cast<size_t>(nw) * N * N);
+        m.trr.alloc(nw);
+    }
+}
+
+EcChol::~EcChol() = default;
+
+int EcChol::run_q(void *V, void *X, std::vector<std::complex<double>> &trace_out,
+                  std::vector<std::complex<double>> &logdet_out, cudaStream_t st)
+{
+    Impl &m = *impl_;
+    const int N = m.N, nw = m.nw;
+    const long long nn = static_cast<long long>(N) * N;
+    int launches = 0;
+    m.err.zero(st);
+    m.bad.zero(st);
+    const SplitBufs bl = m.Bl.bufs(), al = m.Al.bufs(), a1 = m.A1.bufs(), b2 = m.B2.bufs();
+    const long long rowsA = m.cplx ? 2LL * N : N;
+    if (m.cplx)
+    {
+        cuDoubleComplex *Vc = static_cast<cuDoubleComplex *>(V);
+        cuDoubleComplex *Xc = static_cast<cuDoubleComplex *>(X);
+        k_trace_prod_c<<<nw, 256, 0, st>>>(Vc, Xc, N, m.trc.get());
+        GB_LAUNCH_CHECK();
+        // V = L L^H (V is overwritten by L)
+        launches += chol_batched_c(Vc, N, 1, m.diagV.get(), m.bad.get(), st);
+        zero_upper_c(Vc, N, 1, st);
+        k_embed_Bt<<<blocks_for(N * m.kpad), 256, 0, st>>>(Vc, N, N, static_cast<int>(m.kpad), bl.p[0], bl.p[1], bl.p[2]);
+        k_embed_A<<<dim3(blocks_for(rowsA * m.kpad), 1), 256, 0, st>>>(Vc, 0, N, N, static_cast<int>(m.kpad), true,
+                                                                        al.p[0], al.p[1], al.p[2], 0);
+        k_embed_A<<<dim3(blocks_for(rowsA * m.kpad), nw), 256, 0, st>>>(Xc, nn, N, N, static_cast<int>(m.kpad), false,
+                                                                         a1.p[0], a1.p[1], a1.p[2], rowsA * m.kpad);
+        GB_LAUNCH_CHECK();
+        launches += 5;
+    }
+    else
+    {
+        double *Vr = static_cast<double *>(V);
+        double *Xr = static_cast<double *>(X);
+        k_trace_prod_r<<<nw, 256, 0, st>>>(Vr, Xr, N, m.trr.get());
+        GB_LAUNCH_CHECK();
+        launches += chol_batched_r(Vr, N, 1, m.diagV.get(), m.bad.get(), st);
+        zero_upper_r(Vr, N, 1, st);
+        // B^T of L and A = L^T are the same K-major matrix: row n = L(:, n)
+        split_transpose_f64(Vr, N, N, N, static_cast<int>(m.kpad), bl, st);
+        split_transpose_f64(Vr, N, N, N, static_cast<int>(m.kpad), al, st);
+        for (int w = 0; w < nw; ++w)
+        {
+            SplitBufs aw{3, {a1.p[0] + w * rowsA * m.kpad, a1.p[1] + w * rowsA * m.kpad, a1.p[2] + w * rowsA * m.kpad}};
+            split_rows_f64(Xr + w * nn, N, N, N, static_cast<int>(m.kpad), aw, st);
+        }
+        launches += 4 + nw;
+    }
+    // T = chi0 L  (rowsA x N per w)
+    tc_gemm_split(m.A1.mat(rowsA, m.kpad, rowsA * m.kpad), m.Bl.mat(N, m.kpad, 0), static_cast<int>(rowsA), N,
+                  static_cast<int>(m.cplx ? 2 * N : N), nw, m.Tst.get(), N, rowsA * N, false, m.err.get(), st);
+    // B2 = K-major form of T (row n = T(:, n))
+    {
+        dim3 g(static_cast<unsigned>((m.kpad + 31) / 32), static_cast<unsigned>((N + 31) / 32), nw);
+        k_split_T_f32<<<g, dim3(32, 8), 0, st>>>(m.Tst.get(), rowsA * N, static_cast<int>(rowsA), N,
+                                                 static_cast<int>(m.kpad), b2.p[0], b2.p[1], b2.p[2], N * m.kpad);
+        GB_LAUNCH_CHECK();
+    }
+    // L^H T
+    tc_gemm_split(m.Al.mat(rowsA, m.kpad, 0), m.B2.mat(N, m.kpad, N * m.kpad), static_cast<int>(rowsA), N,
+                  static_cast<int>(m.cplx ? 2 * N : N), nw, m.Mst.get(), N, rowsA * N, false, m.err.get(), st);
+    launches += 3;
+    if (m.cplx)
+    {
+        k_form_mprime_c<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpc.get());
+        GB_LAUNCH_CHECK();
+        launches += 1 + chol_batched_c(m.Mpc.get(), N, nw, m.diag.get(), m.bad.get(), st);
+    }
+    else
+    {
+        k_form_mprime_r<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpr.get());
+        GB_LAUNCH_CHECK();
+        launches += 1 + chol_batched_r(m.Mpr.get(), N, nw, m.diag.get(), m.bad.get(), st);
+    }
+    chol_logdet(m.diag.get(), N, nw, m.logdet.get(), st);
+    ++launches;
+    std::vector<double> ld(nw);
+    std::vector<int> bad(nw);
+    int herr = 0;
+    m.logdet.download(ld.data(), nw, st);
+    m.bad.download(bad.data(), nw, st);
+    m.err.download(&herr, 1, st);
+    trace_out.assign(nw, {0.0, 0.0});
+    if (m.cplx)
+    {
+        std::vector<cuDoubleComplex> tr(nw);
+        m.trc.download(tr.data(), nw, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+        for (int w = 0; w < nw; ++w) trace_out[w] = {tr[w].x, tr[w].y};
+    }
+    else
+    {
+        std::vector<double> tr(nw);
+        m.trr.download(tr.data(), nw, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+        for (int w = 0; w < nw; ++w) trace_out[w] = {tr[w], 0.0};
+    }
+    GB_REQUIRE(herr == 0, "tensor-core E_c GEMM reported wait timeout code " + std::to_string(herr));
+    for (int w = 0; w < nw; ++w)
+        GB_REQUIRE(!bad[w], "I - L^H chi0 L is not positive definite (chi0 not negative semidefinite?)");
+    logdet_out.assign(nw, {0.0, 0.0});
+    for (int w = 0; w < nw; ++w) logdet_out[w] = {ld[w], 0.0};
+    return launches;
+}
+
+} // namespace gb

@@ -26,6 +26,7 @@
 #include "chi0_fast.h"
 #include "common.h"
 #include "dataset.h"
+#include "ec_tc.h"
 #include "kernels.h"
 #include "minimax.h"
 
@@ -487,6 +488,9 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     res.per_q.assign(nq, cplx(0, 0));
     const long long NN = static_cast<long long>(N) * N;
     double ec_flops = 0.0;
+    const bool use_chol = go.ec_path == LIBRPA_GB300_EC_CHOL;
+    std::unique_ptr<EcChol> ecc;
+    if (use_chol) ecc = std::make_unique<EcChol>(N, nw, !gamma_only);
     for (int q = 0; q < nq; ++q)
     {
         // V(q) full: blocks of this q inside the staged Coulomb blob
@@ -503,6 +507,37 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         auto d_voff = to_dev(voff, st);
         auto d_vIJ = to_dev(vIJ, st);
         const cuDoubleComplex *vbase = din->vblob.get();
+        if (use_chol)
+        {
+            std::vector<cplx> tr, ld;
+            if (gamma_only)
+            {
+                DevBuf<double> V(NN), X(NN * nw);
+                V.zero(st);
+                launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
+                                  d_nabf.get(), N, true, nullptr, V.get(), st);
+                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
+                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
+                                     d_eoff.get(), true, nullptr, X.get(), NN, st);
+                launches += 2 + ecc->run_q(V.get(), X.get(), tr, ld, st);
+                ec_flops += nw * (2.0 * 2.0 * N * N * N + N * static_cast<double>(N) * N / 3.0);
+            }
+            else
+            {
+                DevBuf<cuDoubleComplex> V(NN), X(NN * nw);
+                V.zero(st);
+                launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
+                                  d_nabf.get(), N, false, V.get(), nullptr, st);
+                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
+                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
+                                     d_eoff.get(), false, X.get(), nullptr, NN, st);
+                launches += 2 + ecc->run_q(V.get(), X.get(), tr, ld, st);
+                ec_flops += nw * (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0);
+            }
+            for (int w = 0; w < nw; ++w)
+                res.per_q[q] += (tr[w] + ld[w]) * tf.omega_w[w] * ibz_w[q] / (2.0 * M_PI);
+            continue;
+        }
         std::vector<double> tr_h(gamma_only ? nw : 2 * nw), ld_h(gamma_only ? nw : 2 * nw);
         if (gamma_only)
         {

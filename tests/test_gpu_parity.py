@@ -80,3 +80,32 @@ def test_reduced_precision_within_tolerance(prec):
     _, e64, _ = run_gpu(s, L.CHI0_FP64)
     _, e, _ = run_gpu(s, prec)
     assert abs(e - e64) <= MEV_PER_ATOM * len(s.nao)
+
+
+def test_h2o_cholesky_ec_path():
+    """Gamma-only (real) E_c through V = L L^T, tensor-core L^T chi0 L and FP64 Cholesky."""
+    s = load_h2o()
+    _, e_lu, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_LU_FP64)
+    _, e_ch, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL)
+    # the tensor-core products carry ~1e-7 relative error; bar: a tenth of 0.1 meV/atom
+    tol = 0.1 * MEV_PER_ATOM * len(s.nao)
+    assert abs(e_ch - e_lu) < tol
+    assert abs(e_ch - s.ec_reference) < tol
+
+
+@pytest.mark.parametrize("period", [(2, 1, 1), (3, 2, 1)])
+def test_complex_cholesky_ec_path(period):
+    s = sy.small_periodic(n_atoms=2, nao=[4, 5], nabf=[9, 12], period=period, nocc=2, seed=5)
+    _, e_lu, q_lu = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_LU_FP64)
+    _, e_ch, q_ch = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL)
+    tol = 0.1 * MEV_PER_ATOM * len(s.nao)
+    assert abs(e_ch - e_lu) <= tol
+    np.testing.assert_allclose(q_ch.real, q_lu.real, atol=tol / L.n_ibz(s))
+
+
+def test_default_fast_path_fcc2():
+    """Default options (3-piece BF16 tcgen05 chi0 + Cholesky E_c) within 0.1 meV/atom of FP64 + LU."""
+    s = sy.fcc2_k222()
+    _, e64, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_LU_FP64)
+    _, e, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    assert abs(e - e64) <= MEV_PER_ATOM * len(s.nao)
