@@ -36,6 +36,15 @@ MEV_PER_ATOM_HA = 3.674932e-6  # 0.1 meV in Hartree
 PREC = {"bf16x3": 1, "fp32": 2, "fp64": 0}
 
 
+# DRAM bytes (read + write) of one per-(tau, spin) chi0 contraction launch set, from one ncu capture
+# per kernel (profiles/*.md, same workload); None where no capture exists.
+PROFILED_TRAFFIC = {
+    "fcc16_k333": {"bytes": 7.0696e9 + 0.0692e9 + 8.0493e9 + 0.3731e9,
+                   "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_t1_tc and k_tc_gemm (X) "
+                             "for tau_0; k_t2 (2.6% of time) not captured"},
+}
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -262,7 +271,9 @@ def run_gb300(args, s, ws, rank, local, dist):
     if args.fp64_check != "off" and prec != 0:
         est = chi0_flops / args.steps / 1.0e12  # seconds at ~1 TFLOP/s FP64
         if args.fp64_check == "on" or est < args.fp64_budget_s:
-            h.set_gb300_options(L.gb300_options(chi0_precision=0, device=local, reuse_device_inputs=1))
+            # the plain FP64 GPU path: FP64 chi0 kernels and the reference-form FP64 LU E_c
+            h.set_gb300_options(L.gb300_options(chi0_precision=0, ec_path=L.EC_LU_FP64, device=local,
+                                                reuse_device_inputs=1))
             t0 = time.perf_counter()
             e64, _ = h.get_rpa_correlation_energy(opts, nq)
             t64 = time.perf_counter() - t0
@@ -277,7 +288,9 @@ def run_gb300(args, s, ws, rank, local, dist):
     peak = peaks.get("bf16_tflops", 1900.0) if prec == 1 else None
     ach = (chi0_flops / args.steps) / (chi0_ms / args.steps / 1e3) / 1e12 if chi0_ms > 0 else None
     roof = {"bound": "tensor", "achieved": ach, "peak": peaks.get("bf16_tflops"), "unit": "TFLOP/s",
-            "frac": (ach / peaks.get("bf16_tflops")) if ach else None, "traffic": None,
+            "frac": (ach / peaks.get("bf16_tflops")) if ach else None,
+            "traffic": PROFILED_TRAFFIC.get(s.name, {}).get("bytes"),
+            "traffic_source": PROFILED_TRAFFIC.get(s.name, {}).get("source"),
             "kernel": "chi0 contraction (X GEMMs + T1/T2 block contraction), per (tau, spin)",
             "flops_per_launch": chi0_flops / max(chi0_n, 1), "ms_per_launch": chi0_ms / max(chi0_n, 1),
             "peak_source": f"{src} bf16_tflops (burst)", "path": args.precision}
