@@ -103,6 +103,20 @@ int librpa_gb300_device_count(void);
  * CUDA-core GEMM.  Returns max|diff| / max|ref| (NaN on error). */
 double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces);
 
+/* No counterpart in the reference.  D = A * B through the tcgen05 split-precision GEMM
+ * (pieces = 2 or 3, as above) without allocating device memory, for callers that cannot
+ * let a library allocate (a host code that has already sized its own pool to the whole
+ * GPU).  A (M x K), B (K x N): FP64 row-major, D (M x N): FP32 row-major, all device
+ * pointers on the current device; stream is a cudaStream_t (NULL: the legacy stream).
+ * Scratch is a fixed 32 MiB device array inside the library: sizes needing more than
+ * pieces * (M + N) * ceil(K / 64) * 64 * 2 bytes (+ alignment) <= 32 MiB are rejected.
+ * The first call on a device does set-up (scratch address lookup, kernel attributes):
+ * make it before any stream capture.  Calls whose GPU work overlaps race on the one
+ * scratch array.  Synchronises the stream before returning.  Returns 0 on success,
+ * nonzero on error (message in librpa_get_last_error(NULL)). */
+int librpa_gb300_tc_gemm_noalloc(int M, int N, int K, const double *A, const double *B, float *D,
+                                 int pieces, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

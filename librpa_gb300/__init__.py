@@ -130,6 +130,7 @@ EXPORTS = [
     "librpa_gb300_init_options", "librpa_gb300_set_options", "librpa_gb300_get_stats",
     "librpa_get_last_error", "librpa_get_last_error_code", "librpa_gb300_minimax_grid",
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
+    "librpa_gb300_tc_gemm_noalloc",
 ]
 
 _lib = None
@@ -180,6 +181,8 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_get_chi0_block": (i, [vp, i, i, i, i, _dp, _dp]),
         "librpa_gb300_device_count": (i, []),
         "librpa_gb300_selftest_tc_gemm": (d, [i, i, i, i, i]),
+        "librpa_gb300_tc_gemm_noalloc": (i, [i, i, i, C.c_void_p, C.c_void_p, C.c_void_p, i,
+                                             C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

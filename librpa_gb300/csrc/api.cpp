@@ -877,4 +877,16 @@ double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces)
     return r;
 }
 
+// No counterpart in the reference: the allocation-free split GEMM (tc_gemm_noalloc.cu).
+int librpa_gb300_tc_gemm_noalloc(int M, int N, int K, const double *A, const double *B, float *D, int pieces,
+                                 void *stream)
+{
+    int rc = 1;
+    guarded(nullptr, [&] {
+        gb::tc_gemm_noalloc(M, N, K, A, B, D, pieces, static_cast<cudaStream_t>(stream));
+        rc = 0;
+    });
+    return rc;
+}
+
 } // extern "C"

@@ -359,6 +359,12 @@ static void launch_tc(const SplitMat &A, const SplitMat &B, int M, int N, int K,
     GB_LAUNCH_CHECK();
 }
 
+void tc_gemm_set_attributes()
+{
+    GB_CUDA(cudaFuncSetAttribute(k_tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<2>::SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(k_tc_gemm<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<3>::SMEM_BYTES));
+}
+
 void tc_gemm_split(const SplitMat &A, const SplitMat &B, int M, int N, int K, int batch, float *D, long long ldd,
                    long long sD, bool accumulate, int *err, cudaStream_t st)
 {

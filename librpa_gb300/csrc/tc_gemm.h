@@ -66,6 +66,11 @@ void split_transpose_f64(const double *src, long long lds, int K, int N, int kpa
 // FP32 TMEM accumulation.
 void tc_gemm_split(const SplitMat &A, const SplitMat &B, int M, int N, int K, int batch, float *D, long long ldd,
                    long long sD, bool accumulate, int *err, cudaStream_t st);
+// Set the split GEMM kernels' shared-memory attribute on the current device.
+void tc_gemm_set_attributes();
+// D = A * B through the split GEMM with all scratch in a fixed static device array
+// (tc_gemm_noalloc.cu); synchronises `st` before returning.
+void tc_gemm_noalloc(int M, int N, int K, const double *A, const double *B, float *D, int ns, cudaStream_t st);
 // Random M x N x K product vs the FP64 SIMT GEMM on the device; returns max |diff| / max |ref|.
 double tc_gemm_selftest(int M, int N, int K, int seed, int ns);
 
