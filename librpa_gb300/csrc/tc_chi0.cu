@@ -9,10 +9,11 @@
 //        E[(cJ,mu)][j, K'] = sum_i Ga[cJ]_{ij} X_b^I[mu i][shift_cJ(K')]
 //     where K' runs over the supercell orbitals (cell R', atom L, orbital l) of C^J's own
 //     frame and shift_cJ maps R' -> R' + R_cJ (the T1 term with R_L = R' + R_J).
-//     Sixteen producer warps form E in FP32 on the CUDA cores, split it into BF16 pieces and
+//     Eight producer warps form E in FP32 on the CUDA cores (packed FP32x2 FMAs, 4 columns a
+//     thread), split it into BF16 pieces and
 //     write the 128 x 64 A tile of each pipeline stage into swizzled shared memory; one lane
 //     streams the matching C^J tile (64 K-elements per row, pre-arranged in HBM) with TMA and
-//     one lane issues the tcgen05.mma terms.  K order: pass, 16-column chunk, group of 4 j.
+//     one lane issues the tcgen05.mma terms.  K order: pass, 8-column chunk, group of 8 j.
 //  3. T2 (small, CUDA cores): D += sum_{i,j} X_b^I[mu i; (cJ,J) j] X_a^J[nu j; (-cJ,I) i].
 // Every wait is bounded (tc_common.cuh) and failures surface through a device error flag.
 #include <cstdlib>
@@ -32,17 +33,19 @@ constexpr int NS = 3;            // BF16 pieces per operand (hi, mid, lo): 6 MMA
 constexpr int T1_BM = 128;       // rows (cJ, mu) per CTA
 constexpr int CW = 8;            // supercell columns per chunk
 constexpr int JG = 8;            // j per pipeline stage (JG * CW = 64 = K per stage)
-constexpr int T1_STAGES = 2;
+constexpr int T1_STAGES = 2;     // A (E tile) ring: producers fill one while the MMAs read the other
+constexpr int T1_MAXB = 8;       // C^J (B tile) ring: up to 8 stages of TMA look-ahead
 constexpr int T1_NMAX = 128;     // max N tile (ABFs of one atom, padded to 16)
-constexpr int PRODUCERS = 512;   // warps 0-15: E tiles (4 threads per row, 2 columns each)
-constexpr int DRAIN_WARP0 = 16;  // warps 16-19: accumulator drain + epilogue
-constexpr int CTRL_WARP = 20;    // warp 20: TMA + MMA issue
-constexpr int T1_THREADS = 21 * 32;
+constexpr int PRODUCERS = 256;   // warps 0-7: E tiles (2 threads per row, 4 columns each)
+constexpr int DRAIN_WARP0 = 8;   // warps 8-11: accumulator drain + epilogue; lane 0 of warp 8
+                                 // also issues the C^J TMA copies and the MMAs
+constexpr int T1_THREADS = 12 * 32;  // 3 warps per scheduler: up to 168 registers a thread
 constexpr int A_TILE = T1_BM * 64 * 2;       // bytes per A piece
 constexpr int T1_MAXA = 32;                  // max NAOs per atom (G buffer row stride)
 constexpr int T1_SMEM_MAX = 227 * 1024;
-// Shared memory: T1_STAGES x [NS A pieces | NS B pieces of b_tile bytes] | G blocks | barriers.
-// b_tile = NT_max * 128 rounded up to 1024; G blocks hold maxcj cells x RA x T1_MAXA floats.
+// Shared memory: T1_STAGES x NS A pieces | nbs x NS B pieces of b_tile bytes | G blocks | barriers.
+// b_tile = NT_max * 128 rounded up to 1024; G blocks hold, per cell, T1_MAXA rows j of
+// rap(RA) entries i, each entry the pair {g_ij, g_ij} (the broadcast operand of a packed FMA).
 
 struct T1Work
 {
@@ -72,7 +75,10 @@ struct T1Args
     const int *aJpad;          // NAOs of each atom rounded up to JG
     int nkc;                   // number of CW-wide chunks of the supercell axis
     int b_tile;                // bytes per B piece (1024-aligned)
+    int nbs;                   // stages of the B ring (2..T1_MAXB)
+    int gj;                    // j entries per i row of the G blocks (largest aJpad)
     int maxcj;                 // distinct cells a 128-row tile can span
+    int vec4;                  // n_ao % 4 == 0: 4-column X gathers are one aligned float4
     double *out;               // chi0R
     int *err;
 };
@@ -82,25 +88,60 @@ __device__ __forceinline__ void named_bar_sync(int id, int n)
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
 }
 
-__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 a, __nv_bfloat16 b)
+__host__ __device__ constexpr int rap(int ra) { return (ra + 1) & ~1; }
+
+__device__ __forceinline__ uint32_t bf2_bits(__nv_bfloat162 h)
 {
-    return static_cast<uint32_t>(__bfloat16_as_ushort(a)) | (static_cast<uint32_t>(__bfloat16_as_ushort(b)) << 16);
+    return *reinterpret_cast<const uint32_t *>(&h);
 }
 
-// RA: register blocking over the NAOs i of atom I (16 or 32); NTC: accumulator columns
-// held by the drain warps (64 or 128).
+// Three-piece BF16 split of a pair of FP32 values (hi, mid, lo), each piece packed as bf16x2
+// (element 0 in the low half): hi = rn(e), mid = rn(e - hi), lo = rn(e - hi - mid).
+__device__ __forceinline__ void split3_pair(float2 e, uint32_t &h, uint32_t &m, uint32_t &l)
+{
+    const float2 neg1 = make_float2(-1.0f, -1.0f);
+    const __nv_bfloat162 hh = __floats2bfloat162_rn(e.x, e.y);
+    const float2 r1 = __ffma2_rn(__bfloat1622float2(hh), neg1, e);
+    const __nv_bfloat162 mm = __floats2bfloat162_rn(r1.x, r1.y);
+    const float2 r2 = __ffma2_rn(__bfloat1622float2(mm), neg1, r1);
+    h = bf2_bits(hh);
+    m = bf2_bits(mm);
+    l = bf2_bits(__floats2bfloat162_rn(r2.x, r2.y));
+}
+
+// RA: register blocking over the NAOs i of atom I (13, 16 or 32: at least the largest NAO
+// count); NTC: accumulator columns held by the drain warps (64 or 128).
+//
+// Both LibRI passes share the B operand C^J, so one A tile carries E(+) + E(-) (pass 0:
+// G(+) with X(-), pass 1: G(-) with X(+)) and each K step is contracted once.  With NTC = 64
+// the three C^J pieces sit on top of each other along N and each K16 step is three MMAs,
+// hi x [Ch;Cm;Cl] (N = 3 NT), mid x [Ch;Cm] (N = 2 NT) and lo x Ch (N = NT), landing in three
+// accumulator blocks of orders 1, 2^-8 and 2^-16; with NTC = 128 the six products are issued
+// one by one into a hi*hi block and a cross-term block.
 template <int RA, int NTC>
 __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__ T1Args a,
                                                         const __grid_constant__ T1Maps maps)
 {
+    constexpr bool STACKN = NTC == 64;
+    constexpr int NBLK = STACKN ? 3 : 2;           // accumulator blocks per buffer
+    constexpr uint32_t TMEM_COLS = 512;
+    static_assert(2 * NBLK * NTC <= static_cast<int>(TMEM_COLS), "TMEM budget");
+    constexpr int RP = rap(RA);
+    constexpr bool BOTHX = RA <= 13;  // keep both passes' X values of a chunk in registers
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const int stage_bytes = NS * (A_TILE + a.b_tile);
-    const int g_floats = a.maxcj * RA * T1_MAXA;
-    float *gsm = reinterpret_cast<float *>(smem + T1_STAGES * stage_bytes);
-    uint64_t *full = reinterpret_cast<uint64_t *>(gsm + g_floats);
-    uint64_t *empty = full + T1_STAGES;
-    uint64_t *accf = empty + T1_STAGES;
+    const int stage_bytes = NS * A_TILE;      // A ring stage
+    const int bstage_bytes = NS * a.b_tile;   // B ring stage
+    const int nbs = a.nbs;
+    const int gst = a.gj;                     // j entries per i row of a G block
+    const int g_floats = 2 * a.maxcj * RP * gst * 2;
+    unsigned char *bring = smem + T1_STAGES * stage_bytes;
+    float *gsm = reinterpret_cast<float *>(bring + nbs * bstage_bytes);
+    uint64_t *full = reinterpret_cast<uint64_t *>(gsm + g_floats);  // A ring: producers filled
+    uint64_t *empty = full + T1_STAGES;                              // A ring: MMAs done
+    uint64_t *bfull = empty + T1_STAGES;                             // B ring: TMA landed
+    uint64_t *bempty = bfull + T1_MAXB;                              // B ring: MMAs done
+    uint64_t *accf = bempty + T1_MAXB;
     uint64_t *acce = accf + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acce + 2);
 
@@ -110,29 +151,33 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
     const int njg = a.aJpad[J] / JG;
     const int NT = (bJ + 15) / 16 * 16;
-    const uint32_t tcols = NTC;          // columns per accumulator
     const int nc = g.n_c, nao = g.n_ao;
     const long long nsup = g.n_sup;
     const int row0 = w.tile * T1_BM;
     const int cj_min = row0 / bI;
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int total_stages = 2 * a.nkc * njg;
+    const int total_stages = a.nkc * njg;
 
     if (threadIdx.x == 0)
     {
         for (int s = 0; s < T1_STAGES; ++s)
         {
-            mbar_init(&full[s], PRODUCERS + 1);
+            mbar_init(&full[s], PRODUCERS / 32);  // one arrival per producer warp
             mbar_init(&empty[s], 1);
+        }
+        for (int s = 0; s < nbs; ++s)
+        {
+            mbar_init(&bfull[s], 1);
+            mbar_init(&bempty[s], 1);
         }
         for (int i = 0; i < 2; ++i)
         {
             mbar_init(&accf[i], 1);
-            mbar_init(&acce[i], 128);
+            mbar_init(&acce[i], 4);               // one arrival per drain warp
         }
         fence_barrier_init();
     }
-    if (warp == 0) tmem_alloc(tmem_slot, 4 * tcols);
+    if (warp == 0) tmem_alloc(tmem_slot, TMEM_COLS);
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
@@ -141,140 +186,237 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     {
         // ---------------- producers: E tiles
         const int t = threadIdx.x;
-        const int r = t >> 2;           // row in tile
-        const int cg = t & 3;           // 2-column group inside the 8-column chunk
+        const int r = t >> 1;           // row in tile
+        const int cq = t & 1;           // 4-column group inside the 8-column chunk
         const int rg = row0 + r;
         const bool valid = rg < nc * bI;
         const int cJ = valid ? rg / bI : 0;
         const int mu = valid ? rg % bI : 0;
         const int cjl = valid ? cJ - cj_min : 0;
         const long long xrow = g.rowc_off[I] + static_cast<long long>(mu) * aI;
-        bool ok = true;
-        int st_count = 0;
-        for (int pass = 0; pass < 2 && ok; ++pass)
+        // G blocks of both passes for the tile's cells, [pass][cell][i][j] as FP32 pairs {g, g}
+        const int ncj = min(a.maxcj, (min(row0 + T1_BM, nc * bI) - 1) / bI - cj_min + 1);
+        const int per_pass = ncj * RP * gst;
+        for (int e = t; e < 2 * per_pass; e += PRODUCERS)
         {
-            // Ga blocks of this pass for the tile's cells, FP32 in shared memory
-            named_bar_sync(1, PRODUCERS);
-            const int ncj = min(a.maxcj, (min(row0 + T1_BM, nc * bI) - 1) / bI - cj_min + 1);
-            const double *Ga = a.G + static_cast<size_t>(pass) * nc * nao * nao;
-            for (int e = t; e < ncj * RA * T1_MAXA; e += PRODUCERS)
-            {
-                const int cl = e / (RA * T1_MAXA), ij = e % (RA * T1_MAXA);
-                const int i = ij / T1_MAXA, j = ij % T1_MAXA;
-                float v = 0.0f;
-                if (i < aI && j < aJ)
-                    v = static_cast<float>(Ga[(static_cast<size_t>(cj_min + cl) * nao + g.ao_off[I] + i) * nao +
-                                              g.ao_off[J] + j]);
-                gsm[e] = v;
-            }
-            named_bar_sync(1, PRODUCERS);
-            const float *Xb = a.X + (pass == 0 ? a.xsign : 0);  // pass 0: Ga = G+, X_b from G-
-            const float *gr = gsm + cjl * RA * T1_MAXA;
-            for (int kc = 0; kc < a.nkc && ok; ++kc)
-            {
-                float xr[RA][2];
-                int srcc[2];
+            const int pass = e / per_pass, rem = e % per_pass;
+            const int cl = rem / (RP * gst), ij = rem % (RP * gst);
+            const int i = ij / gst, j = ij % gst;
+            float v = 0.0f;
+            if (i < aI && j < aJ)
+                v = static_cast<float>(a.G[((static_cast<size_t>(pass) * nc + cj_min + cl) * nao + g.ao_off[I] + i) * nao +
+                                           g.ao_off[J] + j]);
+            reinterpret_cast<float2 *>(gsm)[(static_cast<size_t>(pass) * a.maxcj + cl) * RP * gst + ij] = make_float2(v, v);
+        }
+        named_bar_sync(1, PRODUCERS);
+        const float4 *gp[2];
 #pragma unroll
-                for (int q = 0; q < 2; ++q)
+        for (int pass = 0; pass < 2; ++pass)
+            gp[pass] = reinterpret_cast<const float4 *>(gsm) + (static_cast<size_t>(pass) * a.maxcj + cjl) * RP * gst / 2;
+        const float *Xp[2] = {a.X + a.xsign, a.X};  // pass 0 contracts G(+) with X(-), pass 1 G(-) with X(+)
+        // X_b^I[mu i][shift_cJ(col)] for the thread's 4 columns of chunk kc (np passes from pass p0)
+        auto load_x = [&](int kc, int p0, int np, float4 (&x0)[RA], float4 (&x1)[BOTHX ? RA : 1]) {
+            const long long col0 = static_cast<long long>(kc) * CW + cq * 4;
+            if (a.vec4)
+            {
+                long long src = -1;
+                if (col0 < nsup && valid)
                 {
-                    const long long col = static_cast<long long>(kc) * CW + cg * 2 + q;
+                    const int cp = static_cast<int>(col0 / nao), ao = static_cast<int>(col0 % nao);
+                    src = static_cast<long long>(a.cadd[cp * nc + cJ]) * nao + ao;
+                }
+                const float *b0 = Xp[p0] + xrow * nsup + src;
+#pragma unroll
+                for (int i = 0; i < RA; ++i)
+                    x0[i] = (i < aI && src >= 0) ? __ldg(reinterpret_cast<const float4 *>(b0 + i * nsup))
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+                if constexpr (BOTHX)
+                    if (np == 2)
+                    {
+                        const float *b1 = Xp[p0 + 1] + xrow * nsup + src;
+#pragma unroll
+                        for (int i = 0; i < RA; ++i)
+                            x1[i] = (i < aI && src >= 0) ? __ldg(reinterpret_cast<const float4 *>(b1 + i * nsup))
+                                                         : make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+            }
+            else
+            {
+                long long src[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                {
+                    const long long col = col0 + q;
+                    src[q] = -1;
                     if (col < nsup && valid)
                     {
                         const int cp = static_cast<int>(col / nao), ao = static_cast<int>(col % nao);
-                        srcc[q] = a.cadd[cp * nc + cJ] * nao + ao;
+                        src[q] = static_cast<long long>(a.cadd[cp * nc + cJ]) * nao + ao;
+                    }
+                }
+                auto gather = [&](const float *Xb, float4(&x)[RA]) {
+#pragma unroll
+                    for (int i = 0; i < RA; ++i)
+                    {
+                        const float *xr = Xb + (xrow + i) * nsup;
+                        const bool ri = i < aI;
+                        x[i] = make_float4(ri && src[0] >= 0 ? xr[src[0]] : 0.f, ri && src[1] >= 0 ? xr[src[1]] : 0.f,
+                                           ri && src[2] >= 0 ? xr[src[2]] : 0.f, ri && src[3] >= 0 ? xr[src[3]] : 0.f);
+                    }
+                };
+                gather(Xp[p0], x0);
+                if constexpr (BOTHX)
+                    if (np == 2) gather(Xp[p0 + 1], x1);
+            }
+        };
+        // E[j][col pair] += sum_i g_ij x_i for JH consecutive j from j0
+        constexpr int JH = JG / 2;
+        auto contract = [&](const float4 *gb, int j0, const float4 (&x)[RA], float2 (&e)[JH][2]) {
+#pragma unroll
+            for (int i = 0; i < RA; ++i)
+            {
+                const float4 *gi = gb + (i * gst + j0) / 2;
+                const float2 xa = make_float2(x[i].x, x[i].y), xb = make_float2(x[i].z, x[i].w);
+#pragma unroll
+                for (int q = 0; q < JH / 2; ++q)
+                {
+                    const float4 gg = gi[q];  // {g_ij, g_ij, g_ij+1, g_ij+1}
+                    const float2 ga = make_float2(gg.x, gg.y), gb2 = make_float2(gg.z, gg.w);
+                    e[2 * q][0] = __ffma2_rn(ga, xa, e[2 * q][0]);
+                    e[2 * q][1] = __ffma2_rn(ga, xb, e[2 * q][1]);
+                    e[2 * q + 1][0] = __ffma2_rn(gb2, xa, e[2 * q + 1][0]);
+                    e[2 * q + 1][1] = __ffma2_rn(gb2, xb, e[2 * q + 1][1]);
+                }
+            }
+        };
+        bool ok = true;
+        int st_count = 0;
+        float4 x0[RA], x1[BOTHX ? RA : 1];
+        for (int kc = 0; kc < a.nkc && ok; ++kc)
+        {
+            if constexpr (BOTHX) load_x(kc, 0, 2, x0, x1);
+            for (int jg = 0; jg < njg; ++jg, ++st_count)
+            {
+                const int s = st_count % T1_STAGES, rr = st_count / T1_STAGES;
+                unsigned char *stg = smem + s * stage_bytes;
+#pragma unroll 1
+                for (int h = 0; h < 2; ++h)
+                {
+                    const int j0 = jg * JG + h * JH;
+                    float2 e[JH][2];
+#pragma unroll
+                    for (int jl = 0; jl < JH; ++jl) e[jl][0] = e[jl][1] = make_float2(0.f, 0.f);
+                    if constexpr (BOTHX)
+                    {
+                        contract(gp[0], j0, x0, e);
+                        contract(gp[1], j0, x1, e);
                     }
                     else
-                        srcc[q] = -1;
-                }
-#pragma unroll
-                for (int i = 0; i < RA; ++i)
-                {
-#pragma unroll
-                    for (int q = 0; q < 2; ++q)
-                        xr[i][q] = (i < aI && srcc[q] >= 0) ? Xb[(xrow + i) * nsup + srcc[q]] : 0.0f;
-                }
-                for (int jg = 0; jg < njg; ++jg, ++st_count)
-                {
-                    const int s = st_count % T1_STAGES, rr = st_count / T1_STAGES;
-                    if (!mbar_wait(&empty[s], (rr & 1) ^ 1))
                     {
-                        atomicExch(a.err, 201);
-                        ok = false;
-                        break;
+                        load_x(kc, 0, 1, x0, x1);
+                        contract(gp[0], j0, x0, e);
+                        load_x(kc, 1, 1, x0, x1);
+                        contract(gp[1], j0, x0, e);
                     }
-                    unsigned char *stg = smem + s * stage_bytes;
-#pragma unroll
-                    for (int jl = 0; jl < JG; ++jl)
+                    if (h == 0)
                     {
-                        const int j = jg * JG + jl;  // zero G columns beyond aJ give zero E
-                        float e0 = 0.f, e1 = 0.f;
-#pragma unroll
-                        for (int i = 0; i < RA; ++i)
+                        // warp-uniform outcome: the warp arrives on full[s] as one
+                        if (!__all_sync(0xffffffffu, mbar_wait(&empty[s], (rr & 1) ^ 1)))
                         {
-                            const float gij = gr[i * T1_MAXA + j];
-                            e0 = fmaf(gij, xr[i][0], e0);
-                            e1 = fmaf(gij, xr[i][1], e1);
+                            if (lane == 0) atomicExch(a.err, 201);
+                            ok = false;
+                            break;
                         }
-                        const __nv_bfloat16 h0 = __float2bfloat16_rn(e0), h1 = __float2bfloat16_rn(e1);
-                        const float r0 = e0 - __bfloat162float(h0), r1 = e1 - __bfloat162float(h1);
-                        const __nv_bfloat16 m0 = __float2bfloat16_rn(r0), m1 = __float2bfloat16_rn(r1);
-                        const __nv_bfloat16 l0 = __float2bfloat16_rn(r0 - __bfloat162float(m0));
-                        const __nv_bfloat16 l1 = __float2bfloat16_rn(r1 - __bfloat162float(m1));
-                        const uint32_t off = sw128_offset(r, jl * CW + cg * 2);
-                        *reinterpret_cast<uint32_t *>(stg + off) = pack_bf16(h0, h1);
-                        *reinterpret_cast<uint32_t *>(stg + A_TILE + off) = pack_bf16(m0, m1);
-                        *reinterpret_cast<uint32_t *>(stg + 2 * A_TILE + off) = pack_bf16(l0, l1);
                     }
-                    fence_proxy_async_smem();
-                    mbar_arrive(&full[s]);
+#pragma unroll
+                    for (int jl = 0; jl < JH; ++jl)
+                    {
+                        uint32_t h01, m01, l01, h23, m23, l23;
+                        split3_pair(e[jl][0], h01, m01, l01);
+                        split3_pair(e[jl][1], h23, m23, l23);
+                        const uint32_t off = sw128_offset(r, (h * JH + jl) * CW + cq * 4);
+                        *reinterpret_cast<uint2 *>(stg + off) = make_uint2(h01, h23);
+                        *reinterpret_cast<uint2 *>(stg + A_TILE + off) = make_uint2(m01, m23);
+                        *reinterpret_cast<uint2 *>(stg + 2 * A_TILE + off) = make_uint2(l01, l23);
+                    }
                 }
+                if (!ok) break;
+                fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
             }
         }
     }
-    else if (warp == CTRL_WARP)
+    else
     {
-        if (lane == 0)
-        {
-            // ---------------- TMA for C^J tiles and MMA issue
-            const uint32_t idesc = idesc_bf16_f32(T1_BM, NT);
-            const uint32_t bbytes = static_cast<uint32_t>(NT) * 64 * 2;
-            const int sp = a.spec[J], zj = a.spec_idx[J];
-            const long long ktot = maps.ktot[sp];
-            for (int st = 0; st < total_stages; ++st)
+        // ---------------- warps 8-11: per-stage accumulator blocks -> FP32 registers -> chi0R.
+        // Lane 0 of warp 8 issues, per stage st, the MMAs of st and then the C^J TMA copy of
+        // st + nbs - 1 (nbs - 1 stages of look-ahead hide the HBM latency of the B tiles),
+        // before its warp drains st - 1: the tensor pipe always holds the next stage.
+        const int wq = warp - DRAIN_WARP0;
+        const bool ctrl = wq == 0 && lane == 0;
+        const uint32_t lane_base = static_cast<uint32_t>(wq * 32) << 16;
+        const uint32_t bbytes = static_cast<uint32_t>(NT) * 64 * 2;  // one piece of a B tile
+        const int sp = a.spec[J], zj = a.spec_idx[J];
+        const long long ktot = maps.ktot[sp];
+        auto issue_tma = [&](int st) -> bool {
+            const int s = st % nbs, rr = st / nbs;
+            if (!mbar_wait(&bempty[s], (rr & 1) ^ 1))
             {
-                const int s = st % T1_STAGES, rr = st / T1_STAGES;
-                const int ab = st & 1;
-                if (!mbar_wait(&empty[s], (rr & 1) ^ 1))
-                {
-                    atomicExch(a.err, 202);
-                    break;
-                }
-                const int rem = st % (a.nkc * njg);
-                const int x = rem * 64;  // K offset (kc * njg + jg) * 64
-                if (x < 0 || static_cast<long long>(x) + 64 > ktot || (x & 7) != 0)
-                {
-                    atomicExch(a.err, 205);  // coordinate outside the C^J operand: skip the copy
-                    break;
-                }
-                unsigned char *stg = smem + s * stage_bytes;
-                mbar_arrive_expect_tx(&full[s], NS * bbytes);
+                atomicExch(a.err, 202);
+                return false;
+            }
+            const int x = st * 64;  // K offset (kc * njg + jg) * 64
+            if (x < 0 || static_cast<long long>(x) + 64 > ktot || (x & 7) != 0)
+            {
+                atomicExch(a.err, 205);  // coordinate outside the C^J operand: skip the copy
+                return false;
+            }
+            unsigned char *bst = bring + s * bstage_bytes;
+            mbar_arrive_expect_tx(&bfull[s], NS * bbytes);
 #pragma unroll
-                for (int p = 0; p < NS; ++p)
-                    tma_load_3d(stg + NS * A_TILE + p * a.b_tile, &maps.m[sp][p], x, 0, zj, &full[s]);
-                if (!mbar_wait(&full[s], rr & 1) || !mbar_wait(&acce[ab], ((st >> 1) & 1) ^ 1))
-                {
-                    atomicExch(a.err, 203);
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t t_hh = tmem + ab * 2 * tcols, t_x = t_hh + tcols;
-                uint64_t da[NS], db[NS];
+            for (int p = 0; p < NS; ++p)  // pieces stacked along N: rows [p NT, (p + 1) NT)
+                tma_load_3d(bst + p * bbytes, &maps.m[sp][p], x, 0, zj, &bfull[s]);
+            return true;
+        };
+        auto issue_mma = [&](int st) -> bool {
+            const int s = st % T1_STAGES, rr = st / T1_STAGES;
+            const int sb = st % nbs, rb = st / nbs;
+            const int ab = st & 1;
+            if (!mbar_wait(&full[s], rr & 1) || !mbar_wait(&bfull[sb], rb & 1) ||
+                !mbar_wait(&acce[ab], ((st >> 1) & 1) ^ 1))
+            {
+                atomicExch(a.err, 203);
+                return false;
+            }
+            tc_fence_after();
+            unsigned char *stg = smem + s * stage_bytes;
+            unsigned char *bst = bring + sb * bstage_bytes;
+            const uint32_t tb = tmem + static_cast<uint32_t>(ab * NBLK * NTC);
+            uint64_t da[NS], db[NS];
 #pragma unroll
-                for (int p = 0; p < NS; ++p)
+            for (int p = 0; p < NS; ++p)
+            {
+                da[p] = smem_desc_sw128(stg + p * A_TILE);
+                db[p] = smem_desc_sw128(bst + p * bbytes);
+            }
+            if constexpr (STACKN)
+            {
+                const uint32_t i3 = idesc_bf16_f32(T1_BM, 3 * NT), i2 = idesc_bf16_f32(T1_BM, 2 * NT),
+                               i1 = idesc_bf16_f32(T1_BM, NT);
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
                 {
-                    da[p] = smem_desc_sw128(stg + p * A_TILE);
-                    db[p] = smem_desc_sw128(stg + NS * A_TILE + p * a.b_tile);
+                    const uint64_t dk = static_cast<uint64_t>(k * 32 >> 4);
+                    mma_bf16(tb, da[0] + dk, db[0] + dk, i3, k != 0);                       // hi x [Ch;Cm;Cl]
+                    mma_bf16(tb + NT, da[1] + dk, db[0] + dk, i2, 1);                       // mid x [Ch;Cm]
+                    mma_bf16(tb + 2 * NT, da[2] + dk, db[0] + dk, i1, 1);                   // lo x Ch
                 }
+            }
+            else
+            {
+                const uint32_t idesc = idesc_bf16_f32(T1_BM, NT);
+                const uint32_t t_hh = tb, t_x = tb + NTC;
 #pragma unroll
                 for (int k = 0; k < 4; ++k)
                 {
@@ -287,49 +429,86 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
                     mma_bf16(t_x, da[0] + dk, db[1] + dk, idesc, 1);
                     mma_bf16(t_hh, da[0] + dk, db[0] + dk, idesc, k != 0);
                 }
-                mma_commit(&empty[s]);
-                mma_commit(&accf[ab]);
             }
-        }
-        __syncwarp();
-    }
-    else
-    {
-        // ---------------- drain warps: per-stage accumulator pairs -> FP32 registers -> chi0R
-        const int wq = warp - DRAIN_WARP0;
-        const uint32_t lane_base = static_cast<uint32_t>(wq * 32) << 16;
+            mma_commit(&empty[s]);
+            mma_commit(&bempty[sb]);
+            mma_commit(&accf[ab]);
+            return true;
+        };
         float acc[NTC];
 #pragma unroll
         for (int c = 0; c < NTC; ++c) acc[c] = 0.0f;
         bool ok = true;
-        for (int st = 0; st < total_stages; ++st)
+        int issued = 0, copied = 0;  // MMA stages and B-tile copies issued (control lane)
+        if (ctrl)
+            for (int st = 0; st < nbs - 1 && st < total_stages && ok; ++st)
+                if ((ok = issue_tma(st))) ++copied;
+        for (int st = 0; st <= total_stages; ++st)
         {
-            const int ab = st & 1;
-            if (!mbar_wait(&accf[ab], (st >> 1) & 1))
+            if (wq == 0)
             {
-                atomicExch(a.err, 204);
+                if (ctrl && ok && st < total_stages)
+                {
+                    ok = issue_mma(st);
+                    if (ok) ++issued;
+                    if (ok && st + nbs - 1 < total_stages)
+                        if ((ok = issue_tma(st + nbs - 1))) ++copied;
+                }
+                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            }
+            if (!ok) break;
+            if (st == 0) continue;
+            const int sd = st - 1, ab = sd & 1;
+            if (!__all_sync(0xffffffffu, mbar_wait(&accf[ab], (sd >> 1) & 1)))
+            {
+                if (lane == 0) atomicExch(a.err, 204);
                 ok = false;
                 break;
             }
             tc_fence_after();
-            const uint32_t t_hh = tmem + ab * 2 * tcols, t_x = t_hh + tcols;
+            const uint32_t tb = tmem + static_cast<uint32_t>(ab * NBLK * NTC) + lane_base;
 #pragma unroll
             for (int c0 = 0; c0 < NTC; c0 += 16)
             {
                 if (c0 < NT)
                 {
-                    float v[16];
-                    tmem_ld16(t_x + lane_base + c0, v);
+                    if constexpr (STACKN)
+                    {
+                        uint32_t v0[16], v1[16], v2[16];
+                        tmem_ld16_nowait(tb + c0, v0);
+                        tmem_ld16_nowait(tb + NT + c0, v1);
+                        tmem_ld16_nowait(tb + 2 * NT + c0, v2);
+                        tmem_wait_ld();
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
-                    tmem_ld16(t_hh + lane_base + c0, v);
+                        for (int i = 0; i < 16; ++i)
+                            acc[c0 + i] += __uint_as_float(v0[i]) + (__uint_as_float(v1[i]) + __uint_as_float(v2[i]));
+                    }
+                    else
+                    {
+                        uint32_t vx[16], vh[16];
+                        tmem_ld16_nowait(tb + NTC + c0, vx);
+                        tmem_ld16_nowait(tb + c0, vh);
+                        tmem_wait_ld();
 #pragma unroll
-                    for (int i = 0; i < 16; ++i) acc[c0 + i] += v[i];
+                        for (int i = 0; i < 16; ++i) acc[c0 + i] += __uint_as_float(vx[i]);
+#pragma unroll
+                        for (int i = 0; i < 16; ++i) acc[c0 + i] += __uint_as_float(vh[i]);
+                    }
                 }
             }
             tc_fence_before();
-            mbar_arrive(&acce[ab]);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acce[ab]);
         }
+        if (ctrl && !ok && issued > 0)
+        {
+            // error path: let this CTA's issued MMAs finish before its TMEM is released
+            const int last = issued - 1;
+            mbar_wait(&empty[last % T1_STAGES], (last / T1_STAGES) & 1);
+        }
+        if (ctrl && !ok)
+            for (int st = issued; st < copied; ++st)  // and its B copies land before the CTA exits
+                mbar_wait(&bfull[st % nbs], (st / nbs) & 1);
         const int r = wq * 32 + lane;
         const int rg = row0 + r;
         if (ok && rg < nc * bI)
@@ -343,7 +522,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, 4 * tcols);
+    if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
 }
 
 // T2 for one (pair, cJ): out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i]
@@ -479,13 +658,14 @@ struct TcChi0::Impl
     std::vector<SplitStore> cb;  // per species: C^J of its atoms, stacked
     T1Maps maps{};
     DevBuf<int> spec, spec_idx;
-    int b_tile = 0, maxcj = 0, smem = 0, ra = 16, ntc = 64;
+    int b_tile = 0, maxcj = 0, smem = 0, ra = 16, ntc = 64, nbs = 2, gj = JG;
 };
 
 namespace {
 using T1Fn = void (*)(T1Args, T1Maps);
 T1Fn t1_kernel(int ra, int ntc)
 {
+    if (ra == 13) return ntc == 64 ? k_t1_tc<13, 64> : k_t1_tc<13, 128>;
     if (ra == 16) return ntc == 64 ? k_t1_tc<16, 64> : k_t1_tc<16, 128>;
     return ntc == 64 ? k_t1_tc<32, 64> : k_t1_tc<32, 128>;
 }
@@ -597,10 +777,14 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     }
     m.b_tile = (ntmax * 128 + 1023) / 1024 * 1024;
     m.maxcj = (T1_BM + minb - 1) / minb + 1;
-    m.ra = g.max_nao <= 16 ? 16 : 32;
+    m.ra = g.max_nao == 13 ? 13 : g.max_nao <= 16 ? 16 : 32;
     m.ntc = ntmax <= 64 ? 64 : 128;
-    m.smem = T1_STAGES * NS * (A_TILE + m.b_tile) + m.maxcj * m.ra * T1_MAXA * 4 + 1024 + 256;
-    GB_REQUIRE(m.smem <= T1_SMEM_MAX, "chi0 tile does not fit shared memory (too many cells per tile or too many ABFs)");
+    m.gj = JG;
+    for (int J = 0; J < g.n_at; ++J) m.gj = std::max(m.gj, ajp[J]);
+    const int fixed = T1_STAGES * NS * A_TILE + 2 * m.maxcj * rap(m.ra) * m.gj * 8 + 1024 + 512;
+    m.nbs = std::min(T1_MAXB, (T1_SMEM_MAX - fixed) / (NS * m.b_tile));
+    GB_REQUIRE(m.nbs >= 2, "chi0 tile does not fit shared memory (too many cells per tile or too many ABFs)");
+    m.smem = fixed + m.nbs * NS * m.b_tile;
     GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc), cudaFuncAttributeMaxDynamicSharedMemorySize, m.smem));
     GB_CUDA(cudaStreamSynchronize(st));
 }
@@ -644,7 +828,10 @@ int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t s
         a.aJpad = m.ajpad.get();
         a.nkc = m.nkc;
         a.b_tile = m.b_tile;
+        a.nbs = m.nbs;
+        a.gj = m.gj;
         a.maxcj = m.maxcj;
+        a.vec4 = g.n_ao % 4 == 0 ? 1 : 0;
         a.out = chi0R;
         a.err = m.err.get();
         t1_kernel(m.ra, m.ntc)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
