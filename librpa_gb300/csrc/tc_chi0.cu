@@ -44,8 +44,8 @@ constexpr int A_TILE = T1_BM * 64 * 2;       // bytes per A piece
 constexpr int T1_MAXA = 32;                  // max NAOs per atom (G buffer row stride)
 constexpr int T1_SMEM_MAX = 227 * 1024;
 // Shared memory: T1_STAGES x NS A pieces | nbs x NS B pieces of b_tile bytes | G blocks | barriers.
-// b_tile = NT_max * 128 rounded up to 1024; G blocks hold, per cell, T1_MAXA rows j of
-// rap(RA) entries i, each entry the pair {g_ij, g_ij} (the broadcast operand of a packed FMA).
+// b_tile = NT_max * 128 rounded up to 1024; G blocks hold, per pass and cell, rap(RA) rows i
+// of gj FP32 entries j.
 
 struct T1Work
 {
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     const int bstage_bytes = NS * a.b_tile;   // B ring stage
     const int nbs = a.nbs;
     const int gst = a.gj;                     // j entries per i row of a G block
-    const int g_floats = 2 * a.maxcj * RP * gst * 2;
+    const int g_floats = 2 * a.maxcj * RP * gst;
     unsigned char *bring = smem + T1_STAGES * stage_bytes;
     float *gsm = reinterpret_cast<float *>(bring + nbs * bstage_bytes);
     uint64_t *full = reinterpret_cast<uint64_t *>(gsm + g_floats);  // A ring: producers filled
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         const int mu = valid ? rg % bI : 0;
         const int cjl = valid ? cJ - cj_min : 0;
         const long long xrow = g.rowc_off[I] + static_cast<long long>(mu) * aI;
-        // G blocks of both passes for the tile's cells, [pass][cell][i][j] as FP32 pairs {g, g}
+        // G blocks of both passes for the tile's cells, [pass][cell][i][j] in FP32
         const int ncj = min(a.maxcj, (min(row0 + T1_BM, nc * bI) - 1) / bI - cj_min + 1);
         const int per_pass = ncj * RP * gst;
         for (int e = t; e < 2 * per_pass; e += PRODUCERS)
@@ -206,13 +206,13 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
             if (i < aI && j < aJ)
                 v = static_cast<float>(a.G[((static_cast<size_t>(pass) * nc + cj_min + cl) * nao + g.ao_off[I] + i) * nao +
                                            g.ao_off[J] + j]);
-            reinterpret_cast<float2 *>(gsm)[(static_cast<size_t>(pass) * a.maxcj + cl) * RP * gst + ij] = make_float2(v, v);
+            gsm[(static_cast<size_t>(pass) * a.maxcj + cl) * RP * gst + ij] = v;
         }
         named_bar_sync(1, PRODUCERS);
         const float4 *gp[2];
 #pragma unroll
         for (int pass = 0; pass < 2; ++pass)
-            gp[pass] = reinterpret_cast<const float4 *>(gsm) + (static_cast<size_t>(pass) * a.maxcj + cjl) * RP * gst / 2;
+            gp[pass] = reinterpret_cast<const float4 *>(gsm) + (static_cast<size_t>(pass) * a.maxcj + cjl) * RP * gst / 4;
         const float *Xp[2] = {a.X + a.xsign, a.X};  // pass 0 contracts G(+) with X(-), pass 1 G(-) with X(+)
         // X_b^I[mu i][shift_cJ(col)] for the thread's 4 columns of chunk kc (np passes from pass p0)
         auto load_x = [&](int kc, int p0, int np, float4 (&x0)[RA], float4 (&x1)[BOTHX ? RA : 1]) {
@@ -275,17 +275,18 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
 #pragma unroll
             for (int i = 0; i < RA; ++i)
             {
-                const float4 *gi = gb + (i * gst + j0) / 2;
+                // one 16-byte load gives g_ij for the JH = 4 values of j; each is paired {g, g}
+                // in registers as the broadcast operand of the packed FMAs
+                static_assert(JH == 4, "one float4 of G per (i, half stage)");
+                const float4 gg = gb[(i * gst + j0) / 4];
                 const float2 xa = make_float2(x[i].x, x[i].y), xb = make_float2(x[i].z, x[i].w);
+                const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
 #pragma unroll
-                for (int q = 0; q < JH / 2; ++q)
+                for (int q = 0; q < 4; ++q)
                 {
-                    const float4 gg = gi[q];  // {g_ij, g_ij, g_ij+1, g_ij+1}
-                    const float2 ga = make_float2(gg.x, gg.y), gb2 = make_float2(gg.z, gg.w);
-                    e[2 * q][0] = __ffma2_rn(ga, xa, e[2 * q][0]);
-                    e[2 * q][1] = __ffma2_rn(ga, xb, e[2 * q][1]);
-                    e[2 * q + 1][0] = __ffma2_rn(gb2, xa, e[2 * q + 1][0]);
-                    e[2 * q + 1][1] = __ffma2_rn(gb2, xb, e[2 * q + 1][1]);
+                    const float2 gq = make_float2(gv[q], gv[q]);
+                    e[q][0] = __ffma2_rn(gq, xa, e[q][0]);
+                    e[q][1] = __ffma2_rn(gq, xb, e[q][1]);
                 }
             }
         };
@@ -781,7 +782,7 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     m.ntc = ntmax <= 64 ? 64 : 128;
     m.gj = JG;
     for (int J = 0; J < g.n_at; ++J) m.gj = std::max(m.gj, ajp[J]);
-    const int fixed = T1_STAGES * NS * A_TILE + 2 * m.maxcj * rap(m.ra) * m.gj * 8 + 1024 + 512;
+    const int fixed = T1_STAGES * NS * A_TILE + 2 * m.maxcj * rap(m.ra) * m.gj * 4 + 1024 + 512;
     m.nbs = std::min(T1_MAXB, (T1_SMEM_MAX - fixed) / (NS * m.b_tile));
     GB_REQUIRE(m.nbs >= 2, "chi0 tile does not fit shared memory (too many cells per tile or too many ABFs)");
     m.smem = fixed + m.nbs * NS * m.b_tile;
