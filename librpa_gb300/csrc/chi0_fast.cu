@@ -49,6 +49,8 @@ Chi0Fast::Chi0Fast(int precision, const Geom &g, const Pairs &pr, const double *
 
 Chi0Fast::~Chi0Fast() = default;
 
+TcChi0 *Chi0Fast::tensor_path() { return impl_->tc.get(); }
+
 int Chi0Fast::run(const double *Gs, const double *Gp, const double *Gm, double *chi0R, cudaStream_t st)
 {
     Impl &m = *impl_;

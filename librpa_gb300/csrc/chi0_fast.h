@@ -17,6 +17,8 @@ public:
     // One (tau, spin): from the supercell G (both signs) and the unit-cell G blocks,
     // write chi0(R, tau) upper-pair blocks (FP64) to chi0R.  Returns kernels launched.
     int run(const double *Gs, const double *Gp, const double *Gm, double *chi0R, cudaStream_t st);
+    // The tensor-core path (nullptr for the FP32 CUDA-core path), for block screening.
+    class TcChi0 *tensor_path();
 
     struct Impl;
 

@@ -16,6 +16,7 @@
 //     one lane issues the tcgen05.mma terms.  K order: pass, 8-column chunk, group of 8 j.
 //  3. T2 (small, CUDA cores): D += sum_{i,j} X_b^I[mu i; (cJ,J) j] X_a^J[nu j; (-cJ,I) i].
 // Every wait is bounded (tc_common.cuh) and failures surface through a device error flag.
+#include <algorithm>
 #include <cstdlib>
 #include <vector>
 
@@ -47,9 +48,21 @@ constexpr int T1_SMEM_MAX = 227 * 1024;
 // b_tile = NT_max * 128 rounded up to 1024; G blocks hold, per pass and cell, rap(RA) rows i
 // of gj FP32 entries j.
 
+// A row group: the n_abf(I) rows mu of one chi0 block (pair (I, J), cell cJ).
+struct T1Group
+{
+    int pair, cell;
+};
+
+// A tile: up to 128 consecutive rows of the row groups of one atom J (groups ordered by I,
+// then cell), all contracted with the same C^J operand.
 struct T1Work
 {
-    int pair, tile;
+    int J;      // atom of the B operand
+    int g0;     // first row group
+    int r0;     // first row inside that group
+    int nrows;  // valid rows (<= 128)
+    int nslot;  // row groups the tile touches
 };
 
 constexpr int T1_MAXSPEC = 8;    // distinct (NAO, ABF) species with their own B maps
@@ -70,6 +83,7 @@ struct T1Args
     const double *G;         // [2][n_c][n_ao][n_ao]
     const int *cadd;         // [n_c*n_c] cadd[a*n_c+b] = cell of R_a + R_b
     const T1Work *work;
+    const T1Group *groups;
     const int *spec;           // [n_at] species of each atom
     const int *spec_idx;       // [n_at] index of the atom inside its species
     const int *aJpad;          // NAOs of each atom rounded up to JG
@@ -77,7 +91,7 @@ struct T1Args
     int b_tile;                // bytes per B piece (1024-aligned)
     int nbs;                   // stages of the B ring (2..T1_MAXB)
     int gj;                    // j entries per i row of the G blocks (largest aJpad)
-    int maxcj;                 // distinct cells a 128-row tile can span
+    int maxcj;                 // most row groups a 128-row tile can touch
     int vec4;                  // n_ao % 4 == 0: 4-column X gathers are one aligned float4
     double *out;               // chi0R
     int *err;
@@ -147,14 +161,29 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
 
     const Geom &g = a.g;
     const T1Work w = a.work[blockIdx.x];
-    const int I = a.pr.I[w.pair], J = a.pr.J[w.pair];
-    const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
+    const int J = w.J;
+    const int aJ = g.nao[J], bJ = g.nabf[J];
     const int njg = a.aJpad[J] / JG;
     const int NT = (bJ + 15) / 16 * 16;
     const int nc = g.n_c, nao = g.n_ao;
     const long long nsup = g.n_sup;
-    const int row0 = w.tile * T1_BM;
-    const int cj_min = row0 / bI;
+    // row r of the tile -> (row group, mu); false beyond the tile's valid rows
+    auto row_of = [&](int r, int &grp, int &mu) -> bool {
+        if (r >= w.nrows) return false;
+        int off = w.r0 + r, gi = w.g0;
+        for (int k = 0; k < w.nslot; ++k, ++gi)
+        {
+            const int b = g.nabf[a.pr.I[a.groups[gi].pair]];
+            if (off < b)
+            {
+                grp = gi;
+                mu = off;
+                return true;
+            }
+            off -= b;
+        }
+        return false;
+    };
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int total_stages = a.nkc * njg;
 
@@ -188,31 +217,33 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         const int t = threadIdx.x;
         const int r = t >> 1;           // row in tile
         const int cq = t & 1;           // 4-column group inside the 8-column chunk
-        const int rg = row0 + r;
-        const bool valid = rg < nc * bI;
-        const int cJ = valid ? rg / bI : 0;
-        const int mu = valid ? rg % bI : 0;
-        const int cjl = valid ? cJ - cj_min : 0;
+        int grp = 0, mu = 0;
+        const bool valid = row_of(r, grp, mu);
+        const int slot = valid ? grp - w.g0 : 0;
+        const int I = a.pr.I[a.groups[valid ? grp : w.g0].pair];
+        const int cJ = valid ? a.groups[grp].cell : 0;
+        const int aI = g.nao[I];
         const long long xrow = g.rowc_off[I] + static_cast<long long>(mu) * aI;
-        // G blocks of both passes for the tile's cells, [pass][cell][i][j] in FP32
-        const int ncj = min(a.maxcj, (min(row0 + T1_BM, nc * bI) - 1) / bI - cj_min + 1);
-        const int per_pass = ncj * RP * gst;
+        // G blocks of both passes for the tile's row groups, [pass][slot][i][j] in FP32
+        const int per_pass = w.nslot * RP * gst;
         for (int e = t; e < 2 * per_pass; e += PRODUCERS)
         {
             const int pass = e / per_pass, rem = e % per_pass;
-            const int cl = rem / (RP * gst), ij = rem % (RP * gst);
+            const int sl = rem / (RP * gst), ij = rem % (RP * gst);
             const int i = ij / gst, j = ij % gst;
+            const T1Group gr = a.groups[w.g0 + sl];
+            const int Ig = a.pr.I[gr.pair];
             float v = 0.0f;
-            if (i < aI && j < aJ)
-                v = static_cast<float>(a.G[((static_cast<size_t>(pass) * nc + cj_min + cl) * nao + g.ao_off[I] + i) * nao +
+            if (i < g.nao[Ig] && j < aJ)
+                v = static_cast<float>(a.G[((static_cast<size_t>(pass) * nc + gr.cell) * nao + g.ao_off[Ig] + i) * nao +
                                            g.ao_off[J] + j]);
-            gsm[(static_cast<size_t>(pass) * a.maxcj + cl) * RP * gst + ij] = v;
+            gsm[(static_cast<size_t>(pass) * a.maxcj + sl) * RP * gst + ij] = v;
         }
         named_bar_sync(1, PRODUCERS);
         const float4 *gp[2];
 #pragma unroll
         for (int pass = 0; pass < 2; ++pass)
-            gp[pass] = reinterpret_cast<const float4 *>(gsm) + (static_cast<size_t>(pass) * a.maxcj + cjl) * RP * gst / 4;
+            gp[pass] = reinterpret_cast<const float4 *>(gsm) + (static_cast<size_t>(pass) * a.maxcj + slot) * RP * gst / 4;
         const float *Xp[2] = {a.X + a.xsign, a.X};  // pass 0 contracts G(+) with X(-), pass 1 G(-) with X(+)
         // X_b^I[mu i][shift_cJ(col)] for the thread's 4 columns of chunk kc (np passes from pass p0)
         auto load_x = [&](int kc, int p0, int np, float4 (&x0)[RA], float4 (&x1)[BOTHX ? RA : 1]) {
@@ -510,12 +541,12 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         if (ctrl && !ok)
             for (int st = issued; st < copied; ++st)  // and its B copies land before the CTA exits
                 mbar_wait(&bfull[st % nbs], (st / nbs) & 1);
-        const int r = wq * 32 + lane;
-        const int rg = row0 + r;
-        if (ok && rg < nc * bI)
+        int grp = 0, mu = 0;
+        if (ok && row_of(wq * 32 + lane, grp, mu))
         {
-            const int cJ = rg / bI, mu = rg % bI;
-            double *orow = a.out + a.pr.r_off[w.pair] + (static_cast<long long>(cJ) * bI + mu) * bJ;
+            const T1Group gr = a.groups[grp];
+            const int bI = g.nabf[a.pr.I[gr.pair]];
+            double *orow = a.out + a.pr.r_off[gr.pair] + (static_cast<long long>(gr.cell) * bI + mu) * bJ;
 #pragma unroll
             for (int c = 0; c < NTC; ++c)
                 if (c < bJ) orow[c] = static_cast<double>(acc[c]);
@@ -528,11 +559,11 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
 
 // T2 for one (pair, cJ): out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i]
 __global__ void __launch_bounds__(256) k_t2(const float *__restrict__ X, long long xsign, Geom g, Pairs pr,
-                                           double *__restrict__ out)
+                                           const T1Group *__restrict__ groups, double *__restrict__ out)
 {
     __shared__ float s1[128 * 32];
     __shared__ float s2[128 * 32];
-    const int p = blockIdx.x / g.n_c, cJ = blockIdx.x % g.n_c;
+    const int p = groups[blockIdx.x].pair, cJ = groups[blockIdx.x].cell;
     const int I = pr.I[p], J = pr.J[p];
     const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
     const long long nsup = g.n_sup;
@@ -655,7 +686,13 @@ struct TcChi0::Impl
     DevBuf<float> X, Gf, Cf;
     DevBuf<int> err, cadd, ajpad;
     DevBuf<T1Work> work;
-    int n_work = 0;
+    DevBuf<T1Group> groups;
+    int n_work = 0, n_groups = 0;
+    std::vector<int> hI, hJ, nabf_h;
+    bool all_active = false;  // the uploaded work list covers every (pair, cell)
+    // Row groups of the active (pair, cell) blocks, ordered by J, then I, then cell, and the
+    // 128-row tiles over each J's rows; active == nullptr: every block.
+    void build_work(const unsigned char *active, cudaStream_t st);
     std::vector<SplitStore> cb;  // per species: C^J of its atoms, stacked
     T1Maps maps{};
     DevBuf<int> spec, spec_idx;
@@ -761,15 +798,11 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     m.spec.upload(spec.data(), spec.size(), st);
     m.spec_idx.alloc(spec_idx.size());
     m.spec_idx.upload(spec_idx.data(), spec_idx.size(), st);
-    std::vector<T1Work> work;
-    for (int p = 0; p < pr.n_pairs; ++p)
-    {
-        const int rows = g.n_c * nabf[hI[p]];
-        for (int t = 0; t * T1_BM < rows; ++t) work.push_back({p, t});
-    }
-    m.n_work = static_cast<int>(work.size());
-    m.work.alloc(work.size());
-    m.work.upload(work.data(), work.size(), st);
+    m.hI = hI;
+    m.hJ = hJ;
+    m.nabf_h = nabf;
+    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1));
+    m.groups.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c);
     int ntmax = 16, minb = 1 << 30;
     for (int J = 0; J < g.n_at; ++J)
     {
@@ -778,6 +811,7 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     }
     m.b_tile = (ntmax * 128 + 1023) / 1024 * 1024;
     m.maxcj = (T1_BM + minb - 1) / minb + 1;
+    m.build_work(nullptr, st);
     m.ra = g.max_nao == 13 ? 13 : g.max_nao <= 16 ? 16 : 32;
     m.ntc = ntmax <= 64 ? 64 : 128;
     m.gj = JG;
@@ -790,11 +824,72 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     GB_CUDA(cudaStreamSynchronize(st));
 }
 
+void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
+{
+    if (!active && all_active) return;
+    std::vector<T1Group> grp;
+    std::vector<T1Work> tiles;
+    std::vector<std::vector<int>> pairs_of(g.n_at);
+    for (int p = 0; p < pr.n_pairs; ++p) pairs_of[hJ[p]].push_back(p);
+    for (int J = 0; J < g.n_at; ++J)
+    {
+        std::sort(pairs_of[J].begin(), pairs_of[J].end(), [&](int x, int y) { return hI[x] < hI[y]; });
+        const int gbeg = static_cast<int>(grp.size());
+        for (int p : pairs_of[J])
+            for (int c = 0; c < g.n_c; ++c)
+                if (!active || active[static_cast<size_t>(p) * g.n_c + c]) grp.push_back({p, c});
+        // tiles of 128 rows over the concatenated rows of this J's groups
+        int gi = gbeg, off = 0;  // current group and row inside it
+        while (gi < static_cast<int>(grp.size()))
+        {
+            T1Work t{J, gi, off, 0, 0};
+            int rows = 0, g2 = gi, o2 = off;
+            while (rows < T1_BM && g2 < static_cast<int>(grp.size()))
+            {
+                const int b = nabf_h[hI[grp[g2].pair]];
+                const int take = std::min(b - o2, T1_BM - rows);
+                rows += take;
+                ++t.nslot;
+                o2 += take;
+                if (o2 == b)
+                {
+                    ++g2;
+                    o2 = 0;
+                }
+            }
+            t.nrows = rows;
+            GB_REQUIRE(t.nslot <= maxcj, "chi0 tile touches more row groups than its shared-memory G slots");
+            tiles.push_back(t);
+            gi = g2;
+            off = o2;
+        }
+    }
+    // launch order: by the I atom of a tile's first row group, so the CTAs resident at one time
+    // stream the same X^I rows (the largest operand) through L2
+    std::stable_sort(tiles.begin(), tiles.end(), [&](const T1Work &x, const T1Work &y) {
+        return hI[grp[x.g0].pair] < hI[grp[y.g0].pair];
+    });
+    n_groups = static_cast<int>(grp.size());
+    n_work = static_cast<int>(tiles.size());
+    GB_REQUIRE(tiles.size() <= work.size() && grp.size() <= groups.size(), "chi0 work list overflow");
+    if (n_groups > 0)
+    {
+        groups.upload(grp.data(), grp.size(), st);
+        work.upload(tiles.data(), tiles.size(), st);
+    }
+    all_active = active == nullptr;
+}
+
 TcChi0::~TcChi0() = default;
 
 int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t st)
 {
     (void)Gs;
+    return prepare(G, st) + contract(G, chi0R, nullptr, false, st);
+}
+
+int TcChi0::prepare(const double *G, cudaStream_t st)
+{
     Impl &m = *impl_;
     const Geom &g = m.g;
     const long long nsup = g.n_sup;
@@ -805,9 +900,20 @@ int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t s
     tc_gemm_split(m.csplit.mat(g.rows_c, m.kpad, 0), m.gs.mat(nsup, m.kpad, nsup * m.kpad), static_cast<int>(g.rows_c),
                   static_cast<int>(nsup), static_cast<int>(nsup), 2, m.X.get(), nsup, g.rows_c * nsup, false,
                   m.err.get(), st);
-    int launches = 2;
+    return 2;
+}
+
+int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active, bool zero_first, cudaStream_t st)
+{
+    Impl &m = *impl_;
+    const Geom &g = m.g;
+    const long long nsup = g.n_sup;
+    int launches = 0;
+    if (zero_first)
+        GB_CUDA(cudaMemsetAsync(chi0R, 0, sizeof(double) * static_cast<size_t>(m.pr.e_total) * g.n_c, st));
     if (m.t1_simt)
     {
+        GB_REQUIRE(!active, "block screening needs the tensor-core chi0 kernel");
         const long long ng = static_cast<long long>(g.n_c) * g.n_ao * g.n_ao;
         launch_d2f(G, m.Gf.get(), 2 * ng, st);
         launch_chi0_fp32(m.X.get(), m.X.get() + g.rows_c * nsup, m.Cf.get(), m.Gf.get(), m.Gf.get() + ng, g, m.pr,
@@ -816,6 +922,7 @@ int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t s
     }
     else
     {
+        m.build_work(active, st);
         T1Args a;
         a.g = g;
         a.pr = m.pr;
@@ -824,6 +931,7 @@ int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t s
         a.G = G;
         a.cadd = m.cadd.get();
         a.work = m.work.get();
+        a.groups = m.groups.get();
         a.spec = m.spec.get();
         a.spec_idx = m.spec_idx.get();
         a.aJpad = m.ajpad.get();
@@ -835,11 +943,14 @@ int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t s
         a.vec4 = g.n_ao % 4 == 0 ? 1 : 0;
         a.out = chi0R;
         a.err = m.err.get();
-        t1_kernel(m.ra, m.ntc)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
-        GB_LAUNCH_CHECK();
-        k_t2<<<m.pr.n_pairs * g.n_c, 256, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, chi0R);
-        GB_LAUNCH_CHECK();
-        launches += 2;
+        if (m.n_work > 0)
+        {
+            t1_kernel(m.ra, m.ntc)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
+            GB_LAUNCH_CHECK();
+            k_t2<<<m.n_groups, 256, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, m.groups.get(), chi0R);
+            GB_LAUNCH_CHECK();
+            launches += 2;
+        }
     }
     int herr = 0;
     m.err.download(&herr, 1, st);

@@ -81,6 +81,12 @@ public:
     ~TcChi0();
     // G (both signs, [sign][cell][i][j]) and the supercell G -> chi0(R) upper-pair blocks.
     int run(const double *Gs, const double *G, double *chi0R, cudaStream_t st);
+    // The two halves of run(): X(+-) = C * G_super(+-) ...
+    int prepare(const double *G, cudaStream_t st);
+    // ... and the block contraction of the active (pair, cell) blocks (active: host mask
+    // [pair * n_cells + cell], nullptr = all).  zero_first clears chi0R first, so blocks left
+    // out read zero; a later call with zero_first = false adds further blocks.
+    int contract(const double *G, double *chi0R, const unsigned char *active, bool zero_first, cudaStream_t st);
 
     struct Impl;
 
