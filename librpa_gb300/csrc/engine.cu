@@ -27,6 +27,7 @@
 #include "common.h"
 #include "dataset.h"
 #include "ec_tc.h"
+#include "gk_tc.h"
 #include "kernels.h"
 #include "minimax.h"
 
@@ -377,16 +378,33 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     // ------------------------------------------------------------ tau loop
     const int nw = tf.n;
     DevBuf<double> d_s(2ull * nk * nb);
-    DevBuf<cuDoubleComplex> d_A(2ull * nk * nao * nao);
+    const int prec = go.chi0_precision;
+    const bool tc_path = prec == LIBRPA_GB300_CHI0_BF16X3;
+    DevBuf<cuDoubleComplex> d_A(tc_path ? 0 : 2ull * nk * nao * nao);
     DevBuf<double> d_G(2ull * nc * nao * nao);
-    DevBuf<double> d_Gs(2ull * n_sup * n_sup);
-    DevBuf<double> d_X(2ull * rows_c * n_sup);
+    // the supercell G and FP64 X serve the FP64 and FP32 paths; the tensor-core path builds its
+    // split operands from G directly
+    DevBuf<double> d_Gs(tc_path ? 0 : 2ull * n_sup * n_sup);
+    DevBuf<double> d_X(prec == LIBRPA_GB300_CHI0_FP64 ? 2ull * rows_c * n_sup : 0);
+    DevBuf<int> d_err(1);
+    d_err.zero(st);
+    std::unique_ptr<GkTc> gk;
+    if (tc_path)
+    {
+        bool psi_real = true;
+        for (const auto &z : ds.wfc)
+            if (z.imag() != 0.0)
+            {
+                psi_real = false;
+                break;
+            }
+        gk = std::make_unique<GkTc>(nk, nb, nao, psi_real);
+    }
     DevBuf<double> d_chi0R(static_cast<size_t>(r_tot));
     DevBuf<cuDoubleComplex> d_chi0q(static_cast<size_t>(nw) * nq * e_tot);
     d_chi0q.zero(st);
     DevBuf<double> d_gamma(static_cast<size_t>(nw));
 
-    const int prec = go.chi0_precision;
     std::unique_ptr<Chi0Fast> fast;
     if (prec != LIBRPA_GB300_CHI0_FP64) fast = std::make_unique<Chi0Fast>(prec, g, pr, d_C.get(), st);
 
@@ -407,10 +425,16 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             ev_gf.start(st);
             launch_tau_scale(d_ekb.get() + static_cast<size_t>(is) * nk * nb, d_wg.get() + static_cast<size_t>(is) * nk * nb,
                              nk, nb, ds.efermi, tau, ns, nbands_g, d_s.get(), st);
-            launch_gk_build(d_psi.get() + static_cast<size_t>(is) * nk * nb * nao, d_s.get(), nk, nb, nao, d_A.get(), st);
-            launch_phase_sum(d_A.get(), d_gcos.get(), d_gsin.get(), nk, nc, nao, d_G.get(), st);
-            launch_gsuper(d_G.get(), g, d_Gs.get(), st);
-            launches += 4;
+            if (gk)
+                launches += 1 + gk->run(d_psi.get() + static_cast<size_t>(is) * nk * nb * nao, d_s.get(), d_gcos.get(),
+                                        d_gsin.get(), nc, d_G.get(), d_err.get(), st);
+            else
+            {
+                launch_gk_build(d_psi.get() + static_cast<size_t>(is) * nk * nb * nao, d_s.get(), nk, nb, nao, d_A.get(), st);
+                launch_phase_sum(d_A.get(), d_gcos.get(), d_gsin.get(), nk, nc, nao, d_G.get(), st);
+                launch_gsuper(d_G.get(), g, d_Gs.get(), st);
+                launches += 4;
+            }
             ev_gf.stop(st);
             t_gf += ev_gf.ms();
             ev_chi.start(st);
@@ -468,6 +492,12 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         }
         flops_chi = per * nw * ns;
         flops_libri = 2.0 * lib * nw * ns;
+    }
+    {
+        int herr = 0;
+        d_err.download(&herr, 1, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+        GB_REQUIRE(herr == 0, "tensor-core G build reported wait timeout code " + std::to_string(herr));
     }
     S.t_gf = t_gf * 1e-3;
     S.t_chi0 = t_chi * 1e-3;
