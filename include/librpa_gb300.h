@@ -25,8 +25,12 @@ extern "C" {
 
 /* block screening of chi0 contributions */
 #define LIBRPA_GB300_SCREEN_OFF 0
-#define LIBRPA_GB300_SCREEN_THRESHOLD 1   /* drop (I,J,R) blocks whose bound is below the threshold */
-#define LIBRPA_GB300_SCREEN_MLP 2         /* learned predictor + random audit, threshold as judge */
+#define LIBRPA_GB300_SCREEN_THRESHOLD 1   /* contract every chi0(I,J,R,tau) block, drop those with
+                                             max |chi0| <= screen_threshold (LibRI's max-norm filter
+                                             rule); log block features and norms for training */
+#define LIBRPA_GB300_SCREEN_MLP 2         /* contract only blocks a trained MLP predicts above the
+                                             threshold, plus a random audit share of the others;
+                                             the threshold rule stays the judge and the fallback */
 
 typedef struct
 {
@@ -67,6 +71,8 @@ typedef struct
     long long n_chi0_kernel;    /* launches of the dominant chi0 kernel */
     double h2d_bytes;           /* host -> device bytes staged by this call (0 when the cache was reused) */
     double d2h_bytes;           /* device -> host bytes of results */
+    long long screen_fallbacks; /* (tau, spin) steps where an audited skipped block exceeded the
+                                   threshold and every block was contracted */
 } LibrpaGB300Stats;
 
 /* Set defaults. */
@@ -94,6 +100,30 @@ int librpa_gb300_minimax_grid(int n, double emin, double emax, double regulariza
  * caller as two row-major n_mu x n_nu arrays.  Returns 0 on success. */
 int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq_ibz, int I, int J,
                                 double *re, double *im);
+
+/* Learned screening (no counterpart in the reference).  The model is a 5-64-64-1 GELU MLP
+ * (FP16 weights, FP32 accumulation) predicting log10 max |chi0(I,J,R,tau)| from the block's
+ * distance, log10 tau, log10(max|C_I| max|C_J|) and log10 max |G(+-tau)_IJ(R)|.  Its training
+ * data are the blocks logged by calls with screen_mode = LIBRPA_GB300_SCREEN_THRESHOLD.
+ * librpa_gb300_train_screening trains it on the GPU (Adam, `iterations` steps of up to 16384
+ * samples); a screen_mode = MLP call trains it itself when needed.  Returns 0 on success and
+ * writes the training RMSE (log10 units) to *rmse. */
+int librpa_gb300_train_screening(LibrpaHandler *h, int iterations, double learning_rate, double *rmse);
+/* Logged samples: count, and a copy (x: n x 5 features, y: n targets). */
+long long librpa_gb300_screening_samples(LibrpaHandler *h);
+int librpa_gb300_get_screening_samples(LibrpaHandler *h, float *x, float *y, long long n);
+/* The trained model: 4609 parameters (W1[64][5], b1[64], W2[64][64], b2[64], W3[64], b3) and
+ * 13 normalisation values (feature means[5], scales[5], target mean, target scale, decision
+ * margin).  get returns 0 when a model exists; set installs one. */
+int librpa_gb300_get_screening_model(LibrpaHandler *h, float *params, float *norm);
+int librpa_gb300_set_screening_model(LibrpaHandler *h, const float *params, const float *norm);
+/* Drop the logged samples and the model. */
+void librpa_gb300_clear_screening(LibrpaHandler *h);
+/* The MLP's training kernels on one batch: mean squared error on normalised targets and its
+ * gradient for the given FP32 parameters (rounded to FP16 as the forward pass uses them).
+ * For checking the GPU gradients against a CPU restatement.  Returns 0 on success. */
+int librpa_gb300_mlp_loss_grad(const float *params, const float *norm, const float *x, const float *y, int n,
+                               float *grad, double *loss);
 
 /* Number of CUDA devices visible (0 when there is no GPU). */
 int librpa_gb300_device_count(void);

@@ -28,6 +28,8 @@ TFGRID_UNSET, GaussLegendre, GaussChebyshevI, GaussChebyshevII, Minimax, EvenSpa
 CHI0_FP64, CHI0_BF16X3, CHI0_FP32 = 0, 1, 2
 EC_LU_FP64, EC_CHOL = 0, 1
 SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
+MLP_NPARAM, MLP_NNORM = 4609, 13
+SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
 
 
 class LibrpaOptions(C.Structure):
@@ -104,7 +106,7 @@ class GB300Stats(C.Structure):
         ("gf_flops", C.c_double), ("ftct_bytes", C.c_double), ("n_launches", C.c_longlong),
         ("blocks_total", C.c_longlong), ("blocks_computed", C.c_longlong), ("blocks_audited", C.c_longlong),
         ("audit_max_dropped", C.c_double), ("dt_chi0_kernel_ms", C.c_double), ("n_chi0_kernel", C.c_longlong),
-        ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
+        ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double), ("screen_fallbacks", C.c_longlong),
     ]
 
     def as_dict(self):
@@ -130,7 +132,9 @@ EXPORTS = [
     "librpa_gb300_init_options", "librpa_gb300_set_options", "librpa_gb300_get_stats",
     "librpa_get_last_error", "librpa_get_last_error_code", "librpa_gb300_minimax_grid",
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
-    "librpa_gb300_tc_gemm_noalloc",
+    "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
+    "librpa_gb300_get_screening_samples", "librpa_gb300_get_screening_model", "librpa_gb300_set_screening_model",
+    "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad",
 ]
 
 _lib = None
@@ -183,6 +187,13 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_selftest_tc_gemm": (d, [i, i, i, i, i]),
         "librpa_gb300_tc_gemm_noalloc": (i, [i, i, i, C.c_void_p, C.c_void_p, C.c_void_p, i,
                                              C.c_void_p]),
+        "librpa_gb300_train_screening": (i, [vp, i, d, C.POINTER(C.c_double)]),
+        "librpa_gb300_screening_samples": (C.c_longlong, [vp]),
+        "librpa_gb300_get_screening_samples": (i, [vp, vp, vp, C.c_longlong]),
+        "librpa_gb300_get_screening_model": (i, [vp, vp, vp]),
+        "librpa_gb300_set_screening_model": (i, [vp, vp, vp]),
+        "librpa_gb300_clear_screening": (None, [vp]),
+        "librpa_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, i, vp, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -16,6 +16,7 @@
 #include "../../include/librpa.h"
 #include "common.h"
 #include "dataset.h"
+#include "screen.h"
 #include "minimax.h"
 #include "tc_gemm.h"
 
@@ -875,6 +876,119 @@ double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces)
         r = gb::tc_gemm_selftest(M, N, K, seed, pieces);
     });
     return r;
+}
+
+// ---- learned screening (screen.cu); no counterpart in the reference
+int librpa_gb300_train_screening(LibrpaHandler *h, int iterations, double learning_rate, double *rmse)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(gb::device_count() > 0, "no CUDA device visible");
+        GB_REQUIRE(iterations > 0 && learning_rate > 0, "iterations and learning_rate must be positive");
+        GB_CUDA(cudaSetDevice(ds->gbopt.device));
+        cudaStream_t st;
+        GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        try
+        {
+            gb::mlp_train(ds->screen_model, ds->screen_log.x, ds->screen_log.y, iterations, learning_rate,
+                          ds->gbopt.seed, st);
+        }
+        catch (...)
+        {
+            cudaStreamDestroy(st);
+            throw;
+        }
+        cudaStreamDestroy(st);
+        if (rmse) *rmse = ds->screen_model.train_rmse;
+        rc = 0;
+    });
+    return rc;
+}
+
+long long librpa_gb300_screening_samples(LibrpaHandler *h)
+{
+    long long n = -1;
+    guarded(h, [&] { n = static_cast<long long>(get_ds(h)->screen_log.size()); });
+    return n;
+}
+
+int librpa_gb300_get_screening_samples(LibrpaHandler *h, float *x, float *y, long long n)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        const gb::ScreenLog &lg = get_ds(h)->screen_log;
+        GB_REQUIRE(n >= 0 && static_cast<size_t>(n) <= lg.size(), "more samples requested than logged");
+        std::copy(lg.x.begin(), lg.x.begin() + n * gb::MLP_IN, x);
+        std::copy(lg.y.begin(), lg.y.begin() + n, y);
+        rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_get_screening_model(LibrpaHandler *h, float *params, float *norm)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        const gb::ScreenModel &m = get_ds(h)->screen_model;
+        GB_REQUIRE(m.trained, "no screening model: train one first");
+        std::copy(m.params.begin(), m.params.end(), params);
+        std::copy(m.norm.begin(), m.norm.end(), norm);
+        rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_set_screening_model(LibrpaHandler *h, const float *params, const float *norm)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        gb::ScreenModel &m = get_ds(h)->screen_model;
+        GB_REQUIRE(params && norm, "null model arrays");
+        for (int f = 0; f < gb::MLP_IN; ++f)
+            GB_REQUIRE(norm[gb::MLP_IN + f] > 0.0f, "feature scales must be positive");
+        GB_REQUIRE(norm[2 * gb::MLP_IN + 1] > 0.0f, "target scale must be positive");
+        m.params.assign(params, params + gb::MLP_NPARAM);
+        m.norm.assign(norm, norm + gb::MLP_NNORM);
+        m.trained = true;
+        rc = 0;
+    });
+    return rc;
+}
+
+void librpa_gb300_clear_screening(LibrpaHandler *h)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        ds->screen_log = gb::ScreenLog{};
+        ds->screen_model = gb::ScreenModel{};
+    });
+}
+
+int librpa_gb300_mlp_loss_grad(const float *params, const float *norm, const float *x, const float *y, int n,
+                               float *grad, double *loss)
+{
+    int rc = 1;
+    guarded(nullptr, [&] {
+        GB_REQUIRE(gb::device_count() > 0, "no CUDA device visible");
+        GB_REQUIRE(params && norm && x && y && grad && n > 0, "bad arguments");
+        cudaStream_t st;
+        GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        double l = 0.0;
+        try
+        {
+            l = gb::mlp_loss_grad(params, norm, x, y, n, grad, st);
+        }
+        catch (...)
+        {
+            cudaStreamDestroy(st);
+            throw;
+        }
+        cudaStreamDestroy(st);
+        if (loss) *loss = l;
+        rc = 0;
+    });
+    return rc;
 }
 
 // No counterpart in the reference: the allocation-free split GEMM (tc_gemm_noalloc.cu).

@@ -12,6 +12,7 @@
 
 #include "../../include/librpa_gb300.h"
 #include "../../include/librpa_options.h"
+#include "screen_model.h"
 
 namespace gb {
 
@@ -78,6 +79,8 @@ struct Dataset
 
     // GB300 extensions
     LibrpaGB300Options gbopt{};
+    ScreenLog screen_log;      // block features and norms logged by plain-screening calls
+    ScreenModel screen_model;  // learned block-norm predictor
     LibrpaGB300Stats stats{};
     int last_error_code = 0;
     std::string last_error;

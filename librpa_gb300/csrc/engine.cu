@@ -22,12 +22,15 @@
 #include <cmath>
 #include <map>
 #include <numeric>
+#include <random>
 
 #include "chi0_fast.h"
 #include "common.h"
 #include "dataset.h"
 #include "ec_tc.h"
 #include "gk_tc.h"
+#include "screen.h"
+#include "tc_gemm.h"
 #include "kernels.h"
 #include "minimax.h"
 
@@ -252,7 +255,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             double mx = 0.0;
             const size_t n = static_cast<size_t>(b.ni) * b.nj * b.nmu;
             for (size_t t = 0; t < n; ++t) mx = std::max(mx, std::fabs(ds.cs_blob[b.offset + t]));
-            if (mx < thr_c) continue;
+            if (mx <= thr_c) continue;  // LibRI keeps a block whose max-norm exceeds the threshold
         }
         cs_off.push_back(static_cast<long long>(b.offset));
         cs_meta.insert(cs_meta.end(), {b.I, b.J, c, 0});
@@ -408,6 +411,75 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     std::unique_ptr<Chi0Fast> fast;
     if (prec != LIBRPA_GB300_CHI0_FP64) fast = std::make_unique<Chi0Fast>(prec, g, pr, d_C.get(), st);
 
+    // ---- block screening set-up
+    const int smode = go.screen_mode;
+    GB_REQUIRE(smode == LIBRPA_GB300_SCREEN_OFF || smode == LIBRPA_GB300_SCREEN_THRESHOLD ||
+                   smode == LIBRPA_GB300_SCREEN_MLP,
+               "unknown screen_mode " + std::to_string(smode));
+    const double sthr = go.screen_threshold;
+    const double thr_g = opts.libri_chi0_threshold_G;
+    const int n_blk = n_pairs * nc;
+    DevBuf<double> d_bnorm;
+    DevBuf<float> d_feat, d_pred, d_dist, d_cmax;
+    std::vector<double> h_norm;
+    std::vector<float> h_feat, h_pred;
+    std::vector<unsigned char> active, audited;
+    long long blk_computed = 0, blk_audited = 0, fallbacks = 0;
+    double audit_max = 0.0;
+    std::mt19937_64 audit_rng(go.seed);
+    if (smode != LIBRPA_GB300_SCREEN_OFF)
+    {
+        GB_REQUIRE(sthr >= 0.0, "screen_threshold must be >= 0");
+        // block distance |tau_J + R - tau_I| (Bohr) and the largest |C| of each atom's RI blocks
+        std::vector<float> dist(n_blk), cmax(n_at, 0.0f);
+        for (int p = 0; p < n_pairs; ++p)
+            for (int c = 0; c < nc; ++c)
+            {
+                double d2 = 0.0;
+                for (int d = 0; d < 3; ++d)
+                {
+                    double Rc = 0.0;
+                    for (int a = 0; a < 3; ++a) Rc += cells.R[c][a] * ds.latvec[a * 3 + d];
+                    const double pi = ds.positions.size() >= 3ull * n_at ? ds.positions[3 * pI[p] + d] : 0.0;
+                    const double pj = ds.positions.size() >= 3ull * n_at ? ds.positions[3 * pJ[p] + d] : 0.0;
+                    d2 += (pj + Rc - pi) * (pj + Rc - pi);
+                }
+                dist[static_cast<size_t>(p) * nc + c] = static_cast<float>(std::sqrt(d2));
+            }
+        for (const CsBlock &b : ds.cs_blocks)
+        {
+            const size_t n = static_cast<size_t>(b.ni) * b.nj * b.nmu;
+            double mx = 0.0;
+            for (size_t t = 0; t < n; ++t) mx = std::max(mx, std::fabs(ds.cs_blob[b.offset + t]));
+            cmax[b.I] = std::max(cmax[b.I], static_cast<float>(mx));
+        }
+        d_dist.alloc(n_blk);
+        d_dist.upload(dist.data(), n_blk, st);
+        d_cmax.alloc(n_at);
+        d_cmax.upload(cmax.data(), n_at, st);
+        d_bnorm.alloc(n_blk);
+        d_feat.alloc(static_cast<size_t>(n_blk) * MLP_IN);
+        h_norm.resize(n_blk);
+        h_feat.resize(static_cast<size_t>(n_blk) * MLP_IN);
+    }
+    TcChi0 *tcp = nullptr;
+    if (smode == LIBRPA_GB300_SCREEN_MLP)
+    {
+        tcp = fast ? fast->tensor_path() : nullptr;
+        GB_REQUIRE(tcp, "learned screening needs the tensor-core chi0 path (chi0_precision = BF16X3)");
+        if (!ds.screen_model.trained)
+        {
+            GB_REQUIRE(ds.screen_log.size() >= 16,
+                       "learned screening needs a trained model: run with plain threshold screening first "
+                       "(its block norms are the training data) or call librpa_gb300_train_screening");
+            mlp_train(ds.screen_model, ds.screen_log.x, ds.screen_log.y, 600, 3e-3, go.seed, st);
+        }
+        d_pred.alloc(n_blk);
+        h_pred.resize(n_blk);
+        active.resize(n_blk);
+        audited.resize(n_blk);
+    }
+
     EventTimer ev_gf, ev_x, ev_chi, ev_ft;
     double t_gf = 0, t_chi = 0, t_ft = 0;
     double flops_chi = 0.0, flops_libri = 0.0;
@@ -435,6 +507,11 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 launch_gsuper(d_G.get(), g, d_Gs.get(), st);
                 launches += 4;
             }
+            if (thr_g > 0.0)
+            {
+                launch_g_block_filter(d_G.get(), g, thr_g, st);  // LibRI set_Gs_pos / set_Gs_neg filter
+                ++launches;
+            }
             ev_gf.stop(st);
             t_gf += ev_gf.ms();
             ev_chi.start(st);
@@ -448,11 +525,76 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 ev_x.stop(st);
                 launches += 2;
             }
+            else if (smode == LIBRPA_GB300_SCREEN_MLP)
+            {
+                // predicted block norms -> contract the blocks above the threshold and an audit
+                // share of the rest; an audited block above the threshold means fall back
+                ev_x.start(st);
+                launches += tcp->prepare(d_G.get(), st);
+                launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), tau, d_feat.get(), st);
+                mlp_predict(ds.screen_model, d_feat.get(), n_blk, d_pred.get(), st);
+                launches += 3;
+                d_pred.download(h_pred.data(), n_blk, st);
+                GB_CUDA(cudaStreamSynchronize(st));
+                const double cut = std::log10(std::max(sthr, 1e-300)) - ds.screen_model.norm[MLP_NNORM - 1];
+                std::uniform_real_distribution<double> u01(0.0, 1.0);
+                long long n_act = 0;
+                for (int b = 0; b < n_blk; ++b)
+                {
+                    const bool keep = h_pred[b] > cut;
+                    audited[b] = !keep && u01(audit_rng) < go.audit_fraction;
+                    active[b] = keep || audited[b];
+                    n_act += active[b];
+                    blk_audited += audited[b];
+                }
+                launches += tcp->contract(d_G.get(), d_chi0R.get(), active.data(), true, st);
+                launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
+                ++launches;
+                d_bnorm.download(h_norm.data(), n_blk, st);
+                GB_CUDA(cudaStreamSynchronize(st));
+                bool violated = false;
+                for (int b = 0; b < n_blk; ++b)
+                    if (audited[b])
+                    {
+                        audit_max = std::max(audit_max, h_norm[b]);
+                        violated = violated || h_norm[b] > sthr;
+                    }
+                if (violated)
+                {
+                    for (int b = 0; b < n_blk; ++b) active[b] = !active[b];
+                    launches += tcp->contract(d_G.get(), d_chi0R.get(), active.data(), false, st);
+                    launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
+                    ++launches;
+                    n_act = n_blk;
+                    ++fallbacks;
+                }
+                blk_computed += n_act;
+                ev_x.stop(st);
+            }
             else
             {
                 ev_x.start(st);
                 launches += fast->run(d_Gs.get(), Gp, Gm, d_chi0R.get(), st);
                 ev_x.stop(st);
+            }
+            if (smode == LIBRPA_GB300_SCREEN_THRESHOLD)
+            {
+                // plain screening: every block computed; its features and norm are logged
+                launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
+                launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), tau, d_feat.get(), st);
+                launches += 2;
+                d_bnorm.download(h_norm.data(), n_blk, st);
+                d_feat.download(h_feat.data(), h_feat.size(), st);
+                GB_CUDA(cudaStreamSynchronize(st));
+                ds.screen_log.x.insert(ds.screen_log.x.end(), h_feat.begin(), h_feat.end());
+                for (int b = 0; b < n_blk; ++b)
+                    ds.screen_log.y.push_back(h_norm[b] > 0.0 ? static_cast<float>(std::log10(h_norm[b])) : -40.0f);
+                blk_computed += n_blk;
+            }
+            if (smode != LIBRPA_GB300_SCREEN_OFF)
+            {
+                launch_block_drop(d_chi0R.get(), g, pr, d_bnorm.get(), sthr, st);  // keep max-norm > threshold
+                ++launches;
             }
             ev_chi.stop(st);
             t_chi += ev_chi.ms();
@@ -637,8 +779,11 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     GB_CUDA(cudaStreamSynchronize(st));
     S.n_launches = launches;
     S.d2h_bytes = 16.0 * 2 * nw * nq;
-    S.blocks_total = static_cast<long long>(n_pairs) * nc;
-    S.blocks_computed = S.blocks_total;
+    S.blocks_total = static_cast<long long>(n_blk) * nw * ns;
+    S.blocks_computed = smode == LIBRPA_GB300_SCREEN_OFF ? S.blocks_total : blk_computed;
+    S.blocks_audited = blk_audited;
+    S.audit_max_dropped = audit_max;
+    S.screen_fallbacks = fallbacks;
     S.t_total = wall_seconds() - t_begin;
     return res;
 }

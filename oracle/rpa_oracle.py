@@ -196,16 +196,25 @@ def cs_tensors(inp: RPAInput, threshold: float = 0.0):
     for (I, J, R), m in inp.Cs.items():
         ni, nj = inp.nao[I], inp.nao[J]
         t = m.T.reshape(m.shape[1], ni, nj)
-        if threshold > 0 and np.abs(t).max() < threshold:
+        if threshold > 0 and np.abs(t).max() <= threshold:  # kept when max-norm > threshold (LRI.hpp:20-25)
             continue
         out[(I, J, tuple(R))] = t
     return out
 
 
 def _filter_g(G: dict, threshold: float):
+    """LibRI's set_Gs_pos / set_Gs_neg filter (LRI-set.hpp:56-61): keep blocks with max |G| > threshold."""
     if threshold <= 0:
         return G
-    return {k: v for k, v in G.items() if np.abs(v).max() >= threshold}
+    return {k: v for k, v in G.items() if np.abs(v).max() > threshold}
+
+
+def screen_blocks(chi0s: dict, threshold: float):
+    """The same max-norm rule applied to chi0(I, J, R, tau) blocks: keep max |chi0| > threshold.
+
+    Plain block screening of the GPU library (LibrpaGB300Options.screen_threshold); the
+    reference applies this rule to its input tensors only."""
+    return {k: v for k, v in chi0s.items() if np.abs(v).max() > threshold}
 
 
 def cal_chi0s_loops(C: dict, Gpos: dict, Gneg: dict, n_atoms: int, period, acc: dict | None = None):
@@ -468,7 +477,7 @@ def correlation_energy(chi0q, inp: RPAInput, grid, ibz_order, ibz_weight, opts: 
 # ----------------------------------------------------------------------------- driver
 
 def rpa_correlation_energy(inp: RPAInput, opts: Options | None = None, chi0_impl: str = "dense",
-                           keep_chi0s: bool = False):
+                           keep_chi0s: bool = False, block_threshold: float | None = None):
     """Full oracle pipeline; returns a dict with E_c and intermediates."""
     opts = opts or Options()
     grid = grids_for(inp, opts)
@@ -490,6 +499,8 @@ def rpa_correlation_energy(inp: RPAInput, opts: Options | None = None, chi0_impl
                 chi0s = cal_chi0s_loops(C, Gp, Gn, inp.n_atoms, inp.period)
             else:
                 chi0s = cal_chi0s_dense(C, Gp, Gn, inp.nao, inp.nabf, inp.period)
+            if block_threshold is not None:
+                chi0s = screen_blocks(chi0s, block_threshold)
             if keep_chi0s:
                 chi0s_all.append(chi0s)
             ft_ct_accumulate(chi0q, chi0s, it, grid, klist_ibz, inp.latvec, inp.n_spins, pairs)
