@@ -811,15 +811,21 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     }
     m.b_tile = (ntmax * 128 + 1023) / 1024 * 1024;
     m.maxcj = (T1_BM + minb - 1) / minb + 1;
-    m.build_work(nullptr, st);
     m.ra = g.max_nao == 13 ? 13 : g.max_nao <= 16 ? 16 : 32;
     m.ntc = ntmax <= 64 ? 64 : 128;
     m.gj = JG;
     for (int J = 0; J < g.n_at; ++J) m.gj = std::max(m.gj, ajp[J]);
-    const int fixed = T1_STAGES * NS * A_TILE + 2 * m.maxcj * rap(m.ra) * m.gj * 4 + 1024 + 512;
+    // shared memory: A ring + at least two B stages + the G slots; fewer G slots than a tile of
+    // small row groups could touch only shortens such tiles
+    const int slot_bytes = 2 * rap(m.ra) * m.gj * 4;
+    const int base = T1_STAGES * NS * A_TILE + 1024 + 512;
+    const int fit = (T1_SMEM_MAX - base - 2 * NS * m.b_tile) / slot_bytes;
+    GB_REQUIRE(fit >= 1, "chi0 tile does not fit shared memory (too many ABFs or NAOs per atom)");
+    m.maxcj = std::min(m.maxcj, fit);
+    const int fixed = base + m.maxcj * slot_bytes;
     m.nbs = std::min(T1_MAXB, (T1_SMEM_MAX - fixed) / (NS * m.b_tile));
-    GB_REQUIRE(m.nbs >= 2, "chi0 tile does not fit shared memory (too many cells per tile or too many ABFs)");
     m.smem = fixed + m.nbs * NS * m.b_tile;
+    m.build_work(nullptr, st);
     GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc), cudaFuncAttributeMaxDynamicSharedMemorySize, m.smem));
     GB_CUDA(cudaStreamSynchronize(st));
 }
@@ -844,7 +850,8 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
         {
             T1Work t{J, gi, off, 0, 0};
             int rows = 0, g2 = gi, o2 = off;
-            while (rows < T1_BM && g2 < static_cast<int>(grp.size()))
+            // a tile closes at 128 rows or when it touches maxcj row groups (its G slots)
+            while (rows < T1_BM && g2 < static_cast<int>(grp.size()) && t.nslot < maxcj)
             {
                 const int b = nabf_h[hI[grp[g2].pair]];
                 const int take = std::min(b - o2, T1_BM - rows);
