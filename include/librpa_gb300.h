@@ -40,12 +40,23 @@ typedef struct
     double screen_threshold; /* block-norm threshold for screening (default 1e-6) */
     double audit_fraction;   /* share of skipped blocks computed exactly (default 0.02) */
     unsigned long long seed; /* audit sampling seed */
-    int use_cuda_graph;      /* capture the per-tau launch sequence once and replay it (default 1) */
+    int use_cuda_graph;      /* reserved: this build launches the per-tau sequence directly */
     int keep_chi0;           /* keep chi0(q, omega) on the device for librpa_gb300_get_chi0_block */
     int device;              /* CUDA device ordinal (default 0) */
     int reuse_device_inputs; /* keep the staged inputs on the device between calls while no
                                 librpa_set_* call changed them (default 1); 0 re-uploads every call */
+    /* tau sharding (one slice of the minimax tau points per rank; the chi0(q, omega) partial
+     * sums are reduced over ranks before E_c): */
+    int tau_begin;           /* first tau point of this call (default 0) */
+    int tau_end;             /* one past the last; -1 = all (default -1) */
+    int stage;               /* LIBRPA_GB300_STAGE_* (default FULL) */
 } LibrpaGB300Options;
+
+#define LIBRPA_GB300_STAGE_FULL 0   /* chi0 over [tau_begin, tau_end) and E_c */
+#define LIBRPA_GB300_STAGE_CHI0 1   /* chi0(q, omega) over [tau_begin, tau_end), kept on the device;
+                                       the call returns 0 (no E_c) */
+#define LIBRPA_GB300_STAGE_EC 2     /* E_c from the kept chi0(q, omega) (after
+                                       librpa_gb300_load_chi0_qw); no chi0 work */
 
 /* Timing and work counters of the last librpa_get_rpa_correlation_energy call. */
 typedef struct
@@ -100,6 +111,14 @@ int librpa_gb300_minimax_grid(int n, double emin, double emax, double regulariza
  * caller as two row-major n_mu x n_nu arrays.  Returns 0 on success. */
 int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq_ibz, int I, int J,
                                 double *re, double *im);
+
+/* Kept chi0(q, omega) (keep_chi0 or STAGE_CHI0; no counterpart in the reference): number of
+ * complex elements, [omega][q_ibz][upper-pair blocks] in the order of librpa_gb300_get_chi0_block;
+ * copy out to, or replace from, interleaved (re, im) doubles on the host (on_device = 0) or
+ * the current device (on_device = 1).  Used to all-reduce tau-shard partial sums. */
+long long librpa_gb300_chi0_qw_elems(LibrpaHandler *h);
+int librpa_gb300_copy_chi0_qw(LibrpaHandler *h, double *dst, int on_device);
+int librpa_gb300_load_chi0_qw(LibrpaHandler *h, const double *src, long long n_elems, int on_device);
 
 /* Learned screening (no counterpart in the reference).  The model is a 5-64-64-1 GELU MLP
  * (FP16 weights, FP32 accumulation) predicting log10 max |chi0(I,J,R,tau)| from the block's

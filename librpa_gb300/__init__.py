@@ -29,7 +29,7 @@ CHI0_FP64, CHI0_BF16X3, CHI0_FP32 = 0, 1, 2
 EC_LU_FP64, EC_CHOL = 0, 1
 SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
 MLP_NPARAM, MLP_NNORM = 4609, 13
-SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
+STAGE_FULL, STAGE_CHI0, STAGE_EC = 0, 1, 2
 
 
 class LibrpaOptions(C.Structure):
@@ -94,7 +94,7 @@ class GB300Options(C.Structure):
         ("use_cuda_graph", C.c_int),
         ("keep_chi0", C.c_int),
         ("device", C.c_int),
-        ("reuse_device_inputs", C.c_int),
+        ("reuse_device_inputs", C.c_int), ("tau_begin", C.c_int), ("tau_end", C.c_int), ("stage", C.c_int),
     ]
 
 
@@ -134,7 +134,8 @@ EXPORTS = [
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_get_screening_model", "librpa_gb300_set_screening_model",
-    "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad",
+    "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
+    "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw",
 ]
 
 _lib = None
@@ -193,6 +194,9 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_get_screening_model": (i, [vp, vp, vp]),
         "librpa_gb300_set_screening_model": (i, [vp, vp, vp]),
         "librpa_gb300_clear_screening": (None, [vp]),
+        "librpa_gb300_chi0_qw_elems": (C.c_longlong, [vp]),
+        "librpa_gb300_copy_chi0_qw": (i, [vp, vp, i]),
+        "librpa_gb300_load_chi0_qw": (i, [vp, vp, C.c_longlong, i]),
         "librpa_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, i, vp, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -332,6 +336,22 @@ class Handler:
     def set_gb300_options(self, o: GB300Options):
         self.lib.librpa_gb300_set_options(self.h, C.byref(o))
         self._check()
+
+    def chi0_qw(self) -> np.ndarray:
+        """Copy of the kept chi0(q, omega) (complex128, [omega][q][pair blocks], flattened)."""
+        n = self.lib.librpa_gb300_chi0_qw_elems(self.h)
+        if n <= 0:
+            raise LibrpaError(self.last_error() or "no chi0(q, omega) kept")
+        out = np.zeros(n, np.complex128)
+        if self.lib.librpa_gb300_copy_chi0_qw(self.h, out.ctypes.data_as(C.c_void_p), 0) != 0:
+            raise LibrpaError(self.last_error())
+        return out
+
+    def load_chi0_qw(self, a: np.ndarray):
+        """Replace the kept chi0(q, omega) (e.g. with a sum of tau-shard partials)."""
+        a = np.ascontiguousarray(a, np.complex128)
+        if self.lib.librpa_gb300_load_chi0_qw(self.h, a.ctypes.data_as(C.c_void_p), a.size, 0) != 0:
+            raise LibrpaError(self.last_error())
 
     def stats(self) -> dict:
         s = GB300Stats()

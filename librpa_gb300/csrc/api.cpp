@@ -771,6 +771,9 @@ void librpa_gb300_init_options(LibrpaGB300Options *o)
     o->seed = 12345ULL;
     o->use_cuda_graph = 1;
     o->keep_chi0 = 0;
+    o->tau_begin = 0;
+    o->tau_end = -1;
+    o->stage = LIBRPA_GB300_STAGE_FULL;
     o->device = 0;
     o->reuse_device_inputs = 1;
 }
@@ -876,6 +879,46 @@ double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces)
         r = gb::tc_gemm_selftest(M, N, K, seed, pieces);
     });
     return r;
+}
+
+// ---- kept chi0(q, omega) for tau-shard reductions; no counterpart in the reference
+long long librpa_gb300_chi0_qw_elems(LibrpaHandler *h)
+{
+    long long n = -1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        n = ds->kept_chi0 ? static_cast<long long>(ds->kept_chi0_bytes / sizeof(cplx)) : 0;
+    });
+    return n;
+}
+
+int librpa_gb300_copy_chi0_qw(LibrpaHandler *h, double *dst, int on_device)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ds->kept_chi0, "no chi0(q, omega) kept: run with keep_chi0 = 1 or stage = STAGE_CHI0");
+        GB_REQUIRE(dst, "null destination");
+        GB_CUDA(cudaMemcpy(dst, ds->kept_chi0, ds->kept_chi0_bytes,
+                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost));
+        rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_load_chi0_qw(LibrpaHandler *h, const double *src, long long n_elems, int on_device)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ds->kept_chi0, "no chi0(q, omega) layout kept: run a STAGE_CHI0 call first");
+        GB_REQUIRE(src && n_elems == static_cast<long long>(ds->kept_chi0_bytes / sizeof(cplx)),
+                   "chi0(q, omega) size differs from the kept layout");
+        GB_CUDA(cudaMemcpy(ds->kept_chi0, src, ds->kept_chi0_bytes,
+                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+        rc = 0;
+    });
+    return rc;
 }
 
 // ---- learned screening (screen.cu); no counterpart in the reference

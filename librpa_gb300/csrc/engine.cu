@@ -486,7 +486,18 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     S.dt_chi0_kernel_ms = 0.0;
     S.n_chi0_kernel = 0;
     const double fac = 2.0 / ns;
-    for (int it = 0; it < nw; ++it)
+    // tau slice and stage (tau sharding: partial chi0(q, omega) sums are reduced across ranks)
+    const int tb = std::max(0, go.tau_begin), te = go.tau_end < 0 ? nw : std::min(go.tau_end, nw);
+    GB_REQUIRE(go.stage >= LIBRPA_GB300_STAGE_FULL && go.stage <= LIBRPA_GB300_STAGE_EC, "unknown stage");
+    GB_REQUIRE(tb <= te, "tau_begin > tau_end");
+    const bool do_chi0 = go.stage != LIBRPA_GB300_STAGE_EC;
+    if (!do_chi0)
+    {
+        GB_REQUIRE(ds.kept_chi0 && ds.kept_chi0_bytes == d_chi0q.bytes(),
+                   "STAGE_EC needs the chi0(q, omega) of a STAGE_CHI0 call on the same data (librpa_gb300_load_chi0_qw)");
+        GB_CUDA(cudaMemcpyAsync(d_chi0q.get(), ds.kept_chi0, ds.kept_chi0_bytes, cudaMemcpyDeviceToDevice, st));
+    }
+    for (int it = do_chi0 ? tb : te; it < te; ++it)
     {
         const double tau = tf.tau[it];
         std::vector<double> gam(nw);
@@ -632,8 +643,8 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 lib += nc * (2.0 * bJ * aJ * aI * n_sup + 2.0 * aJ * aI * bI * n_sup + 2.0 * bI * bJ * aJ * aI);
             }
         }
-        flops_chi = per * nw * ns;
-        flops_libri = 2.0 * lib * nw * ns;
+        flops_chi = per * (do_chi0 ? te - tb : 0) * ns;
+        flops_libri = 2.0 * lib * (do_chi0 ? te - tb : 0) * ns;
     }
     {
         int herr = 0;
@@ -646,11 +657,32 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     S.t_ftct = t_ft * 1e-3;
     S.chi0_flops = flops_chi;
     S.chi0_flops_libri = flops_libri;
-    S.gf_flops = static_cast<double>(nw) * ns * 2.0 * (8.0 * nk * nao * nao * nb + 4.0 * nc * nk * nao * nao);
-    S.ftct_bytes = static_cast<double>(nw) * ns * (8.0 * r_tot + 2.0 * 16.0 * nw * nq * e_tot);
+    S.gf_flops = static_cast<double>(do_chi0 ? te - tb : 0) * ns * 2.0 * (8.0 * nk * nao * nao * nb + 4.0 * nc * nk * nao * nao);
+    S.ftct_bytes = static_cast<double>(do_chi0 ? te - tb : 0) * ns * (8.0 * r_tot + 2.0 * 16.0 * nw * nq * e_tot);
     d_X.release();
     d_Gs.release();
     fast.reset();
+
+    if (go.stage == LIBRPA_GB300_STAGE_CHI0)
+    {
+        // keep the partial chi0(q, w) and stop before E_c
+        release_kept(ds);
+        ds.kept_chi0_bytes = d_chi0q.bytes();
+        GB_CUDA(cudaMalloc(&ds.kept_chi0, ds.kept_chi0_bytes));
+        GB_CUDA(cudaMemcpyAsync(ds.kept_chi0, d_chi0q.get(), ds.kept_chi0_bytes, cudaMemcpyDeviceToDevice, st));
+        ds.kept_pair_offset.assign(e_off.begin(), e_off.end());
+        ds.kept_pair_elems = static_cast<size_t>(e_tot);
+        ds.kept_nfreq = nw;
+        ds.kept_nq = nq;
+        GB_CUDA(cudaStreamSynchronize(st));
+        S.n_launches = launches;
+        S.blocks_total = static_cast<long long>(n_blk) * (te - tb) * ns;
+        S.blocks_computed = smode == LIBRPA_GB300_SCREEN_OFF ? S.blocks_total : blk_computed;
+        S.t_total = wall_seconds() - t_begin;
+        RpaResult part;
+        part.per_q.assign(nq, cplx(0, 0));
+        return part;
+    }
 
     // ------------------------------------------------------------ E_c
     EventTimer ev_ec;
@@ -764,9 +796,9 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     S.ec_flops = ec_flops;
     for (const cplx &v : res.per_q) res.ec += v;
 
-    // keep chi0(q, w) for inspection
-    release_kept(ds);
-    if (go.keep_chi0)
+    // keep chi0(q, w) for inspection (a STAGE_EC call keeps the loaded one)
+    if (go.stage == LIBRPA_GB300_STAGE_FULL) release_kept(ds);
+    if (go.keep_chi0 && go.stage == LIBRPA_GB300_STAGE_FULL)
     {
         ds.kept_chi0_bytes = d_chi0q.bytes();
         GB_CUDA(cudaMalloc(&ds.kept_chi0, ds.kept_chi0_bytes));
@@ -779,7 +811,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     GB_CUDA(cudaStreamSynchronize(st));
     S.n_launches = launches;
     S.d2h_bytes = 16.0 * 2 * nw * nq;
-    S.blocks_total = static_cast<long long>(n_blk) * nw * ns;
+    S.blocks_total = static_cast<long long>(n_blk) * (do_chi0 ? te - tb : 0) * ns;
     S.blocks_computed = smode == LIBRPA_GB300_SCREEN_OFF ? S.blocks_total : blk_computed;
     S.blocks_audited = blk_audited;
     S.audit_max_dropped = audit_max;

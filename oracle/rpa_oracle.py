@@ -476,6 +476,33 @@ def correlation_energy(chi0q, inp: RPAInput, grid, ibz_order, ibz_weight, opts: 
 
 # ----------------------------------------------------------------------------- driver
 
+def chi0q_partial(inp: RPAInput, opts: Options, tau_begin: int, tau_end: int):
+    """chi0(q, omega) summed over the minimax tau points [tau_begin, tau_end) only (a tau shard)."""
+    grid = grids_for(inp, opts)
+    klist, kfrac, ibz_order, ibz_weight = k_lists(inp)
+    rlist = r_grid(inp.period)
+    klist_ibz = [klist[i] for i in ibz_order]
+    pairs = upper_pairs(inp.n_atoms)
+    C = cs_tensors(inp, opts.libri_chi0_threshold_C)
+    chi0q = [[{p: np.zeros((inp.nabf[p[0]], inp.nabf[p[1]]), complex) for p in pairs}
+              for _ in ibz_order] for _ in range(opts.nfreq)]
+    for it in range(tau_begin, tau_end):
+        tau = grid["tau"][it]
+        for s in range(inp.n_spins):
+            Gp = blocks_of(build_gf(inp, s, tau, kfrac, rlist, opts.n_bands_chi0), inp.nao)
+            Gn = blocks_of(build_gf(inp, s, -tau, kfrac, rlist, opts.n_bands_chi0), inp.nao)
+            chi0s = cal_chi0s_dense(C, Gp, Gn, inp.nao, inp.nabf, inp.period)
+            ft_ct_accumulate(chi0q, chi0s, it, grid, klist_ibz, inp.latvec, inp.n_spins, pairs)
+    return chi0q
+
+
+def ec_from_chi0q(inp: RPAInput, opts: Options, chi0q):
+    """E_c (correlation_energy) from a given chi0(q, omega)."""
+    grid = grids_for(inp, opts)
+    _, _, ibz_order, ibz_weight = k_lists(inp)
+    return correlation_energy(chi0q, inp, grid, ibz_order, ibz_weight, opts)
+
+
 def rpa_correlation_energy(inp: RPAInput, opts: Options | None = None, chi0_impl: str = "dense",
                            keep_chi0s: bool = False, block_threshold: float | None = None):
     """Full oracle pipeline; returns a dict with E_c and intermediates."""

@@ -1,0 +1,105 @@
+"""Tau sharding across ranks on CPU: the slice partition, and the sharded E_c with
+two gloo ranks.  The per-rank compute is the oracle standing in for a GPU; what is tested is
+the partition, the stage sequence and the all-reduce of tau_shard.sharded_correlation_energy."""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+import librpa_gb300 as L
+from librpa_gb300 import synthetic as sy
+from librpa_gb300.tau_shard import sharded_correlation_energy, tau_slices
+
+
+@pytest.mark.parametrize("n_tau,world", [(16, 1), (16, 2), (16, 3), (24, 5), (3, 4), (0, 2), (32, 8)])
+def test_tau_slices_partition(n_tau, world):
+    sl = tau_slices(n_tau, world)
+    assert len(sl) == world
+    covered = [t for b, e in sl for t in range(b, e)]
+    assert covered == list(range(n_tau))
+    sizes = [e - b for b, e in sl]
+    assert max(sizes) - min(sizes) <= 1
+
+
+def _system():
+    return sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=(2, 1, 1), nocc=2, seed=9)
+
+
+class OracleHandler:
+    """The Handler calls the sharding uses, computed by the oracle (tests only)."""
+
+    def __init__(self, s):
+        from conftest import oracle_input
+        from oracle.rpa_oracle import Options
+        self.inp = oracle_input(s)
+        self.oopts = Options(nfreq=s.nfreq, minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
+        self.go = None
+        self.kept = None
+        self.shape = None
+
+    def set_gb300_options(self, go):
+        self.go = go
+
+    def get_rpa_correlation_energy(self, opts, n_ibz):
+        from oracle.rpa_oracle import chi0q_partial, ec_from_chi0q
+        if self.go.stage == L.STAGE_CHI0:
+            chi0q = chi0q_partial(self.inp, self.oopts, self.go.tau_begin, self.go.tau_end)
+            self.shape = [[{k: v.shape for k, v in d.items()} for d in row] for row in chi0q]
+            self.kept = np.concatenate([v.ravel() for row in chi0q for d in row for v in d.values()])
+            return 0.0, np.zeros(n_ibz, complex)
+        assert self.go.stage == L.STAGE_EC
+        chi0q, off = [], 0
+        for row in self.shape:
+            out_row = []
+            for d in row:
+                blk = {}
+                for k, shp in d.items():
+                    n = shp[0] * shp[1]
+                    blk[k] = self.kept[off:off + n].reshape(shp)
+                    off += n
+                out_row.append(blk)
+            chi0q.append(out_row)
+        ec, per_q, _ = ec_from_chi0q(self.inp, self.oopts, chi0q)
+        return ec.real, np.asarray(per_q)
+
+    def chi0_qw(self):
+        return self.kept.copy()
+
+    def load_chi0_qw(self, a):
+        self.kept = np.array(a, np.complex128)
+
+
+def _rank_main(rank, world, port, out_dir):
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    import torch.distributed as dist
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        s = _system()
+        h = OracleHandler(s)
+        opts = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI)
+        ec, _ = sharded_correlation_energy(h, opts, L.n_ibz(s))
+        np.save(os.path.join(out_dir, f"ec{rank}.npy"), np.array([ec]))
+    finally:
+        dist.destroy_process_group()
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_gloo_two_ranks_sharded_ec_matches_unsharded(tmp_path, lib):
+    import torch.multiprocessing as mp
+    world = 2
+    mp.start_processes(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    from conftest import oracle_input
+    from oracle.rpa_oracle import Options, rpa_correlation_energy
+    s = _system()
+    ref = rpa_correlation_energy(oracle_input(s), Options(nfreq=s.nfreq, minimax_emin=s.minimax_emin,
+                                                          minimax_emax=s.minimax_emax))["ec"].real
+    ecs = [float(np.load(tmp_path / f"ec{r}.npy")[0]) for r in range(world)]
+    assert ecs[0] == ecs[1]  # every rank ends with the same reduced chi0 and E_c
+    assert abs(ecs[0] - ref) <= 1e-12 * abs(ref)
