@@ -147,19 +147,20 @@ __global__ void k_form_mprime_r(const float *__restrict__ Ms, int N, double *__r
 }
 
 // tr(V X[b]) = sum_ij V_ij X_ji (full matrices), FP64, one CTA per batch entry
-__global__ void k_trace_prod_c(const cuDoubleComplex *__restrict__ V, const cuDoubleComplex *__restrict__ X, int N,
-                               cuDoubleComplex *__restrict__ out)
+unsigned blocks_for(long long n) { return static_cast<unsigned>(std::min<long long>((n + 255) / 256, 152LL * 16)); }
+
+
+// tr(M) per frequency from the FP32 products M = L^H chi0 L (diagonal of the Re / Im blocks)
+__global__ void k_diag_trace(const float *__restrict__ Ms, int N, int parts, double2 *__restrict__ tr)
 {
     __shared__ double rr[256], ri[256];
     const long long nn = static_cast<long long>(N) * N;
-    const cuDoubleComplex *Xb = X + blockIdx.x * nn;
+    const float *S = Ms + static_cast<long long>(blockIdx.x) * parts * nn;
     double ar = 0.0, ai = 0.0;
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x)
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
     {
-        const long long i = e / N, j = e % N;
-        const cuDoubleComplex v = V[e], x = Xb[j * N + i];
-        ar += v.x * x.x - v.y * x.y;
-        ai += v.x * x.y + v.y * x.x;
+        ar += S[static_cast<long long>(i) * N + i];
+        if (parts > 1) ai += S[nn + static_cast<long long>(i) * N + i];
     }
     rr[threadIdx.x] = ar;
     ri[threadIdx.x] = ai;
@@ -173,131 +174,121 @@ __global__ void k_trace_prod_c(const cuDoubleComplex *__restrict__ V, const cuDo
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[blockIdx.x] = make_cuDoubleComplex(rr[0], ri[0]);
+    if (threadIdx.x == 0) tr[blockIdx.x] = make_double2(rr[0], ri[0]);
 }
-
-__global__ void k_trace_prod_r(const double *__restrict__ V, const double *__restrict__ X, int N,
-                               double *__restrict__ out)
-{
-    __shared__ double rr[256];
-    const long long nn = static_cast<long long>(N) * N;
-    const double *Xb = X + blockIdx.x * nn;
-    double a = 0.0;
-    for (long long e = threadIdx.x; e < nn; e += blockDim.x)
-    {
-        const long long i = e / N, j = e % N;
-        a += V[e] * Xb[j * N + i];
-    }
-    rr[threadIdx.x] = a;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1)
-    {
-        if (threadIdx.x < s) rr[threadIdx.x] += rr[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) out[blockIdx.x] = rr[0];
-}
-
-unsigned blocks_for(long long n) { return static_cast<unsigned>(std::min<long long>((n + 255) / 256, 152LL * 16)); }
 
 } // namespace
 
 struct EcChol::Impl
 {
-    int N = 0, nw = 0;
+    int N = 0, nw = 0, qb = 1;
     bool cplx = true;
     long long kpad = 0;
-    DevBuf<int> err, bad;
-    // per-q
-    SplitStore Bl, Al;            // L as B^T and L^H (or L^T) as A
+    DevBuf<int> err, bad, badV;
+    SplitStore Bl, Al;            // L as B^T and L^H (or L^T) as A, one q at a time
     DevBuf<double> diagV;
-    // per-(q, w) batch
-    SplitStore A1, B2;
+    SplitStore A1, B2;            // per-(q, w) operands, one q at a time
     DevBuf<float> Tst, Mst;
-    DevBuf<double> diag, logdet;
-    DevBuf<cuDoubleComplex> Mpc, trc;
-    DevBuf<double> Mpr, trr;
+    DevBuf<double> diag, logdet;  // qb * nw matrices
+    DevBuf<double2> tr;
+    DevBuf<cuDoubleComplex> Mpc;
+    DevBuf<double> Mpr;
 };
 
-EcChol::EcChol(int N, int nw, bool complex_path) : impl_(std::make_unique<Impl>())
+EcChol::EcChol(int N, int nw, bool complex_path, int qb) : impl_(std::make_unique<Impl>())
 {
     Impl &m = *impl_;
     m.N = N;
     m.nw = nw;
+    m.qb = qb;
     m.cplx = complex_path;
     const int kdim = complex_path ? 2 * N : N;
     m.kpad = (kdim + 63) / 64 * 64;
     const long long rowsA = kdim;  // rows of the A operands
+    const size_t nmat = static_cast<size_t>(qb) * nw;
     m.err.alloc(1);
-    m.bad.alloc(nw);
+    m.bad.alloc(nmat);
+    m.badV.alloc(qb);
     m.Bl.alloc(3, static_cast<size_t>(N) * m.kpad);
     m.Al.alloc(3, static_cast<size_t>(rowsA) * m.kpad);
-    m.diagV.alloc(N);
+    m.diagV.alloc(static_cast<size_t>(qb) * N);
     m.A1.alloc(3, static_cast<size_t>(nw) * rowsA * m.kpad);
     m.B2.alloc(3, static_cast<size_t>(nw) * N * m.kpad);
     m.Tst.alloc(static_cast<size_t>(nw) * rowsA * N);
     m.Mst.alloc(static_cast<size_t>(nw) * rowsA * N);
-    m.diag.alloc(static_cast<size_t>(nw) * N);
-    m.logdet.alloc(nw);
+    m.diag.alloc(nmat * N);
+    m.logdet.alloc(nmat);
+    m.tr.alloc(nmat);
     if (complex_path)
-    {
-        m.Mpc.alloc(static_cast<size_t>(nw) * N * N);
-        m.trc.alloc(nw);
-    }
+        m.Mpc.alloc(nmat * N * N);
     else
-    {
-        m.Mpr.alloc(static_cast<size_t>(nw) * N * N);
-        m.trr.alloc(nw);
-    }
+        m.Mpr.alloc(nmat * N * N);
 }
 
 EcChol::~EcChol() = default;
 
-int EcChol::run_q(void *V, void *X, std::vector<std::complex<double>> &trace_out,
-                  std::vector<std::complex<double>> &logdet_out, cudaStream_t st)
+int EcChol::factor_v(void *V, int nb, cudaStream_t st)
+{
+    Impl &m = *impl_;
+    GB_REQUIRE(nb >= 1 && nb <= m.qb, "Coulomb batch larger than the E_c batch");
+    m.badV.zero(st);
+    int launches = 1;
+    if (m.cplx)
+    {
+        launches += chol_batched_c(static_cast<cuDoubleComplex *>(V), m.N, nb, m.diagV.get(), m.badV.get(), st);
+        zero_upper_c(static_cast<cuDoubleComplex *>(V), m.N, nb, st);
+    }
+    else
+    {
+        launches += chol_batched_r(static_cast<double *>(V), m.N, nb, m.diagV.get(), m.badV.get(), st);
+        zero_upper_r(static_cast<double *>(V), m.N, nb, st);
+    }
+    std::vector<int> bad(nb);
+    m.badV.download(bad.data(), nb, st);
+    GB_CUDA(cudaStreamSynchronize(st));
+    for (int b = 0; b < nb; ++b) GB_REQUIRE(!bad[b], "V(q) is not positive definite: no Cholesky factor");
+    return launches;
+}
+
+int EcChol::stage_q(const void *L, const void *X, int slot, cudaStream_t st)
 {
     Impl &m = *impl_;
     const int N = m.N, nw = m.nw;
+    GB_REQUIRE(slot >= 0 && slot < m.qb, "E_c batch slot out of range");
     const long long nn = static_cast<long long>(N) * N;
     int launches = 0;
-    m.err.zero(st);
-    m.bad.zero(st);
+    if (slot == 0)
+    {
+        m.err.zero(st);
+        m.bad.zero(st);
+    }
     const SplitBufs bl = m.Bl.bufs(), al = m.Al.bufs(), a1 = m.A1.bufs(), b2 = m.B2.bufs();
     const long long rowsA = m.cplx ? 2LL * N : N;
     if (m.cplx)
     {
-        cuDoubleComplex *Vc = static_cast<cuDoubleComplex *>(V);
-        cuDoubleComplex *Xc = static_cast<cuDoubleComplex *>(X);
-        k_trace_prod_c<<<nw, 256, 0, st>>>(Vc, Xc, N, m.trc.get());
-        GB_LAUNCH_CHECK();
-        // V = L L^H (V is overwritten by L)
-        launches += chol_batched_c(Vc, N, 1, m.diagV.get(), m.bad.get(), st);
-        zero_upper_c(Vc, N, 1, st);
-        k_embed_Bt<<<blocks_for(N * m.kpad), 256, 0, st>>>(Vc, N, N, static_cast<int>(m.kpad), bl.p[0], bl.p[1], bl.p[2]);
-        k_embed_A<<<dim3(blocks_for(rowsA * m.kpad), 1), 256, 0, st>>>(Vc, 0, N, N, static_cast<int>(m.kpad), true,
+        const cuDoubleComplex *Lc = static_cast<const cuDoubleComplex *>(L);
+        const cuDoubleComplex *Xc = static_cast<const cuDoubleComplex *>(X);
+        k_embed_Bt<<<blocks_for(N * m.kpad), 256, 0, st>>>(Lc, N, N, static_cast<int>(m.kpad), bl.p[0], bl.p[1], bl.p[2]);
+        k_embed_A<<<dim3(blocks_for(rowsA * m.kpad), 1), 256, 0, st>>>(Lc, 0, N, N, static_cast<int>(m.kpad), true,
                                                                         al.p[0], al.p[1], al.p[2], 0);
         k_embed_A<<<dim3(blocks_for(rowsA * m.kpad), nw), 256, 0, st>>>(Xc, nn, N, N, static_cast<int>(m.kpad), false,
                                                                          a1.p[0], a1.p[1], a1.p[2], rowsA * m.kpad);
         GB_LAUNCH_CHECK();
-        launches += 5;
+        launches += 3;
     }
     else
     {
-        double *Vr = static_cast<double *>(V);
-        double *Xr = static_cast<double *>(X);
-        k_trace_prod_r<<<nw, 256, 0, st>>>(Vr, Xr, N, m.trr.get());
-        GB_LAUNCH_CHECK();
-        launches += chol_batched_r(Vr, N, 1, m.diagV.get(), m.bad.get(), st);
-        zero_upper_r(Vr, N, 1, st);
+        const double *Lr = static_cast<const double *>(L);
+        const double *Xr = static_cast<const double *>(X);
         // B^T of L and A = L^T are the same K-major matrix: row n = L(:, n)
-        split_transpose_f64(Vr, N, N, N, static_cast<int>(m.kpad), bl, st);
-        split_transpose_f64(Vr, N, N, N, static_cast<int>(m.kpad), al, st);
+        split_transpose_f64(Lr, N, N, N, static_cast<int>(m.kpad), bl, st);
+        split_transpose_f64(Lr, N, N, N, static_cast<int>(m.kpad), al, st);
         for (int w = 0; w < nw; ++w)
         {
             SplitBufs aw{3, {a1.p[0] + w * rowsA * m.kpad, a1.p[1] + w * rowsA * m.kpad, a1.p[2] + w * rowsA * m.kpad}};
             split_rows_f64(Xr + w * nn, N, N, N, static_cast<int>(m.kpad), aw, st);
         }
-        launches += 4 + nw;
+        launches += 2 + nw;
     }
     // T = chi0 L  (rowsA x N per w)
     tc_gemm_split(m.A1.mat(rowsA, m.kpad, rowsA * m.kpad), m.Bl.mat(N, m.kpad, 0), static_cast<int>(rowsA), N,
@@ -309,50 +300,54 @@ int EcChol::run_q(void *V, void *X, std::vector<std::complex<double>> &trace_out
                                                  static_cast<int>(m.kpad), b2.p[0], b2.p[1], b2.p[2], N * m.kpad);
         GB_LAUNCH_CHECK();
     }
-    // L^H T
+    // M = L^H T
     tc_gemm_split(m.Al.mat(rowsA, m.kpad, 0), m.B2.mat(N, m.kpad, N * m.kpad), static_cast<int>(rowsA), N,
                   static_cast<int>(m.cplx ? 2 * N : N), nw, m.Mst.get(), N, rowsA * N, false, m.err.get(), st);
-    launches += 3;
+    // tr(V chi0) = tr(L^H chi0 L) from the same products as M': to first order the FP32
+    // rounding of M cancels between ln det(I - M) and tr(M)
+    k_diag_trace<<<nw, 256, 0, st>>>(m.Mst.get(), N, m.cplx ? 2 : 1, m.tr.get() + static_cast<size_t>(slot) * nw);
+    GB_LAUNCH_CHECK();
+    const size_t off = static_cast<size_t>(slot) * nw * nn;
     if (m.cplx)
-    {
-        k_form_mprime_c<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpc.get());
-        GB_LAUNCH_CHECK();
-        launches += 1 + chol_batched_c(m.Mpc.get(), N, nw, m.diag.get(), m.bad.get(), st);
-    }
+        k_form_mprime_c<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpc.get() + off);
     else
-    {
-        k_form_mprime_r<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpr.get());
-        GB_LAUNCH_CHECK();
-        launches += 1 + chol_batched_r(m.Mpr.get(), N, nw, m.diag.get(), m.bad.get(), st);
-    }
-    chol_logdet(m.diag.get(), N, nw, m.logdet.get(), st);
-    ++launches;
-    std::vector<double> ld(nw);
-    std::vector<int> bad(nw);
+        k_form_mprime_r<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpr.get() + off);
+    GB_LAUNCH_CHECK();
+    return launches + 5;
+}
+
+int EcChol::finish(int nslots, std::vector<std::complex<double>> &trace_out,
+                   std::vector<std::complex<double>> &logdet_out, cudaStream_t st)
+{
+    Impl &m = *impl_;
+    const int N = m.N;
+    GB_REQUIRE(nslots >= 1 && nslots <= m.qb, "E_c batch slot count out of range");
+    const int nmat = nslots * m.nw;
+    int launches = 1;
+    if (m.cplx)
+        launches += chol_batched_c(m.Mpc.get(), N, nmat, m.diag.get(), m.bad.get(), st);
+    else
+        launches += chol_batched_r(m.Mpr.get(), N, nmat, m.diag.get(), m.bad.get(), st);
+    chol_logdet(m.diag.get(), N, nmat, m.logdet.get(), st);
+    std::vector<double> ld(nmat);
+    std::vector<int> bad(nmat);
+    std::vector<double2> tr(nmat);
     int herr = 0;
-    m.logdet.download(ld.data(), nw, st);
-    m.bad.download(bad.data(), nw, st);
+    m.logdet.download(ld.data(), nmat, st);
+    m.bad.download(bad.data(), nmat, st);
+    m.tr.download(tr.data(), nmat, st);
     m.err.download(&herr, 1, st);
-    trace_out.assign(nw, {0.0, 0.0});
-    if (m.cplx)
-    {
-        std::vector<cuDoubleComplex> tr(nw);
-        m.trc.download(tr.data(), nw, st);
-        GB_CUDA(cudaStreamSynchronize(st));
-        for (int w = 0; w < nw; ++w) trace_out[w] = {tr[w].x, tr[w].y};
-    }
-    else
-    {
-        std::vector<double> tr(nw);
-        m.trr.download(tr.data(), nw, st);
-        GB_CUDA(cudaStreamSynchronize(st));
-        for (int w = 0; w < nw; ++w) trace_out[w] = {tr[w], 0.0};
-    }
+    GB_CUDA(cudaStreamSynchronize(st));
     GB_REQUIRE(herr == 0, "tensor-core E_c GEMM reported wait timeout code " + std::to_string(herr));
-    for (int w = 0; w < nw; ++w)
-        GB_REQUIRE(!bad[w], "I - L^H chi0 L is not positive definite (chi0 not negative semidefinite?)");
-    logdet_out.assign(nw, {0.0, 0.0});
-    for (int w = 0; w < nw; ++w) logdet_out[w] = {ld[w], 0.0};
+    for (int b = 0; b < nmat; ++b)
+        GB_REQUIRE(!bad[b], "I - L^H chi0 L is not positive definite (chi0 not negative semidefinite?)");
+    trace_out.assign(nmat, {0.0, 0.0});
+    logdet_out.assign(nmat, {0.0, 0.0});
+    for (int b = 0; b < nmat; ++b)
+    {
+        trace_out[b] = {tr[b].x, m.cplx ? tr[b].y : 0.0};
+        logdet_out[b] = {ld[b], 0.0};
+    }
     return launches;
 }
 

@@ -12,14 +12,20 @@ namespace gb {
 class EcChol
 {
 public:
-    // N: auxiliary-basis size; nw: frequencies handled per call; complex_path: k-point (complex)
-    // matrices, otherwise Gamma-only real parts.
-    EcChol(int N, int nw, bool complex_path);
+    // N: auxiliary-basis size; nw: frequencies per q; complex_path: k-point (complex) matrices,
+    // otherwise Gamma-only real parts; qb: q points whose M' = I - L^H chi0 L are factorised
+    // in one batch.
+    EcChol(int N, int nw, bool complex_path, int qb);
     ~EcChol();
-    // V: full N x N Coulomb matrix of one q (overwritten by its Cholesky factor); X: nw full
-    // chi0(q, w) matrices.  Returns tr(V chi0) and ln det(I - V chi0) per frequency.
-    int run_q(void *V, void *X, std::vector<std::complex<double>> &trace, std::vector<std::complex<double>> &logdet,
-              cudaStream_t st);
+    // V = L L^H in place for nb (<= qb) Coulomb matrices stored one after another (N x N each).
+    int factor_v(void *V, int nb, cudaStream_t st);
+    // For batch slot `slot`: M = L^H chi0 L for the nw chi0 matrices X (tensor-core GEMMs),
+    // M' = I - M kept for finish(), and tr(V chi0) = tr(M) per frequency.
+    int stage_q(const void *L, const void *X, int slot, cudaStream_t st);
+    // Batched FP64 Cholesky of the nslots * nw matrices M'; trace[s * nw + w] = tr(V chi0) and
+    // logdet[s * nw + w] = ln det(I - V chi0) = 2 sum_i ln L'_ii.
+    int finish(int nslots, std::vector<std::complex<double>> &trace, std::vector<std::complex<double>> &logdet,
+               cudaStream_t st);
 
     struct Impl;
 

@@ -693,9 +693,70 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     const long long NN = static_cast<long long>(N) * N;
     double ec_flops = 0.0;
     const bool use_chol = go.ec_path == LIBRPA_GB300_EC_CHOL;
-    std::unique_ptr<EcChol> ecc;
-    if (use_chol) ecc = std::make_unique<EcChol>(N, nw, !gamma_only);
-    for (int q = 0; q < nq; ++q)
+    // V(q) from the blocks of this q inside the staged Coulomb blob
+    auto assemble_v = [&](int q, void *V) {
+        std::vector<long long> voff;
+        std::vector<int> vIJ;
+        for (int bi : vq_of_q[q])
+        {
+            const VqBlock &b = ds.vq_blocks[bi];
+            GB_REQUIRE(b.nmu == ds.nabf_at[b.I] && b.nnu == ds.nabf_at[b.J], "Coulomb block dimensions inconsistent");
+            voff.push_back(static_cast<long long>(b.offset));
+            vIJ.push_back(b.I);
+            vIJ.push_back(b.J);
+        }
+        auto d_voff = to_dev(voff, st);
+        auto d_vIJ = to_dev(vIJ, st);
+        if (gamma_only)
+        {
+            GB_CUDA(cudaMemsetAsync(V, 0, sizeof(double) * NN, st));
+            launch_assemble_v(din->vblob.get(), d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
+                              d_nabf.get(), N, true, nullptr, static_cast<double *>(V), st);
+        }
+        else
+        {
+            GB_CUDA(cudaMemsetAsync(V, 0, sizeof(cuDoubleComplex) * NN, st));
+            launch_assemble_v(din->vblob.get(), d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
+                              d_nabf.get(), N, false, static_cast<cuDoubleComplex *>(V), nullptr, st);
+        }
+        GB_CUDA(cudaStreamSynchronize(st));  // the block tables go out of scope
+        ++launches;
+    };
+    if (use_chol)
+    {
+        // every q's V = L L^H in one batched factorisation, M' = I - L^H chi0 L per q on the tensor
+        // cores, then one batched FP64 Cholesky of all the M'; q points go in batches that keep
+        // the M' store within about 24 GB
+        const size_t esz = gamma_only ? sizeof(double) : sizeof(cuDoubleComplex);
+        const double per_q = static_cast<double>(nw + 1) * NN * esz;
+        const int qb = std::max(1, std::min(nq, static_cast<int>(24.0e9 / per_q)));
+        EcChol ecc(N, nw, !gamma_only, qb);
+        DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
+        for (int q0 = 0; q0 < nq; q0 += qb)
+        {
+            const int nb = std::min(qb, nq - q0);
+            for (int s = 0; s < nb; ++s) assemble_v(q0 + s, Vall.get() + static_cast<size_t>(s) * NN * esz);
+            launches += ecc.factor_v(Vall.get(), nb, st);
+            for (int s = 0; s < nb; ++s)
+            {
+                const int q = q0 + s;
+                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
+                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
+                                     d_eoff.get(), gamma_only,
+                                     gamma_only ? nullptr : reinterpret_cast<cuDoubleComplex *>(X.get()),
+                                     gamma_only ? reinterpret_cast<double *>(X.get()) : nullptr, NN, st);
+                launches += 1 + ecc.stage_q(Vall.get() + static_cast<size_t>(s) * NN * esz, X.get(), s, st);
+            }
+            std::vector<cplx> tr, ld;
+            launches += ecc.finish(nb, tr, ld, st);
+            for (int s = 0; s < nb; ++s)
+                for (int w = 0; w < nw; ++w)
+                    res.per_q[q0 + s] += (tr[s * nw + w] + ld[s * nw + w]) * tf.omega_w[w] * ibz_w[q0 + s] / (2.0 * M_PI);
+            ec_flops += nb * nw * (gamma_only ? (2.0 * 2.0 * N * N * N + N * static_cast<double>(N) * N / 3.0)
+                                              : (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0));
+        }
+    }
+    for (int q = 0; q < nq && !use_chol; ++q)
     {
         // V(q) full: blocks of this q inside the staged Coulomb blob
         std::vector<long long> voff;
@@ -711,37 +772,6 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         auto d_voff = to_dev(voff, st);
         auto d_vIJ = to_dev(vIJ, st);
         const cuDoubleComplex *vbase = din->vblob.get();
-        if (use_chol)
-        {
-            std::vector<cplx> tr, ld;
-            if (gamma_only)
-            {
-                DevBuf<double> V(NN), X(NN * nw);
-                V.zero(st);
-                launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
-                                  d_nabf.get(), N, true, nullptr, V.get(), st);
-                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
-                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
-                                     d_eoff.get(), true, nullptr, X.get(), NN, st);
-                launches += 2 + ecc->run_q(V.get(), X.get(), tr, ld, st);
-                ec_flops += nw * (2.0 * 2.0 * N * N * N + N * static_cast<double>(N) * N / 3.0);
-            }
-            else
-            {
-                DevBuf<cuDoubleComplex> V(NN), X(NN * nw);
-                V.zero(st);
-                launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
-                                  d_nabf.get(), N, false, V.get(), nullptr, st);
-                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
-                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
-                                     d_eoff.get(), false, X.get(), nullptr, NN, st);
-                launches += 2 + ecc->run_q(V.get(), X.get(), tr, ld, st);
-                ec_flops += nw * (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0);
-            }
-            for (int w = 0; w < nw; ++w)
-                res.per_q[q] += (tr[w] + ld[w]) * tf.omega_w[w] * ibz_w[q] / (2.0 * M_PI);
-            continue;
-        }
         std::vector<double> tr_h(gamma_only ? nw : 2 * nw), ld_h(gamma_only ? nw : 2 * nw);
         if (gamma_only)
         {

@@ -391,6 +391,8 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         const uint32_t bbytes = static_cast<uint32_t>(NT) * 64 * 2;  // one piece of a B tile
         const int sp = a.spec[J], zj = a.spec_idx[J];
         const long long ktot = maps.ktot[sp];
+        // C^J tiles stream through L2 once per tile: evict them first, keep the X^I rows
+        const uint64_t pol_b = l2_policy_evict_first();
         auto issue_tma = [&](int st) -> bool {
             const int s = st % nbs, rr = st / nbs;
             if (!mbar_wait(&bempty[s], (rr & 1) ^ 1))
@@ -408,7 +410,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
             mbar_arrive_expect_tx(&bfull[s], NS * bbytes);
 #pragma unroll
             for (int p = 0; p < NS; ++p)  // pieces stacked along N: rows [p NT, (p + 1) NT)
-                tma_load_3d(bst + p * bbytes, &maps.m[sp][p], x, 0, zj, &bfull[s]);
+                tma_load_3d_hint(bst + p * bbytes, &maps.m[sp][p], x, 0, zj, &bfull[s], pol_b);
             return true;
         };
         auto issue_mma = [&](int st) -> bool {
