@@ -271,8 +271,9 @@ def run_gb300(args, s, ws, rank, local, dist):
     if args.fp64_check != "off" and prec != 0:
         est = chi0_flops / args.steps / 1.0e12  # seconds at ~1 TFLOP/s FP64
         if args.fp64_check == "on" or est < args.fp64_budget_s:
-            # the plain FP64 GPU path: FP64 chi0 kernels and the reference-form FP64 LU E_c
-            h.set_gb300_options(L.gb300_options(chi0_precision=0, ec_path=L.EC_LU_FP64, device=local,
+            # the plain FP64 GPU path: FP64 chi0 kernels and the all-FP64 Cholesky-form E_c (FP64
+            # GEMMs for L^H chi0 L, batched FP64 Cholesky)
+            h.set_gb300_options(L.gb300_options(chi0_precision=0, ec_path=L.EC_CHOL_FP64, device=local,
                                                 reuse_device_inputs=1))
             t0 = time.perf_counter()
             e64, _ = h.get_rpa_correlation_energy(opts, nq)

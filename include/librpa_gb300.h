@@ -22,6 +22,7 @@ extern "C" {
 /* E_c kernel path */
 #define LIBRPA_GB300_EC_LU_FP64 0     /* Pi = V chi0 in FP64, FP64 LU, sum log(+-u_ii) (LibRPA form) */
 #define LIBRPA_GB300_EC_CHOL 1        /* L^H chi0 L split-precision GEMMs, FP64 Cholesky */
+#define LIBRPA_GB300_EC_CHOL_FP64 2   /* the same Cholesky form with FP64 GEMMs: an all-FP64 E_c */
 
 /* block screening of chi0 contributions */
 #define LIBRPA_GB300_SCREEN_OFF 0

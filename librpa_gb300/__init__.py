@@ -26,7 +26,7 @@ ROUTING_UNSET, AUTO, RTAU, ATOMPAIR, LIBRI = -101, -51, 0, 1, 2
 TFGRID_UNSET, GaussLegendre, GaussChebyshevI, GaussChebyshevII, Minimax, EvenSpaced, EvenSpaced_TF = (
     -101, 0, 1, 2, 3, 4, 5)
 CHI0_FP64, CHI0_BF16X3, CHI0_FP32 = 0, 1, 2
-EC_LU_FP64, EC_CHOL = 0, 1
+EC_LU_FP64, EC_CHOL, EC_CHOL_FP64 = 0, 1, 2
 SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
 MLP_NPARAM, MLP_NNORM = 4609, 13
 STAGE_FULL, STAGE_CHI0, STAGE_EC = 0, 1, 2

@@ -177,12 +177,82 @@ __global__ void k_diag_trace(const float *__restrict__ Ms, int N, int parts, dou
     if (threadIdx.x == 0) tr[blockIdx.x] = make_double2(rr[0], ri[0]);
 }
 
+// FP64 forms of the same steps (all-FP64 path): out = conj(transpose(L)) (or transpose),
+// M' = I - M and tr(M)
+__global__ void k_adjoint_c(const cuDoubleComplex *__restrict__ L, int N, cuDoubleComplex *__restrict__ out)
+{
+    const long long nn = static_cast<long long>(N) * N;
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const cuDoubleComplex v = L[(e % N) * N + e / N];
+        out[e] = make_cuDoubleComplex(v.x, -v.y);
+    }
+}
+
+__global__ void k_transpose_r(const double *__restrict__ L, int N, double *__restrict__ out)
+{
+    const long long nn = static_cast<long long>(N) * N;
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+        out[e] = L[(e % N) * N + e / N];
+}
+
+template <typename T>
+__device__ inline double2 as_d2(T v);
+template <>
+__device__ inline double2 as_d2<double>(double v) { return make_double2(v, 0.0); }
+template <>
+__device__ inline double2 as_d2<cuDoubleComplex>(cuDoubleComplex v) { return make_double2(v.x, v.y); }
+
+template <typename T>
+__global__ void k_form_mprime64(const T *__restrict__ M, int N, T *__restrict__ Mp, double2 *__restrict__ tr)
+{
+    __shared__ double rr[256], ri[256];
+    const long long nn = static_cast<long long>(N) * N;
+    const T *S = M + blockIdx.y * nn;
+    T *O = Mp + blockIdx.y * nn;
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const double2 v = as_d2(S[e]);
+        const double d = (e / N) == (e % N) ? 1.0 : 0.0;
+        if constexpr (sizeof(T) == sizeof(double))
+            reinterpret_cast<double *>(O)[e] = d - v.x;
+        else
+            reinterpret_cast<cuDoubleComplex *>(O)[e] = make_cuDoubleComplex(d - v.x, -v.y);
+    }
+    if (blockIdx.x != 0) return;
+    double ar = 0.0, ai = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x)
+    {
+        const double2 v = as_d2(S[static_cast<long long>(i) * N + i]);
+        ar += v.x;
+        ai += v.y;
+    }
+    rr[threadIdx.x] = ar;
+    ri[threadIdx.x] = ai;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1)
+    {
+        if (threadIdx.x < s)
+        {
+            rr[threadIdx.x] += rr[threadIdx.x + s];
+            ri[threadIdx.x] += ri[threadIdx.x + s];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) tr[blockIdx.y] = make_double2(rr[0], ri[0]);
+}
+
 } // namespace
 
 struct EcChol::Impl
 {
     int N = 0, nw = 0, qb = 1;
-    bool cplx = true;
+    bool cplx = true, fp64 = false;
+    DevBuf<cuDoubleComplex> T64c, M64c, LHc;  // all-FP64 products
+    DevBuf<double> T64r, M64r, LHr;
     long long kpad = 0;
     DevBuf<int> err, bad, badV;
     SplitStore Bl, Al;            // L as B^T and L^H (or L^T) as A, one q at a time
@@ -195,13 +265,14 @@ struct EcChol::Impl
     DevBuf<double> Mpr;
 };
 
-EcChol::EcChol(int N, int nw, bool complex_path, int qb) : impl_(std::make_unique<Impl>())
+EcChol::EcChol(int N, int nw, bool complex_path, int qb, bool fp64_products) : impl_(std::make_unique<Impl>())
 {
     Impl &m = *impl_;
     m.N = N;
     m.nw = nw;
     m.qb = qb;
     m.cplx = complex_path;
+    m.fp64 = fp64_products;
     const int kdim = complex_path ? 2 * N : N;
     m.kpad = (kdim + 63) / 64 * 64;
     const long long rowsA = kdim;  // rows of the A operands
@@ -209,13 +280,7 @@ EcChol::EcChol(int N, int nw, bool complex_path, int qb) : impl_(std::make_uniqu
     m.err.alloc(1);
     m.bad.alloc(nmat);
     m.badV.alloc(qb);
-    m.Bl.alloc(3, static_cast<size_t>(N) * m.kpad);
-    m.Al.alloc(3, static_cast<size_t>(rowsA) * m.kpad);
     m.diagV.alloc(static_cast<size_t>(qb) * N);
-    m.A1.alloc(3, static_cast<size_t>(nw) * rowsA * m.kpad);
-    m.B2.alloc(3, static_cast<size_t>(nw) * N * m.kpad);
-    m.Tst.alloc(static_cast<size_t>(nw) * rowsA * N);
-    m.Mst.alloc(static_cast<size_t>(nw) * rowsA * N);
     m.diag.alloc(nmat * N);
     m.logdet.alloc(nmat);
     m.tr.alloc(nmat);
@@ -223,6 +288,29 @@ EcChol::EcChol(int N, int nw, bool complex_path, int qb) : impl_(std::make_uniqu
         m.Mpc.alloc(nmat * N * N);
     else
         m.Mpr.alloc(nmat * N * N);
+    if (fp64_products)
+    {
+        const size_t nn = static_cast<size_t>(N) * N;
+        if (complex_path)
+        {
+            m.T64c.alloc(nw * nn);
+            m.M64c.alloc(nw * nn);
+            m.LHc.alloc(nn);
+        }
+        else
+        {
+            m.T64r.alloc(nw * nn);
+            m.M64r.alloc(nw * nn);
+            m.LHr.alloc(nn);
+        }
+        return;
+    }
+    m.Bl.alloc(3, static_cast<size_t>(N) * m.kpad);
+    m.Al.alloc(3, static_cast<size_t>(rowsA) * m.kpad);
+    m.A1.alloc(3, static_cast<size_t>(nw) * rowsA * m.kpad);
+    m.B2.alloc(3, static_cast<size_t>(nw) * N * m.kpad);
+    m.Tst.alloc(static_cast<size_t>(nw) * rowsA * N);
+    m.Mst.alloc(static_cast<size_t>(nw) * rowsA * N);
 }
 
 EcChol::~EcChol() = default;
@@ -261,6 +349,34 @@ int EcChol::stage_q(const void *L, const void *X, int slot, cudaStream_t st)
     {
         m.err.zero(st);
         m.bad.zero(st);
+    }
+    if (m.fp64)
+    {
+        // M = L^H (chi0 L) with FP64 GEMMs, then M' = I - M and tr(M)
+        const size_t off = static_cast<size_t>(slot) * nw * nn;
+        dim3 gf(blocks_for(nn), nw);
+        if (m.cplx)
+        {
+            const cuDoubleComplex *Lc = static_cast<const cuDoubleComplex *>(L);
+            launch_zgemm(N, N, N, static_cast<const cuDoubleComplex *>(X), N, nn, Lc, N, 0, m.T64c.get(), N, nn, nw, st);
+            k_adjoint_c<<<blocks_for(nn), 256, 0, st>>>(Lc, N, m.LHc.get());
+            GB_LAUNCH_CHECK();
+            launch_zgemm(N, N, N, m.LHc.get(), N, 0, m.T64c.get(), N, nn, m.M64c.get(), N, nn, nw, st);
+            k_form_mprime64<cuDoubleComplex><<<gf, 256, 0, st>>>(m.M64c.get(), N, m.Mpc.get() + off,
+                                                                  m.tr.get() + static_cast<size_t>(slot) * nw);
+        }
+        else
+        {
+            const double *Lr = static_cast<const double *>(L);
+            launch_dgemm(N, N, N, static_cast<const double *>(X), N, nn, Lr, N, 0, m.T64r.get(), N, nn, nw, 1.0, 0.0, st);
+            k_transpose_r<<<blocks_for(nn), 256, 0, st>>>(Lr, N, m.LHr.get());
+            GB_LAUNCH_CHECK();
+            launch_dgemm(N, N, N, m.LHr.get(), N, 0, m.T64r.get(), N, nn, m.M64r.get(), N, nn, nw, 1.0, 0.0, st);
+            k_form_mprime64<double><<<gf, 256, 0, st>>>(m.M64r.get(), N, m.Mpr.get() + off,
+                                                         m.tr.get() + static_cast<size_t>(slot) * nw);
+        }
+        GB_LAUNCH_CHECK();
+        return 4;
     }
     const SplitBufs bl = m.Bl.bufs(), al = m.Al.bufs(), a1 = m.A1.bufs(), b2 = m.B2.bufs();
     const long long rowsA = m.cplx ? 2LL * N : N;

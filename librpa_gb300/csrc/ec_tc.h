@@ -14,8 +14,9 @@ class EcChol
 public:
     // N: auxiliary-basis size; nw: frequencies per q; complex_path: k-point (complex) matrices,
     // otherwise Gamma-only real parts; qb: q points whose M' = I - L^H chi0 L are factorised
-    // in one batch.
-    EcChol(int N, int nw, bool complex_path, int qb);
+    // in one batch; fp64_products: M = L^H chi0 L by FP64 CUDA-core GEMMs instead of the
+    // split-precision tensor-core GEMMs.
+    EcChol(int N, int nw, bool complex_path, int qb, bool fp64_products = false);
     ~EcChol();
     // V = L L^H in place for nb (<= qb) Coulomb matrices stored one after another (N x N each).
     int factor_v(void *V, int nb, cudaStream_t st);

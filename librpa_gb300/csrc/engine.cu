@@ -692,7 +692,10 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     res.per_q.assign(nq, cplx(0, 0));
     const long long NN = static_cast<long long>(N) * N;
     double ec_flops = 0.0;
-    const bool use_chol = go.ec_path == LIBRPA_GB300_EC_CHOL;
+    GB_REQUIRE(go.ec_path == LIBRPA_GB300_EC_LU_FP64 || go.ec_path == LIBRPA_GB300_EC_CHOL ||
+                   go.ec_path == LIBRPA_GB300_EC_CHOL_FP64,
+               "unknown ec_path " + std::to_string(go.ec_path));
+    const bool use_chol = go.ec_path != LIBRPA_GB300_EC_LU_FP64;
     // V(q) from the blocks of this q inside the staged Coulomb blob
     auto assemble_v = [&](int q, void *V) {
         std::vector<long long> voff;
@@ -730,7 +733,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         const size_t esz = gamma_only ? sizeof(double) : sizeof(cuDoubleComplex);
         const double per_q = static_cast<double>(nw + 1) * NN * esz;
         const int qb = std::max(1, std::min(nq, static_cast<int>(24.0e9 / per_q)));
-        EcChol ecc(N, nw, !gamma_only, qb);
+        EcChol ecc(N, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
         DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
         for (int q0 = 0; q0 < nq; q0 += qb)
         {

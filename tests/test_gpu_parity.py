@@ -109,3 +109,17 @@ def test_default_fast_path_fcc2():
     _, e64, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_LU_FP64)
     _, e, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
     assert abs(e - e64) <= MEV_PER_ATOM * len(s.nao)
+
+
+@pytest.mark.parametrize("case", ["h2o", "k2x1x1", "k3x2x1"])
+def test_all_fp64_cholesky_ec_matches_lu(case):
+    """The all-FP64 Cholesky form of E_c (the FP64 GPU baseline) equals the reference-form LU."""
+    if case == "h2o":
+        s = load_h2o()
+    else:
+        period = (2, 1, 1) if case == "k2x1x1" else (3, 2, 1)
+        s = sy.small_periodic(n_atoms=2, nao=[4, 5], nabf=[9, 12], period=period, nocc=2, seed=5)
+    _, e_lu, q_lu = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_LU_FP64)
+    _, e_ch, q_ch = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL_FP64)
+    assert abs(e_ch - e_lu) <= 1e-10 * abs(e_lu), (e_ch, e_lu)
+    np.testing.assert_allclose(q_ch.real, q_lu.real, rtol=1e-9, atol=1e-13)
