@@ -18,6 +18,8 @@ ROOT = PKG.parent
 SRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "liblibrpa_gb300.so"
+DRIVER_SRC = PKG / "driver" / "chi0_main.cpp"
+DRIVER = PKG / "chi0_main"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"),
           "-Xptxas", "-warn-spills", "--expt-relaxed-constexpr"]
@@ -70,7 +72,22 @@ def build(verbose: bool = False, jobs: int | None = None, extra: list[str] | Non
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_driver(hmt)
     return LIB
+
+
+def build_driver(headers_mtime: float = 0.0) -> Path:
+    """The task = rpa driver executable (host C++ over the C API), linked to the library."""
+    if DRIVER.exists() and DRIVER.stat().st_mtime > max(DRIVER_SRC.stat().st_mtime, LIB.stat().st_mtime,
+                                                         headers_mtime):
+        return DRIVER
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(DRIVER_SRC), "-L", str(PKG),
+           "-l:liblibrpa_gb300.so", "-Wl,-rpath,$ORIGIN", "-o", str(DRIVER)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":

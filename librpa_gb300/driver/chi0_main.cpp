@@ -1,0 +1,396 @@
+// chi0_main: the task = rpa driver of LibRPA (driver/main.cpp, driver/task/rpa.cpp) on top of
+// this library's C API.
+//
+// Reads `librpa.in` (key = value lines, '#' comments, the last occurrence of a key wins, as in
+// driver/inputfile.cpp) from the working directory, reads the FHI-aims export named by
+// input_dir (formats of driver/read_data.cpp), passes it through the librpa_set_* calls and
+// prints the RPA correlation energy in the layout of driver/task/rpa.cpp.
+//
+// Keys: task (rpa), input_dir, nfreq, tfgrids_type, parallel_routing, cs_threshold,
+// vq_threshold, libri_chi0_threshold_C, libri_chi0_threshold_G, minimax_emin/emax, and the
+// GPU controls gb300_chi0_precision (fp64 | bf16x3 | fp32), gb300_ec_path (lu | chol |
+// chol_fp64), gb300_screen_mode (off | threshold | mlp), gb300_screen_threshold.
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <dirent.h>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "librpa.h"
+
+namespace {
+
+using cplx = std::complex<double>;
+
+[[noreturn]] void die(const std::string &msg)
+{
+    throw std::runtime_error(msg);
+}
+
+std::string trim(const std::string &s)
+{
+    size_t b = s.find_first_not_of(" \t\r\n"), e = s.find_last_not_of(" \t\r\n");
+    return b == std::string::npos ? "" : s.substr(b, e - b + 1);
+}
+
+std::string lower(std::string s)
+{
+    for (auto &c : s) c = static_cast<char>(std::tolower(static_cast<unsigned char>(c)));
+    return s;
+}
+
+std::map<std::string, std::string> read_params(const std::string &fn)
+{
+    std::map<std::string, std::string> p;
+    std::ifstream f(fn);
+    if (!f) return p;
+    std::string line;
+    while (std::getline(f, line))
+    {
+        const auto h = line.find('#');
+        if (h != std::string::npos) line = line.substr(0, h);
+        const auto eq = line.find('=');
+        if (eq == std::string::npos) continue;
+        p[trim(line.substr(0, eq))] = trim(line.substr(eq + 1));  // later lines win
+    }
+    return p;
+}
+
+std::vector<std::string> tokens(const std::string &fn)
+{
+    std::ifstream f(fn);
+    if (!f) die("cannot open " + fn);
+    std::vector<std::string> t;
+    std::string w;
+    while (f >> w) t.push_back(w);
+    return t;
+}
+
+std::vector<char> slurp(const std::string &fn)
+{
+    std::ifstream f(fn, std::ios::binary);
+    if (!f) die("cannot open " + fn);
+    return std::vector<char>((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+
+std::vector<std::string> files_with_prefix(const std::string &dir, const std::string &prefix)
+{
+    std::vector<std::string> out;
+    if (DIR *d = opendir(dir.c_str()))
+    {
+        while (dirent *e = readdir(d))
+        {
+            const std::string n = e->d_name;
+            if (n.compare(0, prefix.size(), prefix) == 0) out.push_back(dir + n);
+        }
+        closedir(d);
+    }
+    std::sort(out.begin(), out.end());
+    return out;
+}
+
+bool exists(const std::string &fn)
+{
+    std::ifstream f(fn);
+    return static_cast<bool>(f);
+}
+
+template <typename T>
+T get(const std::vector<char> &raw, size_t &off)
+{
+    if (off + sizeof(T) > raw.size()) die("binary file ended early");
+    T v;
+    std::memcpy(&v, raw.data() + off, sizeof(T));
+    off += sizeof(T);
+    return v;
+}
+
+struct Mesh
+{
+    int nk = 0, ns = 0, nb = 0, nao = 0, nat = 0;
+    std::vector<int> types, nao_at, nabf_at, ibz;
+    int period[3] = {1, 1, 1};
+    std::vector<double> kvecs;
+};
+
+} // namespace
+
+int main()
+{
+    try
+    {
+        const auto p = read_params("librpa.in");
+        auto par = [&](const std::string &k, const std::string &d) { return p.count(k) ? p.at(k) : d; };
+        const std::string task = lower(par("task", "rpa"));
+        if (task != "rpa") die("this driver runs task = rpa only (got " + task + ")");
+        std::string dir = par("input_dir", "./");
+        if (dir.back() != '/') dir += '/';
+        const double cs_threshold = std::stod(par("cs_threshold", "1e-6"));
+
+        LibrpaOptions opts;
+        librpa_init_options(&opts);
+        opts.nfreq = std::stoi(par("nfreq", "16"));
+        const std::string tf = lower(par("tfgrids_type", "minimax"));
+        opts.tfgrids_type = tf == "minimax" ? Minimax : tf == "evenspaced_tf" ? EvenSpaced_TF
+                          : tf == "evenspaced" ? EvenSpaced : tf == "gl" ? GaussLegendre : Minimax;
+        const std::string rt = lower(par("parallel_routing", "libri"));
+        opts.parallel_routing = rt == "rtau" ? RTAU : rt == "atompair" ? ATOMPAIR : rt == "auto" ? AUTO : LIBRI;
+        opts.vq_threshold = std::stod(par("vq_threshold", "0"));
+        opts.libri_chi0_threshold_C = std::stod(par("libri_chi0_threshold_C", "0"));
+        opts.libri_chi0_threshold_G = std::stod(par("libri_chi0_threshold_G", "0"));
+        opts.minimax_emin = std::stod(par("minimax_emin", "-1"));
+        opts.minimax_emax = std::stod(par("minimax_emax", "-1"));
+
+        LibrpaHandler *h = librpa_create_handler(0);
+        if (!h) die(librpa_get_last_error(nullptr));
+        LibrpaGB300Options go;
+        librpa_gb300_init_options(&go);
+        const std::string prec = lower(par("gb300_chi0_precision", "bf16x3"));
+        go.chi0_precision = prec == "fp64" ? LIBRPA_GB300_CHI0_FP64 : prec == "fp32" ? LIBRPA_GB300_CHI0_FP32
+                                                                                    : LIBRPA_GB300_CHI0_BF16X3;
+        const std::string ecp = lower(par("gb300_ec_path", "chol"));
+        go.ec_path = ecp == "lu" ? LIBRPA_GB300_EC_LU_FP64 : ecp == "chol_fp64" ? LIBRPA_GB300_EC_CHOL_FP64
+                                                                                 : LIBRPA_GB300_EC_CHOL;
+        const std::string sm = lower(par("gb300_screen_mode", "off"));
+        go.screen_mode = sm == "threshold" ? LIBRPA_GB300_SCREEN_THRESHOLD : sm == "mlp" ? LIBRPA_GB300_SCREEN_MLP
+                                                                                         : LIBRPA_GB300_SCREEN_OFF;
+        go.screen_threshold = std::stod(par("gb300_screen_threshold", "1e-6"));
+        librpa_gb300_set_options(h, &go);
+
+        Mesh m;
+        // band_out (read_data.cpp:32-140): nk ns nb nao efermi, then per (k, s) block n f e e_eV
+        {
+            const auto t = tokens(dir + "band_out");
+            size_t q = 0;
+            m.nk = std::stoi(t.at(q++));
+            m.ns = std::stoi(t.at(q++));
+            m.nb = std::stoi(t.at(q++));
+            m.nao = std::stoi(t.at(q++));
+            const double ef = std::stod(t.at(q++));
+            std::vector<double> wg(static_cast<size_t>(m.ns) * m.nk * m.nb), ekb(wg.size());
+            for (int kk = 0; kk < m.nk; ++kk)
+                for (int ss = 0; ss < m.ns; ++ss)
+                {
+                    const int k = std::stoi(t.at(q)) - 1, s = std::stoi(t.at(q + 1)) - 1;
+                    q += 2;
+                    for (int n = 0; n < m.nb; ++n, q += 4)
+                    {
+                        const size_t i = (static_cast<size_t>(s) * m.nk + k) * m.nb + n;
+                        wg[i] = std::stod(t.at(q + 1));
+                        ekb[i] = std::stod(t.at(q + 2));
+                    }
+                }
+            librpa_set_scf_dimension(h, m.ns, m.nk, m.nb, m.nao, 1);
+            librpa_set_wg_ekb_efermi(h, m.ns, m.nk, m.nb, wg.data(), ekb.data(), ef);
+        }
+        // stru_out (read_data.cpp:1814-1867): lattice, reciprocal lattice, natoms, positions + types
+        std::vector<std::string> stru = tokens(dir + "stru_out");
+        {
+            double lat[9], G[9];
+            for (int i = 0; i < 9; ++i) lat[i] = std::stod(stru.at(i));
+            for (int i = 0; i < 9; ++i) G[i] = std::stod(stru.at(9 + i));
+            librpa_set_latvec_and_G(h, lat, G);
+            m.nat = std::stoi(stru.at(18));
+            std::vector<double> pos(3 * m.nat);
+            m.types.resize(m.nat);
+            size_t q = 19;
+            for (int a = 0; a < m.nat; ++a, q += 4)
+            {
+                for (int d = 0; d < 3; ++d) pos[3 * a + d] = std::stod(stru.at(q + d));
+                m.types[a] = std::stoi(stru.at(q + 3)) - 1;
+            }
+            librpa_set_atoms(h, m.nat, m.types.data(), pos.data());
+        }
+        // k mesh: bz_sampling_out (read_data.cpp:1869-1916) or the tail of stru_out
+        if (exists(dir + "bz_sampling_out"))
+        {
+            const auto t = tokens(dir + "bz_sampling_out");
+            for (int d = 0; d < 3; ++d) m.period[d] = std::stoi(t.at(d));
+            const int nkf = std::stoi(t.at(3));
+            m.kvecs.resize(3 * nkf);
+            m.ibz.resize(nkf);
+            size_t q = 5;
+            for (int i = 0; i < nkf; ++i, q += 10)
+            {
+                for (int d = 0; d < 3; ++d) m.kvecs[3 * i + d] = std::stod(t.at(q + 5 + d));
+                m.ibz[i] = std::stoi(t.at(q + 9)) - 1;
+            }
+        }
+        else
+        {
+            size_t q = 19 + 4 * static_cast<size_t>(m.nat);
+            for (int d = 0; d < 3; ++d) m.period[d] = std::stoi(stru.at(q++));
+            const int nkf = m.period[0] * m.period[1] * m.period[2];
+            m.kvecs.resize(3 * nkf);
+            for (int i = 0; i < 3 * nkf; ++i) m.kvecs[i] = std::stod(stru.at(q++));
+            m.ibz.resize(nkf);
+            for (int i = 0; i < nkf; ++i) m.ibz[i] = std::stoi(stru.at(q++)) - 1;
+        }
+        librpa_set_kgrids_kvec(h, m.period[0], m.period[1], m.period[2], m.kvecs.data());
+        librpa_set_ibz_mapping(h, static_cast<int>(m.ibz.size()), m.ibz.data());
+        // basis_out (read_data.cpp:1976-2011): ntypes, 3 header numbers, then (type, n_wfc, n_aux)
+        {
+            const auto t = tokens(dir + "basis_out");
+            const int ntypes = std::stoi(t.at(0));
+            std::map<int, std::pair<int, int>> per_type;
+            size_t q = 4;
+            for (int i = 0; i < ntypes; ++i, q += 3)
+                per_type[std::stoi(t.at(q)) - 1] = {std::stoi(t.at(q + 1)), std::stoi(t.at(q + 2))};
+            std::vector<size_t> nw(m.nat), na(m.nat);
+            for (int a = 0; a < m.nat; ++a)
+            {
+                if (!per_type.count(m.types[a])) die("basis_out lacks atom type " + std::to_string(m.types[a] + 1));
+                nw[a] = per_type[m.types[a]].first;
+                na[a] = per_type[m.types[a]].second;
+                m.nao_at.push_back(static_cast<int>(nw[a]));
+                m.nabf_at.push_back(static_cast<int>(na[a]));
+            }
+            librpa_set_ao_basis_wfc(h, m.nat, nw.data());
+            librpa_set_ao_basis_aux(h, m.nat, na.data());
+        }
+        // KS_eigenvector* (read_data.cpp:184-284): per k: index, then (re, im) in the order
+        // ao, band, spin (slowest to fastest: ao outermost)
+        {
+            const size_t per_k = static_cast<size_t>(m.nao) * m.nb * m.ns;
+            std::vector<std::vector<double>> re(static_cast<size_t>(m.ns) * m.nk), im(re.size());
+            for (const auto &fn : files_with_prefix(dir, "KS_eigenvector"))
+            {
+                const auto t = tokens(fn);
+                size_t q = 0;
+                while (q < t.size())
+                {
+                    const int ik = std::stoi(t[q++]) - 1;
+                    if (q + 2 * per_k > t.size()) die("truncated eigenvector file " + fn);
+                    for (int s = 0; s < m.ns; ++s)
+                    {
+                        re[static_cast<size_t>(s) * m.nk + ik].assign(static_cast<size_t>(m.nb) * m.nao, 0.0);
+                        im[static_cast<size_t>(s) * m.nk + ik].assign(static_cast<size_t>(m.nb) * m.nao, 0.0);
+                    }
+                    for (int iw = 0; iw < m.nao; ++iw)
+                        for (int ib = 0; ib < m.nb; ++ib)
+                            for (int s = 0; s < m.ns; ++s, q += 2)
+                            {
+                                auto &R = re[static_cast<size_t>(s) * m.nk + ik];
+                                auto &I = im[static_cast<size_t>(s) * m.nk + ik];
+                                R[static_cast<size_t>(ib) * m.nao + iw] = std::stod(t[q]);
+                                I[static_cast<size_t>(ib) * m.nao + iw] = std::stod(t[q + 1]);
+                            }
+                }
+            }
+            for (int s = 0; s < m.ns; ++s)
+                for (int k = 0; k < m.nk; ++k)
+                {
+                    const auto &R = re[static_cast<size_t>(s) * m.nk + k];
+                    if (R.empty()) die("no eigenvectors for k point " + std::to_string(k + 1));
+                    librpa_set_wfc(h, s, k, m.nb, m.nao, R.data(), im[static_cast<size_t>(s) * m.nk + k].data());
+                }
+        }
+        // Cs_data* binary (read_data.cpp:690-747): natom ncell nblocks, then per block
+        // I J R1 R2 R3 n_i n_j n_mu and n_i*n_j*n_mu doubles; kept if max |C| >= cs_threshold
+        for (const auto &fn : files_with_prefix(dir, "Cs_data"))
+        {
+            const auto raw = slurp(fn);
+            size_t off = 0;
+            get<int>(raw, off);
+            get<int>(raw, off);
+            const int nblk = get<int>(raw, off);
+            for (int b = 0; b < nblk; ++b)
+            {
+                int v[8];
+                for (auto &x : v) x = get<int>(raw, off);
+                const size_t cnt = static_cast<size_t>(v[5]) * v[6] * v[7];
+                if (off + 8 * cnt > raw.size()) die("truncated RI file " + fn);
+                std::vector<double> c(cnt);
+                std::memcpy(c.data(), raw.data() + off, 8 * cnt);
+                off += 8 * cnt;
+                double mx = 0.0;
+                for (double x : c) mx = std::max(mx, std::fabs(x));
+                if (mx < cs_threshold) continue;
+                const int R[3] = {v[2], v[3], v[4]};
+                librpa_set_lri_coeff(h, static_cast<LibrpaParallelRouting>(opts.parallel_routing), v[0] - 1, v[1] - 1,
+                                     v[5], v[6], v[7], R, c.data());
+            }
+        }
+        // coulomb_mat* binary (read_data.cpp:1472-1577): n_irk n_local, then per block
+        // nbasbas brow erow bcol ecol iq q_weight and the rows (complex); atom-pair blocks I <= J
+        {
+            std::vector<int> off_at(m.nat + 1, 0);
+            for (int a = 0; a < m.nat; ++a) off_at[a + 1] = off_at[a] + m.nabf_at[a];
+            std::map<int, std::vector<cplx>> full;
+            int nbb = 0;
+            for (const auto &fn : files_with_prefix(dir, "coulomb_mat"))
+            {
+                const auto raw = slurp(fn);
+                size_t off = 0;
+                get<int>(raw, off);
+                const int nloc = get<int>(raw, off);
+                for (int b = 0; b < nloc; ++b)
+                {
+                    nbb = get<int>(raw, off);
+                    const int br = get<int>(raw, off) - 1, er = get<int>(raw, off) - 1;
+                    const int bc = get<int>(raw, off) - 1, ec = get<int>(raw, off) - 1;
+                    const int iq = get<int>(raw, off) - 1;
+                    get<double>(raw, off);
+                    auto &M = full[iq];
+                    M.resize(static_cast<size_t>(nbb) * nbb);
+                    const int nc = ec - bc + 1;
+                    for (int r = br; r <= er; ++r)
+                        for (int c = 0; c < nc; ++c)
+                        {
+                            const double x = get<double>(raw, off), y = get<double>(raw, off);
+                            M[static_cast<size_t>(r) * nbb + bc + c] = cplx(x, y);
+                        }
+                }
+            }
+            for (const auto &[iq, M] : full)
+                for (int I = 0; I < m.nat; ++I)
+                    for (int J = I; J < m.nat; ++J)
+                    {
+                        const int nm = m.nabf_at[I], nn = m.nabf_at[J];
+                        std::vector<double> vr(static_cast<size_t>(nm) * nn), vi(vr.size());
+                        for (int a = 0; a < nm; ++a)
+                            for (int c = 0; c < nn; ++c)
+                            {
+                                const cplx z = M[static_cast<size_t>(off_at[I] + a) * nbb + off_at[J] + c];
+                                vr[static_cast<size_t>(a) * nn + c] = z.real();
+                                vi[static_cast<size_t>(a) * nn + c] = z.imag();
+                            }
+                        librpa_set_aux_bare_coulomb_k_atom_pair(h, iq, I, J, nm, nn, vr.data(), vi.data(),
+                                                                opts.vq_threshold);
+                    }
+        }
+
+        int n_ibz = 0;
+        {
+            std::vector<int> seen;
+            for (int k : m.ibz)
+                if (std::find(seen.begin(), seen.end(), k) == seen.end()) seen.push_back(k);
+            n_ibz = static_cast<int>(seen.size());
+        }
+        std::vector<double> re(n_ibz), im(n_ibz);
+        const double ec = librpa_get_rpa_correlation_energy(h, &opts, n_ibz, re.data(), im.data());
+        if (std::isnan(ec)) die(librpa_get_last_error(h));
+        std::printf("RPA correlation energy (Hartree)\n");
+        std::printf("| Weighted contribution from each k:\n");
+        for (int i = 0; i < n_ibz; ++i) std::printf("| %d: (%.12g,%.12g)\n", i + 1, re[i], im[i]);
+        std::printf("| Total EcRPA: %18.9f\n", ec);
+        for (int i = 0; i < n_ibz; ++i)
+            if (std::fabs(im[i]) > 1e-3)
+                std::printf("Warning: considerable imaginary part of EcRPA = %f\n at IBZ k-point %d\n", im[i], i + 1);
+        librpa_destroy_handler(h);
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        std::fprintf(stderr, "chi0_main: %s\n", e.what());
+        return 1;
+    }
+}

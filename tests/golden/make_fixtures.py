@@ -14,6 +14,8 @@ Produces (all committed, so the tests need no reference tree at run time):
                      asserted in src/test/test_timefreq.cpp (check_minimax_ng6_HF_123)
   he_bcc_gamma.json  the BCC He known-answer test of src/test/test_meanfield.cpp
                      (eigenpairs, Fermi level, expected density matrix and G(tau -> 0-))
+  h2o_dataset.tar.gz the H2O regression dataset itself (the reference's FHI-aims export, copied
+                     unchanged), for the task = rpa driver test
 """
 from __future__ import annotations
 
@@ -113,8 +115,16 @@ def he_bcc(ref: Path):
     print("he_bcc_gamma.json written:", len(checks), "checks")
 
 
+def h2o_dataset(ref: Path):
+    import shutil
+    src = ref / "regression_tests/testcases/rpa_aims_mole_H2O_libri/dataset.tar.gz"
+    shutil.copyfile(src, HERE / "h2o_dataset.tar.gz")
+    print("h2o_dataset.tar.gz written")
+
+
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     h2o(ref)
+    h2o_dataset(ref)
     minimax(ref)
     he_bcc(ref)

@@ -1,0 +1,50 @@
+"""The task = rpa driver (librpa_gb300/chi0_main, the counterpart of the reference's
+chi0_main task=rpa) on the H2O regression dataset of the reference (tests/golden)."""
+import re
+import subprocess
+import tarfile
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+DATASET = ROOT / "tests" / "golden" / "h2o_dataset.tar.gz"
+EC_REF = -0.306258510  # refs/rpa_aims_mole_H2O_libri/librpa/librpa_omp1_np4.out:273
+
+
+def _prepare(tmp_path, extra=""):
+    with tarfile.open(DATASET) as tf:
+        tf.extractall(tmp_path, filter="data")
+    data = next(tmp_path.rglob("band_out")).parent
+    (tmp_path / "librpa.in").write_text(f"# driver parameters\ntask = rpa\ninput_dir = {data}\nnfreq = 16\n"
+                                        f"parallel_routing = libri\n{extra}")
+    return tmp_path
+
+
+def _driver(lib):
+    from librpa_gb300.build import DRIVER
+    assert DRIVER.exists(), "driver not built"
+    return str(DRIVER)
+
+
+def test_driver_reads_dataset_without_gpu(tmp_path, lib):
+    """Everything up to the GPU call: on a machine without a GPU the driver reads all files and
+    then reports the missing device (not a parse error)."""
+    if lib.librpa_gb300_device_count() > 0:
+        pytest.skip("a GPU is visible: the GPU test covers the full run")
+    d = _prepare(tmp_path)
+    r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1
+    assert "CUDA" in r.stderr or "device" in r.stderr, r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("extra,tol", [("gb300_chi0_precision = fp64\ngb300_ec_path = lu\n", 2e-9),
+                                       ("", 3 * 3.674932e-6)])
+def test_driver_h2o_regression(tmp_path, lib, extra, tol):
+    d = _prepare(tmp_path, extra)
+    r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    assert "RPA correlation energy (Hartree)" in r.stdout
+    ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))
+    assert abs(ec - EC_REF) <= max(tol, 1e-9), (ec, EC_REF)
