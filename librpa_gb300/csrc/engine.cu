@@ -515,12 +515,16 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             {
                 launch_gk_build(d_psi.get() + static_cast<size_t>(is) * nk * nb * nao, d_s.get(), nk, nb, nao, d_A.get(), st);
                 launch_phase_sum(d_A.get(), d_gcos.get(), d_gsin.get(), nk, nc, nao, d_G.get(), st);
-                launch_gsuper(d_G.get(), g, d_Gs.get(), st);
-                launches += 4;
+                launches += 3;
             }
             if (thr_g > 0.0)
             {
                 launch_g_block_filter(d_G.get(), g, thr_g, st);  // LibRI set_Gs_pos / set_Gs_neg filter
+                ++launches;
+            }
+            if (!gk)
+            {
+                launch_gsuper(d_G.get(), g, d_Gs.get(), st);  // from the filtered blocks
                 ++launches;
             }
             ev_gf.stop(st);
