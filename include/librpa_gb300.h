@@ -153,6 +153,13 @@ int librpa_gb300_device_count(void);
  * CUDA-core GEMM.  Returns max|diff| / max|ref| (NaN on error). */
 double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces);
 
+/* Diagnostic: `batch` random N x N SPD matrices (condition spread by a diagonal scaling of
+ * spread_decades decades) factored by the FP64 CUDA-core Cholesky and by the variant whose
+ * trailing updates run on the tensor cores as exact 7-bit integer slice products.  Returns
+ * the largest |ln det difference| (NaN on error); *max_rel_l (may be NULL) receives
+ * max |L difference| / max |L|. */
+double librpa_gb300_selftest_chol_ozaki(int N, int batch, int seed, int spread_decades, double *max_rel_l);
+
 /* No counterpart in the reference.  D = A * B through the tcgen05 split-precision GEMM
  * (pieces = 2 or 3, as above) without allocating device memory, for callers that cannot
  * let a library allocate (a host code that has already sized its own pool to the whole

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/librpa.h"
+#include "chol.h"
 #include "common.h"
 #include "dataset.h"
 #include "screen.h"
@@ -877,6 +878,17 @@ double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces)
     guarded(nullptr, [&] {
         GB_REQUIRE(gb::device_count() > 0, "no CUDA device visible");
         r = gb::tc_gemm_selftest(M, N, K, seed, pieces);
+    });
+    return r;
+}
+
+double librpa_gb300_selftest_chol_ozaki(int N, int batch, int seed, int spread_decades, double *max_rel_l)
+{
+    double r = std::numeric_limits<double>::quiet_NaN();
+    guarded(nullptr, [&] {
+        GB_REQUIRE(gb::device_count() > 0, "no CUDA device visible");
+        GB_REQUIRE(N > 0 && batch > 0, "N and batch must be positive");
+        r = gb::chol_ozaki_selftest(N, batch, seed, spread_decades, max_rel_l);
     });
     return r;
 }

@@ -263,6 +263,10 @@ struct EcChol::Impl
     DevBuf<double2> tr;
     DevBuf<cuDoubleComplex> Mpc;
     DevBuf<double> Mpr;
+    // real matrices: Cholesky trailing updates on the tensor cores (exact integer slices)
+    bool ozaki = false;
+    OzakiWork oz;
+    ~Impl() { ozaki_free(oz); }
 };
 
 EcChol::EcChol(int N, int nw, bool complex_path, int qb, bool fp64_products) : impl_(std::make_unique<Impl>())
@@ -288,6 +292,8 @@ EcChol::EcChol(int N, int nw, bool complex_path, int qb, bool fp64_products) : i
         m.Mpc.alloc(nmat * N * N);
     else
         m.Mpr.alloc(nmat * N * N);
+    m.ozaki = !complex_path && !fp64_products && N > OZAKI_NB;
+    if (m.ozaki) ozaki_alloc(m.oz, N, static_cast<int>(nmat));
     if (fp64_products)
     {
         const size_t nn = static_cast<size_t>(N) * N;
@@ -328,12 +334,17 @@ int EcChol::factor_v(void *V, int nb, cudaStream_t st)
     }
     else
     {
-        launches += chol_batched_r(static_cast<double *>(V), m.N, nb, m.diagV.get(), m.badV.get(), st);
+        launches += m.ozaki ? chol_batched_r_ozaki(static_cast<double *>(V), m.N, nb, m.diagV.get(), m.badV.get(),
+                                                   m.oz, st)
+                            : chol_batched_r(static_cast<double *>(V), m.N, nb, m.diagV.get(), m.badV.get(), st);
         zero_upper_r(static_cast<double *>(V), m.N, nb, st);
     }
     std::vector<int> bad(nb);
+    int herr = 0;
     m.badV.download(bad.data(), nb, st);
+    if (m.ozaki) GB_CUDA(cudaMemcpyAsync(&herr, m.oz.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
+    GB_REQUIRE(herr == 0, "tensor-core Cholesky update reported wait timeout code " + std::to_string(herr));
     for (int b = 0; b < nb; ++b) GB_REQUIRE(!bad[b], "V(q) is not positive definite: no Cholesky factor");
     return launches;
 }
@@ -443,7 +454,8 @@ int EcChol::finish(int nslots, std::vector<std::complex<double>> &trace_out,
     if (m.cplx)
         launches += chol_batched_c(m.Mpc.get(), N, nmat, m.diag.get(), m.bad.get(), st);
     else
-        launches += chol_batched_r(m.Mpr.get(), N, nmat, m.diag.get(), m.bad.get(), st);
+        launches += m.ozaki ? chol_batched_r_ozaki(m.Mpr.get(), N, nmat, m.diag.get(), m.bad.get(), m.oz, st)
+                            : chol_batched_r(m.Mpr.get(), N, nmat, m.diag.get(), m.bad.get(), st);
     chol_logdet(m.diag.get(), N, nmat, m.logdet.get(), st);
     std::vector<double> ld(nmat);
     std::vector<int> bad(nmat);
@@ -452,9 +464,12 @@ int EcChol::finish(int nslots, std::vector<std::complex<double>> &trace_out,
     m.logdet.download(ld.data(), nmat, st);
     m.bad.download(bad.data(), nmat, st);
     m.tr.download(tr.data(), nmat, st);
+    int herr_oz = 0;
     m.err.download(&herr, 1, st);
+    if (m.ozaki) GB_CUDA(cudaMemcpyAsync(&herr_oz, m.oz.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     GB_REQUIRE(herr == 0, "tensor-core E_c GEMM reported wait timeout code " + std::to_string(herr));
+    GB_REQUIRE(herr_oz == 0, "tensor-core Cholesky update reported wait timeout code " + std::to_string(herr_oz));
     for (int b = 0; b < nmat; ++b)
         GB_REQUIRE(!bad[b], "I - L^H chi0 L is not positive definite (chi0 not negative semidefinite?)");
     trace_out.assign(nmat, {0.0, 0.0});

@@ -1,9 +1,11 @@
 // Batched blocked Cholesky factorisation in FP64 (real symmetric or complex Hermitian).
 //
-// Right-looking, panel width NB = 32, one launch pair per panel step for the whole batch:
-//   k_chol_panel : each CTA factors the diagonal block (redundantly, it is tiny) and solves
-//                  a 64-row slab of the panel below it, X L11^H = A21;
+// Right-looking, panel width NB = 32, three launches per panel step for the whole batch:
+//   k_chol_diag  : one CTA per matrix factors the NB x NB diagonal block in shared memory;
+//   k_chol_panel : each CTA solves a 64-row slab of the panel below it, X L11^H = A21;
 //   k_chol_update: lower-triangle trailing update A22 -= L21 L21^H in 32 x 32 tiles.
+// The real variant chol_batched_r_ozaki uses panels of 64 and does the trailing update on the
+// tensor cores with exact integer slices (k_chol_ozaki.cu).
 // The diagonal of L is written to diag[b][i]; ln det A = 2 sum_i log L_ii (k_chol_logdet).
 // On GB300 the FP64 pipe (~1 TFLOP/s) bounds these kernels; the blocking keeps them off
 // the HBM roofline (each trailing element is read and written once per 32 columns).
@@ -40,8 +42,8 @@ __device__ inline double cfromreal(double x, double) { return x; }
 __device__ inline cuDoubleComplex cfromreal(double x, cuDoubleComplex) { return make_cuDoubleComplex(x, 0.0); }
 
 // Factor the nb x nb diagonal block at k0 into shared memory D (lower triangle).
-template <typename T>
-__device__ void factor_diag(const T *A, int N, int k0, int nb, T (*D)[NB + 1], int *bad)
+template <typename T, int NBT>
+__device__ void factor_diag(const T *A, int N, int k0, int nb, T (*D)[NBT + 1], int *bad)
 {
     for (int t = threadIdx.x; t < nb * nb; t += blockDim.x)
     {
@@ -72,15 +74,15 @@ __device__ void factor_diag(const T *A, int N, int k0, int nb, T (*D)[NB + 1], i
 }
 
 // Factor the diagonal block in place (one CTA per matrix) and record the diagonal of L.
-template <typename T>
+template <typename T, int NBT>
 __global__ void __launch_bounds__(256) k_chol_diag(T *__restrict__ Aall, int N, int k0, double *__restrict__ diag,
                                                   int *__restrict__ bad)
 {
-    __shared__ T D[NB][NB + 1];
+    __shared__ T D[NBT][NBT + 1];
     const int b = blockIdx.x;
     T *A = Aall + static_cast<long long>(b) * N * N;
-    const int nb = min(NB, N - k0);
-    factor_diag(A, N, k0, nb, D, bad + b);
+    const int nb = min(NBT, N - k0);
+    factor_diag<T, NBT>(A, N, k0, nb, D, bad + b);
     for (int t = threadIdx.x; t < nb * nb; t += blockDim.x)
     {
         const int i = t / nb, j = t % nb;
@@ -90,13 +92,13 @@ __global__ void __launch_bounds__(256) k_chol_diag(T *__restrict__ Aall, int N, 
 }
 
 // Panel solve X L11^H = A21 for a 64-row slab per CTA (L11 already factored in A).
-template <typename T>
+template <typename T, int NBT>
 __global__ void __launch_bounds__(64) k_chol_panel(T *__restrict__ Aall, int N, int k0)
 {
-    __shared__ T D[NB][NB + 1];
+    __shared__ T D[NBT][NBT + 1];
     const int b = blockIdx.y;
     T *A = Aall + static_cast<long long>(b) * N * N;
-    const int nb = min(NB, N - k0);
+    const int nb = min(NBT, N - k0);
     for (int t = threadIdx.x; t < nb * nb; t += blockDim.x)
     {
         const int i = t / nb, j = t % nb;
@@ -105,7 +107,7 @@ __global__ void __launch_bounds__(64) k_chol_panel(T *__restrict__ Aall, int N, 
     __syncthreads();
     const int r = k0 + nb + blockIdx.x * 64 + threadIdx.x;
     if (r >= N) return;
-    T x[NB];
+    T x[NBT];
     for (int p = 0; p < nb; ++p) x[p] = A[static_cast<long long>(r) * N + k0 + p];
     for (int p = 0; p < nb; ++p)
     {
@@ -197,13 +199,13 @@ int chol_impl(T *A, int N, int batch, double *diag, int *bad, cudaStream_t st)
     {
         const int nb = std::min(NB, N - k0);
         const int rows_below = N - k0 - nb;
-        k_chol_diag<T><<<batch, 256, 0, st>>>(A, N, k0, diag, bad);
+        k_chol_diag<T, NB><<<batch, 256, 0, st>>>(A, N, k0, diag, bad);
         GB_LAUNCH_CHECK();
         ++launches;
         if (rows_below > 0)
         {
             dim3 gp((rows_below + 63) / 64, batch);
-            k_chol_panel<T><<<gp, 64, 0, st>>>(A, N, k0);
+            k_chol_panel<T, NB><<<gp, 64, 0, st>>>(A, N, k0);
             GB_LAUNCH_CHECK();
             const int ntile = (rows_below + 31) / 32;
             dim3 gu(ntile * (ntile + 1) / 2, batch);
@@ -225,6 +227,28 @@ int chol_batched_c(cuDoubleComplex *A, int N, int batch, double *diag, int *bad,
 int chol_batched_r(double *A, int N, int batch, double *diag, int *bad, cudaStream_t st)
 {
     return chol_impl(A, N, batch, diag, bad, st);
+}
+
+int chol_batched_r_ozaki(double *A, int N, int batch, double *diag, int *bad, OzakiWork &w, cudaStream_t st)
+{
+    constexpr int NBO = OZAKI_NB;
+    int launches = 0;
+    for (int k0 = 0; k0 < N; k0 += NBO)
+    {
+        const int nb = std::min(NBO, N - k0);
+        const int rows_below = N - k0 - nb;
+        k_chol_diag<double, NBO><<<batch, 256, 0, st>>>(A, N, k0, diag, bad);
+        GB_LAUNCH_CHECK();
+        ++launches;
+        if (rows_below > 0)
+        {
+            dim3 gp((rows_below + 63) / 64, batch);
+            k_chol_panel<double, NBO><<<gp, 64, 0, st>>>(A, N, k0);
+            GB_LAUNCH_CHECK();
+            launches += 1 + ozaki_trailing_update(A, N, batch, k0 + nb, k0, nb, w, st);
+        }
+    }
+    return launches;
 }
 
 void chol_logdet(const double *diag, int N, int batch, double *logdet, cudaStream_t st)
