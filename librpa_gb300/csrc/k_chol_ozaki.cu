@@ -2,33 +2,41 @@
 //
 // After a panel step the lower trailing matrix needs A22 -= L21 L21^T, with L21 the panel rows
 // below the diagonal block (OZAKI_NB = 64 columns).  Each row r of L21 is scaled by 2^-e_r (e_r
-// from frexp of the row's largest magnitude, so every scaled value v lies in (-1, 1)) and cut
-// into OZAKI_SLICES = 8 integer slices of 7 bits,
+// the exponent of the row's largest magnitude, so every scaled value v lies in (-1, 1)) and cut
+// into OZAKI_SLICES = 8 integer slices of 7 bits (sign and magnitude digits of |v| 2^56),
 //     v = sum_p s_p 2^{-7(p+1)},   s_p in [-127, 127]   (exact in BF16),
 // so that
 //     (L21 L21^T)[i][j] = 2^{e_i + e_j} sum_{p,q} 2^{-7(p+q+2)} (S_p S_q^T)[i][j].
 // One slice product sums 64 terms below 2^14 in magnitude (below 2^20), and the group of
 // products with the same d = p + q has at most 8 members (below 2^23): integers below 2^24,
 // which the tensor core's FP32 accumulation holds exactly whatever its rounding.  The groups
-// d = 0..7 (36 products) are kept; a dropped product is below 2^-63 |x_i| |x_j| per term, so
-// the update matches FP64 arithmetic.  The epilogue recombines the groups in FP64 and
-// subtracts from A22.
+// d = 0..7 (36 products) are kept; a dropped product is below 2^-56 |v_i| |v_j| per term, so
+// the update matches FP64 arithmetic.
 //
-// One CTA per 128 x 64 tile of the lower trailing matrix: one lane loads the 8 + 8 slice tiles
-// with TMA, one lane issues the MMAs into 8 TMEM accumulators (one per group d), four warps
-// run the epilogue.  Every wait is bounded and reports a timeout through the error flag.
+// The epilogue is integer work: GB300's FP64 pipe issues about two operations per clock per
+// SM, so the 8 groups are converted to int32, combined into a 128-bit fixed-point value
+//     U = sum_d T_d 2^{7(7-d)}   (value = U 2^{e_i + e_j - 63}),
+// rounded to a double by integer operations, and one FP64 subtraction per element applies it.
+//
+// Work item of a CTA: a block of 128 trailing columns j (the MMA's M, TMEM lanes) against up
+// to OZ_CHUNK blocks of 32 trailing rows i (the MMA's N) with i >= j.  The 8 column-side
+// slices stay in shared memory; the row-side slices stream through a 2-stage ring, and two
+// TMEM accumulators (8 groups x 32 columns each) let the epilogue of one row block overlap
+// the MMAs of the next.  Lanes of a warp hold consecutive columns j, so every read-modify-write
+// of A[i][j] is a coalesced 256-byte row segment.  Warp 0 issues TMA, warp 1 the MMAs, warps
+// 2-9 run the epilogue.  Every wait is bounded; a timeout sets the error flag and the CTA
+// winds down (later CTAs return at once).
 #include <cuda_bf16.h>
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "chol.h"
 #include "common.h"
-#include "tc_common.cuh"
 #include "kernels.h"
+#include "tc_common.cuh"
 #include "tc_gemm.h"
-
-#include <vector>
 
 namespace gb {
 
@@ -36,21 +44,74 @@ namespace {
 
 using namespace tc;
 
-constexpr int OM = 128, ON = 64, OK = OZAKI_NB;  // tile rows, tile columns, K
+constexpr int OM = 128, ON = 32, OK = OZAKI_NB;  // columns j per item, rows i per tile, K
 constexpr int SL = OZAKI_SLICES;
+constexpr int OZ_CHUNK = 32;          // row tiles per CTA
 constexpr int TILE_A = OM * OK * 2;   // 16 KB per slice
-constexpr int TILE_B = ON * OK * 2;   // 8 KB per slice
-constexpr int OZ_SMEM = SL * (TILE_A + TILE_B) + 1024 + 256;
+constexpr int TILE_B = ON * OK * 2;   // 4 KB per slice
+constexpr int STAGE_B = SL * TILE_B;  // 32 KB per ring stage
+constexpr int OZ_SMEM = SL * TILE_A + 2 * STAGE_B + 1024 + 256;
 static_assert(OK == 64, "one 128-byte swizzle row per slice row");
 static_assert(OZ_SMEM <= 227 * 1024, "shared memory budget");
-constexpr int OZ_THREADS = 192;  // warp 0: TMA, warp 1: MMA, warps 2-5: epilogue
+constexpr int OZ_EPI_WARPS = 8;
+constexpr int OZ_THREADS = 32 * (2 + OZ_EPI_WARPS);
+constexpr int ACC_COLS = SL * ON;  // 256 TMEM columns per accumulator
 
 struct OzMaps
 {
-    CUtensorMap a, b;  // the same slice buffer with 128-row and 64-row boxes
+    CUtensorMap a, b;  // the same slice buffer with 128-row and 32-row boxes
 };
 
-// One warp per panel row: row scale and the 8 integer slices.
+// value = (hi 2^28 + lo) 2^e0, rounded to nearest even, by integer operations only.
+__device__ __forceinline__ double fixed_to_double(long long hi, long long lo, int e0)
+{
+    const unsigned long long Lh = static_cast<unsigned long long>(hi) << 28;
+    long long H = hi >> 36;
+    const unsigned long long L = Lh + static_cast<unsigned long long>(lo);
+    H += (L < Lh ? 1 : 0) + (lo < 0 ? -1 : 0);
+    const bool neg = H < 0;
+    unsigned long long h = static_cast<unsigned long long>(H), l = L;
+    if (neg)
+    {
+        l = ~l + 1ull;
+        h = ~h + (l == 0 ? 1ull : 0ull);
+    }
+    if ((h | l) == 0) return 0.0;
+    const int lz = h ? __clzll(static_cast<long long>(h)) : 64 + __clzll(static_cast<long long>(l));
+    unsigned long long top, rest;
+    if (lz == 0)
+    {
+        top = h;
+        rest = l;
+    }
+    else if (lz < 64)
+    {
+        top = (h << lz) | (l >> (64 - lz));
+        rest = l << lz;
+    }
+    else
+    {
+        top = l << (lz - 64);
+        rest = 0;
+    }
+    unsigned long long mant = top >> 11;
+    const unsigned long long rb = top & 0x7FFull;
+    if (rb > 0x400ull || (rb == 0x400ull && (rest != 0 || (mant & 1ull)))) ++mant;
+    int ex = 127 - lz + e0;
+    if (mant >> 53)
+    {
+        mant >>= 1;
+        ++ex;
+    }
+    const int be = ex + 1023;
+    if (be <= 0) return 0.0;  // below the normal range: negligible next to the FP64 entries
+    const unsigned long long bits = (static_cast<unsigned long long>(neg) << 63) |
+                                    (static_cast<unsigned long long>(be) << 52) | (mant & 0xFFFFFFFFFFFFFull);
+    return __longlong_as_double(static_cast<long long>(bits));
+}
+
+// One warp per panel row: row exponent and the 8 integer slices, by integer operations on the
+// FP64 bit patterns (the digits of |v| 2^56, v = x 2^-e; subnormal entries count as zero).
 __global__ void k_ozaki_slice(const double *__restrict__ A, int N, int s0, int k0, int nb,
                               __nv_bfloat16 *__restrict__ S, int *__restrict__ E)
 {
@@ -60,52 +121,69 @@ __global__ void k_ozaki_slice(const double *__restrict__ A, int N, int s0, int k
     const int R = N - s0;
     if (rl >= R) return;
     const double *row = A + static_cast<long long>(b) * N * N + static_cast<long long>(s0 + rl) * N + k0;
-    double v[2];
-    double m = 0.0;
+    unsigned long long u[2];
+    unsigned long long m = 0;
 #pragma unroll
     for (int h = 0; h < 2; ++h)
     {
         const int c = lane + 32 * h;
-        v[h] = c < nb ? row[c] : 0.0;
-        m = fmax(m, fabs(v[h]));
+        u[h] = c < nb ? static_cast<unsigned long long>(__double_as_longlong(row[c])) : 0ull;
+        m = max(m, u[h] & 0x7FFFFFFFFFFFFFFFull);  // magnitudes order like their bit patterns
     }
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    int e = 0;
-    if (m > 0.0) frexp(m, &e);  // m = f 2^e, f in [0.5, 1): |v 2^-e| < 1
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const int mexp = static_cast<int>(m >> 52);  // biased exponent of the row maximum
+    const int e = mexp ? mexp - 1022 : 0;       // max < 2^e
     const size_t plane = static_cast<size_t>(N) * OK;
     __nv_bfloat16 *Sb = S + static_cast<size_t>(b) * SL * plane + static_cast<size_t>(rl) * OK;
 #pragma unroll
     for (int h = 0; h < 2; ++h)
     {
         const int c = lane + 32 * h;
-        double t = ldexp(v[h], -e);
+        const int bexp = static_cast<int>((u[h] >> 52) & 0x7FF);
+        const bool neg = (u[h] >> 63) != 0;
+        unsigned long long F = 0;  // |x| 2^(56 - e), truncated
+        if (bexp != 0 && mexp != 0)
+        {
+            const unsigned long long mant = (u[h] & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+            const int sh = (bexp - 1023) + 4 - e;  // |x| = mant 2^(bexp - 1075); <= 3 since |x| < 2^e
+            F = sh >= 0 ? mant << sh : (sh > -64 ? mant >> (-sh) : 0ull);
+        }
 #pragma unroll
         for (int p = 0; p < SL; ++p)
         {
-            t *= 128.0;
-            const double s = trunc(t);
-            t -= s;
-            Sb[p * plane + c] = __double2bfloat16(s);
+            const int dgt = static_cast<int>((F >> (49 - 7 * p)) & 127ull);
+            Sb[p * plane + c] = __float2bfloat16_rn(static_cast<float>(neg ? -dgt : dgt));
         }
     }
     if (lane == 0) E[static_cast<size_t>(b) * N + rl] = e;
 }
 
-__device__ __forceinline__ void tile_of(int t, int nrt, int nct, int &ti, int &tj)
+// Work item t -> (column block jm, first row tile, row tile count)
+__device__ __forceinline__ bool item_of(int t, int njm, int nti, int &jm, int &ti0, int &cnt)
 {
-    // lower tiles: row tile ti (128 rows) meets column tiles tj <= 2 ti + 1 (64 columns)
-    for (ti = 0; ti < nrt; ++ti)
+    for (jm = 0; jm < njm; ++jm)
     {
-        const int cnt = min(2 * ti + 2, nct);
-        if (t < cnt)
+        const int first = 4 * jm;  // row tiles with 32 ti + 31 >= 128 jm
+        const int nch = (nti - first + OZ_CHUNK - 1) / OZ_CHUNK;
+        if (t < nch)
         {
-            tj = t;
-            return;
+            ti0 = first + t * OZ_CHUNK;
+            cnt = min(OZ_CHUNK, nti - ti0);
+            return true;
         }
-        t -= cnt;
+        t -= nch;
     }
-    ti = nrt;  // out of range
-    tj = 0;
+    return false;
+}
+
+// Bounded wait that gives up at once after any earlier timeout of the CTA.
+__device__ __forceinline__ bool oz_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag, int *err, int code)
+{
+    if (*abort_flag) return false;
+    if (mbar_wait(bar, parity)) return true;
+    *abort_flag = 1;
+    atomicExch(err, code);
+    return false;
 }
 
 __global__ void __launch_bounds__(OZ_THREADS, 1)
@@ -115,118 +193,151 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *sA = smem, *sB = smem + SL * TILE_A;
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + SL * (TILE_A + TILE_B));
-    uint64_t *done = full + 1;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(sB + 2 * STAGE_B);
+    uint64_t *fullA = bars, *fullB = bars + 1, *emptyB = bars + 3, *tfull = bars + 5, *tempty = bars + 7,
+             *fin = bars + 9;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 10);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 11);
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int b = blockIdx.y;
     const int R = N - s0;
-    const int nrt = (R + OM - 1) / OM, nct = (R + ON - 1) / ON;
-    int ti, tj;
-    tile_of(blockIdx.x, nrt, nct, ti, tj);
-    if (ti >= nrt) return;  // uniform over the CTA
+    const int nti = (R + ON - 1) / ON, njm = (R + OM - 1) / OM;
+    int jm, ti0, cnt;
+    if (!item_of(blockIdx.x, njm, nti, jm, ti0, cnt)) return;  // uniform over the CTA
+    volatile int *skip_flag = abort_flag + 1;
 
     if (threadIdx.x == 0)
     {
-        mbar_init(full, 1);
-        mbar_init(done, 1);
+        mbar_init(fullA, 1);
+        for (int s = 0; s < 2; ++s)
+        {
+            mbar_init(fullB + s, 1);
+            mbar_init(emptyB + s, 1);
+            mbar_init(tfull + s, 1);
+            mbar_init(tempty + s, OZ_EPI_WARPS);
+        }
+        mbar_init(fin, 1);
+        *abort_flag = 0;
+        *skip_flag = *reinterpret_cast<volatile int *>(err);  // an earlier CTA timed out: no work
         fence_barrier_init();
     }
-    if (warp == 0) tmem_alloc(tmem_slot, SL * ON);  // 8 groups x 64 columns = 512
+    if (warp == 1) tmem_alloc(tmem_slot, 2 * ACC_COLS);
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    bool ok = true;
 
-    if (warp == 0 && lane == 0)
+    if (*skip_flag)
     {
-        mbar_arrive_expect_tx(full, SL * (TILE_A + TILE_B));
-#pragma unroll
-        for (int p = 0; p < SL; ++p)
-        {
-            tma_load_3d(sA + p * TILE_A, &maps.a, 0, ti * OM, b * SL + p, full);
-            tma_load_3d(sB + p * TILE_B, &maps.b, 0, tj * ON, b * SL + p, full);
-        }
-        // the copies must land before the CTA may exit, also when the MMA lane gave up
-        if (!mbar_wait(full, 0)) atomicExch(err, 303);
     }
-    else if (warp == 1 && lane == 0)
+    else if (warp == 0)
     {
-        if (!mbar_wait(full, 0))
+        if (lane == 0)
         {
-            atomicExch(err, 301);
-        }
-        else
-        {
-            tc_fence_after();
-            constexpr uint32_t idesc = idesc_bf16_f32(OM, ON);
-            for (int d = 0; d < SL; ++d)
+            mbar_arrive_expect_tx(fullA, SL * TILE_A);
+            for (int p = 0; p < SL; ++p) tma_load_3d(sA + p * TILE_A, &maps.a, 0, jm * OM, b * SL + p, fullA);
+            int issued = 0;
+            for (int t = 0; t < cnt; ++t)
             {
-                bool first = true;
-                for (int p = 0; p <= d; ++p)
-                {
-                    const int q = d - p;
-                    const uint64_t da = smem_desc_sw128(sA + p * TILE_A), db = smem_desc_sw128(sB + q * TILE_B);
-#pragma unroll
-                    for (int k = 0; k < OK / 16; ++k)
-                    {
-                        const uint64_t dk = static_cast<uint64_t>(k * 32 >> 4);
-                        mma_bf16(tmem + d * ON, da + dk, db + dk, idesc, first && k == 0 ? 0 : 1);
-                    }
-                    first = false;
-                }
+                const int s = t & 1;
+                if (t >= 2 && !oz_wait(emptyB + s, ((t >> 1) - 1) & 1, abort_flag, err, 311)) break;
+                mbar_arrive_expect_tx(fullB + s, STAGE_B);
+                for (int q = 0; q < SL; ++q)
+                    tma_load_3d(sB + s * STAGE_B + q * TILE_B, &maps.b, 0, (ti0 + t) * ON, b * SL + q, fullB + s);
+                issued = t + 1;
             }
+            // the copies must land before the CTA exits, also after a timeout
+            mbar_wait(fullA, 0);
+            for (int t = issued > 2 ? issued - 2 : 0; t < issued; ++t) mbar_wait(fullB + (t & 1), (t >> 1) & 1);
         }
-        mma_commit(done);  // arrives once the issued MMAs (if any) are complete
     }
-    else if (warp >= 2)
+    else if (warp == 1)
     {
-        const int quad = warp % 4;  // TMEM lane quadrant this warp may read
-        const uint32_t lane_base = static_cast<uint32_t>(quad * 32) << 16;
-        if (!__all_sync(0xffffffffu, mbar_wait(done, 0)))
+        if (lane == 0)
         {
-            if (lane == 0) atomicExch(err, 302);
-            ok = false;
-        }
-        if (ok)
-        {
+            constexpr uint32_t idesc = idesc_bf16_f32(OM, ON);
+            bool ok = oz_wait(fullA, 0, abort_flag, err, 312);
             tc_fence_after();
-            const int il = quad * 32 + lane;
-            const int i = s0 + ti * OM + il;
-            const int *E = Eall + static_cast<size_t>(b) * N;
-            const int ei = i < N ? E[i - s0] : 0;
-            double *Arow = Aall + static_cast<long long>(b) * N * N + static_cast<long long>(i) * N;
-#pragma unroll 1
-            for (int c0 = 0; c0 < ON; c0 += 16)
+            for (int t = 0; ok && t < cnt; ++t)
             {
-                double acc[16];
-#pragma unroll
-                for (int c = 0; c < 16; ++c) acc[c] = 0.0;
-#pragma unroll 1
+                const int s = t & 1;
+                if (!oz_wait(fullB + s, (t >> 1) & 1, abort_flag, err, 313)) break;
+                if (t >= 2 && !oz_wait(tempty + s, ((t >> 1) - 1) & 1, abort_flag, err, 314)) break;
+                tc_fence_after();
+                const uint32_t acc = tmem + s * ACC_COLS;
                 for (int d = 0; d < SL; ++d)
-                {
-                    uint32_t v[16];
-                    tmem_ld16_nowait(tmem + d * ON + c0 + lane_base, v);
-                    tmem_wait_ld();
-                    const double sc = ldexp(1.0, -7 * (d + 2));
-#pragma unroll
-                    for (int c = 0; c < 16; ++c) acc[c] += static_cast<double>(__uint_as_float(v[c])) * sc;
-                }
-                if (i < N)
-                {
-#pragma unroll
-                    for (int c = 0; c < 16; ++c)
+                    for (int p = 0; p <= d; ++p)
                     {
-                        const int j = s0 + tj * ON + c0 + c;
-                        if (j < N && j <= i) Arow[j] -= ldexp(acc[c], ei + __ldg(E + (j - s0)));
+                        const uint64_t da = smem_desc_sw128(sA + p * TILE_A);
+                        const uint64_t db = smem_desc_sw128(sB + s * STAGE_B + (d - p) * TILE_B);
+#pragma unroll
+                        for (int k = 0; k < OK / 16; ++k)
+                        {
+                            const uint64_t dk = static_cast<uint64_t>(k * 32 >> 4);
+                            mma_bf16(acc + d * ON, da + dk, db + dk, idesc, (p == 0 && k == 0) ? 0u : 1u);
+                        }
                     }
+                mma_commit(emptyB + s);
+                mma_commit(tfull + s);
+            }
+            // every issued MMA completes before TMEM is released
+            mma_commit(fin);
+            mbar_wait(fin, 0);
+        }
+    }
+    else
+    {
+        const int ew = warp - 2;
+        const int quad = warp % 4;  // TMEM lane quadrant this warp may read
+        const int half = ew / 4;    // which 16 of the 32 tile columns
+        const uint32_t lane_base = static_cast<uint32_t>(quad * 32) << 16;
+        const int jl = jm * OM + quad * 32 + lane;  // trailing column index
+        const int j = s0 + jl;
+        const int *E = Eall + static_cast<size_t>(b) * N;
+        const int ej = j < N ? E[jl] : 0;
+        double *Ab = Aall + static_cast<long long>(b) * N * N;
+        for (int t = 0; t < cnt; ++t)
+        {
+            const int s = t & 1;
+            const bool ok = __all_sync(0xffffffffu, oz_wait(tfull + s, (t >> 1) & 1, abort_flag, err, 315));
+            if (!ok) break;
+            tc_fence_after();
+            const uint32_t acc = tmem + s * ACC_COLS + half * 16 + lane_base;
+            int U[4][16];
+#pragma unroll
+            for (int g = 0; g < 4; ++g)
+            {
+                uint32_t v0[16], v1[16];
+                tmem_ld16_nowait(acc + (2 * g) * ON, v0);
+                tmem_ld16_nowait(acc + (2 * g + 1) * ON, v1);
+                tmem_wait_ld();
+#pragma unroll
+                for (int c = 0; c < 16; ++c)
+                    U[g][c] = __float2int_rn(__uint_as_float(v0[c])) * 128 + __float2int_rn(__uint_as_float(v1[c]));
+            }
+            // TMEM of this accumulator is free again
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty + s);
+            const int ib = s0 + (ti0 + t) * ON + half * 16;
+            const int ei_own = (ib - s0 + (lane & 15)) < R ? E[ib - s0 + (lane & 15)] : 0;
+#pragma unroll
+            for (int c = 0; c < 16; ++c)
+            {
+                const int i = ib + c;
+                const int ei = __shfl_sync(0xffffffffu, ei_own, c);
+                if (i < N && j < N && j <= i)
+                {
+                    const long long hi = (static_cast<long long>(U[0][c]) << 14) + U[1][c];
+                    const long long lo = (static_cast<long long>(U[2][c]) << 14) + U[3][c];
+                    double *a = Ab + static_cast<long long>(i) * N + j;
+                    *a -= fixed_to_double(hi, lo, ei + ej - 63);
                 }
             }
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, SL * ON);
+    if (warp == 1) tmem_dealloc(tmem, 2 * ACC_COLS);
 }
 
 } // namespace
@@ -269,10 +380,10 @@ int ozaki_trailing_update(double *A, int N, int batch, int s0, int k0, int nb, O
         GB_CUDA(cudaFuncSetAttribute(k_ozaki_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
         attr = true;
     }
-    const int nrt = (R + OM - 1) / OM, nct = (R + ON - 1) / ON;
-    long long tiles = 0;
-    for (int ti = 0; ti < nrt; ++ti) tiles += std::min(2 * ti + 2, nct);
-    dim3 grid(static_cast<unsigned>(tiles), batch);
+    const int nti = (R + ON - 1) / ON, njm = (R + OM - 1) / OM;
+    long long items = 0;
+    for (int jm = 0; jm < njm; ++jm) items += (nti - 4 * jm + OZ_CHUNK - 1) / OZ_CHUNK;
+    dim3 grid(static_cast<unsigned>(items), batch);
     k_ozaki_syrk<<<grid, OZ_THREADS, OZ_SMEM, st>>>(maps, A, N, s0, w.expo, w.err);
     GB_LAUNCH_CHECK();
     return 2;
