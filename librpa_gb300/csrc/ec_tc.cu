@@ -141,8 +141,9 @@ __global__ void k_form_mprime_r(const float *__restrict__ Ms, int N, double *__r
     for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
          e += static_cast<long long>(gridDim.x) * blockDim.x)
     {
-        const bool d = (e / N) == (e % N);
-        O[e] = (d ? 1.0 : 0.0) - static_cast<double>(S[e]);
+        // lower triangle only: the product kernel leaves the upper tiles of M unwritten
+        const long long i = e / N, j = e % N;
+        O[e] = j > i ? 0.0 : (i == j ? 1.0 : 0.0) - static_cast<double>(S[e]);
     }
 }
 
@@ -417,9 +418,17 @@ int EcChol::stage_q(const void *L, const void *X, int slot, cudaStream_t st)
         }
         launches += 2 + nw;
     }
-    // T = chi0 L  (rowsA x N per w)
+    // T = chi0 L  (rowsA x N per w); real path: L is lower triangular, so the K range of an
+    // output column block n starts at n
+    TcGemmOpts o1, o2;
+    if (!m.cplx)
+    {
+        o1.tri = 1;
+        o2.tri = 2;             // A = L^T: row m is zero before column m
+        o2.lower_tiles = true;  // M is symmetric: its lower triangle is all that is read
+    }
     tc_gemm_split(m.A1.mat(rowsA, m.kpad, rowsA * m.kpad), m.Bl.mat(N, m.kpad, 0), static_cast<int>(rowsA), N,
-                  static_cast<int>(m.cplx ? 2 * N : N), nw, m.Tst.get(), N, rowsA * N, false, m.err.get(), st);
+                  static_cast<int>(m.cplx ? 2 * N : N), nw, m.Tst.get(), N, rowsA * N, false, m.err.get(), st, o1);
     // B2 = K-major form of T (row n = T(:, n))
     {
         dim3 g(static_cast<unsigned>((m.kpad + 31) / 32), static_cast<unsigned>((N + 31) / 32), nw);
@@ -429,7 +438,7 @@ int EcChol::stage_q(const void *L, const void *X, int slot, cudaStream_t st)
     }
     // M = L^H T
     tc_gemm_split(m.Al.mat(rowsA, m.kpad, 0), m.B2.mat(N, m.kpad, N * m.kpad), static_cast<int>(rowsA), N,
-                  static_cast<int>(m.cplx ? 2 * N : N), nw, m.Mst.get(), N, rowsA * N, false, m.err.get(), st);
+                  static_cast<int>(m.cplx ? 2 * N : N), nw, m.Mst.get(), N, rowsA * N, false, m.err.get(), st, o2);
     // tr(V chi0) = tr(L^H chi0 L) from the same products as M': to first order the FP32
     // rounding of M cancels between ln det(I - M) and tr(M)
     k_diag_trace<<<nw, 256, 0, st>>>(m.Mst.get(), N, m.cplx ? 2 : 1, m.tr.get() + static_cast<size_t>(slot) * nw);

@@ -24,7 +24,7 @@
 // TMEM accumulators (8 groups x 32 columns each) let the epilogue of one row block overlap
 // the MMAs of the next.  Lanes of a warp hold consecutive columns j, so every read-modify-write
 // of A[i][j] is a coalesced 256-byte row segment.  Warp 0 issues TMA, warp 1 the MMAs, warps
-// 2-9 run the epilogue.  Every wait is bounded; a timeout sets the error flag and the CTA
+// 2-17 run the epilogue (each lane reads its A entries before it waits for the MMAs).  Every wait is bounded; a timeout sets the error flag and the CTA
 // winds down (later CTAs return at once).
 #include <cuda_bf16.h>
 
@@ -53,7 +53,10 @@ constexpr int STAGE_B = SL * TILE_B;  // 32 KB per ring stage
 constexpr int OZ_SMEM = SL * TILE_A + 2 * STAGE_B + 1024 + 256;
 static_assert(OK == 64, "one 128-byte swizzle row per slice row");
 static_assert(OZ_SMEM <= 227 * 1024, "shared memory budget");
-constexpr int OZ_EPI_WARPS = 8;
+constexpr int OZ_EPI_WARPS = 16;  // 4 per TMEM lane quadrant, 8 tile columns each
+constexpr int EC = ON / (OZ_EPI_WARPS / 4);
+static_assert(EC == 8, "the epilogue loads 8 TMEM columns at a time");
+
 constexpr int OZ_THREADS = 32 * (2 + OZ_EPI_WARPS);
 constexpr int ACC_COLS = SL * ON;  // 256 TMEM columns per accumulator
 
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     {
         const int ew = warp - 2;
         const int quad = warp % 4;  // TMEM lane quadrant this warp may read
-        const int half = ew / 4;    // which 16 of the 32 tile columns
+        const int part = ew / 4;    // which EC of the 32 tile columns
         const uint32_t lane_base = static_cast<uint32_t>(quad * 32) << 16;
         const int jl = jm * OM + quad * 32 + lane;  // trailing column index
         const int j = s0 + jl;
@@ -298,30 +301,38 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         for (int t = 0; t < cnt; ++t)
         {
             const int s = t & 1;
+            const int ib = s0 + (ti0 + t) * ON + part * EC;
+            // the EC entries of A this lane updates, read while the MMAs run
+            double av[EC];
+#pragma unroll
+            for (int c = 0; c < EC; ++c)
+            {
+                const int i = ib + c;
+                av[c] = (i < N && j < N && j <= i) ? Ab[static_cast<long long>(i) * N + j] : 0.0;
+            }
             const bool ok = __all_sync(0xffffffffu, oz_wait(tfull + s, (t >> 1) & 1, abort_flag, err, 315));
             if (!ok) break;
             tc_fence_after();
-            const uint32_t acc = tmem + s * ACC_COLS + half * 16 + lane_base;
-            int U[4][16];
+            const uint32_t acc = tmem + s * ACC_COLS + part * EC + lane_base;
+            int U[4][EC];
 #pragma unroll
             for (int g = 0; g < 4; ++g)
             {
-                uint32_t v0[16], v1[16];
-                tmem_ld16_nowait(acc + (2 * g) * ON, v0);
-                tmem_ld16_nowait(acc + (2 * g + 1) * ON, v1);
+                uint32_t v0[EC], v1[EC];
+                tmem_ld8_nowait(acc + (2 * g) * ON, v0);
+                tmem_ld8_nowait(acc + (2 * g + 1) * ON, v1);
                 tmem_wait_ld();
 #pragma unroll
-                for (int c = 0; c < 16; ++c)
+                for (int c = 0; c < EC; ++c)
                     U[g][c] = __float2int_rn(__uint_as_float(v0[c])) * 128 + __float2int_rn(__uint_as_float(v1[c]));
             }
             // TMEM of this accumulator is free again
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(tempty + s);
-            const int ib = s0 + (ti0 + t) * ON + half * 16;
-            const int ei_own = (ib - s0 + (lane & 15)) < R ? E[ib - s0 + (lane & 15)] : 0;
+            const int ei_own = (ib - s0 + (lane % EC)) < R ? E[ib - s0 + (lane % EC)] : 0;
 #pragma unroll
-            for (int c = 0; c < 16; ++c)
+            for (int c = 0; c < EC; ++c)
             {
                 const int i = ib + c;
                 const int ei = __shfl_sync(0xffffffffu, ei_own, c);
@@ -329,8 +340,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 {
                     const long long hi = (static_cast<long long>(U[0][c]) << 14) + U[1][c];
                     const long long lo = (static_cast<long long>(U[2][c]) << 14) + U[3][c];
-                    double *a = Ab + static_cast<long long>(i) * N + j;
-                    *a -= fixed_to_double(hi, lo, ei + ej - 63);
+                    Ab[static_cast<long long>(i) * N + j] = av[c] - fixed_to_double(hi, lo, ei + ej - 63);
                 }
             }
         }

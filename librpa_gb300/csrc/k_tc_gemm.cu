@@ -63,11 +63,49 @@ __host__ __device__ constexpr int term_b(int ns, int t)
 // drain warps add each stage's pair into round-to-nearest FP32 registers while the next
 // stage's MMAs run.
 constexpr int GEMM_THREADS = 256;  // warp 0: TMA, warp 1: MMA, warps 4-7: drain + epilogue
+constexpr int RASTER_GROUP = 8;     // output-tile rows per raster group
+
+// Linear CTA index -> output tile.  Tiles run column by column inside groups of RASTER_GROUP
+// tile rows, so the CTAs resident at one time share a few A row panels and B column panels in
+// L2.  lower != 0: only tiles with nt <= mt (square tile grid), in the same grouped order.
+__device__ __forceinline__ void tile_coords(int t, int ntm, int ntn, int lower, int &mt, int &nt)
+{
+    constexpr int G = RASTER_GROUP;
+    if (!lower)
+    {
+        const int g = t / (G * ntn);
+        const int gm = min(G, ntm - g * G);
+        const int l = t - g * G * ntn;
+        mt = g * G + l % gm;
+        nt = l / gm;
+        return;
+    }
+    int g = 0, rem = t;
+    for (;; ++g)
+    {
+        const int gm = min(G, ntm - g * G);
+        const int cnt = gm * (g * G + 1) + gm * (gm - 1) / 2;
+        if (rem < cnt || gm <= 0) break;
+        rem -= cnt;
+    }
+    const int gm = min(G, ntm - g * G), r0 = g * G;
+    for (nt = 0; nt < ntn; ++nt)
+    {
+        const int rows = nt <= r0 ? gm : r0 + gm - nt;
+        if (rem < rows)
+        {
+            mt = (nt <= r0 ? r0 : nt) + rem;
+            return;
+        }
+        rem -= rows;
+    }
+    mt = 0;  // not reached for t below the lower-tile count
+}
 
 template <int NS>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_tc_gemm(const __grid_constant__ TmapSet maps, int M, int N, int K, float *__restrict__ D, long long ldd,
-              long long sD, int accumulate_out, int a_bcast, int b_bcast, int *__restrict__ err)
+              long long sD, int accumulate_out, int a_bcast, int b_bcast, int tri, int lower, int *__restrict__ err)
 {
     constexpr int STAGES = Cfg<NS>::STAGES, STAGE_BYTES = Cfg<NS>::STAGE_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -79,8 +117,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acce + 2);
 
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM, b = blockIdx.z;
+    int mt, nt;
+    tile_coords(blockIdx.x, (M + BM - 1) / BM, (N + BN - 1) / BN, lower, mt, nt);
+    const int n0 = nt * BN, m0 = mt * BM, b = blockIdx.z;
     const int nk = (K + BK - 1) / BK;
+    // K blocks that can be nonzero: B[n][k] = 0 for k < n (tri 1), A[m][k] = 0 for k < m (tri 2)
+    const int kb0 = tri == 1 ? n0 / BK : (tri == 2 ? m0 / BK : 0);
+    const int nsteps = nk - kb0;
 
     if (threadIdx.x == 0)
     {
@@ -105,9 +148,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     if (warp == 0 && lane == 0)
     {
         const int za = a_bcast ? 0 : b, zb = b_bcast ? 0 : b;
-        for (int kb = 0; kb < nk; ++kb)
+        for (int it = 0; it < nsteps; ++it)
         {
-            const int s = kb % STAGES, r = kb / STAGES;
+            const int kb = kb0 + it, s = it % STAGES, r = it / STAGES;
             if (!mbar_wait(&empty[s], (r & 1) ^ 1))
             {
                 atomicExch(err, 101);
@@ -126,11 +169,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     else if (warp == 1 && lane == 0)
     {
         constexpr uint32_t idesc = idesc_bf16_f32(BM, BN);
-        for (int kb = 0; kb < nk; ++kb)
+        for (int it = 0; it < nsteps; ++it)
         {
-            const int s = kb % STAGES, r = kb / STAGES;
-            const int ab = kb & 1;
-            if (!mbar_wait(&full[s], r & 1) || !mbar_wait(&acce[ab], ((kb >> 1) & 1) ^ 1))
+            const int s = it % STAGES, r = it / STAGES;
+            const int ab = it & 1;
+            if (!mbar_wait(&full[s], r & 1) || !mbar_wait(&acce[ab], ((it >> 1) & 1) ^ 1))
             {
                 atomicExch(err, 102);
                 break;
@@ -165,10 +208,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         float acc[BN];
 #pragma unroll
         for (int c = 0; c < BN; ++c) acc[c] = 0.0f;
-        for (int kb = 0; kb < nk; ++kb)
+        for (int it = 0; it < nsteps; ++it)
         {
-            const int ab = kb & 1;
-            if (!mbar_wait(&accf[ab], (kb >> 1) & 1))
+            const int ab = it & 1;
+            if (!mbar_wait(&accf[ab], (it >> 1) & 1))
             {
                 atomicExch(err, 103);
                 ok = false;
@@ -338,7 +381,7 @@ void split_transpose_f64(const double *src, long long lds, int K, int N, int kpa
 
 template <int NS>
 static void launch_tc(const SplitMat &A, const SplitMat &B, int M, int N, int K, int batch, float *D, long long ldd,
-                      long long sD, bool accumulate, int *err, cudaStream_t st)
+                      long long sD, bool accumulate, int *err, cudaStream_t st, const TcGemmOpts &o)
 {
     TmapSet maps;
     const int ba = A.batch_stride == 0 ? 1 : batch, bb = B.batch_stride == 0 ? 1 : batch;
@@ -353,9 +396,15 @@ static void launch_tc(const SplitMat &A, const SplitMat &B, int M, int N, int K,
         GB_CUDA(cudaFuncSetAttribute(k_tc_gemm<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<NS>::SMEM_BYTES));
         attr = true;
     }
-    dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, batch);
+    const long long ntm = (M + BM - 1) / BM, ntn = (N + BN - 1) / BN;
+    GB_REQUIRE(!o.lower_tiles || ntm == ntn, "lower-tile GEMM needs a square tile grid");
+    GB_REQUIRE(o.tri >= 0 && o.tri <= 2, "triangular operand mode must be 0, 1 or 2");
+    GB_REQUIRE(o.tri == 0 || K >= (o.tri == 1 ? N : M), "triangular operand shorter than its K range");
+    const long long tiles = o.lower_tiles ? ntm * (ntm + 1) / 2 : ntm * ntn;
+    dim3 grid(static_cast<unsigned>(tiles), 1, batch);
     k_tc_gemm<NS><<<grid, GEMM_THREADS, Cfg<NS>::SMEM_BYTES, st>>>(maps, M, N, K, D, ldd, sD, accumulate ? 1 : 0,
-                                                          A.batch_stride == 0, B.batch_stride == 0, err);
+                                                          A.batch_stride == 0, B.batch_stride == 0, o.tri,
+                                                          o.lower_tiles ? 1 : 0, err);
     GB_LAUNCH_CHECK();
 }
 
@@ -366,14 +415,14 @@ void tc_gemm_set_attributes()
 }
 
 void tc_gemm_split(const SplitMat &A, const SplitMat &B, int M, int N, int K, int batch, float *D, long long ldd,
-                   long long sD, bool accumulate, int *err, cudaStream_t st)
+                   long long sD, bool accumulate, int *err, cudaStream_t st, const TcGemmOpts &o)
 {
     GB_REQUIRE(A.ns == B.ns && (A.ns == 2 || A.ns == 3), "split operands must have the same piece count (2 or 3)");
     GB_REQUIRE(K <= A.kpad && K <= B.kpad && A.kpad % BK == 0 && B.kpad % BK == 0, "split operand padding");
     if (A.ns == 2)
-        launch_tc<2>(A, B, M, N, K, batch, D, ldd, sD, accumulate, err, st);
+        launch_tc<2>(A, B, M, N, K, batch, D, ldd, sD, accumulate, err, st, o);
     else
-        launch_tc<3>(A, B, M, N, K, batch, D, ldd, sD, accumulate, err, st);
+        launch_tc<3>(A, B, M, N, K, batch, D, ldd, sD, accumulate, err, st, o);
 }
 
 // ------------------------------------------------------------------ self-test

@@ -62,10 +62,19 @@ void split_rows_f32(const float *src, long long lds, long long rows, int cols, i
 // split of the transpose: src [K][N] row-major -> dst [N][kpad]
 void split_transpose_f64(const double *src, long long lds, int K, int N, int kpad, const SplitBufs &o,
                          cudaStream_t st);
+// Structure the split GEMM may skip.  tri = 1: B[n][k] = 0 for k < n (B^T lower triangular),
+// tri = 2: A[m][k] = 0 for k < m; the K loop of an output tile then starts at its first
+// nonzero 64-wide block (the skipped products are exact zeros).  lower_tiles: only output tiles
+// on or below the diagonal are computed (symmetric results); the others are left untouched.
+struct TcGemmOpts
+{
+    int tri = 0;
+    bool lower_tiles = false;
+};
 // D[b] (+)= A[b] * B[b]^T from BF16 split pieces (ns = 2: 3 products, ns = 3: 6 products),
 // FP32 TMEM accumulation.
 void tc_gemm_split(const SplitMat &A, const SplitMat &B, int M, int N, int K, int batch, float *D, long long ldd,
-                   long long sD, bool accumulate, int *err, cudaStream_t st);
+                   long long sD, bool accumulate, int *err, cudaStream_t st, const TcGemmOpts &o = TcGemmOpts{});
 // Set the split GEMM kernels' shared-memory attribute on the current device.
 void tc_gemm_set_attributes();
 // D = A * B through the split GEMM with all scratch in a fixed static device array
