@@ -14,12 +14,15 @@
 // the update matches FP64 arithmetic.
 //
 // The epilogue is integer work: GB300's FP64 pipe issues about two operations per clock per
-// SM, so the 8 groups are converted to int32, combined into a 128-bit fixed-point value
-//     U = sum_d T_d 2^{7(7-d)}   (value = U 2^{e_i + e_j - 63}),
-// rounded to a double by integer operations, and one FP64 subtraction per element applies it.
+// SM, so the 8 groups are converted to int32 and combined into the fixed-point value
+//     U = sum_d T_d 2^{7(7-d)}   (value = U 2^{e_i + e_j - 63}, |U| < 2^69),
+// rounded to W = U / 2^7 in 64 bits (resolution 2^-56 of 2^{e_i + e_j}, below the FP64
+// rounding of the entries it updates), turned into a double by integer operations, and one
+// FP64 subtraction per element applies it.
 //
 // Work item of a CTA: a block of 128 trailing columns j (the MMA's M, TMEM lanes) against up
-// to OZ_CHUNK blocks of 32 trailing rows i (the MMA's N) with i >= j.  The 8 column-side
+// to OZ_CHUNK blocks of 32 trailing rows i (the MMA's N) with i >= j; per 16-wide K step,
+// 8 MMAs (one per column-side slice p, N = 32 (8 - p)) cover the 36 slice products.  The 8 column-side
 // slices stay in shared memory; the row-side slices stream through a 2-stage ring, and two
 // TMEM accumulators (8 groups x 32 columns each) let the epilogue of one row block overlap
 // the MMAs of the next.  Lanes of a warp hold consecutive columns j, so every read-modify-write
@@ -65,52 +68,25 @@ struct OzMaps
     CUtensorMap a, b;  // the same slice buffer with 128-row and 32-row boxes
 };
 
-// value = (hi 2^28 + lo) 2^e0, rounded to nearest even, by integer operations only.
-__device__ __forceinline__ double fixed_to_double(long long hi, long long lo, int e0)
+// value = w 2^e0 for |w| < 2^63, rounded to nearest (ties away from zero), by integer
+// operations only (GB300's FP64 pipe is the scarce unit here).
+__device__ __forceinline__ double fixed_to_double(long long w, int e0)
 {
-    const unsigned long long Lh = static_cast<unsigned long long>(hi) << 28;
-    long long H = hi >> 36;
-    const unsigned long long L = Lh + static_cast<unsigned long long>(lo);
-    H += (L < Lh ? 1 : 0) + (lo < 0 ? -1 : 0);
-    const bool neg = H < 0;
-    unsigned long long h = static_cast<unsigned long long>(H), l = L;
-    if (neg)
-    {
-        l = ~l + 1ull;
-        h = ~h + (l == 0 ? 1ull : 0ull);
-    }
-    if ((h | l) == 0) return 0.0;
-    const int lz = h ? __clzll(static_cast<long long>(h)) : 64 + __clzll(static_cast<long long>(l));
-    unsigned long long top, rest;
-    if (lz == 0)
-    {
-        top = h;
-        rest = l;
-    }
-    else if (lz < 64)
-    {
-        top = (h << lz) | (l >> (64 - lz));
-        rest = l << lz;
-    }
-    else
-    {
-        top = l << (lz - 64);
-        rest = 0;
-    }
-    unsigned long long mant = top >> 11;
-    const unsigned long long rb = top & 0x7FFull;
-    if (rb > 0x400ull || (rb == 0x400ull && (rest != 0 || (mant & 1ull)))) ++mant;
-    int ex = 127 - lz + e0;
+    if (w == 0) return 0.0;
+    const unsigned long long sign = static_cast<unsigned long long>(w) & 0x8000000000000000ull;
+    const unsigned long long mag = static_cast<unsigned long long>(w < 0 ? -w : w);
+    const int lz = __clzll(static_cast<long long>(mag));
+    const unsigned long long norm = mag << lz;            // leading one at bit 63
+    unsigned long long mant = (norm >> 11) + ((norm >> 10) & 1ull);  // 53 bits, rounded
+    int be = 63 - lz + e0 + 1023;
     if (mant >> 53)
     {
         mant >>= 1;
-        ++ex;
+        ++be;
     }
-    const int be = ex + 1023;
     if (be <= 0) return 0.0;  // below the normal range: negligible next to the FP64 entries
-    const unsigned long long bits = (static_cast<unsigned long long>(neg) << 63) |
-                                    (static_cast<unsigned long long>(be) << 52) | (mant & 0xFFFFFFFFFFFFFull);
-    return __longlong_as_double(static_cast<long long>(bits));
+    return __longlong_as_double(
+        static_cast<long long>(sign | (static_cast<unsigned long long>(be) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 // One warp per panel row: row exponent and the 8 integer slices, by integer operations on the
@@ -257,7 +233,6 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     {
         if (lane == 0)
         {
-            constexpr uint32_t idesc = idesc_bf16_f32(OM, ON);
             bool ok = oz_wait(fullA, 0, abort_flag, err, 312);
             tc_fence_after();
             for (int t = 0; ok && t < cnt; ++t)
@@ -266,19 +241,21 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 if (!oz_wait(fullB + s, (t >> 1) & 1, abort_flag, err, 313)) break;
                 if (t >= 2 && !oz_wait(tempty + s, ((t >> 1) - 1) & 1, abort_flag, err, 314)) break;
                 tc_fence_after();
+                // The row-side slices of a stage are stacked (slice q at rows 32 q), so one MMA
+                // with N = 32 (8 - p) forms A_p B_q^T for every q <= 7 - p, and writing it at
+                // TMEM column 32 p puts each block into its group d = p + q.  The first MMA
+                // (p = 0, k = 0) spans all 8 groups and starts them from zero.
                 const uint32_t acc = tmem + s * ACC_COLS;
-                for (int d = 0; d < SL; ++d)
-                    for (int p = 0; p <= d; ++p)
-                    {
-                        const uint64_t da = smem_desc_sw128(sA + p * TILE_A);
-                        const uint64_t db = smem_desc_sw128(sB + s * STAGE_B + (d - p) * TILE_B);
+                const uint64_t db = smem_desc_sw128(sB + s * STAGE_B);
 #pragma unroll
-                        for (int k = 0; k < OK / 16; ++k)
-                        {
-                            const uint64_t dk = static_cast<uint64_t>(k * 32 >> 4);
-                            mma_bf16(acc + d * ON, da + dk, db + dk, idesc, (p == 0 && k == 0) ? 0u : 1u);
-                        }
-                    }
+                for (int k = 0; k < OK / 16; ++k)
+                {
+                    const uint64_t dk = static_cast<uint64_t>(k * 32 >> 4);
+#pragma unroll
+                    for (int p = 0; p < SL; ++p)
+                        mma_bf16(acc + p * ON, smem_desc_sw128(sA + p * TILE_A) + dk, db + dk,
+                                 idesc_bf16_f32(OM, ON * (SL - p)), (p == 0 && k == 0) ? 0u : 1u);
+                }
                 mma_commit(emptyB + s);
                 mma_commit(tfull + s);
             }
@@ -298,18 +275,23 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const int *E = Eall + static_cast<size_t>(b) * N;
         const int ej = j < N ? E[jl] : 0;
         double *Ab = Aall + static_cast<long long>(b) * N * N;
-        for (int t = 0; t < cnt; ++t)
-        {
-            const int s = t & 1;
+        // the EC entries of A this lane updates in tile t, read one tile ahead
+        auto load_a = [&](int t, double (&a)[EC]) {
             const int ib = s0 + (ti0 + t) * ON + part * EC;
-            // the EC entries of A this lane updates, read while the MMAs run
-            double av[EC];
 #pragma unroll
             for (int c = 0; c < EC; ++c)
             {
                 const int i = ib + c;
-                av[c] = (i < N && j < N && j <= i) ? Ab[static_cast<long long>(i) * N + j] : 0.0;
+                a[c] = (i < N && j < N && j <= i) ? Ab[static_cast<long long>(i) * N + j] : 0.0;
             }
+        };
+        double av[EC], an[EC];
+        load_a(0, av);
+        for (int t = 0; t < cnt; ++t)
+        {
+            const int s = t & 1;
+            const int ib = s0 + (ti0 + t) * ON + part * EC;
+            if (t + 1 < cnt) load_a(t + 1, an);
             const bool ok = __all_sync(0xffffffffu, oz_wait(tfull + s, (t >> 1) & 1, abort_flag, err, 315));
             if (!ok) break;
             tc_fence_after();
@@ -338,11 +320,16 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 const int ei = __shfl_sync(0xffffffffu, ei_own, c);
                 if (i < N && j < N && j <= i)
                 {
+                    // U = hi 2^28 + lo (value U 2^(e_i + e_j - 63), |U| < 2^69), kept as
+                    // W = U / 2^7 rounded: an absolute resolution of 2^-56 of the row scales
                     const long long hi = (static_cast<long long>(U[0][c]) << 14) + U[1][c];
                     const long long lo = (static_cast<long long>(U[2][c]) << 14) + U[3][c];
-                    Ab[static_cast<long long>(i) * N + j] = av[c] - fixed_to_double(hi, lo, ei + ej - 63);
+                    const long long w = (hi << 21) + ((lo + 64) >> 7);
+                    Ab[static_cast<long long>(i) * N + j] = av[c] - fixed_to_double(w, ei + ej - 56);
                 }
             }
+#pragma unroll
+            for (int c = 0; c < EC; ++c) av[c] = an[c];
         }
     }
     tc_fence_before();
