@@ -559,60 +559,81 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
 }
 
-// T2 for one (pair, cJ): out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i]
-__global__ void __launch_bounds__(256) k_t2(const float *__restrict__ X, long long xsign, Geom g, Pairs pr,
-                                           const T1Group *__restrict__ groups, double *__restrict__ out)
+// T2 for one (pair, cJ): out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i].
+// Per pass and chunk of i, the two operands are staged K-major in shared memory (K = (i, j)):
+// S1[k][mu] and S2[k][nu]; each thread accumulates a 4 x 4 block of (mu, nu) with two 16-byte
+// shared loads per 16 FMAs.  Blocks beyond 256 threads' worth loop over output block sets.
+constexpr int T2_THREADS = 256;
+constexpr int T2_SMEM_FLOATS = 12288;  // 48 KB
+
+__global__ void __launch_bounds__(T2_THREADS) k_t2(const float *__restrict__ X, long long xsign, Geom g, Pairs pr,
+                                                  const T1Group *__restrict__ groups, double *__restrict__ out)
 {
-    __shared__ float s1[128 * 32];
-    __shared__ float s2[128 * 32];
+    __shared__ __align__(16) float sm[T2_SMEM_FLOATS];
     const int p = groups[blockIdx.x].pair, cJ = groups[blockIdx.x].cell;
     const int I = pr.I[p], J = pr.J[p];
     const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
+    const int bIp = (bI + 3) & ~3, bJp = (bJ + 3) & ~3;
     const long long nsup = g.n_sup;
     const long long colJ = static_cast<long long>(cJ) * g.n_ao + g.ao_off[J];
     const long long colI = static_cast<long long>(g.cneg[cJ]) * g.n_ao + g.ao_off[I];
     double *o = out + pr.r_off[p] + static_cast<long long>(cJ) * bI * bJ;
-    const int nel = bI * bJ;
-    for (int e0 = 0; e0 < nel; e0 += 8 * 256)
+    // i per chunk so that both operands fit: (bIp + bJp) * ic * aJ floats
+    const int ic = max(1, min(aI, T2_SMEM_FLOATS / ((bIp + bJp) * aJ)));
+    float *S1 = sm;                            // [k][bIp]
+    float *S2 = sm + static_cast<size_t>(ic) * aJ * bIp;  // [k][bJp]
+    const int nmb = bIp / 4, nnb = bJp / 4, nblk = nmb * nnb;
+    for (int blk0 = 0; blk0 < nblk; blk0 += T2_THREADS)
     {
-        float acc[8];
-        for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+        const int blk = blk0 + static_cast<int>(threadIdx.x);
+        const int m0 = (blk / nnb) * 4, n0 = (blk % nnb) * 4;
+        float acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
         for (int pass = 0; pass < 2; ++pass)
         {
             const float *Xb = X + (pass == 0 ? xsign : 0);
             const float *Xa = X + (pass == 0 ? 0 : xsign);
-            for (int i = 0; i < aI; ++i)
+            for (int i0 = 0; i0 < aI; i0 += ic)
             {
+                const int ni = min(ic, aI - i0), nk = ni * aJ;
                 __syncthreads();
-                for (int t = threadIdx.x; t < bI * aJ; t += blockDim.x)
+                // S1[(i - i0) aJ + j][mu] = Xb[(I, mu, i)][(cJ, J, j)]  (j fastest: contiguous reads)
+                for (int t = threadIdx.x; t < bIp * nk; t += T2_THREADS)
                 {
-                    const int mu = t / aJ, j = t % aJ;
-                    s1[mu * 32 + j] = Xb[(g.rowc_off[I] + static_cast<long long>(mu) * aI + i) * nsup + colJ + j];
+                    const int mu = t / nk, k = t % nk, il = k / aJ, jj = k % aJ;
+                    S1[k * bIp + mu] =
+                        mu < bI ? Xb[(g.rowc_off[I] + static_cast<long long>(mu) * aI + i0 + il) * nsup + colJ + jj] : 0.f;
                 }
-                for (int t = threadIdx.x; t < bJ * aJ; t += blockDim.x)
+                // S2[(i - i0) aJ + j][nu] = Xa[(J, nu, j)][(-cJ, I, i)]  (i fastest)
+                for (int t = threadIdx.x; t < bJp * nk; t += T2_THREADS)
                 {
-                    const int nu = t / aJ, j = t % aJ;
-                    s2[nu * 32 + j] = Xa[(g.rowc_off[J] + static_cast<long long>(nu) * aJ + j) * nsup + colI + i];
+                    const int nu = t / nk, r = t % nk, jj = r / ni, il = r % ni;
+                    S2[(il * aJ + jj) * bJp + nu] =
+                        nu < bJ ? Xa[(g.rowc_off[J] + static_cast<long long>(nu) * aJ + jj) * nsup + colI + i0 + il] : 0.f;
                 }
                 __syncthreads();
-                for (int q = 0; q < 8; ++q)
-                {
-                    const int e = e0 + threadIdx.x + q * 256;
-                    if (e < nel)
+                if (blk < nblk)
+                    for (int k = 0; k < nk; ++k)
                     {
-                        const int mu = e / bJ, nu = e % bJ;
-                        float v = 0.f;
-                        for (int j = 0; j < aJ; ++j) v = fmaf(s1[mu * 32 + j], s2[nu * 32 + j], v);
-                        acc[q] += v;
+                        const float4 av = *reinterpret_cast<const float4 *>(S1 + k * bIp + m0);
+                        const float4 bv = *reinterpret_cast<const float4 *>(S2 + k * bJp + n0);
+                        const float a4[4] = {av.x, av.y, av.z, av.w}, b4[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+                        for (int a = 0; a < 4; ++a)
+#pragma unroll
+                            for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(a4[a], b4[b], acc[a][b]);
                     }
-                }
             }
         }
-        for (int q = 0; q < 8; ++q)
-        {
-            const int e = e0 + threadIdx.x + q * 256;
-            if (e < nel) o[e] += static_cast<double>(acc[q]);
-        }
+        if (blk < nblk)
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    if (m0 + a < bI && n0 + b < bJ) o[(m0 + a) * bJ + n0 + b] += static_cast<double>(acc[a][b]);
     }
 }
 
@@ -956,7 +977,7 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
         {
             t1_kernel(m.ra, m.ntc)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
             GB_LAUNCH_CHECK();
-            k_t2<<<m.n_groups, 256, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, m.groups.get(), chi0R);
+            k_t2<<<m.n_groups, T2_THREADS, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, m.groups.get(), chi0R);
             GB_LAUNCH_CHECK();
             launches += 2;
         }
