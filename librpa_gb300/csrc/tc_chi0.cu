@@ -142,6 +142,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     static_assert(2 * NBLK * NTC <= static_cast<int>(TMEM_COLS), "TMEM budget");
     constexpr int RP = rap(RA);
     constexpr bool BOTHX = RA <= 13;  // keep both passes' X values of a chunk in registers
+    constexpr bool STREAM = RA <= 16 && JG == 8;  // one chunk = both stages of up to 16 j
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int stage_bytes = NS * A_TILE;      // A ring stage
@@ -323,6 +324,106 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         };
         bool ok = true;
         int st_count = 0;
+        // split E into 3 BF16 pieces and store the 4 x 8 values (jl, column) of j group jh
+        auto store_e = [&](unsigned char *stg, int jh, const float2 (&e)[JH][2]) {
+#pragma unroll
+            for (int jl = 0; jl < JH; ++jl)
+            {
+                uint32_t h01, m01, l01, h23, m23, l23;
+                split3_pair(e[jl][0], h01, m01, l01);
+                split3_pair(e[jl][1], h23, m23, l23);
+                const uint32_t off = sw128_offset(r, (jh * JH + jl) * CW + cq * 4);
+                *reinterpret_cast<uint2 *>(stg + off) = make_uint2(h01, h23);
+                *reinterpret_cast<uint2 *>(stg + A_TILE + off) = make_uint2(m01, m23);
+                *reinterpret_cast<uint2 *>(stg + 2 * A_TILE + off) = make_uint2(l01, l23);
+            }
+        };
+        // the streaming path needs aligned 4-column X gathers (a.vec4); otherwise the chunk's
+        // columns may straddle cells and are gathered one by one below
+        if (STREAM && a.vec4)
+        {
+            // One chunk (both stages, all 16 j) per pass over its 2 RA rows (pass, i) of X.
+            // Row (pass, i) of chunk kc sits in xb[i] from RA steps before its use: reading
+            // pass 0 row i refills xb[i] with pass 1 row i, reading pass 1 row i refills it
+            // with pass 0 row i of chunk kc + 1, so the gathers stay half a chunk ahead.
+            const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+            auto chunk_base = [&](int kc, const float *&b0, const float *&b1) -> bool {
+                const long long col0 = static_cast<long long>(kc) * CW + cq * 4;
+                if (kc >= a.nkc || col0 >= nsup || !valid) return false;
+                const int cp = static_cast<int>(col0 / nao), ao = static_cast<int>(col0 % nao);
+                const long long src = static_cast<long long>(a.cadd[cp * nc + cJ]) * nao + ao;
+                b0 = Xp[0] + xrow * nsup + src;
+                b1 = Xp[1] + xrow * nsup + src;
+                return true;
+            };
+            auto ld = [&](const float *b, int i, bool live) -> float4 {
+                return (live && i < aI) ? __ldg(reinterpret_cast<const float4 *>(b + i * nsup)) : zero4;
+            };
+            const float *c0 = Xp[0], *c1 = Xp[0], *n0 = Xp[0], *n1 = Xp[0];
+            bool clive = chunk_base(0, c0, c1);
+            bool nlive = chunk_base(1, n0, n1);
+            float4 xb[RA];
+#pragma unroll
+            for (int i = 0; i < RA; ++i) xb[i] = ld(c0, i, clive);
+            for (int kc = 0; kc < a.nkc && ok; ++kc)
+            {
+                float2 e[4][JH][2];  // [group of 4 j][jl][column pair]: j 0..15
+#pragma unroll
+                for (int jh = 0; jh < 4; ++jh)
+#pragma unroll
+                    for (int jl = 0; jl < JH; ++jl) e[jh][jl][0] = e[jh][jl][1] = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int pass = 0; pass < 2; ++pass)
+                {
+#pragma unroll
+                    for (int i = 0; i < RA; ++i)
+                    {
+                        const float4 x = xb[i];
+                        xb[i] = pass == 0 ? ld(c1, i, clive) : ld(n0, i, nlive);
+                        const float2 xa = make_float2(x.x, x.y), xc = make_float2(x.z, x.w);
+#pragma unroll
+                        for (int jh = 0; jh < 4; ++jh)
+                        {
+                            const float4 gg = gp[pass][(i * gst + jh * JH) / 4];
+                            const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
+#pragma unroll
+                            for (int q = 0; q < 4; ++q)
+                            {
+                                const float2 gq = make_float2(gv[q], gv[q]);
+                                e[jh][q][0] = __ffma2_rn(gq, xa, e[jh][q][0]);
+                                e[jh][q][1] = __ffma2_rn(gq, xc, e[jh][q][1]);
+                            }
+                        }
+                    }
+                }
+                c0 = n0;
+                c1 = n1;
+                clive = nlive;
+                nlive = chunk_base(kc + 2, n0, n1);
+                // stage (kc, jg) holds j [8 jg, 8 jg + 8): the groups of 4 j are 2 jg and 2 jg + 1
+#pragma unroll
+                for (int jg = 0; jg < 2; ++jg)
+                {
+                    if (jg >= njg || !ok) break;
+                    const int s = st_count % T1_STAGES, rr = st_count / T1_STAGES;
+                    ++st_count;
+                    unsigned char *stg = smem + s * stage_bytes;
+                    if (!__all_sync(0xffffffffu, mbar_wait(&empty[s], (rr & 1) ^ 1)))
+                    {
+                        if (lane == 0) atomicExch(a.err, 201);
+                        ok = false;
+                        break;
+                    }
+                    store_e(stg, 0, e[2 * jg]);
+                    store_e(stg, 1, e[2 * jg + 1]);
+                    fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&full[s]);
+                }
+            }
+        }
+        else
+        {
         float4 x0[RA], x1[BOTHX ? RA : 1];
         for (int kc = 0; kc < a.nkc && ok; ++kc)
         {
@@ -379,6 +480,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
             }
         }
     }
+        }
     else
     {
         // ---------------- warps 8-11: per-stage accumulator blocks -> FP32 registers -> chi0R.
@@ -836,7 +938,7 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     m.maxcj = (T1_BM + minb - 1) / minb + 1;
     m.ra = g.max_nao == 13 ? 13 : g.max_nao <= 16 ? 16 : 32;
     m.ntc = ntmax <= 64 ? 64 : 128;
-    m.gj = JG;
+    m.gj = 2 * JG;  // the streaming producers read 16 values of j per row i
     for (int J = 0; J < g.n_at; ++J) m.gj = std::max(m.gj, ajp[J]);
     // shared memory: A ring + at least two B stages + the G slots; fewer G slots than a tile of
     // small row groups could touch only shortens such tiles
