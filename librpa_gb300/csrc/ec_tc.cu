@@ -46,11 +46,11 @@ __global__ void k_embed_A(const cuDoubleComplex *__restrict__ src, long long sst
         double x = 0.0;
         if (col < 2 * K)
         {
-            const int r = row < M ? row : row - M;
-            const int k = col < K ? col : col - K;
+            // rows and K both interleaved: row 2 r + (0: Re, 1: Im), column 2 k + (0: Re, 1: Im)
+            const int r = row >> 1, k = col >> 1;
             cuDoubleComplex v = ctrans ? S[static_cast<long long>(k) * M + r] : S[static_cast<long long>(r) * K + k];
             if (ctrans) v.y = -v.y;
-            const bool top = row < M, left = col < K;
+            const bool top = (row & 1) == 0, left = (col & 1) == 0;
             x = top ? (left ? v.x : -v.y) : (left ? v.y : v.x);
         }
         __nv_bfloat16 h, m, l;
@@ -75,9 +75,9 @@ __global__ void k_embed_Bt(const cuDoubleComplex *__restrict__ Y, int K, int N, 
         double x = 0.0;
         if (col < 2 * K)
         {
-            const int k = col < K ? col : col - K;
+            const int k = col >> 1;  // K interleaved: 2 k + (0: Re, 1: Im)
             const cuDoubleComplex v = Y[static_cast<long long>(k) * N + row];
-            x = col < K ? v.x : v.y;
+            x = (col & 1) == 0 ? v.x : v.y;
         }
         __nv_bfloat16 h, m, l;
         split3(x, h, m, l);
@@ -117,7 +117,8 @@ __global__ void k_split_T_f32(const float *__restrict__ S, long long sstride, in
     }
 }
 
-// M'[b] = I - (Mstack real part + i imag part), Mstack = [Re; Im] (2N x N FP32)
+// M'[b] = I - (Re M + i Im M), the FP32 product with interleaved rows: row 2 i = Re M(i, :),
+// row 2 i + 1 = Im M(i, :) (2N x N)
 __global__ void k_form_mprime_c(const float *__restrict__ Ms, int N, cuDoubleComplex *__restrict__ Mp)
 {
     const int b = blockIdx.y;
@@ -127,8 +128,9 @@ __global__ void k_form_mprime_c(const float *__restrict__ Ms, int N, cuDoubleCom
     for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
          e += static_cast<long long>(gridDim.x) * blockDim.x)
     {
-        const bool d = (e / N) == (e % N);
-        O[e] = make_cuDoubleComplex((d ? 1.0 : 0.0) - static_cast<double>(S[e]), -static_cast<double>(S[nn + e]));
+        const long long i = e / N, j = e % N;
+        const float *row = S + 2 * i * N + j;
+        O[e] = make_cuDoubleComplex((i == j ? 1.0 : 0.0) - static_cast<double>(row[0]), -static_cast<double>(row[N]));
     }
 }
 
@@ -158,10 +160,11 @@ __global__ void k_diag_trace(const float *__restrict__ Ms, int N, int parts, dou
     const long long nn = static_cast<long long>(N) * N;
     const float *S = Ms + static_cast<long long>(blockIdx.x) * parts * nn;
     double ar = 0.0, ai = 0.0;
+    // rows interleaved by part: row parts * i (+ 1) holds Re (Im) of row i
     for (int i = threadIdx.x; i < N; i += blockDim.x)
     {
-        ar += S[static_cast<long long>(i) * N + i];
-        if (parts > 1) ai += S[nn + static_cast<long long>(i) * N + i];
+        ar += S[static_cast<long long>(parts) * i * N + i];
+        if (parts > 1) ai += S[(static_cast<long long>(parts) * i + 1) * N + i];
     }
     rr[threadIdx.x] = ar;
     ri[threadIdx.x] = ai;
@@ -418,15 +421,15 @@ int EcChol::stage_q(const void *L, const void *X, int slot, cudaStream_t st)
         }
         launches += 2 + nw;
     }
-    // T = chi0 L  (rowsA x N per w); real path: L is lower triangular, so the K range of an
-    // output column block n starts at n
+    // T = chi0 L  (rowsA x N per w); L is lower triangular, so the K range of an output column
+    // block n starts at n (at 2n with the complex path's interleaved K)
     TcGemmOpts o1, o2;
-    if (!m.cplx)
-    {
-        o1.tri = 1;
-        o2.tri = 2;             // A = L^T: row m is zero before column m
+    o1.tri = 1;
+    o2.tri = 2;  // A = L^H: row m is zero before column m (interleaved: row 2m + p before K 2m)
+    if (m.cplx)
+        o1.tri_mul = 2;  // K interleaved: L(:, n) is zero before K index 2n
+    else
         o2.lower_tiles = true;  // M is symmetric: its lower triangle is all that is read
-    }
     tc_gemm_split(m.A1.mat(rowsA, m.kpad, rowsA * m.kpad), m.Bl.mat(N, m.kpad, 0), static_cast<int>(rowsA), N,
                   static_cast<int>(m.cplx ? 2 * N : N), nw, m.Tst.get(), N, rowsA * N, false, m.err.get(), st, o1);
     // B2 = K-major form of T (row n = T(:, n))

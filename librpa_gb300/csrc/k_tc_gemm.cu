@@ -105,7 +105,8 @@ __device__ __forceinline__ void tile_coords(int t, int ntm, int ntn, int lower, 
 template <int NS>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     k_tc_gemm(const __grid_constant__ TmapSet maps, int M, int N, int K, float *__restrict__ D, long long ldd,
-              long long sD, int accumulate_out, int a_bcast, int b_bcast, int tri, int lower, int *__restrict__ err)
+              long long sD, int accumulate_out, int a_bcast, int b_bcast, int tri, int tri_mul, int lower,
+              int *__restrict__ err)
 {
     constexpr int STAGES = Cfg<NS>::STAGES, STAGE_BYTES = Cfg<NS>::STAGE_BYTES;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -121,8 +122,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tile_coords(blockIdx.x, (M + BM - 1) / BM, (N + BN - 1) / BN, lower, mt, nt);
     const int n0 = nt * BN, m0 = mt * BM, b = blockIdx.z;
     const int nk = (K + BK - 1) / BK;
-    // K blocks that can be nonzero: B[n][k] = 0 for k < n (tri 1), A[m][k] = 0 for k < m (tri 2)
-    const int kb0 = tri == 1 ? n0 / BK : (tri == 2 ? m0 / BK : 0);
+    // K blocks that can be nonzero: B[n][k] = 0 for k < tri_mul n (tri 1), A[m][k] = 0 for k < m
+    // (tri 2)
+    const int kb0 = tri == 1 ? tri_mul * n0 / BK : (tri == 2 ? m0 / BK : 0);
     const int nsteps = nk - kb0;
 
     if (threadIdx.x == 0)
@@ -399,12 +401,13 @@ static void launch_tc(const SplitMat &A, const SplitMat &B, int M, int N, int K,
     const long long ntm = (M + BM - 1) / BM, ntn = (N + BN - 1) / BN;
     GB_REQUIRE(!o.lower_tiles || ntm == ntn, "lower-tile GEMM needs a square tile grid");
     GB_REQUIRE(o.tri >= 0 && o.tri <= 2, "triangular operand mode must be 0, 1 or 2");
-    GB_REQUIRE(o.tri == 0 || K >= (o.tri == 1 ? N : M), "triangular operand shorter than its K range");
+    GB_REQUIRE(o.tri_mul == 1 || o.tri_mul == 2, "triangular K multiplier must be 1 or 2");
+    GB_REQUIRE(o.tri == 0 || K >= (o.tri == 1 ? o.tri_mul * N : M), "triangular operand shorter than its K range");
     const long long tiles = o.lower_tiles ? ntm * (ntm + 1) / 2 : ntm * ntn;
     dim3 grid(static_cast<unsigned>(tiles), 1, batch);
     k_tc_gemm<NS><<<grid, GEMM_THREADS, Cfg<NS>::SMEM_BYTES, st>>>(maps, M, N, K, D, ldd, sD, accumulate ? 1 : 0,
                                                           A.batch_stride == 0, B.batch_stride == 0, o.tri,
-                                                          o.lower_tiles ? 1 : 0, err);
+                                                          o.tri_mul, o.lower_tiles ? 1 : 0, err);
     GB_LAUNCH_CHECK();
 }
 

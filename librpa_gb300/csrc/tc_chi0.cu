@@ -389,6 +389,8 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
 #pragma unroll
                             for (int q = 0; q < 4; ++q)
                             {
+                                // RA = 13: no atom has more than 13 NAOs, j = 13..15 stay zero
+                                if (RA == 13 && 4 * jh + q >= 13) continue;
                                 const float2 gq = make_float2(gv[q], gv[q]);
                                 e[jh][q][0] = __ffma2_rn(gq, xa, e[jh][q][0]);
                                 e[jh][q][1] = __ffma2_rn(gq, xc, e[jh][q][1]);

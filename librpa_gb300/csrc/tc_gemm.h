@@ -69,6 +69,7 @@ void split_transpose_f64(const double *src, long long lds, int K, int N, int kpa
 struct TcGemmOpts
 {
     int tri = 0;
+    int tri_mul = 1;  // tri = 1: B[n][k] = 0 for k < tri_mul * n (2 for interleaved complex K)
     bool lower_tiles = false;
 };
 // D[b] (+)= A[b] * B[b]^T from BF16 split pieces (ns = 2: 3 products, ns = 3: 6 products),
