@@ -134,6 +134,33 @@ __global__ void k_form_mprime_c(const float *__restrict__ Ms, int N, cuDoubleCom
     }
 }
 
+// Real embedding of M' = I - M for the tensor-core Cholesky: E[2i + p][2j + q] =
+// [[Re M'_ij, -Im M'_ij], [Im M'_ij, Re M'_ij]][p][q], lower triangle only (upper zero);
+// Ms has interleaved rows (2 i: Re M(i, :), 2 i + 1: Im M(i, :)).  E is symmetric positive
+// definite when M' is Hermitian positive definite, and ln det E = 2 ln det M'.
+__global__ void k_form_mprime_emb(const float *__restrict__ Ms, int N, double *__restrict__ Ep)
+{
+    const int b = blockIdx.y;
+    const long long nn = static_cast<long long>(N) * N, n2 = 2LL * N;
+    const float *S = Ms + b * 2 * nn;
+    double *O = Ep + b * n2 * n2;
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < n2 * n2;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long r = e / n2, c = e % n2;
+        const long long i = r >> 1, j = c >> 1;
+        const int p = static_cast<int>(r & 1), q = static_cast<int>(c & 1);
+        double v = 0.0;
+        if (c <= r)
+        {
+            const double re = (i == j ? 1.0 : 0.0) - static_cast<double>(S[2 * i * N + j]);
+            const double im = -static_cast<double>(S[(2 * i + 1) * N + j]);
+            v = p == q ? re : (p == 1 ? im : -im);
+        }
+        O[e] = v;
+    }
+}
+
 __global__ void k_form_mprime_r(const float *__restrict__ Ms, int N, double *__restrict__ Mp)
 {
     const int b = blockIdx.y;
@@ -267,8 +294,9 @@ struct EcChol::Impl
     DevBuf<double2> tr;
     DevBuf<cuDoubleComplex> Mpc;
     DevBuf<double> Mpr;
-    // real matrices: Cholesky trailing updates on the tensor cores (exact integer slices)
-    bool ozaki = false;
+    // real matrices: Cholesky trailing updates on the tensor cores (exact integer slices);
+    // complex M' is factored as its real 2N x 2N embedding (emb) by the same kernels
+    bool ozaki = false, emb = false;
     OzakiWork oz;
     ~Impl() { ozaki_free(oz); }
 };
@@ -289,15 +317,21 @@ EcChol::EcChol(int N, int nw, bool complex_path, int qb, bool fp64_products) : i
     m.bad.alloc(nmat);
     m.badV.alloc(qb);
     m.diagV.alloc(static_cast<size_t>(qb) * N);
-    m.diag.alloc(nmat * N);
+    m.emb = complex_path && !fp64_products && N > OZAKI_NB / 2;
+    const size_t ndiag = m.emb ? 2 * static_cast<size_t>(N) : N;
+    m.diag.alloc(nmat * ndiag);
     m.logdet.alloc(nmat);
     m.tr.alloc(nmat);
-    if (complex_path)
+    if (m.emb)
+        m.Mpr.alloc(nmat * 4 * N * N);
+    else if (complex_path)
         m.Mpc.alloc(nmat * N * N);
     else
         m.Mpr.alloc(nmat * N * N);
+    // V (one per q) and, for real matrices, M' go through the tensor-core Cholesky
     m.ozaki = !complex_path && !fp64_products && N > OZAKI_NB;
     if (m.ozaki) ozaki_alloc(m.oz, N, static_cast<int>(nmat));
+    if (m.emb) ozaki_alloc(m.oz, 2 * N, static_cast<int>(nmat));
     if (fp64_products)
     {
         const size_t nn = static_cast<size_t>(N) * N;
@@ -447,7 +481,9 @@ int EcChol::stage_q(const void *L, const void *X, int slot, cudaStream_t st)
     k_diag_trace<<<nw, 256, 0, st>>>(m.Mst.get(), N, m.cplx ? 2 : 1, m.tr.get() + static_cast<size_t>(slot) * nw);
     GB_LAUNCH_CHECK();
     const size_t off = static_cast<size_t>(slot) * nw * nn;
-    if (m.cplx)
+    if (m.emb)
+        k_form_mprime_emb<<<dim3(blocks_for(4 * nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpr.get() + 4 * off);
+    else if (m.cplx)
         k_form_mprime_c<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpc.get() + off);
     else
         k_form_mprime_r<<<dim3(blocks_for(nn), nw), 256, 0, st>>>(m.Mst.get(), N, m.Mpr.get() + off);
@@ -463,12 +499,14 @@ int EcChol::finish(int nslots, std::vector<std::complex<double>> &trace_out,
     GB_REQUIRE(nslots >= 1 && nslots <= m.qb, "E_c batch slot count out of range");
     const int nmat = nslots * m.nw;
     int launches = 1;
-    if (m.cplx)
+    if (m.emb)
+        launches += chol_batched_r_ozaki(m.Mpr.get(), 2 * N, nmat, m.diag.get(), m.bad.get(), m.oz, st);
+    else if (m.cplx)
         launches += chol_batched_c(m.Mpc.get(), N, nmat, m.diag.get(), m.bad.get(), st);
     else
         launches += m.ozaki ? chol_batched_r_ozaki(m.Mpr.get(), N, nmat, m.diag.get(), m.bad.get(), m.oz, st)
                             : chol_batched_r(m.Mpr.get(), N, nmat, m.diag.get(), m.bad.get(), st);
-    chol_logdet(m.diag.get(), N, nmat, m.logdet.get(), st);
+    chol_logdet(m.diag.get(), m.emb ? 2 * N : N, nmat, m.logdet.get(), st);
     std::vector<double> ld(nmat);
     std::vector<int> bad(nmat);
     std::vector<double2> tr(nmat);
@@ -478,7 +516,7 @@ int EcChol::finish(int nslots, std::vector<std::complex<double>> &trace_out,
     m.tr.download(tr.data(), nmat, st);
     int herr_oz = 0;
     m.err.download(&herr, 1, st);
-    if (m.ozaki) GB_CUDA(cudaMemcpyAsync(&herr_oz, m.oz.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (m.ozaki || m.emb) GB_CUDA(cudaMemcpyAsync(&herr_oz, m.oz.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
     GB_REQUIRE(herr == 0, "tensor-core E_c GEMM reported wait timeout code " + std::to_string(herr));
     GB_REQUIRE(herr_oz == 0, "tensor-core Cholesky update reported wait timeout code " + std::to_string(herr_oz));
@@ -489,7 +527,7 @@ int EcChol::finish(int nslots, std::vector<std::complex<double>> &trace_out,
     for (int b = 0; b < nmat; ++b)
     {
         trace_out[b] = {tr[b].x, m.cplx ? tr[b].y : 0.0};
-        logdet_out[b] = {ld[b], 0.0};
+        logdet_out[b] = {m.emb ? 0.5 * ld[b] : ld[b], 0.0};  // ln det E = 2 ln det M'
     }
     return launches;
 }

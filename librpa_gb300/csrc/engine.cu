@@ -735,7 +735,8 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         // cores, then one batched FP64 Cholesky of all the M'; q points go in batches that keep
         // the M' store within about 24 GB
         const size_t esz = gamma_only ? sizeof(double) : sizeof(cuDoubleComplex);
-        const double per_q = static_cast<double>(nw + 1) * NN * esz;
+        // complex M' is factored as its real 2N x 2N embedding: 32 bytes per element of M'
+        const double per_q = static_cast<double>(nw) * NN * (gamma_only ? esz : 2 * esz) + NN * esz;
         const int qb = std::max(1, std::min(nq, static_cast<int>(24.0e9 / per_q)));
         EcChol ecc(N, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
         DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
