@@ -15,6 +15,7 @@
 #include <map>
 #include <mutex>
 #include <sstream>
+#include <tuple>
 
 #include "common.h"
 
@@ -242,7 +243,29 @@ std::string minimax_table_path()
     return "data/greenx_minimax_tables.txt";
 }
 
+static TimeFreqGrids minimax_grids_uncached(int n, double emin, double emax, double reg);
+
+// The grids are a pure function of (n, e_min, e_max, regularisation): repeated E_c calls on the
+// same system reuse the last few results instead of refitting (the fit costs tens of ms).
 TimeFreqGrids minimax_grids(int n, double emin, double emax, double reg)
+{
+    using Key = std::tuple<int, double, double, double>;
+    static std::mutex mu;
+    static std::map<Key, TimeFreqGrids> cache;
+    const Key key{n, emin, emax, reg};
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    TimeFreqGrids g = minimax_grids_uncached(n, emin, emax, reg);
+    std::lock_guard<std::mutex> lk(mu);
+    if (cache.size() >= 16) cache.clear();
+    cache.emplace(key, g);
+    return g;
+}
+
+static TimeFreqGrids minimax_grids_uncached(int n, double emin, double emax, double reg)
 {
     GB_REQUIRE(emin > 0 && emax > emin, "minimax grid needs 0 < e_min < e_max");
     const Tables &t = load_tables(minimax_table_path());
