@@ -91,11 +91,15 @@ __global__ void __launch_bounds__(256) k_chol_diag(T *__restrict__ Aall, int N, 
     for (int i = threadIdx.x; i < nb; i += blockDim.x) diag[static_cast<long long>(b) * N + k0 + i] = cre(D[i][i]);
 }
 
-// Panel solve X L11^H = A21 for a 64-row slab per CTA (L11 already factored in A).
+// Panel solve X L11^H = A21 for a 64-row slab per CTA (L11 already factored in A).  Full
+// panels run right-looking with the row in registers (x[p] /= L_pp, then x[q] -= x[p] conj L_qp
+// for every q > p: independent updates instead of one serial sum per p) and the reciprocal
+// diagonal precomputed once per CTA.
 template <typename T, int NBT>
 __global__ void __launch_bounds__(64) k_chol_panel(T *__restrict__ Aall, int N, int k0)
 {
     __shared__ T D[NBT][NBT + 1];
+    __shared__ double invd[NBT];
     const int b = blockIdx.y;
     T *A = Aall + static_cast<long long>(b) * N * N;
     const int nb = min(NBT, N - k0);
@@ -105,17 +109,36 @@ __global__ void __launch_bounds__(64) k_chol_panel(T *__restrict__ Aall, int N, 
         D[i][j] = j <= i ? A[static_cast<long long>(k0 + i) * N + k0 + j] : czero<T>();
     }
     __syncthreads();
+    for (int p = threadIdx.x; p < nb; p += blockDim.x) invd[p] = 1.0 / cre(D[p][p]);
+    __syncthreads();
     const int r = k0 + nb + blockIdx.x * 64 + threadIdx.x;
     if (r >= N) return;
+    T *row = A + static_cast<long long>(r) * N + k0;
+    if (nb == NBT)
+    {
+        T x[NBT];
+#pragma unroll
+        for (int p = 0; p < NBT; ++p) x[p] = row[p];
+#pragma unroll
+        for (int p = 0; p < NBT; ++p)
+        {
+            x[p] = cscale(x[p], invd[p]);
+#pragma unroll
+            for (int q = p + 1; q < NBT; ++q) x[q] = csub(x[q], cconjmul_acc(czero<T>(), x[p], D[q][p]));
+        }
+#pragma unroll
+        for (int p = 0; p < NBT; ++p) row[p] = x[p];
+        return;
+    }
     T x[NBT];
-    for (int p = 0; p < nb; ++p) x[p] = A[static_cast<long long>(r) * N + k0 + p];
+    for (int p = 0; p < nb; ++p) x[p] = row[p];
     for (int p = 0; p < nb; ++p)
     {
         T s = x[p];
         for (int q = 0; q < p; ++q) s = csub(s, cconjmul_acc(czero<T>(), x[q], D[p][q]));
-        x[p] = cscale(s, 1.0 / cre(D[p][p]));
+        x[p] = cscale(s, invd[p]);
     }
-    for (int p = 0; p < nb; ++p) A[static_cast<long long>(r) * N + k0 + p] = x[p];
+    for (int p = 0; p < nb; ++p) row[p] = x[p];
 }
 
 // Trailing update of the lower triangle, 32 x 32 tiles (ti >= tj), K = panel width.
