@@ -153,12 +153,14 @@ int librpa_gb300_device_count(void);
  * CUDA-core GEMM.  Returns max|diff| / max|ref| (NaN on error). */
 double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces);
 
-/* Diagnostic: `batch` random N x N SPD matrices (condition spread by a diagonal scaling of
- * spread_decades decades) factored by the FP64 CUDA-core Cholesky and by the variant whose
- * trailing updates run on the tensor cores as exact 7-bit integer slice products.  Returns
- * the largest |ln det difference| (NaN on error); *max_rel_l (may be NULL) receives
+/* Diagnostic: `batch` random N x N SPD matrices D (X X^T / N + shift I) D (X uniform, D a
+ * diagonal scaling spread over spread_decades decades; a small shift makes them ill-conditioned)
+ * factored by the FP64 CUDA-core Cholesky and by the variant whose panel solves and trailing
+ * updates run on the tensor cores as exact 7-bit integer slice products.  Returns the largest
+ * |ln det difference| (NaN on error); *max_rel_l (may be NULL) receives
  * max |L difference| / max |L|. */
-double librpa_gb300_selftest_chol_ozaki(int N, int batch, int seed, int spread_decades, double *max_rel_l);
+double librpa_gb300_selftest_chol_ozaki(int N, int batch, int seed, int spread_decades, double shift,
+                                        double *max_rel_l);
 
 /* No counterpart in the reference.  D = A * B through the tcgen05 split-precision GEMM
  * (pieces = 2 or 3, as above) without allocating device memory, for callers that cannot

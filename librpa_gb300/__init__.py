@@ -186,7 +186,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_get_chi0_block": (i, [vp, i, i, i, i, _dp, _dp]),
         "librpa_gb300_device_count": (i, []),
         "librpa_gb300_selftest_tc_gemm": (d, [i, i, i, i, i]),
-        "librpa_gb300_selftest_chol_ozaki": (d, [i, i, i, i, C.POINTER(C.c_double)]),
+        "librpa_gb300_selftest_chol_ozaki": (d, [i, i, i, i, d, C.POINTER(C.c_double)]),
         "librpa_gb300_tc_gemm_noalloc": (i, [i, i, i, C.c_void_p, C.c_void_p, C.c_void_p, i,
                                              C.c_void_p]),
         "librpa_gb300_train_screening": (i, [vp, i, d, C.POINTER(C.c_double)]),

@@ -882,13 +882,14 @@ double librpa_gb300_selftest_tc_gemm(int M, int N, int K, int seed, int pieces)
     return r;
 }
 
-double librpa_gb300_selftest_chol_ozaki(int N, int batch, int seed, int spread_decades, double *max_rel_l)
+double librpa_gb300_selftest_chol_ozaki(int N, int batch, int seed, int spread_decades, double shift, double *max_rel_l)
 {
     double r = std::numeric_limits<double>::quiet_NaN();
     guarded(nullptr, [&] {
         GB_REQUIRE(gb::device_count() > 0, "no CUDA device visible");
         GB_REQUIRE(N > 0 && batch > 0, "N and batch must be positive");
-        r = gb::chol_ozaki_selftest(N, batch, seed, spread_decades, max_rel_l);
+        GB_REQUIRE(shift > 0.0, "the diagonal shift must be positive");
+        r = gb::chol_ozaki_selftest(N, batch, seed, spread_decades, shift, max_rel_l);
     });
     return r;
 }

@@ -91,6 +91,49 @@ __global__ void __launch_bounds__(256) k_chol_diag(T *__restrict__ Aall, int N, 
     for (int i = threadIdx.x; i < nb; i += blockDim.x) diag[static_cast<long long>(b) * N + k0 + i] = cre(D[i][i]);
 }
 
+// Real diagonal block for the tensor-core panel solve: factor L11 as k_chol_diag does and also
+// form W = L11^-1 (lower triangular, FP64) into Wb[b][64][64], so that the panel becomes the
+// product L21 = A21 W^T.  Thread c (< nb) builds column c of W by forward substitution,
+// W_cc = 1 / L_cc, W_ic = -(sum_{k=c}^{i-1} L_ik W_kc) / L_ii.  Dynamic shared memory: D, W.
+constexpr int DINV_SMEM = 2 * OZAKI_NB * (OZAKI_NB + 1) * static_cast<int>(sizeof(double));
+__global__ void __launch_bounds__(256) k_chol_diag_inv(double *__restrict__ Aall, int N, int k0,
+                                                      double *__restrict__ diag, int *__restrict__ bad,
+                                                      double *__restrict__ Wb)
+{
+    constexpr int NBT = OZAKI_NB;
+    extern __shared__ double dsm[];
+    double (*D)[NBT + 1] = reinterpret_cast<double (*)[NBT + 1]>(dsm);
+    double (*W)[NBT + 1] = reinterpret_cast<double (*)[NBT + 1]>(dsm + NBT * (NBT + 1));
+    const int b = blockIdx.x;
+    double *A = Aall + static_cast<long long>(b) * N * N;
+    const int nb = min(NBT, N - k0);
+    factor_diag<double, NBT>(A, N, k0, nb, D, bad + b);
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x)
+    {
+        const int i = t / nb, j = t % nb;
+        if (j <= i) A[static_cast<long long>(k0 + i) * N + k0 + j] = D[i][j];
+    }
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) diag[static_cast<long long>(b) * N + k0 + i] = D[i][i];
+    const int c = threadIdx.x;
+    if (c < nb)
+    {
+        W[c][c] = 1.0 / D[c][c];
+        for (int i = c + 1; i < nb; ++i)
+        {
+            double sacc = 0.0;
+            for (int k = c; k < i; ++k) sacc = fma(D[i][k], W[k][c], sacc);
+            W[i][c] = -sacc / D[i][i];
+        }
+    }
+    __syncthreads();
+    double *Wo = Wb + static_cast<long long>(b) * NBT * NBT;
+    for (int t = threadIdx.x; t < NBT * NBT; t += blockDim.x)
+    {
+        const int i = t / NBT, j = t % NBT;
+        Wo[t] = (i < nb && j <= i) ? W[i][j] : 0.0;
+    }
+}
+
 // Panel solve X L11^H = A21 for a 64-row slab per CTA (L11 already factored in A).  Full
 // panels run right-looking with the row in registers (x[p] /= L_pp, then x[q] -= x[p] conj L_qp
 // for every q > p: independent updates instead of one serial sum per p) and the reciprocal
@@ -255,21 +298,29 @@ int chol_batched_r(double *A, int N, int batch, double *diag, int *bad, cudaStre
 int chol_batched_r_ozaki(double *A, int N, int batch, double *diag, int *bad, OzakiWork &w, cudaStream_t st)
 {
     constexpr int NBO = OZAKI_NB;
+    static bool attr = false;
+    if (!attr)
+    {
+        GB_CUDA(cudaFuncSetAttribute(k_chol_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, DINV_SMEM));
+        attr = true;
+    }
     int launches = 0;
     for (int k0 = 0; k0 < N; k0 += NBO)
     {
         const int nb = std::min(NBO, N - k0);
         const int rows_below = N - k0 - nb;
-        k_chol_diag<double, NBO><<<batch, 256, 0, st>>>(A, N, k0, diag, bad);
-        GB_LAUNCH_CHECK();
-        ++launches;
-        if (rows_below > 0)
+        if (rows_below == 0)
         {
-            dim3 gp((rows_below + 63) / 64, batch);
-            k_chol_panel<double, NBO><<<gp, 64, 0, st>>>(A, N, k0);
+            k_chol_diag<double, NBO><<<batch, 256, 0, st>>>(A, N, k0, diag, bad);
             GB_LAUNCH_CHECK();
-            launches += 1 + ozaki_trailing_update(A, N, batch, k0 + nb, k0, nb, w, st);
+            ++launches;
+            continue;
         }
+        // every panel with rows below it is a full 64-wide one (panels step by 64)
+        k_chol_diag_inv<<<batch, 256, DINV_SMEM, st>>>(A, N, k0, diag, bad, w.winv);
+        GB_LAUNCH_CHECK();
+        launches += 1 + ozaki_panel_solve(A, N, batch, k0, w, st);
+        launches += ozaki_trailing_update(A, N, batch, k0 + nb, k0, nb, w, st);
     }
     return launches;
 }

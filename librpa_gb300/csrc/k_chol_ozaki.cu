@@ -89,17 +89,19 @@ __device__ __forceinline__ double fixed_to_double(long long w, int e0)
         static_cast<long long>(sign | (static_cast<unsigned long long>(be) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
-// One warp per panel row: row exponent and the 8 integer slices, by integer operations on the
-// FP64 bit patterns (the digits of |v| 2^56, v = x 2^-e; subnormal entries count as zero).
-__global__ void k_ozaki_slice(const double *__restrict__ A, int N, int s0, int k0, int nb,
-                              __nv_bfloat16 *__restrict__ S, int *__restrict__ E)
+// One warp per row: row exponent and the 8 integer slices, by integer operations on the FP64 bit
+// patterns (the digits of |v| 2^56, v = x 2^-e; subnormal entries count as zero).  Row rl of the
+// slab is A[b][row0 + rl][col0 .. col0 + nb) (matrices bstride elements apart, row stride lda);
+// its slices go to S[b][p][rl][0..64) with dst_rows rows per slice plane, its exponent to
+// E[b * dst_rows + rl].
+__global__ void k_ozaki_slice(const double *__restrict__ A, long long bstride, int lda, int row0, int col0, int nb,
+                              int R, __nv_bfloat16 *__restrict__ S, int *__restrict__ E, int dst_rows)
 {
     const int b = blockIdx.y;
-    const int rl = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;  // row inside the panel
+    const int rl = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;  // row inside the slab
     const int lane = threadIdx.x % 32;
-    const int R = N - s0;
     if (rl >= R) return;
-    const double *row = A + static_cast<long long>(b) * N * N + static_cast<long long>(s0 + rl) * N + k0;
+    const double *row = A + static_cast<long long>(b) * bstride + static_cast<long long>(row0 + rl) * lda + col0;
     unsigned long long u[2];
     unsigned long long m = 0;
 #pragma unroll
@@ -112,7 +114,7 @@ __global__ void k_ozaki_slice(const double *__restrict__ A, int N, int s0, int k
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
     const int mexp = static_cast<int>(m >> 52);  // biased exponent of the row maximum
     const int e = mexp ? mexp - 1022 : 0;       // max < 2^e
-    const size_t plane = static_cast<size_t>(N) * OK;
+    const size_t plane = static_cast<size_t>(dst_rows) * OK;
     __nv_bfloat16 *Sb = S + static_cast<size_t>(b) * SL * plane + static_cast<size_t>(rl) * OK;
 #pragma unroll
     for (int h = 0; h < 2; ++h)
@@ -134,7 +136,7 @@ __global__ void k_ozaki_slice(const double *__restrict__ A, int N, int s0, int k
             Sb[p * plane + c] = __float2bfloat16_rn(static_cast<float>(neg ? -dgt : dgt));
         }
     }
-    if (lane == 0) E[static_cast<size_t>(b) * N + rl] = e;
+    if (lane == 0) E[static_cast<size_t>(b) * dst_rows + rl] = e;
 }
 
 // Work item t -> (column block jm, first row tile, row tile count)
@@ -165,9 +167,14 @@ __device__ __forceinline__ bool oz_wait(uint64_t *bar, uint32_t parity, volatile
     return false;
 }
 
+// TRSM = false: trailing update, A[i][j] -= (L21 L21^T)[i][j] for s0 <= j <= i (column side
+// = row side = the panel rows, exponents Erow).  TRSM = true: panel product, A[i][k0 + c] =
+// (A21 W^T)[i][c] for the OZAKI_NB rows c of W = L11^-1 (column side = W's slices, exponents
+// Ecol[b][c], 2 OZAKI_NB per matrix), all rows i >= s0 = k0 + OZAKI_NB.
+template <bool TRSM>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_ozaki_syrk(const __grid_constant__ OzMaps maps, double *__restrict__ Aall, int N, int s0,
-                 const int *__restrict__ Eall, int *__restrict__ err)
+                 const int *__restrict__ Erow, const int *__restrict__ Ecol, int k0, int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int b = blockIdx.y;
     const int R = N - s0;
-    const int nti = (R + ON - 1) / ON, njm = (R + OM - 1) / OM;
+    const int nti = (R + ON - 1) / ON, njm = TRSM ? 1 : (R + OM - 1) / OM;
     int jm, ti0, cnt;
     if (!item_of(blockIdx.x, njm, nti, jm, ti0, cnt)) return;  // uniform over the CTA
     volatile int *skip_flag = abort_flag + 1;
@@ -270,10 +277,12 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         const int quad = warp % 4;  // TMEM lane quadrant this warp may read
         const int part = ew / 4;    // which EC of the 32 tile columns
         const uint32_t lane_base = static_cast<uint32_t>(quad * 32) << 16;
-        const int jl = jm * OM + quad * 32 + lane;  // trailing column index
-        const int j = s0 + jl;
-        const int *E = Eall + static_cast<size_t>(b) * N;
-        const int ej = j < N ? E[jl] : 0;
+        const int jl = jm * OM + quad * 32 + lane;  // column-side index (trailing column or row c of W)
+        // output column and its validity
+        const int j = TRSM ? k0 + jl : s0 + jl;
+        const bool jok = TRSM ? jl < OZAKI_NB : j < N;
+        const int *E = Erow + static_cast<size_t>(b) * N;
+        const int ej = jok ? (TRSM ? Ecol[static_cast<size_t>(b) * 2 * OZAKI_NB + jl] : E[jl]) : 0;
         double *Ab = Aall + static_cast<long long>(b) * N * N;
         // the EC entries of A this lane updates in tile t, read one tile ahead
         auto load_a = [&](int t, double (&a)[EC]) {
@@ -282,7 +291,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             for (int c = 0; c < EC; ++c)
             {
                 const int i = ib + c;
-                a[c] = (i < N && j < N && j <= i) ? Ab[static_cast<long long>(i) * N + j] : 0.0;
+                a[c] = (!TRSM && i < N && jok && j <= i) ? Ab[static_cast<long long>(i) * N + j] : 0.0;
             }
         };
         double av[EC], an[EC];
@@ -318,14 +327,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
             {
                 const int i = ib + c;
                 const int ei = __shfl_sync(0xffffffffu, ei_own, c);
-                if (i < N && j < N && j <= i)
+                if (i < N && jok && (TRSM || j <= i))
                 {
                     // U = hi 2^28 + lo (value U 2^(e_i + e_j - 63), |U| < 2^69), kept as
                     // W = U / 2^7 rounded: an absolute resolution of 2^-56 of the row scales
                     const long long hi = (static_cast<long long>(U[0][c]) << 14) + U[1][c];
                     const long long lo = (static_cast<long long>(U[2][c]) << 14) + U[3][c];
                     const long long w = (hi << 21) + ((lo + 64) >> 7);
-                    Ab[static_cast<long long>(i) * N + j] = av[c] - fixed_to_double(w, ei + ej - 56);
+                    const double v = fixed_to_double(w, ei + ej - 56);
+                    Ab[static_cast<long long>(i) * N + j] = TRSM ? v : av[c] - v;
                 }
             }
 #pragma unroll
@@ -346,6 +356,12 @@ void ozaki_alloc(OzakiWork &w, int N, int batch)
     GB_CUDA(cudaMalloc(&w.expo, sizeof(int) * static_cast<size_t>(batch) * N));
     GB_CUDA(cudaMalloc(&w.err, sizeof(int)));
     GB_CUDA(cudaMemset(w.err, 0, sizeof(int)));
+    GB_CUDA(cudaMalloc(&w.winv, sizeof(double) * static_cast<size_t>(batch) * OK * OK));
+    const size_t wsl = static_cast<size_t>(batch) * SL * 2 * OK * OK;
+    GB_CUDA(cudaMalloc(&w.wslices, sizeof(__nv_bfloat16) * wsl));
+    GB_CUDA(cudaMemset(w.wslices, 0, sizeof(__nv_bfloat16) * wsl));  // rows OK..2 OK stay zero
+    GB_CUDA(cudaMalloc(&w.wexpo, sizeof(int) * static_cast<size_t>(batch) * 2 * OK));
+    GB_CUDA(cudaMemset(w.wexpo, 0, sizeof(int) * static_cast<size_t>(batch) * 2 * OK));
     w.N = N;
     w.batch = batch;
 }
@@ -355,8 +371,24 @@ void ozaki_free(OzakiWork &w)
     if (w.slices) cudaFree(w.slices);
     if (w.expo) cudaFree(w.expo);
     if (w.err) cudaFree(w.err);
+    if (w.winv) cudaFree(w.winv);
+    if (w.wslices) cudaFree(w.wslices);
+    if (w.wexpo) cudaFree(w.wexpo);
     w = OzakiWork{};
 }
+
+namespace {
+void set_syrk_attributes()
+{
+    static bool attr = false;
+    if (!attr)
+    {
+        GB_CUDA(cudaFuncSetAttribute(k_ozaki_syrk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+        GB_CUDA(cudaFuncSetAttribute(k_ozaki_syrk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
+        attr = true;
+    }
+}
+} // namespace
 
 int ozaki_trailing_update(double *A, int N, int batch, int s0, int k0, int nb, OzakiWork &w, cudaStream_t st)
 {
@@ -365,30 +397,51 @@ int ozaki_trailing_update(double *A, int N, int batch, int s0, int k0, int nb, O
     const int R = N - s0;
     __nv_bfloat16 *S = static_cast<__nv_bfloat16 *>(w.slices);
     dim3 gs(static_cast<unsigned>((R + 7) / 8), batch);
-    k_ozaki_slice<<<gs, 256, 0, st>>>(A, N, s0, k0, nb, S, w.expo);
+    k_ozaki_slice<<<gs, 256, 0, st>>>(A, static_cast<long long>(N) * N, N, s0, k0, nb, R, S, w.expo, N);
     GB_LAUNCH_CHECK();
     OzMaps maps;
     // dims {K = 64, rows R, planes batch * 8}; plane stride N * 64 elements
     make_tmap_bf16(&maps.a, S, OK, R, static_cast<long long>(batch) * SL, OK, static_cast<long long>(N) * OK, OK, OM);
     make_tmap_bf16(&maps.b, S, OK, R, static_cast<long long>(batch) * SL, OK, static_cast<long long>(N) * OK, OK, ON);
-    static bool attr = false;
-    if (!attr)
-    {
-        GB_CUDA(cudaFuncSetAttribute(k_ozaki_syrk, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
-        attr = true;
-    }
+    set_syrk_attributes();
     const int nti = (R + ON - 1) / ON, njm = (R + OM - 1) / OM;
     long long items = 0;
     for (int jm = 0; jm < njm; ++jm) items += (nti - 4 * jm + OZ_CHUNK - 1) / OZ_CHUNK;
     dim3 grid(static_cast<unsigned>(items), batch);
-    k_ozaki_syrk<<<grid, OZ_THREADS, OZ_SMEM, st>>>(maps, A, N, s0, w.expo, w.err);
+    k_ozaki_syrk<false><<<grid, OZ_THREADS, OZ_SMEM, st>>>(maps, A, N, s0, w.expo, w.expo, k0, w.err);
     GB_LAUNCH_CHECK();
     return 2;
 }
 
-double chol_ozaki_selftest(int N, int batch, int seed, int spread_decades, double *max_rel_l)
+int ozaki_panel_solve(double *A, int N, int batch, int k0, OzakiWork &w, cudaStream_t st)
 {
-    // SPD test matrices A = D (X X^T / N + 0.05 I) D with D = diag(10^u), u uniform in
+    GB_REQUIRE(w.slices && w.winv && w.N == N && batch <= w.batch, "Ozaki work space does not match the factorisation");
+    const int s0 = k0 + OK;
+    const int R = N - s0;
+    GB_REQUIRE(R > 0, "panel solve without rows below the diagonal block");
+    __nv_bfloat16 *S = static_cast<__nv_bfloat16 *>(w.slices), *SW = static_cast<__nv_bfloat16 *>(w.wslices);
+    // rows of W = L11^-1 (64 per matrix, planes of 128 rows whose upper half stays zero)
+    k_ozaki_slice<<<dim3(OK / 8, batch), 256, 0, st>>>(w.winv, static_cast<long long>(OK) * OK, OK, 0, 0, OK, OK, SW,
+                                                       w.wexpo, 2 * OK);
+    GB_LAUNCH_CHECK();
+    // rows of A21
+    k_ozaki_slice<<<dim3(static_cast<unsigned>((R + 7) / 8), batch), 256, 0, st>>>(
+        A, static_cast<long long>(N) * N, N, s0, k0, OK, R, S, w.expo, N);
+    GB_LAUNCH_CHECK();
+    OzMaps maps;
+    make_tmap_bf16(&maps.a, SW, OK, 2 * OK, static_cast<long long>(batch) * SL, OK, 2LL * OK * OK, OK, OM);
+    make_tmap_bf16(&maps.b, S, OK, R, static_cast<long long>(batch) * SL, OK, static_cast<long long>(N) * OK, OK, ON);
+    set_syrk_attributes();
+    const int nti = (R + ON - 1) / ON;
+    dim3 grid(static_cast<unsigned>((nti + OZ_CHUNK - 1) / OZ_CHUNK), batch);
+    k_ozaki_syrk<true><<<grid, OZ_THREADS, OZ_SMEM, st>>>(maps, A, N, s0, w.expo, w.wexpo, k0, w.err);
+    GB_LAUNCH_CHECK();
+    return 3;
+}
+
+double chol_ozaki_selftest(int N, int batch, int seed, int spread_decades, double shift, double *max_rel_l)
+{
+    // SPD test matrices A = D (X X^T / N + shift I) D with D = diag(10^u), u uniform in
     // [-spread/2, spread/2]; factored by the FP64 CUDA-core Cholesky and by the tensor-core
     // variant.  Returns max_b |logdet difference|; *max_rel_l = max |L difference| / max |L|.
     cudaStream_t st;
@@ -424,7 +477,7 @@ double chol_ozaki_selftest(int N, int batch, int seed, int spread_decades, doubl
             for (int j = 0; j < N; ++j)
             {
                 double &v = ha[b * nn + static_cast<size_t>(i) * N + j];
-                v = (v + (i == j ? 0.05 : 0.0)) * dsc[i] * dsc[j];
+                v = (v + (i == j ? shift : 0.0)) * dsc[i] * dsc[j];
             }
     }
     a1.upload(ha.data(), ha.size(), st);

@@ -132,7 +132,7 @@ __device__ __forceinline__ void split3_pair(float2 e, uint32_t &h, uint32_t &m, 
 // hi x [Ch;Cm;Cl] (N = 3 NT), mid x [Ch;Cm] (N = 2 NT) and lo x Ch (N = NT), landing in three
 // accumulator blocks of orders 1, 2^-8 and 2^-16; with NTC = 128 the six products are issued
 // one by one into a hi*hi block and a cross-term block.
-template <int RA, int NTC>
+template <int RA, int NTC, bool SV>
 __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__ T1Args a,
                                                         const __grid_constant__ T1Maps maps)
 {
@@ -142,7 +142,10 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     static_assert(2 * NBLK * NTC <= static_cast<int>(TMEM_COLS), "TMEM budget");
     constexpr int RP = rap(RA);
     constexpr bool BOTHX = RA <= 13;  // keep both passes' X values of a chunk in registers
-    constexpr bool STREAM = RA <= 16 && JG == 8;  // one chunk = both stages of up to 16 j
+    // SV: 4-column X gathers are aligned (n_ao % 4 == 0), so the producers stream X through a
+    // register ring, one chunk (both stages, up to 16 j) per pass; otherwise the gathers go one
+    // column at a time below
+    constexpr bool STREAM = SV && RA <= 16 && JG == 8;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int stage_bytes = NS * A_TILE;      // A ring stage
@@ -338,9 +341,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
                 *reinterpret_cast<uint2 *>(stg + 2 * A_TILE + off) = make_uint2(l01, l23);
             }
         };
-        // the streaming path needs aligned 4-column X gathers (a.vec4); otherwise the chunk's
-        // columns may straddle cells and are gathered one by one below
-        if (STREAM && a.vec4)
+        if constexpr (STREAM)
         {
             // One chunk (both stages, all 16 j) per pass over its 2 RA rows (pass, i) of X.
             // Row (pass, i) of chunk kc sits in xb[i] from RA steps before its use: reading
@@ -828,11 +829,13 @@ struct TcChi0::Impl
 
 namespace {
 using T1Fn = void (*)(T1Args, T1Maps);
-T1Fn t1_kernel(int ra, int ntc)
+T1Fn t1_kernel(int ra, int ntc, bool sv)
 {
-    if (ra == 13) return ntc == 64 ? k_t1_tc<13, 64> : k_t1_tc<13, 128>;
-    if (ra == 16) return ntc == 64 ? k_t1_tc<16, 64> : k_t1_tc<16, 128>;
-    return ntc == 64 ? k_t1_tc<32, 64> : k_t1_tc<32, 128>;
+    if (ra == 13 && sv) return ntc == 64 ? k_t1_tc<13, 64, true> : k_t1_tc<13, 128, true>;
+    if (ra == 13) return ntc == 64 ? k_t1_tc<13, 64, false> : k_t1_tc<13, 128, false>;
+    if (ra == 16 && sv) return ntc == 64 ? k_t1_tc<16, 64, true> : k_t1_tc<16, 128, true>;
+    if (ra == 16) return ntc == 64 ? k_t1_tc<16, 64, false> : k_t1_tc<16, 128, false>;
+    return ntc == 64 ? k_t1_tc<32, 64, false> : k_t1_tc<32, 128, false>;
 }
 } // namespace
 
@@ -953,7 +956,8 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     m.nbs = std::min(T1_MAXB, (T1_SMEM_MAX - fixed) / (NS * m.b_tile));
     m.smem = fixed + m.nbs * NS * m.b_tile;
     m.build_work(nullptr, st);
-    GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc), cudaFuncAttributeMaxDynamicSharedMemorySize, m.smem));
+    GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc, g.n_ao % 4 == 0), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 m.smem));
     GB_CUDA(cudaStreamSynchronize(st));
 }
 
@@ -1079,7 +1083,7 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
         a.err = m.err.get();
         if (m.n_work > 0)
         {
-            t1_kernel(m.ra, m.ntc)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
+            t1_kernel(m.ra, m.ntc, a.vec4 != 0)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
             GB_LAUNCH_CHECK();
             k_t2<<<m.n_groups, T2_THREADS, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, m.groups.get(), chi0R);
             GB_LAUNCH_CHECK();
