@@ -51,6 +51,11 @@ typedef struct
     int tau_begin;           /* first tau point of this call (default 0) */
     int tau_end;             /* one past the last; -1 = all (default -1) */
     int stage;               /* LIBRPA_GB300_STAGE_* (default FULL) */
+    /* q sharding of E_c: the E_c of a FULL or EC call covers the IBZ q points [q_begin, q_end)
+     * only; the per-q outputs of the others are 0 (a rank then owns those q of the reduce-
+     * scattered chi0(q, omega) and the per-q sums are all-reduced) */
+    int q_begin;             /* first IBZ q point (default 0) */
+    int q_end;               /* one past the last; -1 = all (default -1) */
 } LibrpaGB300Options;
 
 #define LIBRPA_GB300_STAGE_FULL 0   /* chi0 over [tau_begin, tau_end) and E_c */

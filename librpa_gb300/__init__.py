@@ -95,6 +95,7 @@ class GB300Options(C.Structure):
         ("keep_chi0", C.c_int),
         ("device", C.c_int),
         ("reuse_device_inputs", C.c_int), ("tau_begin", C.c_int), ("tau_end", C.c_int), ("stage", C.c_int),
+        ("q_begin", C.c_int), ("q_end", C.c_int),
     ]
 
 

@@ -774,6 +774,8 @@ void librpa_gb300_init_options(LibrpaGB300Options *o)
     o->keep_chi0 = 0;
     o->tau_begin = 0;
     o->tau_end = -1;
+    o->q_begin = 0;
+    o->q_end = -1;
     o->stage = LIBRPA_GB300_STAGE_FULL;
     o->device = 0;
     o->reuse_device_inputs = 1;

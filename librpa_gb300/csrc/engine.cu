@@ -694,6 +694,9 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     const bool gamma_only = (nk == 1);
     RpaResult res;
     res.per_q.assign(nq, cplx(0, 0));
+    // q sharding: this call's E_c covers the IBZ q points [qa, qe)
+    const int qa = std::max(0, go.q_begin), qe = go.q_end < 0 ? nq : std::min(go.q_end, nq);
+    GB_REQUIRE(qa <= qe, "q_begin > q_end");
     const long long NN = static_cast<long long>(N) * N;
     double ec_flops = 0.0;
     GB_REQUIRE(go.ec_path == LIBRPA_GB300_EC_LU_FP64 || go.ec_path == LIBRPA_GB300_EC_CHOL ||
@@ -737,12 +740,12 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         const size_t esz = gamma_only ? sizeof(double) : sizeof(cuDoubleComplex);
         // complex M' is factored as its real 2N x 2N embedding: 32 bytes per element of M'
         const double per_q = static_cast<double>(nw) * NN * (gamma_only ? esz : 2 * esz) + NN * esz;
-        const int qb = std::max(1, std::min(nq, static_cast<int>(24.0e9 / per_q)));
+        const int qb = std::max(1, std::min(std::max(qe - qa, 1), static_cast<int>(24.0e9 / per_q)));
         EcChol ecc(N, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
         DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
-        for (int q0 = 0; q0 < nq; q0 += qb)
+        for (int q0 = qa; q0 < qe; q0 += qb)
         {
-            const int nb = std::min(qb, nq - q0);
+            const int nb = std::min(qb, qe - q0);
             for (int s = 0; s < nb; ++s) assemble_v(q0 + s, Vall.get() + static_cast<size_t>(s) * NN * esz);
             launches += ecc.factor_v(Vall.get(), nb, st);
             for (int s = 0; s < nb; ++s)
@@ -764,7 +767,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                                               : (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0));
         }
     }
-    for (int q = 0; q < nq && !use_chol; ++q)
+    for (int q = qa; q < qe && !use_chol; ++q)
     {
         // V(q) full: blocks of this q inside the staged Coulomb blob
         std::vector<long long> voff;

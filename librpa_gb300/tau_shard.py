@@ -1,12 +1,13 @@
-"""Tau sharding of the RPA correlation energy across ranks (one process, one GPU per rank).
+"""Tau and q sharding of the RPA correlation energy across ranks (one process, one GPU per rank).
 
 chi0(q, omega) = sum_tau gamma(omega, tau) FT[chi0(R, tau)] (LibRPA chi0.cpp:507-596) is a sum
 over the minimax tau points, and each term needs only that tau's G(R, +-tau).  Rank r
 therefore builds the partial sum over a contiguous slice of tau points
-(LibrpaGB300Options.tau_begin / tau_end, stage CHI0), one all-reduce over the process group
-adds the partials, and every rank then evaluates E_c from the full chi0(q, omega) (stage EC).
-The all-reduce is the path's only exchange step; its size is n_omega * n_q * sum_pairs
-n_mu n_nu complex numbers.
+(LibrpaGB300Options.tau_begin / tau_end, stage CHI0).  One reduce-scatter over the process
+group, keyed by q, hands each rank the summed chi0(q, omega) of its own slice of IBZ q points.
+The rank then evaluates the E_c terms of those q (stage EC with q_begin / q_end), and an
+all-reduce of the n_q per-q sums gives every rank the same E_c.  The reduce-scatter is the
+path's one bulk exchange: n_omega * n_q * sum_pairs n_mu n_nu complex numbers in total.
 """
 from __future__ import annotations
 
@@ -43,19 +44,62 @@ def allreduce_sum(a: np.ndarray, group=None) -> np.ndarray:
     return t.cpu().numpy().view(np.complex128).reshape(np.shape(a))
 
 
-def sharded_correlation_energy(h, opts, n_ibz: int, group=None, reduce=allreduce_sum, **gb_options):
-    """E_c with this rank's tau slice; `h` is a Handler with the system loaded, `opts` the
-    LibrpaOptions of the call, gb_options further LibrpaGB300Options fields.  Returns what
-    Handler.get_rpa_correlation_energy returns, identical on every rank."""
+def q_slices(n_q: int, world: int) -> list[tuple[int, int]]:
+    """Contiguous, balanced [begin, end) slices of the IBZ q points over `world` ranks."""
+    return tau_slices(n_q, world)
+
+
+def reduce_scatter_q(part: np.ndarray, n_w: int, n_q: int, group=None) -> tuple[np.ndarray, tuple[int, int]]:
+    """Sum the [omega][q][pair blocks] partials over the ranks; this rank receives the sum for
+    its own q slice (returned in the full layout, other q zero) and the slice.  NCCL groups use
+    one reduce-scatter of q-major, equally padded rank blocks; gloo, which has no
+    reduce-scatter, all-reduces the same buffer and keeps this rank's block."""
+    import torch
+    import torch.distributed as dist
+
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    a = np.ascontiguousarray(part, np.complex128).reshape(n_w, n_q, -1)
+    sl = q_slices(n_q, world)
+    width = max(1, max(e - b for b, e in sl))
+    buf = np.zeros((world, width, n_w, a.shape[2]), np.complex128)
+    for r, (b, e) in enumerate(sl):
+        buf[r, :e - b] = a[:, b:e, :].transpose(1, 0, 2)
+    t = torch.from_numpy(buf.view(np.float64).reshape(-1).copy())
+    if dist.get_backend(group) == "nccl":
+        t = t.cuda()
+        out = torch.empty(t.numel() // world, dtype=t.dtype, device=t.device)
+        dist.reduce_scatter_tensor(out, t, op=dist.ReduceOp.SUM, group=group)
+    else:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        out = t.view(world, -1)[rank]
+    mine = out.cpu().numpy().view(np.complex128).reshape(width, n_w, a.shape[2])
+    b, e = sl[rank]
+    full = np.zeros_like(a)
+    full[:, b:e, :] = mine[:e - b].transpose(1, 0, 2)
+    return full.reshape(-1), (b, e)
+
+
+def sharded_correlation_energy(h, opts, n_ibz: int, group=None, **gb_options):
+    """E_c with this rank's tau slice and q slice; `h` is a Handler with the system loaded,
+    `opts` the LibrpaOptions of the call, gb_options further LibrpaGB300Options fields.
+    Returns (E_c, per-q contributions), identical on every rank."""
     import torch.distributed as dist
 
     rank = dist.get_rank(group) if dist.is_initialized() else 0
     world = dist.get_world_size(group) if dist.is_initialized() else 1
-    b, e = tau_slices(int(opts.nfreq), world)[rank]
+    n_w = int(opts.nfreq)
+    b, e = tau_slices(n_w, world)[rank]
     h.set_gb300_options(gb300_options(**gb_options, tau_begin=b, tau_end=e, stage=STAGE_CHI0))
     h.get_rpa_correlation_energy(opts, n_ibz)
     part = h.chi0_qw()
-    total = reduce(part, group) if world > 1 else part
-    h.load_chi0_qw(total)
-    h.set_gb300_options(gb300_options(**gb_options, stage=STAGE_EC))
-    return h.get_rpa_correlation_energy(opts, n_ibz)
+    if world > 1:
+        mine, (qa, qe) = reduce_scatter_q(part, n_w, n_ibz, group)
+    else:
+        mine, (qa, qe) = part, (0, n_ibz)
+    h.load_chi0_qw(mine)
+    h.set_gb300_options(gb300_options(**gb_options, stage=STAGE_EC, q_begin=qa, q_end=qe))
+    _, per_q = h.get_rpa_correlation_energy(opts, n_ibz)
+    per_q = np.asarray(per_q, np.complex128)
+    if world > 1:
+        per_q = allreduce_sum(per_q, group)
+    return float(per_q.sum().real), per_q

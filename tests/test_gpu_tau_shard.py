@@ -1,11 +1,12 @@
-"""Tau-shard stages through the C ABI on one GPU: the partial chi0(q, omega) of two tau slices,
-summed on the host and loaded back, give the unsharded E_c (needs a GB300)."""
+"""Tau- and q-shard stages through the C ABI on one GPU, one emulated rank after the other: the
+partial chi0(q, omega) of the tau slices, summed on the host and loaded back, give the
+unsharded E_c, and the E_c stages restricted to disjoint q slices add up to it (needs a GB300)."""
 import numpy as np
 import pytest
 
 import librpa_gb300 as L
 from librpa_gb300 import synthetic as sy
-from librpa_gb300.tau_shard import tau_slices
+from librpa_gb300.tau_shard import q_slices, tau_slices
 
 pytestmark = pytest.mark.gpu
 
@@ -39,3 +40,33 @@ def test_sequential_shards_match_full(prec, ec_path, world):
     ec, perq = h.get_rpa_correlation_energy(o, L.n_ibz(s))
     assert abs(ec - full) <= 1e-12 * abs(full), (ec, full)
     np.testing.assert_allclose(perq, full_q, rtol=1e-11, atol=1e-14)
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_q_sliced_ec_stages_add_up(world):
+    s = sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=(3, 1, 1), nocc=2, seed=9)
+    h = L.Handler()
+    L.load_system(h, s)
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
+    nq = L.n_ibz(s)
+    h.set_gb300_options(L.gb300_options(keep_chi0=0))
+    full, full_q = h.get_rpa_correlation_energy(o, nq)
+    h.set_gb300_options(L.gb300_options(stage=L.STAGE_CHI0))
+    h.get_rpa_correlation_energy(o, nq)
+    chi0 = h.chi0_qw()
+    per_q = np.zeros(nq, complex)
+    for qa, qe in q_slices(nq, world):
+        # the rank's share after the reduce-scatter: its own q columns, the others zero
+        mine = chi0.reshape(s.nfreq, nq, -1).copy()
+        mine[:, :qa, :] = 0
+        mine[:, qe:, :] = 0
+        h.load_chi0_qw(mine.reshape(-1))
+        h.set_gb300_options(L.gb300_options(stage=L.STAGE_EC, q_begin=qa, q_end=qe))
+        ec, pq = h.get_rpa_correlation_energy(o, nq)
+        assert np.all(pq[:qa] == 0) and np.all(pq[qe:] == 0)
+        assert abs(ec - pq.sum().real) <= 1e-13 * max(1.0, abs(ec))
+        per_q += pq
+    np.testing.assert_allclose(per_q, full_q, rtol=1e-11, atol=1e-14)
+    assert abs(per_q.sum().real - full) <= 1e-12 * abs(full)
+

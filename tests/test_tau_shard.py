@@ -1,6 +1,7 @@
-"""Tau sharding across ranks on CPU: the slice partition, and the sharded E_c with
-two gloo ranks.  The per-rank compute is the oracle standing in for a GPU; what is tested is
-the partition, the stage sequence and the all-reduce of tau_shard.sharded_correlation_energy."""
+"""Tau and q sharding across ranks on CPU: the slice partitions, and the sharded E_c with two
+and three gloo ranks.  The per-rank compute is the oracle standing in for a GPU; what is tested
+is the partition, the stage sequence, the reduce-scatter by q and the all-reduce of the per-q
+sums in tau_shard.sharded_correlation_energy."""
 import os
 import socket
 
@@ -61,7 +62,12 @@ class OracleHandler:
                 out_row.append(blk)
             chi0q.append(out_row)
         ec, per_q, _ = ec_from_chi0q(self.inp, self.oopts, chi0q)
-        return ec.real, np.asarray(per_q)
+        per_q = np.asarray(per_q, complex)
+        qa, qe = self.go.q_begin, (len(per_q) if self.go.q_end < 0 else self.go.q_end)
+        keep = np.zeros(len(per_q), bool)
+        keep[qa:qe] = True
+        per_q = np.where(keep, per_q, 0)  # the E_c terms of this call's q slice only
+        return per_q.sum().real, per_q
 
     def chi0_qw(self):
         return self.kept.copy()
@@ -79,8 +85,9 @@ def _rank_main(rank, world, port, out_dir):
         s = _system()
         h = OracleHandler(s)
         opts = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI)
-        ec, _ = sharded_correlation_energy(h, opts, L.n_ibz(s))
+        ec, per_q = sharded_correlation_energy(h, opts, L.n_ibz(s))
         np.save(os.path.join(out_dir, f"ec{rank}.npy"), np.array([ec]))
+        np.save(os.path.join(out_dir, f"perq{rank}.npy"), per_q)
     finally:
         dist.destroy_process_group()
 
@@ -91,15 +98,27 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def test_gloo_two_ranks_sharded_ec_matches_unsharded(tmp_path, lib):
+@pytest.mark.parametrize("world", [2, 3])
+def test_gloo_ranks_sharded_ec_matches_unsharded(tmp_path, lib, world):
     import torch.multiprocessing as mp
-    world = 2
     mp.start_processes(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
     from conftest import oracle_input
     from oracle.rpa_oracle import Options, rpa_correlation_energy
     s = _system()
-    ref = rpa_correlation_energy(oracle_input(s), Options(nfreq=s.nfreq, minimax_emin=s.minimax_emin,
-                                                          minimax_emax=s.minimax_emax))["ec"].real
-    ecs = [float(np.load(tmp_path / f"ec{r}.npy")[0]) for r in range(world)]
-    assert ecs[0] == ecs[1]  # every rank ends with the same reduced chi0 and E_c
+    r = rpa_correlation_energy(oracle_input(s), Options(nfreq=s.nfreq, minimax_emin=s.minimax_emin,
+                                                        minimax_emax=s.minimax_emax))
+    ref = r["ec"].real
+    ecs = [float(np.load(tmp_path / f"ec{k}.npy")[0]) for k in range(world)]
+    perqs = [np.load(tmp_path / f"perq{k}.npy") for k in range(world)]
+    # every rank ends with the same per-q sums and E_c; each q was evaluated by one rank only
+    assert all(e == ecs[0] for e in ecs)
+    assert all(np.array_equal(p, perqs[0]) for p in perqs)
     assert abs(ecs[0] - ref) <= 1e-12 * abs(ref)
+    np.testing.assert_allclose(perqs[0], np.asarray(r["per_q"]), rtol=1e-11, atol=1e-15)
+
+
+@pytest.mark.parametrize("n_q,world", [(2, 2), (2, 3), (27, 4), (1, 2)])
+def test_q_slices_partition(n_q, world):
+    from librpa_gb300.tau_shard import q_slices
+    sl = q_slices(n_q, world)
+    assert [q for b, e in sl for q in range(b, e)] == list(range(n_q))
