@@ -51,16 +51,19 @@ __device__ void factor_diag(const T *A, int N, int k0, int nb, T (*D)[NBT + 1], 
         D[i][j] = j <= i ? A[static_cast<long long>(k0 + i) * N + k0 + j] : czero<T>();
     }
     __syncthreads();
+    __shared__ double sinv;  // reciprocal of the current pivot, formed once per step
     for (int p = 0; p < nb; ++p)
     {
         if (threadIdx.x == 0)
         {
             const double d2 = cre(D[p][p]);
             if (!(d2 > 0.0)) *bad = 1;
-            D[p][p] = cfromreal(sqrt(fmax(d2, 1e-300)), D[p][p]);
+            const double l = sqrt(fmax(d2, 1e-300));
+            D[p][p] = cfromreal(l, D[p][p]);
+            sinv = 1.0 / l;
         }
         __syncthreads();
-        const double inv = 1.0 / cre(D[p][p]);
+        const double inv = sinv;
         for (int i = p + 1 + threadIdx.x; i < nb; i += blockDim.x) D[i][p] = cscale(D[i][p], inv);
         __syncthreads();
         const int m = nb - p - 1;
@@ -114,15 +117,24 @@ __global__ void __launch_bounds__(256) k_chol_diag_inv(double *__restrict__ Aall
         if (j <= i) A[static_cast<long long>(k0 + i) * N + k0 + j] = D[i][j];
     }
     for (int i = threadIdx.x; i < nb; i += blockDim.x) diag[static_cast<long long>(b) * N + k0 + i] = D[i][i];
+    __shared__ double invd[NBT];
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) invd[i] = 1.0 / D[i][i];
+    __syncthreads();
     const int c = threadIdx.x;
     if (c < nb)
     {
-        W[c][c] = 1.0 / D[c][c];
+        W[c][c] = invd[c];
         for (int i = c + 1; i < nb; ++i)
         {
-            double sacc = 0.0;
-            for (int k = c; k < i; ++k) sacc = fma(D[i][k], W[k][c], sacc);
-            W[i][c] = -sacc / D[i][i];
+            double s0 = 0.0, s1 = 0.0;  // two chains for the dependent FMA latency
+            int k = c;
+            for (; k + 1 < i; k += 2)
+            {
+                s0 = fma(D[i][k], W[k][c], s0);
+                s1 = fma(D[i][k + 1], W[k + 1][c], s1);
+            }
+            if (k < i) s0 = fma(D[i][k], W[k][c], s0);
+            W[i][c] = -(s0 + s1) * invd[i];
         }
     }
     __syncthreads();
