@@ -5,26 +5,31 @@
 Loads the workload with the librpa_set_* setters, makes ``--repeat`` calls of
 librpa_get_rpa_correlation_energy (the call ``task=rpa`` of the reference driver makes,
 driver/task/rpa.cpp:30) and prints one JSON line per call with E_c and the stage times.
-This is the command the kernel profiles are captured with.
+This is the command the kernel profiles are captured with.  A batch workload (a list of
+independent systems, synthetic.BATCHES) is loaded into one handler per system and every
+repeat evaluates them all, one call each; its line reports the summed wall time and the
+per-system energies.
 """
 import argparse
 import json
 import time
 
-from . import load_system, n_ibz, Handler, Options, gb300_options, Minimax, LIBRI, EC_CHOL, EC_LU_FP64
+from . import load_system, n_ibz, Handler, Options, gb300_options, Minimax, LIBRI, EC_CHOL, EC_CHOL_FP64, EC_LU_FP64
 from . import synthetic
 
 CHI0 = {"fp64": 0, "bf16x3": 1, "fp32": 2}
-EC = {"lu": EC_LU_FP64, "chol": EC_CHOL}
+EC = {"lu": EC_LU_FP64, "chol": EC_CHOL, "chol64": EC_CHOL_FP64}
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="fcc16_k333", choices=sorted(synthetic.WORKLOADS))
+    ap.add_argument("--workload", default="fcc16_k333", choices=sorted(synthetic.WORKLOADS) + sorted(synthetic.BATCHES))
     ap.add_argument("--chi0", default="bf16x3", choices=list(CHI0))
     ap.add_argument("--ec", default="chol", choices=list(EC))
     ap.add_argument("--repeat", type=int, default=1)
     a = ap.parse_args(argv)
+    if a.workload in synthetic.BATCHES:
+        return run_batch(a)
     s = synthetic.WORKLOADS[a.workload]()
     h = Handler()
     load_system(h, s)
@@ -39,6 +44,24 @@ def main(argv=None):
         print(json.dumps({"workload": a.workload, "chi0": a.chi0, "ec_path": a.ec, "ec": ec, "wall_s": dt,
                           **{k: st[k] for k in ("t_gf", "t_chi0", "t_ftct", "t_ec", "chi0_flops", "ec_flops",
                                                 "n_launches")}}), flush=True)
+
+
+def run_batch(a):
+    systems = synthetic.BATCHES[a.workload]()
+    hs = []
+    for s in systems:
+        h = Handler()
+        load_system(h, s)
+        h.set_gb300_options(gb300_options(chi0_precision=CHI0[a.chi0], ec_path=EC[a.ec]))
+        o = Options(nfreq=s.nfreq, tfgrids_type=Minimax, parallel_routing=LIBRI, minimax_emin=s.minimax_emin,
+                    minimax_emax=s.minimax_emax)
+        hs.append((h, o, s))
+    for _ in range(a.repeat):
+        t = time.time()
+        ecs = [h.get_rpa_correlation_energy(o, n_ibz(s))[0] for h, o, s in hs]
+        dt = time.time() - t
+        print(json.dumps({"workload": a.workload, "chi0": a.chi0, "ec_path": a.ec, "systems": len(hs),
+                          "atoms": [s.n_atoms for _, _, s in hs], "ec": ecs, "wall_s": dt}), flush=True)
 
 
 if __name__ == "__main__":

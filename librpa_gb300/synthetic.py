@@ -11,6 +11,9 @@ Workloads (sizes as named in the benchmark table):
                 16 occupied, 13 NAO / 40 ABF per atom.
   mixed64_g   : 64 atoms of random species (NAO/ABF 5/20, 13/60, 26/110), Gamma only.
   sc256_g     : 256 atoms, 13 NAO / 40 ABF, C decay length 1.5 A, Gamma only.
+  batch32_small (BATCHES): 32 independent Gamma cells of 2-8 atoms of random species
+                (NAO/ABF 5/20, 13/60, 26/110), 24 minimax points (the small-cell batch
+                of the mixed-species configuration).
 
 Distributions: KS energies uniform in [-0.8,-0.2] Ha (occupied) and
 [0.1,2.0] Ha (virtual); eigenvectors from the QR factor of a complex
@@ -248,9 +251,22 @@ def mixed64_g(seed=64):
     return cluster_gamma("mixed64_g", 64, [(5, 20), (13, 60), (26, 110)], seed, nfreq=24)
 
 
+def batch32_small(seed=32):
+    """32 independent Gamma-only cells of 2-8 atoms of random species, each its own system."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(2, 9, 32)
+    return [cluster_gamma(f"batch32_small_{i}", int(n), [(5, 20), (13, 60), (26, 110)], seed * 1000 + i, nfreq=24)
+            for i, n in enumerate(sizes)]
+
+
 def sc256_g(seed=256):
     return cluster_gamma("sc256_g", 256, [(13, 40)], seed, decay_ang=1.5, nfreq=16)
 
+
+# workloads that are a list of independent systems, each evaluated by its own call
+BATCHES = {
+    "batch32_small": batch32_small,
+}
 
 WORKLOADS = {
     "fcc2_k222": fcc2_k222,

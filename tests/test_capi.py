@@ -95,3 +95,16 @@ def test_vq_threshold_drops_blocks(lib):
         h.set_aux_bare_coulomb_k_atom_pair(0, 0, 1, 2, 2, np.full(4, 1e-3), np.zeros(4), 1e-2)
         h.set_aux_bare_coulomb_k_atom_pair(0, 0, 0, 2, 2, np.full(4, 1.0), np.zeros(4), 1e-2)
         assert lib.librpa_get_last_error_code(h.h) == 0
+
+
+def test_small_cell_batch_workload():
+    """The 32-cell batch of the mixed-species configuration: independent Gamma cells of 2-8
+    atoms of the three species, reproducible from its seed."""
+    from librpa_gb300 import synthetic as sy
+    a, b = sy.batch32_small(), sy.batch32_small()
+    assert len(a) == 32
+    species = {(5, 20), (13, 60), (26, 110)}
+    for s, t in zip(a, b):
+        assert 2 <= s.n_atoms <= 8 and s.n_kpts == 1 and s.nfreq == 24
+        assert set(zip(s.nao, s.nabf)) <= species
+        assert s.n_atoms == t.n_atoms and np.array_equal(s.ekb, t.ekb)
