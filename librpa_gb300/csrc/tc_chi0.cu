@@ -58,11 +58,13 @@ struct T1Group
 // then cell), all contracted with the same C^J operand.
 struct T1Work
 {
-    int J;      // atom of the B operand
-    int g0;     // first row group
-    int r0;     // first row inside that group
-    int nrows;  // valid rows (<= 128)
-    int nslot;  // row groups the tile touches
+    int J;         // atom of the B operand
+    int g0;        // first row group
+    int r0;        // first row inside that group
+    int nrows;     // valid rows (<= 128)
+    int nslot;     // row groups the tile touches
+    int kc0, kc1;  // chunks [kc0, kc1) of the supercell axis this CTA contracts
+    int split;     // 1: one of several K parts of the tile, added atomically to the output
 };
 
 constexpr int T1_MAXSPEC = 8;    // distinct (NAO, ABF) species with their own B maps
@@ -189,7 +191,8 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         return false;
     };
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int total_stages = a.nkc * njg;
+    const int kc0 = w.kc0, kc1 = w.kc1;
+    const int total_stages = (kc1 - kc0) * njg;
 
     if (threadIdx.x == 0)
     {
@@ -350,7 +353,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
             const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
             auto chunk_base = [&](int kc, const float *&b0, const float *&b1) -> bool {
                 const long long col0 = static_cast<long long>(kc) * CW + cq * 4;
-                if (kc >= a.nkc || col0 >= nsup || !valid) return false;
+                if (kc >= kc1 || col0 >= nsup || !valid) return false;
                 const int cp = static_cast<int>(col0 / nao), ao = static_cast<int>(col0 % nao);
                 const long long src = static_cast<long long>(a.cadd[cp * nc + cJ]) * nao + ao;
                 b0 = Xp[0] + xrow * nsup + src;
@@ -361,12 +364,12 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
                 return (live && i < aI) ? __ldg(reinterpret_cast<const float4 *>(b + i * nsup)) : zero4;
             };
             const float *c0 = Xp[0], *c1 = Xp[0], *n0 = Xp[0], *n1 = Xp[0];
-            bool clive = chunk_base(0, c0, c1);
-            bool nlive = chunk_base(1, n0, n1);
+            bool clive = chunk_base(kc0, c0, c1);
+            bool nlive = chunk_base(kc0 + 1, n0, n1);
             float4 xb[RA];
 #pragma unroll
             for (int i = 0; i < RA; ++i) xb[i] = ld(c0, i, clive);
-            for (int kc = 0; kc < a.nkc && ok; ++kc)
+            for (int kc = kc0; kc < kc1 && ok; ++kc)
             {
                 float2 e[4][JH][2];  // [group of 4 j][jl][column pair]: j 0..15
 #pragma unroll
@@ -428,7 +431,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         else
         {
         float4 x0[RA], x1[BOTHX ? RA : 1];
-        for (int kc = 0; kc < a.nkc && ok; ++kc)
+        for (int kc = kc0; kc < kc1 && ok; ++kc)
         {
             if constexpr (BOTHX) load_x(kc, 0, 2, x0, x1);
             for (int jg = 0; jg < njg; ++jg, ++st_count)
@@ -505,7 +508,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
                 atomicExch(a.err, 202);
                 return false;
             }
-            const int x = st * 64;  // K offset (kc * njg + jg) * 64
+            const int x = (kc0 * njg + st) * 64;  // K offset (kc * njg + jg) * 64
             if (x < 0 || static_cast<long long>(x) + 64 > ktot || (x & 7) != 0)
             {
                 atomicExch(a.err, 205);  // coordinate outside the C^J operand: skip the copy
@@ -656,7 +659,13 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
             double *orow = a.out + a.pr.r_off[gr.pair] + (static_cast<long long>(gr.cell) * bI + mu) * bJ;
 #pragma unroll
             for (int c = 0; c < NTC; ++c)
-                if (c < bJ) orow[c] = static_cast<double>(acc[c]);
+                if (c < bJ)
+                {
+                    if (w.split)
+                        atomicAdd(orow + c, static_cast<double>(acc[c]));
+                    else
+                        orow[c] = static_cast<double>(acc[c]);
+                }
         }
     }
     tc_fence_before();
@@ -818,6 +827,8 @@ struct TcChi0::Impl
     int n_work = 0, n_groups = 0;
     std::vector<int> hI, hJ, nabf_h;
     bool all_active = false;  // the uploaded work list covers every (pair, cell)
+    bool has_split = false;   // some tiles are K parts that add into chi0(R) atomically
+    int n_sm = 0;
     // Row groups of the active (pair, cell) blocks, ordered by J, then I, then cell, and the
     // 128-row tiles over each J's rows; active == nullptr: every block.
     void build_work(const unsigned char *active, cudaStream_t st);
@@ -931,7 +942,13 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     m.hI = hI;
     m.hJ = hJ;
     m.nabf_h = nabf;
-    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1));
+    {
+        int dev = 0;
+        GB_CUDA(cudaGetDevice(&dev));
+        GB_CUDA(cudaDeviceGetAttribute(&m.n_sm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1) +
+                 8 * static_cast<size_t>(m.n_sm));
     m.groups.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c);
     int ntmax = 16, minb = 1 << 30;
     for (int J = 0; J < g.n_at; ++J)
@@ -979,7 +996,7 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
         int gi = gbeg, off = 0;  // current group and row inside it
         while (gi < static_cast<int>(grp.size()))
         {
-            T1Work t{J, gi, off, 0, 0};
+            T1Work t{J, gi, off, 0, 0, 0, nkc, 0};
             int rows = 0, g2 = gi, o2 = off;
             // a tile closes at 128 rows or when it touches maxcj row groups (its G slots)
             while (rows < T1_BM && g2 < static_cast<int>(grp.size()) && t.nslot < maxcj)
@@ -1007,6 +1024,40 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
     std::stable_sort(tiles.begin(), tiles.end(), [&](const T1Work &x, const T1Work &y) {
         return hI[grp[x.g0].pair] < hI[grp[y.g0].pair];
     });
+    // Every tile contracts the same K range, so the last, partial wave of CTAs leaves SMs idle:
+    // its tiles are cut into K parts (added atomically into chi0(R)) when that shortens the
+    // makespan, e.g. 91 tiles over 152 SMs become 5 x 91 fifth-tiles in 3 fifth-waves.
+    has_split = false;
+    const int nt = static_cast<int>(tiles.size()), rem = n_sm > 0 ? nt % n_sm : 0;
+    if (n_sm > 0 && nt >= n_sm && rem > 0 && nkc >= 2)
+    {
+        int parts = 1;
+        double best = 1.0;
+        for (int sp = 2; sp <= 8 && sp <= nkc; ++sp)
+        {
+            const double c = std::ceil(static_cast<double>(sp) * rem / n_sm) / sp + 0.01 * sp;
+            if (c < best)
+            {
+                best = c;
+                parts = sp;
+            }
+        }
+        if (parts > 1)
+        {
+            std::vector<T1Work> tail(tiles.end() - rem, tiles.end());
+            tiles.resize(nt - rem);
+            for (const T1Work &t : tail)
+                for (int q = 0; q < parts; ++q)
+                {
+                    T1Work u = t;
+                    u.kc0 = static_cast<int>(static_cast<long long>(nkc) * q / parts);
+                    u.kc1 = static_cast<int>(static_cast<long long>(nkc) * (q + 1) / parts);
+                    u.split = 1;
+                    if (u.kc1 > u.kc0) tiles.push_back(u);
+                }
+            has_split = true;
+        }
+    }
     n_groups = static_cast<int>(grp.size());
     n_work = static_cast<int>(tiles.size());
     GB_REQUIRE(tiles.size() <= work.size() && grp.size() <= groups.size(), "chi0 work list overflow");
@@ -1047,7 +1098,9 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
     const Geom &g = m.g;
     const long long nsup = g.n_sup;
     int launches = 0;
-    if (zero_first)
+    if (!m.t1_simt) m.build_work(active, st);
+    // K-part tiles add into chi0(R), so their rows start from zero
+    if (zero_first || (!m.t1_simt && m.has_split))
         GB_CUDA(cudaMemsetAsync(chi0R, 0, sizeof(double) * static_cast<size_t>(m.pr.e_total) * g.n_c, st));
     if (m.t1_simt)
     {
@@ -1060,7 +1113,6 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
     }
     else
     {
-        m.build_work(active, st);
         T1Args a;
         a.g = g;
         a.pr = m.pr;
