@@ -68,6 +68,7 @@ struct T1Work
 };
 
 constexpr int T1_MAXSPEC = 8;    // distinct (NAO, ABF) species with their own B maps
+constexpr int T1_KPARTS = 4;     // K parts per tile (each part a CTA, added into chi0(R) atomically)
 
 // C^J B-operand maps, one rank-3 map per (species, piece): dims {ktot, nabf, atoms of the species}.
 struct T1Maps
@@ -947,7 +948,7 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
         GB_CUDA(cudaGetDevice(&dev));
         GB_CUDA(cudaDeviceGetAttribute(&m.n_sm, cudaDevAttrMultiProcessorCount, dev));
     }
-    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1) +
+    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1) * T1_KPARTS +
                  8 * static_cast<size_t>(m.n_sm));
     m.groups.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c);
     int ntmax = 16, minb = 1 << 30;
@@ -1028,6 +1029,26 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
     // its tiles are cut into K parts (added atomically into chi0(R)) when that shortens the
     // makespan, e.g. 91 tiles over 152 SMs become 5 x 91 fifth-tiles in 3 fifth-waves.
     has_split = false;
+    // launches of under 16 waves: every tile in T1_KPARTS K parts, finer units for the scheduler
+    // (measured: the 16-atom workload's 1155 tiles ran 6% faster as 4 parts, 8 parts no better;
+    // the 256-atom workload's 10k tiles gained nothing)
+    const int kparts = static_cast<long long>(tiles.size()) < 16LL * std::max(n_sm, 1) ? T1_KPARTS : 1;
+    if (kparts > 1 && nkc >= 2 * kparts)
+    {
+        std::vector<T1Work> all;
+        all.reserve(tiles.size() * kparts);
+        for (const T1Work &t : tiles)
+            for (int q = 0; q < kparts; ++q)
+            {
+                T1Work u = t;
+                u.kc0 = static_cast<int>(static_cast<long long>(nkc) * q / kparts);
+                u.kc1 = static_cast<int>(static_cast<long long>(nkc) * (q + 1) / kparts);
+                u.split = 1;
+                all.push_back(u);
+            }
+        tiles.swap(all);
+        has_split = true;
+    }
     const int nt = static_cast<int>(tiles.size()), rem = n_sm > 0 ? nt % n_sm : 0;
     if (n_sm > 0 && nt >= n_sm && rem > 0 && nkc >= 2)
     {
@@ -1050,8 +1071,8 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
                 for (int q = 0; q < parts; ++q)
                 {
                     T1Work u = t;
-                    u.kc0 = static_cast<int>(static_cast<long long>(nkc) * q / parts);
-                    u.kc1 = static_cast<int>(static_cast<long long>(nkc) * (q + 1) / parts);
+                    u.kc0 = t.kc0 + static_cast<int>(static_cast<long long>(t.kc1 - t.kc0) * q / parts);
+                    u.kc1 = t.kc0 + static_cast<int>(static_cast<long long>(t.kc1 - t.kc0) * (q + 1) / parts);
                     u.split = 1;
                     if (u.kc1 > u.kc0) tiles.push_back(u);
                 }
