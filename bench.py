@@ -39,9 +39,9 @@ PREC = {"bf16x3": 1, "fp32": 2, "fp64": 0}
 # DRAM bytes (read + write) of one per-(tau, spin) chi0 contraction launch set, from one ncu capture
 # per kernel (profiles/*.md, same workload); None where no capture exists.
 PROFILED_TRAFFIC = {
-    "fcc16_k333": {"bytes": 22.3087e9 + 0.0549e9 + 5.2037e9 + 0.3735e9,
+    "fcc16_k333": {"bytes": 18.4119e9 + 0.0625e9 + 5.2037e9 + 0.3735e9,
                    "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_t1_tc (tau_1) and the X "
-                             "k_tc_gemm (tau_0); k_t2 (1.1% of time) not captured"},
+                             "k_tc_gemm (tau_0); k_t2 (1.4% of time) not captured"},
 }
 
 def _peaks():
