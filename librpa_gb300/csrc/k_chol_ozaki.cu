@@ -1,4 +1,7 @@
-// Trailing update of the real batched Cholesky on the tensor cores, to FP64 accuracy.
+// Panel solve and trailing update of the real batched Cholesky on the tensor cores, to FP64
+// accuracy.  The panel L21 = A21 W^T (W = L11^-1 from k_chol_diag_inv) and the update below are
+// the same exact slice products; they differ only in the operands and in the epilogue, which
+// writes the panel and subtracts from the trailing matrix (k_ozaki_syrk<TRSM>).
 //
 // After a panel step the lower trailing matrix needs A22 -= L21 L21^T, with L21 the panel rows
 // below the diagonal block (OZAKI_NB = 64 columns).  Each row r of L21 is scaled by 2^-e_r (e_r
