@@ -41,6 +41,7 @@
 #include "chol.h"
 #include "common.h"
 #include "kernels.h"
+#include "ozaki_fixed.h"
 #include "tc_common.cuh"
 #include "tc_gemm.h"
 
@@ -52,6 +53,7 @@ using namespace tc;
 
 constexpr int OM = 128, ON = 32, OK = OZAKI_NB;  // columns j per item, rows i per tile, K
 constexpr int SL = OZAKI_SLICES;
+static_assert(SL == ozaki::OZ_SLICES, "slice count of the integer arithmetic");
 constexpr int OZ_CHUNK = 32;          // row tiles per CTA
 constexpr int TILE_A = OM * OK * 2;   // 16 KB per slice
 constexpr int TILE_B = ON * OK * 2;   // 4 KB per slice
@@ -70,27 +72,6 @@ struct OzMaps
 {
     CUtensorMap a, b;  // the same slice buffer with 128-row and 32-row boxes
 };
-
-// value = w 2^e0 for |w| < 2^63, rounded to nearest (ties away from zero), by integer
-// operations only (GB300's FP64 pipe is the scarce unit here).
-__device__ __forceinline__ double fixed_to_double(long long w, int e0)
-{
-    if (w == 0) return 0.0;
-    const unsigned long long sign = static_cast<unsigned long long>(w) & 0x8000000000000000ull;
-    const unsigned long long mag = static_cast<unsigned long long>(w < 0 ? -w : w);
-    const int lz = __clzll(static_cast<long long>(mag));
-    const unsigned long long norm = mag << lz;            // leading one at bit 63
-    unsigned long long mant = (norm >> 11) + ((norm >> 10) & 1ull);  // 53 bits, rounded
-    int be = 63 - lz + e0 + 1023;
-    if (mant >> 53)
-    {
-        mant >>= 1;
-        ++be;
-    }
-    if (be <= 0) return 0.0;  // below the normal range: negligible next to the FP64 entries
-    return __longlong_as_double(
-        static_cast<long long>(sign | (static_cast<unsigned long long>(be) << 52) | (mant & 0xFFFFFFFFFFFFFull)));
-}
 
 // One warp per row: row exponent and the 8 integer slices, by integer operations on the FP64 bit
 // patterns (the digits of |v| 2^56, v = x 2^-e; subnormal entries count as zero).  Row rl of the
@@ -115,29 +96,18 @@ __global__ void k_ozaki_slice(const double *__restrict__ A, long long bstride, i
         m = max(m, u[h] & 0x7FFFFFFFFFFFFFFFull);  // magnitudes order like their bit patterns
     }
     for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    const int mexp = static_cast<int>(m >> 52);  // biased exponent of the row maximum
-    const int e = mexp ? mexp - 1022 : 0;       // max < 2^e
+    const int e = ozaki::row_exponent(m);  // max < 2^e
+    const bool nonzero = (m >> 52) != 0;
     const size_t plane = static_cast<size_t>(dst_rows) * OK;
     __nv_bfloat16 *Sb = S + static_cast<size_t>(b) * SL * plane + static_cast<size_t>(rl) * OK;
 #pragma unroll
     for (int h = 0; h < 2; ++h)
     {
         const int c = lane + 32 * h;
-        const int bexp = static_cast<int>((u[h] >> 52) & 0x7FF);
-        const bool neg = (u[h] >> 63) != 0;
-        unsigned long long F = 0;  // |x| 2^(56 - e), truncated
-        if (bexp != 0 && mexp != 0)
-        {
-            const unsigned long long mant = (u[h] & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-            const int sh = (bexp - 1023) + 4 - e;  // |x| = mant 2^(bexp - 1075); <= 3 since |x| < 2^e
-            F = sh >= 0 ? mant << sh : (sh > -64 ? mant >> (-sh) : 0ull);
-        }
+        int dig[SL];
+        ozaki::slice_digits(u[h], e, nonzero, dig);
 #pragma unroll
-        for (int p = 0; p < SL; ++p)
-        {
-            const int dgt = static_cast<int>((F >> (49 - 7 * p)) & 127ull);
-            Sb[p * plane + c] = __float2bfloat16_rn(static_cast<float>(neg ? -dgt : dgt));
-        }
+        for (int p = 0; p < SL; ++p) Sb[p * plane + c] = __float2bfloat16_rn(static_cast<float>(dig[p]));
     }
     if (lane == 0) E[static_cast<size_t>(b) * dst_rows + rl] = e;
 }
@@ -334,10 +304,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 {
                     // U = hi 2^28 + lo (value U 2^(e_i + e_j - 63), |U| < 2^69), kept as
                     // W = U / 2^7 rounded: an absolute resolution of 2^-56 of the row scales
-                    const long long hi = (static_cast<long long>(U[0][c]) << 14) + U[1][c];
-                    const long long lo = (static_cast<long long>(U[2][c]) << 14) + U[3][c];
-                    const long long w = (hi << 21) + ((lo + 64) >> 7);
-                    const double v = fixed_to_double(w, ei + ej - 56);
+                    const long long w = ozaki::combine_groups(U[0][c], U[1][c], U[2][c], U[3][c]);
+                    const double v = ozaki::fixed_to_double(w, ei + ej - 56);
                     Ab[static_cast<long long>(i) * N + j] = TRSM ? v : av[c] - v;
                 }
             }
