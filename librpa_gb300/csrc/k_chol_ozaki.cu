@@ -42,6 +42,7 @@
 #include "common.h"
 #include "kernels.h"
 #include "ozaki_fixed.h"
+#include "work_schedule.h"
 #include "tc_common.cuh"
 #include "tc_gemm.h"
 
@@ -115,19 +116,7 @@ __global__ void k_ozaki_slice(const double *__restrict__ A, long long bstride, i
 // Work item t -> (column block jm, first row tile, row tile count)
 __device__ __forceinline__ bool item_of(int t, int njm, int nti, int &jm, int &ti0, int &cnt)
 {
-    for (jm = 0; jm < njm; ++jm)
-    {
-        const int first = 4 * jm;  // row tiles with 32 ti + 31 >= 128 jm
-        const int nch = (nti - first + OZ_CHUNK - 1) / OZ_CHUNK;
-        if (t < nch)
-        {
-            ti0 = first + t * OZ_CHUNK;
-            cnt = min(OZ_CHUNK, nti - ti0);
-            return true;
-        }
-        t -= nch;
-    }
-    return false;
+    return sched::ozaki_item(t, njm, nti, OZ_CHUNK, jm, ti0, cnt);
 }
 
 // Bounded wait that gives up at once after any earlier timeout of the CTA.
@@ -376,8 +365,7 @@ int ozaki_trailing_update(double *A, int N, int batch, int s0, int k0, int nb, O
     make_tmap_bf16(&maps.b, S, OK, R, static_cast<long long>(batch) * SL, OK, static_cast<long long>(N) * OK, OK, ON);
     set_syrk_attributes();
     const int nti = (R + ON - 1) / ON, njm = (R + OM - 1) / OM;
-    long long items = 0;
-    for (int jm = 0; jm < njm; ++jm) items += (nti - 4 * jm + OZ_CHUNK - 1) / OZ_CHUNK;
+    const long long items = sched::ozaki_items(njm, nti, OZ_CHUNK);
     dim3 grid(static_cast<unsigned>(items), batch);
     k_ozaki_syrk<false><<<grid, OZ_THREADS, OZ_SMEM, st>>>(maps, A, N, s0, w.expo, w.expo, k0, w.err);
     GB_LAUNCH_CHECK();

@@ -19,6 +19,7 @@
 
 #include "common.h"
 #include "tc_common.cuh"
+#include "work_schedule.h"
 #include "tc_gemm.h"
 
 namespace gb {
@@ -63,44 +64,7 @@ __host__ __device__ constexpr int term_b(int ns, int t)
 // drain warps add each stage's pair into round-to-nearest FP32 registers while the next
 // stage's MMAs run.
 constexpr int GEMM_THREADS = 256;  // warp 0: TMA, warp 1: MMA, warps 4-7: drain + epilogue
-constexpr int RASTER_GROUP = 8;     // output-tile rows per raster group
-
-// Linear CTA index -> output tile.  Tiles run column by column inside groups of RASTER_GROUP
-// tile rows, so the CTAs resident at one time share a few A row panels and B column panels in
-// L2.  lower != 0: only tiles with nt <= mt (square tile grid), in the same grouped order.
-__device__ __forceinline__ void tile_coords(int t, int ntm, int ntn, int lower, int &mt, int &nt)
-{
-    constexpr int G = RASTER_GROUP;
-    if (!lower)
-    {
-        const int g = t / (G * ntn);
-        const int gm = min(G, ntm - g * G);
-        const int l = t - g * G * ntn;
-        mt = g * G + l % gm;
-        nt = l / gm;
-        return;
-    }
-    int g = 0, rem = t;
-    for (;; ++g)
-    {
-        const int gm = min(G, ntm - g * G);
-        const int cnt = gm * (g * G + 1) + gm * (gm - 1) / 2;
-        if (rem < cnt || gm <= 0) break;
-        rem -= cnt;
-    }
-    const int gm = min(G, ntm - g * G), r0 = g * G;
-    for (nt = 0; nt < ntn; ++nt)
-    {
-        const int rows = nt <= r0 ? gm : r0 + gm - nt;
-        if (rem < rows)
-        {
-            mt = (nt <= r0 ? r0 : nt) + rem;
-            return;
-        }
-        rem -= rows;
-    }
-    mt = 0;  // not reached for t below the lower-tile count
-}
+using sched::tile_coords;  // grouped raster / lower-tile order of the output tiles (work_schedule.h)
 
 template <int NS>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "../../include/librpa_gb300.h"
+#include "work_schedule.h"
 #include "tc_common.cuh"
 #include "tc_gemm.h"
 
@@ -1027,57 +1028,25 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
     });
     // Every tile contracts the same K range, so the last, partial wave of CTAs leaves SMs idle:
     // its tiles are cut into K parts (added atomically into chi0(R)) when that shortens the
-    // makespan, e.g. 91 tiles over 152 SMs become 5 x 91 fifth-tiles in 3 fifth-waves.
+    // makespan.  Launches of under 16 waves run every tile in T1_KPARTS K parts, finer units
+    // for the scheduler (measured: the 16-atom workload's 1155 tiles ran 6% faster as 4 parts,
+    // 8 parts no better; the 256-atom workload's 10k tiles gained nothing).
     has_split = false;
-    // launches of under 16 waves: every tile in T1_KPARTS K parts, finer units for the scheduler
-    // (measured: the 16-atom workload's 1155 tiles ran 6% faster as 4 parts, 8 parts no better;
-    // the 256-atom workload's 10k tiles gained nothing)
-    const int kparts = static_cast<long long>(tiles.size()) < 16LL * std::max(n_sm, 1) ? T1_KPARTS : 1;
-    if (kparts > 1 && nkc >= 2 * kparts)
     {
-        std::vector<T1Work> all;
-        all.reserve(tiles.size() * kparts);
-        for (const T1Work &t : tiles)
-            for (int q = 0; q < kparts; ++q)
-            {
-                T1Work u = t;
-                u.kc0 = static_cast<int>(static_cast<long long>(nkc) * q / kparts);
-                u.kc1 = static_cast<int>(static_cast<long long>(nkc) * (q + 1) / kparts);
-                u.split = 1;
-                all.push_back(u);
-            }
-        tiles.swap(all);
-        has_split = true;
-    }
-    const int nt = static_cast<int>(tiles.size()), rem = n_sm > 0 ? nt % n_sm : 0;
-    if (n_sm > 0 && nt >= n_sm && rem > 0 && nkc >= 2)
-    {
-        int parts = 1;
-        double best = 1.0;
-        for (int sp = 2; sp <= 8 && sp <= nkc; ++sp)
+        const std::vector<sched::KPart> plan =
+            sched::plan_kparts(static_cast<int>(tiles.size()), n_sm, nkc, T1_KPARTS);
+        std::vector<T1Work> cut;
+        cut.reserve(plan.size());
+        for (const sched::KPart &k : plan)
         {
-            const double c = std::ceil(static_cast<double>(sp) * rem / n_sm) / sp + 0.01 * sp;
-            if (c < best)
-            {
-                best = c;
-                parts = sp;
-            }
+            T1Work u = tiles[k.tile];
+            u.kc0 = k.kc0;
+            u.kc1 = k.kc1;
+            u.split = k.split;
+            has_split = has_split || k.split != 0;
+            cut.push_back(u);
         }
-        if (parts > 1)
-        {
-            std::vector<T1Work> tail(tiles.end() - rem, tiles.end());
-            tiles.resize(nt - rem);
-            for (const T1Work &t : tail)
-                for (int q = 0; q < parts; ++q)
-                {
-                    T1Work u = t;
-                    u.kc0 = t.kc0 + static_cast<int>(static_cast<long long>(t.kc1 - t.kc0) * q / parts);
-                    u.kc1 = t.kc0 + static_cast<int>(static_cast<long long>(t.kc1 - t.kc0) * (q + 1) / parts);
-                    u.split = 1;
-                    if (u.kc1 > u.kc0) tiles.push_back(u);
-                }
-            has_split = true;
-        }
+        tiles.swap(cut);
     }
     n_groups = static_cast<int>(grp.size());
     n_work = static_cast<int>(tiles.size());
