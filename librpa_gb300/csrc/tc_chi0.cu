@@ -994,31 +994,17 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
         for (int p : pairs_of[J])
             for (int c = 0; c < g.n_c; ++c)
                 if (!active || active[static_cast<size_t>(p) * g.n_c + c]) grp.push_back({p, c});
-        // tiles of 128 rows over the concatenated rows of this J's groups
-        int gi = gbeg, off = 0;  // current group and row inside it
-        while (gi < static_cast<int>(grp.size()))
+        // tiles of 128 rows over the concatenated rows of this J's groups; a tile closes at 128
+        // rows or when it touches maxcj row groups (its G slots)
+        const int gend = static_cast<int>(grp.size());
+        std::vector<int> grows(gend - gbeg);
+        for (int gi = gbeg; gi < gend; ++gi) grows[gi - gbeg] = nabf_h[hI[grp[gi].pair]];
+        std::vector<sched::RowTile> rt;
+        sched::pack_row_tiles(grows.data(), gend - gbeg, gbeg, T1_BM, maxcj, rt);
+        for (const sched::RowTile &r : rt)
         {
-            T1Work t{J, gi, off, 0, 0, 0, nkc, 0};
-            int rows = 0, g2 = gi, o2 = off;
-            // a tile closes at 128 rows or when it touches maxcj row groups (its G slots)
-            while (rows < T1_BM && g2 < static_cast<int>(grp.size()) && t.nslot < maxcj)
-            {
-                const int b = nabf_h[hI[grp[g2].pair]];
-                const int take = std::min(b - o2, T1_BM - rows);
-                rows += take;
-                ++t.nslot;
-                o2 += take;
-                if (o2 == b)
-                {
-                    ++g2;
-                    o2 = 0;
-                }
-            }
-            t.nrows = rows;
-            GB_REQUIRE(t.nslot <= maxcj, "chi0 tile touches more row groups than its shared-memory G slots");
-            tiles.push_back(t);
-            gi = g2;
-            off = o2;
+            GB_REQUIRE(r.nslot <= maxcj, "chi0 tile touches more row groups than its shared-memory G slots");
+            tiles.push_back(T1Work{J, r.g0, r.r0, r.nrows, r.nslot, 0, nkc, 0});
         }
     }
     // launch order: by the I atom of a tile's first row group, so the CTAs resident at one time

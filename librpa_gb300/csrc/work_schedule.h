@@ -1,6 +1,6 @@
 // Work scheduling shared by the kernels and host-compiled unit tests: the tile order of the
-// split GEMM, the work items of the tensor-core Cholesky update and the K parts of the chi0
-// contraction's tiles.
+// split GEMM, the work items of the tensor-core Cholesky update, and the row tiles and K parts
+// of the chi0 contraction.
 #pragma once
 
 #include <cmath>
@@ -83,6 +83,41 @@ inline long long ozaki_items(int njm, int nti, int chunk)
     long long items = 0;
     for (int jm = 0; jm < njm; ++jm) items += (nti - 4 * jm + chunk - 1) / chunk;
     return items;
+}
+
+// chi0 contraction: the rows of n row groups (group g has rows[g] rows), taken in order,
+// packed into tiles of at most bm rows that touch at most max_slots >= 1 groups (the G slots of
+// a CTA).  A tile closes when it is full, when it has used its slots or after the last group.
+// Group indices in the tiles are offset by g_base.
+struct RowTile
+{
+    int g0, r0, nrows, nslot;  // first group, first row inside it, rows, groups touched
+};
+
+inline void pack_row_tiles(const int *rows, int n, int g_base, int bm, int max_slots, std::vector<RowTile> &out)
+{
+    int gi = 0, off = 0;  // current group and row inside it
+    while (gi < n)
+    {
+        RowTile t{g_base + gi, off, 0, 0};
+        int g2 = gi, o2 = off;
+        while (t.nrows < bm && g2 < n && t.nslot < max_slots)
+        {
+            const int b = rows[g2];
+            const int take = imin(b - o2, bm - t.nrows);
+            t.nrows += take;
+            ++t.nslot;
+            o2 += take;
+            if (o2 == b)
+            {
+                ++g2;
+                o2 = 0;
+            }
+        }
+        out.push_back(t);
+        gi = g2;
+        off = o2;
+    }
 }
 
 // chi0 contraction: how the n_tiles equal tiles (each nkc chunks of K) become CTAs.

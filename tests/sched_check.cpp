@@ -4,6 +4,7 @@
 //   O njm nti chunk        -> "items", one line "jm ti0 cnt" per item, then "end <ok>" where ok
 //                             says whether the item after the last is rejected
 //   K n_tiles n_sm nkc kmax -> "units", then one line "tile kc0 kc1 split" per CTA
+//   P bm slots n r_0 .. r_{n-1} -> "tiles", then one line "g0 r0 nrows nslot" per row tile
 #include <iostream>
 #include <string>
 
@@ -48,6 +49,17 @@ int main()
             const std::vector<KPart> plan = plan_kparts(n_tiles, n_sm, nkc, kmax);
             std::cout << plan.size() << '\n';
             for (const KPart &k : plan) std::cout << k.tile << ' ' << k.kc0 << ' ' << k.kc1 << ' ' << k.split << '\n';
+        }
+        else if (op == "P")
+        {
+            int bm, slots, n;
+            std::cin >> bm >> slots >> n;
+            std::vector<int> rows(n);
+            for (int &r : rows) std::cin >> r;
+            std::vector<RowTile> tiles;
+            pack_row_tiles(rows.data(), n, 0, bm, slots, tiles);
+            std::cout << tiles.size() << '\n';
+            for (const RowTile &t : tiles) std::cout << t.g0 << ' ' << t.r0 << ' ' << t.nrows << ' ' << t.nslot << '\n';
         }
         else
         {

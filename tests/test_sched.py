@@ -6,6 +6,9 @@
 - ozaki_item (tensor-core Cholesky update, k_chol_ozaki.cu): the row tiles that meet the lower
   triangle of each 128-column block exactly once, in chunks of at most OZ_CHUNK row tiles, and
   nothing past the grid size ozaki_items reports;
+- pack_row_tiles (chi0 contraction, tc_chi0.cu): every row of every row group exactly once, in
+  order, in tiles of at most 128 rows over at most max_slots groups, each tile closed only when
+  full, out of slots or at the last group;
 - plan_kparts (chi0 contraction, tc_chi0.cu): the K chunks of every tile exactly once, K parts
   flagged for atomic accumulation, the plan within the work list the contraction allocates
   (n_tiles T1_KPARTS + 8 n_sm entries) and a greedy makespan within one part of the uncut
@@ -81,6 +84,60 @@ def test_cholesky_update_items_cover_the_lower_triangle(sched, R, trsm):
     # 32 ti + 31 >= 128 jm
     want = {(jm, ti) for jm in range(njm) for ti in range(nti) if 32 * ti + 31 >= 128 * jm}
     assert seen == want
+
+
+def _pack(sched, rows, bm, slots):
+    out = sched(f"P {bm} {slots} {len(rows)} " + " ".join(map(str, rows)))
+    n = int(out[0])
+    return [tuple(map(int, l.split())) for l in out[1:1 + n]]
+
+
+def _check_pack(tiles, rows, bm, slots):
+    covered = []  # (group, row) in tile order
+    for g0, r0, nrows, nslot in tiles:
+        assert 1 <= nslot <= slots and 0 <= nrows <= bm
+        g, r, left, touched = g0, r0, nrows, 0
+        while left > 0 or (touched < nslot and g < len(rows)):
+            take = min(rows[g] - r, left)
+            covered += [(g, r + k) for k in range(take)]
+            left -= take
+            touched += 1
+            r += take
+            if r == rows[g]:
+                g, r = g + 1, 0
+            if touched == nslot:
+                break
+        assert left == 0 and touched == nslot
+        # closed because full, out of slots or past the last group
+        assert nrows == bm or nslot == slots or g == len(rows)
+    assert covered == [(g, r) for g in range(len(rows)) for r in range(rows[g])]
+
+
+@pytest.mark.parametrize("rows,slots", [
+    ([40] * 7, 5), ([40] * 30, 5), ([13, 200, 7, 128, 128, 1], 4), ([128] * 5, 2), ([129, 127, 2], 3),
+    ([300], 2), ([1] * 300, 4), ([40, 0, 40, 40, 40], 5), ([], 3)])
+def test_row_tiles_cover_each_row_once(sched, rows, slots):
+    tiles = _pack(sched, rows, 128, slots)
+    _check_pack(tiles, rows, 128, slots)
+
+
+def test_row_tiles_random_groups(sched):
+    rng = random.Random(13)
+    for _ in range(200):
+        rows = [rng.choice([rng.randint(1, 300), 40, 80, 128]) for _ in range(rng.randint(1, 60))]
+        slots = max(2, (128 + min(rows) - 1) // min(rows) + 1) if rng.random() < 0.7 else rng.randint(1, 6)
+        _check_pack(_pack(sched, rows, 128, slots), rows, 128, slots)
+
+
+def test_row_tiles_slot_count_never_binds_at_the_default(sched):
+    # the contraction gives every tile ceil(128 / min rows) + 1 slots; with that many no tile
+    # closes for lack of slots before it is full (except the last)
+    rng = random.Random(17)
+    for _ in range(200):
+        rows = [rng.randint(8, 260) for _ in range(rng.randint(1, 40))]
+        slots = (128 + min(rows) - 1) // min(rows) + 1
+        tiles = _pack(sched, rows, 128, slots)
+        assert all(t[2] == 128 for t in tiles[:-1]), (rows, tiles)
 
 
 def _makespan(units, n_sm, nkc):
