@@ -8,6 +8,8 @@ Follows the driver readers of the reference (driver/read_data.cpp):
   KS_eigenvector_*  handle_KS_file             :184-284  (order: ao, spinor, band, spin)
   Cs_data_* (bin)   handle_Cs_file_binary      :690-747  (keep if max|C| >= cs_threshold, default 1e-6)
   coulomb_mat_*     handle_Vq_row_file (bin)   :1472-1577 (upper atom blocks)
+  coulomb_cut_*     the same format (truncated Coulomb of G0W0, driver/task/g0w0.cpp:33-45)
+  vxc_out           read_vxc                   :142-182
 Only the unformatted-binary Cs/V variants are handled (the regression datasets use them).
 """
 from __future__ import annotations
@@ -117,9 +119,20 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
             if np.abs(m).max() >= cs_threshold:
                 Cs[(I - 1, J - 1, (r1, r2, r3))] = m
 
+    Vq = read_coulomb(d, "coulomb_mat", nabf_at)
+
+    return RPAInput(n_spins=ns, n_kpts=nk, n_bands=nb, n_ao=nao, wg=wg, ekb=ekb, efermi=efermi,
+                    wfc=wfc, latvec=lat, period=period, kvecs=kv, ibz_map=ibz,
+                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos)
+
+
+def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
+    """V(q) upper atom blocks {(iq, I, J): (n_mu, n_nu) complex} from the binary row files."""
+    d = d.rstrip("/") + "/"
+    nat = len(nabf_at)
     aoff = np.concatenate([[0], np.cumsum(nabf_at)]).astype(int)
     Vq = {}
-    for fn in sorted(glob.glob(d + "coulomb_mat*")):
+    for fn in sorted(glob.glob(d + prefix + "*")):
         raw = open(fn, "rb").read()
         _nirk, nloc = struct.unpack_from("<2i", raw, 0)
         off = 8
@@ -138,7 +151,19 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
             for I in range(nat):
                 for J in range(I, nat):
                     Vq[(iq, I, J)] = M[aoff[I]:aoff[I + 1], aoff[J]:aoff[J + 1]].copy()
+    return Vq
 
-    return RPAInput(n_spins=ns, n_kpts=nk, n_bands=nb, n_ao=nao, wg=wg, ekb=ekb, efermi=efermi,
-                    wfc=wfc, latvec=lat, period=period, kvecs=kv, ibz_map=ibz,
-                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos)
+
+def read_vxc(path: str) -> np.ndarray:
+    """<psi_n|v_xc|psi_n> in Hartree, shape (n_spins, n_kpts, n_states) (read_data.cpp:142-182:
+    header n_kpts n_spins n_states, then per k and spin one "Ha eV" pair per state)."""
+    t = _tokens(path)
+    nk, ns, nst = int(t[0]), int(t[1]), int(t[2])
+    out = np.zeros((ns, nk, nst))
+    p = 3
+    for k in range(nk):
+        for s in range(ns):
+            for i in range(nst):
+                out[s, k, i] = float(t[p])
+                p += 2
+    return out

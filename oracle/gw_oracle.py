@@ -1,0 +1,274 @@
+"""Oracle (test infrastructure only): G0W0 quasi-particle energies at the Gamma point.
+
+CPU FP64 restatement of LibRPA's G0W0 chain (task = g0w0) for Gamma-only inputs (molecules
+and Gamma-point cells), built on the RPA oracle's chi0(q, omega):
+
+  exchange  H(R) = LibRI Exx::cal_Hs, labels a0b0_{a1b1,a1b2,a2b1,a2b2}
+                   (thirdparty/LibRI/include/RI/physics/Exx.hpp:242-283) with
+                   D(R) = MeanField::get_dmat_cplx_R (src/core/meanfield.cpp:201-244) and
+                   V(R) = FT_Vq of the truncated Coulomb (src/core/coulmat.cpp:7-90);
+                   v_exx_n = -<psi_n|H(k)|psi_n> (src/core/exx.cpp:820-860)
+  W_c       Wc(omega) = Vcut^1/2 [(1 - V^1/2 chi0 V^1/2)^-1 - 1] Vcut^1/2, square roots by
+                   eigen-decomposition with eigenvalues below the threshold dropped
+                   (src/core/epsilon.cpp:1763-2322, default branch without head correction;
+                   power_hemat_blacs src/math/utils_matrix_m_mpi.h:597-720)
+            Wc(tau) = sum_omega costrans_f2t(tau, omega) Wc(omega)
+                   (CT_FT_Wc_freq_q, src/core/epsilon.cpp:2490-2660; one k-point: no q sum)
+  Sigma_c   Sigma(+-tau) = LibRI GW::cal_Sigmas with the same four labels
+                   (thirdparty/LibRI/include/RI/physics/GW.hpp:102-125), G(+-tau) of
+                   src/core/meanfield.cpp:270-307;
+            Sigma(i omega) = sum_tau [cos_t2f 1/2 (S+ + S-) + i sin_t2f 1/2 (S+ - S-)]
+                   (src/core/gw.cpp:627-700); KS diagonal <psi_n|Sigma|psi_n> (gw.cpp:1100-1140)
+  continuation  Thiele reciprocal differences (AnalyContPade, src/core/analycont.cpp:12-70)
+  QP equation   damped fixed point (qpe_solver_pade_self_consistent, src/core/qpe_solver.cpp)
+
+The reference's own regression output for the H2O molecule (24 states, 16 minimax points,
+16 Pade parameters) pins the result: tests/golden/h2o_g0w0.npz.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .rpa_oracle import (Options, RPAInput, assemble_full, blocks_of, build_gf, centred_mod,
+                         chi0q_partial, cs_tensors, grids_for, k_lists, r_grid, upper_pairs)
+
+HA2EV = 27.211386245988  # src/utils/constants.cpp:13 (the driver's default "internal" choice)
+
+
+# ----------------------------------------------------------------------------- LibRI loop3, 4 labels
+
+def cal_hs_loops(C: dict, W: dict, D: dict, n_atoms: int, period):
+    """H = LRI::cal_loop3 over labels a0b0_a1b1, a0b0_a1b2, a0b0_a2b1, a0b0_a2b2.
+
+    a = C[(I, K, RK)] (mu on I, i on I, k on K@RK), b = C[(J, L, RL - RJ)] (nu on J@RJ, j, l on
+    L@RL), a0b0 = W[(I, J, RJ)].  The label names the two orbital indices that D contracts; the
+    other two index the result:
+      a2b2: D[k, l] -> H[(I, J)]_{ij}      a1b1: D[i, j] -> H[(K, L)]_{kl}
+      a1b2: D[i, l] -> H[(K, J)]_{kj}      a2b1: D[k, j] -> H[(I, L)]_{il}
+    Blocks missing from a map are skipped (an empty tensor contributes nothing).
+    """
+    cells = r_grid(period)
+    sites = [(A, c) for A in range(n_atoms) for c in cells]
+    H = {}
+
+    def sub(b, a):
+        return centred_mod((b[0] - a[0], b[1] - a[1], b[2] - a[2]), period)
+
+    def add(key, val):
+        if key in H:
+            H[key] = H[key] + val
+        else:
+            H[key] = val.copy()
+
+    for I in range(n_atoms):
+        for (K, RK) in sites:
+            Ca = C.get((I, K, RK))
+            if Ca is None:
+                continue
+            for (J, RJ) in sites:
+                Wab = W.get((I, J, RJ))
+                if Wab is None:
+                    continue
+                # a W: (nu, i, k) = sum_mu W[mu, nu] Ca[mu, i, k]
+                CW = np.einsum("mn,mik->nik", Wab, Ca)
+                for (L, RL) in sites:
+                    Cb = C.get((J, L, sub(RL, RJ)))
+                    if Cb is None:
+                        continue
+                    # T[i, k, j, l] = sum_nu CW[nu, i, k] Cb[nu, j, l]
+                    T = np.einsum("nik,njl->ikjl", CW, Cb)
+                    d = D.get((K, L, sub(RL, RK)))
+                    if d is not None:
+                        add((I, J, RJ), np.einsum("ikjl,kl->ij", T, d))
+                    d = D.get((I, J, RJ))
+                    if d is not None:
+                        add((K, L, sub(RL, RK)), np.einsum("ikjl,ij->kl", T, d))
+                    d = D.get((I, L, RL))
+                    if d is not None:
+                        add((K, J, sub(RJ, RK)), np.einsum("ikjl,il->kj", T, d))
+                    d = D.get((K, J, sub(RJ, RK)))
+                    if d is not None:
+                        add((I, L, RL), np.einsum("ikjl,kj->il", T, d))
+    return H
+
+
+def ordered_blocks(full: np.ndarray, nb) -> dict:
+    """Atom blocks (I, J, (0,0,0)) of a full Gamma-point matrix, all ordered pairs."""
+    off = np.concatenate([[0], np.cumsum(nb)]).astype(int)
+    return {(I, J, (0, 0, 0)): full[off[I]:off[I + 1], off[J]:off[J + 1]].copy()
+            for I in range(len(nb)) for J in range(len(nb))}
+
+
+def full_from_blocks(blocks: dict, nb) -> np.ndarray:
+    off = np.concatenate([[0], np.cumsum(nb)]).astype(int)
+    first = next(iter(blocks.values()))
+    M = np.zeros((off[-1], off[-1]), first.dtype)
+    for (I, J, _R), b in blocks.items():
+        M[off[I]:off[I + 1], off[J]:off[J + 1]] += b
+    return M
+
+
+# ----------------------------------------------------------------------------- W_c
+
+def power_hemat(A: np.ndarray, power: float, threshold: float):
+    """Z diag(w^p) Z^H over ascending eigenvalues, those below the threshold set to zero
+    (utils_matrix_m_mpi.h:677-720: n_filtered = first index with w >= threshold)."""
+    w, Z = np.linalg.eigh(A)
+    nf = len(w)
+    for i in range(len(w)):
+        if w[i] >= threshold:
+            nf = i
+            break
+    wp = np.zeros_like(w)
+    wp[nf:] = np.power(w[nf:], power)
+    return (Z * wp) @ Z.conj().T
+
+
+def wc_freq(chi0: np.ndarray, v_eps: np.ndarray, v_cut: np.ndarray, sqrt_threshold: float = 0.0):
+    """Wc = Vcut^1/2 [eps^-1 - 1] Vcut^1/2, eps = 1 - V^1/2 chi0 V^1/2 (epsilon.cpp:2140-2300)."""
+    s = power_hemat(v_eps, 0.5, sqrt_threshold)
+    sc = power_hemat(v_cut, 0.5, sqrt_threshold)
+    eps = np.eye(len(s)) - s @ chi0 @ s
+    x = np.linalg.solve(eps, sc) - sc
+    return sc @ x
+
+
+# ----------------------------------------------------------------------------- continuation + QPE
+
+class Pade:
+    """AnalyContPade (analycont.cpp:12-70): Thiele's reciprocal differences on n_pars points."""
+
+    def __init__(self, n_pars: int, xs, data):
+        xs = list(xs)
+        data = list(data)
+        n_data = len(data)
+        if n_pars < 0:
+            n_pars = n_data
+        if n_data <= n_pars:
+            n_pars = n_data
+            px, dn = xs, data
+        else:
+            step = n_data // (n_pars - 1)
+            px = [xs[i * step] for i in range(n_pars - 1)] + [None]
+            dn = [data[i * step] for i in range(n_pars - 1)] + [data[n_data - 1]]
+            px[n_pars - 1] = 0j  # par_x of the last point is left value-initialised (analycont.cpp:35-41)
+        g = np.zeros((n_pars, n_pars), complex)
+        g[:, 0] = dn
+        for p in range(1, n_pars):
+            for i in range(p, n_pars):
+                g[i, p] = (g[p - 1, p - 1] - g[i, p - 1]) / ((px[i] - px[p - 1]) * g[i, p - 1])
+        self.n = n_pars
+        self.x = np.array(px, complex)
+        self.y = np.array([g[i, i] for i in range(n_pars)])
+
+    def __call__(self, x: complex) -> complex:
+        t = 1.0 + 0j
+        for p in range(self.n - 1, 0, -1):
+            t = 1.0 + self.y[p] * (x - self.x[p - 1]) / t
+        return self.y[0] / t
+
+
+def qpe_solve(pade: Pade, e_mf, e_fermi, vxc, sigma_x, diff_init=1.0e-3, thres=1.0e-5, n_iter_max=200):
+    """qpe_solver_pade_self_consistent (qpe_solver.cpp): returns (info, e_qp, sigc)."""
+    escale = 0.1
+    n_iter = 0
+    e_last = e_mf
+    diff = diff_init
+    sig_last = 0j
+    while True:
+        n_iter += 1
+        if not n_iter <= n_iter_max:
+            break
+        e_this = e_last + escale * diff
+        sig = pade(complex(e_this - e_fermi))
+        diff = e_mf - vxc + sigma_x + sig.real - e_this
+        e_last = e_mf - vxc + sigma_x + sig.real
+        sig_last = sig
+        if abs(diff) < thres or n_iter == n_iter_max - 1:
+            break
+    info = 1 if n_iter > n_iter_max - 1 else 0
+    return info, e_last, sig_last
+
+
+# ----------------------------------------------------------------------------- pipeline
+
+def dmat(inp: RPAInput, ispin: int) -> np.ndarray:
+    """D = sum_n w_n psi_n psi_n^*, w = wg/n_k * n_s/2, states taken up to the first below
+    1e-4/n_k (meanfield.cpp:201-228); Gamma point, real part."""
+    wg = inp.wg[ispin, 0] / inp.n_kpts
+    ev = inp.wfc[ispin, 0]
+    D = np.zeros((inp.n_ao, inp.n_ao), complex)
+    for n in range(inp.n_bands):
+        w = wg[n] * 0.5 * inp.n_spins
+        if w < 1e-4 / inp.n_kpts:
+            break
+        D += w * np.outer(ev[n], ev[n].conj())
+    return D.real
+
+
+def g0w0_gamma(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None = None,
+               n_params: int = -1, sqrt_threshold: float = 0.0):
+    """G0W0 at the Gamma point.  inp.Vq holds the Coulomb matrix of the dielectric function,
+    v_cut the truncated Coulomb (W and exchange); vxc (n_spins, 1, n_states) in Hartree.
+    Returns per spin arrays (Hartree): vexx, sigc (complex, at e_qp), e_qp, sigc_iw (KS
+    diagonal on the imaginary axis) and the grids."""
+    if inp.n_kpts != 1 or tuple(inp.period) != (1, 1, 1):
+        raise ValueError("the G0W0 oracle covers Gamma-only inputs")
+    opts = opts or Options()
+    grid = grids_for(inp, opts)
+    nb, nao = inp.nabf, inp.nao
+    nf = opts.nfreq
+    C = cs_tensors(inp, 0.0)
+    z = (0, 0, 0)
+
+    # chi0(omega) at q = 0 and the two Coulomb matrices (real at Gamma)
+    chi0q = chi0q_partial(inp, opts, 0, nf)
+    pairs = upper_pairs(inp.n_atoms)
+    v_eps = assemble_full({p: inp.Vq[(0, *p)].real for p in pairs if (0, *p) in inp.Vq}, nb, dtype=float)
+    v_c = assemble_full({p: v_cut[(0, *p)].real for p in pairs if (0, *p) in v_cut}, nb, dtype=float)
+
+    # exchange: V(R = 0) of the truncated Coulomb, all ordered pairs
+    VR = ordered_blocks(v_c, nb)
+    out = {"grid": grid, "vexx": [], "sigc": [], "e_qp": [], "sigc_iw": [], "info": []}
+    for s in range(inp.n_spins):
+        D = ordered_blocks(dmat(inp, s), nao)
+        H = full_from_blocks(cal_hs_loops(C, VR, D, inp.n_atoms, (1, 1, 1)), nao)
+        ev = inp.wfc[s, 0]
+        out["vexx"].append(-np.einsum("ni,ij,nj->n", ev.conj(), H, ev).real)
+
+    # Wc(omega) -> Wc(tau)
+    Wf = []
+    for iw in range(nf):
+        X = assemble_full({k: v.real for k, v in chi0q[iw][0].items()}, nb, dtype=float)
+        Wf.append(wc_freq(X, v_eps, v_c, sqrt_threshold))
+    Wt = [sum(grid["cos_f2t"][it, iw] * Wf[iw] for iw in range(nf)) for it in range(nf)]
+
+    kfrac = np.zeros((1, 3))
+    for s in range(inp.n_spins):
+        sig_w = np.zeros((nf, inp.n_ao, inp.n_ao), complex)
+        for it, tau in enumerate(grid["tau"]):
+            Wb = ordered_blocks(Wt[it], nb)
+            Gp = blocks_of(build_gf(inp, s, tau, kfrac, [z]), nao)
+            Gn = blocks_of(build_gf(inp, s, -tau, kfrac, [z]), nao)
+            Sp = full_from_blocks(cal_hs_loops(C, Wb, Gp, inp.n_atoms, (1, 1, 1)), nao)
+            Sn = full_from_blocks(cal_hs_loops(C, Wb, Gn, inp.n_atoms, (1, 1, 1)), nao)
+            cos_part, sin_part = 0.5 * (Sp + Sn), 0.5 * (Sp - Sn)
+            for iw in range(nf):
+                sig_w[iw] += grid["cos_t2f"][iw, it] * cos_part + 1j * grid["sin_t2f"][iw, it] * sin_part
+        ev = inp.wfc[s, 0]
+        sig_ks = np.einsum("ni,wij,nj->nw", ev.conj(), sig_w, ev)
+        xs = [1j * w for w in grid["omega"]]
+        e_qp, sigc, info = [], [], []
+        for n in range(inp.n_bands):
+            pade = Pade(n_params, xs, sig_ks[n])
+            f, e, sg = qpe_solve(pade, inp.ekb[s, 0, n], inp.efermi, vxc[s, 0, n], out["vexx"][s][n])
+            info.append(f)
+            e_qp.append(e)
+            sigc.append(sg)
+        out["sigc_iw"].append(sig_ks)
+        out["e_qp"].append(np.array(e_qp))
+        out["sigc"].append(np.array(sigc))
+        out["info"].append(info)
+    return out

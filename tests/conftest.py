@@ -51,6 +51,26 @@ def load_h2o():
         minimax_emin=-1.0, minimax_emax=-1.0)
 
 
+def load_h2o_g0w0():
+    """H2O G0W0 regression inputs: the RPA fixture (its Coulomb matrix is the run's truncated
+    Coulomb) plus the dielectric Coulomb matrix, v_xc and the reference quasi-particle table."""
+    s = load_h2o()
+    z = np.load(GOLDEN / "h2o_g0w0.npz")
+    veps = {}
+    off = 0
+    for ik, I, J in z["veps_meta"]:
+        n = s.nabf[I] * s.nabf[J]
+        veps[(int(ik), int(I), int(J))] = z["veps_data"][off:off + n].reshape(s.nabf[I], s.nabf[J])
+        off += n
+    s.v_cut = s.Vq
+    s.Vq = veps
+    s.vxc = z["vxc"]
+    s.qp_table = z["table"]
+    s.nfreq = int(z["nfreq"])
+    s.n_params_anacon = int(z["n_params_anacon"])
+    return s
+
+
 def minimax_ref():
     return json.loads((GOLDEN / "minimax_ref.json").read_text())
 

@@ -16,6 +16,17 @@ Produces (all committed, so the tests need no reference tree at run time):
                      (eigenpairs, Fermi level, expected density matrix and G(tau -> 0-))
   h2o_dataset.tar.gz the H2O regression dataset itself (the reference's FHI-aims export, copied
                      unchanged), for the task = rpa driver test
+  h2o_g0w0.npz       inputs of the H2O G0W0 regression dataset
+                     (regression_tests/testcases/g0w0_aims_mole_H2O_libri/dataset.tar.gz) that
+                     h2o_libri.npz lacks: the Coulomb matrix of the dielectric function
+                     (coulomb_mat, upper atom blocks) and <psi_n|v_xc|psi_n> (vxc_out); its
+                     Cs, eigenpairs and truncated Coulomb (coulomb_cut) are checked to equal
+                     h2o_libri.npz's.  Plus the quasi-particle table printed by the reference run
+                     (refs/g0w0_aims_mole_H2O_libri/librpa/librpa.out: state, occ, e_mf, v_xc,
+                     v_exx, ReSigc, ImSigc, e_qp in eV) and its librpa.in settings.
+
+Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
+h2o_dataset|g0w0 ...].
 """
 from __future__ import annotations
 
@@ -31,7 +42,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parent.parent))
 
-from oracle.aims_dataset import read_dataset  # noqa: E402
+from oracle.aims_dataset import read_coulomb, read_dataset, read_vxc  # noqa: E402
 
 
 def _floats(s):
@@ -122,9 +133,44 @@ def h2o_dataset(ref: Path):
     print("h2o_dataset.tar.gz written")
 
 
+def g0w0(ref: Path):
+    tgz = ref / "regression_tests/testcases/g0w0_aims_mole_H2O_libri/dataset.tar.gz"
+    rpa_tgz = ref / "regression_tests/testcases/rpa_aims_mole_H2O_libri/dataset.tar.gz"
+    log = (ref / "regression_tests/refs/g0w0_aims_mole_H2O_libri/librpa/librpa.out").read_text().splitlines()
+    i0 = next(k for k, l in enumerate(log) if re.match(r"State\s+occ\s+e_mf", l)) + 2
+    table = []
+    while i0 < len(log) and log[i0].strip():
+        table.append(_floats(log[i0]))
+        i0 += 1
+    params = (ref / "regression_tests/testcases/g0w0_aims_mole_H2O_libri/librpa/librpa.in").read_text()
+    nfreq = int(re.search(r"nfreq\s*=\s*(\d+)", params).group(1))
+    n_params = int(re.search(r"n_params_anacon\s*=\s*(\d+)", params).group(1))
+    with tempfile.TemporaryDirectory() as td, tempfile.TemporaryDirectory() as td2:
+        with tarfile.open(tgz) as tf:
+            tf.extractall(td, filter="data")
+        with tarfile.open(rpa_tgz) as tf:
+            tf.extractall(td2, filter="data")
+        d = next(Path(td).rglob("band_out")).parent
+        d2 = next(Path(td2).rglob("band_out")).parent
+        inp = read_dataset(str(d))
+        rpa = read_dataset(str(d2))
+        cut = read_coulomb(str(d), "coulomb_cut", inp.nabf)
+        vxc = read_vxc(str(d / "vxc_out"))
+    # what the G0W0 run shares with the RPA fixture
+    assert sorted(inp.Cs) == sorted(rpa.Cs) and all(np.array_equal(inp.Cs[k], rpa.Cs[k]) for k in inp.Cs)
+    assert np.array_equal(inp.wfc, rpa.wfc) and np.array_equal(inp.ekb, rpa.ekb) and np.array_equal(inp.wg, rpa.wg)
+    assert sorted(cut) == sorted(rpa.Vq) and all(np.array_equal(cut[k], rpa.Vq[k]) for k in cut)
+    vkeys = sorted(inp.Vq)
+    np.savez_compressed(
+        HERE / "h2o_g0w0.npz",
+        veps_meta=np.array(vkeys, np.int32),
+        veps_data=np.concatenate([inp.Vq[k].ravel() for k in vkeys]),
+        vxc=vxc, table=np.array(table), nfreq=nfreq, n_params_anacon=n_params)
+    print("h2o_g0w0.npz written:", len(table), "states")
+
+
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-    h2o(ref)
-    h2o_dataset(ref)
-    minimax(ref)
-    he_bcc(ref)
+    which = sys.argv[2:] or ["h2o", "h2o_dataset", "minimax", "he_bcc", "g0w0"]
+    for name in which:
+        {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0}[name](ref)

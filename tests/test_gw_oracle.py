@@ -1,0 +1,125 @@
+"""The G0W0 oracle (oracle/gw_oracle.py) pinned against the reference's H2O G0W0 regression run,
+and its pieces checked on their own (no GPU)."""
+import numpy as np
+import pytest
+
+from conftest import load_h2o_g0w0, oracle_input
+from oracle.gw_oracle import (HA2EV, Pade, cal_hs_loops, full_from_blocks, g0w0_gamma, ordered_blocks,
+                              power_hemat, qpe_solve, wc_freq)
+from oracle.rpa_oracle import Options, cs_tensors
+
+
+@pytest.fixture(scope="module")
+def h2o():
+    s = load_h2o_g0w0()
+    inp = oracle_input(s)
+    r = g0w0_gamma(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon)
+    return s, inp, r
+
+
+def test_h2o_quasiparticle_table(h2o):
+    """Every column of the reference's table (refs/g0w0_aims_mole_H2O_libri/librpa/librpa.out,
+    printed to 5 decimals in eV; the regression suite allows 5e-4 eV) to its print precision."""
+    s, inp, r = h2o
+    t = s.qp_table
+    assert t.shape == (24, 8) and all(f == 0 for f in r["info"][0])
+    got = {
+        "e_mf": inp.ekb[0, 0] * HA2EV,
+        "v_xc": s.vxc[0, 0] * HA2EV,
+        "v_exx": r["vexx"][0] * HA2EV,
+        "ReSigc": r["sigc"][0].real * HA2EV,
+        "ImSigc": r["sigc"][0].imag * HA2EV,
+        "e_qp": r["e_qp"][0] * HA2EV,
+    }
+    for col, name in enumerate(["e_mf", "v_xc", "v_exx", "ReSigc", "ImSigc", "e_qp"], start=2):
+        np.testing.assert_allclose(got[name], t[:, col], rtol=0, atol=6e-6, err_msg=name)
+    # the printed e_qp is e_mf - v_xc + v_exx + Re Sigma_c (driver/task/g0w0.cpp:274)
+    np.testing.assert_allclose(t[:, 2] - t[:, 3] + t[:, 4] + t[:, 5], t[:, 7], atol=2.5e-5)
+
+
+def test_sigma_on_the_imaginary_axis_has_negative_imaginary_part(h2o):
+    """Sigma_c(i omega) = sum_s |M_s|^2 / (i omega - E_s) with positive weights, so every KS
+    diagonal element has Im Sigma_c(i omega) < 0 at omega > 0, and |Sigma_c| -> 0 as omega grows."""
+    s, inp, r = h2o
+    sig = r["sigc_iw"][0]
+    assert np.all(sig.imag < 0)
+    assert np.all(np.abs(sig[:, -1]) < np.abs(sig).max(axis=1))
+
+
+def _dense_hs(C, W, D, nao, nabf):
+    """H_{pq} = sum U[a, p, r] W[a, b] U[b, q, s] D[r, s] with U[a, p, r] = C_a[p, r] + C_a[r, p]
+    the orbital-symmetrised coefficient: the four LibRI labels summed in closed form."""
+    oa = np.concatenate([[0], np.cumsum(nao)]).astype(int)
+    ob = np.concatenate([[0], np.cumsum(nabf)]).astype(int)
+    T = np.zeros((ob[-1], oa[-1], oa[-1]))
+    for (I, K, _R), c in C.items():
+        T[ob[I]:ob[I + 1], oa[I]:oa[I + 1], oa[K]:oa[K + 1]] += c
+    U = T + T.transpose(0, 2, 1)
+    return np.einsum("apr,ab,bqs,rs->pq", U, W, U, D, optimize=True)
+
+
+def test_label_sum_equals_symmetrised_dense_form(h2o):
+    s, inp, r = h2o
+    rng = np.random.default_rng(3)
+    C = cs_tensors(inp, 0.0)
+    nb, na = sum(inp.nabf), inp.n_ao
+    W = rng.standard_normal((nb, nb))
+    W = W + W.T
+    D = rng.standard_normal((na, na))
+    D = D + D.T
+    H = full_from_blocks(cal_hs_loops(C, ordered_blocks(W, inp.nabf), ordered_blocks(D, inp.nao),
+                                      inp.n_atoms, (1, 1, 1)), inp.nao)
+    Hd = _dense_hs(C, W, D, inp.nao, inp.nabf)
+    np.testing.assert_allclose(H, Hd, rtol=0, atol=1e-12 * np.abs(Hd).max())
+
+
+def test_pade_reproduces_a_rational_function():
+    rng = np.random.default_rng(0)
+    poles = rng.uniform(-2, 2, 3) + 1j * rng.uniform(0.1, 1, 3)
+    res = rng.uniform(0.2, 1, 3)
+
+    def f(z):
+        return sum(a / (z - p) for a, p in zip(res, poles))
+
+    xs = [1j * w for w in np.linspace(0.05, 8, 16)]
+    pade = Pade(16, xs, [f(x) for x in xs])
+    for z in [0.3, -1.1 + 0.2j, 2.5j, -0.7]:
+        assert abs(pade(z) - f(z)) < 1e-8 * max(1.0, abs(f(z)))
+    # more points than parameters: evenly spaced selection, the last point kept
+    p2 = Pade(6, xs, [f(x) for x in xs])
+    assert p2.n == 6 and p2.y[0] == f(xs[0])
+
+
+def test_qpe_solver_fixed_point():
+    # Sigma(x) = A / (x - P): a two-point Thiele fraction represents a single pole exactly
+    A, P = 0.1, -2.0
+    xs = [0.5j, 1.5j]
+    pade = Pade(2, xs, [A / (x - P) for x in xs])
+    assert abs(pade(0.7) - A / (0.7 - P)) < 1e-14
+    e_mf, ef, vxc, sx = -0.4, -0.1, -0.3, -0.6
+    info, e, sig = qpe_solve(pade, e_mf=e_mf, e_fermi=ef, vxc=vxc, sigma_x=sx)
+    assert info == 0
+    assert abs(sig - A / (e - ef - P)) < 1e-6          # Sigma at the last iterate
+    assert abs(e - (e_mf - vxc + sx + A / (e - ef - P))) < 1e-5   # the QP equation
+
+
+def test_power_hemat_filters_below_threshold():
+    rng = np.random.default_rng(1)
+    Q, _ = np.linalg.qr(rng.standard_normal((6, 6)))
+    w = np.array([-1e-3, 1e-9, 0.5, 1.0, 2.0, 4.0])
+    A = (Q * w) @ Q.T
+    S = power_hemat(A, 0.5, 0.0)       # negative eigenvalue dropped
+    np.testing.assert_allclose(S @ S, (Q * np.where(w >= 0, w, 0)) @ Q.T, atol=1e-12)
+    S = power_hemat(A, 0.5, 1e-6)      # everything below 1e-6 dropped
+    np.testing.assert_allclose(S @ S, (Q * np.where(w >= 1e-6, w, 0)) @ Q.T, atol=1e-12)
+
+
+def test_wc_is_vcut_half_epsinv_minus_one_vcut_half():
+    """Without truncation (V_cut = V) and a small chi0, Wc = (1 - V chi0)^-1 V - V."""
+    rng = np.random.default_rng(2)
+    A = rng.standard_normal((8, 8))
+    V = A @ A.T + 8 * np.eye(8)
+    B = rng.standard_normal((8, 8))
+    chi = -0.01 * (B @ B.T)
+    W = wc_freq(chi, V, V)
+    np.testing.assert_allclose(W, np.linalg.solve(np.eye(8) - V @ chi, V) - V, atol=1e-10)
