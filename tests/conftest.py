@@ -25,9 +25,18 @@ def lib():
     return L.load_library()
 
 
-def load_h2o():
-    """H2O regression dataset inputs (golden fixture made by tests/golden/make_fixtures.py)."""
-    z = np.load(GOLDEN / "h2o_libri.npz")
+def _blocks(meta, data, nabf):
+    out, off = {}, 0
+    for ik, I, J in meta:
+        n = nabf[I] * nabf[J]
+        out[(int(ik), int(I), int(J))] = data[off:off + n].reshape(nabf[I], nabf[J])
+        off += n
+    return out
+
+
+def load_h2o(fixture="h2o_libri.npz"):
+    """Regression dataset inputs (golden fixture made by tests/golden/make_fixtures.py)."""
+    z = np.load(GOLDEN / fixture)
     Cs = {}
     off = 0
     nao = [int(x) for x in z["nao"]]
@@ -47,8 +56,22 @@ def load_h2o():
         n_ao=int(z["n_ao"]), wg=z["wg"], ekb=z["ekb"], efermi=float(z["efermi"]), wfc=z["wfc"],
         latvec=z["latvec"], period=tuple(int(x) for x in z["period"]), kvecs=z["kvecs"],
         ibz_map=z["ibz_map"], nao=nao, nabf=nabf, positions=z["positions"], types=np.zeros(len(nao), int),
-        Cs=Cs, Vq=Vq, nfreq=int(z["nfreq"]), ec_reference=float(z["ec_reference"]),
+        Cs=Cs, Vq=Vq, nfreq=int(z["nfreq"]),
+        ec_reference=float(z["ec_reference"]) if "ec_reference" in z else None,
         minimax_emin=-1.0, minimax_emax=-1.0)
+
+
+def load_li_g0w0():
+    """The spin-polarised Li atom G0W0 regression case: inputs, truncated Coulomb, v_xc and the
+    reference quasi-particle tables (one per spin)."""
+    s = load_h2o("li_g0w0.npz")
+    z = np.load(GOLDEN / "li_g0w0.npz")
+    s.name = "li"
+    s.v_cut = _blocks(z["vcut_meta"], z["vcut_data"], s.nabf)
+    s.vxc = z["vxc"]
+    s.qp_tables = z["tables"]
+    s.n_params_anacon = int(z["n_params_anacon"])
+    return s
 
 
 def load_h2o_g0w0():
@@ -56,14 +79,8 @@ def load_h2o_g0w0():
     Coulomb) plus the dielectric Coulomb matrix, v_xc and the reference quasi-particle table."""
     s = load_h2o()
     z = np.load(GOLDEN / "h2o_g0w0.npz")
-    veps = {}
-    off = 0
-    for ik, I, J in z["veps_meta"]:
-        n = s.nabf[I] * s.nabf[J]
-        veps[(int(ik), int(I), int(J))] = z["veps_data"][off:off + n].reshape(s.nabf[I], s.nabf[J])
-        off += n
     s.v_cut = s.Vq
-    s.Vq = veps
+    s.Vq = _blocks(z["veps_meta"], z["veps_data"], s.nabf)
     s.vxc = z["vxc"]
     s.qp_table = z["table"]
     s.nfreq = int(z["nfreq"])

@@ -25,8 +25,14 @@ Produces (all committed, so the tests need no reference tree at run time):
                      (refs/g0w0_aims_mole_H2O_libri/librpa/librpa.out: state, occ, e_mf, v_xc,
                      v_exx, ReSigc, ImSigc, e_qp in eV) and its librpa.in settings.
 
+  li_g0w0.npz        the spin-polarised Li atom G0W0 regression case
+                     (regression_tests/testcases/g0w0_aims_Li_atom_libri/dataset.tar.gz):
+                     all of its inputs in the h2o_libri.npz layout, its truncated Coulomb and
+                     v_xc, and both spin channels' quasi-particle tables
+                     (refs/g0w0_aims_Li_atom_libri/librpa/librpa.out)
+
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|g0w0 ...].
+h2o_dataset|g0w0|li_g0w0 ...].
 """
 from __future__ import annotations
 
@@ -169,8 +175,54 @@ def g0w0(ref: Path):
     print("h2o_g0w0.npz written:", len(table), "states")
 
 
+def _qp_tables(log_lines):
+    """Every "State occ e_mf ..." table of a G0W0 log (one per spin channel and k-point)."""
+    tables = []
+    for k, l in enumerate(log_lines):
+        if re.match(r"State\s+occ\s+e_mf", l):
+            i, rows = k + 2, []
+            while i < len(log_lines) and log_lines[i].strip():
+                rows.append(_floats(log_lines[i]))
+                i += 1
+            tables.append(rows)
+    return tables
+
+
+def li_g0w0(ref: Path):
+    case = "g0w0_aims_Li_atom_libri"
+    tgz = ref / f"regression_tests/testcases/{case}/dataset.tar.gz"
+    log = (ref / f"regression_tests/refs/{case}/librpa/librpa.out").read_text().splitlines()
+    params = (ref / f"regression_tests/testcases/{case}/librpa/librpa.in").read_text()
+    nfreq = int(re.search(r"nfreq\s*=\s*(\d+)", params).group(1))
+    m = re.search(r"n_params_anacon\s*=\s*(-?\d+)", params)
+    n_params = int(m.group(1)) if m else -1  # the option's default (src/api/options.cpp:45)
+    with tempfile.TemporaryDirectory() as td:
+        with tarfile.open(tgz) as tf:
+            tf.extractall(td, filter="data")
+        d = next(Path(td).rglob("band_out")).parent
+        inp = read_dataset(str(d))
+        cut = read_coulomb(str(d), "coulomb_cut", inp.nabf)
+        vxc = read_vxc(str(d / "vxc_out"))
+    keys = sorted(inp.Cs)
+    vkeys = sorted(inp.Vq)
+    ckeys = sorted(cut)
+    np.savez_compressed(
+        HERE / "li_g0w0.npz",
+        n_spins=inp.n_spins, n_kpts=inp.n_kpts, n_bands=inp.n_bands, n_ao=inp.n_ao,
+        wg=inp.wg, ekb=inp.ekb, efermi=inp.efermi, wfc=inp.wfc, latvec=inp.latvec,
+        period=np.array(inp.period), kvecs=inp.kvecs, ibz_map=inp.ibz_map,
+        nao=np.array(inp.nao), nabf=np.array(inp.nabf), positions=inp.positions,
+        cs_meta=np.array([[I, J, *R] for (I, J, R) in keys], np.int32),
+        cs_data=np.concatenate([inp.Cs[k].ravel() for k in keys]),
+        vq_meta=np.array(vkeys, np.int32), vq_data=np.concatenate([inp.Vq[k].ravel() for k in vkeys]),
+        vcut_meta=np.array(ckeys, np.int32), vcut_data=np.concatenate([cut[k].ravel() for k in ckeys]),
+        vxc=vxc, tables=np.array(_qp_tables(log)), nfreq=nfreq, n_params_anacon=n_params)
+    print("li_g0w0.npz written")
+
+
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-    which = sys.argv[2:] or ["h2o", "h2o_dataset", "minimax", "he_bcc", "g0w0"]
+    which = sys.argv[2:] or ["h2o", "h2o_dataset", "minimax", "he_bcc", "g0w0", "li_g0w0"]
     for name in which:
-        {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0}[name](ref)
+        {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
+         "li_g0w0": li_g0w0}[name](ref)

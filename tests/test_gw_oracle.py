@@ -3,7 +3,7 @@ and its pieces checked on their own (no GPU)."""
 import numpy as np
 import pytest
 
-from conftest import load_h2o_g0w0, oracle_input
+from conftest import load_h2o_g0w0, load_li_g0w0, oracle_input
 from oracle.gw_oracle import (HA2EV, Pade, cal_hs_loops, full_from_blocks, g0w0_gamma, ordered_blocks,
                               power_hemat, qpe_solve, wc_freq)
 from oracle.rpa_oracle import Options, cs_tensors
@@ -35,6 +35,20 @@ def test_h2o_quasiparticle_table(h2o):
         np.testing.assert_allclose(got[name], t[:, col], rtol=0, atol=6e-6, err_msg=name)
     # the printed e_qp is e_mf - v_xc + v_exx + Re Sigma_c (driver/task/g0w0.cpp:274)
     np.testing.assert_allclose(t[:, 2] - t[:, 3] + t[:, 4] + t[:, 5], t[:, 7], atol=2.5e-5)
+
+
+def test_li_atom_both_spin_channels():
+    """The spin-polarised Li atom (refs/g0w0_aims_Li_atom_libri/librpa/librpa.out, 16 points,
+    all of them in the Pade fit): every column of both spin channels to print precision."""
+    s = load_li_g0w0()
+    inp = oracle_input(s)
+    assert inp.n_spins == 2
+    r = g0w0_gamma(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon)
+    for sp in range(2):
+        t = s.qp_tables[sp]
+        got = np.c_[inp.ekb[sp, 0] * HA2EV, s.vxc[sp, 0] * HA2EV, r["vexx"][sp] * HA2EV,
+                    r["sigc"][sp].real * HA2EV, r["sigc"][sp].imag * HA2EV, r["e_qp"][sp] * HA2EV]
+        np.testing.assert_allclose(got, t[:, 2:], rtol=0, atol=6e-6, err_msg=f"spin {sp}")
 
 
 def test_sigma_on_the_imaginary_axis_has_negative_imaginary_part(h2o):
