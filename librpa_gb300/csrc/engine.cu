@@ -26,6 +26,7 @@
 
 #include "chi0_fast.h"
 #include "common.h"
+#include "cs_fold.h"
 #include "dataset.h"
 #include "ec_tc.h"
 #include "gk_tc.h"
@@ -37,13 +38,6 @@
 namespace gb {
 
 namespace {
-
-int centred_mod(int i, int n)
-{
-    int r = i % n;  // C semantics, like LibRI's Array_Operator::operator%
-    r = (r + 3 * n / 2) % n;
-    return r - n / 2;
-}
 
 struct Cells
 {
@@ -239,27 +233,19 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     for (int I = 0; I < n_at; ++I)
         for (int a = abf_off[I]; a < abf_off[I + 1]; ++a) atom_of[a] = I;
 
-    // RI blocks -> (I, J, cell) table; LibRI skips keys outside the BvK cell list
-    const double thr_c = opts.libri_chi0_threshold_C;
-    std::vector<long long> cs_off;
-    std::vector<int> cs_meta;
+    // RI blocks -> (I, J, cell) table: cell vectors folded into the BvK cell list, blocks that
+    // fold onto one key summed, then LibRI's threshold filter (cs_fold.h)
     for (const CsBlock &b : ds.cs_blocks)
     {
         GB_REQUIRE(b.I >= 0 && b.I < n_at && b.J >= 0 && b.J < n_at, "RI block atom index out of range");
         GB_REQUIRE(b.ni == ds.nao_at[b.I] && b.nj == ds.nao_at[b.J] && b.nmu == ds.nabf_at[b.I],
                    "RI block dimensions inconsistent with the bases");
-        const int c = cells.index.count({b.R[0], b.R[1], b.R[2]}) ? cells.index.at({b.R[0], b.R[1], b.R[2]}) : -1;
-        if (c < 0) continue;
-        if (thr_c > 0)
-        {
-            double mx = 0.0;
-            const size_t n = static_cast<size_t>(b.ni) * b.nj * b.nmu;
-            for (size_t t = 0; t < n; ++t) mx = std::max(mx, std::fabs(ds.cs_blob[b.offset + t]));
-            if (mx <= thr_c) continue;  // LibRI keeps a block whose max-norm exceeds the threshold
-        }
-        cs_off.push_back(static_cast<long long>(b.offset));
-        cs_meta.insert(cs_meta.end(), {b.I, b.J, c, 0});
     }
+    CsFold csf = fold_cs_blocks(
+        ds.cs_blocks, ds.cs_blob.data(), ds.cs_blob.size(), ds.period,
+        [&](const std::array<int, 3> &R) { return cells.find(R[0], R[1], R[2]); }, opts.libri_chi0_threshold_C);
+    const std::vector<long long> &cs_off = csf.off;
+    const std::vector<int> &cs_meta = csf.meta;
 
     // Coulomb blocks per IBZ q (upper pairs)
     std::vector<std::vector<int>> vq_of_q(nq);
@@ -326,8 +312,11 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         din->psi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()), ds.wfc.size(), st);
         din->vblob.alloc(ds.vq_blob.size());
         din->vblob.upload(reinterpret_cast<const cuDoubleComplex *>(ds.vq_blob.data()), ds.vq_blob.size(), st);
-        DevBuf<double> d_csblob(ds.cs_blob.size());
+        DevBuf<double> d_csblob(ds.cs_blob.size() + csf.extra.size());
         d_csblob.upload(ds.cs_blob.data(), ds.cs_blob.size(), st);
+        if (!csf.extra.empty())
+            GB_CUDA(cudaMemcpyAsync(d_csblob.get() + ds.cs_blob.size(), csf.extra.data(),
+                                    csf.extra.size() * sizeof(double), cudaMemcpyHostToDevice, st));
         auto d_csoff = to_dev(cs_off, st);
         auto d_csmeta = to_dev(cs_meta, st);
         h2d = 8.0 * (ds.ekb.size() + ds.wg.size() + ds.cs_blob.size()) + 16.0 * (ds.wfc.size() + ds.vq_blob.size());

@@ -283,3 +283,24 @@ def to_oracle_input(s: SynthSystem):
                     ekb=s.ekb, efermi=s.efermi, wfc=s.wfc, latvec=s.latvec, period=s.period,
                     kvecs=s.kvecs, ibz_map=s.ibz_map, nao=s.nao, nabf=s.nabf, Cs=s.Cs, Vq=s.Vq,
                     positions=s.positions)
+
+
+def with_cells_relabelled(s, split: bool = False):
+    """The same system with every C block's cell vector given in [0, n) (the Born-von Karman
+    range FHI-aims writes) instead of the centred range; split=True also spreads each block over
+    two images one period apart (halves that LibRI's folding sums back)."""
+    import copy
+
+    t = copy.copy(s)
+    per = tuple(s.period)
+    cs = {}
+    for (I, J, R), m in s.Cs.items():
+        r0 = tuple(int(R[d]) % per[d] for d in range(3))
+        if not split:
+            cs[(I, J, r0)] = m
+            continue
+        r1 = (r0[0] + per[0], r0[1], r0[2])
+        cs[(I, J, r0)] = m * 0.5
+        cs[(I, J, r1)] = m - m * 0.5
+    t.Cs = cs
+    return t

@@ -31,7 +31,7 @@ import math
 
 import numpy as np
 
-from .rpa_oracle import (Options, RPAInput, assemble_full, blocks_of, build_gf, centred_mod,
+from .rpa_oracle import (TWO_PI, Options, RPAInput, assemble_full, blocks_of, build_gf, centred_mod,
                          chi0q_partial, cs_tensors, grids_for, k_lists, r_grid, upper_pairs)
 
 HA2EV = 27.211386245988  # src/utils/constants.cpp:13 (the driver's default "internal" choice)
@@ -190,6 +190,100 @@ def qpe_solve(pade: Pade, e_mf, e_fermi, vxc, sigma_x, diff_init=1.0e-3, thres=1
             break
     info = 1 if n_iter > n_iter_max - 1 else 0
     return info, e_last, sig_last
+
+
+# ----------------------------------------------------------------------------- periodic exchange
+
+def coulomb_r(inp: RPAInput, vq: dict, rlist):
+    """FT_Vq (coulmat.cpp:7-90) with ordered atom pairs: V(R) = Re sum_q sum_{q' in star(q)}
+    e^{-i 2 pi q'.R} / n_k V(q) (conjugated for q' != q, the time-reversed partner)."""
+    klist, _, ibz_order, _ = k_lists(inp)
+    star = {r: [k for k in range(inp.n_kpts) if int(inp.ibz_map[k]) == r] for r in ibz_order}
+    out = {}
+    for R in rlist:
+        Rc = np.asarray(R, float) @ inp.latvec
+        for (iq, I, J), v in vq.items():
+            acc = np.zeros_like(v, dtype=complex)
+            acc_t = np.zeros((v.shape[1], v.shape[0]), complex)
+            for kb in star[iq]:
+                ph = np.exp(-1j * TWO_PI * float(np.dot(klist[kb], Rc))) / inp.n_kpts
+                if kb == iq:
+                    acc += v * ph
+                    acc_t += v.conj().T * ph
+                else:
+                    acc += v.conj() * ph
+                    acc_t += v.T * ph
+            key = (I, J, tuple(R))
+            out[key] = out.get(key, 0) + acc.real
+            if I != J and (iq, J, I) not in vq:
+                key = (J, I, tuple(R))
+                out[key] = out.get(key, 0) + acc_t.real
+    return out
+
+
+def dmat_r(inp: RPAInput, ispin: int, rlist):
+    """get_dmat_cplx_R (meanfield.cpp:201-244): D(R) = sum_k e^{-i 2 pi k.R} D(k),
+    D(k)_ij = sum_n w_n psi_ni psi_nj^*, real part; atom blocks of every ordered pair."""
+    _, kfrac, _, _ = k_lists(inp)
+    wg = inp.wg[ispin] / inp.n_kpts
+    dk = []
+    for k in range(inp.n_kpts):
+        ev = inp.wfc[ispin, k]
+        w = np.zeros(inp.n_bands)
+        for n in range(inp.n_bands):
+            w[n] = wg[k, n] * 0.5 * inp.n_spins
+            if w[n] < 1e-4 / inp.n_kpts:
+                w[n] = 0.0
+                break
+        dk.append(ev.T @ (w[:, None] * ev.conj()))
+    full = {}
+    for R in rlist:
+        acc = np.zeros((inp.n_ao, inp.n_ao), complex)
+        for k in range(inp.n_kpts):
+            acc += np.exp(-1j * TWO_PI * float(np.dot(kfrac[k], R))) * dk[k]
+        full[tuple(R)] = acc.real
+    return blocks_of(full, inp.nao)
+
+
+def shift_bvk(H: dict, inp: RPAInput):
+    """Each (I, J, R) block moved to the image R + n period (n in {-1, 0, 1}^3) nearest to
+    x_I - x_J - R (exx.cpp:683-725; applied when fractional coordinates are set)."""
+    frac = inp.positions @ np.linalg.inv(inp.latvec)
+    per = np.asarray(inp.period)
+    out = {}
+    for (I, J, R), m in H.items():
+        best, Rb = math.inf, None
+        for i in (-1, 0, 1):
+            for j in (-1, 0, 1):
+                for k in (-1, 0, 1):
+                    Rij = np.asarray(R) + per * np.array([i, j, k])
+                    d = (frac[I] - frac[J] - Rij) @ inp.latvec
+                    n2 = float(d @ d)
+                    if n2 < best:
+                        best, Rb = n2, tuple(int(x) for x in Rij)
+        out[(I, J, Rb)] = m
+    return out
+
+
+def exx_kgrid(inp: RPAInput, v_cut: dict):
+    """v_exx[s, k, n] (Hartree) on the SCF k-grid (task = exx; exx.cpp:213-500, :720-860)."""
+    _, kfrac, _, _ = k_lists(inp)
+    rlist = r_grid(inp.period)
+    C = cs_tensors(inp, 0.0)
+    VR = coulomb_r(inp, v_cut, rlist)
+    out = np.zeros((inp.n_spins, inp.n_kpts, inp.n_bands))
+    off = np.concatenate([[0], np.cumsum(inp.nao)]).astype(int)
+    for s in range(inp.n_spins):
+        H = cal_hs_loops(C, VR, dmat_r(inp, s, rlist), inp.n_atoms, inp.period)
+        H = shift_bvk(H, inp)
+        for k in range(inp.n_kpts):
+            Hk = np.zeros((inp.n_ao, inp.n_ao), complex)
+            for (I, J, R), m in H.items():
+                ph = np.exp(1j * TWO_PI * float(np.dot(kfrac[k], R)))
+                Hk[off[I]:off[I + 1], off[J]:off[J + 1]] += ph * m
+            ev = inp.wfc[s, k]
+            out[s, k] = -np.einsum("ni,ij,nj->n", ev.conj(), Hk, ev).real
+    return out
 
 
 # ----------------------------------------------------------------------------- pipeline

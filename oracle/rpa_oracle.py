@@ -191,14 +191,22 @@ def blocks_of(full: dict, nao):
 # ----------------------------------------------------------------------------- chi0 (LibRI algebra)
 
 def cs_tensors(inp: RPAInput, threshold: float = 0.0):
-    """LibRI form C[I][(J,R)] with shape (n_mu, n_i, n_j) (input.cpp:525-541); threshold filter."""
-    out = {}
+    """LibRI form C[I][(J,R)] with shape (n_mu, n_i, n_j) (input.cpp:525-541).
+
+    As LibRI's set_tensors does (RI_Tools::cal_period, LRI-set.hpp:47-52 and RI_Tools.hpp:49-67),
+    the cell vector is first taken modulo the BvK period into the centred range, blocks that land
+    on the same key are summed, and only then the threshold filter applies."""
+    summed = {}
     for (I, J, R), m in inp.Cs.items():
         ni, nj = inp.nao[I], inp.nao[J]
         t = m.T.reshape(m.shape[1], ni, nj)
+        key = (I, J, centred_mod(tuple(R), inp.period))
+        summed[key] = summed[key] + t if key in summed else t
+    out = {}
+    for key, t in summed.items():
         if threshold > 0 and np.abs(t).max() <= threshold:  # kept when max-norm > threshold (LRI.hpp:20-25)
             continue
-        out[(I, J, tuple(R))] = t
+        out[key] = t
     return out
 
 

@@ -88,6 +88,17 @@ def load_h2o_g0w0():
     return s
 
 
+def load_he_exx():
+    """The periodic BCC He exchange case: inputs, truncated Coulomb V(q) and the reference
+    v_exx tables (per k-point: band, Hartree, eV)."""
+    s = load_h2o("he_exx.npz")
+    z = np.load(GOLDEN / "he_exx.npz")
+    s.name = "he_exx"
+    s.v_cut = _blocks(z["vcut_meta"], z["vcut_data"], s.nabf)
+    s.exx_tables = z["tables"]
+    return s
+
+
 def minimax_ref():
     return json.loads((GOLDEN / "minimax_ref.json").read_text())
 

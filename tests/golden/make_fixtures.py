@@ -31,8 +31,14 @@ Produces (all committed, so the tests need no reference tree at run time):
                      v_xc, and both spin channels' quasi-particle tables
                      (refs/g0w0_aims_Li_atom_libri/librpa/librpa.out)
 
+  he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
+                     regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
+                     its inputs, truncated Coulomb V(q) and the v_exx tables of every k-point
+                     printed by the reference run (refs/exx_aims_bccHe_k_parallel_libri/librpa/
+                     librpa.out, Hartree and eV; the suite checks the first to 1e-4)
+
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|g0w0|li_g0w0 ...].
+h2o_dataset|g0w0|li_g0w0|he_exx ...].
 """
 from __future__ import annotations
 
@@ -220,9 +226,43 @@ def li_g0w0(ref: Path):
     print("li_g0w0.npz written")
 
 
+def he_exx(ref: Path):
+    case = "exx_aims_bccHe_k_parallel_libri"
+    tgz = ref / f"regression_tests/testcases/{case}/dataset.tar.gz"
+    log = (ref / f"regression_tests/refs/{case}/librpa/librpa.out").read_text().splitlines()
+    tables = []
+    for k, l in enumerate(log):
+        if re.match(r"Band\s+e_exx", l):
+            i, rows = k + 1, []
+            while i < len(log) and log[i].strip():
+                rows.append(_floats(log[i]))
+                i += 1
+            tables.append(rows)
+    with tempfile.TemporaryDirectory() as td:
+        with tarfile.open(tgz) as tf:
+            tf.extractall(td, filter="data")
+        d = next(Path(td).rglob("band_out")).parent
+        inp = read_dataset(str(d))
+        cut = read_coulomb(str(d), "coulomb_cut", inp.nabf)
+    keys = sorted(inp.Cs)
+    ckeys = sorted(cut)
+    np.savez_compressed(
+        HERE / "he_exx.npz",
+        n_spins=inp.n_spins, n_kpts=inp.n_kpts, n_bands=inp.n_bands, n_ao=inp.n_ao,
+        wg=inp.wg, ekb=inp.ekb, efermi=inp.efermi, wfc=inp.wfc, latvec=inp.latvec,
+        period=np.array(inp.period), kvecs=inp.kvecs, ibz_map=inp.ibz_map,
+        nao=np.array(inp.nao), nabf=np.array(inp.nabf), positions=inp.positions,
+        cs_meta=np.array([[I, J, *R] for (I, J, R) in keys], np.int32),
+        cs_data=np.concatenate([inp.Cs[k].ravel() for k in keys]),
+        vq_meta=np.zeros((0, 3), np.int32), vq_data=np.zeros(0, complex),
+        vcut_meta=np.array(ckeys, np.int32), vcut_data=np.concatenate([cut[k].ravel() for k in ckeys]),
+        tables=np.array(tables), nfreq=0)
+    print("he_exx.npz written:", len(tables), "k-points")
+
+
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-    which = sys.argv[2:] or ["h2o", "h2o_dataset", "minimax", "he_bcc", "g0w0", "li_g0w0"]
+    which = sys.argv[2:] or ["h2o", "h2o_dataset", "minimax", "he_bcc", "g0w0", "li_g0w0", "he_exx"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
-         "li_g0w0": li_g0w0}[name](ref)
+         "li_g0w0": li_g0w0, "he_exx": he_exx}[name](ref)

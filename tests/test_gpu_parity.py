@@ -65,6 +65,20 @@ def test_small_periodic_fp64_vs_oracle(period, nao, nabf, nocc):
                 np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("split", [False, True])
+def test_cell_vectors_outside_the_centred_range(split):
+    """C blocks given on cells [0, n) (as FHI-aims writes them), or split over two images a
+    period apart, are folded into the centred BvK range and summed as LibRI does: the same
+    E_c as the centred input, on the FP64 and the tensor-core paths."""
+    s = sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=(3, 2, 1), nocc=2, seed=5)
+    t = sy.with_cells_relabelled(s, split=split)
+    for prec in (L.CHI0_FP64, L.CHI0_BF16X3):
+        _, a, pa = run_gpu(s, prec)
+        _, b, pb = run_gpu(t, prec)
+        assert abs(a - b) <= 1e-12 * abs(a), (prec, a, b)
+        np.testing.assert_allclose(pb, pa, rtol=1e-11, atol=1e-15)
+
+
 def test_fcc2_k222_fp64_vs_oracle():
     s = sy.fcc2_k222()
     h, ec, perq = run_gpu(s, L.CHI0_FP64)

@@ -3,9 +3,9 @@ and its pieces checked on their own (no GPU)."""
 import numpy as np
 import pytest
 
-from conftest import load_h2o_g0w0, load_li_g0w0, oracle_input
-from oracle.gw_oracle import (HA2EV, Pade, cal_hs_loops, full_from_blocks, g0w0_gamma, ordered_blocks,
-                              power_hemat, qpe_solve, wc_freq)
+from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, oracle_input
+from oracle.gw_oracle import (HA2EV, Pade, cal_hs_loops, exx_kgrid, full_from_blocks, g0w0_gamma,
+                              ordered_blocks, power_hemat, qpe_solve, wc_freq)
 from oracle.rpa_oracle import Options, cs_tensors
 
 
@@ -49,6 +49,20 @@ def test_li_atom_both_spin_channels():
         got = np.c_[inp.ekb[sp, 0] * HA2EV, s.vxc[sp, 0] * HA2EV, r["vexx"][sp] * HA2EV,
                     r["sigc"][sp].real * HA2EV, r["sigc"][sp].imag * HA2EV, r["e_qp"][sp] * HA2EV]
         np.testing.assert_allclose(got, t[:, 2:], rtol=0, atol=6e-6, err_msg=f"spin {sp}")
+
+
+def test_periodic_exchange_bcc_he_every_k_point():
+    """Periodic exchange (2-atom cell, 2x2x2 k-points, C blocks given on cells [0, 2) that LibRI
+    folds into the centred BvK range): v_exx of all 8 bands at all 8 k-points against
+    refs/exx_aims_bccHe_k_parallel_libri/librpa/librpa.out (5 decimals in Hartree; the suite
+    checks the first k-point to 1e-4)."""
+    s = load_he_exx()
+    inp = oracle_input(s)
+    assert inp.n_kpts == 8 and any(max(R) > 0 for (_I, _J, R) in inp.Cs)
+    e = exx_kgrid(inp, s.v_cut)
+    t = s.exx_tables
+    assert t.shape == (8, 8, 3)
+    np.testing.assert_allclose(e[0], t[:, :, 1], rtol=0, atol=6e-6)
 
 
 def test_sigma_on_the_imaginary_axis_has_negative_imaginary_part(h2o):

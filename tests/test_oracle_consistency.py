@@ -52,3 +52,17 @@ def test_ec_negative_and_real_parts_consistent():
                                                         minimax_emax=s.minimax_emax))
     assert r["ec"].real < 0
     assert abs(r["ec"].imag) < 1e-10 * abs(r["ec"].real)
+
+
+@pytest.mark.parametrize("split", [False, True])
+def test_cell_vectors_fold_like_libri(split):
+    """C blocks given on cells [0, n), or split over two images a period apart, give the E_c of
+    the centred input: cs_tensors folds them as LibRI's cal_period does."""
+    from oracle.rpa_oracle import rpa_correlation_energy
+    s = sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=(3, 2, 1), nocc=2, seed=5)
+    t = sy.with_cells_relabelled(s, split=split)
+    assert set(t.Cs) != set(s.Cs)
+    o = Options(nfreq=s.nfreq, minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
+    a = rpa_correlation_energy(oracle_input(s), o)["ec"]
+    b = rpa_correlation_energy(oracle_input(t), o)["ec"]
+    assert abs(a - b) <= 1e-13 * abs(a)
