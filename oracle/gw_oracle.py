@@ -1,7 +1,9 @@
-"""Oracle (test infrastructure only): G0W0 quasi-particle energies at the Gamma point.
+"""Oracle (test infrastructure only): exact exchange on k-grids and G0W0 quasi-particle
+energies at the Gamma point.
 
-CPU FP64 restatement of LibRPA's G0W0 chain (task = g0w0) for Gamma-only inputs (molecules
-and Gamma-point cells), built on the RPA oracle's chi0(q, omega):
+CPU FP64 restatement of LibRPA's EXX (task = exx, any k-grid: exx_kgrid) and G0W0 chain
+(task = g0w0, Gamma-only inputs: molecules and Gamma-point cells; g0w0_gamma), built on the RPA
+oracle's chi0(q, omega):
 
   exchange  H(R) = LibRI Exx::cal_Hs, labels a0b0_{a1b1,a1b2,a2b1,a2b2}
                    (thirdparty/LibRI/include/RI/physics/Exx.hpp:242-283) with
@@ -22,8 +24,9 @@ and Gamma-point cells), built on the RPA oracle's chi0(q, omega):
   continuation  Thiele reciprocal differences (AnalyContPade, src/core/analycont.cpp:12-70)
   QP equation   damped fixed point (qpe_solver_pade_self_consistent, src/core/qpe_solver.cpp)
 
-The reference's own regression output for the H2O molecule (24 states, 16 minimax points,
-16 Pade parameters) pins the result: tests/golden/h2o_g0w0.npz.
+Pinned by the reference's own regression outputs: the H2O molecule (24 states, 16 minimax
+points, 16 Pade parameters; tests/golden/h2o_g0w0.npz), the spin-polarised Li atom
+(li_g0w0.npz) and the periodic BCC He exchange on a 2x2x2 k-grid (he_exx.npz).
 """
 from __future__ import annotations
 
