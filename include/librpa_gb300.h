@@ -113,6 +113,20 @@ int librpa_gb300_minimax_grid(int n, double emin, double emax, double regulariza
                               double *cos_t2f, double *cos_f2t, double *sin_t2f,
                               double *duality_error);
 
+/* G0W0 quasi-particle equation for n_states states (host only, no GPU needed): the Thiele-Pade
+ * continuation of each state's Sigma_c(i omega_k), k < n_freq (sigc_re/im[state * n_freq + k],
+ * omega_k > 0 the imaginary frequencies), with n_params parameters (< 0: all points), then the
+ * damped fixed point e = e_mf - vxc + vexx + Re Sigma_c(e - e_fermi).  Replaces the per-state
+ * loop of librpa_get_g0w0_sigc_kgrid (src/api/compute_g0w0.cpp:270-300; AnalyContPade,
+ * src/core/analycont.cpp:12-70; qpe_solver_pade_self_consistent, src/core/qpe_solver.cpp).
+ * Outputs per state: e_qp and Sigma_c(e_qp); NaN where the iteration hit its limit (counted in
+ * the return value) or the continued fraction broke down (0/0), as the reference reports them.
+ * Returns the number of states that hit the iteration limit, or -1 on error. */
+int librpa_gb300_solve_qpe(int n_states, int n_freq, const double *omegas, const double *sigc_re,
+                           const double *sigc_im, int n_params, const double *e_mf, double e_fermi,
+                           const double *vxc, const double *vexx, double *e_qp, double *sigc_qp_re,
+                           double *sigc_qp_im);
+
 /* After a call with keep_chi0 = 1: copy chi0(q_ibz, omega) block (I<=J) to the
  * caller as two row-major n_mu x n_nu arrays.  Returns 0 on success. */
 int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq_ibz, int I, int J,

@@ -137,6 +137,7 @@ EXPORTS = [
     "librpa_gb300_get_screening_samples", "librpa_gb300_get_screening_model", "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
+    "librpa_gb300_solve_qpe",
 ]
 
 _lib = None
@@ -200,6 +201,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_copy_chi0_qw": (i, [vp, vp, i]),
         "librpa_gb300_load_chi0_qw": (i, [vp, vp, C.c_longlong, i]),
         "librpa_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, i, vp, C.POINTER(C.c_double)]),
+        "librpa_gb300_solve_qpe": (i, [i, i, _dp, _dp, _dp, i, _dp, d, _dp, _dp, _dp, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -383,6 +385,21 @@ class Handler:
         if math.isnan(ec):
             raise LibrpaError(self.last_error())
         return ec, re[:n_ibz_kpoints] + 1j * im[:n_ibz_kpoints]
+
+
+def solve_qpe(omegas, sigc_iw, e_mf, e_fermi, vxc, vexx, n_params=-1):
+    """Pade continuation + quasi-particle equation per state (librpa_gb300_solve_qpe, host only).
+    sigc_iw: (n_states, n_freq) complex.  Returns (e_qp, sigc_qp complex, n_unconverged)."""
+    lib = load_library()
+    sig = np.ascontiguousarray(sigc_iw, complex)
+    ns, nf = sig.shape
+    e_qp, sr, si = np.zeros(ns), np.zeros(ns), np.zeros(ns)
+    f64 = lambda a: np.ascontiguousarray(a, np.float64)
+    rc = lib.librpa_gb300_solve_qpe(ns, nf, f64(omegas), f64(sig.real), f64(sig.imag), n_params, f64(e_mf),
+                                    float(e_fermi), f64(vxc), f64(vexx), e_qp, sr, si)
+    if rc < 0:
+        raise LibrpaError(lib.librpa_get_last_error(None).decode())
+    return e_qp, sr + 1j * si, rc
 
 
 def minimax_grid(n, emin, emax, regularization=0.0):

@@ -19,6 +19,7 @@
 #include "dataset.h"
 #include "screen.h"
 #include "minimax.h"
+#include "qpe.h"
 #include "tc_gemm.h"
 
 namespace {
@@ -842,6 +843,42 @@ int librpa_gb300_minimax_grid(int n, double emin, double emax, double reg, doubl
         cp(sin_t2f, g.sin_t2f);
         if (dual) *dual = g.cosft_duality_error;
         rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_solve_qpe(int n_states, int n_freq, const double *omegas, const double *sigc_re,
+                           const double *sigc_im, int n_params, const double *e_mf, double e_fermi,
+                           const double *vxc, const double *vexx, double *e_qp, double *sigc_qp_re,
+                           double *sigc_qp_im)
+{
+    int rc = -1;
+    guarded(nullptr, [&] {
+        GB_REQUIRE(n_states >= 0 && n_freq > 0, "need n_states >= 0 and n_freq > 0");
+        GB_REQUIRE(omegas && sigc_re && sigc_im && e_mf && vxc && vexx && e_qp && sigc_qp_re && sigc_qp_im,
+                   "null array");
+        std::vector<std::complex<double>> x(n_freq), f(n_freq);
+        for (int k = 0; k < n_freq; ++k) x[k] = {0.0, omegas[k]};
+        int failed = 0;
+        for (int s = 0; s < n_states; ++s)
+        {
+            for (int k = 0; k < n_freq; ++k)
+                f[k] = {sigc_re[static_cast<size_t>(s) * n_freq + k], sigc_im[static_cast<size_t>(s) * n_freq + k]};
+            const gb::PadeContinuation pade(n_params, x, f);
+            const gb::QpeResult r = gb::solve_qpe(pade, e_mf[s], e_fermi, vxc[s], vexx[s]);
+            if (r.info == 0)
+            {
+                e_qp[s] = r.e_qp;
+                sigc_qp_re[s] = r.sigc.real();
+                sigc_qp_im[s] = r.sigc.imag();
+            }
+            else
+            {
+                e_qp[s] = sigc_qp_re[s] = sigc_qp_im[s] = std::numeric_limits<double>::quiet_NaN();
+                ++failed;
+            }
+        }
+        rc = failed;
     });
     return rc;
 }
