@@ -33,7 +33,8 @@ Produces (all committed, so the tests need no reference tree at run time):
 
   he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
                      regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
-                     its inputs, truncated Coulomb V(q) and the v_exx tables of every k-point
+                     its inputs (bare Coulomb V(q) included, for RPA runs on real periodic
+                     FHI-aims data), truncated Coulomb V(q) and the v_exx tables of every k-point
                      printed by the reference run (refs/exx_aims_bccHe_k_parallel_libri/librpa/
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
@@ -254,9 +255,10 @@ def he_exx(ref: Path):
         nao=np.array(inp.nao), nabf=np.array(inp.nabf), positions=inp.positions,
         cs_meta=np.array([[I, J, *R] for (I, J, R) in keys], np.int32),
         cs_data=np.concatenate([inp.Cs[k].ravel() for k in keys]),
-        vq_meta=np.zeros((0, 3), np.int32), vq_data=np.zeros(0, complex),
+        vq_meta=np.array(sorted(inp.Vq), np.int32),
+        vq_data=np.concatenate([inp.Vq[k].ravel() for k in sorted(inp.Vq)]),
         vcut_meta=np.array(ckeys, np.int32), vcut_data=np.concatenate([cut[k].ravel() for k in ckeys]),
-        tables=np.array(tables), nfreq=0)
+        tables=np.array(tables), nfreq=16)
     print("he_exx.npz written:", len(tables), "k-points")
 
 

@@ -3,7 +3,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_h2o, oracle_input
+from conftest import load_h2o, load_he_exx, oracle_input
 from librpa_gb300 import synthetic as sy
 from oracle.rpa_oracle import Options as OOpts, rpa_correlation_energy
 
@@ -77,6 +77,18 @@ def test_cell_vectors_outside_the_centred_range(split):
         _, b, pb = run_gpu(t, prec)
         assert abs(a - b) <= 1e-12 * abs(a), (prec, a, b)
         np.testing.assert_allclose(pb, pa, rtol=1e-11, atol=1e-15)
+
+
+def test_he_bcc_fhi_aims_periodic_vs_oracle():
+    """Real periodic FHI-aims input (BCC He, 2x2x2 k-points, C cells written in [0, 2)): FP64 path
+    vs the oracle, and the default tensor-core path within 0.1 meV/atom."""
+    s = load_he_exx()
+    o = run_oracle(s)
+    _, ec, perq = run_gpu(s, L.CHI0_FP64)
+    assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
+    np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
+    _, ec2, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
 
 
 def test_fcc2_k222_fp64_vs_oracle():

@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import he_ref, load_h2o, minimax_ref, oracle_input
+from conftest import he_ref, load_h2o, load_he_exx, minimax_ref, oracle_input
 from oracle.minimax import minimax_grid
 from oracle.rpa_oracle import Options, build_gf, e_min_max, k_lists, r_grid, rpa_correlation_energy
 
@@ -59,3 +59,15 @@ def test_he_bcc_gf_minus_density_matrix():
     for c in d["checks"]:
         val = D[c["i"], c["j"]] if c["what"] == "dmat_gamma" else G[c["i"], c["j"]]
         assert abs(val - c["value"]) < d["thres"]
+
+
+def test_he_bcc_periodic_rpa_loops_equal_dense():
+    """Real periodic FHI-aims data (BCC He, 2x2x2 k-points, C cells in [0, 2) that LibRI folds):
+    the literal LibRI-loop chi0 and the dense restatement give one E_c.  The loop conventions
+    they share are pinned by the periodic exchange of the same dataset (test_gw_oracle.py)."""
+    s = load_he_exx()
+    inp = oracle_input(s)
+    a = rpa_correlation_energy(inp, Options(nfreq=16), chi0_impl="dense")["ec"]
+    b = rpa_correlation_energy(inp, Options(nfreq=16), chi0_impl="loops")["ec"]
+    assert a.real < 0 and abs(a.imag) < 1e-12
+    assert abs(a - b) <= 1e-11 * abs(a)
