@@ -31,6 +31,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      v_xc, and both spin channels' quasi-particle tables
                      (refs/g0w0_aims_Li_atom_libri/librpa/librpa.out)
 
+  he_bcc_dataset.tar.gz  the BCC He dataset itself (copied unchanged), for the driver's periodic test
   he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
                      regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
                      its inputs (bare Coulomb V(q) included, for RPA runs on real periodic
@@ -39,7 +40,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|g0w0|li_g0w0|he_exx ...].
+h2o_dataset|he_dataset|g0w0|li_g0w0|he_exx ...].
 """
 from __future__ import annotations
 
@@ -144,6 +145,13 @@ def h2o_dataset(ref: Path):
     src = ref / "regression_tests/testcases/rpa_aims_mole_H2O_libri/dataset.tar.gz"
     shutil.copyfile(src, HERE / "h2o_dataset.tar.gz")
     print("h2o_dataset.tar.gz written")
+
+
+def he_dataset(ref: Path):
+    import shutil
+    src = ref / "regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz"
+    shutil.copyfile(src, HERE / "he_bcc_dataset.tar.gz")
+    print("he_bcc_dataset.tar.gz written")
 
 
 def g0w0(ref: Path):
@@ -264,7 +272,8 @@ def he_exx(ref: Path):
 
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-    which = sys.argv[2:] or ["h2o", "h2o_dataset", "minimax", "he_bcc", "g0w0", "li_g0w0", "he_exx"]
+    which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "minimax", "he_bcc", "g0w0", "li_g0w0",
+                             "he_exx"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
-         "li_g0w0": li_g0w0, "he_exx": he_exx}[name](ref)
+         "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset}[name](ref)

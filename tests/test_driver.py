@@ -12,8 +12,11 @@ DATASET = ROOT / "tests" / "golden" / "h2o_dataset.tar.gz"
 EC_REF = -0.306258510  # refs/rpa_aims_mole_H2O_libri/librpa/librpa_omp1_np4.out:273
 
 
-def _prepare(tmp_path, extra=""):
-    with tarfile.open(DATASET) as tf:
+HE_DATASET = ROOT / "tests" / "golden" / "he_bcc_dataset.tar.gz"
+
+
+def _prepare(tmp_path, extra="", dataset=DATASET):
+    with tarfile.open(dataset) as tf:
         tf.extractall(tmp_path, filter="data")
     data = next(tmp_path.rglob("band_out")).parent
     (tmp_path / "librpa.in").write_text(f"# driver parameters\ntask = rpa\ninput_dir = {data}\nnfreq = 16\n"
@@ -48,3 +51,26 @@ def test_driver_h2o_regression(tmp_path, lib, extra, tol):
     assert "RPA correlation energy (Hartree)" in r.stdout
     ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))
     assert abs(ec - EC_REF) <= max(tol, 1e-9), (ec, EC_REF)
+
+
+def test_driver_reads_periodic_dataset_without_gpu(tmp_path, lib):
+    """The periodic BCC He dataset (8 k-points, cells in [0, 2)) parses up to the GPU call."""
+    if lib.librpa_gb300_device_count() > 0:
+        pytest.skip("a GPU is visible: the GPU test covers the full run")
+    d = _prepare(tmp_path, dataset=HE_DATASET)
+    r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1
+    assert "CUDA" in r.stderr or "device" in r.stderr, r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_he_bcc_periodic(tmp_path, lib):
+    """task = rpa on real periodic FHI-aims files (BCC He, 2x2x2 k-points) against the oracle."""
+    from conftest import load_he_exx, oracle_input
+    from oracle.rpa_oracle import Options, rpa_correlation_energy
+    ref = rpa_correlation_energy(oracle_input(load_he_exx()), Options(nfreq=16))["ec"].real
+    d = _prepare(tmp_path, "gb300_chi0_precision = fp64\ngb300_ec_path = lu\n", dataset=HE_DATASET)
+    r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))
+    assert abs(ec - ref) <= 1e-9, (ec, ref)
