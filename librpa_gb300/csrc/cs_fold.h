@@ -30,7 +30,9 @@ struct CsFold
 };
 
 // blocks: objects with I, J, R[3], ni, nj, nmu, offset (into blob).  cell_of(Rfolded) -> cell
-// index or -1.  Blocks keep their order; a key met again is summed into its first block's slot.
+// index or -1.  Staged blocks keep the order of their keys' first appearance.  A key held by
+// one block points into blob; blocks sharing a key are summed into `extra`, whose offsets count
+// from blob_size (the caller stages blob ++ extra).
 template <typename Block, typename CellOf>
 CsFold fold_cs_blocks(const std::vector<Block> &blocks, const double *blob, std::size_t blob_size,
                       const int period[3], CellOf cell_of, double threshold)
