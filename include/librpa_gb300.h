@@ -127,6 +127,17 @@ int librpa_gb300_solve_qpe(int n_states, int n_freq, const double *omegas, const
                            const double *vxc, const double *vexx, double *e_qp, double *sigc_qp_re,
                            double *sigc_qp_im);
 
+/* Diagnostic (no counterpart in the reference; host only, no GPU needed): the index and phase
+ * tables the GPU path builds from the handler's data.  With all arrays NULL it only writes
+ * *n_cells and *n_q.  Then: cells[3 n_cells] (the BvK cell vectors, centred range, x outer,
+ * z inner: construct_R_grid, src/core/pbc.cpp:178-190), ibz_rep[n_q] (full k index of each IBZ
+ * point, first-seen order) and ibz_w[n_q] (count / n_k) (pbc.cpp:110-153), g_phase[n_k][n_cells][2]
+ * = (cos, sin) of 2 pi kfrac_k . R (G(R) = sum_k e^{-i...} G(k), src/core/chi0.cpp:379-380) and
+ * q_phase[n_q][n_cells][2] = (cos, sin) of 2 pi q . (R latvec) (FT of chi0, chi0.cpp:582).
+ * Returns 0 on success. */
+int librpa_gb300_phase_tables(LibrpaHandler *h, int *n_cells, int *n_q, int *cells, int *ibz_rep, double *ibz_w,
+                              double *g_phase, double *q_phase);
+
 /* After a call with keep_chi0 = 1: copy chi0(q_ibz, omega) block (I<=J) to the
  * caller as two row-major n_mu x n_nu arrays.  Returns 0 on success. */
 int librpa_gb300_get_chi0_block(LibrpaHandler *h, int ifreq, int iq_ibz, int I, int J,

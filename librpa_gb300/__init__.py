@@ -137,7 +137,7 @@ EXPORTS = [
     "librpa_gb300_get_screening_samples", "librpa_gb300_get_screening_model", "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
-    "librpa_gb300_solve_qpe",
+    "librpa_gb300_solve_qpe", "librpa_gb300_phase_tables",
 ]
 
 _lib = None
@@ -202,6 +202,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_load_chi0_qw": (i, [vp, vp, C.c_longlong, i]),
         "librpa_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, i, vp, C.POINTER(C.c_double)]),
         "librpa_gb300_solve_qpe": (i, [i, i, _dp, _dp, _dp, i, _dp, d, _dp, _dp, _dp, _dp, _dp]),
+        "librpa_gb300_phase_tables": (i, [vp, vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -385,6 +386,26 @@ class Handler:
         if math.isnan(ec):
             raise LibrpaError(self.last_error())
         return ec, re[:n_ibz_kpoints] + 1j * im[:n_ibz_kpoints]
+
+
+def phase_tables(h, n_kpts):
+    """The host index/phase tables of the GPU path for handler h (librpa_gb300_phase_tables)."""
+    lib = load_library()
+    nc, nq = C.c_int(0), C.c_int(0)
+    null = None
+    if lib.librpa_gb300_phase_tables(h.h, C.byref(nc), C.byref(nq), null, null, null, null, null) != 0:
+        raise LibrpaError(h.last_error())
+    nk = n_kpts
+    cells = np.zeros(3 * nc.value, np.int32)
+    rep = np.zeros(nq.value, np.int32)
+    w = np.zeros(nq.value)
+    gp = np.zeros(2 * nk * nc.value)
+    qp = np.zeros(2 * nq.value * nc.value)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    if lib.librpa_gb300_phase_tables(h.h, None, None, ptr(cells), ptr(rep), ptr(w), ptr(gp), ptr(qp)) != 0:
+        raise LibrpaError(h.last_error())
+    return {"cells": cells.reshape(-1, 3), "ibz_rep": rep, "ibz_w": w,
+            "g_phase": gp.reshape(nk, nc.value, 2), "q_phase": qp.reshape(nq.value, nc.value, 2)}
 
 
 def solve_qpe(omegas, sigc_iw, e_mf, e_fermi, vxc, vexx, n_params=-1):

@@ -18,6 +18,7 @@
 #include "common.h"
 #include "dataset.h"
 #include "screen.h"
+#include "host_tables.h"
 #include "minimax.h"
 #include "qpe.h"
 #include "tc_gemm.h"
@@ -842,6 +843,40 @@ int librpa_gb300_minimax_grid(int n, double emin, double emax, double reg, doubl
         cp(cos_f2t, g.cos_f2t);
         cp(sin_t2f, g.sin_t2f);
         if (dual) *dual = g.cosft_duality_error;
+        rc = 0;
+    });
+    return rc;
+}
+
+int librpa_gb300_phase_tables(LibrpaHandler *h, int *n_cells, int *n_q, int *cells, int *ibz_rep, double *ibz_w,
+                              double *g_phase, double *q_phase)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        const gb::PhaseTables t = gb::build_phase_tables(*ds);
+        if (n_cells) *n_cells = t.nc;
+        if (n_q) *n_q = t.nq;
+        if (cells)
+            for (int c = 0; c < t.nc; ++c)
+                for (int d = 0; d < 3; ++d) cells[3 * c + d] = t.cells.R[c][d];
+        for (int q = 0; q < t.nq; ++q)
+        {
+            if (ibz_rep) ibz_rep[q] = t.ibz_rep[q];
+            if (ibz_w) ibz_w[q] = t.ibz_w[q];
+        }
+        if (g_phase)
+            for (size_t i = 0; i < t.gcos.size(); ++i)
+            {
+                g_phase[2 * i] = t.gcos[i];
+                g_phase[2 * i + 1] = t.gsin[i];
+            }
+        if (q_phase)
+            for (size_t i = 0; i < t.qcos.size(); ++i)
+            {
+                q_phase[2 * i] = t.qcos[i];
+                q_phase[2 * i + 1] = t.qsin[i];
+            }
         rc = 0;
     });
     return rc;

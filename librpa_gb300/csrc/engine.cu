@@ -27,6 +27,7 @@
 #include "chi0_fast.h"
 #include "common.h"
 #include "cs_fold.h"
+#include "host_tables.h"
 #include "dataset.h"
 #include "ec_tc.h"
 #include "gk_tc.h"
@@ -38,34 +39,6 @@
 namespace gb {
 
 namespace {
-
-struct Cells
-{
-    std::vector<std::array<int, 3>> R;
-    std::map<std::array<int, 3>, int> index;
-    int period[3];
-    int find(int x, int y, int z) const
-    {
-        std::array<int, 3> k{centred_mod(x, period[0]), centred_mod(y, period[1]), centred_mod(z, period[2])};
-        auto it = index.find(k);
-        return it == index.end() ? -1 : it->second;
-    }
-};
-
-Cells make_cells(const int period[3])
-{
-    Cells c;
-    for (int d = 0; d < 3; ++d) c.period[d] = period[d];
-    // construct_R_grid (pbc.cpp:178-190): x outer, z inner, centred range
-    for (int x = -(period[0]) / 2; x <= (period[0] - 1) / 2; ++x)
-        for (int y = -(period[1]) / 2; y <= (period[1] - 1) / 2; ++y)
-            for (int z = -(period[2]) / 2; z <= (period[2] - 1) / 2; ++z)
-            {
-                c.index[{x, y, z}] = static_cast<int>(c.R.size());
-                c.R.push_back({x, y, z});
-            }
-    return c;
-}
 
 template <typename T>
 DevBuf<T> to_dev(const std::vector<T> &h, cudaStream_t st)
@@ -154,63 +127,17 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     }
     GB_REQUIRE(tot_ao == nao, "sum of per-atom NAOs differs from the mean-field basis size");
     const int N = abf_off[n_at];
-    const Cells cells = make_cells(ds.period);
-    const int nc = static_cast<int>(cells.R.size());
+    const PhaseTables pt = build_phase_tables(ds);
+    const Cells &cells = pt.cells;
+    const int nc = pt.nc;
     GB_REQUIRE(nc == nk, "number of BvK cells must equal the number of k points");
-    std::vector<int> cdiff(static_cast<size_t>(nc) * nc), cneg(nc);
-    for (int a = 0; a < nc; ++a)
-    {
-        for (int b = 0; b < nc; ++b)
-            cdiff[a * nc + b] = cells.find(cells.R[a][0] - cells.R[b][0], cells.R[a][1] - cells.R[b][1],
-                                           cells.R[a][2] - cells.R[b][2]);
-        cneg[a] = cells.find(-cells.R[a][0], -cells.R[a][1], -cells.R[a][2]);
-    }
+    const std::vector<int> &cdiff = pt.cdiff, &cneg = pt.cneg;
     const long long n_sup = static_cast<long long>(nc) * nao;
-
-    // G phases: theta = 2pi kfrac_k . R_c  (kphase = e^{-i theta}, chi0.cpp:379-380)
-    std::vector<double> gcos(static_cast<size_t>(nk) * nc), gsin(static_cast<size_t>(nk) * nc);
-    for (int k = 0; k < nk; ++k)
-        for (int c = 0; c < nc; ++c)
-        {
-            const double th = 2.0 * M_PI *
-                              (ds.kfrac[3 * k] * cells.R[c][0] + ds.kfrac[3 * k + 1] * cells.R[c][1] +
-                               ds.kfrac[3 * k + 2] * cells.R[c][2]);
-            gcos[k * nc + c] = std::cos(th);
-            gsin[k * nc + c] = std::sin(th);
-        }
-    // IBZ list (pbc.cpp:110-153): representatives in order of first appearance, weight count/nk
-    std::vector<int> ibz_rep;
-    std::vector<double> ibz_w;
-    {
-        std::map<int, int> seen;
-        for (int k = 0; k < nk; ++k)
-        {
-            const int r = ds.ibz_map[k];
-            auto it = seen.find(r);
-            if (it == seen.end())
-            {
-                seen[r] = static_cast<int>(ibz_rep.size());
-                ibz_rep.push_back(r);
-                ibz_w.push_back(1.0 / nk);
-            }
-            else
-                ibz_w[it->second] += 1.0 / nk;
-        }
-    }
-    const int nq = static_cast<int>(ibz_rep.size());
-    // FT phases: 2pi q.(R latvec) with q = k_cart / 2pi  (chi0.cpp:582)
-    std::vector<double> qcos(static_cast<size_t>(nq) * nc), qsin(static_cast<size_t>(nq) * nc);
-    for (int q = 0; q < nq; ++q)
-        for (int c = 0; c < nc; ++c)
-        {
-            double Rc[3] = {0, 0, 0};
-            for (int d = 0; d < 3; ++d)
-                for (int a = 0; a < 3; ++a) Rc[d] += cells.R[c][a] * ds.latvec[a * 3 + d];
-            const double *qv = &ds.klist[3 * ibz_rep[q]];
-            const double arg = (qv[0] * Rc[0] + qv[1] * Rc[1] + qv[2] * Rc[2]) * 2.0 * M_PI;
-            qcos[q * nc + c] = std::cos(arg);
-            qsin[q * nc + c] = std::sin(arg);
-        }
+    const std::vector<double> &gcos = pt.gcos, &gsin = pt.gsin;   // G phases (chi0.cpp:379-380)
+    const std::vector<int> &ibz_rep = pt.ibz_rep;                 // IBZ list (pbc.cpp:110-153)
+    const std::vector<double> &ibz_w = pt.ibz_w;
+    const int nq = pt.nq;
+    const std::vector<double> &qcos = pt.qcos, &qsin = pt.qsin;   // FT phases (chi0.cpp:582)
 
     // upper atom pairs
     std::vector<int> pI, pJ, pair_of(static_cast<size_t>(n_at) * n_at, -1);
