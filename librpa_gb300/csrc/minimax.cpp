@@ -204,11 +204,20 @@ std::vector<double> fit_weights(int n, const std::vector<double> &tau, const std
         }
         std::vector<double> Ain = A;
         jacobi_svd(A, num_x, n, S, V);
-        // w = sum_j V[:, j] * S_j/(reg^2+S_j^2) * (u_j . psi),  u_j = A_j / S_j
+        // w = sum_j V[:, j] * S_j/(reg^2+S_j^2) * (u_j . psi),  u_j = A_j / S_j, over the
+        // numerical rank: singular values below num_x * eps * S_max are dropped, the rank rule
+        // of a least-squares solver.  GreenX keeps them all, which only matters for fits that are
+        // singular to double precision (many points over a small energy range, e.g. 32 points
+        // at E_max/E_min = 80, where the exp(-x tau) columns are graded down to 1e-150): there its
+        // weights are set by LAPACK's rounding, while 1/S of the exact tiny singular values the
+        // Jacobi SVD resolves gives weights of 1e30 and beyond.
+        double smax = 0.0;
+        for (int j = 0; j < n; ++j) smax = std::fmax(smax, S[j]);
+        const double s_floor = static_cast<double>(num_x) * 2.220446049250313e-16 * smax;
         std::vector<double> w(n, 0.0);
         for (int j = 0; j < n; ++j)
         {
-            if (S[j] == 0.0) continue;
+            if (!(S[j] > s_floor)) continue;
             double ut = 0.0;
             const double *a = &A[static_cast<size_t>(j) * num_x];
             for (int i = 0; i < num_x; ++i) ut += a[i] * psi[i];

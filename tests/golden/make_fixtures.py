@@ -11,7 +11,8 @@ Produces (all committed, so the tests need no reference tree at run time):
   minimax_ref.json   grids printed by the reference run (16 points, H2O window):
                      omega/tau nodes and weights (16 digits), cosine/sine t->f and cosine
                      f->t matrices (6 significant digits); the 6-point omega nodes/weights
-                     asserted in src/test/test_timefreq.cpp (check_minimax_ng6_HF_123)
+                     asserted in src/test/test_timefreq.cpp (check_minimax_ng6_HF_123); the
+                     32-point grids of the H2 G0W0 run (nodes, weights, t->f matrices)
   he_bcc_gamma.json  the BCC He known-answer test of src/test/test_meanfield.cpp
                      (eigenpairs, Fermi level, expected density matrix and G(tau -> 0-))
   h2o_dataset.tar.gz the H2O regression dataset itself (the reference's FHI-aims export, copied
@@ -120,9 +121,44 @@ def minimax(ref: Path):
         "h2o16": {"omega": om, "omega_w": omw, "tau": tau, "tau_w": tauw,
                   "cos_t2f": cos_t2f, "sin_t2f": sin_t2f, "cos_f2t": cos_f2t},
         "ng6_HF_123": {"emin": emin, "emax": emax, "omega": fn, "omega_w": fw, "tol": 1e-5},
+        "h2_32": _minimax_h2_32(ref),
     }
     (HERE / "minimax_ref.json").write_text(json.dumps(out, indent=1))
     print("minimax_ref.json written")
+
+
+def _minimax_h2_32(ref: Path):
+    """32-point grids printed by the H2 G0W0 run (refs/g0w0_aims_mole_H2_libri/librpa/librpa.out)
+    with the window its band_out gives (gap, band width).  The cosine f->t matrix is left out: at
+    32 points its least-squares fit is singular to double precision (condition number ~7e16), so
+    the printed weights are not reproducible across LAPACK builds."""
+    from oracle.rpa_oracle import e_min_max
+    log = (ref / "regression_tests/refs/g0w0_aims_mole_H2_libri/librpa/librpa.out").read_text().splitlines()
+    n = 32
+
+    def table(start_pat):
+        i = next(k for k, l in enumerate(log) if start_pat in l)
+        rows = [_floats(log[i + 1 + r]) for r in range(n)]
+        return [r[1] for r in rows], [r[2] for r in rows], i + 1 + n
+
+    om, omw, end = table("Frequency node & weight")
+    tau, tauw, end = table("Time node & weight")
+
+    def matrix(after, title):
+        i = next(k for k in range(after, len(log)) if title in log[k])
+        i += 2
+        return [_floats(log[i + r]) for r in range(n)], i + n
+
+    cos_t2f, e1 = matrix(end, "Cosine transform matrix")
+    sin_t2f, _ = matrix(e1, "Sine transform matrix")
+    tgz = ref / "regression_tests/testcases/g0w0_aims_mole_H2_libri/dataset.tar.gz"
+    with tempfile.TemporaryDirectory() as td:
+        with tarfile.open(tgz) as tf:
+            tf.extractall(td, filter="data")
+        d = next(Path(td).rglob("band_out")).parent
+        gap, width = e_min_max(read_dataset(str(d)))
+    return {"emin": float(gap), "emax": float(width), "omega": om, "omega_w": omw, "tau": tau, "tau_w": tauw,
+            "cos_t2f": cos_t2f, "sin_t2f": sin_t2f}
 
 
 def he_bcc(ref: Path):

@@ -55,6 +55,38 @@ def test_cpp_minimax_reference_log(lib):
     assert np.abs(g["omega"] - ref["omega"]).max() < ref["tol"]
 
 
+def _fit_errors(g, emin, emax):
+    """GreenX's fit errors (calculate_max_error) of the three transforms of a grid: the largest
+    deviation of sum_j w_j cos/sin(...) e^{-x tau_j} (or 2x/(x^2+w_j^2)) from the target function
+    over the log-spaced x nodes of get_transformation_weights."""
+    n = len(g["tau"])
+    tau, om = np.asarray(g["tau"]), np.asarray(g["omega"])
+    nx = max((int(np.log10(emax / emin)) + 1) * 200, n)
+    x = emin * (emax / emin) ** (np.arange(nx) / (nx - 1.0))
+    e = np.exp(-np.outer(x, tau))
+    cos_e = max(np.abs(2 * x / (x * x + w * w) - e @ g["cos_t2f"][i]).max() for i, w in enumerate(om))
+    sin_e = max(np.abs(2 * w / (x * x + w * w) - e @ g["sin_t2f"][i]).max() for i, w in enumerate(om))
+    lor = 2 * x[:, None] / (x[:, None] ** 2 + om[None, :] ** 2)
+    f2t_e = max(np.abs(np.exp(-x * t) - lor @ g["cos_f2t"][i]).max() for i, t in enumerate(tau))
+    return np.array([cos_e, sin_e, f2t_e])
+
+
+def test_cpp_minimax_32_points_reference_log(lib):
+    """32 points over the H2 run's window (E_max/E_min = 79): the nodes and weights of the
+    reference log.  The transforms' least-squares fits are singular to double precision there;
+    GreenX (and the oracle, through LAPACK) keep every singular value and reach weights of 1e6 to
+    1e8 that follow LAPACK's rounding, the library drops those below its numerical rank.  Its
+    fits are as accurate as the oracle's, with bounded weights."""
+    ref = minimax_ref()["h2_32"]
+    g = L.minimax_grid(32, ref["emin"], ref["emax"])
+    for k in ("omega", "omega_w", "tau", "tau_w"):
+        np.testing.assert_allclose(g[k], ref[k], rtol=1e-13, atol=1e-16)
+    o = oracle_grid(32, ref["emin"], ref["emax"])
+    el, eo = _fit_errors(g, ref["emin"], ref["emax"]), _fit_errors(o, ref["emin"], ref["emax"])
+    assert np.all(el <= 2.0 * eo), (el, eo)
+    assert max(np.abs(g[k]).max() for k in ("cos_t2f", "sin_t2f", "cos_f2t")) < 1e4
+    assert max(np.abs(o[k]).max() for k in ("cos_t2f", "sin_t2f", "cos_f2t")) > 1e6
+
 def test_frequency_grid_api_uses_mean_field_window(lib):
     s = load_h2o()
     with L.Handler() as h:

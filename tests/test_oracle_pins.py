@@ -33,6 +33,18 @@ def test_minimax_h2o16_matches_reference_log():
         np.testing.assert_allclose(g[k], np.array(ref[k]), rtol=6e-6, atol=1e-10)
 
 
+def test_minimax_h2_32_matches_reference_log():
+    """32-point grids of the H2 G0W0 run: nodes/weights to the printed 16 digits, cosine and sine
+    t->f matrices to their 6 digits (the f->t fit is singular at 32 points and not compared)."""
+    ref = minimax_ref()["h2_32"]
+    g = minimax_grid(32, ref["emin"], ref["emax"])
+    for k in ("omega", "omega_w", "tau", "tau_w"):
+        np.testing.assert_allclose(g[k], ref[k], rtol=1e-13, atol=1e-16)
+    for k in ("cos_t2f", "sin_t2f"):
+        m = np.array(ref[k])
+        np.testing.assert_allclose(g[k], m, rtol=0, atol=6e-6 * np.abs(m).max())
+
+
 def test_minimax_ng6_reference_unit_test():
     """check_minimax_ng6_HF_123 of the reference unit tests (omega nodes/weights to 1e-5)."""
     ref = minimax_ref()["ng6_HF_123"]
