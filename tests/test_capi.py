@@ -140,3 +140,23 @@ def test_small_cell_batch_workload():
         assert 2 <= s.n_atoms <= 8 and s.n_kpts == 1 and s.nfreq == 24
         assert set(zip(s.nao, s.nabf)) <= species
         assert s.n_atoms == t.n_atoms and np.array_equal(s.ekb, t.ekb)
+
+
+def test_rank_cut_grid_gives_the_oracle_ec_on_an_ill_conditioned_window(lib):
+    """BCC He: E_max/E_min = 1.6 over 16 points makes every fit singular (singular values down to
+    1e-22 of the largest).  The library's rank-cut transforms (weights below 3e3) and the oracle's
+    LAPACK ones (weights up to 1e8) give one RPA E_c to 1e-10 when fed to the same oracle."""
+    import oracle.rpa_oracle as R
+    from conftest import load_he_exx, oracle_input
+    inp = oracle_input(load_he_exx())
+    emin, emax = R.e_min_max(inp)
+    g = L.minimax_grid(16, emin, emax)
+    assert max(np.abs(g[k]).max() for k in ("cos_t2f", "sin_t2f", "cos_f2t")) < 1e4
+    ref = R.rpa_correlation_energy(inp, R.Options(nfreq=16))["ec"].real
+    saved = R.grids_for
+    try:
+        R.grids_for = lambda inp_, opts_: dict(g)
+        ec = R.rpa_correlation_energy(inp, R.Options(nfreq=16))["ec"].real
+    finally:
+        R.grids_for = saved
+    assert abs(ec - ref) <= 1e-10 * abs(ref), (ec, ref)
