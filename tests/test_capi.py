@@ -96,6 +96,21 @@ def test_frequency_grid_api_uses_mean_field_window(lib):
     np.testing.assert_allclose(w, minimax_ref()["h2o16"]["omega_w"], rtol=2e-15)
 
 
+def test_frequency_grid_window_on_periodic_input(lib):
+    """The mean-field window (band gap over all k, band width) on the periodic BCC He input with
+    its 8 k-points, against the oracle's e_min_max (MeanField::get_E_min_max, get_band_gap)."""
+    from conftest import load_he_exx, oracle_input
+    from oracle.rpa_oracle import e_min_max
+    s = load_he_exx()
+    emin, emax = e_min_max(oracle_input(s))
+    with L.Handler() as h:
+        L.load_system(h, s)
+        om, w = h.get_imaginary_frequency_grids(L.Options(nfreq=16, tfgrids_type=L.Minimax))
+    g = oracle_grid(16, emin, emax)
+    np.testing.assert_allclose(om, g["omega"], rtol=1e-14)
+    np.testing.assert_allclose(w, g["omega_w"], rtol=1e-14)
+
+
 def test_errors_are_recorded_not_thrown(lib):
     with L.Handler() as h:
         # wrong grid type -> error message, NaN, handler stays usable
