@@ -220,6 +220,8 @@ void merge_vq_2d(Dataset *ds)
     std::map<int, std::vector<cplx>> full;
     for (const auto &b : ds->vq_2d)
     {
+        GB_REQUIRE(b.mu_begin >= 0 && b.mu_end <= N && b.nu_begin >= 0 && b.nu_end <= N,
+                   "2D Coulomb block outside the auxiliary basis");
         auto &M = full[b.ik];
         if (M.empty()) M.assign(static_cast<size_t>(N) * N, cplx(0, 0));
         const int nr = b.mu_end - b.mu_begin, ncl = b.nu_end - b.nu_begin;

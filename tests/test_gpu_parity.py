@@ -1,4 +1,6 @@
 """GPU path vs the oracle through the C ABI (needs a GB300)."""
+import copy
+
 import numpy as np
 import pytest
 
@@ -89,6 +91,36 @@ def test_he_bcc_fhi_aims_periodic_vs_oracle():
     np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
     _, ec2, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
     assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
+
+
+def test_coulomb_given_as_2d_blocks():
+    """V(q) handed over as 2D blocks of the full matrix (librpa_set_aux_bare_coulomb_k_2d_block,
+    the BLACS-distributed form of the FHI-aims interface) gives the E_c of the atom-pair form."""
+    s = sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=(3, 1, 1), nocc=2, seed=5)
+    _, ref, pref = run_gpu(s, L.CHI0_FP64)
+    nb = s.nabf
+    off = np.concatenate([[0], np.cumsum(nb)]).astype(int)
+    N = int(off[-1])
+    h = L.Handler()
+    t = copy.copy(s)
+    t.Vq = {}
+    L.load_system(h, t)
+    for ik in sorted({k[0] for k in s.Vq}):
+        M = np.zeros((N, N), complex)
+        for (kk, I, J), v in s.Vq.items():
+            if kk != ik:
+                continue
+            M[off[I]:off[I + 1], off[J]:off[J + 1]] = v
+            M[off[J]:off[J + 1], off[I]:off[I + 1]] = v.conj().T
+        # two row blocks, as two BLACS processes would hand them over
+        for r0, r1 in ((0, N // 2), (N // 2, N)):
+            blk = np.ascontiguousarray(M[r0:r1, :])
+            h.set_aux_bare_coulomb_k_2d_block(ik, r0, r1, 0, N, np.ascontiguousarray(blk.real),
+                                              np.ascontiguousarray(blk.imag))
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    ec, perq = h.get_rpa_correlation_energy(_opts(s), L.n_ibz(s))
+    assert abs(ec - ref) <= 1e-12 * abs(ref)
+    np.testing.assert_allclose(perq, pref, rtol=1e-11, atol=1e-15)
 
 
 def test_fcc2_k222_fp64_vs_oracle():
