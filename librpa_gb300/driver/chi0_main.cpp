@@ -103,6 +103,17 @@ bool exists(const std::string &fn)
     return static_cast<bool>(f);
 }
 
+// The reference's format check (check_Cs_file_binary / check_coulomb_file_binary,
+// driver/read_data.cpp:414-453): a file whose first token parses as an integer is text (the
+// ASCII files ABACUS writes), otherwise unformatted binary (FHI-aims).
+bool is_text_file(const std::string &fn)
+{
+    std::ifstream f(fn);
+    int v = 0;
+    f >> v;
+    return static_cast<bool>(f);
+}
+
 template <typename T>
 T get(const std::vector<char> &raw, size_t &off)
 {
@@ -293,10 +304,38 @@ int main()
                     librpa_set_wfc(h, s, k, m.nb, m.nao, R.data(), im[static_cast<size_t>(s) * m.nk + k].data());
                 }
         }
-        // Cs_data* binary (read_data.cpp:690-747): natom ncell nblocks, then per block
-        // I J R1 R2 R3 n_i n_j n_mu and n_i*n_j*n_mu doubles; kept if max |C| >= cs_threshold
+        // Cs_data*: binary (read_data.cpp:690-747): natom ncell nblocks, then per block
+        // I J R1 R2 R3 n_i n_j n_mu and n_i*n_j*n_mu doubles; text (read_data.cpp:618-688):
+        // natom ncell, then blocks of the same 8 integers and values to the end of the file.
+        // A block is kept if max |C| >= cs_threshold.
+        auto set_cs = [&](const int *v, std::vector<double> &c) {
+            double mx = 0.0;
+            for (double x : c) mx = std::max(mx, std::fabs(x));
+            if (mx < cs_threshold) return;
+            const int R[3] = {v[2], v[3], v[4]};
+            librpa_set_lri_coeff(h, static_cast<LibrpaParallelRouting>(opts.parallel_routing), v[0] - 1, v[1] - 1,
+                                 v[5], v[6], v[7], R, c.data());
+        };
         for (const auto &fn : files_with_prefix(dir, "Cs_data"))
         {
+            if (is_text_file(fn))
+            {
+                const auto t = tokens(fn);
+                size_t q = 2;  // natom, ncell
+                while (q + 8 <= t.size())
+                {
+                    int v[8];
+                    for (int i = 0; i < 8; ++i) v[i] = std::stoi(t[q + i]);
+                    q += 8;
+                    const size_t cnt = static_cast<size_t>(v[5]) * v[6] * v[7];
+                    if (q + cnt > t.size()) die("truncated RI file " + fn);
+                    std::vector<double> c(cnt);
+                    for (size_t i = 0; i < cnt; ++i) c[i] = std::stod(t[q + i]);
+                    q += cnt;
+                    set_cs(v, c);
+                }
+                continue;
+            }
             const auto raw = slurp(fn);
             size_t off = 0;
             get<int>(raw, off);
@@ -311,12 +350,7 @@ int main()
                 std::vector<double> c(cnt);
                 std::memcpy(c.data(), raw.data() + off, 8 * cnt);
                 off += 8 * cnt;
-                double mx = 0.0;
-                for (double x : c) mx = std::max(mx, std::fabs(x));
-                if (mx < cs_threshold) continue;
-                const int R[3] = {v[2], v[3], v[4]};
-                librpa_set_lri_coeff(h, static_cast<LibrpaParallelRouting>(opts.parallel_routing), v[0] - 1, v[1] - 1,
-                                     v[5], v[6], v[7], R, c.data());
+                set_cs(v, c);
             }
         }
         // coulomb_mat* binary (read_data.cpp:1472-1577): n_irk n_local, then per block
@@ -328,6 +362,31 @@ int main()
             int nbb = 0;
             for (const auto &fn : files_with_prefix(dir, "coulomb_mat"))
             {
+                if (is_text_file(fn))
+                {
+                    // text (read_data.cpp:1580-1650): n_irk, then blocks of nbasbas brow erow bcol
+                    // ecol, iq q_weight and the (re, im) pairs of the rows
+                    const auto t = tokens(fn);
+                    size_t q = 1;
+                    while (q + 7 <= t.size())
+                    {
+                        nbb = std::stoi(t[q]);
+                        const int br = std::stoi(t[q + 1]) - 1, er = std::stoi(t[q + 2]) - 1;
+                        const int bc = std::stoi(t[q + 3]) - 1, ec = std::stoi(t[q + 4]) - 1;
+                        const int iq = std::stoi(t[q + 5]) - 1;
+                        q += 7;
+                        if (er < br || ec < bc || iq < 0 || br < 0 || bc < 0 || er >= nbb || ec >= nbb)
+                            die("bad Coulomb block header in " + fn);
+                        const size_t cnt = static_cast<size_t>(er - br + 1) * (ec - bc + 1);
+                        if (q + 2 * cnt > t.size()) die("truncated Coulomb file " + fn);
+                        auto &M = full[iq];
+                        M.resize(static_cast<size_t>(nbb) * nbb);
+                        for (int r = br; r <= er; ++r)
+                            for (int c = bc; c <= ec; ++c, q += 2)
+                                M[static_cast<size_t>(r) * nbb + c] = cplx(std::stod(t[q]), std::stod(t[q + 1]));
+                    }
+                    continue;
+                }
                 const auto raw = slurp(fn);
                 size_t off = 0;
                 get<int>(raw, off);

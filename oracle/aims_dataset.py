@@ -6,11 +6,13 @@ Follows the driver readers of the reference (driver/read_data.cpp):
   bz_sampling_out   read_bz_sampling           :1869-1916
   basis_out         read_basis                 :1976-2011
   KS_eigenvector_*  handle_KS_file             :184-284  (order: ao, spinor, band, spin)
-  Cs_data_* (bin)   handle_Cs_file_binary      :690-747  (keep if max|C| >= cs_threshold, default 1e-6)
-  coulomb_mat_*     handle_Vq_row_file (bin)   :1472-1577 (upper atom blocks)
+  Cs_data_*         handle_Cs_file_binary      :690-747  (keep if max|C| >= cs_threshold, default 1e-6)
+                    handle_Cs_file (text)      :618-688
+  coulomb_mat_*     handle_Vq_row_file         :1472-1650 (binary and text; upper atom blocks)
   coulomb_cut_*     the same format (truncated Coulomb of G0W0, driver/task/g0w0.cpp:33-45)
   vxc_out           read_vxc                   :142-182
-Only the unformatted-binary Cs/V variants are handled (the regression datasets use them).
+Binary (FHI-aims) or text (ABACUS) is told apart as the reference does (check_Cs_file_binary,
+check_coulomb_file_binary, :414-453): a file whose first token parses as an integer is text.
 """
 from __future__ import annotations
 
@@ -26,6 +28,18 @@ from .rpa_oracle import RPAInput
 def _tokens(path):
     with open(path) as f:
         return f.read().split()
+
+
+def is_text_file(path) -> bool:
+    """The first whitespace-separated token parses as an integer (read_data.cpp:414-453)."""
+    with open(path, "rb") as f:
+        head = f.read(64)
+    try:
+        tok = head.split()[0].decode("ascii")
+        int(tok)
+        return True
+    except (IndexError, UnicodeDecodeError, ValueError):
+        return False
 
 
 def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
@@ -107,6 +121,18 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
 
     Cs = {}
     for fn in sorted(glob.glob(d + "Cs_data*")):
+        if is_text_file(fn):
+            t = _tokens(fn)
+            p = 2  # natom, ncell
+            while p + 8 <= len(t):
+                I, J, r1, r2, r3, ni, nj, nmu = (int(x) for x in t[p:p + 8])
+                p += 8
+                cnt = ni * nj * nmu
+                m = np.array([float(x) for x in t[p:p + cnt]]).reshape(ni * nj, nmu)
+                p += cnt
+                if np.abs(m).max() >= cs_threshold:
+                    Cs[(I - 1, J - 1, (r1, r2, r3))] = m
+            continue
         raw = open(fn, "rb").read()
         natom, ncell, nblk = struct.unpack_from("<3i", raw, 0)
         off = 12
@@ -133,6 +159,24 @@ def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
     aoff = np.concatenate([[0], np.cumsum(nabf_at)]).astype(int)
     Vq = {}
     for fn in sorted(glob.glob(d + prefix + "*")):
+        if is_text_file(fn):
+            t = _tokens(fn)
+            p = 1  # n_irk
+            full = {}
+            while p + 7 <= len(t):
+                nbb, br, er, bc, ec, iq = (int(x) for x in t[p:p + 6])
+                p += 7  # the q weight follows iq
+                br, er, bc, ec, iq = br - 1, er - 1, bc - 1, ec - 1, iq - 1
+                nr, nc = er - br + 1, ec - bc + 1
+                v = np.array([float(x) for x in t[p:p + 2 * nr * nc]]).reshape(nr, nc, 2)
+                p += 2 * nr * nc
+                M = full.setdefault(iq, np.zeros((nbb, nbb), complex))
+                M[br:er + 1, bc:ec + 1] = v[..., 0] + 1j * v[..., 1]
+            for iq, M in full.items():
+                for I in range(nat):
+                    for J in range(I, nat):
+                        Vq[(iq, I, J)] = M[aoff[I]:aoff[I + 1], aoff[J]:aoff[J + 1]].copy()
+            continue
         raw = open(fn, "rb").read()
         _nirk, nloc = struct.unpack_from("<2i", raw, 0)
         off = 8
