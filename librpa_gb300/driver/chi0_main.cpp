@@ -247,7 +247,56 @@ int main()
         }
         librpa_set_kgrids_kvec(h, m.period[0], m.period[1], m.period[2], m.kvecs.data());
         librpa_set_ibz_mapping(h, static_cast<int>(m.ibz.size()), m.ibz.data());
-        // basis_out (read_data.cpp:1976-2011): ntypes, 3 header numbers, then (type, n_wfc, n_aux)
+        // basis_out (read_data.cpp:1976-2011): ntypes, 3 header numbers, then (type, n_wfc, n_aux);
+        // without it (ABACUS exports) the sizes come from the RI blocks, as read_basis_from_Cs
+        // does (read_data.cpp:2083-2152): n_i and n_mu of the first atom, n_j of the second
+        if (!exists(dir + "basis_out"))
+        {
+            std::map<int, int> aw, aa;
+            for (const auto &fn : files_with_prefix(dir, "Cs_data"))
+            {
+                auto note = [&](const int *v) {
+                    aw[v[0] - 1] = v[5];
+                    aw[v[1] - 1] = v[6];
+                    aa[v[0] - 1] = v[7];
+                };
+                if (is_text_file(fn))
+                {
+                    const auto t = tokens(fn);
+                    size_t q = 2;
+                    while (q + 8 <= t.size())
+                    {
+                        int v[8];
+                        for (int i = 0; i < 8; ++i) v[i] = std::stoi(t[q + i]);
+                        note(v);
+                        q += 8 + static_cast<size_t>(v[5]) * v[6] * v[7];
+                    }
+                    continue;
+                }
+                const auto raw = slurp(fn);
+                size_t off = 8;
+                const int nblk = get<int>(raw, off);
+                for (int b = 0; b < nblk; ++b)
+                {
+                    int v[8];
+                    for (auto &x : v) x = get<int>(raw, off);
+                    note(v);
+                    off += 8 * static_cast<size_t>(v[5]) * v[6] * v[7];
+                }
+            }
+            std::vector<size_t> nw(m.nat), na(m.nat);
+            for (int a = 0; a < m.nat; ++a)
+            {
+                if (!aw.count(a) || !aa.count(a)) die("no RI block gives the basis sizes of atom " + std::to_string(a + 1));
+                nw[a] = static_cast<size_t>(aw[a]);
+                na[a] = static_cast<size_t>(aa[a]);
+                m.nao_at.push_back(aw[a]);
+                m.nabf_at.push_back(aa[a]);
+            }
+            librpa_set_ao_basis_wfc(h, m.nat, nw.data());
+            librpa_set_ao_basis_aux(h, m.nat, na.data());
+        }
+        else
         {
             const auto t = tokens(dir + "basis_out");
             const int ntypes = std::stoi(t.at(0));
@@ -409,6 +458,9 @@ int main()
                         }
                 }
             }
+            if (!full.empty() && nbb != off_at[m.nat])
+                die("Coulomb matrices are " + std::to_string(nbb) + " x " + std::to_string(nbb) + " but the bases give " +
+                    std::to_string(off_at[m.nat]) + " auxiliary functions (shrunk ABF sets are not supported)");
             for (const auto &[iq, M] : full)
                 for (int I = 0; I < m.nat; ++I)
                     for (int J = I; J < m.nat; ++J)

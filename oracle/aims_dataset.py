@@ -42,6 +42,39 @@ def is_text_file(path) -> bool:
         return False
 
 
+def _cs_headers(fn):
+    """(I, J, R1, R2, R3, n_i, n_j, n_mu) of every block of one Cs_data file, 1-based atoms."""
+    out = []
+    if is_text_file(fn):
+        t = _tokens(fn)
+        p = 2
+        while p + 8 <= len(t):
+            v = [int(x) for x in t[p:p + 8]]
+            out.append(v)
+            p += 8 + v[5] * v[6] * v[7]
+        return out
+    raw = open(fn, "rb").read()
+    _natom, _ncell, nblk = struct.unpack_from("<3i", raw, 0)
+    off = 12
+    for _ in range(nblk):
+        v = list(struct.unpack_from("<8i", raw, off))
+        out.append(v)
+        off += 32 + 8 * v[5] * v[6] * v[7]
+    return out
+
+
+def _basis_from_cs(d: str, nat: int):
+    """read_basis_from_Cs (read_data.cpp:2083-2152): per atom, n_i and n_mu of blocks where it is
+    the first atom and n_j where it is the second."""
+    aw, aa = {}, {}
+    for fn in sorted(glob.glob(d + "Cs_data*")):
+        for I, J, _r1, _r2, _r3, ni, nj, nmu in _cs_headers(fn):
+            aw[I - 1] = ni
+            aw[J - 1] = nj
+            aa[I - 1] = nmu
+    return [aw[a] for a in range(nat)], [aa[a] for a in range(nat)]
+
+
 def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
     d = d.rstrip("/") + "/"
     t = _tokens(d + "band_out")
@@ -92,17 +125,20 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
         p += 3 * nkf
         ibz = np.array([int(x) - 1 for x in t[p:p + nkf]])
 
-    t = _tokens(d + "basis_out")
-    ntypes = int(t[0])
-    p = 4
-    mw, ma = {}, {}
-    for _ in range(ntypes):
-        ty = int(t[p]) - 1
-        mw[ty] = int(t[p + 1])
-        ma[ty] = int(t[p + 2])
-        p += 3
-    nao_at = [mw[types[a]] for a in range(nat)]
-    nabf_at = [ma[types[a]] for a in range(nat)]
+    if os.path.exists(d + "basis_out"):
+        t = _tokens(d + "basis_out")
+        ntypes = int(t[0])
+        p = 4
+        mw, ma = {}, {}
+        for _ in range(ntypes):
+            ty = int(t[p]) - 1
+            mw[ty] = int(t[p + 1])
+            ma[ty] = int(t[p + 2])
+            p += 3
+        nao_at = [mw[types[a]] for a in range(nat)]
+        nabf_at = [ma[types[a]] for a in range(nat)]
+    else:
+        nao_at, nabf_at = _basis_from_cs(d, nat)
 
     wfc = np.zeros((ns, nk, nb, nao), complex)
     for fn in sorted(glob.glob(d + "KS_eigenvector*")):
@@ -158,6 +194,11 @@ def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
     nat = len(nabf_at)
     aoff = np.concatenate([[0], np.cumsum(nabf_at)]).astype(int)
     Vq = {}
+
+    def check(nbb):
+        if nbb != aoff[-1]:
+            raise ValueError(f"Coulomb matrices are {nbb} x {nbb} but the bases give {aoff[-1]} auxiliary "
+                             "functions (shrunk ABF sets are not supported)")
     for fn in sorted(glob.glob(d + prefix + "*")):
         if is_text_file(fn):
             t = _tokens(fn)
@@ -165,6 +206,7 @@ def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
             full = {}
             while p + 7 <= len(t):
                 nbb, br, er, bc, ec, iq = (int(x) for x in t[p:p + 6])
+                check(nbb)
                 p += 7  # the q weight follows iq
                 br, er, bc, ec, iq = br - 1, er - 1, bc - 1, ec - 1, iq - 1
                 nr, nc = er - br + 1, ec - bc + 1
@@ -183,6 +225,7 @@ def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
         full = {}
         for _ in range(nloc):
             nbb, br, er, bc, ec, iq = struct.unpack_from("<6i", raw, off)
+            check(nbb)
             off += 24
             off += 8  # q weight
             br, er, bc, ec, iq = br - 1, er - 1, bc - 1, ec - 1, iq - 1

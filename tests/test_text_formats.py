@@ -1,7 +1,8 @@
 """Text (ABACUS-style) RI coefficient and Coulomb files, in the reference's text layouts
 (driver/read_data.cpp:618-688 and :1580-1650), read by the oracle's reader and the task = rpa
-driver: a text copy of the periodic BCC He dataset gives the binary original's inputs (no GPU)
-and its E_c (GPU)."""
+driver: a text copy of the periodic BCC He dataset, without basis_out (the sizes then come from
+the RI blocks, as read_basis_from_Cs does), gives the binary original's inputs (no GPU) and its
+E_c (GPU).  A Coulomb matrix whose size differs from the auxiliary basis is refused."""
 import re
 import struct
 import subprocess
@@ -58,6 +59,7 @@ def he_dirs(tmp_path):
             tf.extractall(tmp_path / name, filter="data")
         out.append(next((tmp_path / name).rglob("band_out")).parent)
     _to_text(out[1])
+    (out[1] / "basis_out").unlink()  # as in ABACUS exports: sizes come from the RI blocks
     return out
 
 
@@ -103,3 +105,9 @@ def test_driver_text_and_binary_give_one_ec(he_dirs, lib):
         assert r.returncode == 0, r.stderr
         ec.append(float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1)))
     assert abs(ec[0] - ec[1]) <= 1e-12, ec
+
+
+def test_coulomb_size_mismatch_is_refused(he_dirs):
+    b, _t = he_dirs
+    with pytest.raises(ValueError, match="auxiliary"):
+        read_coulomb(str(b), "coulomb_mat", [13, 12])
