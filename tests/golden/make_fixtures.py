@@ -33,6 +33,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      (refs/g0w0_aims_Li_atom_libri/librpa/librpa.out)
 
   he_bcc_dataset.tar.gz  the BCC He dataset itself (copied unchanged), for the driver's periodic test
+  li_dataset.tar.gz  the spin-polarised Li atom dataset itself (copied unchanged), for the driver
   he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
                      regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
                      its inputs (bare Coulomb V(q) included, for RPA runs on real periodic
@@ -41,7 +42,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|he_dataset|g0w0|li_g0w0|he_exx ...].
+h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx ...].
 """
 from __future__ import annotations
 
@@ -183,6 +184,13 @@ def h2o_dataset(ref: Path):
     print("h2o_dataset.tar.gz written")
 
 
+def li_dataset(ref: Path):
+    import shutil
+    src = ref / "regression_tests/testcases/g0w0_aims_Li_atom_libri/dataset.tar.gz"
+    shutil.copyfile(src, HERE / "li_dataset.tar.gz")
+    print("li_dataset.tar.gz written")
+
+
 def he_dataset(ref: Path):
     import shutil
     src = ref / "regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz"
@@ -308,8 +316,8 @@ def he_exx(ref: Path):
 
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
-    which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "minimax", "he_bcc", "g0w0", "li_g0w0",
-                             "he_exx"]
+    which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "li_dataset", "minimax", "he_bcc", "g0w0",
+                             "li_g0w0", "he_exx"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
-         "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset}[name](ref)
+         "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset, "li_dataset": li_dataset}[name](ref)

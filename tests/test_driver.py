@@ -13,6 +13,7 @@ EC_REF = -0.306258510  # refs/rpa_aims_mole_H2O_libri/librpa/librpa_omp1_np4.out
 
 
 HE_DATASET = ROOT / "tests" / "golden" / "he_bcc_dataset.tar.gz"
+LI_DATASET = ROOT / "tests" / "golden" / "li_dataset.tar.gz"
 
 
 def _prepare(tmp_path, extra="", dataset=DATASET):
@@ -70,6 +71,29 @@ def test_driver_he_bcc_periodic(tmp_path, lib):
     from oracle.rpa_oracle import Options, rpa_correlation_energy
     ref = rpa_correlation_energy(oracle_input(load_he_exx()), Options(nfreq=16))["ec"].real
     d = _prepare(tmp_path, "gb300_chi0_precision = fp64\ngb300_ec_path = lu\n", dataset=HE_DATASET)
+    r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))
+    assert abs(ec - ref) <= 1e-9, (ec, ref)
+
+
+def test_driver_reads_spin_polarised_dataset_without_gpu(tmp_path, lib):
+    """The spin-polarised Li atom dataset (two spin channels) parses up to the GPU call."""
+    if lib.librpa_gb300_device_count() > 0:
+        pytest.skip("a GPU is visible: the GPU test covers the full run")
+    d = _prepare(tmp_path, dataset=LI_DATASET)
+    r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1
+    assert "CUDA" in r.stderr or "device" in r.stderr, r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_li_spin_polarised(tmp_path, lib):
+    """task = rpa on the spin-polarised Li atom files against the oracle."""
+    from conftest import load_li_g0w0, oracle_input
+    from oracle.rpa_oracle import Options, rpa_correlation_energy
+    ref = rpa_correlation_energy(oracle_input(load_li_g0w0()), Options(nfreq=16))["ec"].real
+    d = _prepare(tmp_path, "gb300_chi0_precision = fp64\ngb300_ec_path = lu\n", dataset=LI_DATASET)
     r = subprocess.run([_driver(lib)], cwd=d, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_h2o, load_he_exx, oracle_input
+from conftest import load_h2o, load_he_exx, load_li_g0w0, oracle_input
 from librpa_gb300 import synthetic as sy
 from oracle.rpa_oracle import Options as OOpts, rpa_correlation_energy
 
@@ -121,6 +121,14 @@ def test_coulomb_given_as_2d_blocks():
     ec, perq = h.get_rpa_correlation_energy(_opts(s), L.n_ibz(s))
     assert abs(ec - ref) <= 1e-12 * abs(ref)
     np.testing.assert_allclose(perq, pref, rtol=1e-11, atol=1e-15)
+
+
+def test_li_spin_polarised_vs_oracle():
+    """Two spin channels (the Li atom of the reference's G0W0 suite): FP64 path vs the oracle."""
+    s = load_li_g0w0()
+    o = run_oracle(s)
+    _, ec, perq = run_gpu(s, L.CHI0_FP64)
+    assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
 
 
 def test_fcc2_k222_fp64_vs_oracle():

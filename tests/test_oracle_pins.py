@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import he_ref, load_h2o, load_he_exx, minimax_ref, oracle_input
+from conftest import he_ref, load_h2o, load_he_exx, load_li_g0w0, minimax_ref, oracle_input
 from oracle.minimax import minimax_grid
 from oracle.rpa_oracle import Options, build_gf, e_min_max, k_lists, r_grid, rpa_correlation_energy
 
@@ -83,3 +83,12 @@ def test_he_bcc_periodic_rpa_loops_equal_dense():
     b = rpa_correlation_energy(inp, Options(nfreq=16), chi0_impl="loops")["ec"]
     assert a.real < 0 and abs(a.imag) < 1e-12
     assert abs(a - b) <= 1e-11 * abs(a)
+
+
+def test_li_spin_polarised_rpa_loops_equal_dense():
+    """Two spin channels (the Li atom): the LibRI-loop and dense chi0 give one E_c."""
+    inp = oracle_input(load_li_g0w0())
+    assert inp.n_spins == 2
+    a = rpa_correlation_energy(inp, Options(nfreq=16), chi0_impl="dense")["ec"]
+    b = rpa_correlation_energy(inp, Options(nfreq=16), chi0_impl="loops")["ec"]
+    assert a.real < 0 and abs(a - b) <= 1e-12 * abs(a)
