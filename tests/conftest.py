@@ -99,6 +99,16 @@ def load_he_exx():
     return s
 
 
+def load_mgo_exx():
+    """MgO exchange inputs (3x3x3 k-points, 14 IBZ points) and the reference v_exx (eV, [k][state])."""
+    s = load_h2o("mgo_exx.npz")
+    z = np.load(GOLDEN / "mgo_exx.npz")
+    s.name = "mgo_exx"
+    s.v_cut = _blocks(z["vcut_meta"], z["vcut_data"], s.nabf)
+    s.vexx_ev = z["vexx_ev"]
+    return s
+
+
 def minimax_ref():
     return json.loads((GOLDEN / "minimax_ref.json").read_text())
 

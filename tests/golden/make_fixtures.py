@@ -34,6 +34,8 @@ Produces (all committed, so the tests need no reference tree at run time):
 
   he_bcc_dataset.tar.gz  the BCC He dataset itself (copied unchanged), for the driver's periodic test
   li_dataset.tar.gz  the spin-polarised Li atom dataset itself (copied unchanged), for the driver
+  mgo_exx.npz        the exchange inputs of the MgO G0W0 case (3x3x3 k-points, 14 IBZ points) and
+                     the v_exx column of its 27 tables (refs/g0w0_aims_MgO_libri/librpa/librpa.out)
   he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
                      regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
                      its inputs (bare Coulomb V(q) included, for RPA runs on real periodic
@@ -42,7 +44,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx ...].
+h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_exx ...].
 """
 from __future__ import annotations
 
@@ -184,6 +186,35 @@ def h2o_dataset(ref: Path):
     print("h2o_dataset.tar.gz written")
 
 
+def mgo_exx(ref: Path):
+    """The exchange inputs of the MgO G0W0 case (2 atoms, 3x3x3 k-points reduced to 14 IBZ points
+    by time reversal) and the v_exx column (eV) of its 27 quasi-particle tables."""
+    case = "g0w0_aims_MgO_libri"
+    tgz = ref / f"regression_tests/testcases/{case}/dataset.tar.gz"
+    log = (ref / f"regression_tests/refs/{case}/librpa/librpa.out").read_text().splitlines()
+    vexx = np.array([[row[4] for row in t] for t in _qp_tables(log)])
+    with tempfile.TemporaryDirectory() as td:
+        with tarfile.open(tgz) as tf:
+            tf.extractall(td, filter="data")
+        d = next(Path(td).rglob("band_out")).parent
+        inp = read_dataset(str(d))
+        cut = read_coulomb(str(d), "coulomb_cut", inp.nabf)
+    keys = sorted(inp.Cs)
+    ckeys = sorted(cut)
+    np.savez_compressed(
+        HERE / "mgo_exx.npz",
+        n_spins=inp.n_spins, n_kpts=inp.n_kpts, n_bands=inp.n_bands, n_ao=inp.n_ao,
+        wg=inp.wg, ekb=inp.ekb, efermi=inp.efermi, wfc=inp.wfc, latvec=inp.latvec,
+        period=np.array(inp.period), kvecs=inp.kvecs, ibz_map=inp.ibz_map,
+        nao=np.array(inp.nao), nabf=np.array(inp.nabf), positions=inp.positions,
+        cs_meta=np.array([[I, J, *R] for (I, J, R) in keys], np.int32),
+        cs_data=np.concatenate([inp.Cs[k].ravel() for k in keys]),
+        vq_meta=np.zeros((0, 3), np.int32), vq_data=np.zeros(0, complex),
+        vcut_meta=np.array(ckeys, np.int32), vcut_data=np.concatenate([cut[k].ravel() for k in ckeys]),
+        vexx_ev=vexx, nfreq=6)
+    print("mgo_exx.npz written:", vexx.shape)
+
+
 def li_dataset(ref: Path):
     import shutil
     src = ref / "regression_tests/testcases/g0w0_aims_Li_atom_libri/dataset.tar.gz"
@@ -317,7 +348,8 @@ def he_exx(ref: Path):
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "li_dataset", "minimax", "he_bcc", "g0w0",
-                             "li_g0w0", "he_exx"]
+                             "li_g0w0", "he_exx", "mgo_exx"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
-         "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset, "li_dataset": li_dataset}[name](ref)
+         "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset, "li_dataset": li_dataset,
+         "mgo_exx": mgo_exx}[name](ref)

@@ -3,7 +3,7 @@ and its pieces checked on their own (no GPU)."""
 import numpy as np
 import pytest
 
-from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, oracle_input
+from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo_exx, oracle_input
 from oracle.gw_oracle import (HA2EV, Pade, cal_hs_loops, exx_kgrid, full_from_blocks, g0w0_gamma,
                               ordered_blocks, power_hemat, qpe_solve, wc_freq)
 from oracle.rpa_oracle import Options, cs_tensors
@@ -63,6 +63,18 @@ def test_periodic_exchange_bcc_he_every_k_point():
     t = s.exx_tables
     assert t.shape == (8, 8, 3)
     np.testing.assert_allclose(e[0], t[:, :, 1], rtol=0, atol=6e-6)
+
+
+def test_periodic_exchange_mgo_ibz_reduced():
+    """MgO, 3x3x3 k-points of which 14 are irreducible by time reversal: the truncated Coulomb is
+    given at the IBZ points only, so V(R) takes the conjugated partners (FT_Vq, coulmat.cpp:7-90).
+    v_exx of all 17 states at all 27 k-points against refs/g0w0_aims_MgO_libri/librpa/librpa.out
+    (5 decimals in eV)."""
+    s = load_mgo_exx()
+    inp = oracle_input(s)
+    assert inp.n_kpts == 27 and len(set(int(x) for x in inp.ibz_map)) == 14
+    e = exx_kgrid(inp, s.v_cut)
+    np.testing.assert_allclose(e[0] * HA2EV, s.vexx_ev, rtol=0, atol=6e-6)
 
 
 def test_sigma_on_the_imaginary_axis_has_negative_imaginary_part(h2o):
