@@ -34,8 +34,9 @@ Produces (all committed, so the tests need no reference tree at run time):
 
   he_bcc_dataset.tar.gz  the BCC He dataset itself (copied unchanged), for the driver's periodic test
   li_dataset.tar.gz  the spin-polarised Li atom dataset itself (copied unchanged), for the driver
-  mgo_exx.npz        the exchange inputs of the MgO G0W0 case (3x3x3 k-points, 14 IBZ points) and
-                     the v_exx column of its 27 tables (refs/g0w0_aims_MgO_libri/librpa/librpa.out)
+  mgo_exx.npz        the inputs of the MgO G0W0 case (3x3x3 k-points, 14 IBZ points; bare and
+                     truncated Coulomb) and the v_exx column of its 27 tables
+                     (refs/g0w0_aims_MgO_libri/librpa/librpa.out)
   he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
                      regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
                      its inputs (bare Coulomb V(q) included, for RPA runs on real periodic
@@ -187,8 +188,9 @@ def h2o_dataset(ref: Path):
 
 
 def mgo_exx(ref: Path):
-    """The exchange inputs of the MgO G0W0 case (2 atoms, 3x3x3 k-points reduced to 14 IBZ points
-    by time reversal) and the v_exx column (eV) of its 27 quasi-particle tables."""
+    """The inputs of the MgO G0W0 case (2 atoms, 3x3x3 k-points reduced to 14 IBZ points by time
+    reversal; bare and truncated Coulomb at the IBZ points) and the v_exx column (eV) of its 27
+    quasi-particle tables.  Also the only real input with an IBZ reduction, for RPA runs."""
     case = "g0w0_aims_MgO_libri"
     tgz = ref / f"regression_tests/testcases/{case}/dataset.tar.gz"
     log = (ref / f"regression_tests/refs/{case}/librpa/librpa.out").read_text().splitlines()
@@ -209,7 +211,8 @@ def mgo_exx(ref: Path):
         nao=np.array(inp.nao), nabf=np.array(inp.nabf), positions=inp.positions,
         cs_meta=np.array([[I, J, *R] for (I, J, R) in keys], np.int32),
         cs_data=np.concatenate([inp.Cs[k].ravel() for k in keys]),
-        vq_meta=np.zeros((0, 3), np.int32), vq_data=np.zeros(0, complex),
+        vq_meta=np.array(sorted(inp.Vq), np.int32),
+        vq_data=np.concatenate([inp.Vq[k].ravel() for k in sorted(inp.Vq)]),
         vcut_meta=np.array(ckeys, np.int32), vcut_data=np.concatenate([cut[k].ravel() for k in ckeys]),
         vexx_ev=vexx, nfreq=6)
     print("mgo_exx.npz written:", vexx.shape)

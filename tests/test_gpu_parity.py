@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_h2o, load_he_exx, load_li_g0w0, oracle_input
+from conftest import load_h2o, load_he_exx, load_li_g0w0, load_mgo_exx, oracle_input
 from librpa_gb300 import synthetic as sy
 from oracle.rpa_oracle import Options as OOpts, rpa_correlation_energy
 
@@ -129,6 +129,21 @@ def test_li_spin_polarised_vs_oracle():
     o = run_oracle(s)
     _, ec, perq = run_gpu(s, L.CHI0_FP64)
     assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
+
+
+def test_mgo_ibz_reduced_vs_oracle():
+    """MgO (FHI-aims, 3x3x3 k-points of which 14 are irreducible, V(q) given at those only): the
+    IBZ path of the library (chi0 and E_c at the irreducible q, weights count/n_k) against the
+    oracle, FP64 and tensor-core paths.  The synthetic inputs have no IBZ reduction."""
+    s = load_mgo_exx()
+    s.nfreq = 6
+    o = run_oracle(s)
+    _, ec, perq = run_gpu(s, L.CHI0_FP64)
+    assert len(perq) == 14
+    assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
+    np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
+    _, ec2, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
 
 
 def test_fcc2_k222_fp64_vs_oracle():

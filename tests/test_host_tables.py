@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_he_exx, oracle_input
+from conftest import load_he_exx, load_mgo_exx, oracle_input
 from librpa_gb300 import synthetic as sy
 from oracle.rpa_oracle import TWO_PI, k_lists, r_grid
 
@@ -46,3 +46,10 @@ def test_synthetic_tables(lib, period):
     s = sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=period, nocc=2, seed=5)
     t = _check(s)
     assert len(t["ibz_rep"]) <= s.n_kpts
+
+
+def test_mgo_ibz_reduced_tables(lib):
+    """The only real input with an IBZ reduction (MgO: 27 k-points, 14 irreducible)."""
+    t = _check(load_mgo_exx())
+    assert len(t["cells"]) == 27 and len(t["ibz_rep"]) == 14
+    assert abs(t["ibz_w"].sum() - 1.0) < 1e-14
