@@ -24,9 +24,15 @@ oracle's chi0(q, omega):
   continuation  Thiele reciprocal differences (AnalyContPade, src/core/analycont.cpp:12-70)
   QP equation   damped fixed point (qpe_solver_pade_self_consistent, src/core/qpe_solver.cpp)
 
+g0w0_kgrid extends the chain to k-grids: W_c at the IBZ q-points (with the head of the
+dielectric matrix replaced by eps_mac at Gamma when asked), the q -> R transform with the
+time-reversed partners (FT_Wc_freq_q, epsilon.cpp:2323-2488), Sigma_c(R) shifted to the nearest
+BvK image and summed into Sigma_c(k) (gw.cpp:1010-1140).
+
 Pinned by the reference's own regression outputs: the H2O molecule (24 states, 16 minimax
 points, 16 Pade parameters; tests/golden/h2o_g0w0.npz), the spin-polarised Li atom
-(li_g0w0.npz) and the periodic BCC He exchange on a 2x2x2 k-grid (he_exx.npz).
+(li_g0w0.npz), the periodic BCC He exchange on a 2x2x2 k-grid (he_exx.npz) and the MgO G0W0
+run on a 3x3x3 k-grid with 14 IBZ points and the head correction (mgo_g0w0.npz).
 """
 from __future__ import annotations
 
@@ -94,6 +100,66 @@ def cal_hs_loops(C: dict, W: dict, D: dict, n_atoms: int, period):
                     d = D.get((K, J, sub(RJ, RK)))
                     if d is not None:
                         add((I, L, RL), np.einsum("ikjl,kj->il", T, d))
+    return H
+
+
+def cal_hs_batched(C: dict, W: dict, D: dict, n_atoms: int, period):
+    """cal_hs_loops with the innermost site loop (L, R_L) batched over the cells of each L atom:
+    the same sums, in a different order.  For k-grids, where the literal loops are slow."""
+    cells = r_grid(period)
+    sites = [(A, c) for A in range(n_atoms) for c in cells]
+    H = {}
+
+    def sub(b, a):
+        return centred_mod((b[0] - a[0], b[1] - a[1], b[2] - a[2]), period)
+
+    def add(key, val):
+        if key in H:
+            H[key] = H[key] + val
+        else:
+            H[key] = val.copy()
+
+    for I in range(n_atoms):
+        for (K, RK) in sites:
+            Ca = C.get((I, K, RK))
+            if Ca is None:
+                continue
+            for (J, RJ) in sites:
+                Wab = W.get((I, J, RJ))
+                if Wab is None:
+                    continue
+                CW = np.einsum("mn,mik->nik", Wab, Ca)
+                d_ij = D.get((I, J, RJ))
+                d_kj = D.get((K, J, sub(RJ, RK)))
+                for L in range(n_atoms):
+                    RLs = [RL for RL in cells if (J, L, sub(RL, RJ)) in C]
+                    if not RLs:
+                        continue
+                    Cb = np.stack([C[(J, L, sub(RL, RJ))] for RL in RLs])  # (c, nu, j, l)
+                    # a2b2: D[k, l] with (K, L@RL); result (I, J@RJ)
+                    sel = [c for c, RL in enumerate(RLs) if (K, L, sub(RL, RK)) in D]
+                    if sel:
+                        Ds = np.stack([D[(K, L, sub(RLs[c], RK))] for c in sel])
+                        Y = np.einsum("cnjl,ckl->cnjk", Cb[sel], Ds, optimize=True)
+                        add((I, J, RJ), np.einsum("nik,cnjk->ij", CW, Y, optimize=True))
+                    # a1b1: D[i, j]; result (K@RK, L@RL)
+                    if d_ij is not None:
+                        Z = np.einsum("nik,ij->nkj", CW, d_ij, optimize=True)
+                        R = np.einsum("nkj,cnjl->ckl", Z, Cb, optimize=True)
+                        for c, RL in enumerate(RLs):
+                            add((K, L, sub(RL, RK)), R[c])
+                    # a1b2: D[i, l] with (I, L@RL); result (K@RK, J@RJ)
+                    sel = [c for c, RL in enumerate(RLs) if (I, L, RL) in D]
+                    if sel:
+                        Ds = np.stack([D[(I, L, RLs[c])] for c in sel])
+                        P = np.einsum("nik,cil->cnkl", CW, Ds, optimize=True)
+                        add((K, J, sub(RJ, RK)), np.einsum("cnkl,cnjl->kj", P, Cb[sel], optimize=True))
+                    # a2b1: D[k, j]; result (I, L@RL)
+                    if d_kj is not None:
+                        Q = np.einsum("nik,kj->nij", CW, d_kj, optimize=True)
+                        R = np.einsum("nij,cnjl->cil", Q, Cb, optimize=True)
+                        for c, RL in enumerate(RLs):
+                            add((I, L, RL), R[c])
     return H
 
 
@@ -277,7 +343,7 @@ def exx_kgrid(inp: RPAInput, v_cut: dict):
     out = np.zeros((inp.n_spins, inp.n_kpts, inp.n_bands))
     off = np.concatenate([[0], np.cumsum(inp.nao)]).astype(int)
     for s in range(inp.n_spins):
-        H = cal_hs_loops(C, VR, dmat_r(inp, s, rlist), inp.n_atoms, inp.period)
+        H = cal_hs_batched(C, VR, dmat_r(inp, s, rlist), inp.n_atoms, inp.period)
         H = shift_bvk(H, inp)
         for k in range(inp.n_kpts):
             Hk = np.zeros((inp.n_ao, inp.n_ao), complex)
@@ -368,4 +434,137 @@ def g0w0_gamma(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
         out["e_qp"].append(np.array(e_qp))
         out["sigc"].append(np.array(sigc))
         out["info"].append(info)
+    return out
+
+
+# ----------------------------------------------------------------------------- G0W0 on k-grids
+
+def power_hemat_real(A: np.ndarray, power: float, threshold: float):
+    """power_hemat_blacs_real (utils_matrix_m_mpi.h:886-1010), used at the Gamma point: the
+    eigenpairs of Re A with eigenvalues in descending order, those below the threshold (counted
+    from the smallest) set to zero.  Returns (A^p, Z, Z w^p (column scaled), n_nonsingular)."""
+    w, Z = np.linalg.eigh(-A.real)
+    w = -w
+    n = len(w)
+    n_filtered = n
+    for i in range(n):
+        if w[n - 1 - i] >= threshold:
+            n_filtered = i
+            break
+    nn = n - n_filtered
+    wp = np.zeros(n)
+    wp[:nn] = np.power(w[:nn], power)
+    scaled = Z * wp
+    return scaled @ Z.T, Z, scaled, nn
+
+
+def wc_freq_head(chi0, v_eps, v_cut, epsmac, sqrt_threshold=0.0):
+    """The Gamma-point branch with the head of the dielectric matrix replaced (replace_w_head,
+    option_dielect_func != 3; epsilon.cpp:2030-2120): in the basis of V's eigenvectors (descending
+    eigenvalues), eps = 1 - Z (L^1/2 Z^T chi0 Z L^1/2)' Z^T where ' sets the (0, 0) element (the
+    largest Coulomb eigenvalue) to 1 - eps_mac."""
+    _, Z, sq, nn = power_hemat_real(v_eps, 0.5, sqrt_threshold)
+    X = sq[:, :nn].conj().T @ chi0 @ sq[:, :nn]
+    X[0, 0] = 1.0 - epsmac
+    eps = np.eye(len(Z)) - Z[:, :nn] @ X @ Z[:, :nn].conj().T
+    sc = power_hemat(v_cut, 0.5, sqrt_threshold)
+    return sc @ (np.linalg.solve(eps, sc) - sc)
+
+
+def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None = None, n_params: int = -1,
+               epsmac=None, sqrt_threshold: float = 0.0):
+    """G0W0 on the SCF k-grid (task = g0w0 with k-points; epsilon.cpp:1763-2322, :2323-2660,
+    gw.cpp:217-876, :884-1240).  inp.Vq: Coulomb matrix of the dielectric function at the IBZ
+    q-points, v_cut: truncated Coulomb there; epsmac: the macroscopic dielectric function at the
+    minimax frequencies (replace_w_head with option 0 copies dielecfunc_out), or None.
+    Returns per spin (n_k, n_states) arrays in Hartree: vexx, sigc at e_qp, e_qp."""
+    opts = opts or Options()
+    grid = grids_for(inp, opts)
+    nb, nao = inp.nabf, inp.nao
+    nf = opts.nfreq
+    klist, kfrac, ibz_order, _ = k_lists(inp)
+    rl = r_grid(inp.period)
+    C = cs_tensors(inp, 0.0)
+    pairs = upper_pairs(inp.n_atoms)
+    nbt = int(sum(nb))
+    chi0q = chi0q_partial(inp, opts, 0, nf)
+
+    # Wc(q, omega) at the IBZ points
+    Wq = {}
+    for iq, kq in enumerate(ibz_order):
+        v_e = assemble_full({p: inp.Vq[(kq, *p)] for p in pairs if (kq, *p) in inp.Vq}, nb)
+        v_c = assemble_full({p: v_cut[(kq, *p)] for p in pairs if (kq, *p) in v_cut}, nb)
+        gamma = bool(np.all(np.abs(klist[kq]) < 1e-10))
+        for iw in range(nf):
+            X = assemble_full(chi0q[iw][iq], nb)
+            if gamma and epsmac is not None:
+                Wq[(iq, iw)] = wc_freq_head(X, v_e, v_c, epsmac[iw], sqrt_threshold)
+            else:
+                s_e = power_hemat(v_e, 0.5, sqrt_threshold)
+                s_c = power_hemat(v_c, 0.5, sqrt_threshold)
+                eps = np.eye(nbt) - s_e @ X @ s_e
+                Wq[(iq, iw)] = s_c @ (np.linalg.solve(eps, s_c) - s_c)
+
+    # Wc(R, omega) (FT_Wc_freq_q: the BZ from the IBZ with W(-q) = W(q)^*, 1/n_k), real part,
+    # then Wc(R, tau) = sum_omega f2t(tau, omega) Wc(R, omega)
+    ibz_of = {kq: iq for iq, kq in enumerate(ibz_order)}
+    WR = {}
+    for c, R in enumerate(rl):
+        Rc = np.asarray(R, float) @ inp.latvec
+        for iw in range(nf):
+            acc = np.zeros((nbt, nbt), complex)
+            for k in range(inp.n_kpts):
+                rep = int(inp.ibz_map[k])
+                m = Wq[(ibz_of[rep], iw)]
+                if k != rep:
+                    m = m.conj()
+                acc += np.exp(-1j * TWO_PI * float(np.dot(klist[k], Rc))) / inp.n_kpts * m
+            WR[(c, iw)] = acc.real
+    Wt = []
+    for it in range(nf):
+        blocks = {}
+        off = np.concatenate([[0], np.cumsum(nb)]).astype(int)
+        for c, R in enumerate(rl):
+            full = sum(grid["cos_f2t"][it, iw] * WR[(c, iw)] for iw in range(nf))
+            for I in range(inp.n_atoms):
+                for J in range(inp.n_atoms):
+                    blocks[(I, J, tuple(R))] = full[off[I]:off[I + 1], off[J]:off[J + 1]].copy()
+        Wt.append(blocks)
+
+    out = {"grid": grid, "vexx": exx_kgrid(inp, v_cut), "sigc": [], "e_qp": [], "sigc_iw": []}
+    offa = np.concatenate([[0], np.cumsum(nao)]).astype(int)
+    for s in range(inp.n_spins):
+        sig_R = {}  # (I, J, R) -> (nf, n_I, n_J) complex
+        for it, tau in enumerate(grid["tau"]):
+            Gp = blocks_of(build_gf(inp, s, tau, kfrac, rl), nao)
+            Gn = blocks_of(build_gf(inp, s, -tau, kfrac, rl), nao)
+            Sp = cal_hs_batched(C, Wt[it], Gp, inp.n_atoms, inp.period)
+            Sn = cal_hs_batched(C, Wt[it], Gn, inp.n_atoms, inp.period)
+            for key in Sp:
+                if key not in Sn:
+                    continue
+                cp, sn = 0.5 * (Sp[key] + Sn[key]), 0.5 * (Sp[key] - Sn[key])
+                acc = sig_R.setdefault(key, np.zeros((nf,) + cp.shape, complex))
+                for iw in range(nf):
+                    acc[iw] += grid["cos_t2f"][iw, it] * cp + 1j * grid["sin_t2f"][iw, it] * sn
+        sig_R = shift_bvk(sig_R, inp)
+        sig_ks = np.zeros((inp.n_kpts, inp.n_bands, nf), complex)
+        for k in range(inp.n_kpts):
+            Sk = np.zeros((nf, inp.n_ao, inp.n_ao), complex)
+            for (I, J, R), m in sig_R.items():
+                ph = np.exp(1j * TWO_PI * float(np.dot(kfrac[k], R)))
+                Sk[:, offa[I]:offa[I + 1], offa[J]:offa[J + 1]] += ph * m
+            ev = inp.wfc[s, k]
+            sig_ks[k] = np.einsum("ni,wij,nj->nw", ev.conj(), Sk, ev)
+        xs = [1j * w for w in grid["omega"]]
+        e_qp = np.zeros((inp.n_kpts, inp.n_bands))
+        sigc = np.zeros((inp.n_kpts, inp.n_bands), complex)
+        for k in range(inp.n_kpts):
+            for n in range(inp.n_bands):
+                pade = Pade(n_params, xs, sig_ks[k, n])
+                _f, e, sg = qpe_solve(pade, inp.ekb[s, k, n], inp.efermi, vxc[s, k, n], out["vexx"][s, k, n])
+                e_qp[k, n], sigc[k, n] = e, sg
+        out["sigc_iw"].append(sig_ks)
+        out["e_qp"].append(e_qp)
+        out["sigc"].append(sigc)
     return out

@@ -99,13 +99,17 @@ def load_he_exx():
     return s
 
 
-def load_mgo_exx():
-    """MgO exchange inputs (3x3x3 k-points, 14 IBZ points) and the reference v_exx (eV, [k][state])."""
-    s = load_h2o("mgo_exx.npz")
-    z = np.load(GOLDEN / "mgo_exx.npz")
-    s.name = "mgo_exx"
+def load_mgo():
+    """MgO G0W0 case (3x3x3 k-points, 14 IBZ points): inputs, truncated Coulomb, v_xc, eps_mac
+    at the minimax frequencies and the reference quasi-particle tables ([k][state][column], eV)."""
+    s = load_h2o("mgo_g0w0.npz")
+    z = np.load(GOLDEN / "mgo_g0w0.npz")
+    s.name = "mgo"
     s.v_cut = _blocks(z["vcut_meta"], z["vcut_data"], s.nabf)
-    s.vexx_ev = z["vexx_ev"]
+    s.vxc = z["vxc"]
+    s.epsmac = z["epsmac"]
+    s.qp_tables = z["tables"]
+    s.n_params_anacon = int(z["n_params_anacon"])
     return s
 
 

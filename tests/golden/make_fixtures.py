@@ -34,8 +34,8 @@ Produces (all committed, so the tests need no reference tree at run time):
 
   he_bcc_dataset.tar.gz  the BCC He dataset itself (copied unchanged), for the driver's periodic test
   li_dataset.tar.gz  the spin-polarised Li atom dataset itself (copied unchanged), for the driver
-  mgo_exx.npz        the inputs of the MgO G0W0 case (3x3x3 k-points, 14 IBZ points; bare and
-                     truncated Coulomb) and the v_exx column of its 27 tables
+  mgo_g0w0.npz       the MgO G0W0 case (3x3x3 k-points, 14 IBZ points; bare and truncated Coulomb,
+                     v_xc, eps_mac of dielecfunc_out) and its 27 quasi-particle tables
                      (refs/g0w0_aims_MgO_libri/librpa/librpa.out)
   he_exx.npz         the periodic BCC He exchange case (2-atom cubic cell, 2x2x2 k-points;
                      regression_tests/testcases/exx_aims_bccHe_k_parallel_libri/dataset.tar.gz):
@@ -45,7 +45,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_exx ...].
+h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_g0w0 ...].
 """
 from __future__ import annotations
 
@@ -187,24 +187,29 @@ def h2o_dataset(ref: Path):
     print("h2o_dataset.tar.gz written")
 
 
-def mgo_exx(ref: Path):
-    """The inputs of the MgO G0W0 case (2 atoms, 3x3x3 k-points reduced to 14 IBZ points by time
-    reversal; bare and truncated Coulomb at the IBZ points) and the v_exx column (eV) of its 27
-    quasi-particle tables.  Also the only real input with an IBZ reduction, for RPA runs."""
+def mgo_g0w0(ref: Path):
+    """The MgO G0W0 case (2 atoms, 3x3x3 k-points reduced to 14 IBZ points by time reversal; bare and
+    truncated Coulomb at the IBZ points, v_xc, the macroscopic dielectric function of its head
+    correction) and its 27 quasi-particle tables.  Also the only real input with an IBZ reduction,
+    for RPA runs."""
     case = "g0w0_aims_MgO_libri"
     tgz = ref / f"regression_tests/testcases/{case}/dataset.tar.gz"
     log = (ref / f"regression_tests/refs/{case}/librpa/librpa.out").read_text().splitlines()
-    vexx = np.array([[row[4] for row in t] for t in _qp_tables(log)])
+    tables = np.array(_qp_tables(log))
     with tempfile.TemporaryDirectory() as td:
         with tarfile.open(tgz) as tf:
             tf.extractall(td, filter="data")
         d = next(Path(td).rglob("band_out")).parent
         inp = read_dataset(str(d))
         cut = read_coulomb(str(d), "coulomb_cut", inp.nabf)
+        vxc = read_vxc(str(d / "vxc_out"))
+        # dielecfunc_out: omega, Re eps_mac, Im eps_mac; replace_w_head with option 0 copies the
+        # real parts onto the minimax frequencies (read_dielec_func, interpolate_dielec_func)
+        epsmac = np.array([_floats(l)[1] for l in (d / "dielecfunc_out").read_text().splitlines() if l.strip()])
     keys = sorted(inp.Cs)
     ckeys = sorted(cut)
     np.savez_compressed(
-        HERE / "mgo_exx.npz",
+        HERE / "mgo_g0w0.npz",
         n_spins=inp.n_spins, n_kpts=inp.n_kpts, n_bands=inp.n_bands, n_ao=inp.n_ao,
         wg=inp.wg, ekb=inp.ekb, efermi=inp.efermi, wfc=inp.wfc, latvec=inp.latvec,
         period=np.array(inp.period), kvecs=inp.kvecs, ibz_map=inp.ibz_map,
@@ -214,8 +219,8 @@ def mgo_exx(ref: Path):
         vq_meta=np.array(sorted(inp.Vq), np.int32),
         vq_data=np.concatenate([inp.Vq[k].ravel() for k in sorted(inp.Vq)]),
         vcut_meta=np.array(ckeys, np.int32), vcut_data=np.concatenate([cut[k].ravel() for k in ckeys]),
-        vexx_ev=vexx, nfreq=6)
-    print("mgo_exx.npz written:", vexx.shape)
+        vxc=vxc, epsmac=epsmac, tables=tables, nfreq=6, n_params_anacon=-1)
+    print("mgo_g0w0.npz written:", tables.shape)
 
 
 def li_dataset(ref: Path):
@@ -351,8 +356,8 @@ def he_exx(ref: Path):
 if __name__ == "__main__":
     ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "li_dataset", "minimax", "he_bcc", "g0w0",
-                             "li_g0w0", "he_exx", "mgo_exx"]
+                             "li_g0w0", "he_exx", "mgo_g0w0"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
          "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset, "li_dataset": li_dataset,
-         "mgo_exx": mgo_exx}[name](ref)
+         "mgo_g0w0": mgo_g0w0}[name](ref)

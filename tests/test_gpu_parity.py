@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_h2o, load_he_exx, load_li_g0w0, load_mgo_exx, oracle_input
+from conftest import load_h2o, load_he_exx, load_li_g0w0, load_mgo, oracle_input
 from librpa_gb300 import synthetic as sy
 from oracle.rpa_oracle import Options as OOpts, rpa_correlation_energy
 
@@ -135,7 +135,7 @@ def test_mgo_ibz_reduced_vs_oracle():
     """MgO (FHI-aims, 3x3x3 k-points of which 14 are irreducible, V(q) given at those only): the
     IBZ path of the library (chi0 and E_c at the irreducible q, weights count/n_k) against the
     oracle, FP64 and tensor-core paths.  The synthetic inputs have no IBZ reduction."""
-    s = load_mgo_exx()
+    s = load_mgo()
     s.nfreq = 6
     o = run_oracle(s)
     _, ec, perq = run_gpu(s, L.CHI0_FP64)

@@ -1,11 +1,14 @@
 """The G0W0 oracle (oracle/gw_oracle.py) pinned against the reference's H2O G0W0 regression run,
 and its pieces checked on their own (no GPU)."""
+import os
+
 import numpy as np
 import pytest
 
-from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo_exx, oracle_input
-from oracle.gw_oracle import (HA2EV, Pade, cal_hs_loops, exx_kgrid, full_from_blocks, g0w0_gamma,
-                              ordered_blocks, power_hemat, qpe_solve, wc_freq)
+from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
+from oracle.gw_oracle import (HA2EV, Pade, cal_hs_batched, cal_hs_loops, coulomb_r, dmat_r, exx_kgrid,
+                              full_from_blocks, g0w0_gamma, g0w0_kgrid, ordered_blocks, power_hemat,
+                              qpe_solve, wc_freq)
 from oracle.rpa_oracle import Options, cs_tensors
 
 
@@ -70,11 +73,43 @@ def test_periodic_exchange_mgo_ibz_reduced():
     given at the IBZ points only, so V(R) takes the conjugated partners (FT_Vq, coulmat.cpp:7-90).
     v_exx of all 17 states at all 27 k-points against refs/g0w0_aims_MgO_libri/librpa/librpa.out
     (5 decimals in eV)."""
-    s = load_mgo_exx()
+    s = load_mgo()
     inp = oracle_input(s)
     assert inp.n_kpts == 27 and len(set(int(x) for x in inp.ibz_map)) == 14
     e = exx_kgrid(inp, s.v_cut)
-    np.testing.assert_allclose(e[0] * HA2EV, s.vexx_ev, rtol=0, atol=6e-6)
+    np.testing.assert_allclose(e[0] * HA2EV, s.qp_tables[:, :, 4], rtol=0, atol=6e-6)
+
+
+def test_batched_label_sum_equals_literal_loops():
+    """cal_hs_batched (the site loop over L batched by cells) against the literal loops, on the
+    periodic BCC He exchange (8 cells)."""
+    from oracle.rpa_oracle import r_grid
+    s = load_he_exx()
+    inp = oracle_input(s)
+    rl = r_grid(inp.period)
+    C = cs_tensors(inp)
+    VR, D = coulomb_r(inp, s.v_cut, rl), dmat_r(inp, 0, rl)
+    a = cal_hs_loops(C, VR, D, inp.n_atoms, inp.period)
+    b = cal_hs_batched(C, VR, D, inp.n_atoms, inp.period)
+    assert sorted(a) == sorted(b)
+    for k in a:
+        np.testing.assert_allclose(b[k], a[k], rtol=0, atol=1e-13 * np.abs(a[k]).max() + 1e-16)
+
+
+@pytest.mark.skipif(os.environ.get("LIBRPA_GB300_SLOW_TESTS") != "1",
+                    reason="about 5 minutes of CPU: set LIBRPA_GB300_SLOW_TESTS=1")
+def test_mgo_kgrid_g0w0_tables():
+    """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
+    replaced by eps_mac, 6 minimax points, all 6 in the Pade fit): every column of all 27 tables
+    of refs/g0w0_aims_MgO_libri/librpa/librpa.out to print precision.  Measured: all 459 states
+    within 5e-6 eV in every column."""
+    s = load_mgo()
+    inp = oracle_input(s)
+    r = g0w0_kgrid(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon, epsmac=s.epsmac)
+    t = s.qp_tables
+    got = np.stack([r["vexx"][0] * HA2EV, r["sigc"][0].real * HA2EV, r["sigc"][0].imag * HA2EV,
+                    r["e_qp"][0] * HA2EV], axis=-1)
+    np.testing.assert_allclose(got, t[:, :, 4:8], rtol=0, atol=6e-6)
 
 
 def test_sigma_on_the_imaginary_axis_has_negative_imaginary_part(h2o):

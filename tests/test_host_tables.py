@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_he_exx, load_mgo_exx, oracle_input
+from conftest import load_he_exx, load_mgo, oracle_input
 from librpa_gb300 import synthetic as sy
 from oracle.rpa_oracle import TWO_PI, k_lists, r_grid
 
@@ -50,6 +50,6 @@ def test_synthetic_tables(lib, period):
 
 def test_mgo_ibz_reduced_tables(lib):
     """The only real input with an IBZ reduction (MgO: 27 k-points, 14 irreducible)."""
-    t = _check(load_mgo_exx())
+    t = _check(load_mgo())
     assert len(t["cells"]) == 27 and len(t["ibz_rep"]) == 14
     assert abs(t["ibz_w"].sum() - 1.0) < 1e-14
