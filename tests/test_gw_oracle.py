@@ -80,6 +80,16 @@ def test_periodic_exchange_mgo_ibz_reduced():
     np.testing.assert_allclose(e[0] * HA2EV, s.qp_tables[:, :, 4], rtol=0, atol=6e-6)
 
 
+def test_kgrid_chain_reduces_to_the_gamma_chain(h2o):
+    """g0w0_kgrid on the H2O molecule (one k-point, no head correction) gives g0w0_gamma's
+    quasi-particle energies: the IBZ unfolding, BvK shift and Bloch sums reduce to the identity."""
+    s, inp, r = h2o
+    k = g0w0_kgrid(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon)
+    np.testing.assert_allclose(k["vexx"][0, 0], r["vexx"][0], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(k["e_qp"][0][0], r["e_qp"][0], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(k["sigc"][0][0], r["sigc"][0], rtol=0, atol=1e-10)
+
+
 def test_batched_label_sum_equals_literal_loops():
     """cal_hs_batched (the site loop over L batched by cells) against the literal loops, on the
     periodic BCC He exchange (8 cells)."""
