@@ -163,6 +163,71 @@ def cal_hs_batched(C: dict, W: dict, D: dict, n_atoms: int, period):
     return H
 
 
+def cal_hs_cells(C: dict, W: dict, D: dict, nao, nabf, period):
+    """The four-label sum of cal_hs_loops vectorised over the BvK cells: for each quadruple of
+    atoms (I, J, K, L) the cell sums become batched contractions over cell-indexed arrays
+    (absent blocks are zeros, which add nothing).  With u = R_L - R_J (the cell of C^J's second
+    atom) and v = R_J - R_K:
+      a2b2: H[I,J,R_J]   = sum C[I,K,R_K] W[I,J,R_J] E1[v],  E1[v] = sum_u C[J,L,u] D[K,L,v+u]
+      a1b1: H[K,L,v+u]  += sum C[I,K,R_K] W[I,J,R_J] D[I,J,R_J] C[J,L,u]
+      a1b2: H[K,J,v]    += sum C[I,K,R_K] W[I,J,R_J] P[R_J],  P[R_J] = sum_u C[J,L,u] D[I,L,R_J+u]
+      a2b1: H[I,L,R_J+u] += sum S[R_J] C[J,L,u],  S[R_J] = W[I,J,R_J]^T sum_K C[I,K,R_K] D[K,J,v]
+    Returns every (X, Y, R) block, zero blocks included."""
+    cells = r_grid(period)
+    nc = len(cells)
+    cidx = {c: i for i, c in enumerate(cells)}
+    add = np.array([[cidx[centred_mod(tuple(a[d] + b[d] for d in range(3)), period)] for b in cells] for a in cells])
+    sub = np.array([[cidx[centred_mod(tuple(a[d] - b[d] for d in range(3)), period)] for b in cells] for a in cells])
+    na = len(nao)
+
+    def arr(T, A, B, shape):
+        out = np.zeros((nc,) + shape)
+        for c, R in enumerate(cells):
+            t = T.get((A, B, R))
+            if t is not None:
+                out[c] = t
+        return out
+
+    Ca = {(A, B): arr(C, A, B, (nabf[A], nao[A], nao[B])) for A in range(na) for B in range(na)}
+    Wa = {(A, B): arr(W, A, B, (nabf[A], nabf[B])) for A in range(na) for B in range(na)}
+    Da = {(A, B): arr(D, A, B, (nao[A], nao[B])) for A in range(na) for B in range(na)}
+    H = {(A, B): np.zeros((nc, nao[A], nao[B])) for A in range(na) for B in range(na)}
+    RJ, RK = np.meshgrid(np.arange(nc), np.arange(nc), indexing="ij")  # [R_J, R_K]
+    V = sub[RJ, RK]                                                   # v = R_J - R_K
+    for I in range(na):
+        for J in range(na):
+            Wij = Wa[(I, J)]                       # [R_J] mu nu
+            Dij = Da[(I, J)]                       # [R_J] i j
+            for K in range(na):
+                Cik = Ca[(I, K)]                   # [R_K] mu i k
+                # a2b1 intermediate: T[R_J] = sum_{R_K} C[I,K,R_K] D[K,J,R_J - R_K]
+                Dkj = Da[(K, J)][V]                # [R_J, R_K] k j
+                Tsum = np.einsum("bmik,abkj->amij", Cik, Dkj, optimize=True)
+                S4 = np.einsum("amn,amij->anij", Wij, Tsum, optimize=True)  # [R_J] nu i j
+                for L in range(na):
+                    Cjl = Ca[(J, L)]               # [u] nu j l
+                    # a2b2
+                    Dkl = Da[(K, L)]               # [w] k l
+                    E1 = np.einsum("unjl,vukl->vnjk", Cjl, Dkl[add], optimize=True)  # [v] nu j k
+                    CW = np.einsum("amn,bmik->abnik", Wij, Cik, optimize=True)         # [R_J, R_K]
+                    H[(I, J)] += np.einsum("abnik,abnjk->aij", CW, E1[V], optimize=True)
+                    # a1b1: result cell v + u
+                    F = np.einsum("abnik,aij->abnkj", CW, Dij, optimize=True)
+                    G = np.einsum("abnkj,unjl->abukl", F, Cjl, optimize=True)
+                    tgt = add[V.reshape(-1)].reshape(nc, nc, nc)  # cell v + u for [R_J, R_K, u]
+                    np.add.at(H[(K, L)], tgt.reshape(-1), G.reshape((-1,) + G.shape[3:]))
+                    # a1b2: result cell v
+                    Dil = Da[(I, L)]               # [R_L] i l
+                    P = np.einsum("unjl,auil->anji", Cjl, Dil[add], optimize=True)  # [R_J] nu j i
+                    Qm = np.einsum("amn,anji->amji", Wij, P, optimize=True)
+                    R3 = np.einsum("bmik,amji->abkj", Cik, Qm, optimize=True)
+                    np.add.at(H[(K, J)], V.reshape(-1), R3.reshape((-1,) + R3.shape[2:]))
+                    # a2b1: result cell R_J + u
+                    R4 = np.einsum("anij,unjl->auil", S4, Cjl, optimize=True)
+                    np.add.at(H[(I, L)], add.reshape(-1), R4.reshape((-1,) + R4.shape[2:]))
+    return {(A, B, cells[c]): H[(A, B)][c] for (A, B) in H for c in range(nc)}
+
+
 def ordered_blocks(full: np.ndarray, nb) -> dict:
     """Atom blocks (I, J, (0,0,0)) of a full Gamma-point matrix, all ordered pairs."""
     off = np.concatenate([[0], np.cumsum(nb)]).astype(int)
@@ -343,7 +408,7 @@ def exx_kgrid(inp: RPAInput, v_cut: dict):
     out = np.zeros((inp.n_spins, inp.n_kpts, inp.n_bands))
     off = np.concatenate([[0], np.cumsum(inp.nao)]).astype(int)
     for s in range(inp.n_spins):
-        H = cal_hs_batched(C, VR, dmat_r(inp, s, rlist), inp.n_atoms, inp.period)
+        H = cal_hs_cells(C, VR, dmat_r(inp, s, rlist), inp.nao, inp.nabf, inp.period)
         H = shift_bvk(H, inp)
         for k in range(inp.n_kpts):
             Hk = np.zeros((inp.n_ao, inp.n_ao), complex)
@@ -538,8 +603,8 @@ def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
         for it, tau in enumerate(grid["tau"]):
             Gp = blocks_of(build_gf(inp, s, tau, kfrac, rl), nao)
             Gn = blocks_of(build_gf(inp, s, -tau, kfrac, rl), nao)
-            Sp = cal_hs_batched(C, Wt[it], Gp, inp.n_atoms, inp.period)
-            Sn = cal_hs_batched(C, Wt[it], Gn, inp.n_atoms, inp.period)
+            Sp = cal_hs_cells(C, Wt[it], Gp, nao, nb, inp.period)
+            Sn = cal_hs_cells(C, Wt[it], Gn, nao, nb, inp.period)
             for key in Sp:
                 if key not in Sn:
                     continue

@@ -1,12 +1,10 @@
 """The G0W0 oracle (oracle/gw_oracle.py) pinned against the reference's H2O G0W0 regression run,
 and its pieces checked on their own (no GPU)."""
-import os
-
 import numpy as np
 import pytest
 
 from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
-from oracle.gw_oracle import (HA2EV, Pade, cal_hs_batched, cal_hs_loops, coulomb_r, dmat_r, exx_kgrid,
+from oracle.gw_oracle import (HA2EV, Pade, cal_hs_batched, cal_hs_cells, cal_hs_loops, coulomb_r, dmat_r, exx_kgrid,
                               full_from_blocks, g0w0_gamma, g0w0_kgrid, ordered_blocks, power_hemat,
                               qpe_solve, wc_freq)
 from oracle.rpa_oracle import Options, cs_tensors
@@ -91,8 +89,8 @@ def test_kgrid_chain_reduces_to_the_gamma_chain(h2o):
 
 
 def test_batched_label_sum_equals_literal_loops():
-    """cal_hs_batched (the site loop over L batched by cells) against the literal loops, on the
-    periodic BCC He exchange (8 cells)."""
+    """cal_hs_batched (the site loop over L batched by cells) and cal_hs_cells (every cell sum
+    vectorised) against the literal loops, on the periodic BCC He exchange (8 cells)."""
     from oracle.rpa_oracle import r_grid
     s = load_he_exx()
     inp = oracle_input(s)
@@ -101,18 +99,19 @@ def test_batched_label_sum_equals_literal_loops():
     VR, D = coulomb_r(inp, s.v_cut, rl), dmat_r(inp, 0, rl)
     a = cal_hs_loops(C, VR, D, inp.n_atoms, inp.period)
     b = cal_hs_batched(C, VR, D, inp.n_atoms, inp.period)
-    assert sorted(a) == sorted(b)
+    c = cal_hs_cells(C, VR, D, inp.nao, inp.nabf, inp.period)
+    assert sorted(a) == sorted(b) and set(a) <= set(c)
+    scale = max(np.abs(v).max() for v in a.values())
     for k in a:
-        np.testing.assert_allclose(b[k], a[k], rtol=0, atol=1e-13 * np.abs(a[k]).max() + 1e-16)
+        np.testing.assert_allclose(b[k], a[k], rtol=0, atol=1e-13 * scale)
+        np.testing.assert_allclose(c[k], a[k], rtol=0, atol=1e-13 * scale)
+    assert all(np.abs(c[k]).max() == 0.0 for k in c if k not in a)
 
 
-@pytest.mark.skipif(os.environ.get("LIBRPA_GB300_SLOW_TESTS") != "1",
-                    reason="about 5 minutes of CPU: set LIBRPA_GB300_SLOW_TESTS=1")
 def test_mgo_kgrid_g0w0_tables():
     """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
     replaced by eps_mac, 6 minimax points, all 6 in the Pade fit): every column of all 27 tables
-    of refs/g0w0_aims_MgO_libri/librpa/librpa.out to print precision.  Measured: all 459 states
-    within 5e-6 eV in every column."""
+    of refs/g0w0_aims_MgO_libri/librpa/librpa.out to print precision (459 states)."""
     s = load_mgo()
     inp = oracle_input(s)
     r = g0w0_kgrid(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon, epsmac=s.epsmac)
