@@ -146,6 +146,17 @@ def test_mgo_ibz_reduced_vs_oracle():
     assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
 
 
+def test_mgo_ibz_reduced_equals_full_bz():
+    """The library's E_c of MgO over the 14 irreducible q-points equals its E_c with all 27
+    k-points irreducible (V(-q) = V(q)^*)."""
+    from test_oracle_pins import unfold_ibz
+    s = load_mgo()
+    _, a, _ = run_gpu(s, L.CHI0_FP64)
+    _, b, pb = run_gpu(unfold_ibz(s), L.CHI0_FP64)
+    assert len(pb) == 27
+    assert abs(a - b) <= 1e-10 * abs(a)
+
+
 def test_fcc2_k222_fp64_vs_oracle():
     s = sy.fcc2_k222()
     h, ec, perq = run_gpu(s, L.CHI0_FP64)
