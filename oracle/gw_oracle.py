@@ -37,6 +37,7 @@ run on a 3x3x3 k-grid with 14 IBZ points and the head correction (mgo_g0w0.npz).
 from __future__ import annotations
 
 import math
+from dataclasses import dataclass
 
 import numpy as np
 
@@ -399,23 +400,36 @@ def shift_bvk(H: dict, inp: RPAInput):
     return out
 
 
-def exx_kgrid(inp: RPAInput, v_cut: dict):
-    """v_exx[s, k, n] (Hartree) on the SCF k-grid (task = exx; exx.cpp:213-500, :720-860)."""
+@dataclass
+class BandPoints:
+    """k-points off the SCF grid (task = exx_band / g0w0_band): fractional coordinates, their
+    mean-field eigenpairs and v_xc (librpa_set_band_kvec, set_band_occ_eigval, set_wfc_band)."""
+    kfrac: np.ndarray   # (n, 3)
+    wfc: np.ndarray     # (n_spins, n, n_bands, n_ao)
+    ekb: np.ndarray     # (n_spins, n, n_bands) Hartree
+    efermi: float
+    vxc: np.ndarray | None = None  # (n_spins, n, n_bands) Hartree
+
+
+def exx_kgrid(inp: RPAInput, v_cut: dict, band: BandPoints | None = None):
+    """v_exx[s, k, n] (Hartree) on the SCF k-grid (task = exx; exx.cpp:213-500, :720-860), or at
+    the band points: H(R) summed with e^{i 2 pi k.R} at any k (Exx::build_KS_band)."""
     _, kfrac, _, _ = k_lists(inp)
+    kpts, wfc = (kfrac, inp.wfc) if band is None else (band.kfrac, band.wfc)
     rlist = r_grid(inp.period)
     C = cs_tensors(inp, 0.0)
     VR = coulomb_r(inp, v_cut, rlist)
-    out = np.zeros((inp.n_spins, inp.n_kpts, inp.n_bands))
+    out = np.zeros((inp.n_spins, len(kpts), inp.n_bands))
     off = np.concatenate([[0], np.cumsum(inp.nao)]).astype(int)
     for s in range(inp.n_spins):
         H = cal_hs_cells(C, VR, dmat_r(inp, s, rlist), inp.nao, inp.nabf, inp.period)
         H = shift_bvk(H, inp)
-        for k in range(inp.n_kpts):
+        for k in range(len(kpts)):
             Hk = np.zeros((inp.n_ao, inp.n_ao), complex)
             for (I, J, R), m in H.items():
-                ph = np.exp(1j * TWO_PI * float(np.dot(kfrac[k], R)))
+                ph = np.exp(1j * TWO_PI * float(np.dot(kpts[k], R)))
                 Hk[off[I]:off[I + 1], off[J]:off[J + 1]] += ph * m
-            ev = inp.wfc[s, k]
+            ev = wfc[s, k]
             out[s, k] = -np.einsum("ni,ij,nj->n", ev.conj(), Hk, ev).real
     return out
 
@@ -537,12 +551,14 @@ def wc_freq_head(chi0, v_eps, v_cut, epsmac, sqrt_threshold=0.0):
 
 
 def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None = None, n_params: int = -1,
-               epsmac=None, sqrt_threshold: float = 0.0):
+               epsmac=None, sqrt_threshold: float = 0.0, band: BandPoints | None = None):
     """G0W0 on the SCF k-grid (task = g0w0 with k-points; epsilon.cpp:1763-2322, :2323-2660,
     gw.cpp:217-876, :884-1240).  inp.Vq: Coulomb matrix of the dielectric function at the IBZ
     q-points, v_cut: truncated Coulomb there; epsmac: the macroscopic dielectric function at the
     minimax frequencies (replace_w_head with option 0 copies dielecfunc_out), or None.
-    Returns per spin (n_k, n_states) arrays in Hartree: vexx, sigc at e_qp, e_qp."""
+    Returns per spin (n_k, n_states) arrays in Hartree: vexx, sigc at e_qp, e_qp.  With band,
+    Sigma_c(R) and H_x(R) are summed at the band points instead and the QP equation takes their
+    eigenvalues, Fermi level and v_xc (librpa_get_g0w0_sigc_band_k, compute_g0w0.cpp:300-366)."""
     opts = opts or Options()
     grid = grids_for(inp, opts)
     nb, nao = inp.nabf, inp.nao
@@ -596,7 +612,11 @@ def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
                     blocks[(I, J, tuple(R))] = full[off[I]:off[I + 1], off[J]:off[J + 1]].copy()
         Wt.append(blocks)
 
-    out = {"grid": grid, "vexx": exx_kgrid(inp, v_cut), "sigc": [], "e_qp": [], "sigc_iw": []}
+    out = {"grid": grid, "vexx": exx_kgrid(inp, v_cut, band), "sigc": [], "e_qp": [], "sigc_iw": []}
+    if band is None:
+        kpts, wfc, ekb, ef, vx = kfrac, inp.wfc, inp.ekb, inp.efermi, vxc
+    else:
+        kpts, wfc, ekb, ef, vx = band.kfrac, band.wfc, band.ekb, band.efermi, band.vxc
     offa = np.concatenate([[0], np.cumsum(nao)]).astype(int)
     for s in range(inp.n_spins):
         sig_R = {}  # (I, J, R) -> (nf, n_I, n_J) complex
@@ -613,21 +633,22 @@ def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
                 for iw in range(nf):
                     acc[iw] += grid["cos_t2f"][iw, it] * cp + 1j * grid["sin_t2f"][iw, it] * sn
         sig_R = shift_bvk(sig_R, inp)
-        sig_ks = np.zeros((inp.n_kpts, inp.n_bands, nf), complex)
-        for k in range(inp.n_kpts):
+        nkp = len(kpts)
+        sig_ks = np.zeros((nkp, inp.n_bands, nf), complex)
+        for k in range(nkp):
             Sk = np.zeros((nf, inp.n_ao, inp.n_ao), complex)
             for (I, J, R), m in sig_R.items():
-                ph = np.exp(1j * TWO_PI * float(np.dot(kfrac[k], R)))
+                ph = np.exp(1j * TWO_PI * float(np.dot(kpts[k], R)))
                 Sk[:, offa[I]:offa[I + 1], offa[J]:offa[J + 1]] += ph * m
-            ev = inp.wfc[s, k]
+            ev = wfc[s, k]
             sig_ks[k] = np.einsum("ni,wij,nj->nw", ev.conj(), Sk, ev)
         xs = [1j * w for w in grid["omega"]]
-        e_qp = np.zeros((inp.n_kpts, inp.n_bands))
-        sigc = np.zeros((inp.n_kpts, inp.n_bands), complex)
-        for k in range(inp.n_kpts):
+        e_qp = np.zeros((nkp, inp.n_bands))
+        sigc = np.zeros((nkp, inp.n_bands), complex)
+        for k in range(nkp):
             for n in range(inp.n_bands):
                 pade = Pade(n_params, xs, sig_ks[k, n])
-                _f, e, sg = qpe_solve(pade, inp.ekb[s, k, n], inp.efermi, vxc[s, k, n], out["vexx"][s, k, n])
+                _f, e, sg = qpe_solve(pade, ekb[s, k, n], ef, vx[s, k, n], out["vexx"][s, k, n])
                 e_qp[k, n], sigc[k, n] = e, sg
         out["sigc_iw"].append(sig_ks)
         out["e_qp"].append(e_qp)

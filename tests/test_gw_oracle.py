@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
-from oracle.gw_oracle import (HA2EV, Pade, cal_hs_batched, cal_hs_cells, cal_hs_loops, coulomb_r, dmat_r, exx_kgrid,
+from oracle.gw_oracle import (HA2EV, BandPoints, Pade, cal_hs_batched, cal_hs_cells, cal_hs_loops, coulomb_r, dmat_r, exx_kgrid,
                               full_from_blocks, g0w0_gamma, g0w0_kgrid, ordered_blocks, power_hemat,
                               qpe_solve, wc_freq)
 from oracle.rpa_oracle import Options, cs_tensors
@@ -86,6 +86,24 @@ def test_kgrid_chain_reduces_to_the_gamma_chain(h2o):
     np.testing.assert_allclose(k["vexx"][0, 0], r["vexx"][0], rtol=0, atol=1e-12)
     np.testing.assert_allclose(k["e_qp"][0][0], r["e_qp"][0], rtol=0, atol=1e-10)
     np.testing.assert_allclose(k["sigc"][0][0], r["sigc"][0], rtol=0, atol=1e-10)
+
+
+def test_band_points_on_the_scf_grid_reproduce_the_kgrid_results():
+    """Band k-points (task = g0w0_band) placed on SCF k-points, with the SCF eigenpairs, give the
+    k-grid quasi-particle energies: Sigma_c(R) and H_x(R) summed at arbitrary k are the same
+    Bloch sums.  Three MgO k-points, one of them off the IBZ representatives."""
+    from oracle.rpa_oracle import k_lists
+    s = load_mgo()
+    inp = oracle_input(s)
+    _, kfrac, _, _ = k_lists(inp)
+    pick = [0, 5, 17]
+    band = BandPoints(kfrac=kfrac[pick], wfc=inp.wfc[:, pick], ekb=inp.ekb[:, pick], efermi=inp.efermi,
+                      vxc=s.vxc[:, pick])
+    o = Options(nfreq=s.nfreq)
+    full = g0w0_kgrid(inp, s.v_cut, s.vxc, o, n_params=s.n_params_anacon, epsmac=s.epsmac)
+    part = g0w0_kgrid(inp, s.v_cut, s.vxc, o, n_params=s.n_params_anacon, epsmac=s.epsmac, band=band)
+    np.testing.assert_allclose(part["vexx"][0], full["vexx"][0][pick], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(part["e_qp"][0], full["e_qp"][0][pick], rtol=0, atol=1e-10)
 
 
 def test_batched_label_sum_equals_literal_loops():
