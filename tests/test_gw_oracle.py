@@ -88,20 +88,18 @@ def test_kgrid_chain_reduces_to_the_gamma_chain(h2o):
     np.testing.assert_allclose(k["sigc"][0][0], r["sigc"][0], rtol=0, atol=1e-10)
 
 
-def test_band_points_on_the_scf_grid_reproduce_the_kgrid_results():
+def test_band_points_on_the_scf_grid_reproduce_the_kgrid_results(mgo):
     """Band k-points (task = g0w0_band) placed on SCF k-points, with the SCF eigenpairs, give the
     k-grid quasi-particle energies: Sigma_c(R) and H_x(R) summed at arbitrary k are the same
     Bloch sums.  Three MgO k-points, one of them off the IBZ representatives."""
     from oracle.rpa_oracle import k_lists
-    s = load_mgo()
-    inp = oracle_input(s)
+    s, inp, full = mgo
     _, kfrac, _, _ = k_lists(inp)
     pick = [0, 5, 17]
     band = BandPoints(kfrac=kfrac[pick], wfc=inp.wfc[:, pick], ekb=inp.ekb[:, pick], efermi=inp.efermi,
                       vxc=s.vxc[:, pick])
-    o = Options(nfreq=s.nfreq)
-    full = g0w0_kgrid(inp, s.v_cut, s.vxc, o, n_params=s.n_params_anacon, epsmac=s.epsmac)
-    part = g0w0_kgrid(inp, s.v_cut, s.vxc, o, n_params=s.n_params_anacon, epsmac=s.epsmac, band=band)
+    part = g0w0_kgrid(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon, epsmac=s.epsmac,
+                      band=band)
     np.testing.assert_allclose(part["vexx"][0], full["vexx"][0][pick], rtol=0, atol=1e-12)
     np.testing.assert_allclose(part["e_qp"][0], full["e_qp"][0][pick], rtol=0, atol=1e-10)
 
@@ -126,13 +124,19 @@ def test_batched_label_sum_equals_literal_loops():
     assert all(np.abs(c[k]).max() == 0.0 for k in c if k not in a)
 
 
-def test_mgo_kgrid_g0w0_tables():
-    """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
-    replaced by eps_mac, 6 minimax points, all 6 in the Pade fit): every column of all 27 tables
-    of refs/g0w0_aims_MgO_libri/librpa/librpa.out to print precision (459 states)."""
+@pytest.fixture(scope="module")
+def mgo():
     s = load_mgo()
     inp = oracle_input(s)
     r = g0w0_kgrid(inp, s.v_cut, s.vxc, Options(nfreq=s.nfreq), n_params=s.n_params_anacon, epsmac=s.epsmac)
+    return s, inp, r
+
+
+def test_mgo_kgrid_g0w0_tables(mgo):
+    """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
+    replaced by eps_mac, 6 minimax points, all 6 in the Pade fit): every column of all 27 tables
+    of refs/g0w0_aims_MgO_libri/librpa/librpa.out to print precision (459 states)."""
+    s, inp, r = mgo
     t = s.qp_tables
     got = np.stack([r["vexx"][0] * HA2EV, r["sigc"][0].real * HA2EV, r["sigc"][0].imag * HA2EV,
                     r["e_qp"][0] * HA2EV], axis=-1)
