@@ -90,6 +90,9 @@ typedef struct
     double d2h_bytes;           /* device -> host bytes of results */
     long long screen_fallbacks; /* (tau, spin) steps where an audited skipped block exceeded the
                                    threshold and every block was contracted */
+    long long ec_lu_fallback_q; /* IBZ q points whose V(q) had no Cholesky factor (indefinite, as
+                                   the Gamma-point bare Coulomb matrix of a crystal can be) and
+                                   whose E_c term the Cholesky path took by the LU form instead */
 } LibrpaGB300Stats;
 
 /* Set defaults. */

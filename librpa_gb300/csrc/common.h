@@ -8,6 +8,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -99,6 +100,30 @@ public:
 private:
     T *p_ = nullptr;
     size_t n_ = 0;
+};
+
+// Per-device one-time set-up (kernel attributes act on the current device only).  The
+// caller keeps one PerDeviceOnce per set-up step; run() calls f() the first time it is used
+// with a given device current, and is safe to call from several host threads.
+class PerDeviceOnce
+{
+public:
+    template <typename F>
+    void run(F &&f)
+    {
+        int dev = -1;
+        GB_CUDA(cudaGetDevice(&dev));
+        GB_REQUIRE(dev >= 0 && dev < kMaxDevices, "device ordinal out of range");
+        std::lock_guard<std::mutex> lk(mu_);
+        if (done_[dev]) return;
+        f();
+        done_[dev] = true;
+    }
+
+private:
+    static constexpr int kMaxDevices = 64;
+    std::mutex mu_;
+    bool done_[kMaxDevices] = {};
 };
 
 inline double wall_seconds()

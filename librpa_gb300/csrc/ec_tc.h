@@ -19,7 +19,10 @@ public:
     EcChol(int N, int nw, bool complex_path, int qb, bool fp64_products = false);
     ~EcChol();
     // V = L L^H in place for nb (<= qb) Coulomb matrices stored one after another (N x N each).
-    int factor_v(void *V, int nb, cudaStream_t st);
+    // bad[b] != 0 where V has no Cholesky factor (not positive definite: the Gamma-point bare
+    // Coulomb matrix of a real crystal can be indefinite); the caller evaluates those q by
+    // the LU form, which needs no definiteness.
+    int factor_v(void *V, int nb, std::vector<int> &bad, cudaStream_t st);
     // For batch slot `slot`: M = L^H chi0 L for the nw chi0 matrices X (tensor-core GEMMs),
     // M' = I - M kept for finish(), and tr(V chi0) = tr(M) per frequency.
     int stage_q(const void *L, const void *X, int slot, cudaStream_t st);

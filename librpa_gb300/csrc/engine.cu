@@ -648,42 +648,9 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         GB_CUDA(cudaStreamSynchronize(st));  // the block tables go out of scope
         ++launches;
     };
-    if (use_chol)
-    {
-        // every q's V = L L^H in one batched factorisation, M' = I - L^H chi0 L per q on the tensor
-        // cores, then one batched FP64 Cholesky of all the M'; q points go in batches that keep
-        // the M' store within about 24 GB
-        const size_t esz = gamma_only ? sizeof(double) : sizeof(cuDoubleComplex);
-        // complex M' is factored as its real 2N x 2N embedding: 32 bytes per element of M'
-        const double per_q = static_cast<double>(nw) * NN * (gamma_only ? esz : 2 * esz) + NN * esz;
-        const int qb = std::max(1, std::min(std::max(qe - qa, 1), static_cast<int>(24.0e9 / per_q)));
-        EcChol ecc(N, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
-        DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
-        for (int q0 = qa; q0 < qe; q0 += qb)
-        {
-            const int nb = std::min(qb, qe - q0);
-            for (int s = 0; s < nb; ++s) assemble_v(q0 + s, Vall.get() + static_cast<size_t>(s) * NN * esz);
-            launches += ecc.factor_v(Vall.get(), nb, st);
-            for (int s = 0; s < nb; ++s)
-            {
-                const int q = q0 + s;
-                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
-                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
-                                     d_eoff.get(), gamma_only,
-                                     gamma_only ? nullptr : reinterpret_cast<cuDoubleComplex *>(X.get()),
-                                     gamma_only ? reinterpret_cast<double *>(X.get()) : nullptr, NN, st);
-                launches += 1 + ecc.stage_q(Vall.get() + static_cast<size_t>(s) * NN * esz, X.get(), s, st);
-            }
-            std::vector<cplx> tr, ld;
-            launches += ecc.finish(nb, tr, ld, st);
-            for (int s = 0; s < nb; ++s)
-                for (int w = 0; w < nw; ++w)
-                    res.per_q[q0 + s] += (tr[s * nw + w] + ld[s * nw + w]) * tf.omega_w[w] * ibz_w[q0 + s] / (2.0 * M_PI);
-            ec_flops += nb * nw * (gamma_only ? (2.0 * 2.0 * N * N * N + N * static_cast<double>(N) * N / 3.0)
-                                              : (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0));
-        }
-    }
-    for (int q = qa; q < qe && !use_chol; ++q)
+    // Reference form for one q: Pi = V chi0 in FP64, LU with partial pivoting, sum log(+-u_ii)
+    // + tr Pi (epsilon.cpp:414-536).  It needs no definiteness of V(q).
+    auto ec_lu_q = [&](int q)
     {
         // V(q) full: blocks of this q inside the staged Coulomb blob
         std::vector<long long> voff;
@@ -747,10 +714,62 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             }
             ec_flops += nw * (8.0 * N * N * N + 8.0 * N * N * N / 3.0);
         }
+    };
+    int lu_fallback_q = 0;
+    if (use_chol)
+    {
+        // every q's V = L L^H in one batched factorisation, M' = I - L^H chi0 L per q on the tensor
+        // cores, then one batched FP64 Cholesky of all the M'; q points go in batches that keep
+        // the M' store within about 24 GB
+        const size_t esz = gamma_only ? sizeof(double) : sizeof(cuDoubleComplex);
+        // complex M' is factored as its real 2N x 2N embedding: 32 bytes per element of M'
+        const double per_q = static_cast<double>(nw) * NN * (gamma_only ? esz : 2 * esz) + NN * esz;
+        const int qb = std::max(1, std::min(std::max(qe - qa, 1), static_cast<int>(24.0e9 / per_q)));
+        EcChol ecc(N, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
+        DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
+        for (int q0 = qa; q0 < qe; q0 += qb)
+        {
+            const int nb = std::min(qb, qe - q0);
+            for (int s = 0; s < nb; ++s) assemble_v(q0 + s, Vall.get() + static_cast<size_t>(s) * NN * esz);
+            std::vector<int> badv;
+            launches += ecc.factor_v(Vall.get(), nb, badv, st);
+            // q whose V(q) has no Cholesky factor (an indefinite Gamma-point Coulomb matrix)
+            // take the LU form; the others fill the batch slots in order
+            std::vector<int> slot_q;
+            for (int s = 0; s < nb; ++s)
+            {
+                const int q = q0 + s;
+                if (badv[s])
+                {
+                    ec_lu_q(q);
+                    ++lu_fallback_q;
+                    continue;
+                }
+                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
+                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
+                                     d_eoff.get(), gamma_only,
+                                     gamma_only ? nullptr : reinterpret_cast<cuDoubleComplex *>(X.get()),
+                                     gamma_only ? reinterpret_cast<double *>(X.get()) : nullptr, NN, st);
+                launches += 1 + ecc.stage_q(Vall.get() + static_cast<size_t>(s) * NN * esz, X.get(),
+                                            static_cast<int>(slot_q.size()), st);
+                slot_q.push_back(q);
+            }
+            const int ns_ok = static_cast<int>(slot_q.size());
+            if (ns_ok == 0) continue;
+            std::vector<cplx> tr, ld;
+            launches += ecc.finish(ns_ok, tr, ld, st);
+            for (int s = 0; s < ns_ok; ++s)
+                for (int w = 0; w < nw; ++w)
+                    res.per_q[slot_q[s]] += (tr[s * nw + w] + ld[s * nw + w]) * tf.omega_w[w] * ibz_w[slot_q[s]] / (2.0 * M_PI);
+            ec_flops += ns_ok * nw * (gamma_only ? (2.0 * 2.0 * N * N * N + N * static_cast<double>(N) * N / 3.0)
+                                                 : (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0));
+        }
     }
+    for (int q = qa; q < qe && !use_chol; ++q) ec_lu_q(q);
     ev_ec.stop(st);
     S.t_ec = ev_ec.ms() * 1e-3;
     S.ec_flops = ec_flops;
+    S.ec_lu_fallback_q = lu_fallback_q;
     for (const cplx &v : res.per_q) res.ec += v;
 
     // keep chi0(q, w) for inspection (a STAGE_EC call keeps the loaded one)

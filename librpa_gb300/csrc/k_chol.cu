@@ -310,12 +310,10 @@ int chol_batched_r(double *A, int N, int batch, double *diag, int *bad, cudaStre
 int chol_batched_r_ozaki(double *A, int N, int batch, double *diag, int *bad, OzakiWork &w, cudaStream_t st)
 {
     constexpr int NBO = OZAKI_NB;
-    static bool attr = false;
-    if (!attr)
-    {
+    static PerDeviceOnce attr;
+    attr.run([] {
         GB_CUDA(cudaFuncSetAttribute(k_chol_diag_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, DINV_SMEM));
-        attr = true;
-    }
+    });
     int launches = 0;
     for (int k0 = 0; k0 < N; k0 += NBO)
     {

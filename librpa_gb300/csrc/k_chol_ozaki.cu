@@ -340,13 +340,11 @@ void ozaki_free(OzakiWork &w)
 namespace {
 void set_syrk_attributes()
 {
-    static bool attr = false;
-    if (!attr)
-    {
+    static PerDeviceOnce attr;
+    attr.run([] {
         GB_CUDA(cudaFuncSetAttribute(k_ozaki_syrk<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
         GB_CUDA(cudaFuncSetAttribute(k_ozaki_syrk<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM));
-        attr = true;
-    }
+    });
 }
 } // namespace
 

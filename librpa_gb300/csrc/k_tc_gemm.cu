@@ -356,12 +356,10 @@ static void launch_tc(const SplitMat &A, const SplitMat &B, int M, int N, int K,
         make_tmap_bf16(&maps.a[p], A.p[p], A.kpad, A.rows, ba, A.kpad, A.batch_stride, BK, BM);
         make_tmap_bf16(&maps.b[p], B.p[p], B.kpad, B.rows, bb, B.kpad, B.batch_stride, BK, BN);
     }
-    static bool attr = false;
-    if (!attr)
-    {
+    static PerDeviceOnce attr;
+    attr.run([] {
         GB_CUDA(cudaFuncSetAttribute(k_tc_gemm<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, Cfg<NS>::SMEM_BYTES));
-        attr = true;
-    }
+    });
     const long long ntm = (M + BM - 1) / BM, ntn = (N + BN - 1) / BN;
     GB_REQUIRE(!o.lower_tiles || ntm == ntn, "lower-tile GEMM needs a square tile grid");
     GB_REQUIRE(o.tri >= 0 && o.tri <= 2, "triangular operand mode must be 0, 1 or 2");

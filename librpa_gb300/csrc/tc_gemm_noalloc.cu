@@ -9,8 +9,9 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the array's
 // device address with cudaGetSymbolAddress and sets the GEMM kernels' shared-memory
-// attribute there; make that first call before any stream capture. Later calls on the
-// device only launch kernels and read back the 4-byte error flag.
+// attribute there; make that first call before any stream capture. Every call, the first
+// and the later ones, launches its kernels, then synchronises the stream and copies the
+// 4-byte error flag to the host before it returns.
 //
 // There is one scratch array per device, so calls whose GPU work overlaps (two host
 // threads, or two streams on the same device) race on it: serialise them.

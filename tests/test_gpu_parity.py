@@ -89,8 +89,15 @@ def test_he_bcc_fhi_aims_periodic_vs_oracle():
     _, ec, perq = run_gpu(s, L.CHI0_FP64)
     assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
     np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
-    _, ec2, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    # default path: V(Gamma) of MgO is indefinite, so that q goes through the LU form
+    h2, ec2, perq2 = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    assert h2.stats()["ec_lu_fallback_q"] == 1
     assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
+    np.testing.assert_allclose(perq2, o["per_q"], rtol=0, atol=MEV_PER_ATOM * len(s.nao))
+    # the all-FP64 Cholesky form takes the same fallback and keeps FP64 accuracy
+    h3, ec3, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL_FP64)
+    assert h3.stats()["ec_lu_fallback_q"] == 1
+    assert abs(ec3 - o["ec"].real) <= 1e-9 * abs(o["ec"].real)
 
 
 def test_coulomb_given_as_2d_blocks():
@@ -142,8 +149,15 @@ def test_mgo_ibz_reduced_vs_oracle():
     assert len(perq) == 14
     assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
     np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
-    _, ec2, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    # default path: V(Gamma) of MgO is indefinite, so that q goes through the LU form
+    h2, ec2, perq2 = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    assert h2.stats()["ec_lu_fallback_q"] == 1
     assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
+    np.testing.assert_allclose(perq2, o["per_q"], rtol=0, atol=MEV_PER_ATOM * len(s.nao))
+    # the all-FP64 Cholesky form takes the same fallback and keeps FP64 accuracy
+    h3, ec3, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL_FP64)
+    assert h3.stats()["ec_lu_fallback_q"] == 1
+    assert abs(ec3 - o["ec"].real) <= 1e-9 * abs(o["ec"].real)
 
 
 def test_mgo_ibz_reduced_equals_full_bz():

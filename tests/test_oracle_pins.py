@@ -118,3 +118,21 @@ def test_mgo_ibz_reduction_gives_the_full_bz_ec():
     b = rpa_correlation_energy(oracle_input(unfold_ibz(s)), Options(nfreq=s.nfreq))
     assert len(a["per_q"]) == 14 and len(b["per_q"]) == 27
     assert abs(a["ec"] - b["ec"]) <= 1e-10 * abs(a["ec"])  # rounding: 2.5e-12 measured
+
+
+def test_mgo_gamma_coulomb_is_indefinite():
+    """The bare Coulomb matrix V(q = Gamma) of the real MgO input is indefinite (its smallest
+    eigenvalue is about -0.2, the largest about 42), so V = L L^H does not exist there and a
+    Cholesky-form E_c must take that q by the LU form (epsilon.cpp:489-536), which needs no
+    definiteness.  The other irreducible q have positive definite V(q).  This keeps the GPU
+    path's LU fallback exercised by the MgO parity test."""
+    from oracle.rpa_oracle import assemble_full, k_lists
+    s = load_mgo()
+    inp = oracle_input(s)
+    _, _, ibz_order, _ = k_lists(inp)
+    lows = []
+    for ikf in ibz_order:
+        blocks = {(I, J): v for (ik, I, J), v in inp.Vq.items() if ik == ikf}
+        lows.append(np.linalg.eigvalsh(assemble_full(blocks, inp.nabf)).min())
+    assert lows[0] < -0.1  # Gamma
+    assert all(v > 0 for v in lows[1:])

@@ -81,3 +81,41 @@ def test_noalloc_gemm_rejects_oversized(lib):
     assert "scratch" in msg and "33554432" in msg, msg
     rc = lib.librpa_gb300_tc_gemm_noalloc(64, 64, 64, t.data_ptr(), t.data_ptr(), t.data_ptr(), 4, None)
     assert rc != 0 and "pieces" in lib.librpa_get_last_error(None).decode()
+
+
+def test_noalloc_gemm_at_the_scratch_limit(lib):
+    """A request that needs exactly the 32 MiB of scratch runs (the error flag then sits in the
+    array's last 256 bytes) and gives the split GEMM's accuracy on two calls in a row; one row
+    more is rejected, and the entry point still works after the rejection.  With 2 pieces and
+    K = 64 (one 64-wide K block), the scratch need is 2 * (M + N) * 64 * 2 + 256 bytes."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    limit = 32 << 20
+    K, N = 64, 128
+    M = (limit - 256) // 256 - N  # 2 * (M + N) * 64 * 2 + 256 == limit
+    assert 2 * (M + N) * 64 * 2 + 256 == limit
+    rng = np.random.default_rng(5)
+    a = rng.uniform(-1, 1, (M, K))
+    b = rng.uniform(-1, 1, (K, N))
+    ref = a @ b
+    da = torch.from_numpy(a).to(dev)
+    db = torch.from_numpy(b).to(dev)
+    outs = []
+    for _ in range(2):
+        dd = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+        rc = lib.librpa_gb300_tc_gemm_noalloc(M, N, K, da.data_ptr(), db.data_ptr(), dd.data_ptr(), 2, None)
+        assert rc == 0, lib.librpa_get_last_error(None).decode()
+        torch.cuda.synchronize()
+        outs.append(dd.cpu().numpy().astype(np.float64))
+    assert np.array_equal(outs[0], outs[1])
+    assert np.abs(outs[0] - ref).max() / np.abs(ref).max() < bound(2, K)
+    # one more row needs 256 bytes beyond the array
+    big = torch.zeros((M + 1) * K, dtype=torch.float64, device=dev)
+    dd = torch.zeros((M + 1) * N, dtype=torch.float32, device=dev)
+    rc = lib.librpa_gb300_tc_gemm_noalloc(M + 1, N, K, big.data_ptr(), db.data_ptr(), dd.data_ptr(), 2, None)
+    assert rc != 0 and "scratch" in lib.librpa_get_last_error(None).decode()
+    dd = torch.full((M, N), float("nan"), dtype=torch.float32, device=dev)
+    rc = lib.librpa_gb300_tc_gemm_noalloc(M, N, K, da.data_ptr(), db.data_ptr(), dd.data_ptr(), 2, None)
+    assert rc == 0, lib.librpa_get_last_error(None).decode()
+    torch.cuda.synchronize()
+    assert np.array_equal(dd.cpu().numpy().astype(np.float64), outs[0])
