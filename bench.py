@@ -37,7 +37,7 @@ PREC = {"bf16x3": 1, "fp32": 2, "fp64": 0}
 
 
 # DRAM bytes (read + write) of one per-(tau, spin) chi0 contraction launch set, from one ncu capture
-# per kernel (profiles/*.md, same workload); None where no capture exists.
+# per kernel on the same workload; None where no capture exists.
 PROFILED_TRAFFIC = {
     "fcc16_k333": {"bytes": 18.4119e9 + 0.0625e9 + 5.2037e9 + 0.3735e9,
                    "source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_t1_tc (tau_1) and the X "

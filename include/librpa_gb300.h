@@ -154,19 +154,25 @@ long long librpa_gb300_chi0_qw_elems(LibrpaHandler *h);
 int librpa_gb300_copy_chi0_qw(LibrpaHandler *h, double *dst, int on_device);
 int librpa_gb300_load_chi0_qw(LibrpaHandler *h, const double *src, long long n_elems, int on_device);
 
-/* Learned screening (no counterpart in the reference).  The model is a 5-64-64-1 GELU MLP
- * (FP16 weights, FP32 accumulation) predicting log10 max |chi0(I,J,R,tau)| from the block's
- * distance, log10 tau, log10(max|C_I| max|C_J|) and log10 max |G(+-tau)_IJ(R)|.  Its training
- * data are the blocks logged by calls with screen_mode = LIBRPA_GB300_SCREEN_THRESHOLD.
+/* Learned screening (no counterpart in the reference).  The model is a 9-64-64-1 GELU MLP
+ * (FP16 weights, FP32 accumulation) predicting log10 max |chi0(I,J,R,tau)| from nine features
+ * of the block: distance (Bohr), log10 tau, log10(max|C_I| max|C_J|), log10 max |G(+tau)_IJ(R)|,
+ * log10 max |G(-tau)_IJ(R)|, log10(n_abf(I) n_abf(J)), log10(n_ao(I) n_ao(J)) and the species
+ * of I and of J (the types given to librpa_set_atoms).  Its training data are the blocks logged
+ * by calls with screen_mode = LIBRPA_GB300_SCREEN_THRESHOLD, on this handler or added from
+ * others with librpa_gb300_add_screening_samples.
  * librpa_gb300_train_screening trains it on the GPU (Adam, `iterations` steps of up to 16384
  * samples); a screen_mode = MLP call trains it itself when needed.  Returns 0 on success and
  * writes the training RMSE (log10 units) to *rmse. */
 int librpa_gb300_train_screening(LibrpaHandler *h, int iterations, double learning_rate, double *rmse);
-/* Logged samples: count, and a copy (x: n x 5 features, y: n targets). */
+/* Logged samples: count, and a copy (x: n x 9 features, y: n targets). */
 long long librpa_gb300_screening_samples(LibrpaHandler *h);
 int librpa_gb300_get_screening_samples(LibrpaHandler *h, float *x, float *y, long long n);
-/* The trained model: 4609 parameters (W1[64][5], b1[64], W2[64][64], b2[64], W3[64], b3) and
- * 13 normalisation values (feature means[5], scales[5], target mean, target scale, decision
+/* Append n samples (x: n x 9 features, y: n targets) logged elsewhere, e.g. by the plain runs
+ * of other systems, to this handler's training set.  Returns 0 on success. */
+int librpa_gb300_add_screening_samples(LibrpaHandler *h, const float *x, const float *y, long long n);
+/* The trained model: 4865 parameters (W1[64][9], b1[64], W2[64][64], b2[64], W3[64], b3) and
+ * 21 normalisation values (feature means[9], scales[9], target mean, target scale, decision
  * margin).  get returns 0 when a model exists; set installs one. */
 int librpa_gb300_get_screening_model(LibrpaHandler *h, float *params, float *norm);
 int librpa_gb300_set_screening_model(LibrpaHandler *h, const float *params, const float *norm);

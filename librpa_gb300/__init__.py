@@ -28,7 +28,8 @@ TFGRID_UNSET, GaussLegendre, GaussChebyshevI, GaussChebyshevII, Minimax, EvenSpa
 CHI0_FP64, CHI0_BF16X3, CHI0_FP32 = 0, 1, 2
 EC_LU_FP64, EC_CHOL, EC_CHOL_FP64 = 0, 1, 2
 SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
-MLP_NPARAM, MLP_NNORM = 4609, 13
+MLP_IN = 9
+MLP_NPARAM, MLP_NNORM = 64 * MLP_IN + 64 + 64 * 64 + 64 + 64 + 1, 2 * MLP_IN + 3
 STAGE_FULL, STAGE_CHI0, STAGE_EC = 0, 1, 2
 
 
@@ -135,7 +136,8 @@ EXPORTS = [
     "librpa_get_last_error", "librpa_get_last_error_code", "librpa_gb300_minimax_grid",
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
-    "librpa_gb300_get_screening_samples", "librpa_gb300_get_screening_model", "librpa_gb300_set_screening_model",
+    "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
+    "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
     "librpa_gb300_solve_qpe", "librpa_gb300_phase_tables",
@@ -195,6 +197,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_train_screening": (i, [vp, i, d, C.POINTER(C.c_double)]),
         "librpa_gb300_screening_samples": (C.c_longlong, [vp]),
         "librpa_gb300_get_screening_samples": (i, [vp, vp, vp, C.c_longlong]),
+        "librpa_gb300_add_screening_samples": (i, [vp, vp, vp, C.c_longlong]),
         "librpa_gb300_get_screening_model": (i, [vp, vp, vp]),
         "librpa_gb300_set_screening_model": (i, [vp, vp, vp]),
         "librpa_gb300_clear_screening": (None, [vp]),

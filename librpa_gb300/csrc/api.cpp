@@ -1058,6 +1058,24 @@ int librpa_gb300_get_screening_samples(LibrpaHandler *h, float *x, float *y, lon
     return rc;
 }
 
+// No counterpart in the reference: append block samples logged elsewhere (another handler's
+// plain-screening runs, other systems), so one model trains on the logs of several systems.
+int librpa_gb300_add_screening_samples(LibrpaHandler *h, const float *x, const float *y, long long n)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        GB_REQUIRE(n >= 0, "negative sample count");
+        GB_REQUIRE(n == 0 || (x && y), "null sample arrays");
+        for (long long t = 0; t < n; ++t) GB_REQUIRE(std::isfinite(y[t]), "non-finite sample target");
+        for (long long t = 0; t < n * gb::MLP_IN; ++t) GB_REQUIRE(std::isfinite(x[t]), "non-finite sample feature");
+        gb::ScreenLog &lg = get_ds(h)->screen_log;
+        lg.x.insert(lg.x.end(), x, x + n * gb::MLP_IN);
+        lg.y.insert(lg.y.end(), y, y + n);
+        rc = 0;
+    });
+    return rc;
+}
+
 int librpa_gb300_get_screening_model(LibrpaHandler *h, float *params, float *norm)
 {
     int rc = 1;

@@ -336,7 +336,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     const double thr_g = opts.libri_chi0_threshold_G;
     const int n_blk = n_pairs * nc;
     DevBuf<double> d_bnorm;
-    DevBuf<float> d_feat, d_pred, d_dist, d_cmax;
+    DevBuf<float> d_feat, d_pred, d_dist, d_cmax, d_kind;
     std::vector<double> h_norm;
     std::vector<float> h_feat, h_pred;
     std::vector<unsigned char> active, audited;
@@ -373,6 +373,12 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         d_dist.upload(dist.data(), n_blk, st);
         d_cmax.alloc(n_at);
         d_cmax.upload(cmax.data(), n_at, st);
+        // species of each atom: the type given to librpa_set_atoms (0 when none was given)
+        std::vector<float> kind(n_at, 0.0f);
+        if (static_cast<int>(ds.types.size()) >= n_at)
+            for (int I = 0; I < n_at; ++I) kind[I] = static_cast<float>(ds.types[I]);
+        d_kind.alloc(n_at);
+        d_kind.upload(kind.data(), n_at, st);
         d_bnorm.alloc(n_blk);
         d_feat.alloc(static_cast<size_t>(n_blk) * MLP_IN);
         h_norm.resize(n_blk);
@@ -462,7 +468,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 // share of the rest; an audited block above the threshold means fall back
                 ev_x.start(st);
                 launches += tcp->prepare(d_G.get(), st);
-                launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), tau, d_feat.get(), st);
+                launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), d_kind.get(), tau, d_feat.get(), st);
                 mlp_predict(ds.screen_model, d_feat.get(), n_blk, d_pred.get(), st);
                 launches += 3;
                 d_pred.download(h_pred.data(), n_blk, st);
@@ -512,7 +518,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             {
                 // plain screening: every block computed; its features and norm are logged
                 launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
-                launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), tau, d_feat.get(), st);
+                launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), d_kind.get(), tau, d_feat.get(), st);
                 launches += 2;
                 d_bnorm.download(h_norm.data(), n_blk, st);
                 d_feat.download(h_feat.data(), h_feat.size(), st);

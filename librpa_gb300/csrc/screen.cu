@@ -74,7 +74,8 @@ __global__ void k_block_drop(double *__restrict__ chi0R, Geom g, Pairs pr, const
 
 // one warp per (pair, cell) block
 __global__ void k_block_features(const double *__restrict__ G, Geom g, Pairs pr, const float *__restrict__ dist,
-                                 const float *__restrict__ cmax, float ltau, float *__restrict__ feat, int n_blk)
+                                 const float *__restrict__ cmax, const float *__restrict__ kind, float ltau,
+                                 float *__restrict__ feat, int n_blk)
 {
     const int b = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
@@ -99,6 +100,10 @@ __global__ void k_block_features(const double *__restrict__ G, Geom g, Pairs pr,
         f[2] = cc > 0.0f ? log10f(cc) : LOG_FLOOR;
         f[3] = gm[0] > 0.0f ? log10f(gm[0]) : LOG_FLOOR;
         f[4] = gm[1] > 0.0f ? log10f(gm[1]) : LOG_FLOOR;
+        f[5] = log10f(static_cast<float>(g.nabf[I]) * static_cast<float>(g.nabf[J]));
+        f[6] = log10f(static_cast<float>(ni) * static_cast<float>(nj));
+        f[7] = kind[I];
+        f[8] = kind[J];
     }
 }
 
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(GB) k_mlp_grad(const __half *__restrict__ W, c
     // dW1[k][f] = sum_t dz1_t[k] xn_t[f]; db1[k] = sum_t dz1_t[k]
     {
         const int k = t;
-        float a[MLP_IN] = {0.f, 0.f, 0.f, 0.f, 0.f};
+        float a[MLP_IN] = {};
         float b = 0.0f;
         for (int u = 0; u < GB; ++u)
         {
@@ -295,10 +300,10 @@ void launch_block_drop(double *chi0R, const Geom &g, const Pairs &pr, const doub
 }
 
 void launch_block_features(const double *G, const Geom &g, const Pairs &pr, const float *dist, const float *cmax,
-                           double tau, float *feat, cudaStream_t st)
+                           const float *kind, double tau, float *feat, cudaStream_t st)
 {
     const int n_blk = pr.n_pairs * g.n_c;
-    k_block_features<<<(n_blk + 3) / 4, 128, 0, st>>>(G, g, pr, dist, cmax, static_cast<float>(std::log10(tau)),
+    k_block_features<<<(n_blk + 3) / 4, 128, 0, st>>>(G, g, pr, dist, cmax, kind, static_cast<float>(std::log10(tau)),
                                                       feat, n_blk);
     GB_LAUNCH_CHECK();
 }

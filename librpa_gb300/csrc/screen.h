@@ -4,7 +4,7 @@
 // its max-norm exceeds the threshold.  The same rule, applied to the chi0 output blocks with
 // LibrpaGB300Options.screen_threshold, is the plain screening: every block is contracted and
 // blocks with max |chi0| <= threshold are dropped.  The learned screening predicts
-// log10 max |chi0| per block with a small MLP (5 inputs, two hidden layers of 64, GELU, FP16
+// log10 max |chi0| per block with a small MLP (9 inputs, two hidden layers of 64, GELU, FP16
 // weights, FP32 accumulation) and contracts only the blocks predicted above the threshold,
 // plus a random audit share of the others; an audited block above the threshold makes the
 // whole (tau, spin) fall back to the plain rule.
@@ -29,9 +29,11 @@ void launch_block_maxnorm(const double *chi0R, const Geom &g, const Pairs &pr, d
 void launch_block_drop(double *chi0R, const Geom &g, const Pairs &pr, const double *norm, double thr,
                        cudaStream_t st);
 // features of every (pair, cell) block at one tau: distance (Bohr), log10 tau,
-// log10(cmax_I cmax_J), log10 max |G+_IJ(cell)|, log10 max |G-_IJ(cell)|
+// log10(cmax_I cmax_J), log10 max |G+_IJ(cell)|, log10 max |G-_IJ(cell)|, log10 of the ABF and
+// of the NAO block dimensions (n_abf(I) n_abf(J), n_ao(I) n_ao(J)), and the species (kind) of I
+// and of J
 void launch_block_features(const double *G, const Geom &g, const Pairs &pr, const float *dist,
-                           const float *cmax, double tau, float *feat, cudaStream_t st);
+                           const float *cmax, const float *kind, double tau, float *feat, cudaStream_t st);
 
 // ---- MLP (screen.cu): predictions, training, and the gradient self-check
 // y[n] = model(x[n]) in the target's own units (log10 max |chi0|).

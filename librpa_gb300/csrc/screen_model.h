@@ -6,7 +6,9 @@
 
 namespace gb {
 
-constexpr int MLP_IN = 5;
+// Block features: distance (Bohr), log10 tau, log10(max|C_I| max|C_J|), log10 max|G+_IJ(R)|,
+// log10 max|G-_IJ(R)|, log10(n_abf(I) n_abf(J)), log10(n_ao(I) n_ao(J)), species of I, species of J
+constexpr int MLP_IN = 9;
 constexpr int MLP_H = 64;
 // W1 [H][IN], b1 [H], W2 [H][H], b2 [H], W3 [H], b3
 constexpr int MLP_NPARAM = MLP_H * MLP_IN + MLP_H + MLP_H * MLP_H + MLP_H + MLP_H + 1;

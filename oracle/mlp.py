@@ -1,6 +1,6 @@
 """CPU restatement of the learned block-screening MLP (test infrastructure only).
 
-Checks the GPU forward / backward kernels of librpa_gb300/csrc/screen.cu: a 5-64-64-1 network
+Checks the GPU forward / backward kernels of librpa_gb300/csrc/screen.cu: a 9-64-64-1 network
 with GELU activations, parameters rounded to FP16 (the GPU stores FP16 weights and
 accumulates in FP32; this restatement accumulates in FP64), normalised inputs and targets,
 and the mean squared error on normalised targets.  The network has no counterpart in the
@@ -11,7 +11,7 @@ import math
 
 import numpy as np
 
-IN, H = 5, 64
+IN, H = 9, 64
 NPARAM = H * IN + H + H * H + H + H + 1
 NNORM = 2 * IN + 3
 _ERF = np.vectorize(math.erf)
@@ -39,7 +39,7 @@ def gelu_d(z):
 
 
 def forward(params, norm, x):
-    """Prediction in target units (log10 max |chi0|) for features x [n, 5]."""
+    """Prediction in target units (log10 max |chi0|) for features x [n, 9]."""
     W1, b1, W2, b2, W3, b3 = unpack(params)
     norm = np.asarray(norm, np.float64)
     xn = (np.asarray(x, np.float64) - norm[:IN]) / norm[IN:2 * IN]

@@ -1,7 +1,8 @@
 """Generate the golden fixtures of tests/golden/ from the LibRPA reference tree.
 
-Run in a container where the reference is mounted (default /root/reference):
-    python tests/golden/make_fixtures.py [/path/to/reference]
+Run where a LibRPA source tree is available, naming it by argument or by the environment
+variable LIBRPA_REFERENCE:
+    python tests/golden/make_fixtures.py /path/to/reference [fixture ...]
 
 Produces (all committed, so the tests need no reference tree at run time):
   h2o_libri.npz      inputs of the H2O regression dataset
@@ -51,6 +52,7 @@ from __future__ import annotations
 
 import json
 import re
+import os
 import sys
 import tarfile
 import tempfile
@@ -354,7 +356,10 @@ def he_exx(ref: Path):
 
 
 if __name__ == "__main__":
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LIBRPA_REFERENCE")
+    if not src:
+        sys.exit("usage: make_fixtures.py /path/to/reference [fixture ...] (or set LIBRPA_REFERENCE)")
+    ref = Path(src)
     which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "li_dataset", "minimax", "he_bcc", "g0w0",
                              "li_g0w0", "he_exx", "mgo_g0w0"]
     for name in which:

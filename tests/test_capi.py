@@ -126,6 +126,16 @@ def test_errors_are_recorded_not_thrown(lib):
         lib.librpa_get_rpa_correlation_energy(None, None, 0, np.zeros(1), np.zeros(1))  # NaN
 
 
+def test_invalid_routing_is_rejected_before_any_gpu_work(lib):
+    """A parallel_routing value outside the reference's enum (librpa_enums.h: AUTO, RTAU, ATOMPAIR,
+    LIBRI) is an error recorded on the handler, as the reference's option parser rejects it."""
+    s = load_h2o()
+    with L.Handler() as h:
+        L.load_system(h, s)
+        with pytest.raises(L.LibrpaError, match="invalid parallel routing"):
+            h.get_rpa_correlation_energy(L.Options(nfreq=16, tfgrids_type=L.Minimax, parallel_routing=7), 1)
+
+
 def test_no_gpu_means_loud_error_not_fallback(lib):
     if lib.librpa_gb300_device_count() > 0:
         pytest.skip("GPU present")

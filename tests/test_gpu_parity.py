@@ -89,14 +89,14 @@ def test_he_bcc_fhi_aims_periodic_vs_oracle():
     _, ec, perq = run_gpu(s, L.CHI0_FP64)
     assert abs(ec - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
     np.testing.assert_allclose(perq, o["per_q"], rtol=1e-9, atol=1e-12)
-    # default path: V(Gamma) of MgO is indefinite, so that q goes through the LU form
+    # default path: every V(q) of He is positive definite, so no q needs the LU form
     h2, ec2, perq2 = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
-    assert h2.stats()["ec_lu_fallback_q"] == 1
+    assert h2.stats()["ec_lu_fallback_q"] == 0
     assert abs(ec2 - o["ec"].real) <= MEV_PER_ATOM * len(s.nao)
     np.testing.assert_allclose(perq2, o["per_q"], rtol=0, atol=MEV_PER_ATOM * len(s.nao))
-    # the all-FP64 Cholesky form takes the same fallback and keeps FP64 accuracy
+    # the all-FP64 Cholesky form keeps FP64 accuracy
     h3, ec3, _ = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL_FP64)
-    assert h3.stats()["ec_lu_fallback_q"] == 1
+    assert h3.stats()["ec_lu_fallback_q"] == 0
     assert abs(ec3 - o["ec"].real) <= 1e-9 * abs(o["ec"].real)
 
 
@@ -229,3 +229,24 @@ def test_all_fp64_cholesky_ec_matches_lu(case):
     _, e_ch, q_ch = run_gpu(s, L.CHI0_FP64, ec_path=L.EC_CHOL_FP64)
     assert abs(e_ch - e_lu) <= 1e-10 * abs(e_lu), (e_ch, e_lu)
     np.testing.assert_allclose(q_ch.real, q_lu.real, rtol=1e-9, atol=1e-13)
+
+
+@pytest.mark.parametrize("case", ["fcc2_k222", "h2o"])
+def test_every_routing_gives_the_libri_ec(case):
+    """parallel_routing = RTAU, ATOMPAIR and AUTO return the LibRI routing's E_c through the C ABI:
+    this build runs one block schedule (the LibRI algebra) for every routing value.  On the 2-atom
+    fcc cell the reference's AUTO would pick RTAU (3 atom pairs < 8 cells; decide_auto_routing,
+    src/mpi/base_mpi.cpp:149-153); its RTAU and ATOMPAIR chi0 builders are not used as an oracle
+    because the reference marks them broken, so the LibRI E_c (itself checked against the oracle
+    above) is the target for all four."""
+    s = sy.fcc2_k222() if case == "fcc2_k222" else load_h2o()
+    out = {}
+    for routing in (L.LIBRI, L.RTAU, L.ATOMPAIR, L.AUTO):
+        h = L.Handler()
+        L.load_system(h, s)
+        h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+        o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=routing,
+                      minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
+        out[routing], _ = h.get_rpa_correlation_energy(o, L.n_ibz(s))
+    for routing in (L.RTAU, L.ATOMPAIR, L.AUTO):
+        assert out[routing] == out[L.LIBRI]

@@ -49,8 +49,10 @@ def test_mlp_gradients_match_cpu_oracle(lib):
     rng = np.random.default_rng(11)
     n = 300
     params = rng.normal(0.0, 0.25, mlp.NPARAM).astype(np.float32)
-    norm = np.array([5.0, 0.0, -2.0, -3.0, -3.0, 3.0, 1.0, 1.0, 2.0, 2.0, -5.0, 2.0, 0.5], np.float32)
-    x = (rng.normal(0.0, 1.0, (n, mlp.IN)) * norm[5:10] + norm[:5]).astype(np.float32)
+    norm = np.concatenate([[5.0, 0.0, -2.0, -3.0, -3.0, 3.2, 2.2, 0.5, 0.5], [3.0, 1.0, 1.0, 2.0, 2.0, 0.4, 0.3, 0.5, 0.5],
+                           [-5.0, 2.0, 0.5]]).astype(np.float32)
+    assert norm.size == mlp.NNORM
+    x = (rng.normal(0.0, 1.0, (n, mlp.IN)) * norm[mlp.IN:2 * mlp.IN] + norm[:mlp.IN]).astype(np.float32)
     y = rng.normal(-5.0, 2.0, n).astype(np.float32)
     grad = np.zeros(mlp.NPARAM, np.float32)
     loss = C.c_double()
@@ -107,3 +109,43 @@ def test_learned_screening_skips_blocks_at_the_plain_result(cluster, lib):
     assert st["screen_fallbacks"] == 0
     assert st["audit_max_dropped"] <= THR
     assert abs(ec_mlp - ec_plain) < 1e-10, (ec_mlp, ec_plain)
+
+
+def test_learned_screening_transfers_across_mixed_species_cells(lib, capsys):
+    """Mixed species (NAO/ABF 5/20, 13/60, 26/110, the shapes of the mixed-species workload): the
+    MLP trains on block norms logged by the plain runs of three other small cells, pooled with
+    librpa_gb300_add_screening_samples, and screens a 12-atom cell it has never seen.  Against
+    the plain threshold rule on that cell it contracts fewer blocks at an E_c within 0.1 meV/atom;
+    the species and block-dimension features tell the three species apart."""
+    spec = [(5, 20), (13, 60), (26, 110)]
+    xs, ys = [], []
+    for n, seed in [(6, 911), (7, 912), (8, 913)]:
+        s = sy.cluster_gamma(f"train{n}", n, spec, seed, decay_ang=1.5)
+        h = _handler(s, chi0_precision=1, screen_mode=L.SCREEN_THRESHOLD, screen_threshold=THR)
+        h.get_rpa_correlation_energy(_opts(s), 1)
+        m = lib.librpa_gb300_screening_samples(h.h)
+        x = np.zeros((m, mlp.IN), np.float32)
+        y = np.zeros(m, np.float32)
+        assert lib.librpa_gb300_get_screening_samples(h.h, _ptr(x), _ptr(y), m) == 0
+        assert set(np.unique(x[:, 7])) <= {0.0, 1.0, 2.0}  # species feature
+        xs.append(x)
+        ys.append(y)
+    x = np.concatenate(xs)
+    y = np.concatenate(ys)
+    t = sy.cluster_gamma("target12", 12, spec, 901, decay_ang=1.5)
+    hp = _handler(t, chi0_precision=1, screen_mode=L.SCREEN_THRESHOLD, screen_threshold=THR)
+    ec_plain, _ = hp.get_rpa_correlation_energy(_opts(t), 1)
+    h = _handler(t, chi0_precision=1, screen_mode=L.SCREEN_MLP, screen_threshold=THR, audit_fraction=0.02, seed=3)
+    assert lib.librpa_gb300_add_screening_samples(h.h, _ptr(x), _ptr(y), len(y)) == 0
+    assert lib.librpa_gb300_screening_samples(h.h) == len(y)
+    rmse = C.c_double()
+    assert lib.librpa_gb300_train_screening(h.h, 1500, 3e-3, C.byref(rmse)) == 0, lib.librpa_get_last_error(None).decode()
+    ec_mlp, _ = h.get_rpa_correlation_energy(_opts(t), 1)
+    st = h.stats()
+    skipped = 1.0 - st["blocks_computed"] / st["blocks_total"]
+    with capsys.disabled():
+        print(f"\nmixed-species transfer: train rmse {rmse.value:.3f} dec, skipped {skipped:.1%} of "
+              f"{st['blocks_total']} blocks, audited {st['blocks_audited']}, fallbacks {st['screen_fallbacks']}, "
+              f"dEc vs plain {abs(ec_mlp - ec_plain) / len(t.nao) * 27211.386:.2e} meV/atom")
+    assert skipped >= 0.10
+    assert abs(ec_mlp - ec_plain) <= MEV_PER_ATOM * len(t.nao)

@@ -8,7 +8,10 @@ from oracle.rpa_oracle import screen_blocks, _filter_g
 def _problem(seed=3, n=40):
     rng = np.random.default_rng(seed)
     params = rng.normal(0.0, 0.3, mlp.NPARAM)
-    norm = np.array([3.0, 0.0, -2.0, -3.0, -3.0, 2.0, 1.0, 1.0, 2.0, 2.0, -5.0, 2.0, 0.5])
+    # feature means, feature scales, target mean and scale, margin
+    norm = np.concatenate([[3.0, 0.0, -2.0, -3.0, -3.0, 3.2, 2.2, 0.5, 0.5], [2.0, 1.0, 1.0, 2.0, 2.0, 0.4, 0.3, 0.5, 0.5],
+                           [-5.0, 2.0, 0.5]])
+    assert norm.size == mlp.NNORM
     x = rng.normal(0.0, 1.0, (n, mlp.IN)) * norm[mlp.IN:2 * mlp.IN] + norm[:mlp.IN]
     y = rng.normal(-5.0, 2.0, n)
     return params, norm, x, y
@@ -33,8 +36,8 @@ def test_mlp_oracle_forward_consistent_with_loss():
     params, norm, x, y = _problem(5)
     pred = mlp.forward(params, norm, x)
     loss, _ = mlp.loss_grad(params, norm, x, y)
-    tn = (y - norm[10]) / norm[11]
-    pn = (pred - norm[10]) / norm[11]
+    tn = (y - norm[2 * mlp.IN]) / norm[2 * mlp.IN + 1]
+    pn = (pred - norm[2 * mlp.IN]) / norm[2 * mlp.IN + 1]
     assert np.isclose(loss, np.mean((pn - tn) ** 2), rtol=1e-12)
 
 

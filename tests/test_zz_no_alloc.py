@@ -84,16 +84,25 @@ def test_noalloc_gemm_rejects_oversized(lib):
 
 
 def test_noalloc_gemm_at_the_scratch_limit(lib):
-    """A request that needs exactly the 32 MiB of scratch runs (the error flag then sits in the
-    array's last 256 bytes) and gives the split GEMM's accuracy on two calls in a row; one row
-    more is rejected, and the entry point still works after the rejection.  With 2 pieces and
-    K = 64 (one 64-wide K block), the scratch need is 2 * (M + N) * 64 * 2 + 256 bytes."""
+    """The largest request that fits the 32 MiB scratch runs and gives the split GEMM's accuracy
+    on two calls in a row; one row more is rejected, and the entry point still works after the
+    rejection.  Each operand piece takes its size rounded up to 256 bytes, and the error flag
+    one more 256-byte slot, so the need is pieces * (a_piece + b_piece) + 256.  2^25 - 256 is
+    256 times a prime, so no request fills the array exactly: the largest (2 pieces, K = 64,
+    M + N = 131070 rows of 128 bytes) leaves its last 256 bytes unused and puts the error flag
+    in the 256 bytes before them."""
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda", torch.cuda.current_device())
     limit = 32 << 20
+
+    def need(m, n, k, pieces):
+        kpad = (k + 63) // 64 * 64
+        r = lambda x: (x + 255) // 256 * 256
+        return pieces * (r(m * kpad * 2) + r(n * kpad * 2)) + 256
+
     K, N = 64, 128
-    M = (limit - 256) // 256 - N  # 2 * (M + N) * 64 * 2 + 256 == limit
-    assert 2 * (M + N) * 64 * 2 + 256 == limit
+    M = 131070 - N
+    assert need(M, N, K, 2) == limit - 256 and need(M + 1, N, K, 2) > limit
     rng = np.random.default_rng(5)
     a = rng.uniform(-1, 1, (M, K))
     b = rng.uniform(-1, 1, (K, N))
