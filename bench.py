@@ -143,72 +143,93 @@ def _opts(L, s):
                      minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
 
 
-def cpu_sample(s, n_rows=1, n_cols=2):
-    """Oracle port on a bounded sample: one tau point, n_rows x n_cols atom blocks, one (q, w) E_c term.
+def _config(s):
+    """The workload descriptor both arms print (identical by construction)."""
+    n_sup = s.n_kpts * s.n_ao  # BvK cells = k points
+    c_bytes = 8.0 * sum(a * b for a, b in zip(s.nao, s.nabf)) * n_sup
+    l2 = (f"inputs larger than L2: RI matrix {c_bytes / 1e6:.0f} MB > 129 MB" if c_bytes > 129e6
+          else f"RI matrix {c_bytes / 1e6:.1f} MB fits L2")
+    return {"workload": s.name, "n_atoms": s.n_atoms, "n_kpts": s.n_kpts, "n_ao": s.n_ao,
+            "n_abf": int(sum(s.nabf)), "nfreq": s.nfreq, "l2": l2}
 
-    Returns (seconds per E_c extrapolated, description)."""
-    from oracle.rpa_oracle import (Options as OO, blocks_of, build_gf, cal_chi0s_dense, correlation_energy,
-                                   cs_tensors, grids_for, k_lists, r_grid)
+
+def _cpu_path(s):
+    """The host-core RPA path (oracle port, FP64, OpenMP + OpenBLAS) on the workload's inputs."""
+    from oracle.cpu_path import CpuPath
+    from oracle.rpa_oracle import Options as OO
     from librpa_gb300.synthetic import to_oracle_input
-    inp = to_oracle_input(s)
-    o = OO(nfreq=s.nfreq, minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
-    grid = grids_for(inp, o)
-    _, kfrac, ibz, ibzw = k_lists(inp)
-    rl = r_grid(inp.period)
-    C = cs_tensors(inp)
+    return CpuPath(to_oracle_input(s), OO(nfreq=s.nfreq, minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax))
+
+
+def cpu_sample(s):
+    """CPU baseline on a bounded sample: one complete tau slice (G, X GEMMs, chi0 of every upper
+    atom pair and cell, FT to every q) and the whole E_c stage (every (q, omega) LU), timed on
+    all host cores; scaled to one E_c by the tau count.  Returns (seconds per E_c, description)."""
+    cp = _cpu_path(s)
     t0 = time.perf_counter()
-    tau = grid["tau"][0]
-    Gp = blocks_of(build_gf(inp, 0, tau, kfrac, rl), inp.nao)
-    Gn = blocks_of(build_gf(inp, 0, -tau, kfrac, rl), inp.nao)
-    t_g = time.perf_counter() - t0
+    cp.tau_slice(0)
+    t_tau = time.perf_counter() - t0
     t0 = time.perf_counter()
-    n_cols = min(n_cols, inp.n_atoms)
-    tm = {}
-    cal_chi0s_dense(C, Gp, Gn, inp.nao, inp.nabf, inp.period, rows=list(range(n_rows)),
-                    cols=list(range(n_cols)), timings=tm)
-    n_pairs = inp.n_atoms * (inp.n_atoms + 1) / 2
-    t_chi = tm["x_per_atom"] * inp.n_atoms + tm["blocks_per_pair"] * n_pairs
-    # one E_c term: a single (q, w) with a dense chi0 of the right size
-    N = int(sum(inp.nabf))
-    rng = np.random.default_rng(0)
-    dt = float if inp.n_kpts == 1 else complex
-    X = rng.standard_normal((N, N)).astype(dt) * 1e-3
-    V = rng.standard_normal((N, N)).astype(dt)
-    import scipy.linalg
-    t0 = time.perf_counter()
-    P = V @ X
-    scipy.linalg.lu_factor(np.eye(N) - P, check_finite=False)
+    cp.correlation_energy()
     t_ec = time.perf_counter() - t0
-    nt = len(grid["tau"])
-    # upper pairs only are needed: n_at (n_at + 1) / 2 blocks per cell
-    scale_blocks = n_pairs / (n_rows * n_cols)
-    total = nt * (t_g + t_chi) + len(ibz) * nt * t_ec
-    desc = (f"oracle port (numpy/OpenBLAS) on {os.cpu_count()} host threads: G build + chi0 for 1 of {nt} tau "
-            f"and {n_rows}x{n_cols} of the {inp.n_atoms * (inp.n_atoms + 1) // 2} upper atom-pair blocks "
-            f"(all cells) and their X GEMMs, one of {len(ibz) * nt} (q,w) LU terms; scaled x{nt} (tau), "
-            f"x{scale_blocks:.0f} (blocks), x{inp.n_atoms}/{len(set(range(n_rows)) | set(range(n_cols)))} (X rows), "
-            f"x{len(ibz) * nt} (E_c)")
-    return total, desc
+    nt = len(cp.grid["tau"])
+    desc = (f"oracle port (FP64; OpenMP chi0 and LU kernels, OpenBLAS GEMMs) on {os.cpu_count()} host threads: "
+            f"tau slice 0 of {nt} measured {t_tau:.2f} s, the whole E_c stage ({cp.nq} q x "
+            f"{len(cp.grid['omega'])} omega LU terms) measured {t_ec:.2f} s; value = {nt} x tau slice + E_c")
+    return nt * t_tau + t_ec, desc
 
 
 def run_reference(args, s, ws, rank, dist):
+    """The reference CPU path (oracle port, the reference itself cannot be built here) on all host
+    cores.  One E_c is n_tau + 1 stages: the tau slices, then the E_c stage.  Step k runs stage
+    k mod (n_tau + 1) of successive passes (a new pass starts from zero at stage 0); the first
+    `warmup` steps are not timed.  value = the sum over the stages of each stage's mean timed
+    duration: the measured wall time of one whole E_c when every stage was timed at least once
+    (steps >= n_tau + 1), which value_complete records."""
     if rank != 0:
         return
-    for _ in range(args.warmup):
-        pass  # each sample is already a bounded, self-contained measurement
-    vals = []
-    desc = ""
-    for _ in range(args.steps):
-        v, desc = cpu_sample(s)
-        vals.append(v)
-    v = statistics.median(vals)
-    line = {"impl": "reference", "metric": "rpa_ec_wall_time", "value": v, "unit": "s", "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": s.name, "n_atoms": s.n_atoms, "n_kpts": s.n_kpts, "nfreq": s.nfreq,
-                       "note": "reference CPU path = oracle port (the reference needs MPI/ScaLAPACK/Fortran, absent)"},
-            "cpu_baseline": {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port", "sample": desc},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    cp = _cpu_path(s)
+    nt = len(cp.grid["tau"])
+    nstage = nt + 1
+    times = {k: [] for k in range(nstage)}
+    ec = None
+    for k in range(args.warmup + args.steps):
+        st = k % nstage
+        if st == 0:
+            cp.chi0q_tau[:] = 0.0
+        t0 = time.perf_counter()
+        if st < nt:
+            cp.tau_slice(st)
+        else:
+            ec, _ = cp.correlation_energy()
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times[st].append(dt)
+    timed = {k: statistics.mean(v) for k, v in times.items() if v}
+    complete = len(timed) == nstage
+    tau_mean = statistics.mean([v for k, v in timed.items() if k < nt]) if any(k < nt for k in timed) else None
+    value = sum(timed.values())
+    missing = [k for k in range(nstage) if k not in timed]
+    est = {}
+    if not complete:
+        # not every stage ran in the timed region: the value is incomplete; an estimate that
+        # fills the missing tau slices with the mean timed slice goes in its own field
+        est = {"value_estimated": value + sum(tau_mean or 0.0 for k in missing if k < nt),
+               "estimated_stages": missing}
+    total_steps = args.steps
+    line = {"impl": "reference", "metric": "rpa_ec_wall_time", "value": value, "unit": "s", "n_gpus": ws,
+            "steps": total_steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(sum(v) for v in times.values()) / max(total_steps, 1),
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "precision": "fp64", "parallelism": f"host cores x{os.cpu_count()}",
+            "config": _config(s), "value_complete": complete, **est,
+            "stage_s": {("tau_%d" % k if k < nt else "ec"): round(v, 4) for k, v in timed.items()},
+            "ec": None if ec is None else ec.real,
+            "cpu_baseline": {"value": value, "unit": "s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"every stage of the E_c path: {nt} tau slices (G, X GEMMs, chi0 of all "
+                                       f"upper atom pairs and cells, FT) and the E_c stage; step k = stage "
+                                       f"k mod {nstage}; oracle port (FP64, OpenMP chi0/LU kernels, OpenBLAS)"},
+            "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -242,6 +263,7 @@ def run_gb300(args, s, ws, rank, local, dist):
         torch.cuda.synchronize()
         e0.record()
         for _ in range(args.steps):
+            lib.librpa_gb300_clear_grid_cache()  # every step fits its minimax grids, as the reference does
             ec, perq = h.get_rpa_correlation_energy(opts, nq)
             st = h.stats()
             launches += st["n_launches"]
@@ -260,6 +282,7 @@ def run_gb300(args, s, ws, rank, local, dist):
     _barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        lib.librpa_gb300_clear_grid_cache()
         ec2, _ = h.get_rpa_correlation_energy(opts, nq)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -303,9 +326,8 @@ def run_gb300(args, s, ws, rank, local, dist):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": {"bf16x3": "bf16x3/f32acc+f64", "fp32": "f32+f64", "fp64": "f64"}[args.precision],
         "data": "synthetic",
-        "config": {"workload": s.name, "n_atoms": s.n_atoms, "n_kpts": s.n_kpts, "n_ao": s.n_ao,
-                   "n_abf": int(sum(s.nabf)), "nfreq": s.nfreq, "precision": args.precision,
-                   "parallelism": f"replicas x{ws}", "l2": "inputs larger than L2 (RI matrix > 129 MB)"},
+        "precision": args.precision, "parallelism": f"replicas x{ws}",
+        "config": _config(s),
         "ec": ec, "chi0_tflops": ach, "chi0_flops_per_step": chi0_flops / args.steps,
         "stage_s": {k: st2[k] for k in ("t_grids", "t_upload", "t_gf", "t_chi0", "t_ftct", "t_ec", "t_total")},
         "fp64_gpu": fp64,
@@ -316,7 +338,77 @@ def run_gb300(args, s, ws, rank, local, dist):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
     }
+    del h
+    if ws == 1 and args.north_star:
+        line["north_star_256"] = run_north_star(L, lib, torch, local, args)
     print(json.dumps(line), flush=True)
+
+
+def run_north_star(L, lib, torch, local, args):
+    """The 256-atom Gamma cell (13 NAO / 40 ABF per atom, C decay 1.5 A, 16 minimax points): the
+    default path over 3 timed steps (grids fitted every step), the plain FP64 GPU path once (the
+    denominator of the wall-time target), and the block-screened paths: the plain threshold
+    rule at 1e-6 and the learned screening (trained on the plain run's logged blocks, 2% audit)."""
+    from librpa_gb300 import synthetic as sy
+    s = sy.sc256_g()
+    opts = _opts(L, s)
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=1, device=local, reuse_device_inputs=1))
+    h.get_rpa_correlation_energy(opts, 1)
+    torch.cuda.synchronize()
+    steps = 3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        lib.librpa_gb300_clear_grid_cache()
+        ec, _ = h.get_rpa_correlation_energy(opts, 1)
+    e1.record()
+    torch.cuda.synchronize()
+    t_fast = e0.elapsed_time(e1) / steps / 1e3
+    st = h.stats()
+    out = {"workload": s.name, "n_atoms": s.n_atoms, "n_abf": int(sum(s.nabf)), "steps": steps,
+           "seconds": t_fast, "ec": ec, "stage_s": {k: st[k] for k in ("t_gf", "t_chi0", "t_ftct", "t_ec")},
+           "chi0_tflops": st["chi0_flops"] / (st["dt_chi0_kernel_ms"] / 1e3) / 1e12 if st["dt_chi0_kernel_ms"] else None}
+    if args.fp64_check != "off":
+        h.set_gb300_options(L.gb300_options(chi0_precision=0, ec_path=L.EC_CHOL_FP64, device=local,
+                                            reuse_device_inputs=1))
+        lib.librpa_gb300_clear_grid_cache()
+        t0 = time.perf_counter()
+        e64, _ = h.get_rpa_correlation_energy(opts, 1)
+        t64 = time.perf_counter() - t0
+        out["fp64_gpu"] = {"seconds": t64, "ec": e64, "speedup": t64 / t_fast,
+                           "dEc_meV_per_atom": abs(ec - e64) / s.n_atoms / (MEV_PER_ATOM_HA * 10)}
+    # block screening: plain threshold rule (logs the training blocks), then the learned predictor
+    thr = 1e-6
+    h.set_gb300_options(L.gb300_options(chi0_precision=1, device=local, reuse_device_inputs=1,
+                                        screen_mode=L.SCREEN_THRESHOLD, screen_threshold=thr))
+    t0 = time.perf_counter()
+    e_plain, _ = h.get_rpa_correlation_energy(opts, 1)
+    t_plain = time.perf_counter() - t0
+    import ctypes
+    rmse = ctypes.c_double()
+    t0 = time.perf_counter()
+    rc = lib.librpa_gb300_train_screening(h.h, 800, 3e-3, ctypes.byref(rmse))
+    t_train = time.perf_counter() - t0
+    if rc == 0:
+        h.set_gb300_options(L.gb300_options(chi0_precision=1, device=local, reuse_device_inputs=1,
+                                            screen_mode=L.SCREEN_MLP, screen_threshold=thr, audit_fraction=0.02,
+                                            seed=7))
+        lib.librpa_gb300_clear_grid_cache()
+        t0 = time.perf_counter()
+        e_mlp, _ = h.get_rpa_correlation_energy(opts, 1)
+        t_mlp = time.perf_counter() - t0
+        sm = h.stats()
+        out["screening"] = {
+            "threshold": thr, "plain_threshold_s": t_plain, "mlp_s": t_mlp, "train_s": t_train,
+            "train_rmse_log10": rmse.value, "blocks_total": sm["blocks_total"],
+            "blocks_computed": sm["blocks_computed"], "blocks_audited": sm["blocks_audited"],
+            "fallbacks": sm["screen_fallbacks"],
+            "dEc_vs_plain_meV_per_atom": abs(e_mlp - e_plain) / s.n_atoms / (MEV_PER_ATOM_HA * 10),
+            "dEc_vs_unscreened_meV_per_atom": abs(e_mlp - ec) / s.n_atoms / (MEV_PER_ATOM_HA * 10)}
+    del h
+    return out
 
 
 def main():
@@ -330,6 +422,8 @@ def main():
     ap.add_argument("--fp64-check", default="auto", choices=["auto", "on", "off"])
     ap.add_argument("--fp64-budget-s", type=float, default=90.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-north-star", dest="north_star", action="store_false",
+                    help="skip the 256-atom sub-record (default path, FP64 denominator, screening)")
     args = ap.parse_args()
     ws, rank, local, dist = _dist()
     from librpa_gb300 import synthetic as sy

@@ -116,6 +116,12 @@ int librpa_gb300_minimax_grid(int n, double emin, double emax, double regulariza
                               double *cos_t2f, double *cos_f2t, double *sin_t2f,
                               double *duality_error);
 
+/* No counterpart in the reference: forget the minimax grids this process has fitted.  E_c calls
+ * keep the grids of the last few (n, e_min, e_max, regularization) windows and reuse them;
+ * after this call the next E_c call fits its grids again, as every call of the reference does
+ * (TFGrids::generate_minimax, src/core/timefreq.cpp:193-236).  Host only. */
+void librpa_gb300_clear_grid_cache(void);
+
 /* G0W0 quasi-particle equation for n_states states (host only, no GPU needed): the Thiele-Pade
  * continuation of each state's Sigma_c(i omega_k), k < n_freq (sigc_re/im[state * n_freq + k],
  * omega_k > 0 the imaginary frequencies), with n_params parameters (< 0: all points), then the

@@ -137,6 +137,7 @@ EXPORTS = [
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
+    "librpa_gb300_clear_grid_cache",
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
@@ -198,6 +199,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_screening_samples": (C.c_longlong, [vp]),
         "librpa_gb300_get_screening_samples": (i, [vp, vp, vp, C.c_longlong]),
         "librpa_gb300_add_screening_samples": (i, [vp, vp, vp, C.c_longlong]),
+        "librpa_gb300_clear_grid_cache": (None, []),
         "librpa_gb300_get_screening_model": (i, [vp, vp, vp]),
         "librpa_gb300_set_screening_model": (i, [vp, vp, vp]),
         "librpa_gb300_clear_screening": (None, [vp]),

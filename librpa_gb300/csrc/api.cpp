@@ -1076,6 +1076,11 @@ int librpa_gb300_add_screening_samples(LibrpaHandler *h, const float *x, const f
     return rc;
 }
 
+void librpa_gb300_clear_grid_cache(void)
+{
+    guarded(nullptr, [&] { gb::clear_grid_cache(); });
+}
+
 int librpa_gb300_get_screening_model(LibrpaHandler *h, float *params, float *norm)
 {
     int rc = 1;

@@ -256,12 +256,23 @@ static TimeFreqGrids minimax_grids_uncached(int n, double emin, double emax, dou
 
 // The grids are a pure function of (n, e_min, e_max, regularisation): repeated E_c calls on the
 // same system reuse the last few results instead of refitting (the fit costs tens of ms).
+namespace {
+using GridKey = std::tuple<int, double, double, double>;
+std::mutex g_grid_mu;
+std::map<GridKey, TimeFreqGrids> g_grid_cache;
+} // namespace
+
+void clear_grid_cache()
+{
+    std::lock_guard<std::mutex> lk(g_grid_mu);
+    g_grid_cache.clear();
+}
+
 TimeFreqGrids minimax_grids(int n, double emin, double emax, double reg)
 {
-    using Key = std::tuple<int, double, double, double>;
-    static std::mutex mu;
-    static std::map<Key, TimeFreqGrids> cache;
-    const Key key{n, emin, emax, reg};
+    std::mutex &mu = g_grid_mu;
+    std::map<GridKey, TimeFreqGrids> &cache = g_grid_cache;
+    const GridKey key{n, emin, emax, reg};
     {
         std::lock_guard<std::mutex> lk(mu);
         auto it = cache.find(key);

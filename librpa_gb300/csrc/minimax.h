@@ -29,6 +29,9 @@ struct TimeFreqGrids
 std::string minimax_table_path();
 
 // Throws gb::Error for unsupported n (GreenX supports 6, 8, ..., 34) or bad energies.
+// Results are kept per (n, e_min, e_max, regularization) for later calls in the process.
 TimeFreqGrids minimax_grids(int n, double emin, double emax, double regularization);
+// Forget the kept grids: the next call fits them again.
+void clear_grid_cache();
 
 } // namespace gb
