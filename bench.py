@@ -329,6 +329,7 @@ def run_gb300(args, s, ws, rank, local, dist):
         "precision": args.precision, "parallelism": f"replicas x{ws}",
         "config": _config(s),
         "ec": ec, "chi0_tflops": ach, "chi0_flops_per_step": chi0_flops / args.steps,
+        "t1_choice": {"narrow_producers": st["t1_narrow"], "kparts": st["t1_kparts"]},
         "stage_s": {k: st2[k] for k in ("t_grids", "t_upload", "t_gf", "t_chi0", "t_ftct", "t_ec", "t_total")},
         "fp64_gpu": fp64,
         "e2e": {"value": e2e_ms / 1e3, "unit": "s", "h2d_bytes_per_step": st2["h2d_bytes"],

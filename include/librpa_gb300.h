@@ -93,6 +93,9 @@ typedef struct
     long long ec_lu_fallback_q; /* IBZ q points whose V(q) had no Cholesky factor (indefinite, as
                                    the Gamma-point bare Coulomb matrix of a crystal can be) and
                                    whose E_c term the Cholesky path took by the LU form instead */
+    int t1_narrow;              /* tensor-core chi0 contraction: 1 = 16 producer warps of 2 columns,
+                                   0 = 8 of 4 columns (the tuner's choice for this shape) */
+    int t1_kparts;              /* K parts per 128-row tile of that contraction (tuner's choice) */
 } LibrpaGB300Stats;
 
 /* Set defaults. */

@@ -109,7 +109,7 @@ class GB300Stats(C.Structure):
         ("blocks_total", C.c_longlong), ("blocks_computed", C.c_longlong), ("blocks_audited", C.c_longlong),
         ("audit_max_dropped", C.c_double), ("dt_chi0_kernel_ms", C.c_double), ("n_chi0_kernel", C.c_longlong),
         ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double), ("screen_fallbacks", C.c_longlong),
-        ("ec_lu_fallback_q", C.c_longlong),
+        ("ec_lu_fallback_q", C.c_longlong), ("t1_narrow", C.c_int), ("t1_kparts", C.c_int),
     ]
 
     def as_dict(self):

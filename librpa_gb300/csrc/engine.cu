@@ -578,6 +578,13 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         GB_CUDA(cudaStreamSynchronize(st));
         GB_REQUIRE(herr == 0, "tensor-core G build reported wait timeout code " + std::to_string(herr));
     }
+    if (TcChi0 *tp = fast ? fast->tensor_path() : nullptr)
+    {
+        int nar = 0, kp = 0;
+        tp->launch_choice(nar, kp);
+        S.t1_narrow = nar;
+        S.t1_kparts = kp;
+    }
     S.t_gf = t_gf * 1e-3;
     S.t_chi0 = t_chi * 1e-3;
     S.t_ftct = t_ft * 1e-3;

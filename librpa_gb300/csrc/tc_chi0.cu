@@ -17,6 +17,9 @@
 //  3. T2 (small, CUDA cores): D += sum_{i,j} X_b^I[mu i; (cJ,J) j] X_a^J[nu j; (-cJ,I) i].
 // Every wait is bounded (tc_common.cuh) and failures surface through a device error flag.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
 #include <cstdlib>
 #include <vector>
 
@@ -38,10 +41,19 @@ constexpr int JG = 8;            // j per pipeline stage (JG * CW = 64 = K per s
 constexpr int T1_STAGES = 2;     // A (E tile) ring: producers fill one while the MMAs read the other
 constexpr int T1_MAXB = 8;       // C^J (B tile) ring: up to 8 stages of TMA look-ahead
 constexpr int T1_NMAX = 128;     // max N tile (ABFs of one atom, padded to 16)
-constexpr int PRODUCERS = 256;   // warps 0-7: E tiles (2 threads per row, 4 columns each)
-constexpr int DRAIN_WARP0 = 8;   // warps 8-11: accumulator drain + epilogue; lane 0 of warp 8
-                                 // also issues the C^J TMA copies and the MMAs
-constexpr int T1_THREADS = 12 * 32;  // 3 warps per scheduler: up to 168 registers a thread
+// Two producer layouts.  Wide (P2 = false): warps 0-7 build E, 2 threads per row with 4
+// columns each; 12 warps, up to 168 registers a thread.  Narrow (P2 = true, the streamed
+// 4-column-aligned case): warps 0-15 build E, 4 threads per row with 2 columns each, so twice
+// the warps hide the X gather latency; 20 warps, up to 102 registers a thread.  In both, the
+// 4 warps after the producers drain the accumulators, and lane 0 of the first of them also
+// issues the C^J TMA copies and the MMAs.
+template <bool P2>
+struct T1Layout
+{
+    static constexpr int producers = P2 ? 512 : 256;
+    static constexpr int drain_warp0 = producers / 32;
+    static constexpr int threads = producers + 128;
+};
 constexpr int A_TILE = T1_BM * 64 * 2;       // bytes per A piece
 constexpr int T1_MAXA = 32;                  // max NAOs per atom (G buffer row stride)
 constexpr int T1_SMEM_MAX = 227 * 1024;
@@ -69,7 +81,8 @@ struct T1Work
 };
 
 constexpr int T1_MAXSPEC = 8;    // distinct (NAO, ABF) species with their own B maps
-constexpr int T1_KPARTS = 4;     // K parts per tile (each part a CTA, added into chi0(R) atomically)
+constexpr int T1_KPARTS = 4;     // default K parts per tile (each part a CTA, added into chi0(R) atomically)
+constexpr int T1_KPARTS_MAX = 8; // largest K-part count the tuner tries
 
 // C^J B-operand maps, one rank-3 map per (species, piece): dims {ktot, nabf, atoms of the species}.
 struct T1Maps
@@ -136,10 +149,12 @@ __device__ __forceinline__ void split3_pair(float2 e, uint32_t &h, uint32_t &m, 
 // hi x [Ch;Cm;Cl] (N = 3 NT), mid x [Ch;Cm] (N = 2 NT) and lo x Ch (N = NT), landing in three
 // accumulator blocks of orders 1, 2^-8 and 2^-16; with NTC = 128 the six products are issued
 // one by one into a hi*hi block and a cross-term block.
-template <int RA, int NTC, bool SV>
-__global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__ T1Args a,
-                                                        const __grid_constant__ T1Maps maps)
+template <int RA, int NTC, bool SV, bool P2>
+__global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid_constant__ T1Args a,
+                                                                   const __grid_constant__ T1Maps maps)
 {
+    constexpr int PRODUCERS = T1Layout<P2>::producers;
+    constexpr int DRAIN_WARP0 = T1Layout<P2>::drain_warp0;
     constexpr bool STACKN = NTC == 64;
     constexpr int NBLK = STACKN ? 3 : 2;           // accumulator blocks per buffer
     constexpr uint32_t TMEM_COLS = 512;
@@ -150,6 +165,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     // register ring, one chunk (both stages, up to 16 j) per pass; otherwise the gathers go one
     // column at a time below
     constexpr bool STREAM = SV && RA <= 16 && JG == 8;
+    static_assert(!P2 || STREAM, "the narrow producer layout streams 4-column-aligned X");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int stage_bytes = NS * A_TILE;      // A ring stage
@@ -224,8 +240,8 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
     {
         // ---------------- producers: E tiles
         const int t = threadIdx.x;
-        const int r = t >> 1;           // row in tile
-        const int cq = t & 1;           // 4-column group inside the 8-column chunk
+        const int r = P2 ? t >> 2 : t >> 1;  // row in tile
+        const int cq = P2 ? t & 3 : t & 1;   // 2- (narrow) or 4-column (wide) group inside the 8-column chunk
         int grp = 0, mu = 0;
         const bool valid = row_of(r, grp, mu);
         const int slot = valid ? grp - w.g0 : 0;
@@ -346,7 +362,100 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
                 *reinterpret_cast<uint2 *>(stg + 2 * A_TILE + off) = make_uint2(l01, l23);
             }
         };
-        if constexpr (STREAM)
+        if constexpr (P2)
+        {
+            // Narrow layout: 2 columns a thread (float2 gathers, one packed FMA per (i, j)).  The
+            // chunk's 2 RA rows (pass, i) are read in the flat order q = pass RA + i, each XD steps
+            // before its use from an XD-entry register ring; the last XD reads of a chunk fetch the
+            // first rows of the next one.  The order is padded to QP, a multiple of XD, so that
+            // row q of every chunk sits in ring slot q mod XD.
+            constexpr int XD = 8;
+            constexpr int QP = (2 * RA + XD - 1) / XD * XD;
+            static_assert(XD <= 2 * RA, "ring deeper than a chunk");
+            const float2 zero2 = make_float2(0.f, 0.f);
+            auto chunk_base = [&](int kc, const float *&b0, const float *&b1) -> bool {
+                const long long col0 = static_cast<long long>(kc) * CW + cq * 2;
+                if (kc >= kc1 || col0 >= nsup || !valid) return false;
+                const int cp = static_cast<int>(col0 / nao), ao = static_cast<int>(col0 % nao);
+                const long long src = static_cast<long long>(a.cadd[cp * nc + cJ]) * nao + ao;
+                b0 = Xp[0] + xrow * nsup + src;
+                b1 = Xp[1] + xrow * nsup + src;
+                return true;
+            };
+            auto ld = [&](const float *b0, const float *b1, int q, bool live) -> float2 {
+                const int i = q % RA;
+                const float *b = q < RA ? b0 : b1;
+                return (live && q < 2 * RA && i < aI) ? __ldg(reinterpret_cast<const float2 *>(b + i * nsup)) : zero2;
+            };
+            const float *c0 = Xp[0], *c1 = Xp[0], *n0 = Xp[0], *n1 = Xp[0];
+            bool clive = chunk_base(kc0, c0, c1);
+            bool nlive = chunk_base(kc0 + 1, n0, n1);
+            float2 xb[XD];
+#pragma unroll
+            for (int q = 0; q < XD; ++q) xb[q] = ld(c0, c1, q, clive);
+            for (int kc = kc0; kc < kc1 && ok; ++kc)
+            {
+                float2 e[4][JH];  // [group of 4 j][jl]: j 0..15, the thread's 2 columns
+#pragma unroll
+                for (int jh = 0; jh < 4; ++jh)
+#pragma unroll
+                    for (int jl = 0; jl < JH; ++jl) e[jh][jl] = zero2;
+#pragma unroll
+                for (int q = 0; q < QP; ++q)
+                {
+                    const int pass = q / RA, i = q % RA;
+                    const float2 x = xb[q % XD];
+                    xb[q % XD] = q + XD < QP ? ld(c0, c1, q + XD, clive) : ld(n0, n1, q + XD - QP, nlive);
+                    if (q >= 2 * RA) continue;  // padding of the read order
+#pragma unroll
+                    for (int jh = 0; jh < 4; ++jh)
+                    {
+                        const float4 gg = gp[pass][(i * gst + jh * JH) / 4];
+                        const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq)
+                        {
+                            if (RA == 13 && 4 * jh + qq >= 13) continue;
+                            e[jh][qq] = __ffma2_rn(make_float2(gv[qq], gv[qq]), x, e[jh][qq]);
+                        }
+                    }
+                }
+                c0 = n0;
+                c1 = n1;
+                clive = nlive;
+                nlive = chunk_base(kc + 2, n0, n1);
+#pragma unroll
+                for (int jg = 0; jg < 2; ++jg)
+                {
+                    if (jg >= njg || !ok) break;
+                    const int s = st_count % T1_STAGES, rr = st_count / T1_STAGES;
+                    ++st_count;
+                    unsigned char *stg = smem + s * stage_bytes;
+                    if (!__all_sync(0xffffffffu, mbar_wait(&empty[s], (rr & 1) ^ 1)))
+                    {
+                        if (lane == 0) atomicExch(a.err, 201);
+                        ok = false;
+                        break;
+                    }
+#pragma unroll
+                    for (int jh = 0; jh < 2; ++jh)
+#pragma unroll
+                        for (int jl = 0; jl < JH; ++jl)
+                        {
+                            uint32_t h, m, l;
+                            split3_pair(e[2 * jg + jh][jl], h, m, l);
+                            const uint32_t off = sw128_offset(r, (jh * JH + jl) * CW + cq * 2);
+                            *reinterpret_cast<uint32_t *>(stg + off) = h;
+                            *reinterpret_cast<uint32_t *>(stg + A_TILE + off) = m;
+                            *reinterpret_cast<uint32_t *>(stg + 2 * A_TILE + off) = l;
+                        }
+                    fence_proxy_async_smem();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&full[s]);
+                }
+            }
+        }
+        else if constexpr (STREAM)
         {
             // One chunk (both stages, all 16 j) per pass over its 2 RA rows (pass, i) of X.
             // Row (pass, i) of chunk kc sits in xb[i] from RA steps before its use: reading
@@ -491,7 +600,7 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
         }
     else
     {
-        // ---------------- warps 8-11: per-stage accumulator blocks -> FP32 registers -> chi0R.
+        // ---------------- drain warps: per-stage accumulator blocks -> FP32 registers -> chi0R.
         // Lane 0 of warp 8 issues, per stage st, the MMAs of st and then the C^J TMA copy of
         // st + nbs - 1 (nbs - 1 stages of look-ahead hide the HBM latency of the B tiles),
         // before its warp drains st - 1: the tensor pipe always holds the next stage.
@@ -616,7 +725,21 @@ __global__ void __launch_bounds__(T1_THREADS, 1) k_t1_tc(const __grid_constant__
             {
                 if (c0 < NT)
                 {
-                    if constexpr (STACKN)
+                    if constexpr (STACKN && P2)
+                    {
+                        // narrow layout (96 registers a thread): one block of 16 loaded values live
+                        // at a time, added into the running sums from the leading block down
+#pragma unroll
+                        for (int b = 0; b < 3; ++b)
+                        {
+                            uint32_t v[16];
+                            tmem_ld16_nowait(tb + b * NT + c0, v);
+                            tmem_wait_ld();
+#pragma unroll
+                            for (int i = 0; i < 16; ++i) acc[c0 + i] += __uint_as_float(v[i]);
+                        }
+                    }
+                    else if constexpr (STACKN)
                     {
                         uint32_t v0[16], v1[16], v2[16];
                         tmem_ld16_nowait(tb + c0, v0);
@@ -838,17 +961,44 @@ struct TcChi0::Impl
     T1Maps maps{};
     DevBuf<int> spec, spec_idx;
     int b_tile = 0, maxcj = 0, smem = 0, ra = 16, ntc = 64, nbs = 2, gj = JG;
+    // Launch choices of the contraction: producer layout and K parts per tile.  The tuner
+    // times the candidates on the first unscreened contraction of a shape and keeps the
+    // fastest for every later call on that shape (tuned_choice).
+    bool narrow_ok = false, narrow = false;
+    int kparts = T1_KPARTS;
+    bool kparts_forced = false, tuned = false;
+    std::string shape_key;
+    void autotune(const double *G, double *chi0R, cudaStream_t st);
+    void launch_t1(const T1Args &a, cudaStream_t st);
 };
 
 namespace {
-using T1Fn = void (*)(T1Args, T1Maps);
-T1Fn t1_kernel(int ra, int ntc, bool sv)
+struct T1Choice
 {
-    if (ra == 13 && sv) return ntc == 64 ? k_t1_tc<13, 64, true> : k_t1_tc<13, 128, true>;
-    if (ra == 13) return ntc == 64 ? k_t1_tc<13, 64, false> : k_t1_tc<13, 128, false>;
-    if (ra == 16 && sv) return ntc == 64 ? k_t1_tc<16, 64, true> : k_t1_tc<16, 128, true>;
-    if (ra == 16) return ntc == 64 ? k_t1_tc<16, 64, false> : k_t1_tc<16, 128, false>;
-    return ntc == 64 ? k_t1_tc<32, 64, false> : k_t1_tc<32, 128, false>;
+    bool narrow;
+    int kparts;
+    double ms;
+};
+std::mutex g_tune_mu;
+std::map<std::string, T1Choice> g_tuned;  // shape key -> choice (process-wide)
+} // namespace
+
+namespace {
+using T1Fn = void (*)(T1Args, T1Maps);
+// The narrow producer layout serves the streamed (4-column-aligned, RA <= 16) cases with up
+// to 64 ABFs on atom J (its 96 registers a thread hold 64 accumulator columns, not 128).
+bool t1_narrow_ok(int ra, int ntc, bool sv) { return ra <= 16 && sv && ntc == 64; }
+
+int t1_threads(bool narrow) { return narrow ? T1Layout<true>::threads : T1Layout<false>::threads; }
+
+T1Fn t1_kernel(int ra, int ntc, bool sv, bool narrow)
+{
+    if (narrow) return ra == 13 ? k_t1_tc<13, 64, true, true> : k_t1_tc<16, 64, true, true>;
+    if (ra == 13 && sv) return ntc == 64 ? k_t1_tc<13, 64, true, false> : k_t1_tc<13, 128, true, false>;
+    if (ra == 13) return ntc == 64 ? k_t1_tc<13, 64, false, false> : k_t1_tc<13, 128, false, false>;
+    if (ra == 16 && sv) return ntc == 64 ? k_t1_tc<16, 64, true, false> : k_t1_tc<16, 128, true, false>;
+    if (ra == 16) return ntc == 64 ? k_t1_tc<16, 64, false, false> : k_t1_tc<16, 128, false, false>;
+    return ntc == 64 ? k_t1_tc<32, 64, false, false> : k_t1_tc<32, 128, false, false>;
 }
 } // namespace
 
@@ -949,7 +1099,7 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
         GB_CUDA(cudaGetDevice(&dev));
         GB_CUDA(cudaDeviceGetAttribute(&m.n_sm, cudaDevAttrMultiProcessorCount, dev));
     }
-    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1) * T1_KPARTS +
+    m.work.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c * ((g.max_nabf + T1_BM - 1) / T1_BM + 1) * T1_KPARTS_MAX +
                  8 * static_cast<size_t>(m.n_sm));
     m.groups.alloc(static_cast<size_t>(pr.n_pairs) * g.n_c);
     int ntmax = 16, minb = 1 << 30;
@@ -974,10 +1124,114 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     const int fixed = base + m.maxcj * slot_bytes;
     m.nbs = std::min(T1_MAXB, (T1_SMEM_MAX - fixed) / (NS * m.b_tile));
     m.smem = fixed + m.nbs * NS * m.b_tile;
-    m.build_work(nullptr, st);
-    GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc, g.n_ao % 4 == 0), cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const bool sv = g.n_ao % 4 == 0;
+    m.narrow_ok = t1_narrow_ok(m.ra, m.ntc, sv);
+    m.narrow = m.narrow_ok;
+    GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc, sv, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  m.smem));
+    if (m.narrow_ok)
+        GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc, sv, true), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     m.smem));
+    // the shape the tuner's choice is kept for: per-atom sizes, cells, pairs, SM count
+    {
+        std::string key = std::to_string(g.n_c) + ":" + std::to_string(g.n_ao) + ":" + std::to_string(pr.n_pairs) +
+                          ":" + std::to_string(m.n_sm) + ":";
+        for (int J = 0; J < g.n_at; ++J) key += std::to_string(nao[J]) + "/" + std::to_string(nabf[J]) + ",";
+        m.shape_key = key;
+        // LIBRPA_GB300_T1_LAUNCH = "narrow:<kparts>" or "wide:<kparts>" fixes the choice (no tuning)
+        if (const char *fx = std::getenv("LIBRPA_GB300_T1_LAUNCH"))
+        {
+            const std::string v(fx);
+            const size_t c = v.find(':');
+            GB_REQUIRE(c != std::string::npos, "LIBRPA_GB300_T1_LAUNCH must read narrow:<kparts> or wide:<kparts>");
+            const std::string lay = v.substr(0, c);
+            const int kp = std::atoi(v.c_str() + c + 1);
+            GB_REQUIRE((lay == "narrow" || lay == "wide") && kp >= 1 && kp <= T1_KPARTS_MAX,
+                       "LIBRPA_GB300_T1_LAUNCH must read narrow:<kparts> or wide:<kparts>, kparts 1-8");
+            m.narrow = lay == "narrow" && m.narrow_ok;
+            m.kparts = kp;
+            m.kparts_forced = true;
+            m.tuned = true;
+        }
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = m.tuned ? g_tuned.end() : g_tuned.find(key);
+        if (it != g_tuned.end())
+        {
+            m.narrow = it->second.narrow;
+            m.kparts = it->second.kparts;
+            m.kparts_forced = true;
+            m.tuned = true;
+        }
+    }
+    m.build_work(nullptr, st);
     GB_CUDA(cudaStreamSynchronize(st));
+}
+
+void TcChi0::Impl::launch_t1(const T1Args &a, cudaStream_t st)
+{
+    t1_kernel(ra, ntc, a.vec4 != 0, narrow)<<<n_work, t1_threads(narrow), smem, st>>>(a, maps);
+    GB_LAUNCH_CHECK();
+}
+
+// Times every candidate (producer layout x K parts per tile) on this contraction's own inputs,
+// one warm and one timed launch each, and keeps the fastest.  The candidates write chi0R; the
+// caller's own launch after the tuning overwrites it (zeroing it first when tiles are split).
+void TcChi0::Impl::autotune(const double *G, double *chi0R, cudaStream_t st)
+{
+    T1Args a{};
+    a.g = g;
+    a.pr = pr;
+    a.X = X.get();
+    a.xsign = g.rows_c * g.n_sup;
+    a.G = G;
+    a.cadd = cadd.get();
+    a.work = work.get();
+    a.groups = groups.get();
+    a.spec = spec.get();
+    a.spec_idx = spec_idx.get();
+    a.aJpad = ajpad.get();
+    a.nkc = nkc;
+    a.b_tile = b_tile;
+    a.nbs = nbs;
+    a.gj = gj;
+    a.maxcj = maxcj;
+    a.vec4 = g.n_ao % 4 == 0 ? 1 : 0;
+    a.out = chi0R;
+    a.err = err.get();
+    cudaEvent_t e0, e1;
+    GB_CUDA(cudaEventCreate(&e0));
+    GB_CUDA(cudaEventCreate(&e1));
+    T1Choice best{narrow, kparts, 1e30};
+    const int kp_cand[] = {1, 2, 4, 8};
+    for (int lay = 0; lay < (narrow_ok ? 2 : 1); ++lay)
+        for (int kp : kp_cand)
+        {
+            if (kp > T1_KPARTS_MAX || (kp > 1 && nkc < 2 * kp)) continue;
+            narrow = lay == 0 && narrow_ok;
+            kparts = kp;
+            kparts_forced = true;
+            all_active = false;
+            build_work(nullptr, st);
+            if (n_work == 0) continue;
+            launch_t1(a, st);
+            GB_CUDA(cudaEventRecord(e0, st));
+            launch_t1(a, st);
+            GB_CUDA(cudaEventRecord(e1, st));
+            GB_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best.ms) best = T1Choice{narrow, kp, ms};
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    narrow = best.narrow;
+    kparts = best.kparts;
+    kparts_forced = true;
+    all_active = false;
+    tuned = true;
+    build_work(nullptr, st);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[shape_key] = best;
 }
 
 void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
@@ -1020,7 +1274,7 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
     has_split = false;
     {
         const std::vector<sched::KPart> plan =
-            sched::plan_kparts(static_cast<int>(tiles.size()), n_sm, nkc, T1_KPARTS);
+            sched::plan_kparts(static_cast<int>(tiles.size()), n_sm, nkc, kparts, kparts_forced);
         std::vector<T1Work> cut;
         cut.reserve(plan.size());
         for (const sched::KPart &k : plan)
@@ -1046,6 +1300,12 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
 }
 
 TcChi0::~TcChi0() = default;
+
+void TcChi0::launch_choice(int &narrow, int &kparts) const
+{
+    narrow = impl_->narrow ? 1 : 0;
+    kparts = impl_->kparts;
+}
 
 int TcChi0::run(const double *Gs, const double *G, double *chi0R, cudaStream_t st)
 {
@@ -1074,6 +1334,7 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
     const Geom &g = m.g;
     const long long nsup = g.n_sup;
     int launches = 0;
+    if (!m.t1_simt && !active && !m.tuned) m.autotune(G, chi0R, st);
     if (!m.t1_simt) m.build_work(active, st);
     // K-part tiles add into chi0(R), so their rows start from zero
     if (zero_first || (!m.t1_simt && m.has_split))
@@ -1111,8 +1372,7 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
         a.err = m.err.get();
         if (m.n_work > 0)
         {
-            t1_kernel(m.ra, m.ntc, a.vec4 != 0)<<<m.n_work, T1_THREADS, m.smem, st>>>(a, m.maps);
-            GB_LAUNCH_CHECK();
+            m.launch_t1(a, st);
             k_t2<<<m.n_groups, T2_THREADS, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, m.groups.get(), chi0R);
             GB_LAUNCH_CHECK();
             launches += 2;

@@ -97,6 +97,8 @@ public:
     // [pair * n_cells + cell], nullptr = all).  zero_first clears chi0R first, so blocks left
     // out read zero; a later call with zero_first = false adds further blocks.
     int contract(const double *G, double *chi0R, const unsigned char *active, bool zero_first, cudaStream_t st);
+    // The contraction's launch choice: narrow producer layout (1) or wide (0), K parts per tile.
+    void launch_choice(int &narrow, int &kparts) const;
 
     struct Impl;
 

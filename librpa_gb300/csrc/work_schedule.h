@@ -134,10 +134,13 @@ struct KPart
     int tile, kc0, kc1, split;
 };
 
-inline std::vector<KPart> plan_kparts(int n_tiles, int n_sm, int nkc, int kparts_max)
+// force: cut every tile into kparts_max parts whatever the wave count (a tuner's candidate);
+// otherwise only launches of under 16 waves are cut.
+inline std::vector<KPart> plan_kparts(int n_tiles, int n_sm, int nkc, int kparts_max, bool force = false)
 {
     std::vector<KPart> out;
-    const int kparts = static_cast<long long>(n_tiles) < 16LL * (n_sm > 0 ? n_sm : 1) ? kparts_max : 1;
+    const int kparts =
+        force || static_cast<long long>(n_tiles) < 16LL * (n_sm > 0 ? n_sm : 1) ? kparts_max : 1;
     const bool cut = kparts > 1 && nkc >= 2 * kparts;
     for (int t = 0; t < n_tiles; ++t)
     {
