@@ -319,7 +319,32 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             }
         gk = std::make_unique<GkTc>(nk, nb, nao, psi_real);
     }
-    DevBuf<double> d_chi0R(static_cast<size_t>(r_tot));
+    // Reduced-precision paths keep the chi0(R) of a batch of (tau, spin) slots and transform the
+    // batch in one pass (launch_ftct_slots: chi0(q, w) read and written once per batch, not once
+    // per slot); the FP64 path transforms each slot in FP64 (launch_ftct).  Batches are sized to
+    // keep the slots within about 16 GB.
+    const bool batch_ft = prec != LIBRPA_GB300_CHI0_FP64 && ftct_slots_smem(nc, nq, tf.n) <= 227 * 1024;
+    const int n_slots_all =
+        go.stage != LIBRPA_GB300_STAGE_EC
+            ? (std::min(go.tau_end < 0 ? tf.n : go.tau_end, tf.n) - std::max(0, go.tau_begin)) * ns
+            : 0;
+    const int slot_batch =
+        batch_ft ? std::max(1, std::min(n_slots_all, static_cast<int>(16.0e9 / (8.0 * std::max<long long>(r_tot, 1)))))
+                 : 0;
+    DevBuf<double> d_chi0R(batch_ft ? 0 : static_cast<size_t>(r_tot));
+    DevBuf<double> d_slots(batch_ft ? static_cast<size_t>(slot_batch) * r_tot : 0);
+    DevBuf<float2> d_qph;
+    if (batch_ft)
+    {
+        std::vector<float2> qph(static_cast<size_t>(nq) * nc);
+        for (size_t t = 0; t < qph.size(); ++t)
+            qph[t] = make_float2(static_cast<float>(qcos[t]), static_cast<float>(qsin[t]));
+        d_qph = to_dev(qph, st);
+    }
+    DevBuf<double> d_gslot(batch_ft ? static_cast<size_t>(tf.n) * slot_batch : 0);
+    std::vector<double> h_gslot;
+    int slots_filled = 0;
+    double ftct_bytes = 0.0;
     DevBuf<cuDoubleComplex> d_chi0q(static_cast<size_t>(nw) * nq * e_tot);
     d_chi0q.zero(st);
     DevBuf<double> d_gamma(static_cast<size_t>(nw));
@@ -427,6 +452,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         d_gamma.upload(gam.data(), nw, st);
         for (int is = 0; is < ns; ++is)
         {
+            double *chi0R_cur = batch_ft ? d_slots.get() + static_cast<size_t>(slots_filled) * r_tot : d_chi0R.get();
             ev_gf.start(st);
             launch_tau_scale(d_ekb.get() + static_cast<size_t>(is) * nk * nb, d_wg.get() + static_cast<size_t>(is) * nk * nb,
                              nk, nb, ds.efermi, tau, ns, nbands_g, d_s.get(), st);
@@ -458,7 +484,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 launch_dgemm(static_cast<int>(rows_c), static_cast<int>(n_sup), static_cast<int>(n_sup), d_C.get(), n_sup, 0,
                              d_Gs.get(), n_sup, n_sup * n_sup, d_X.get(), n_sup, rows_c * n_sup, 2, 1.0, 0.0, st);
                 ev_x.start(st);
-                launch_chi0_fp64(d_X.get(), d_X.get() + rows_c * n_sup, d_C.get(), Gp, Gm, g, pr, d_chi0R.get(), st);
+                launch_chi0_fp64(d_X.get(), d_X.get() + rows_c * n_sup, d_C.get(), Gp, Gm, g, pr, chi0R_cur, st);
                 ev_x.stop(st);
                 launches += 2;
             }
@@ -484,8 +510,8 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                     n_act += active[b];
                     blk_audited += audited[b];
                 }
-                launches += tcp->contract(d_G.get(), d_chi0R.get(), active.data(), true, st);
-                launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
+                launches += tcp->contract(d_G.get(), chi0R_cur, active.data(), true, st);
+                launch_block_maxnorm(chi0R_cur, g, pr, d_bnorm.get(), st);
                 ++launches;
                 d_bnorm.download(h_norm.data(), n_blk, st);
                 GB_CUDA(cudaStreamSynchronize(st));
@@ -499,8 +525,8 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 if (violated)
                 {
                     for (int b = 0; b < n_blk; ++b) active[b] = !active[b];
-                    launches += tcp->contract(d_G.get(), d_chi0R.get(), active.data(), false, st);
-                    launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
+                    launches += tcp->contract(d_G.get(), chi0R_cur, active.data(), false, st);
+                    launch_block_maxnorm(chi0R_cur, g, pr, d_bnorm.get(), st);
                     ++launches;
                     n_act = n_blk;
                     ++fallbacks;
@@ -511,13 +537,13 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             else
             {
                 ev_x.start(st);
-                launches += fast->run(d_Gs.get(), Gp, Gm, d_chi0R.get(), st);
+                launches += fast->run(d_Gs.get(), Gp, Gm, chi0R_cur, st);
                 ev_x.stop(st);
             }
             if (smode == LIBRPA_GB300_SCREEN_THRESHOLD)
             {
                 // plain screening: every block computed; its features and norm are logged
-                launch_block_maxnorm(d_chi0R.get(), g, pr, d_bnorm.get(), st);
+                launch_block_maxnorm(chi0R_cur, g, pr, d_bnorm.get(), st);
                 launch_block_features(d_G.get(), g, pr, d_dist.get(), d_cmax.get(), d_kind.get(), tau, d_feat.get(), st);
                 launches += 2;
                 d_bnorm.download(h_norm.data(), n_blk, st);
@@ -530,7 +556,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             }
             if (smode != LIBRPA_GB300_SCREEN_OFF)
             {
-                launch_block_drop(d_chi0R.get(), g, pr, d_bnorm.get(), sthr, st);  // keep max-norm > threshold
+                launch_block_drop(chi0R_cur, g, pr, d_bnorm.get(), sthr, st);  // keep max-norm > threshold
                 ++launches;
             }
             ev_chi.stop(st);
@@ -538,8 +564,33 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             S.dt_chi0_kernel_ms += ev_x.ms();
             S.n_chi0_kernel += 1;
             ev_ft.start(st);
-            launch_ftct(d_chi0R.get(), g, pr, d_qcos.get(), d_qsin.get(), nq, d_gamma.get(), nw, fac, d_chi0q.get(), st);
-            ++launches;
+            if (batch_ft)
+            {
+                // this slot's column of the transform; the batch runs once full or at the last slot
+                for (int w = 0; w < nw; ++w) h_gslot.push_back(fac * gam[w]);
+                ++slots_filled;
+                if (slots_filled == slot_batch || (it == te - 1 && is == ns - 1))
+                {
+                    std::vector<double> gt(static_cast<size_t>(nw) * slots_filled);  // [w][slot]
+                    for (int sl = 0; sl < slots_filled; ++sl)
+                        for (int w = 0; w < nw; ++w)
+                            gt[static_cast<size_t>(w) * slots_filled + sl] = h_gslot[static_cast<size_t>(sl) * nw + w];
+                    d_gslot.upload(gt.data(), gt.size(), st);
+                    launch_ftct_slots(d_slots.get(), r_tot, slots_filled, g, pr, d_qph.get(), nq, d_gslot.get(), nw,
+                                      d_chi0q.get(), st);
+                    ++launches;
+                    ftct_bytes += 8.0 * r_tot * slots_filled + 2.0 * 16.0 * nw * nq * e_tot;
+                    GB_CUDA(cudaStreamSynchronize(st));  // the slots and gt are reused after this
+                    h_gslot.clear();
+                    slots_filled = 0;
+                }
+            }
+            else
+            {
+                launch_ftct(chi0R_cur, g, pr, d_qcos.get(), d_qsin.get(), nq, d_gamma.get(), nw, fac, d_chi0q.get(), st);
+                ++launches;
+                ftct_bytes += 8.0 * r_tot + 2.0 * 16.0 * nw * nq * e_tot;
+            }
             ev_ft.stop(st);
             t_ft += ev_ft.ms();
         }
@@ -591,7 +642,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     S.chi0_flops = flops_chi;
     S.chi0_flops_libri = flops_libri;
     S.gf_flops = static_cast<double>(do_chi0 ? te - tb : 0) * ns * 2.0 * (8.0 * nk * nao * nao * nb + 4.0 * nc * nk * nao * nao);
-    S.ftct_bytes = static_cast<double>(do_chi0 ? te - tb : 0) * ns * (8.0 * r_tot + 2.0 * 16.0 * nw * nq * e_tot);
+    S.ftct_bytes = ftct_bytes;
     d_X.release();
     d_Gs.release();
     fast.reset();

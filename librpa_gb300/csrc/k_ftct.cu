@@ -61,4 +61,101 @@ void launch_ftct(const double *chi0R, const Geom &g, const Pairs &pr, const doub
     GB_LAUNCH_CHECK();
 }
 
+// ---------------------------------------------------------------------------------------------
+// The same transform over a batch of stored chi0(R, tau) slots, applied once per batch instead
+// of once per slot (slot = one (tau, spin) contraction output; the reduced-precision chi0 paths):
+//   chi0(q, w) += sum_slot fac gamma(w, slot) sum_R e^{+i 2pi q.R} chi0_slot(R)
+// The cosine transform over the slots (a minimax quadrature sum) runs in FP64; the R -> q
+// phase sum of its result in FP32 (the precision of the chi0 blocks these paths produce).
+// One CTA per (pair, 32 block elements): the CTA stages C(R, w, e) = sum_slot gamma chi0 in
+// shared memory, then each output (q, w, e) is an n_c-term sum read from there, and chi0(q, w)
+// is read and written once per batch.
+namespace {
+
+constexpr int FT_E = 32;      // block elements per CTA
+constexpr int FT_MAXW = 34;   // largest minimax grid
+
+__global__ void __launch_bounds__(256) k_ftct_slots(const double *__restrict__ slots, long long slot_stride, int nslot,
+                                                   Geom g, Pairs pr, const float2 *__restrict__ qph, int nq,
+                                                   const double *__restrict__ gam, int nw,
+                                                   cuDoubleComplex *__restrict__ chi0q)
+{
+    extern __shared__ __align__(16) unsigned char ft_smem[];
+    const int nc = g.n_c;
+    float *Cw = reinterpret_cast<float *>(ft_smem);                                       // [nc][nw][FT_E]
+    float2 *ph = reinterpret_cast<float2 *>(Cw + static_cast<size_t>(nc) * nw * FT_E);    // [nq][nc]
+    const int p = blockIdx.x;
+    const int I = pr.I[p], J = pr.J[p];
+    const int nel = g.nabf[I] * g.nabf[J];
+    const int e0 = blockIdx.y * FT_E;
+    if (e0 >= nel) return;  // uniform over the CTA
+    for (int t = threadIdx.x; t < nq * nc; t += blockDim.x) ph[t] = qph[t];
+    // cosine transform over the slots, FP64: item (R, e)
+    for (int it = threadIdx.x; it < nc * FT_E; it += blockDim.x)
+    {
+        const int R = it / FT_E, e = it % FT_E;
+        double c[FT_MAXW];
+#pragma unroll
+        for (int w = 0; w < FT_MAXW; ++w) c[w] = 0.0;
+        if (e0 + e < nel)
+        {
+            const double *src = slots + pr.r_off[p] + static_cast<long long>(R) * nel + e0 + e;
+            for (int s = 0; s < nslot; ++s)
+            {
+                const double v = src[static_cast<long long>(s) * slot_stride];
+#pragma unroll
+                for (int w = 0; w < FT_MAXW; ++w)
+                    if (w < nw) c[w] = fma(gam[static_cast<size_t>(w) * nslot + s], v, c[w]);
+            }
+        }
+#pragma unroll
+        for (int w = 0; w < FT_MAXW; ++w)
+            if (w < nw) Cw[(static_cast<size_t>(R) * nw + w) * FT_E + e] = static_cast<float>(c[w]);
+    }
+    __syncthreads();
+    // R -> q: output (q, w, e), e fastest across the lanes of a warp
+    const int e = threadIdx.x % FT_E;
+    if (e0 + e >= nel) return;
+    const long long eoff = pr.e_off[p] + e0 + e;
+    for (int qw = threadIdx.x / FT_E; qw < nq * nw; qw += blockDim.x / FT_E)
+    {
+        const int q = qw / nw, w = qw % nw;
+        float re = 0.0f, im = 0.0f;
+        for (int R = 0; R < nc; ++R)
+        {
+            const float v = Cw[(static_cast<size_t>(R) * nw + w) * FT_E + e];
+            const float2 f = ph[q * nc + R];
+            re = fmaf(f.x, v, re);
+            im = fmaf(f.y, v, im);
+        }
+        cuDoubleComplex *d = chi0q + (static_cast<long long>(w) * nq + q) * pr.e_total + eoff;
+        cuDoubleComplex o = *d;
+        o.x += static_cast<double>(re);
+        o.y += static_cast<double>(im);
+        *d = o;
+    }
+}
+
+} // namespace
+
+size_t ftct_slots_smem(int nc, int nq, int nw)
+{
+    return sizeof(float) * static_cast<size_t>(nc) * nw * FT_E + sizeof(float2) * static_cast<size_t>(nq) * nc;
+}
+
+void launch_ftct_slots(const double *slots, long long slot_stride, int nslot, const Geom &g, const Pairs &pr,
+                       const float2 *qphase, int nq, const double *gamma, int nw, cuDoubleComplex *chi0q,
+                       cudaStream_t st)
+{
+    GB_REQUIRE(nw >= 1 && nw <= FT_MAXW, "minimax grid larger than the FT/CT kernel supports");
+    const size_t smem = ftct_slots_smem(g.n_c, nq, nw);
+    GB_REQUIRE(smem <= 227 * 1024, "FT/CT staging does not fit shared memory (too many cells x frequencies)");
+    static PerDeviceOnce attr;
+    attr.run([] { GB_CUDA(cudaFuncSetAttribute(k_ftct_slots, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024)); });
+    const int maxel = g.max_nabf * g.max_nabf;
+    dim3 grid(pr.n_pairs, (maxel + FT_E - 1) / FT_E);
+    k_ftct_slots<<<grid, 256, smem, st>>>(slots, slot_stride, nslot, g, pr, qphase, nq, gamma, nw, chi0q);
+    GB_LAUNCH_CHECK();
+}
+
 } // namespace gb

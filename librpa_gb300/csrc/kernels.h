@@ -84,6 +84,14 @@ void launch_chi0_fp32(const float *Xp, const float *Xm, const float *Cm, const f
 void launch_ftct(const double *chi0R, const Geom &g, const Pairs &pr, const double *qcos,
                  const double *qsin, int nq, const double *gamma_w, int nw, double fac,
                  cuDoubleComplex *chi0q, cudaStream_t st);
+// The same transform over nslot stored chi0(R) slots (slot s at slots + s * slot_stride, each laid
+// out like chi0R): chi0q += sum_s gamma[w][s] FT(chi0_s), gamma including 2/n_s.  FP64 sum over
+// the slots, FP32 phase sum over R; qphase[q][c] = (cos, sin) of 2 pi q.R_c.
+void launch_ftct_slots(const double *slots, long long slot_stride, int nslot, const Geom &g, const Pairs &pr,
+                       const float2 *qphase, int nq, const double *gamma, int nw, cuDoubleComplex *chi0q,
+                       cudaStream_t st);
+// Shared memory the batched transform needs (it runs when this is at most 227 KB).
+size_t ftct_slots_smem(int nc, int nq, int nw);
 
 // ---------------------------------------------------------------- k_ec.cu
 // Full N x N Hermitian (complex) or symmetric (real part) matrices from upper atom blocks.

@@ -13,7 +13,9 @@
 #include <cstdlib>
 #include <fstream>
 #include <map>
+#include <atomic>
 #include <mutex>
+#include <thread>
 #include <sstream>
 #include <tuple>
 
@@ -177,10 +179,10 @@ std::vector<double> fit_weights(int n, const std::vector<double> &tau, const std
     std::vector<double> x(num_x);
     for (int i = 0; i < num_x; ++i) x[i] = emin * std::pow(x_factor, i);
     std::vector<double> W(static_cast<size_t>(n) * n, 0.0);
-    std::vector<double> A(static_cast<size_t>(num_x) * n), psi(num_x), S, V;
-    max_err = 0.0;
-    for (int ip = 0; ip < n; ++ip)
-    {
+    std::vector<double> errs(n, 0.0);
+    // one least-squares fit per point ip, independent of the others: spread over host threads
+    auto fit_point = [&](int ip) {
+        std::vector<double> A(static_cast<size_t>(num_x) * n), psi(num_x), S, V;
         for (int j = 0; j < n; ++j)
             for (int i = 0; i < num_x; ++i)
             {
@@ -226,13 +228,30 @@ std::vector<double> fit_weights(int n, const std::vector<double> &tau, const std
             for (int k = 0; k < n; ++k) w[k] += V[static_cast<size_t>(j) * n + k] * f;
         }
         for (int k = 0; k < n; ++k) W[static_cast<size_t>(ip) * n + k] = w[k];
+        double e = 0.0;
         for (int i = 0; i < num_x; ++i)
         {
             double fv = 0.0;
             for (int k = 0; k < n; ++k) fv += w[k] * Ain[static_cast<size_t>(k) * num_x + i];
-            max_err = std::fmax(max_err, std::fabs(psi[i] - fv));
+            e = std::fmax(e, std::fabs(psi[i] - fv));
         }
+        errs[ip] = e;
+    };
+    const int nthr = std::max(1, std::min(n, static_cast<int>(std::thread::hardware_concurrency())));
+    if (nthr <= 1)
+        for (int ip = 0; ip < n; ++ip) fit_point(ip);
+    else
+    {
+        std::atomic<int> next{0};
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthr; ++t)
+            pool.emplace_back([&] {
+                for (int ip = next++; ip < n; ip = next++) fit_point(ip);
+            });
+        for (std::thread &th : pool) th.join();
     }
+    max_err = 0.0;
+    for (double e : errs) max_err = std::fmax(max_err, e);
     return W;
 }
 

@@ -38,8 +38,13 @@ def test_sequential_shards_match_full(prec, ec_path, world):
     h.load_chi0_qw(total)
     h.set_gb300_options(L.gb300_options(chi0_precision=prec, ec_path=ec_path, stage=L.STAGE_EC))
     ec, perq = h.get_rpa_correlation_energy(o, L.n_ibz(s))
-    assert abs(ec - full) <= 1e-12 * abs(full), (ec, full)
-    np.testing.assert_allclose(perq, full_q, rtol=1e-11, atol=1e-14)
+    # FP64 path: every slot is transformed in FP64, so the shards add up to rounding.  Tensor-core
+    # path: each call's slots are transformed together with an FP32 phase sum over R, so a
+    # different grouping of the tau slots changes E_c at the FP32 level (measured 4e-9 relative),
+    # far below the 0.1 meV/atom bar
+    rtol = 1e-12 if prec == L.CHI0_FP64 else 1e-7
+    assert abs(ec - full) <= rtol * abs(full), (ec, full)
+    np.testing.assert_allclose(perq, full_q, rtol=10 * rtol, atol=1e-14 if prec == L.CHI0_FP64 else 1e-12)
 
 
 @pytest.mark.parametrize("world", [2, 3])
