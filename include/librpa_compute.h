@@ -1,8 +1,9 @@
 #pragma once
 /*
  * Compute entry points (replaces LibRPA include/librpa_compute.h:26-142).
- * The RPA calls run on one GB300 GPU; the EXX and G0W0 entries are exported
- * for ABI compatibility and record an "unsupported" error.
+ * The RPA calls run on one GB300 GPU.  The exchange and G0W0 calls run on the GPU for
+ * Gamma-point inputs (molecules and Gamma-point cells); k-grid inputs and the band-k-point
+ * variants record an error.
  */
 #include "librpa_handler.h"
 #include "librpa_options.h"
@@ -22,19 +23,28 @@ double librpa_get_rpa_correlation_energy(LibrpaHandler *h, const LibrpaOptions *
                                          int n_ibz_kpoints, double *rpa_corr_ibzk_contrib_re,
                                          double *rpa_corr_ibzk_contrib_im);
 
-/* librpa_compute.h:51-142 -- not part of the RPA path; each records an error. */
+/* librpa_compute.h:51-70 -- exchange at the Gamma point: H_x from the density matrix and the
+ * truncated Coulomb matrix (librpa_set_aux_cut_coulomb_*); v_exx of states
+ * [i_state_low, i_state_high), vexx[(isp * n_kpts_this + ik_this) * n_states + i]; iks_this must
+ * hold k-point 0.  Errors are recorded on the handler. */
 void librpa_build_exx(LibrpaHandler *h, const LibrpaOptions *p_opts);
 void librpa_get_exx_pot_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts,
                               const int n_spins, const int n_kpts_this, const int *iks_this,
                               int i_state_low, int i_state_high, double *vexx);
+/* librpa_compute.h:72-88 -- band k-points: not built; records an error. */
 void librpa_get_exx_pot_band_k(LibrpaHandler *h, const LibrpaOptions *p_opts,
                                const int n_spins, const int n_kpts_band_this, const int *iks_band_this,
                                int i_state_low, int i_state_high, double *vexx_band);
+/* librpa_compute.h:90-125 -- G0W0 at the Gamma point: chi0, W_c (bare Coulomb for the dielectric
+ * function, truncated Coulomb for W) and Sigma_c on the GPU; Sigma_c at the quasi-particle
+ * energy of states [i_state_low, i_state_high) after the Pade continuation (n_params_anacon)
+ * and the quasi-particle equation, in the layout of vexx; NaN where the solver failed. */
 void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *p_opts);
 void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts,
                                 const int n_spins, const int n_kpts_this,
                                 const int *iks_this, int i_state_low, int i_state_high,
                                 const double *vxc, const double *vexx, double *sigc_re, double *sigc_im);
+/* librpa_compute.h:127-142 -- band k-points: not built; records an error. */
 void librpa_get_g0w0_sigc_band_k(LibrpaHandler *h, const LibrpaOptions *p_opts,
                                  const int n_spins, const int n_kpts_band_this,
                                  const int *iks_band_this, int i_state_low, int i_state_high,

@@ -137,7 +137,7 @@ EXPORTS = [
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
-    "librpa_gb300_clear_grid_cache",
+    "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw",
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
@@ -183,6 +183,12 @@ def load_library(path: str | Path | None = None):
         "librpa_get_imaginary_frequency_grids": (None, [vp, C.POINTER(LibrpaOptions), _dp, _dp]),
         "librpa_get_rpa_correlation_energy": (d, [vp, C.POINTER(LibrpaOptions), i, _dp, _dp]),
         "librpa_build_exx": (None, [vp, C.POINTER(LibrpaOptions)]),
+        "librpa_set_aux_cut_coulomb_k_atom_pair": (None, [vp, i, i, i, i, i, _dp, _dp, d]),
+        "librpa_set_aux_cut_coulomb_k_2d_block": (None, [vp, i, i, i, i, i, _dp, _dp]),
+        "librpa_get_exx_pot_kgrid": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp]),
+        "librpa_build_g0w0_sigma": (None, [vp, C.POINTER(LibrpaOptions)]),
+        "librpa_get_g0w0_sigc_kgrid": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp, _dp, _dp, _dp]),
+        "librpa_gb300_get_g0w0_sigc_iw": (i, [vp, i, i, i, _dp, _dp]),
         "librpa_gb300_init_options": (None, [C.POINTER(GB300Options)]),
         "librpa_gb300_set_options": (None, [vp, C.POINTER(GB300Options)]),
         "librpa_gb300_get_stats": (None, [vp, C.POINTER(GB300Stats)]),
@@ -338,6 +344,41 @@ class Handler:
                                                           _f64(Vq_imag).ravel(), float(vq_threshold))
         self._check()
 
+    def set_aux_cut_coulomb_k_atom_pair(self, ik, I, J, naux_mu, naux_nu, Vq_real, Vq_imag, vq_threshold=0.0):
+        self.lib.librpa_set_aux_cut_coulomb_k_atom_pair(self.h, ik, I, J, naux_mu, naux_nu, _f64(Vq_real).ravel(),
+                                                         _f64(Vq_imag).ravel(), float(vq_threshold))
+        self._check()
+
+    def get_exx_pot_kgrid(self, opts, n_spins, iks, i_state_low, i_state_high):
+        """v_exx [n_spins][len(iks)][states] (compute_exx.cpp layout); raises LibrpaError on failure."""
+        iks = np.ascontiguousarray(iks, np.int32)
+        nc = i_state_high - i_state_low
+        out = np.zeros(n_spins * len(iks) * max(nc, 0))
+        self.lib.librpa_get_exx_pot_kgrid(self.h, C.byref(opts), n_spins, len(iks), iks, i_state_low, i_state_high,
+                                          out)
+        self._check()
+        return out.reshape(n_spins, len(iks), nc)
+
+    def get_g0w0_sigc_kgrid(self, opts, n_spins, iks, i_state_low, i_state_high, vxc, vexx):
+        """Sigma_c at the quasi-particle energy, complex [n_spins][len(iks)][states]; NaN where the
+        quasi-particle solver failed.  vxc, vexx in the same layout (Hartree)."""
+        iks = np.ascontiguousarray(iks, np.int32)
+        nc = i_state_high - i_state_low
+        re = np.zeros(n_spins * len(iks) * max(nc, 0))
+        im = np.zeros_like(re)
+        self.lib.librpa_get_g0w0_sigc_kgrid(self.h, C.byref(opts), n_spins, len(iks), iks, i_state_low,
+                                            i_state_high, _f64(vxc).ravel(), _f64(vexx).ravel(), re, im)
+        self._check()
+        return (re + 1j * im).reshape(n_spins, len(iks), nc)
+
+    def g0w0_sigc_iw(self, ispin, lo, hi, nfreq):
+        """KS-diagonal Sigma_c(i omega) [state][omega] of the last G0W0 build."""
+        re = np.zeros((hi - lo) * nfreq)
+        im = np.zeros_like(re)
+        if self.lib.librpa_gb300_get_g0w0_sigc_iw(self.h, ispin, lo, hi, re, im) != 0:
+            raise LibrpaError(self.last_error())
+        return (re + 1j * im).reshape(hi - lo, nfreq)
+
     def set_aux_bare_coulomb_k_2d_block(self, ik, mu_begin, mu_end, nu_begin, nu_end, Vq_real, Vq_imag):
         self.lib.librpa_set_aux_bare_coulomb_k_2d_block(self.h, ik, mu_begin, mu_end, nu_begin, nu_end,
                                                          _f64(Vq_real).ravel(), _f64(Vq_imag).ravel())
@@ -463,6 +504,8 @@ def load_system(h: Handler, s, routing=LIBRI):
         h.set_lri_coeff(routing, I, J, s.nao[I], s.nao[J], s.nabf[I], R, m)
     for (ik, I, J), v in s.Vq.items():
         h.set_aux_bare_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
+    for (ik, I, J), v in getattr(s, "v_cut", {}).items():
+        h.set_aux_cut_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
 
 
 def n_ibz(s) -> int:

@@ -20,6 +20,7 @@
 #include "screen.h"
 #include "host_tables.h"
 #include "minimax.h"
+#include "gw.h"
 #include "qpe.h"
 #include "tc_gemm.h"
 
@@ -186,8 +187,19 @@ void set_wfc_impl(Dataset *ds, int ispin, int isoc, int ik, int nstates_local, i
     ds->wfc_set[(static_cast<size_t>(ispin) * ds->n_spinor + isoc) * ds->n_kpts + ik] = 1;
 }
 
-void add_vq_block(Dataset *ds, int ik, int I, int J, int nmu, int nnu, const double *re, const double *im,
-                  double thr)
+// One Coulomb store: the bare matrix (V of chi0 and of the dielectric function) or the truncated
+// one (exchange and W); both are kept as (ik, I, J) blocks.
+struct VqStore
+{
+    std::vector<cplx> &blob;
+    std::vector<gb::VqBlock> &blocks;
+    std::map<std::array<int, 3>, size_t> &index;
+    std::vector<gb::Vq2DBlock> &blocks_2d;
+};
+VqStore bare_store(Dataset *ds) { return {ds->vq_blob, ds->vq_blocks, ds->vq_index, ds->vq_2d}; }
+VqStore cut_store(Dataset *ds) { return {ds->vq_cut_blob, ds->vq_cut_blocks, ds->vq_cut_index, ds->vq_cut_2d}; }
+
+void add_vq_block(VqStore st, int ik, int I, int J, int nmu, int nnu, const double *re, const double *im, double thr)
 {
     // input.cpp:556-581: keep the block if max |Re V| >= threshold
     double mx = 0.0;
@@ -195,30 +207,43 @@ void add_vq_block(Dataset *ds, int ik, int I, int J, int nmu, int nnu, const dou
     for (size_t t = 0; t < n; ++t) mx = std::max(mx, std::fabs(re[t]));
     if (!(mx >= thr)) return;
     std::array<int, 3> key{ik, I, J};
-    auto it = ds->vq_index.find(key);
-    if (it != ds->vq_index.end() && ds->vq_blocks[it->second].nmu == nmu && ds->vq_blocks[it->second].nnu == nnu)
+    auto it = st.index.find(key);
+    if (it != st.index.end() && st.blocks[it->second].nmu == nmu && st.blocks[it->second].nnu == nnu)
     {
-        const size_t off = ds->vq_blocks[it->second].offset;
-        for (size_t t = 0; t < n; ++t) ds->vq_blob[off + t] = cplx(re[t], im[t]);
+        const size_t off = st.blocks[it->second].offset;
+        for (size_t t = 0; t < n; ++t) st.blob[off + t] = cplx(re[t], im[t]);
         return;
     }
-    gb::VqBlock b{ik, I, J, nmu, nnu, ds->vq_blob.size()};
-    for (size_t t = 0; t < n; ++t) ds->vq_blob.emplace_back(re[t], im[t]);
-    ds->vq_index[key] = ds->vq_blocks.size();
-    ds->vq_blocks.push_back(b);
+    gb::VqBlock b{ik, I, J, nmu, nnu, st.blob.size()};
+    for (size_t t = 0; t < n; ++t) st.blob.emplace_back(re[t], im[t]);
+    st.index[key] = st.blocks.size();
+    st.blocks.push_back(b);
+}
+
+void add_vq_block(Dataset *ds, int ik, int I, int J, int nmu, int nnu, const double *re, const double *im,
+                  double thr)
+{
+    add_vq_block(bare_store(ds), ik, I, J, nmu, nnu, re, im, thr);
 }
 
 // Redistribute 2D-block Coulomb input into atom-pair blocks (Dataset::redistribute_coulomb_blacs2ap).
+void merge_vq_2d(Dataset *ds, VqStore st);
 void merge_vq_2d(Dataset *ds)
 {
-    if (ds->vq_2d.empty()) return;
+    merge_vq_2d(ds, bare_store(ds));
+    merge_vq_2d(ds, cut_store(ds));
+}
+
+void merge_vq_2d(Dataset *ds, VqStore st)
+{
+    if (st.blocks_2d.empty()) return;
     const int nat = static_cast<int>(ds->nabf_at.size());
     GB_REQUIRE(nat > 0, "auxiliary basis needed to use 2D-block Coulomb input");
     std::vector<int> off(nat + 1, 0);
     for (int I = 0; I < nat; ++I) off[I + 1] = off[I] + ds->nabf_at[I];
     const int N = off[nat];
     std::map<int, std::vector<cplx>> full;
-    for (const auto &b : ds->vq_2d)
+    for (const auto &b : st.blocks_2d)
     {
         GB_REQUIRE(b.mu_begin >= 0 && b.mu_end <= N && b.nu_begin >= 0 && b.nu_end <= N,
                    "2D Coulomb block outside the auxiliary basis");
@@ -242,9 +267,9 @@ void merge_vq_2d(Dataset *ds)
                         re[static_cast<size_t>(a) * nnu + b] = v.real();
                         im[static_cast<size_t>(a) * nnu + b] = v.imag();
                     }
-                add_vq_block(ds, kv.first, I, J, nmu, nnu, re.data(), im.data(), -1.0);
+                add_vq_block(st, kv.first, I, J, nmu, nnu, re.data(), im.data(), -1.0);
             }
-    ds->vq_2d.clear();
+    st.blocks_2d.clear();
 }
 
 } // namespace
@@ -567,14 +592,14 @@ void librpa_set_aux_bare_coulomb_k_atom_pair(LibrpaHandler *h, int ik, int I, in
     });
 }
 
-void librpa_set_aux_cut_coulomb_k_atom_pair(LibrpaHandler *h, int, int, int, int nmu, int nnu, const double *re,
-                                            const double *im, double)
+void librpa_set_aux_cut_coulomb_k_atom_pair(LibrpaHandler *h, int ik, int I, int J, int nmu, int nnu,
+                                            const double *re, const double *im, double thr)
 {
+    // input.cpp:584-610: the truncated Coulomb blocks, stored like the bare ones
     guarded(h, [&] {
         Dataset *ds = get_ds(h); ds->generation++;
-        const size_t n = static_cast<size_t>(nmu) * nnu;
-        for (size_t t = 0; t < n; ++t) ds->vq_cut_blob.emplace_back(re[t], im[t]);
-        ds->n_vq_cut_blocks++;
+        GB_REQUIRE(ik >= 0 && ik < static_cast<int>(ds->ibz_map.size()) || ds->klist.empty(), "k index out of range");
+        add_vq_block(cut_store(ds), ik, I, J, nmu, nnu, re, im, thr);
     });
 }
 
@@ -592,13 +617,17 @@ void librpa_set_aux_bare_coulomb_k_2d_block(LibrpaHandler *h, int ik, int mb, in
     });
 }
 
-void librpa_set_aux_cut_coulomb_k_2d_block(LibrpaHandler *h, int, int mb, int me, int nb_, int ne, const double *re,
-                                           const double *im)
+void librpa_set_aux_cut_coulomb_k_2d_block(LibrpaHandler *h, int ik, int mb, int me, int nb_, int ne,
+                                           const double *re, const double *im)
 {
     guarded(h, [&] {
         Dataset *ds = get_ds(h); ds->generation++;
-        const size_t n = static_cast<size_t>(std::max(0, me - mb)) * std::max(0, ne - nb_);
-        for (size_t t = 0; t < n; ++t) ds->vq_cut_blob.emplace_back(re[t], im[t]);
+        const int nr = me - mb, ncl = ne - nb_;
+        if (nr < 1 || ncl < 1) return;
+        gb::Vq2DBlock b{ik, mb, me, nb_, ne, {}};
+        b.data.resize(static_cast<size_t>(nr) * ncl);
+        for (size_t t = 0; t < b.data.size(); ++t) b.data[t] = cplx(re[t], im[t]);
+        ds->vq_cut_2d.push_back(std::move(b));
     });
 }
 
@@ -740,23 +769,167 @@ double librpa_get_rpa_correlation_energy(LibrpaHandler *h, const LibrpaOptions *
 #define GB_UNSUPPORTED(name)                                                                        \
     guarded(h, [&] { GB_FAIL(std::string(name) + " is outside the RPA path of this GB300 build"); })
 
-void librpa_build_exx(LibrpaHandler *h, const LibrpaOptions *) { GB_UNSUPPORTED("librpa_build_exx"); }
-void librpa_get_exx_pot_kgrid(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
-                              double *)
+namespace {
+// Set-up shared by the exchange and G0W0 calls: Gamma-only default lattice, 2D Coulomb input
+// redistributed to atom pairs.
+void prepare_gw(Dataset *ds)
 {
-    GB_UNSUPPORTED("librpa_get_exx_pot_kgrid");
+    if (ds->klist.empty())
+    {
+        ds->klist.assign(3, 0.0);
+        ds->kfrac.assign(3, 0.0);
+        ds->ibz_map.assign(1, 0);
+    }
+    merge_vq_2d(ds);
 }
+
+// -<psi_n|H_x|psi_n> at Gamma for state n of spin s (exx.cpp:820-860)
+double vexx_state(const Dataset &ds, int s, int n)
+{
+    const int nao = ds.n_ao;
+    const cplx *v = ds.wfc.data() + (static_cast<size_t>(s) * ds.n_states + n) * nao;
+    const std::vector<double> &H = ds.hx[s];
+    double acc = 0.0;
+    for (int p = 0; p < nao; ++p)
+    {
+        cplx hv = 0.0;
+        for (int q = 0; q < nao; ++q) hv += H[static_cast<size_t>(p) * nao + q] * v[q];
+        acc += (std::conj(v[p]) * hv).real();
+    }
+    return -acc;
+}
+} // namespace
+
+// compute_exx.cpp: librpa_build_exx (Gamma-point inputs on the GPU; gw.cu)
+void librpa_build_exx(LibrpaHandler *h, const LibrpaOptions *p_opts)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts, "null options");
+        prepare_gw(ds);
+        gb::build_exx_gamma(*ds, *p_opts);
+    });
+}
+
+// compute_exx.cpp:56-112: v_exx of states [i_state_low, i_state_high) at the given k-points,
+// vexx[(isp * n_kpts_this + ik_this) * n_states_calc + i]
+void librpa_get_exx_pot_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, const int n_spins, const int n_kpts_this,
+                              const int *iks_this, int i_state_low, int i_state_high, double *vexx)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts && iks_this && vexx, "null argument");
+        i_state_low = std::max(0, i_state_low);
+        i_state_high = std::min(ds->n_states, i_state_high);
+        GB_REQUIRE(n_spins == ds->n_spins, "parsed nspins is not consistent with the SCF starting point");
+        if (i_state_high <= i_state_low) return;
+        if (ds->hx.empty() || ds->exx_generation != ds->generation)
+        {
+            prepare_gw(ds);
+            gb::build_exx_gamma(*ds, *p_opts);
+        }
+        const int nc = i_state_high - i_state_low;
+        for (int isp = 0; isp < n_spins; ++isp)
+            for (int k = 0; k < n_kpts_this; ++k)
+            {
+                GB_REQUIRE(iks_this[k] == 0, "the Gamma-point exchange has k-point 0 only");
+                for (int i = 0; i < nc; ++i)
+                    vexx[(static_cast<size_t>(isp) * n_kpts_this + k) * nc + i] = vexx_state(*ds, isp, i_state_low + i);
+            }
+    });
+}
+
 void librpa_get_exx_pot_band_k(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
                                double *)
 {
     GB_UNSUPPORTED("librpa_get_exx_pot_band_k");
 }
-void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *) { GB_UNSUPPORTED("librpa_build_g0w0_sigma"); }
-void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
-                                const double *, const double *, double *, double *)
+
+// compute_g0w0.cpp:22-166: chi0, W_c and Sigma_c (Gamma-point inputs on the GPU; gw.cu)
+void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *p_opts)
 {
-    GB_UNSUPPORTED("librpa_get_g0w0_sigc_kgrid");
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts, "null options");
+        prepare_gw(ds);
+        const auto g = make_grids(*ds, *p_opts);
+        GB_REQUIRE(!g.tau.empty(), "time grids required for the space-time method");
+        gb::build_g0w0_gamma(*ds, *p_opts, g);
+    });
 }
+
+// compute_g0w0.cpp:168-260: Sigma_c of states [i_state_low, i_state_high) at the quasi-particle
+// energy (Pade continuation with n_params_anacon, damped fixed point); NaN where the solver failed
+// No counterpart in the reference: the KS-diagonal Sigma_c(i omega) that the quasi-particle step
+// continues, after librpa_build_g0w0_sigma; [state][omega] for states [lo, hi) of one spin.
+int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
+                                  double *im)
+{
+    int rc = 1;
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(!ds->sigc_ks.empty() && ds->g0w0_generation == ds->generation,
+                   "no self-energy: call librpa_build_g0w0_sigma first");
+        GB_REQUIRE(ispin >= 0 && ispin < static_cast<int>(ds->sigc_ks.size()), "spin index out of range");
+        GB_REQUIRE(0 <= i_state_low && i_state_low <= i_state_high && i_state_high <= ds->n_states,
+                   "state range out of range");
+        GB_REQUIRE(re && im, "null array");
+        const int nw = static_cast<int>(ds->gw_omega.size());
+        for (int n = i_state_low; n < i_state_high; ++n)
+            for (int w = 0; w < nw; ++w)
+            {
+                const cplx v = ds->sigc_ks[ispin][static_cast<size_t>(n) * nw + w];
+                re[static_cast<size_t>(n - i_state_low) * nw + w] = v.real();
+                im[static_cast<size_t>(n - i_state_low) * nw + w] = v.imag();
+            }
+        rc = 0;
+    });
+    return rc;
+}
+
+void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, const int n_spins, const int n_kpts_this,
+                                const int *iks_this, int i_state_low, int i_state_high, const double *vxc,
+                                const double *vexx, double *sigc_re, double *sigc_im)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts && iks_this && vxc && vexx && sigc_re && sigc_im, "null argument");
+        i_state_low = std::max(0, i_state_low);
+        i_state_high = std::min(ds->n_states, i_state_high);
+        GB_REQUIRE(n_spins == ds->n_spins, "parsed nspins is not consistent with the SCF starting point");
+        if (i_state_high <= i_state_low) return;
+        if (ds->sigc_ks.empty() || ds->g0w0_generation != ds->generation)
+        {
+            prepare_gw(ds);
+            const auto g = make_grids(*ds, *p_opts);
+            gb::build_g0w0_gamma(*ds, *p_opts, g);
+        }
+        const int nc = i_state_high - i_state_low, nw = static_cast<int>(ds->gw_omega.size());
+        std::vector<std::complex<double>> x(nw), f(nw);
+        for (int w = 0; w < nw; ++w) x[w] = {0.0, ds->gw_omega[w]};
+        for (int isp = 0; isp < n_spins; ++isp)
+            for (int k = 0; k < n_kpts_this; ++k)
+            {
+                GB_REQUIRE(iks_this[k] == 0, "the Gamma-point G0W0 has k-point 0 only");
+                for (int i = 0; i < nc; ++i)
+                {
+                    const int n = i_state_low + i;
+                    const size_t o = (static_cast<size_t>(isp) * n_kpts_this + k) * nc + i;
+                    for (int w = 0; w < nw; ++w) f[w] = ds->sigc_ks[isp][static_cast<size_t>(n) * nw + w];
+                    const gb::PadeContinuation pade(p_opts->n_params_anacon, x, f);
+                    const gb::QpeResult r = gb::solve_qpe(pade, ds->ekb[static_cast<size_t>(isp) * ds->n_states + n],
+                                                          ds->efermi, vxc[o], vexx[o]);
+                    sigc_re[o] = r.info == 0 ? r.sigc.real() : std::numeric_limits<double>::quiet_NaN();
+                    sigc_im[o] = r.info == 0 ? r.sigc.imag() : std::numeric_limits<double>::quiet_NaN();
+                }
+            }
+    });
+}
+
 void librpa_get_g0w0_sigc_band_k(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
                                  const double *, const double *, double *, double *)
 {

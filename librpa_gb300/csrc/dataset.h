@@ -69,8 +69,17 @@ struct Dataset
     std::vector<VqBlock> vq_blocks;
     std::map<std::array<int, 3>, size_t> vq_index;   // (ik,I,J) -> index
     std::vector<Vq2DBlock> vq_2d;
-    std::vector<cplx> vq_cut_blob;                   // truncated Coulomb (stored, unused by RPA)
-    size_t n_vq_cut_blocks = 0;
+    // truncated Coulomb matrix (exchange and W of G0W0), stored like the bare one
+    std::vector<cplx> vq_cut_blob;
+    std::vector<VqBlock> vq_cut_blocks;
+    std::map<std::array<int, 3>, size_t> vq_cut_index;
+    std::vector<Vq2DBlock> vq_cut_2d;
+
+    // Gamma-point exchange and G0W0 results (gw.cu), valid while generation is unchanged
+    std::vector<std::vector<double>> hx;       // per spin: H_x, n_ao x n_ao
+    std::vector<std::vector<cplx>> sigc_ks;    // per spin: Sigma_c(i omega) on the KS states, [n][omega]
+    std::vector<double> gw_omega;              // the imaginary frequencies of sigc_ks
+    unsigned long long exx_generation = 0, g0w0_generation = 0;
 
     // GW-side inputs that the RPA path does not use (kept so the setters behave)
     std::vector<double> dielect_omega, dielect_eps;

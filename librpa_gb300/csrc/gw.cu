@@ -1,0 +1,654 @@
+// Exact exchange and the G0W0 correlation self-energy at the Gamma point, on the GPU.
+//
+// The chain of LibRPA's task = g0w0 for Gamma-only inputs (molecules and Gamma-point cells):
+//   chi0(omega)      the RPA path's chi0(q = 0, omega) (engine.cu, any chi0 precision)
+//   W_c(omega)       S_c [(1 - S chi0 S)^-1 - 1] S_c with S = V^1/2, S_c = V_cut^1/2, the square
+//                    roots by eigen-decomposition with eigenvalues below the threshold dropped
+//                    (compute_Wc_freq_q_blacs, src/core/epsilon.cpp:1763-2322, default branch;
+//                    power_hemat_blacs, src/math/utils_matrix_m_mpi.h:597-720)
+//   W_c(tau)         sum_omega costrans_f2t(tau, omega) W_c(omega) (CT_FT_Wc_freq_q,
+//                    epsilon.cpp:2490-2660; one k-point: no q sum)
+//   Sigma(+-tau)     LibRI GW::cal_Sigmas (thirdparty/LibRI/include/RI/physics/GW.hpp:102-125)
+//   Sigma(i omega)   sum_tau [cos_t2f (S+ + S-)/2 + i sin_t2f (S+ - S-)/2] (src/core/gw.cpp:627-700)
+//   KS diagonal      <psi_n|Sigma(i omega)|psi_n> (gw.cpp:1100-1140)
+// and the exchange of task = exx at Gamma: H_x by LibRI Exx::cal_Hs (Exx.hpp:242-283) with the
+// density matrix D (MeanField::get_dmat_cplx_R, src/core/meanfield.cpp:201-244) and the truncated
+// Coulomb V_cut, v_exx_n = -<psi_n|H_x|psi_n>.
+//
+// The four LibRI labels of cal_Hs / cal_Sigmas sum to one closed form,
+//   H_pq = sum_{a,b,r,s} U[a,p,r] W[a,b] U[b,q,s] D[r,s],   U[a,p,r] = C_a[p,r] + C_a[r,p],
+// which runs here as three FP64 GEMMs over dense operands: Y = U D ([(a,p), s]), Z = W U
+// ([a, (q,s)]) and H = Y' Z' over (a, s).  The dense U holds N_abf n_ao^2 values, which bounds
+// this formulation to cells of a few hundred orbitals; larger cells need the atom-pair-sparse
+// form of the χ0 contraction.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <vector>
+
+#include "common.h"
+#include "dataset.h"
+#include "gw.h"
+#include "kernels.h"
+#include "minimax.h"
+
+namespace gb {
+
+namespace {
+
+// G[i][j] = sgn sum_n s_n Re(psi_ni conj(psi_nj)) (Gamma point: chi0.cpp:332-423 without the
+// phase sum; with s_n the density-matrix weights it is D of meanfield.cpp:201-244)
+__global__ void k_gamma_dm(const cuDoubleComplex *__restrict__ psi, const double *__restrict__ s, int nb, int nao,
+                           double sgn, double *__restrict__ G)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nao * nao) return;
+    const int i = t / nao, j = t % nao;
+    double acc = 0.0;
+    for (int n = 0; n < nb; ++n)
+    {
+        const cuDoubleComplex a = psi[static_cast<size_t>(n) * nao + i], b = psi[static_cast<size_t>(n) * nao + j];
+        acc += s[n] * (a.x * b.x + a.y * b.y);
+    }
+    G[t] = sgn * acc;
+}
+
+// Yt[p][(a, s)] = Y[(a, p), s]
+__global__ void k_perm_y(const double *__restrict__ Y, int N, int nao, double *__restrict__ Yt)
+{
+    const long long n = static_cast<long long>(N) * nao * nao;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long a = t / (static_cast<long long>(nao) * nao);
+        const int p = static_cast<int>((t / nao) % nao), s = static_cast<int>(t % nao);
+        Yt[(static_cast<long long>(p) * N + a) * nao + s] = Y[t];
+    }
+}
+
+// Zt[(a, s)][q] = Z[a][(q, s)]
+__global__ void k_perm_z(const double *__restrict__ Z, int N, int nao, double *__restrict__ Zt)
+{
+    const long long n = static_cast<long long>(N) * nao * nao;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long a = t / (static_cast<long long>(nao) * nao);
+        const int q = static_cast<int>((t / nao) % nao), s = static_cast<int>(t % nao);
+        Zt[(a * nao + s) * nao + q] = Z[t];
+    }
+}
+
+// In place: A <- I - A (batch of N x N)
+__global__ void k_one_minus(double *__restrict__ A, int N, int batch)
+{
+    const long long nn = static_cast<long long>(N) * N, n = nn * batch;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long e = t % nn;
+        A[t] = ((e / N) == (e % N) ? 1.0 : 0.0) - A[t];
+    }
+}
+
+// Solve A X = B in place (B <- X) by Gauss-Jordan elimination with partial pivoting, one CTA per
+// batch entry: A N x N, B N x M, both row-major in global memory.  *bad is set when a pivot is 0.
+__global__ void __launch_bounds__(256) k_gj_solve(double *__restrict__ Aall, double *__restrict__ Ball, int N, int M,
+                                                  int *__restrict__ bad)
+{
+    double *A = Aall + static_cast<size_t>(blockIdx.x) * N * N;
+    double *B = Ball + static_cast<size_t>(blockIdx.x) * N * M;
+    extern __shared__ double col[];  // column k of A before the elimination step
+    __shared__ double rv[256];
+    __shared__ int ri[256];
+    for (int k = 0; k < N; ++k)
+    {
+        // pivot: largest |A[i][k]|, i >= k
+        double best = -1.0;
+        int bi = k;
+        for (int i = k + threadIdx.x; i < N; i += blockDim.x)
+        {
+            const double v = fabs(A[static_cast<size_t>(i) * N + k]);
+            if (v > best)
+            {
+                best = v;
+                bi = i;
+            }
+        }
+        rv[threadIdx.x] = best;
+        ri[threadIdx.x] = bi;
+        __syncthreads();
+        for (int s = blockDim.x / 2; s > 0; s >>= 1)
+        {
+            if (threadIdx.x < s && (rv[threadIdx.x + s] > rv[threadIdx.x] ||
+                                    (rv[threadIdx.x + s] == rv[threadIdx.x] && ri[threadIdx.x + s] < ri[threadIdx.x])))
+            {
+                rv[threadIdx.x] = rv[threadIdx.x + s];
+                ri[threadIdx.x] = ri[threadIdx.x + s];
+            }
+            __syncthreads();
+        }
+        const int piv = ri[0];
+        if (threadIdx.x == 0 && !(rv[0] > 0.0)) atomicExch(bad, 1);
+        __syncthreads();
+        if (piv != k)
+        {
+            for (int j = threadIdx.x; j < N; j += blockDim.x)
+            {
+                const double t = A[static_cast<size_t>(k) * N + j];
+                A[static_cast<size_t>(k) * N + j] = A[static_cast<size_t>(piv) * N + j];
+                A[static_cast<size_t>(piv) * N + j] = t;
+            }
+            for (int j = threadIdx.x; j < M; j += blockDim.x)
+            {
+                const double t = B[static_cast<size_t>(k) * M + j];
+                B[static_cast<size_t>(k) * M + j] = B[static_cast<size_t>(piv) * M + j];
+                B[static_cast<size_t>(piv) * M + j] = t;
+            }
+        }
+        __syncthreads();
+        const double pv = A[static_cast<size_t>(k) * N + k];
+        const double inv = pv != 0.0 ? 1.0 / pv : 0.0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < N; j += blockDim.x) A[static_cast<size_t>(k) * N + j] *= inv;
+        for (int j = threadIdx.x; j < M; j += blockDim.x) B[static_cast<size_t>(k) * M + j] *= inv;
+        for (int i = threadIdx.x; i < N; i += blockDim.x) col[i] = A[static_cast<size_t>(i) * N + k];
+        __syncthreads();
+        // eliminate column k from every other row
+        for (long long t = threadIdx.x; t < static_cast<long long>(N) * (N + M); t += blockDim.x)
+        {
+            const int i = static_cast<int>(t / (N + M)), j = static_cast<int>(t % (N + M));
+            if (i == k) continue;
+            const double f = col[i];
+            if (f == 0.0) continue;
+            if (j < N)
+                A[static_cast<size_t>(i) * N + j] -= f * A[static_cast<size_t>(k) * N + j];
+            else
+                B[static_cast<size_t>(i) * M + (j - N)] -= f * B[static_cast<size_t>(k) * M + (j - N)];
+        }
+        __syncthreads();
+    }
+}
+
+// Sig[w][pq] += c[w] (S+ + S-)/2 + i sn[w] (S+ - S-)/2
+__global__ void k_sigma_accumulate(const double *__restrict__ Sp, const double *__restrict__ Sm, int nn,
+                                   const double *__restrict__ cw, const double *__restrict__ sw, int nw,
+                                   cuDoubleComplex *__restrict__ Sig)
+{
+    const long long n = static_cast<long long>(nn) * nw;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const int w = static_cast<int>(t / nn), e = static_cast<int>(t % nn);
+        const double cp = 0.5 * (Sp[e] + Sm[e]), sp = 0.5 * (Sp[e] - Sm[e]);
+        cuDoubleComplex o = Sig[t];
+        o.x += cw[w] * cp;
+        o.y += sw[w] * sp;
+        Sig[t] = o;
+    }
+}
+
+// KS diagonal: out[n][w] = sum_pq conj(psi_np) Sig[w][p][q] psi_nq
+__global__ void k_ks_diag(const cuDoubleComplex *__restrict__ psi, const cuDoubleComplex *__restrict__ Sig, int nb,
+                          int nao, int nw, cuDoubleComplex *__restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nb * nw) return;
+    const int n = t / nw, w = t % nw;
+    const cuDoubleComplex *S = Sig + static_cast<size_t>(w) * nao * nao;
+    const cuDoubleComplex *v = psi + static_cast<size_t>(n) * nao;
+    double re = 0.0, im = 0.0;
+    for (int p = 0; p < nao; ++p)
+    {
+        double ar = 0.0, ai = 0.0;  // (Sig psi)_p
+        for (int q = 0; q < nao; ++q)
+        {
+            const cuDoubleComplex s = S[static_cast<size_t>(p) * nao + q], x = v[q];
+            ar += s.x * x.x - s.y * x.y;
+            ai += s.x * x.y + s.y * x.x;
+        }
+        re += v[p].x * ar + v[p].y * ai;  // conj(psi_p) (Sig psi)_p
+        im += v[p].x * ai - v[p].y * ar;
+    }
+    out[t] = make_cuDoubleComplex(re, im);
+}
+
+unsigned grid_for(long long n) { return static_cast<unsigned>(std::min<long long>((n + 255) / 256, 152LL * 32)); }
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (row-major, destroyed):
+// eigenvalues w ascending, eigenvectors as the columns of Z (row-major n x n).
+void sym_eig(std::vector<double> &A, int n, std::vector<double> &w, std::vector<double> &Z)
+{
+    Z.assign(static_cast<size_t>(n) * n, 0.0);
+    for (int i = 0; i < n; ++i) Z[static_cast<size_t>(i) * n + i] = 1.0;
+    auto a = [&](int i, int j) -> double & { return A[static_cast<size_t>(i) * n + j]; };
+    double scale = 0.0;
+    for (size_t t = 0; t < A.size(); ++t) scale = std::max(scale, std::fabs(A[t]));
+    for (int sweep = 0; sweep < 100; ++sweep)
+    {
+        double off = 0.0;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) off = std::max(off, std::fabs(a(p, q)));
+        if (off <= 1e-15 * scale) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q)
+            {
+                const double apq = a(p, q);
+                if (std::fabs(apq) <= 1e-300) continue;
+                const double theta = (a(q, q) - a(p, p)) / (2.0 * apq);
+                const double t = std::copysign(1.0, theta) / (std::fabs(theta) + std::sqrt(1.0 + theta * theta));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
+                for (int k = 0; k < n; ++k)
+                {
+                    const double akp = a(k, p), akq = a(k, q);
+                    a(k, p) = c * akp - s * akq;
+                    a(k, q) = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k)
+                {
+                    const double apk = a(p, k), aqk = a(q, k);
+                    a(p, k) = c * apk - s * aqk;
+                    a(q, k) = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k)
+                {
+                    double &zp = Z[static_cast<size_t>(k) * n + p], &zq = Z[static_cast<size_t>(k) * n + q];
+                    const double x = zp, y = zq;
+                    zp = c * x - s * y;
+                    zq = s * x + c * y;
+                }
+            }
+    }
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    std::sort(ord.begin(), ord.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
+    w.resize(n);
+    std::vector<double> Zs(Z.size());
+    for (int j = 0; j < n; ++j)
+    {
+        w[j] = a(ord[j], ord[j]);
+        for (int k = 0; k < n; ++k) Zs[static_cast<size_t>(k) * n + j] = Z[static_cast<size_t>(k) * n + ord[j]];
+    }
+    Z.swap(Zs);
+}
+
+// A^p over the eigenvalues at or above the threshold (ascending order: the ones before the first
+// eigenvalue >= threshold are dropped), as power_hemat_blacs does.
+std::vector<double> power_sym(const std::vector<double> &A, int n, double power, double threshold)
+{
+    std::vector<double> B = A, w, Z;
+    sym_eig(B, n, w, Z);
+    int nf = n;
+    for (int i = 0; i < n; ++i)
+        if (w[i] >= threshold)
+        {
+            nf = i;
+            break;
+        }
+    std::vector<double> out(static_cast<size_t>(n) * n, 0.0);
+    for (int j = nf; j < n; ++j)
+    {
+        const double f = std::pow(w[j], power);
+        for (int r = 0; r < n; ++r)
+        {
+            const double zr = Z[static_cast<size_t>(r) * n + j] * f;
+            for (int c = 0; c < n; ++c) out[static_cast<size_t>(r) * n + c] += zr * Z[static_cast<size_t>(c) * n + j];
+        }
+    }
+    return out;
+}
+
+// Full real symmetric N x N matrix of the Gamma-point Coulomb blocks (upper pairs, real part).
+std::vector<double> coulomb_gamma(const std::vector<VqBlock> &blocks, const std::vector<cplx> &blob,
+                                  const std::vector<int> &abf_off, int N)
+{
+    std::vector<double> V(static_cast<size_t>(N) * N, 0.0);
+    for (const VqBlock &b : blocks)
+    {
+        if (b.ik != 0 || b.I > b.J) continue;
+        for (int m = 0; m < b.nmu; ++m)
+            for (int n = 0; n < b.nnu; ++n)
+            {
+                const double v = blob[b.offset + static_cast<size_t>(m) * b.nnu + n].real();
+                V[static_cast<size_t>(abf_off[b.I] + m) * N + abf_off[b.J] + n] = v;
+                V[static_cast<size_t>(abf_off[b.J] + n) * N + abf_off[b.I] + m] = v;
+            }
+    }
+    return V;
+}
+
+struct GammaSetup
+{
+    int n_at = 0, N = 0, nao = 0;
+    std::vector<int> abf_off, ao_off;
+    DevBuf<double> U;  // [(a, p), r]
+};
+
+// U[a][p][r] = T[a][p][r] + T[a][r][p], T from the RI blocks folded to the Gamma cell (every cell
+// vector folds onto R = 0 with one k-point), blocks with max |C| <= thr dropped after folding
+// (LibRI set_tensors, RI_Tools.hpp:49-67, LRI-set.hpp:33-75).
+void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
+{
+    const int n_at = ds.n_atoms();
+    GB_REQUIRE(n_at > 0 && static_cast<int>(ds.nao_at.size()) == n_at && static_cast<int>(ds.nabf_at.size()) == n_at,
+               "wave-function and auxiliary bases must be set for every atom");
+    gs.n_at = n_at;
+    gs.abf_off.assign(n_at + 1, 0);
+    gs.ao_off.assign(n_at + 1, 0);
+    for (int I = 0; I < n_at; ++I)
+    {
+        gs.abf_off[I + 1] = gs.abf_off[I] + ds.nabf_at[I];
+        gs.ao_off[I + 1] = gs.ao_off[I] + ds.nao_at[I];
+    }
+    gs.N = gs.abf_off[n_at];
+    gs.nao = gs.ao_off[n_at];
+    GB_REQUIRE(gs.nao == ds.n_ao, "sum of per-atom NAOs differs from the mean-field basis size");
+    const int N = gs.N, nao = gs.nao;
+    GB_REQUIRE(static_cast<double>(N) * nao * nao <= 2.0e9,
+               "the Gamma-point G0W0/EXX path holds the dense RI tensor (N_abf n_ao^2 values): input too large");
+    // fold blocks per (I, K) and filter
+    std::vector<std::vector<double>> folded(static_cast<size_t>(n_at) * n_at);
+    for (const CsBlock &b : ds.cs_blocks)
+    {
+        GB_REQUIRE(b.ni == ds.nao_at[b.I] && b.nj == ds.nao_at[b.J] && b.nmu == ds.nabf_at[b.I],
+                   "RI block dimensions inconsistent with the bases");
+        std::vector<double> &f = folded[static_cast<size_t>(b.I) * n_at + b.J];
+        const size_t n = static_cast<size_t>(b.ni) * b.nj * b.nmu;
+        if (f.empty()) f.assign(n, 0.0);
+        for (size_t t = 0; t < n; ++t) f[t] += ds.cs_blob[b.offset + t];
+    }
+    std::vector<double> T(static_cast<size_t>(N) * nao * nao, 0.0);
+    for (int I = 0; I < n_at; ++I)
+        for (int K = 0; K < n_at; ++K)
+        {
+            const std::vector<double> &f = folded[static_cast<size_t>(I) * n_at + K];
+            if (f.empty()) continue;
+            double mx = 0.0;
+            for (double v : f) mx = std::max(mx, std::fabs(v));
+            if (thr > 0.0 && mx <= thr) continue;
+            const int ni = ds.nao_at[I], nk = ds.nao_at[K], nmu = ds.nabf_at[I];
+            // block layout: (i * n_k + k) * n_mu + mu  (input.cpp:525-541)
+            for (int i = 0; i < ni; ++i)
+                for (int k = 0; k < nk; ++k)
+                    for (int mu = 0; mu < nmu; ++mu)
+                    {
+                        const double v = f[(static_cast<size_t>(i) * nk + k) * nmu + mu];
+                        const size_t a = gs.abf_off[I] + mu, p = gs.ao_off[I] + i, r = gs.ao_off[K] + k;
+                        T[(a * nao + p) * nao + r] += v;
+                        T[(a * nao + r) * nao + p] += v;
+                    }
+        }
+    gs.U.alloc(T.size());
+    gs.U.upload(T.data(), T.size(), st);
+    GB_CUDA(cudaStreamSynchronize(st));
+}
+
+// H[p][q] = sum U[a,p,r] W[a,b] U[b,q,s] D[r,s] for each of nd matrices D (nd <= 2); Z = W U is
+// formed once.  Work buffers: Y, Yt, Z, Zt.
+struct HsWork
+{
+    DevBuf<double> Y, Yt, Z, Zt;
+};
+
+void hs_closed_form(const GammaSetup &gs, const double *W, const double *const *D, int nd, double *const *H,
+                    HsWork &wk, cudaStream_t st)
+{
+    const int N = gs.N, nao = gs.nao;
+    const long long nn = static_cast<long long>(nao) * nao, big = static_cast<long long>(N) * nn;
+    if (wk.Y.size() < static_cast<size_t>(big))
+    {
+        wk.Y.alloc(big);
+        wk.Yt.alloc(big);
+        wk.Z.alloc(big);
+        wk.Zt.alloc(big);
+    }
+    launch_dgemm(N, static_cast<int>(nn), N, W, N, 0, gs.U.get(), nn, 0, wk.Z.get(), nn, 0, 1, 1.0, 0.0, st);
+    k_perm_z<<<grid_for(big), 256, 0, st>>>(wk.Z.get(), N, nao, wk.Zt.get());
+    GB_LAUNCH_CHECK();
+    for (int d = 0; d < nd; ++d)
+    {
+        launch_dgemm(N * nao, nao, nao, gs.U.get(), nao, 0, D[d], nao, 0, wk.Y.get(), nao, 0, 1, 1.0, 0.0, st);
+        k_perm_y<<<grid_for(big), 256, 0, st>>>(wk.Y.get(), N, nao, wk.Yt.get());
+        GB_LAUNCH_CHECK();
+        launch_dgemm(nao, nao, static_cast<int>(static_cast<long long>(N) * nao), wk.Yt.get(), static_cast<long long>(N) * nao,
+                     0, wk.Zt.get(), nao, 0, H[d], nao, 0, 1, 1.0, 0.0, st);
+    }
+}
+
+void require_gamma(const Dataset &ds)
+{
+    GB_REQUIRE(ds.n_kpts == 1 && ds.period[0] == 1 && ds.period[1] == 1 && ds.period[2] == 1,
+               "the GPU G0W0 and exchange path covers Gamma-point inputs (molecules and Gamma-point cells); "
+               "k-grid inputs are not supported");
+    GB_REQUIRE(ds.n_spinor == 1, "spinor (SOC) wave functions are not supported");
+    GB_REQUIRE(ds.occ_set, "occupations/eigenvalues not set");
+    for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some spin");
+}
+
+} // namespace
+
+void build_exx_gamma(Dataset &ds, const LibrpaOptions &opts)
+{
+    require_gamma(ds);
+    GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
+    GB_CUDA(cudaSetDevice(ds.gbopt.device));
+    cudaStream_t st;
+    GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct Guard
+    {
+        cudaStream_t s;
+        ~Guard() { cudaStreamDestroy(s); }
+    } guard{st};
+    GammaSetup gs;
+    setup_gamma(ds, opts.libri_exx_threshold_C, gs, st);
+    const int N = gs.N, nao = gs.nao, nb = ds.n_states, ns = ds.n_spins;
+    const std::vector<double> vc = coulomb_gamma(ds.vq_cut_blocks, ds.vq_cut_blob, gs.abf_off, N);
+    DevBuf<double> dV(vc.size()), dD(static_cast<size_t>(nao) * nao), dH(static_cast<size_t>(nao) * nao), ds_w(nb);
+    dV.upload(vc.data(), vc.size(), st);
+    DevBuf<cuDoubleComplex> dpsi(static_cast<size_t>(nb) * nao);
+    HsWork wk;
+    ds.hx.assign(ns, {});
+    for (int s = 0; s < ns; ++s)
+    {
+        // density-matrix weights: wg n_s/2 per state, up to the first below 1e-4/n_k
+        // (meanfield.cpp:201-228; wg is stored already divided by n_k)
+        std::vector<double> w(nb, 0.0);
+        for (int n = 0; n < nb; ++n)
+        {
+            const double v = ds.wg[static_cast<size_t>(s) * nb + n] * 0.5 * ns;
+            if (v < 1e-4 / ds.n_kpts) break;
+            w[n] = v;
+        }
+        ds_w.upload(w.data(), nb, st);
+        dpsi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()) + static_cast<size_t>(s) * nb * nao,
+                    static_cast<size_t>(nb) * nao, st);
+        k_gamma_dm<<<(nao * nao + 255) / 256, 256, 0, st>>>(dpsi.get(), ds_w.get(), nb, nao, 1.0, dD.get());
+        GB_LAUNCH_CHECK();
+        const double *Dp[1] = {dD.get()};
+        double *Hp[1] = {dH.get()};
+        hs_closed_form(gs, dV.get(), Dp, 1, Hp, wk, st);
+        ds.hx[s].resize(static_cast<size_t>(nao) * nao);
+        dH.download(ds.hx[s].data(), ds.hx[s].size(), st);
+        GB_CUDA(cudaStreamSynchronize(st));
+    }
+    ds.exx_generation = ds.generation;
+}
+
+void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)
+{
+    require_gamma(ds);
+    GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
+    GB_REQUIRE(!ds.vq_blocks.empty(), "the Coulomb matrix of the dielectric function is not set");
+    GB_REQUIRE(opts.replace_w_head != LIBRPA_SWITCH_ON,
+               "the head correction of W belongs to k-grid inputs; the Gamma-point path does not apply it");
+    // chi0(q = 0, omega) from the RPA path, kept on the device
+    {
+        const LibrpaGB300Options saved = ds.gbopt;
+        ds.gbopt.stage = LIBRPA_GB300_STAGE_CHI0;
+        ds.gbopt.tau_begin = 0;
+        ds.gbopt.tau_end = -1;
+        try
+        {
+            run_rpa_gpu(ds, opts, tf, opts.n_bands_chi0);
+        }
+        catch (...)
+        {
+            ds.gbopt = saved;
+            throw;
+        }
+        ds.gbopt = saved;
+    }
+    GB_REQUIRE(ds.kept_chi0 && ds.kept_nq == 1 && ds.kept_nfreq == tf.n, "chi0(omega) was not kept");
+    GB_CUDA(cudaSetDevice(ds.gbopt.device));
+    cudaStream_t st;
+    GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct Guard
+    {
+        cudaStream_t s;
+        ~Guard() { cudaStreamDestroy(s); }
+    } guard{st};
+    GammaSetup gs;
+    setup_gamma(ds, opts.libri_g0w0_threshold_C, gs, st);
+    const int N = gs.N, nao = gs.nao, nb = ds.n_states, ns = ds.n_spins, nw = tf.n;
+    const long long NN = static_cast<long long>(N) * N, nn = static_cast<long long>(nao) * nao;
+
+    // S = V^1/2, S_c = V_cut^1/2 on the host (one eigen-decomposition each), then on the device
+    const std::vector<double> ve = coulomb_gamma(ds.vq_blocks, ds.vq_blob, gs.abf_off, N);
+    const std::vector<double> vc = coulomb_gamma(ds.vq_cut_blocks, ds.vq_cut_blob, gs.abf_off, N);
+    const std::vector<double> hS = power_sym(ve, N, 0.5, opts.sqrt_coulomb_threshold);
+    const std::vector<double> hSc = power_sym(vc, N, 0.5, opts.sqrt_coulomb_threshold);
+    DevBuf<double> S(NN), Sc(NN), ScSc(NN);
+    S.upload(hS.data(), NN, st);
+    Sc.upload(hSc.data(), NN, st);
+    launch_dgemm(N, N, N, Sc.get(), N, 0, Sc.get(), N, 0, ScSc.get(), N, 0, 1, 1.0, 0.0, st);
+
+    // chi0(omega) as full real matrices (real part at Gamma, lower blocks the transposes)
+    DevBuf<double> X(NN * nw), T(NN * nw), Wf(NN * nw), Y(NN * nw);
+    {
+        std::vector<int> atom_of(N), pair_of(static_cast<size_t>(gs.n_at) * gs.n_at, -1), abf_off_n(gs.n_at),
+            nabf(gs.n_at);
+        std::vector<long long> eoff;
+        long long e = 0;
+        for (int I = 0; I < gs.n_at; ++I)
+            for (int J = I; J < gs.n_at; ++J)
+            {
+                pair_of[static_cast<size_t>(I) * gs.n_at + J] = static_cast<int>(eoff.size());
+                eoff.push_back(e);
+                e += static_cast<long long>(ds.nabf_at[I]) * ds.nabf_at[J];
+            }
+        for (int I = 0; I < gs.n_at; ++I)
+        {
+            abf_off_n[I] = gs.abf_off[I];
+            nabf[I] = ds.nabf_at[I];
+            for (int a = gs.abf_off[I]; a < gs.abf_off[I + 1]; ++a) atom_of[a] = I;
+        }
+        GB_REQUIRE(static_cast<size_t>(e) == ds.kept_pair_elems, "kept chi0 layout does not match the bases");
+        DevBuf<int> d_atom(N), d_pair(pair_of.size()), d_off(gs.n_at), d_nabf(gs.n_at);
+        DevBuf<long long> d_eoff(eoff.size());
+        d_atom.upload(atom_of.data(), N, st);
+        d_pair.upload(pair_of.data(), pair_of.size(), st);
+        d_off.upload(abf_off_n.data(), gs.n_at, st);
+        d_nabf.upload(nabf.data(), gs.n_at, st);
+        d_eoff.upload(eoff.data(), eoff.size(), st);
+        launch_assemble_chi0(static_cast<const cuDoubleComplex *>(ds.kept_chi0), e, nw, N, d_atom.get(), d_off.get(),
+                             d_nabf.get(), d_pair.get(), gs.n_at, d_eoff.get(), true, nullptr, X.get(), NN, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+    }
+    // eps = 1 - S chi0 S; W_c = S_c eps^-1 S_c - S_c S_c (the solve: Y = eps^-1 S_c)
+    launch_dgemm(N, N, N, S.get(), N, 0, X.get(), N, NN, T.get(), N, NN, nw, 1.0, 0.0, st);
+    launch_dgemm(N, N, N, T.get(), N, NN, S.get(), N, 0, X.get(), N, NN, nw, 1.0, 0.0, st);  // X <- S chi0 S
+    k_one_minus<<<grid_for(NN * nw), 256, 0, st>>>(X.get(), N, nw);
+    GB_LAUNCH_CHECK();
+    for (int w = 0; w < nw; ++w)
+        GB_CUDA(cudaMemcpyAsync(Y.get() + w * NN, Sc.get(), sizeof(double) * NN, cudaMemcpyDeviceToDevice, st));
+    DevBuf<int> bad(1);
+    bad.zero(st);
+    const size_t gj_smem = sizeof(double) * N;
+    GB_REQUIRE(gj_smem <= 48 * 1024, "auxiliary basis too large for the Gamma-point W_c solve");
+    k_gj_solve<<<nw, 256, gj_smem, st>>>(X.get(), Y.get(), N, N, bad.get());
+    GB_LAUNCH_CHECK();
+    launch_dgemm(N, N, N, Sc.get(), N, 0, Y.get(), N, NN, Wf.get(), N, NN, nw, 1.0, 0.0, st);
+    {
+        // W_c(omega) -= S_c S_c for every frequency: one GEMM with a column of -1
+        std::vector<double> ones(nw, -1.0);
+        DevBuf<double> d_ones(nw);
+        d_ones.upload(ones.data(), nw, st);
+        launch_dgemm(nw, static_cast<int>(NN), 1, d_ones.get(), 1, 0, ScSc.get(), NN, 0, Wf.get(), NN, 0, 1, 1.0, 1.0, st);
+        int hbad = 0;
+        bad.download(&hbad, 1, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+        GB_REQUIRE(hbad == 0, "1 - S chi0 S is singular: no W_c");
+    }
+    // W_c(tau) = sum_omega cos_f2t[tau][omega] W_c(omega): one GEMM over the frequency axis
+    DevBuf<double> d_f2t(static_cast<size_t>(nw) * nw), Wt(NN * nw);
+    d_f2t.upload(tf.cos_f2t.data(), static_cast<size_t>(nw) * nw, st);
+    launch_dgemm(nw, static_cast<int>(NN), nw, d_f2t.get(), nw, 0, Wf.get(), NN, 0, Wt.get(), NN, 0, 1, 1.0, 0.0, st);
+    X.release();
+    T.release();
+    Y.release();
+    Wf.release();
+
+    // Sigma_c(i omega) = sum_tau [cos_t2f (S+ + S-)/2 + i sin_t2f (S+ - S-)/2] per spin, then the KS diagonal
+    DevBuf<cuDoubleComplex> Sig(nn * nw), dpsi(static_cast<size_t>(nb) * nao), sks(static_cast<size_t>(nb) * nw);
+    DevBuf<double> sgn_s(2ull * nb), Gp(nn), Gm(nn), Sp(nn), Sm(nn), cw(nw), sw(nw);
+    HsWork wk;
+    ds.sigc_ks.assign(ns, {});
+    for (int s = 0; s < ns; ++s)
+    {
+        Sig.zero(st);
+        dpsi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()) + static_cast<size_t>(s) * nb * nao,
+                    static_cast<size_t>(nb) * nao, st);
+        for (int it = 0; it < nw; ++it)
+        {
+            const double tau = tf.tau[it];
+            // G(+-tau) weights (chi0.cpp:348-365): w+ = max(0, 1/n_k - f n_s/2) unoccupied side,
+            // w- = f n_s/2 with sign -1; s = exp(min(0, -tau (e - e_F))) w
+            std::vector<double> sp(nb), sm(nb);
+            for (int n = 0; n < nb; ++n)
+            {
+                const double f = ds.wg[static_cast<size_t>(s) * nb + n];
+                const double e = ds.ekb[static_cast<size_t>(s) * nb + n] - ds.efermi;
+                const double wp = std::max(0.0, 1.0 / ds.n_kpts - f * 0.5 * ns), wm = f * 0.5 * ns;
+                if (opts.n_bands_chi0 >= 0 && n >= opts.n_bands_chi0)
+                {
+                    sp[n] = sm[n] = 0.0;
+                    continue;
+                }
+                sp[n] = std::exp(std::min(0.0, -tau * e)) * wp;
+                sm[n] = std::exp(std::min(0.0, tau * e)) * wm;
+            }
+            sgn_s.upload(sp.data(), nb, st);
+            k_gamma_dm<<<(nao * nao + 255) / 256, 256, 0, st>>>(dpsi.get(), sgn_s.get(), nb, nao, 1.0, Gp.get());
+            GB_LAUNCH_CHECK();
+            GB_CUDA(cudaStreamSynchronize(st));
+            sgn_s.upload(sm.data(), nb, st);
+            k_gamma_dm<<<(nao * nao + 255) / 256, 256, 0, st>>>(dpsi.get(), sgn_s.get(), nb, nao, -1.0, Gm.get());
+            GB_LAUNCH_CHECK();
+            const double *Dp[2] = {Gp.get(), Gm.get()};
+            double *Hp[2] = {Sp.get(), Sm.get()};
+            hs_closed_form(gs, Wt.get() + it * NN, Dp, 2, Hp, wk, st);
+            std::vector<double> c(nw), sn(nw);
+            for (int w = 0; w < nw; ++w)
+            {
+                c[w] = tf.cos_t2f[static_cast<size_t>(w) * nw + it];
+                sn[w] = tf.sin_t2f[static_cast<size_t>(w) * nw + it];
+            }
+            cw.upload(c.data(), nw, st);
+            sw.upload(sn.data(), nw, st);
+            k_sigma_accumulate<<<grid_for(nn * nw), 256, 0, st>>>(Sp.get(), Sm.get(), static_cast<int>(nn), cw.get(),
+                                                                   sw.get(), nw, Sig.get());
+            GB_LAUNCH_CHECK();
+            GB_CUDA(cudaStreamSynchronize(st));  // the host weight vectors are reused
+        }
+        k_ks_diag<<<(nb * nw + 127) / 128, 128, 0, st>>>(dpsi.get(), Sig.get(), nb, nao, nw, sks.get());
+        GB_LAUNCH_CHECK();
+        ds.sigc_ks[s].resize(static_cast<size_t>(nb) * nw);
+        sks.download(reinterpret_cast<cuDoubleComplex *>(ds.sigc_ks[s].data()), ds.sigc_ks[s].size(), st);
+        GB_CUDA(cudaStreamSynchronize(st));
+    }
+    ds.gw_omega = tf.omega;
+    ds.g0w0_generation = ds.generation;
+    release_kept(ds);
+}
+
+} // namespace gb

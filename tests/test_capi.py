@@ -120,7 +120,7 @@ def test_errors_are_recorded_not_thrown(lib):
             h.set_lri_coeff(L.LIBRI, 0, 0, 2, 2, 3, (0, 0, 0), np.zeros(12))
         h.set_scf_dimension(1, 1, 4, 4)
         assert lib.librpa_get_last_error_code(h.h) == 0
-        lib.librpa_build_exx(h.h, C.byref(L.Options()))
+        lib.librpa_get_exx_pot_band_k(h.h, C.byref(L.Options()), 1, 0, None, 0, 1, None)
         assert "outside the RPA path" in h.last_error()
     assert lib.librpa_get_rpa_correlation_energy(None, None, 0, np.zeros(1), np.zeros(1)) != \
         lib.librpa_get_rpa_correlation_energy(None, None, 0, np.zeros(1), np.zeros(1))  # NaN
@@ -134,6 +134,24 @@ def test_invalid_routing_is_rejected_before_any_gpu_work(lib):
         L.load_system(h, s)
         with pytest.raises(L.LibrpaError, match="invalid parallel routing"):
             h.get_rpa_correlation_energy(L.Options(nfreq=16, tfgrids_type=L.Minimax, parallel_routing=7), 1)
+
+
+def test_g0w0_and_exchange_reject_k_grids_before_any_gpu_work(lib):
+    """The GPU exchange and G0W0 chain covers Gamma-point inputs; a k-grid input (MgO, 3x3x3) is
+    refused with a message, as is a Gamma input without the truncated Coulomb matrix."""
+    from conftest import load_mgo
+    s = load_mgo()
+    with L.Handler() as h:
+        L.load_system(h, s)
+        with pytest.raises(L.LibrpaError, match="Gamma-point inputs"):
+            h.get_exx_pot_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4)
+        with pytest.raises(L.LibrpaError, match="Gamma-point inputs"):
+            h.get_g0w0_sigc_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4, np.zeros(4), np.zeros(4))
+    s = load_h2o()
+    with L.Handler() as h:
+        L.load_system(h, s)
+        with pytest.raises(L.LibrpaError, match="truncated Coulomb"):
+            h.get_exx_pot_kgrid(L.Options(nfreq=16, tfgrids_type=L.Minimax), 1, [0], 0, 4)
 
 
 def test_no_gpu_means_loud_error_not_fallback(lib):

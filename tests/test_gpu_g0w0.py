@@ -1,0 +1,93 @@
+"""Exchange and G0W0 at the Gamma point on the GPU through the C ABI (librpa_get_exx_pot_kgrid,
+librpa_get_g0w0_sigc_kgrid), against the reference's own quasi-particle tables and the CPU
+oracle (needs a GB300)."""
+import numpy as np
+import pytest
+
+import librpa_gb300 as L
+from conftest import load_h2o_g0w0, load_li_g0w0, oracle_input
+from oracle.gw_oracle import HA2EV, g0w0_gamma
+from oracle.rpa_oracle import Options as OOpts
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(lib):
+    if lib.librpa_gb300_device_count() == 0:
+        pytest.fail("no CUDA device visible for a gpu-marked test")
+
+
+def _opts(s):
+    return L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                     n_params_anacon=s.n_params_anacon)
+
+
+def _run(s, prec, keep=None):
+    """v_exx and Sigma_c(e_qp) of every state, per spin, through the library; e_qp from them.
+    keep (a list) receives the handler."""
+    h = L.Handler()
+    if keep is not None:
+        keep.append(h)
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=prec, ec_path=L.EC_LU_FP64))
+    o = _opts(s)
+    nb = s.n_bands
+    vexx = h.get_exx_pot_kgrid(o, s.n_spins, [0], 0, nb)
+    vxc = s.vxc.reshape(s.n_spins, 1, nb)
+    sig = h.get_g0w0_sigc_kgrid(o, s.n_spins, [0], 0, nb, vxc, vexx)
+    e_qp = s.ekb[:, :1, :] - vxc + vexx + sig.real
+    return vexx[:, 0], sig[:, 0], e_qp[:, 0]
+
+
+@pytest.fixture(scope="module")
+def h2o():
+    s = load_h2o_g0w0()
+    return s, g0w0_gamma(oracle_input(s), s.v_cut, s.vxc, OOpts(nfreq=s.nfreq), n_params=s.n_params_anacon)
+
+
+def test_h2o_table_fp64(h2o):
+    """H2O (24 states, 16 minimax points, 16 Pade parameters), FP64 chi0: v_exx, Re/Im Sigma_c and
+    e_qp of every state against the reference's table (refs/g0w0_aims_mole_H2O_libri, printed
+    to 5 decimals in eV) and against the oracle."""
+    s, r = h2o
+    vexx, sig, e_qp = _run(s, L.CHI0_FP64)
+    t = s.qp_table
+    np.testing.assert_allclose(vexx[0] * HA2EV, t[:, 4], rtol=0, atol=6e-6)
+    np.testing.assert_allclose(sig[0].real * HA2EV, t[:, 5], rtol=0, atol=6e-6)
+    np.testing.assert_allclose(sig[0].imag * HA2EV, t[:, 6], rtol=0, atol=6e-6)
+    np.testing.assert_allclose(e_qp[0] * HA2EV, t[:, 7], rtol=0, atol=3e-5)
+    np.testing.assert_allclose(vexx[0], r["vexx"][0], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(sig[0], r["sigc"][0], rtol=0, atol=1e-7)
+    # the GPU's imaginary-axis self-energy itself
+    h = []
+    _run(s, L.CHI0_FP64, h)
+    np.testing.assert_allclose(h[0].g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq), r["sigc_iw"][0], rtol=0, atol=1e-10)
+
+
+def test_h2o_tensor_core_chi0_within_1mev(h2o):
+    """The default 3-piece BF16 tensor-core chi0 feeding the same chain: the KS-diagonal
+    Sigma_c(i omega) of every state and frequency within 1 meV of the FP64 oracle (the G0W0 bar).
+    The analytic continuation to the real axis with 16 Pade parameters is ill-conditioned for the
+    high virtual states (measured: up to 0.15 eV at the quasi-particle energy for the highest
+    states from the tensor-core chi0), so at the quasi-particle energy the bar is applied to the
+    states around the gap: the top three occupied and the first three empty ones."""
+    s, r = h2o
+    hs = []
+    _, sig, _ = _run(s, L.CHI0_BF16X3, hs)
+    iw = hs[0].g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq)
+    assert np.abs(iw - r["sigc_iw"][0]).max() * HA2EV < 1e-3, np.abs(iw - r["sigc_iw"][0]).max() * HA2EV
+    homo = int(np.sum(s.wg[0, 0] > 0)) - 1
+    frontier = slice(homo - 2, homo + 4)
+    assert np.abs(sig[0][frontier] - r["sigc"][0][frontier]).max() * HA2EV < 1e-3
+
+
+def test_li_spin_polarised_table():
+    """Spin-polarised Li atom (refs/g0w0_aims_Li_atom_libri): both spin channels, every column."""
+    s = load_li_g0w0()
+    vexx, sig, e_qp = _run(s, L.CHI0_FP64)
+    for sp in range(2):
+        t = s.qp_tables[sp]
+        got = np.c_[vexx[sp] * HA2EV, sig[sp].real * HA2EV, sig[sp].imag * HA2EV]
+        np.testing.assert_allclose(got, t[:, 4:7], rtol=0, atol=6e-6, err_msg=f"spin {sp}")
+        np.testing.assert_allclose(e_qp[sp] * HA2EV, t[:, 7], rtol=0, atol=3e-5)
