@@ -67,17 +67,19 @@ void launch_ftct(const double *chi0R, const Geom &g, const Pairs &pr, const doub
 //   chi0(q, w) += sum_slot fac gamma(w, slot) sum_R e^{+i 2pi q.R} chi0_slot(R)
 // The cosine transform over the slots (a minimax quadrature sum) runs in FP64; the R -> q
 // phase sum of its result in FP32 (the precision of the chi0 blocks these paths produce).
-// One CTA per (pair, 32 block elements): the CTA stages C(R, w, e) = sum_slot gamma chi0 in
+// One CTA per (pair, FT_E block elements): the CTA stages C(R, w, e) = sum_slot gamma chi0 in
 // shared memory, then each output (q, w, e) is an n_c-term sum read from there, and chi0(q, w)
-// is read and written once per batch.
+// is read and written once per batch.  FT_E is 32 with many cells and up to 256 with few, so
+// that the 256 threads of a CTA have n_c FT_E >= 256 items in the first phase.
 namespace {
 
-constexpr int FT_E = 32;      // block elements per CTA
 constexpr int FT_MAXW = 34;   // largest minimax grid
+
+int ft_elems(int nc) { return nc >= 8 ? 32 : nc >= 2 ? 128 : 256; }
 
 __global__ void __launch_bounds__(256) k_ftct_slots(const double *__restrict__ slots, long long slot_stride, int nslot,
                                                    Geom g, Pairs pr, const float2 *__restrict__ qph, int nq,
-                                                   const double *__restrict__ gam, int nw,
+                                                   const double *__restrict__ gam, int nw, int FT_E,
                                                    cuDoubleComplex *__restrict__ chi0q)
 {
     extern __shared__ __align__(16) unsigned char ft_smem[];
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(256) k_ftct_slots(const double *__restrict__ s
 
 size_t ftct_slots_smem(int nc, int nq, int nw)
 {
-    return sizeof(float) * static_cast<size_t>(nc) * nw * FT_E + sizeof(float2) * static_cast<size_t>(nq) * nc;
+    return sizeof(float) * static_cast<size_t>(nc) * nw * ft_elems(nc) + sizeof(float2) * static_cast<size_t>(nq) * nc;
 }
 
 void launch_ftct_slots(const double *slots, long long slot_stride, int nslot, const Geom &g, const Pairs &pr,
@@ -152,9 +154,9 @@ void launch_ftct_slots(const double *slots, long long slot_stride, int nslot, co
     GB_REQUIRE(smem <= 227 * 1024, "FT/CT staging does not fit shared memory (too many cells x frequencies)");
     static PerDeviceOnce attr;
     attr.run([] { GB_CUDA(cudaFuncSetAttribute(k_ftct_slots, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024)); });
-    const int maxel = g.max_nabf * g.max_nabf;
-    dim3 grid(pr.n_pairs, (maxel + FT_E - 1) / FT_E);
-    k_ftct_slots<<<grid, 256, smem, st>>>(slots, slot_stride, nslot, g, pr, qphase, nq, gamma, nw, chi0q);
+    const int maxel = g.max_nabf * g.max_nabf, fe = ft_elems(g.n_c);
+    dim3 grid(pr.n_pairs, (maxel + fe - 1) / fe);
+    k_ftct_slots<<<grid, 256, smem, st>>>(slots, slot_stride, nslot, g, pr, qphase, nq, gamma, nw, fe, chi0q);
     GB_LAUNCH_CHECK();
 }
 
