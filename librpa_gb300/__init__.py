@@ -137,7 +137,7 @@ EXPORTS = [
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
-    "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw",
+    "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw", "librpa_gb300_get_rpa_correlation_energy_batch",
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
@@ -189,6 +189,7 @@ def load_library(path: str | Path | None = None):
         "librpa_build_g0w0_sigma": (None, [vp, C.POINTER(LibrpaOptions)]),
         "librpa_get_g0w0_sigc_kgrid": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp, _dp, _dp, _dp]),
         "librpa_gb300_get_g0w0_sigc_iw": (i, [vp, i, i, i, _dp, _dp]),
+        "librpa_gb300_get_rpa_correlation_energy_batch": (i, [vp, i, vp, i, _dp]),
         "librpa_gb300_init_options": (None, [C.POINTER(GB300Options)]),
         "librpa_gb300_set_options": (None, [vp, C.POINTER(GB300Options)]),
         "librpa_gb300_get_stats": (None, [vp, C.POINTER(GB300Stats)]),
@@ -506,6 +507,25 @@ def load_system(h: Handler, s, routing=LIBRI):
         h.set_aux_bare_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
     for (ik, I, J), v in getattr(s, "v_cut", {}).items():
         h.set_aux_cut_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
+
+
+def rpa_correlation_energy_batch(handlers, opts, n_threads=0):
+    """E_c of several independent handlers in one concurrent call; opts: one Options or a list."""
+    lib = load_library()
+    n = len(handlers)
+    hs = (C.c_void_p * n)(*[h.h for h in handlers])
+    ol = opts if isinstance(opts, (list, tuple)) else [opts] * n
+    oa = (LibrpaOptions * n)()
+    for i, o in enumerate(ol):
+        oa[i] = LibrpaOptions.from_buffer_copy(o)
+    ec = np.zeros(n)
+    failed = lib.librpa_gb300_get_rpa_correlation_energy_batch(hs, n, oa, n_threads, ec)
+    if failed < 0:
+        raise LibrpaError(lib.librpa_get_last_error(None).decode())
+    if failed > 0:
+        msgs = [h.last_error() for h, e in zip(handlers, ec) if math.isnan(e)]
+        raise LibrpaError(f"{failed} of {n} calls failed: " + "; ".join(msgs[:3]))
+    return ec
 
 
 def n_ibz(s) -> int:

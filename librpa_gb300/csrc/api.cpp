@@ -8,6 +8,9 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <atomic>
+#include <thread>
+#include <algorithm>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -764,6 +767,51 @@ double librpa_get_rpa_correlation_energy(LibrpaHandler *h, const LibrpaOptions *
         out = res.ec.real();
     });
     return out;
+}
+
+// No counterpart in the reference: the E_c call of n independent handlers, run concurrently on
+// host threads (each call stages its inputs and launches on its own CUDA stream, so the GPU
+// overlaps the calls' kernels, transfers and host set-up).
+int librpa_gb300_get_rpa_correlation_energy_batch(LibrpaHandler **hs, int n, const LibrpaOptions *opts, int n_threads,
+                                                  double *ec)
+{
+    int failed = -1;
+    guarded(nullptr, [&] {
+        GB_REQUIRE(n >= 0 && (n == 0 || (hs && opts && ec)), "null argument");
+        {
+            // one thread per handler at a time: a handler listed twice would race with itself
+            std::vector<LibrpaHandler *> seen(hs, hs + n);
+            std::sort(seen.begin(), seen.end());
+            GB_REQUIRE(std::adjacent_find(seen.begin(), seen.end()) == seen.end(),
+                       "librpa_gb300_get_rpa_correlation_energy_batch: a handler is listed twice");
+        }
+        std::vector<int> nq(n, 1);
+        for (int i = 0; i < n; ++i)
+        {
+            const Dataset *ds = get_ds(hs[i]);
+            std::vector<int> reps(ds->ibz_map.begin(), ds->ibz_map.end());
+            std::sort(reps.begin(), reps.end());
+            nq[i] = std::max<int>(1, static_cast<int>(std::unique(reps.begin(), reps.end()) - reps.begin()));
+        }
+        const int hw = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+        const int nt = std::max(1, std::min(n, n_threads > 0 ? n_threads : std::min(8, hw)));
+        std::atomic<int> next{0}, bad{0};
+        auto work = [&] {
+            std::vector<double> re, im;
+            for (int i = next++; i < n; i = next++)
+            {
+                re.assign(nq[i], 0.0);
+                im.assign(nq[i], 0.0);
+                ec[i] = librpa_get_rpa_correlation_energy(hs[i], &opts[i], nq[i], re.data(), im.data());
+                if (std::isnan(ec[i])) ++bad;
+            }
+        };
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t) pool.emplace_back(work);
+        for (std::thread &th : pool) th.join();
+        failed = bad.load();
+    });
+    return failed;
 }
 
 #define GB_UNSUPPORTED(name)                                                                        \

@@ -170,8 +170,9 @@ void launch_chi0_simt(const T *Xp, const T *Xm, const T *Cm, const T *Gp, const 
     const int MA = g.max_nao;
     const size_t smem = sizeof(T) * (static_cast<size_t>(MA) * MA + 3ull * TT * MA * LC);
     GB_REQUIRE(smem <= 227 * 1024, "atom NAO count too large for the SIMT chi0 kernel");
-    GB_CUDA(cudaFuncSetAttribute(k_chi0_simt<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(smem)));
+    // the cap once per device (calls of other shapes may run on other host threads)
+    static PerDeviceOnce attr;
+    attr.run([] { GB_CUDA(cudaFuncSetAttribute(k_chi0_simt<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024)); });
     const int tiles_mu = (g.max_nabf + TT - 1) / TT;
     dim3 grid(pr.n_pairs * g.n_c, tiles_mu, tiles_mu);
     k_chi0_simt<T><<<grid, 256, smem, st>>>(Xp, Xm, Cm, Gp, Gm, g, pr, out);

@@ -798,12 +798,18 @@ __global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid
     if (warp == 0) tmem_dealloc(tmem, TMEM_COLS);
 }
 
-// T2 for one (pair, cJ): out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i].
-// Per pass and chunk of i, the two operands are staged K-major in shared memory (K = (i, j)):
-// S1[k][mu] and S2[k][nu]; each thread accumulates a 4 x 4 block of (mu, nu) with two 16-byte
-// shared loads per 16 FMAs.  Blocks beyond 256 threads' worth loop over output block sets.
+// T2 for one (pair, cJ) and one 64 x 64 tile of its (mu, nu) block:
+//   out[mu][nu] += sum_pass sum_{i,j} Xb^I[mu i; (cJ,J) j] * Xa^J[nu j; (-cJ,I) i].
+// Grid: x = (pair, cJ) group, y = output tile (T2_TILES x T2_TILES of them; CTAs beyond the
+// pair's own block return at once), so that a Gamma-only cell, with one group per pair, still
+// spreads over the SMs.  Per pass and chunk of i, the two operands are staged K-major in
+// shared memory (K = (i, j)): S1[k][mu] and S2[k][nu]; each of the 256 threads accumulates a
+// 4 x 4 block of (mu, nu) with two 16-byte shared loads per 16 FMAs.  Tiles are disjoint and the
+// CTA sums both passes before its one add, so the result does not depend on CTA order.
 constexpr int T2_THREADS = 256;
-constexpr int T2_SMEM_FLOATS = 12288;  // 48 KB
+constexpr int T2_TILE = 64;
+constexpr int T2_TILES = T1_NMAX / T2_TILE;  // per dimension: up to 128 ABFs per atom
+constexpr int T2_SMEM_FLOATS = 12288;        // 48 KB
 
 __global__ void __launch_bounds__(T2_THREADS) k_t2(const float *__restrict__ X, long long xsign, Geom g, Pairs pr,
                                                   const T1Group *__restrict__ groups, double *__restrict__ out)
@@ -812,68 +818,67 @@ __global__ void __launch_bounds__(T2_THREADS) k_t2(const float *__restrict__ X, 
     const int p = groups[blockIdx.x].pair, cJ = groups[blockIdx.x].cell;
     const int I = pr.I[p], J = pr.J[p];
     const int aI = g.nao[I], aJ = g.nao[J], bI = g.nabf[I], bJ = g.nabf[J];
-    const int bIp = (bI + 3) & ~3, bJp = (bJ + 3) & ~3;
+    const int mt0 = static_cast<int>(blockIdx.y / T2_TILES) * T2_TILE, nt0 = static_cast<int>(blockIdx.y % T2_TILES) * T2_TILE;
+    if (mt0 >= bI || nt0 >= bJ) return;  // whole CTA: no barrier skipped by part of it
+    const int mn = min(T2_TILE, bI - mt0), nn = min(T2_TILE, bJ - nt0);
     const long long nsup = g.n_sup;
     const long long colJ = static_cast<long long>(cJ) * g.n_ao + g.ao_off[J];
     const long long colI = static_cast<long long>(g.cneg[cJ]) * g.n_ao + g.ao_off[I];
     double *o = out + pr.r_off[p] + static_cast<long long>(cJ) * bI * bJ;
-    // i per chunk so that both operands fit: (bIp + bJp) * ic * aJ floats
-    const int ic = max(1, min(aI, T2_SMEM_FLOATS / ((bIp + bJp) * aJ)));
-    float *S1 = sm;                            // [k][bIp]
-    float *S2 = sm + static_cast<size_t>(ic) * aJ * bIp;  // [k][bJp]
-    const int nmb = bIp / 4, nnb = bJp / 4, nblk = nmb * nnb;
-    for (int blk0 = 0; blk0 < nblk; blk0 += T2_THREADS)
+    // i per chunk so that both operands fit: 2 * T2_TILE * ic * aJ floats
+    const int ic = max(1, min(aI, T2_SMEM_FLOATS / (2 * T2_TILE * aJ)));
+    float *S1 = sm;                                                // [k][T2_TILE]
+    float *S2 = sm + static_cast<size_t>(ic) * aJ * T2_TILE;       // [k][T2_TILE]
+    const int m0 = (static_cast<int>(threadIdx.x) / (T2_TILE / 4)) * 4;
+    const int n0 = (static_cast<int>(threadIdx.x) % (T2_TILE / 4)) * 4;
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+    for (int pass = 0; pass < 2; ++pass)
     {
-        const int blk = blk0 + static_cast<int>(threadIdx.x);
-        const int m0 = (blk / nnb) * 4, n0 = (blk % nnb) * 4;
-        float acc[4][4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
-        for (int pass = 0; pass < 2; ++pass)
+        const float *Xb = X + (pass == 0 ? xsign : 0);
+        const float *Xa = X + (pass == 0 ? 0 : xsign);
+        for (int i0 = 0; i0 < aI; i0 += ic)
         {
-            const float *Xb = X + (pass == 0 ? xsign : 0);
-            const float *Xa = X + (pass == 0 ? 0 : xsign);
-            for (int i0 = 0; i0 < aI; i0 += ic)
+            const int ni = min(ic, aI - i0), nk = ni * aJ;
+            __syncthreads();
+            // S1[(i - i0) aJ + j][mu] = Xb[(I, mt0 + mu, i)][(cJ, J, j)]  (j fastest: contiguous reads)
+            for (int t = threadIdx.x; t < T2_TILE * nk; t += T2_THREADS)
             {
-                const int ni = min(ic, aI - i0), nk = ni * aJ;
-                __syncthreads();
-                // S1[(i - i0) aJ + j][mu] = Xb[(I, mu, i)][(cJ, J, j)]  (j fastest: contiguous reads)
-                for (int t = threadIdx.x; t < bIp * nk; t += T2_THREADS)
-                {
-                    const int mu = t / nk, k = t % nk, il = k / aJ, jj = k % aJ;
-                    S1[k * bIp + mu] =
-                        mu < bI ? Xb[(g.rowc_off[I] + static_cast<long long>(mu) * aI + i0 + il) * nsup + colJ + jj] : 0.f;
-                }
-                // S2[(i - i0) aJ + j][nu] = Xa[(J, nu, j)][(-cJ, I, i)]  (i fastest)
-                for (int t = threadIdx.x; t < bJp * nk; t += T2_THREADS)
-                {
-                    const int nu = t / nk, r = t % nk, jj = r / ni, il = r % ni;
-                    S2[(il * aJ + jj) * bJp + nu] =
-                        nu < bJ ? Xa[(g.rowc_off[J] + static_cast<long long>(nu) * aJ + jj) * nsup + colI + i0 + il] : 0.f;
-                }
-                __syncthreads();
-                if (blk < nblk)
-                    for (int k = 0; k < nk; ++k)
-                    {
-                        const float4 av = *reinterpret_cast<const float4 *>(S1 + k * bIp + m0);
-                        const float4 bv = *reinterpret_cast<const float4 *>(S2 + k * bJp + n0);
-                        const float a4[4] = {av.x, av.y, av.z, av.w}, b4[4] = {bv.x, bv.y, bv.z, bv.w};
+                const int mu = t / nk, k = t % nk, il = k / aJ, jj = k % aJ;
+                S1[k * T2_TILE + mu] =
+                    mu < mn ? Xb[(g.rowc_off[I] + static_cast<long long>(mt0 + mu) * aI + i0 + il) * nsup + colJ + jj]
+                            : 0.f;
+            }
+            // S2[(i - i0) aJ + j][nu] = Xa[(J, nt0 + nu, j)][(-cJ, I, i)]  (i fastest)
+            for (int t = threadIdx.x; t < T2_TILE * nk; t += T2_THREADS)
+            {
+                const int nu = t / nk, r = t % nk, jj = r / ni, il = r % ni;
+                S2[(il * aJ + jj) * T2_TILE + nu] =
+                    nu < nn ? Xa[(g.rowc_off[J] + static_cast<long long>(nt0 + nu) * aJ + jj) * nsup + colI + i0 + il]
+                            : 0.f;
+            }
+            __syncthreads();
+            for (int k = 0; k < nk; ++k)
+            {
+                const float4 av = *reinterpret_cast<const float4 *>(S1 + k * T2_TILE + m0);
+                const float4 bv = *reinterpret_cast<const float4 *>(S2 + k * T2_TILE + n0);
+                const float a4[4] = {av.x, av.y, av.z, av.w}, b4[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
-                        for (int a = 0; a < 4; ++a)
+                for (int a = 0; a < 4; ++a)
 #pragma unroll
-                            for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(a4[a], b4[b], acc[a][b]);
-                    }
+                    for (int b = 0; b < 4; ++b) acc[a][b] = fmaf(a4[a], b4[b], acc[a][b]);
             }
         }
-        if (blk < nblk)
-#pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int b = 0; b < 4; ++b)
-                    if (m0 + a < bI && n0 + b < bJ) o[(m0 + a) * bJ + n0 + b] += static_cast<double>(acc[a][b]);
     }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+            if (m0 + a < mn && n0 + b < nn)
+                o[static_cast<long long>(mt0 + m0 + a) * bJ + nt0 + n0 + b] += static_cast<double>(acc[a][b]);
 }
 
 // B operand of X = C * Gs: row n = (cL, l), column k = (cK, k'):  Gs^T[n][k] = G[cdiff(cL,cK)][k'][l]
@@ -1127,11 +1132,13 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     const bool sv = g.n_ao % 4 == 0;
     m.narrow_ok = t1_narrow_ok(m.ra, m.ntc, sv);
     m.narrow = m.narrow_ok;
+    // the cap, not this shape's own size: contractions of other shapes on other host threads share
+    // the kernel, and a smaller value set by one of them would fail this one's launch
     GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc, sv, false), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 m.smem));
+                                 T1_SMEM_MAX));
     if (m.narrow_ok)
         GB_CUDA(cudaFuncSetAttribute(t1_kernel(m.ra, m.ntc, sv, true), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     m.smem));
+                                     T1_SMEM_MAX));
     // the shape the tuner's choice is kept for: per-atom sizes, cells, pairs, SM count
     {
         std::string key = std::to_string(g.n_c) + ":" + std::to_string(g.n_ao) + ":" + std::to_string(pr.n_pairs) +
@@ -1373,7 +1380,8 @@ int TcChi0::contract(const double *G, double *chi0R, const unsigned char *active
         if (m.n_work > 0)
         {
             m.launch_t1(a, st);
-            k_t2<<<m.n_groups, T2_THREADS, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr, m.groups.get(), chi0R);
+            k_t2<<<dim3(m.n_groups, T2_TILES * T2_TILES), T2_THREADS, 0, st>>>(m.X.get(), g.rows_c * nsup, g, m.pr,
+                                                                             m.groups.get(), chi0R);
             GB_LAUNCH_CHECK();
             launches += 2;
         }

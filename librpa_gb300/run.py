@@ -7,14 +7,14 @@ librpa_get_rpa_correlation_energy (the call ``task=rpa`` of the reference driver
 driver/task/rpa.cpp:30) and prints one JSON line per call with E_c and the stage times.
 This is the command the kernel profiles are captured with.  A batch workload (a list of
 independent systems, synthetic.BATCHES) is loaded into one handler per system and every
-repeat evaluates them all, one call each; its line reports the summed wall time and the
-per-system energies.
+repeat evaluates them all, one call each (or, with ``--concurrent``, one batch call that runs them
+concurrently); its line reports the summed wall time and the per-system energies.
 """
 import argparse
 import json
 import time
 
-from . import load_system, n_ibz, Handler, Options, gb300_options, Minimax, LIBRI, EC_CHOL, EC_CHOL_FP64, EC_LU_FP64
+from . import load_system, n_ibz, rpa_correlation_energy_batch, Handler, Options, gb300_options, Minimax, LIBRI, EC_CHOL, EC_CHOL_FP64, EC_LU_FP64
 from . import synthetic
 
 CHI0 = {"fp64": 0, "bf16x3": 1, "fp32": 2}
@@ -27,6 +27,8 @@ def main(argv=None):
     ap.add_argument("--chi0", default="bf16x3", choices=list(CHI0))
     ap.add_argument("--ec", default="chol", choices=list(EC))
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--concurrent", action="store_true",
+                    help="batch workloads: one librpa_gb300_get_rpa_correlation_energy_batch call for all systems")
     a = ap.parse_args(argv)
     if a.workload in synthetic.BATCHES:
         return run_batch(a)
@@ -58,10 +60,14 @@ def run_batch(a):
         hs.append((h, o, s))
     for _ in range(a.repeat):
         t = time.time()
-        ecs = [h.get_rpa_correlation_energy(o, n_ibz(s))[0] for h, o, s in hs]
+        if a.concurrent:
+            ecs = list(rpa_correlation_energy_batch([h for h, _, _ in hs], [o for _, o, _ in hs]))
+        else:
+            ecs = [h.get_rpa_correlation_energy(o, n_ibz(s))[0] for h, o, s in hs]
         dt = time.time() - t
         print(json.dumps({"workload": a.workload, "chi0": a.chi0, "ec_path": a.ec, "systems": len(hs),
-                          "atoms": [s.n_atoms for _, _, s in hs], "ec": ecs, "wall_s": dt}), flush=True)
+                          "concurrent": a.concurrent, "atoms": [s.n_atoms for _, _, s in hs], "ec": ecs,
+                          "wall_s": dt}), flush=True)
 
 
 if __name__ == "__main__":

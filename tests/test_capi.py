@@ -164,6 +164,18 @@ def test_no_gpu_means_loud_error_not_fallback(lib):
             h.get_rpa_correlation_energy(L.Options(nfreq=16, tfgrids_type=L.Minimax), 1)
 
 
+def test_batch_call_checks_its_arguments_before_any_gpu_work(lib):
+    """librpa_gb300_get_rpa_correlation_energy_batch refuses a handler listed twice (two threads
+    would work on one handler) and returns -1 with the message; an empty batch is a no-op."""
+    s = load_h2o()
+    o = L.Options(nfreq=16, tfgrids_type=L.Minimax)
+    with L.Handler() as h:
+        L.load_system(h, s)
+        with pytest.raises(L.LibrpaError, match="listed twice"):
+            L.rpa_correlation_energy_batch([h, h], o)
+    assert len(L.rpa_correlation_energy_batch([], o)) == 0
+
+
 def test_vq_threshold_drops_blocks(lib):
     with L.Handler() as h:
         h.set_ao_basis_aux([2, 2])

@@ -250,3 +250,19 @@ def test_every_routing_gives_the_libri_ec(case):
         out[routing], _ = h.get_rpa_correlation_energy(o, L.n_ibz(s))
     for routing in (L.RTAU, L.ATOMPAIR, L.AUTO):
         assert out[routing] == out[L.LIBRI]
+
+
+def test_batch_call_equals_single_calls():
+    """librpa_gb300_get_rpa_correlation_energy_batch: several independent small cells of mixed
+    species evaluated concurrently give each cell's own E_c, as its single call does."""
+    cells = sy.batch32_small()[:8]
+    single, hs, opts = [], [], []
+    for s in cells:
+        h, ec, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+        single.append(ec)
+        hs.append(h)
+        opts.append(L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                              minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax))
+    got = L.rpa_correlation_energy_batch(hs, opts, n_threads=4)
+    # the K parts of the contraction add into chi0 atomically, in varying order
+    np.testing.assert_allclose(got, single, rtol=1e-9, atol=0)
