@@ -210,6 +210,21 @@ int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, 
 int librpa_gb300_get_rpa_correlation_energy_batch(LibrpaHandler **hs, int n, const LibrpaOptions *opts, int n_threads,
                                                   double *ec);
 
+/* ABF shrink (LibrpaOptions.use_shrink_abfs): chi0 is built in the ABF basis of the RI
+ * coefficients (librpa_set_ao_basis_aux), then taken to a smaller ABF basis by
+ * chi0_s(q) = U(q) chi0(q) U(q)^H (shrink_abfs_chi0, src/core/chi0.cpp:711-898), and E_c is
+ * evaluated there, with the Coulomb matrix given in the small basis.  The reference holds these
+ * inputs in Dataset::basis_aux_shrink and Dataset::sinvS (src/api/dataset.h:67-88) and its driver
+ * reads them from Cs_shrinked_data_* and shrink_sinvS_* (driver/read_data.cpp:2455-2622); its C
+ * API has no setter for them.
+ * set_shrink_basis: small ABF count per atom.
+ * set_shrink_sinvS: U(q) for the IBZ point whose representative is k index ik (the index the
+ * Coulomb setters use), n_small x n_large row-major (rows: small ABFs); im may be NULL (real U).
+ * At the Gamma point U must be real. */
+void librpa_gb300_set_shrink_basis(LibrpaHandler *h, int natoms, const size_t *nbs_aux_small);
+void librpa_gb300_set_shrink_sinvS(LibrpaHandler *h, int ik, int n_small, int n_large, const double *re,
+                                   const double *im);
+
 /* Number of CUDA devices visible (0 when there is no GPU). */
 int librpa_gb300_device_count(void);
 

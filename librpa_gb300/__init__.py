@@ -138,6 +138,7 @@ EXPORTS = [
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
     "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw", "librpa_gb300_get_rpa_correlation_energy_batch",
+    "librpa_gb300_set_shrink_basis", "librpa_gb300_set_shrink_sinvS",
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
@@ -190,6 +191,8 @@ def load_library(path: str | Path | None = None):
         "librpa_get_g0w0_sigc_kgrid": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp, _dp, _dp, _dp]),
         "librpa_gb300_get_g0w0_sigc_iw": (i, [vp, i, i, i, _dp, _dp]),
         "librpa_gb300_get_rpa_correlation_energy_batch": (i, [vp, i, vp, i, _dp]),
+        "librpa_gb300_set_shrink_basis": (None, [vp, i, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]),
+        "librpa_gb300_set_shrink_sinvS": (None, [vp, i, i, i, _dp, _dp]),
         "librpa_gb300_init_options": (None, [C.POINTER(GB300Options)]),
         "librpa_gb300_set_options": (None, [vp, C.POINTER(GB300Options)]),
         "librpa_gb300_get_stats": (None, [vp, C.POINTER(GB300Stats)]),
@@ -315,6 +318,19 @@ class Handler:
     def set_ao_basis_aux(self, nbs):
         a = np.ascontiguousarray(nbs, dtype=np.uint64)
         self.lib.librpa_set_ao_basis_aux(self.h, len(a), a)
+        self._check()
+
+    def set_shrink_basis(self, nbs_small):
+        """Small ABF count per atom of the ABF shrink (use_shrink_abfs)."""
+        a = np.ascontiguousarray(nbs_small, dtype=np.uint64)
+        self.lib.librpa_gb300_set_shrink_basis(self.h, len(a), a)
+        self._check()
+
+    def set_shrink_sinvS(self, ik, U):
+        """U(q) (n_small x n_large) of the IBZ point whose representative is k index ik."""
+        U = np.asarray(U)
+        self.lib.librpa_gb300_set_shrink_sinvS(self.h, ik, U.shape[0], U.shape[1], _f64(U.real).ravel(),
+                                               _f64(U.imag).ravel())
         self._check()
 
     def set_latvec_and_G(self, lat_mat, G_mat):
@@ -503,8 +519,15 @@ def load_system(h: Handler, s, routing=LIBRI):
     h.set_ibz_mapping(s.ibz_map)
     for (I, J, R), m in s.Cs.items():
         h.set_lri_coeff(routing, I, J, s.nao[I], s.nao[J], s.nabf[I], R, m)
+    # with an ABF shrink the Coulomb matrix is in the small basis, U(q) keyed by IBZ order
+    nbv = getattr(s, "nabf_small", None) or s.nabf
     for (ik, I, J), v in s.Vq.items():
-        h.set_aux_bare_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
+        h.set_aux_bare_coulomb_k_atom_pair(ik, I, J, nbv[I], nbv[J], v.real, v.imag, 0.0)
+    if getattr(s, "sinvS", None):
+        h.set_shrink_basis(s.nabf_small)
+        reps = list(dict.fromkeys(int(x) for x in s.ibz_map))
+        for iq, U in s.sinvS.items():
+            h.set_shrink_sinvS(reps[iq], U)
     for (ik, I, J), v in getattr(s, "v_cut", {}).items():
         h.set_aux_cut_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
 

@@ -72,9 +72,21 @@ void clear_error(Dataset *ds)
     ds->last_error_code = 0;
 }
 
+// Runs one API call: the handler's error state then reflects this call alone (the last-error
+// contract: code 0 when the last call on h succeeded).
 template <typename F>
 void guarded(LibrpaHandler *h, F &&f)
 {
+    if (h)
+    {
+        const int id = h->instance_id_;
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (id > 0 && id < static_cast<int>(g_instances.size()) && g_instances[id])
+        {
+            g_instances[id]->last_error.clear();
+            g_instances[id]->last_error_code = 0;
+        }
+    }
     try
     {
         f();
@@ -230,20 +242,22 @@ void add_vq_block(Dataset *ds, int ik, int I, int J, int nmu, int nnu, const dou
 }
 
 // Redistribute 2D-block Coulomb input into atom-pair blocks (Dataset::redistribute_coulomb_blacs2ap).
-void merge_vq_2d(Dataset *ds, VqStore st);
-void merge_vq_2d(Dataset *ds)
+void merge_vq_2d(Dataset *ds, VqStore st, const std::vector<int> &nabf);
+void merge_vq_2d(Dataset *ds, bool shrink = false)
 {
-    merge_vq_2d(ds, bare_store(ds));
-    merge_vq_2d(ds, cut_store(ds));
+    merge_vq_2d(ds, bare_store(ds), shrink ? ds->shrink_nabf : ds->nabf_at);
+    merge_vq_2d(ds, cut_store(ds), ds->nabf_at);
 }
 
-void merge_vq_2d(Dataset *ds, VqStore st)
+// nabf: the ABF basis the 2D matrices are given in (the small one of the ABF shrink for the bare
+// Coulomb matrix with use_shrink_abfs)
+void merge_vq_2d(Dataset *ds, VqStore st, const std::vector<int> &nabf)
 {
     if (st.blocks_2d.empty()) return;
-    const int nat = static_cast<int>(ds->nabf_at.size());
+    const int nat = static_cast<int>(nabf.size());
     GB_REQUIRE(nat > 0, "auxiliary basis needed to use 2D-block Coulomb input");
     std::vector<int> off(nat + 1, 0);
-    for (int I = 0; I < nat; ++I) off[I + 1] = off[I] + ds->nabf_at[I];
+    for (int I = 0; I < nat; ++I) off[I + 1] = off[I] + nabf[I];
     const int N = off[nat];
     std::map<int, std::vector<cplx>> full;
     for (const auto &b : st.blocks_2d)
@@ -261,7 +275,7 @@ void merge_vq_2d(Dataset *ds, VqStore st)
         for (int I = 0; I < nat; ++I)
             for (int J = I; J < nat; ++J)
             {
-                const int nmu = ds->nabf_at[I], nnu = ds->nabf_at[J];
+                const int nmu = nabf[I], nnu = nabf[J];
                 std::vector<double> re(static_cast<size_t>(nmu) * nnu), im(re.size());
                 for (int a = 0; a < nmu; ++a)
                     for (int b = 0; b < nnu; ++b)
@@ -494,6 +508,33 @@ void librpa_set_ao_basis_aux(LibrpaHandler *h, int natoms, const size_t *nbs)
         Dataset *ds = get_ds(h); ds->generation++;
         GB_REQUIRE(natoms > 0, "natoms must be positive");
         ds->nabf_at.assign(nbs, nbs + natoms);
+    });
+}
+
+// ABF shrink inputs.  The reference keeps them in Dataset::basis_aux_shrink and Dataset::sinvS
+// (src/api/dataset.h:67-88); its driver reads them from Cs_shrinked_data_* and shrink_sinvS_*
+// (driver/read_data.cpp:2455-2622).  They are read per call, so no staged input is invalidated.
+void librpa_gb300_set_shrink_basis(LibrpaHandler *h, int natoms, const size_t *nbs_aux_small)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(natoms > 0 && nbs_aux_small, "natoms must be positive and the counts given");
+        ds->shrink_nabf.assign(nbs_aux_small, nbs_aux_small + natoms);
+    });
+}
+
+void librpa_gb300_set_shrink_sinvS(LibrpaHandler *h, int ik, int n_small, int n_large, const double *re,
+                                   const double *im)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ik >= 0 && n_small > 0 && n_large > 0 && re, "invalid shrink transform arguments");
+        Dataset::ShrinkU &u = ds->shrink_u[ik];
+        u.n_small = n_small;
+        u.n_large = n_large;
+        const size_t n = static_cast<size_t>(n_small) * n_large;
+        u.u.resize(n);
+        for (size_t t = 0; t < n; ++t) u.u[t] = cplx(re[t], im ? im[t] : 0.0);
     });
 }
 
@@ -739,7 +780,6 @@ double librpa_get_rpa_correlation_energy(LibrpaHandler *h, const LibrpaOptions *
         case AUTO: case RTAU: case ATOMPAIR: case LIBRI: break;
         default: GB_FAIL("invalid parallel routing");
         }
-        GB_REQUIRE(!o.use_shrink_abfs, "use_shrink_abfs is not supported by the GPU RPA path");
         if (ds->klist.empty())
         {
             // Gamma-only default lattice (PeriodicBoundaryData constructor, pbc.cpp:16-32)
@@ -747,7 +787,8 @@ double librpa_get_rpa_correlation_energy(LibrpaHandler *h, const LibrpaOptions *
             ds->kfrac.assign(3, 0.0);
             ds->ibz_map.assign(1, 0);
         }
-        merge_vq_2d(ds);
+        // with use_shrink_abfs the Coulomb matrix is given in the small ABF basis
+        merge_vq_2d(ds, o.use_shrink_abfs == LIBRPA_SWITCH_ON);
         std::memset(&ds->stats, 0, sizeof(ds->stats));
         const double t0 = gb::wall_seconds();
         const auto g = make_grids(*ds, o);

@@ -75,6 +75,17 @@ struct Dataset
     std::map<std::array<int, 3>, size_t> vq_cut_index;
     std::vector<Vq2DBlock> vq_cut_2d;
 
+    // ABF shrink (use_shrink_abfs, chi0.cpp:711-898): the small ABF count per atom (the basis of
+    // the Coulomb matrix and of E_c then) and U(q) = sinvS(q), n_small x n_large row-major, keyed
+    // like the Coulomb blocks by the k index of the IBZ representative
+    struct ShrinkU
+    {
+        int n_small = 0, n_large = 0;
+        std::vector<cplx> u;
+    };
+    std::vector<int> shrink_nabf;
+    std::map<int, ShrinkU> shrink_u;
+
     // Gamma-point exchange and G0W0 results (gw.cu), valid while generation is unchanged
     std::vector<std::vector<double>> hx;       // per spin: H_x, n_ao x n_ao
     std::vector<std::vector<cplx>> sigc_ks;    // per spin: Sigma_c(i omega) on the KS states, [n][omega]

@@ -677,7 +677,93 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     // q sharding: this call's E_c covers the IBZ q points [qa, qe)
     const int qa = std::max(0, go.q_begin), qe = go.q_end < 0 ? nq : std::min(go.q_end, nq);
     GB_REQUIRE(qa <= qe, "q_begin > q_end");
-    const long long NN = static_cast<long long>(N) * N;
+    // The basis E_c runs in: the ABFs of chi0, or with use_shrink_abfs the small ABFs of the
+    // Coulomb matrix, chi0(q, w) taken there by U(q) chi0 U(q)^H (shrink_abfs_chi0,
+    // chi0.cpp:711-898).  The reference transforms chi0(q, tau) ahead of the cosine transform
+    // (chi0.cpp:1110-1137); both steps are linear, so transforming chi0(q, w) is the same.
+    const bool shrink = opts.use_shrink_abfs == LIBRPA_SWITCH_ON;
+    const std::vector<int> &nabf_e = shrink ? ds.shrink_nabf : ds.nabf_at;
+    int Ne = N;
+    long long e_tot_e = e_tot;
+    const cuDoubleComplex *chi0_e = d_chi0q.get();
+    const int *atom_of_e = d_atom_of.get(), *abf_off_e = d_abf_off.get(), *nabf_dev_e = d_nabf.get();
+    const long long *eoff_e = d_eoff.get();
+    DevBuf<int> d_atom_of_s, d_abf_off_s, d_nabf_s;
+    DevBuf<long long> d_eoff_s;
+    DevBuf<cuDoubleComplex> d_chi0q_s;
+    if (shrink)
+    {
+        GB_REQUIRE(static_cast<int>(ds.shrink_nabf.size()) == n_at,
+                   "use_shrink_abfs: the small ABF basis must be set for every atom (librpa_gb300_set_shrink_basis)");
+        std::vector<int> abf_off_s(n_at + 1, 0);
+        for (int I = 0; I < n_at; ++I)
+        {
+            GB_REQUIRE(ds.shrink_nabf[I] > 0, "use_shrink_abfs: small ABF counts must be positive");
+            abf_off_s[I + 1] = abf_off_s[I] + ds.shrink_nabf[I];
+        }
+        Ne = abf_off_s[n_at];
+        std::vector<int> atom_of_s(Ne);
+        for (int I = 0; I < n_at; ++I)
+            for (int a = abf_off_s[I]; a < abf_off_s[I + 1]; ++a) atom_of_s[a] = I;
+        std::vector<long long> e_off_s;
+        e_tot_e = 0;
+        for (int p = 0; p < n_pairs; ++p)
+        {
+            e_off_s.push_back(e_tot_e);
+            e_tot_e += static_cast<long long>(ds.shrink_nabf[pI[p]]) * ds.shrink_nabf[pJ[p]];
+        }
+        abf_off_s.pop_back();
+        d_atom_of_s = to_dev(atom_of_s, st);
+        d_abf_off_s = to_dev(abf_off_s, st);
+        d_nabf_s = to_dev(ds.shrink_nabf, st);
+        d_eoff_s = to_dev(e_off_s, st);
+        d_chi0q_s.alloc(static_cast<size_t>(nw) * nq * e_tot_e);
+        d_chi0q_s.zero(st);
+        const long long NL2 = static_cast<long long>(N) * N, NSL = static_cast<long long>(Ne) * N,
+                        NS2 = static_cast<long long>(Ne) * Ne;
+        DevBuf<cuDoubleComplex> XL(static_cast<size_t>(nw) * NL2), T(static_cast<size_t>(nw) * NSL),
+            XS(static_cast<size_t>(nw) * NS2), U(NSL), UH(NSL);
+        std::vector<cuDoubleComplex> hu(NSL), huh(NSL);
+        for (int q = qa; q < qe; ++q)
+        {
+            auto it = ds.shrink_u.find(ibz_rep[q]);
+            GB_REQUIRE(it != ds.shrink_u.end(), "use_shrink_abfs: no shrink transform U(q) for IBZ k index " +
+                                                    std::to_string(ibz_rep[q]) + " (librpa_gb300_set_shrink_sinvS)");
+            const Dataset::ShrinkU &su = it->second;
+            GB_REQUIRE(su.n_small == Ne && su.n_large == N,
+                       "use_shrink_abfs: U(q) must be (sum of small ABFs) x (sum of ABFs) = " + std::to_string(Ne) +
+                           " x " + std::to_string(N));
+            for (int r = 0; r < Ne; ++r)
+                for (int c = 0; c < N; ++c)
+                {
+                    const cplx v = su.u[static_cast<size_t>(r) * N + c];
+                    // the Gamma-point E_c is real (epsilon.cpp:43-268): a complex U(Gamma) would
+                    // leave an imaginary part that path drops
+                    GB_REQUIRE(!gamma_only || v.imag() == 0.0, "use_shrink_abfs: U(q) must be real at the Gamma point");
+                    hu[static_cast<size_t>(r) * N + c] = make_cuDoubleComplex(v.real(), v.imag());
+                    huh[static_cast<size_t>(c) * Ne + r] = make_cuDoubleComplex(v.real(), -v.imag());
+                }
+            U.upload(hu.data(), NSL, st);
+            UH.upload(huh.data(), NSL, st);
+            // chi0(q, w) of the large basis in full (Hermitian fill), then U chi0 U^H per w
+            launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot, nw,
+                                 N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at, d_eoff.get(),
+                                 false, XL.get(), nullptr, NL2, st);
+            launch_zgemm(Ne, N, N, U.get(), N, 0, XL.get(), N, NL2, T.get(), N, NSL, nw, st);
+            launch_zgemm(Ne, Ne, N, T.get(), N, NSL, UH.get(), Ne, 0, XS.get(), Ne, NS2, nw, st);
+            launch_scatter_pairs(XS.get(), NS2, nw, Ne, d_pI.get(), d_pJ.get(), n_pairs, d_abf_off_s.get(),
+                                 d_nabf_s.get(), d_eoff_s.get(), d_chi0q_s.get() + static_cast<long long>(q) * e_tot_e,
+                                 static_cast<long long>(nq) * e_tot_e, st);
+            launches += 4;
+            GB_CUDA(cudaStreamSynchronize(st));  // hu / huh are refilled for the next q
+        }
+        chi0_e = d_chi0q_s.get();
+        atom_of_e = d_atom_of_s.get();
+        abf_off_e = d_abf_off_s.get();
+        nabf_dev_e = d_nabf_s.get();
+        eoff_e = d_eoff_s.get();
+    }
+    const long long NN = static_cast<long long>(Ne) * Ne;
     double ec_flops = 0.0;
     GB_REQUIRE(go.ec_path == LIBRPA_GB300_EC_LU_FP64 || go.ec_path == LIBRPA_GB300_EC_CHOL ||
                    go.ec_path == LIBRPA_GB300_EC_CHOL_FP64,
@@ -690,7 +776,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         for (int bi : vq_of_q[q])
         {
             const VqBlock &b = ds.vq_blocks[bi];
-            GB_REQUIRE(b.nmu == ds.nabf_at[b.I] && b.nnu == ds.nabf_at[b.J], "Coulomb block dimensions inconsistent");
+            GB_REQUIRE(b.nmu == nabf_e[b.I] && b.nnu == nabf_e[b.J], "Coulomb block dimensions inconsistent");
             voff.push_back(static_cast<long long>(b.offset));
             vIJ.push_back(b.I);
             vIJ.push_back(b.J);
@@ -700,14 +786,14 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         if (gamma_only)
         {
             GB_CUDA(cudaMemsetAsync(V, 0, sizeof(double) * NN, st));
-            launch_assemble_v(din->vblob.get(), d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
-                              d_nabf.get(), N, true, nullptr, static_cast<double *>(V), st);
+            launch_assemble_v(din->vblob.get(), d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), abf_off_e,
+                              nabf_dev_e, Ne, true, nullptr, static_cast<double *>(V), st);
         }
         else
         {
             GB_CUDA(cudaMemsetAsync(V, 0, sizeof(cuDoubleComplex) * NN, st));
-            launch_assemble_v(din->vblob.get(), d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
-                              d_nabf.get(), N, false, static_cast<cuDoubleComplex *>(V), nullptr, st);
+            launch_assemble_v(din->vblob.get(), d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), abf_off_e,
+                              nabf_dev_e, Ne, false, static_cast<cuDoubleComplex *>(V), nullptr, st);
         }
         GB_CUDA(cudaStreamSynchronize(st));  // the block tables go out of scope
         ++launches;
@@ -722,7 +808,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         for (int bi : vq_of_q[q])
         {
             const VqBlock &b = ds.vq_blocks[bi];
-            GB_REQUIRE(b.nmu == ds.nabf_at[b.I] && b.nnu == ds.nabf_at[b.J], "Coulomb block dimensions inconsistent");
+            GB_REQUIRE(b.nmu == nabf_e[b.I] && b.nnu == nabf_e[b.J], "Coulomb block dimensions inconsistent");
             voff.push_back(static_cast<long long>(b.offset));
             vIJ.push_back(b.I);
             vIJ.push_back(b.J);
@@ -735,14 +821,14 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         {
             DevBuf<double> V(NN), X(NN * nw), P(NN * nw), tr(nw), ld(nw);
             V.zero(st);
-            launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
-                              d_nabf.get(), N, true, nullptr, V.get(), st);
-            launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot, nw, N,
-                                 d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at, d_eoff.get(), true,
+            launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), abf_off_e,
+                              nabf_dev_e, Ne, true, nullptr, V.get(), st);
+            launch_assemble_chi0(chi0_e + static_cast<long long>(q) * e_tot_e, static_cast<long long>(nq) * e_tot_e, nw, Ne,
+                                 atom_of_e, abf_off_e, nabf_dev_e, d_pair_of.get(), n_at, eoff_e, true,
                                  nullptr, X.get(), NN, st);
-            launch_dgemm(N, N, N, V.get(), N, 0, X.get(), N, NN, P.get(), N, NN, nw, 1.0, 0.0, st);
-            launch_trace_and_negate_r(P.get(), N, nw, tr.get(), st);
-            launch_lu_logdet_r(P.get(), N, nw, ld.get(), st);
+            launch_dgemm(Ne, Ne, Ne, V.get(), Ne, 0, X.get(), Ne, NN, P.get(), Ne, NN, nw, 1.0, 0.0, st);
+            launch_trace_and_negate_r(P.get(), Ne, nw, tr.get(), st);
+            launch_lu_logdet_r(P.get(), Ne, nw, ld.get(), st);
             launches += 5;
             tr.download(tr_h.data(), nw, st);
             ld.download(ld_h.data(), nw, st);
@@ -752,20 +838,20 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 const cplx v = cplx(tr_h[w] + ld_h[w], 0.0) * tf.omega_w[w] * ibz_w[q] / (2.0 * M_PI);
                 res.per_q[q] += v;
             }
-            ec_flops += nw * (2.0 * N * N * N + 2.0 * N * N * N / 3.0);
+            ec_flops += nw * (2.0 * Ne * Ne * Ne + 2.0 * Ne * Ne * Ne / 3.0);
         }
         else
         {
             DevBuf<cuDoubleComplex> V(NN), X(NN * nw), P(NN * nw), tr(nw), ld(nw);
             V.zero(st);
-            launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), d_abf_off.get(),
-                              d_nabf.get(), N, false, V.get(), nullptr, st);
-            launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot, nw, N,
-                                 d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at, d_eoff.get(), false,
+            launch_assemble_v(vbase, d_voff.get(), d_vIJ.get(), static_cast<int>(voff.size()), abf_off_e,
+                              nabf_dev_e, Ne, false, V.get(), nullptr, st);
+            launch_assemble_chi0(chi0_e + static_cast<long long>(q) * e_tot_e, static_cast<long long>(nq) * e_tot_e, nw, Ne,
+                                 atom_of_e, abf_off_e, nabf_dev_e, d_pair_of.get(), n_at, eoff_e, false,
                                  X.get(), nullptr, NN, st);
-            launch_zgemm(N, N, N, V.get(), N, 0, X.get(), N, NN, P.get(), N, NN, nw, st);
-            launch_trace_and_negate_c(P.get(), N, nw, tr.get(), st);
-            launch_lu_logdet_c(P.get(), N, nw, ld.get(), st);
+            launch_zgemm(Ne, Ne, Ne, V.get(), Ne, 0, X.get(), Ne, NN, P.get(), Ne, NN, nw, st);
+            launch_trace_and_negate_c(P.get(), Ne, nw, tr.get(), st);
+            launch_lu_logdet_c(P.get(), Ne, nw, ld.get(), st);
             launches += 5;
             tr.download(reinterpret_cast<cuDoubleComplex *>(tr_h.data()), nw, st);
             ld.download(reinterpret_cast<cuDoubleComplex *>(ld_h.data()), nw, st);
@@ -776,7 +862,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                                tf.omega_w[w] * ibz_w[q] / (2.0 * M_PI);
                 res.per_q[q] += v;
             }
-            ec_flops += nw * (8.0 * N * N * N + 8.0 * N * N * N / 3.0);
+            ec_flops += nw * (8.0 * Ne * Ne * Ne + 8.0 * Ne * Ne * Ne / 3.0);
         }
     };
     int lu_fallback_q = 0;
@@ -789,7 +875,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         // complex M' is factored as its real 2N x 2N embedding: 32 bytes per element of M'
         const double per_q = static_cast<double>(nw) * NN * (gamma_only ? esz : 2 * esz) + NN * esz;
         const int qb = std::max(1, std::min(std::max(qe - qa, 1), static_cast<int>(24.0e9 / per_q)));
-        EcChol ecc(N, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
+        EcChol ecc(Ne, nw, !gamma_only, qb, go.ec_path == LIBRPA_GB300_EC_CHOL_FP64);
         DevBuf<unsigned char> Vall(static_cast<size_t>(qb) * NN * esz), X(static_cast<size_t>(nw) * NN * esz);
         for (int q0 = qa; q0 < qe; q0 += qb)
         {
@@ -809,9 +895,9 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                     ++lu_fallback_q;
                     continue;
                 }
-                launch_assemble_chi0(d_chi0q.get() + static_cast<long long>(q) * e_tot, static_cast<long long>(nq) * e_tot,
-                                     nw, N, d_atom_of.get(), d_abf_off.get(), d_nabf.get(), d_pair_of.get(), n_at,
-                                     d_eoff.get(), gamma_only,
+                launch_assemble_chi0(chi0_e + static_cast<long long>(q) * e_tot_e, static_cast<long long>(nq) * e_tot_e,
+                                     nw, Ne, atom_of_e, abf_off_e, nabf_dev_e, d_pair_of.get(), n_at,
+                                     eoff_e, gamma_only,
                                      gamma_only ? nullptr : reinterpret_cast<cuDoubleComplex *>(X.get()),
                                      gamma_only ? reinterpret_cast<double *>(X.get()) : nullptr, NN, st);
                 launches += 1 + ecc.stage_q(Vall.get() + static_cast<size_t>(s) * NN * esz, X.get(),
@@ -825,8 +911,8 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             for (int s = 0; s < ns_ok; ++s)
                 for (int w = 0; w < nw; ++w)
                     res.per_q[slot_q[s]] += (tr[s * nw + w] + ld[s * nw + w]) * tf.omega_w[w] * ibz_w[slot_q[s]] / (2.0 * M_PI);
-            ec_flops += ns_ok * nw * (gamma_only ? (2.0 * 2.0 * N * N * N + N * static_cast<double>(N) * N / 3.0)
-                                                 : (2.0 * 8.0 * N * N * N + 4.0 * N * static_cast<double>(N) * N / 3.0));
+            ec_flops += ns_ok * nw * (gamma_only ? (2.0 * 2.0 * Ne * Ne * Ne + Ne * static_cast<double>(Ne) * Ne / 3.0)
+                                                 : (2.0 * 8.0 * Ne * Ne * Ne + 4.0 * Ne * static_cast<double>(Ne) * Ne / 3.0));
         }
     }
     for (int q = qa; q < qe && !use_chol; ++q) ec_lu_q(q);

@@ -481,6 +481,8 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     GB_REQUIRE(!ds.vq_blocks.empty(), "the Coulomb matrix of the dielectric function is not set");
     GB_REQUIRE(opts.replace_w_head != LIBRPA_SWITCH_ON,
                "the head correction of W belongs to k-grid inputs; the Gamma-point path does not apply it");
+    GB_REQUIRE(opts.use_shrink_abfs != LIBRPA_SWITCH_ON,
+               "use_shrink_abfs: the Gamma-point G0W0 chain has no unfolding of W to the large ABF basis");
     // chi0(q = 0, omega) from the RPA path, kept on the device
     {
         const LibrpaGB300Options saved = ds.gbopt;

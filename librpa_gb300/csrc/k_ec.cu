@@ -6,6 +6,8 @@
 // (utils_matrix_m_mpi.h:393-455), Pi = V chi0, tr Pi, M = I - Pi, LU, and
 // ln det = sum_i log(u_ii) if Re u_ii > 0 else log(-u_ii) (epsilon.cpp:578-592, :640-671).
 // Pivot choice follows LAPACK's i*amax: largest |Re|+|Im| (|x| for real), first index on ties.
+#include <algorithm>
+
 #include "kernels.h"
 #include "common.h"
 
@@ -213,6 +215,42 @@ void launch_assemble_chi0(const cuDoubleComplex *src, long long slab_stride, int
     dim3 grid(static_cast<unsigned>(std::min<long long>((nn + 255) / 256, 65535)), n_slabs);
     k_assemble_chi0<<<grid, 256, 0, st>>>(src, slab_stride, N, atom_of, abf_off, nabf, pair_of, n_at, e_off,
                                           real_only, outc, outr, out_stride);
+    GB_LAUNCH_CHECK();
+}
+
+// The inverse of k_assemble_chi0 on the upper atom pairs: out[s][e_off[p] + a nabf[J] + b] =
+// dense[s][(abf_off[I] + a) N + abf_off[J] + b] for pair p = (I, J), a < nabf[I], b < nabf[J].
+__global__ void k_scatter_pairs(const cuDoubleComplex *__restrict__ dense, long long dense_stride, int N,
+                                const int *__restrict__ pI, const int *__restrict__ pJ, int n_pairs,
+                                const int *__restrict__ abf_off, const int *__restrict__ nabf,
+                                const long long *__restrict__ e_off, cuDoubleComplex *__restrict__ out,
+                                long long slab_stride)
+{
+    const int s = blockIdx.z;
+    for (int p = blockIdx.y; p < n_pairs; p += gridDim.y)
+    {
+        const int I = pI[p], J = pJ[p], nJ = nabf[J];
+        const long long nel = static_cast<long long>(nabf[I]) * nJ;
+        const cuDoubleComplex *src = dense + s * dense_stride;
+        cuDoubleComplex *dst = out + s * slab_stride + e_off[p];
+        for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < nel;
+             t += static_cast<long long>(gridDim.x) * blockDim.x)
+        {
+            const int a = static_cast<int>(t / nJ), b = static_cast<int>(t % nJ);
+            dst[t] = src[static_cast<long long>(abf_off[I] + a) * N + abf_off[J] + b];
+        }
+    }
+}
+
+void launch_scatter_pairs(const cuDoubleComplex *dense, long long dense_stride, int n_slabs, int N, const int *pI,
+                          const int *pJ, int n_pairs, const int *abf_off, const int *nabf, const long long *e_off,
+                          cuDoubleComplex *out, long long slab_stride, cudaStream_t st)
+{
+    if (n_pairs == 0 || n_slabs == 0) return;
+    GB_REQUIRE(n_slabs <= 65535, "too many slabs for one scatter launch");
+    const dim3 grid(8, std::min(n_pairs, 65535), n_slabs);
+    k_scatter_pairs<<<grid, 256, 0, st>>>(dense, dense_stride, N, pI, pJ, n_pairs, abf_off, nabf, e_off, out,
+                                          slab_stride);
     GB_LAUNCH_CHECK();
 }
 

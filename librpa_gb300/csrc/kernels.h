@@ -100,6 +100,10 @@ void launch_assemble_chi0(const cuDoubleComplex *src, long long slab_stride, int
                           const int *atom_of, const int *abf_off, const int *nabf, const int *pair_of,
                           int n_at, const long long *e_off, bool real_only, cuDoubleComplex *outc,
                           double *outr, long long out_stride, cudaStream_t st);
+// Dense n_slabs x (N x N) matrices -> their upper atom-pair blocks (the inverse of assemble_chi0).
+void launch_scatter_pairs(const cuDoubleComplex *dense, long long dense_stride, int n_slabs, int N, const int *pI,
+                          const int *pJ, int n_pairs, const int *abf_off, const int *nabf, const long long *e_off,
+                          cuDoubleComplex *out, long long slab_stride, cudaStream_t st);
 void launch_assemble_v(const cuDoubleComplex *blob, const long long *blk_off, const int *blk_IJ,
                        int n_blocks, const int *abf_off, const int *nabf, int N, bool real_only,
                        cuDoubleComplex *outc, double *outr, cudaStream_t st);

@@ -10,6 +10,9 @@
 // vq_threshold, libri_chi0_threshold_C, libri_chi0_threshold_G, minimax_emin/emax, and the
 // GPU controls gb300_chi0_precision (fp64 | bf16x3 | fp32), gb300_ec_path (lu | chol |
 // chol_fp64), gb300_screen_mode (off | threshold | mlp), gb300_screen_threshold.
+// use_shrink_abfs = t reads the ABF shrink as driver/read_data.cpp:2455-2622 does: the small ABF
+// count per atom from the Cs_shrinked_data headers, U(q) from shrink_sinvS_*, and the Coulomb
+// matrix in the small basis.
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -159,6 +162,9 @@ int main()
         opts.libri_chi0_threshold_G = std::stod(par("libri_chi0_threshold_G", "0"));
         opts.minimax_emin = std::stod(par("minimax_emin", "-1"));
         opts.minimax_emax = std::stod(par("minimax_emax", "-1"));
+        const std::string shr = lower(par("use_shrink_abfs", "f"));
+        const bool shrink = shr == "t" || shr == "true" || shr == ".true." || shr == "1";
+        opts.use_shrink_abfs = shrink ? LIBRPA_SWITCH_ON : LIBRPA_SWITCH_OFF;
 
         LibrpaHandler *h = librpa_create_handler(0);
         if (!h) die(librpa_get_last_error(nullptr));
@@ -402,11 +408,119 @@ int main()
                 set_cs(v, c);
             }
         }
+        // ABF shrink: small basis from the n_mu of the Cs_shrinked_data blocks (first atom of a
+        // block), U(q) from shrink_sinvS_* (handle_sinvS_file, read_data.cpp:2455-2568: n_irk, then
+        // blocks n_small n_large brow erow bcol ecol iq q_weight and the (re, im) of the rows; iq
+        // counts the IBZ points in order)
+        std::vector<int> nabf_v = m.nabf_at;  // the basis of the Coulomb matrix
+        if (shrink)
+        {
+            std::map<int, int> aa;
+            for (const auto &fn : files_with_prefix(dir, "Cs_shrinked_data"))
+            {
+                if (is_text_file(fn))
+                {
+                    const auto t = tokens(fn);
+                    size_t q = 2;
+                    while (q + 8 <= t.size())
+                    {
+                        int v[8];
+                        for (int i = 0; i < 8; ++i) v[i] = std::stoi(t[q + i]);
+                        aa[v[0] - 1] = v[7];
+                        q += 8 + static_cast<size_t>(v[5]) * v[6] * v[7];
+                    }
+                    continue;
+                }
+                const auto raw = slurp(fn);
+                size_t off = 8;
+                const int nblk = get<int>(raw, off);
+                for (int b = 0; b < nblk; ++b)
+                {
+                    int v[8];
+                    for (auto &x : v) x = get<int>(raw, off);
+                    aa[v[0] - 1] = v[7];
+                    off += 8 * static_cast<size_t>(v[5]) * v[6] * v[7];
+                }
+            }
+            std::vector<size_t> ns(m.nat);
+            for (int a = 0; a < m.nat; ++a)
+            {
+                if (!aa.count(a)) die("use_shrink_abfs: no Cs_shrinked_data block gives the small basis of atom " +
+                                      std::to_string(a + 1));
+                ns[a] = static_cast<size_t>(aa[a]);
+                nabf_v[a] = aa[a];
+            }
+            librpa_gb300_set_shrink_basis(h, m.nat, ns.data());
+            std::vector<int> reps;  // IBZ representatives in order of appearance
+            for (int k : m.ibz)
+                if (std::find(reps.begin(), reps.end(), k) == reps.end()) reps.push_back(k);
+            std::map<int, std::vector<cplx>> U;
+            int n_s = 0, n_l = 0;
+            auto block = [&](int nsm, int nlg, int br, int er, int bc, int ec, int iq, const std::string &fn) {
+                if (er < br || ec < bc || br < 0 || bc < 0 || er >= nsm || ec >= nlg || iq < 0 ||
+                    iq >= static_cast<int>(reps.size()))
+                    die("bad shrink transform block header in " + fn);
+                n_s = nsm;
+                n_l = nlg;
+                auto &M = U[iq];
+                M.resize(static_cast<size_t>(nsm) * nlg);
+                return &M;
+            };
+            for (const auto &fn : files_with_prefix(dir, "shrink_sinvS"))
+            {
+                if (is_text_file(fn))
+                {
+                    const auto t = tokens(fn);
+                    size_t q = 1;
+                    while (q + 8 <= t.size())
+                    {
+                        int v[7];
+                        for (int i = 0; i < 7; ++i) v[i] = std::stoi(t[q + i]);
+                        q += 8;
+                        auto *M = block(v[0], v[1], v[2] - 1, v[3] - 1, v[4] - 1, v[5] - 1, v[6] - 1, fn);
+                        const size_t cnt = static_cast<size_t>(v[3] - v[2] + 1) * (v[5] - v[4] + 1);
+                        if (q + 2 * cnt > t.size()) die("truncated shrink transform file " + fn);
+                        for (int r = v[2] - 1; r < v[3]; ++r)
+                            for (int c = v[4] - 1; c < v[5]; ++c, q += 2)
+                                (*M)[static_cast<size_t>(r) * v[1] + c] = cplx(std::stod(t[q]), std::stod(t[q + 1]));
+                    }
+                    continue;
+                }
+                const auto raw = slurp(fn);
+                size_t off = 0;
+                get<int>(raw, off);
+                const int nloc = get<int>(raw, off);
+                for (int b = 0; b < nloc; ++b)
+                {
+                    int v[7];
+                    for (auto &x : v) x = get<int>(raw, off);
+                    get<double>(raw, off);
+                    auto *M = block(v[0], v[1], v[2] - 1, v[3] - 1, v[4] - 1, v[5] - 1, v[6] - 1, fn);
+                    for (int r = v[2] - 1; r < v[3]; ++r)
+                        for (int c = v[4] - 1; c < v[5]; ++c)
+                        {
+                            const double x = get<double>(raw, off), y = get<double>(raw, off);
+                            (*M)[static_cast<size_t>(r) * v[1] + c] = cplx(x, y);
+                        }
+                }
+            }
+            if (U.empty()) die("use_shrink_abfs: no shrink_sinvS file in " + dir);
+            for (const auto &[iq, M] : U)
+            {
+                std::vector<double> ur(M.size()), ui(M.size());
+                for (size_t i = 0; i < M.size(); ++i)
+                {
+                    ur[i] = M[i].real();
+                    ui[i] = M[i].imag();
+                }
+                librpa_gb300_set_shrink_sinvS(h, reps[iq], n_s, n_l, ur.data(), ui.data());
+            }
+        }
         // coulomb_mat* binary (read_data.cpp:1472-1577): n_irk n_local, then per block
         // nbasbas brow erow bcol ecol iq q_weight and the rows (complex); atom-pair blocks I <= J
         {
             std::vector<int> off_at(m.nat + 1, 0);
-            for (int a = 0; a < m.nat; ++a) off_at[a + 1] = off_at[a] + m.nabf_at[a];
+            for (int a = 0; a < m.nat; ++a) off_at[a + 1] = off_at[a] + nabf_v[a];
             std::map<int, std::vector<cplx>> full;
             int nbb = 0;
             for (const auto &fn : files_with_prefix(dir, "coulomb_mat"))
@@ -460,12 +574,13 @@ int main()
             }
             if (!full.empty() && nbb != off_at[m.nat])
                 die("Coulomb matrices are " + std::to_string(nbb) + " x " + std::to_string(nbb) + " but the bases give " +
-                    std::to_string(off_at[m.nat]) + " auxiliary functions (shrunk ABF sets are not supported)");
+                    std::to_string(off_at[m.nat]) + " auxiliary functions" +
+                    (shrink ? "" : " (a shrunk ABF set needs use_shrink_abfs = t)"));
             for (const auto &[iq, M] : full)
                 for (int I = 0; I < m.nat; ++I)
                     for (int J = I; J < m.nat; ++J)
                     {
-                        const int nm = m.nabf_at[I], nn = m.nabf_at[J];
+                        const int nm = nabf_v[I], nn = nabf_v[J];
                         std::vector<double> vr(static_cast<size_t>(nm) * nn), vi(vr.size());
                         for (int a = 0; a < nm; ++a)
                             for (int c = 0; c < nn; ++c)

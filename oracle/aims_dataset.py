@@ -11,6 +11,8 @@ Follows the driver readers of the reference (driver/read_data.cpp):
   coulomb_mat_*     handle_Vq_row_file         :1472-1650 (binary and text; upper atom blocks)
   coulomb_cut_*     the same format (truncated Coulomb of G0W0, driver/task/g0w0.cpp:33-45)
   vxc_out           read_vxc                   :142-182
+  shrink_sinvS_*    handle_sinvS_file          :2455-2568 (ABF shrink transform U(q), text and binary)
+  Cs_shrinked_data_* read_ri_shrink            :2570-2622 (only its per-atom n_mu: the small ABF basis)
 Binary (FHI-aims) or text (ABACUS) is told apart as the reference does (check_Cs_file_binary,
 check_coulomb_file_binary, :414-453): a file whose first token parses as an integer is text.
 """
@@ -63,11 +65,11 @@ def _cs_headers(fn):
     return out
 
 
-def _basis_from_cs(d: str, nat: int):
+def _basis_from_cs(d: str, nat: int, prefix: str = "Cs_data"):
     """read_basis_from_Cs (read_data.cpp:2083-2152): per atom, n_i and n_mu of blocks where it is
     the first atom and n_j where it is the second."""
     aw, aa = {}, {}
-    for fn in sorted(glob.glob(d + "Cs_data*")):
+    for fn in sorted(glob.glob(d + prefix + "*")):
         for I, J, _r1, _r2, _r3, ni, nj, nmu in _cs_headers(fn):
             aw[I - 1] = ni
             aw[J - 1] = nj
@@ -181,11 +183,17 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
             if np.abs(m).max() >= cs_threshold:
                 Cs[(I - 1, J - 1, (r1, r2, r3))] = m
 
-    Vq = read_coulomb(d, "coulomb_mat", nabf_at)
+    nabf_small = sinvS = None
+    if glob.glob(d + "shrink_sinvS*"):
+        # ABF shrink (use_shrink_abfs): the Coulomb matrix is given in the small basis
+        nabf_small = _basis_from_cs(d, nat, "Cs_shrinked_data")[1]
+        sinvS = read_sinvS(d, "shrink_sinvS")
+    Vq = read_coulomb(d, "coulomb_mat", nabf_small if nabf_small is not None else nabf_at)
 
     return RPAInput(n_spins=ns, n_kpts=nk, n_bands=nb, n_ao=nao, wg=wg, ekb=ekb, efermi=efermi,
                     wfc=wfc, latvec=lat, period=period, kvecs=kv, ibz_map=ibz,
-                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos)
+                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos, nabf_small=nabf_small,
+                    sinvS=sinvS)
 
 
 def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
@@ -239,6 +247,39 @@ def read_coulomb(d: str, prefix: str, nabf_at) -> dict:
                 for J in range(I, nat):
                     Vq[(iq, I, J)] = M[aoff[I]:aoff[I + 1], aoff[J]:aoff[J + 1]].copy()
     return Vq
+
+
+def read_sinvS(d: str, prefix: str) -> dict:
+    """U(q) = sinvS(q) of the ABF shrink, {iq_ibz: (n_small, n_large) complex}: per IBZ q, row
+    blocks [brow, erow] x [bcol, ecol] (1-based) filled row-major (handle_sinvS_file,
+    read_data.cpp:2455-2568, the "for abacus" orientation: rows are the small ABFs)."""
+    d = d.rstrip("/") + "/"
+    U = {}
+    for fn in sorted(glob.glob(d + prefix + "*")):
+        if is_text_file(fn):
+            t = _tokens(fn)
+            p = 1  # n_irk
+            while p + 8 <= len(t):
+                ns_, nl, br, er, bc, ec, iq = (int(x) for x in t[p:p + 7])
+                p += 8  # the q weight follows iq
+                nr, nc = er - br + 1, ec - bc + 1
+                v = np.array([float(x) for x in t[p:p + 2 * nr * nc]]).reshape(nr, nc, 2)
+                p += 2 * nr * nc
+                M = U.setdefault(iq - 1, np.zeros((ns_, nl), complex))
+                M[br - 1:er, bc - 1:ec] = v[..., 0] + 1j * v[..., 1]
+            continue
+        raw = open(fn, "rb").read()
+        _nirk, nloc = struct.unpack_from("<2i", raw, 0)
+        off = 8
+        for _ in range(nloc):
+            ns_, nl, br, er, bc, ec, iq = struct.unpack_from("<7i", raw, off)
+            off += 28 + 8  # q weight
+            nr, nc = er - br + 1, ec - bc + 1
+            blk = np.frombuffer(raw, "<c16", nr * nc, off).reshape(nr, nc)
+            off += 16 * nr * nc
+            M = U.setdefault(iq - 1, np.zeros((ns_, nl), complex))
+            M[br - 1:er, bc - 1:ec] = blk
+    return U
 
 
 def read_vxc(path: str) -> np.ndarray:

@@ -23,12 +23,13 @@ Reference functions followed (paths inside the LibRPA project):
 * E_c, k-points (complex, BLACS form) .... src/core/epsilon.cpp:270-558, log(+-u_ii) at :600-693
 * E_c, Gamma only (real parts) .......... src/core/epsilon.cpp:43-268, :560-598
 * upper atom blocks -> full Hermitian .... src/math/utils_matrix_m_mpi.h:393-455
+* ABF shrink U chi0 U^H (use_shrink_abfs)  src/core/chi0.cpp:711-898, applied at :1110-1137
 """
 from __future__ import annotations
 
 import itertools
 import math
-from dataclasses import dataclass, field
+from dataclasses import dataclass, field, replace
 
 import numpy as np
 import scipy.linalg
@@ -59,6 +60,9 @@ class RPAInput:
     Cs: dict                  # (I, J, (R1,R2,R3)) -> (n_i*n_j, n_mu) row-major
     Vq: dict                  # (ik_full, I, J) with I <= J -> complex (n_mu, n_nu)
     positions: np.ndarray | None = None  # (n_atoms, 3) Cartesian Bohr (screening features only)
+    # ABF shrink (use_shrink_abfs): small ABFs per atom (the basis of Vq then) and U(q) per IBZ q
+    nabf_small: list | None = None
+    sinvS: dict | None = None             # iq_ibz -> (sum nabf_small, sum nabf) complex
 
     @property
     def n_atoms(self):
@@ -75,6 +79,7 @@ class Options:
     vq_threshold: float = 0.0
     libri_chi0_threshold_C: float = 0.0
     libri_chi0_threshold_G: float = 0.0
+    use_shrink_abfs: bool = False
 
 
 # ----------------------------------------------------------------------------- helpers
@@ -438,6 +443,27 @@ def assemble_full(blocks: dict, nb, conj=True, dtype=complex):
     return M
 
 
+def shrink_chi0q(chi0q, sinvS: dict, nabf_large, nabf_small):
+    """shrink_abfs_chi0 (chi0.cpp:711-898) for every (omega, IBZ q): the full chi0(q) of the large
+    ABF basis from its upper atom-pair blocks (Hermitian fill, collect_block_from_ALL_IJ_Tensor),
+    chi0_s = U(q) chi0 U(q)^H (the two pgemm calls, :829-836), and chi0_s's upper atom-pair blocks
+    in the small basis (map_block_to_IJ_storage_new).  The reference applies it to chi0(q, tau)
+    ahead of the cosine transform (:1110-1137); both steps are linear, so applying it to
+    chi0(q, omega) gives the same chi0_s(q, omega)."""
+    offs = np.concatenate([[0], np.cumsum(nabf_small)]).astype(int)
+    na = len(nabf_small)
+    out = []
+    for row in chi0q:
+        orow = []
+        for iq, blocks in enumerate(row):
+            U = sinvS[iq]
+            X = U @ assemble_full(blocks, nabf_large) @ U.conj().T
+            orow.append({(I, J): X[offs[I]:offs[I + 1], offs[J]:offs[J + 1]].copy()
+                         for I in range(na) for J in range(I, na)})
+        out.append(orow)
+    return out
+
+
 def ln_det_pm(M):
     """LU (partial pivot) then sum log(+-u_ii), sign by Re(u_ii) > 0 (epsilon.cpp:578-592, :640-671)."""
     lu, _piv = scipy.linalg.lu_factor(M, check_finite=False)
@@ -539,6 +565,11 @@ def rpa_correlation_energy(inp: RPAInput, opts: Options | None = None, chi0_impl
             if keep_chi0s:
                 chi0s_all.append(chi0s)
             ft_ct_accumulate(chi0q, chi0s, it, grid, klist_ibz, inp.latvec, inp.n_spins, pairs)
-    ec, per_q, terms = correlation_energy(chi0q, inp, grid, ibz_order, ibz_weight, opts)
+    ec_inp, ec_chi0q = inp, chi0q
+    if opts.use_shrink_abfs:
+        # chi0 of the Cs basis -> the small basis of the Coulomb matrix (chi0.cpp:1110-1137)
+        ec_chi0q = shrink_chi0q(chi0q, inp.sinvS, inp.nabf, inp.nabf_small)
+        ec_inp = replace(inp, nabf=list(inp.nabf_small))
+    ec, per_q, terms = correlation_energy(ec_chi0q, ec_inp, grid, ibz_order, ibz_weight, opts)
     return {"ec": ec, "per_q": per_q, "grid": grid, "chi0q": chi0q, "terms": terms,
             "chi0s": chi0s_all, "ibz_order": ibz_order, "ibz_weight": ibz_weight}

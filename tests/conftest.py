@@ -113,6 +113,62 @@ def load_mgo():
     return s
 
 
+_BN_DIR = None
+
+
+def bn_shrink_dir():
+    """The BN shrink dataset (tests/golden/bn_shrink_dataset.tar.gz) extracted once per session."""
+    global _BN_DIR
+    if _BN_DIR is None:
+        import atexit
+        import shutil
+        import tarfile
+        import tempfile
+        td = tempfile.mkdtemp(prefix="bn_shrink_")
+        atexit.register(shutil.rmtree, td, True)
+        with tarfile.open(GOLDEN / "bn_shrink_dataset.tar.gz") as tf:
+            tf.extractall(td, filter="data")
+        _BN_DIR = next(Path(td).rglob("band_out")).parent
+    return _BN_DIR
+
+
+def load_bn_shrink():
+    """The ABACUS BN case with an ABF shrink, read as the reference's driver reads it: Cs in the
+    large ABF basis (60 + 59), the Coulomb matrix in the small basis (17 + 17) and U(q) = sinvS(q)
+    per IBZ point."""
+    from oracle.aims_dataset import read_dataset
+    inp = read_dataset(str(bn_shrink_dir()))
+    return SimpleNamespace(**{k: getattr(inp, k) for k in inp.__dataclass_fields__}, name="bn_shrink",
+                           types=np.zeros(len(inp.nao), int), nfreq=16, minimax_emin=-1.0, minimax_emax=-1.0)
+
+
+def shrunk_copy(s, nabf_small, seed=5, unitary=False):
+    """s with an ABF shrink added: per IBZ point a U(q) of orthonormal rows (a complex unitary
+    when unitary=True and the sizes agree; real at the Gamma point) and the Coulomb matrix taken to
+    the small basis as U V U^H.  With a unitary U, E_c is that of s itself."""
+    import copy
+    from oracle.rpa_oracle import assemble_full
+    rng = np.random.default_rng(seed)
+    t = copy.copy(s)
+    nl, ns_ = int(sum(s.nabf)), int(sum(nabf_small))
+    assert ns_ <= nl and (not unitary or ns_ == nl)
+    gamma = s.n_kpts == 1
+    reps = list(dict.fromkeys(int(x) for x in s.ibz_map))
+    offs = np.concatenate([[0], np.cumsum(nabf_small)]).astype(int)
+    na = len(s.nabf)
+    t.nabf_small, t.sinvS, t.Vq = list(nabf_small), {}, {}
+    for iq, ik in enumerate(reps):
+        A = rng.standard_normal((nl, nl)) + (0 if gamma else 1j * rng.standard_normal((nl, nl)))
+        Q, _ = np.linalg.qr(A)
+        U = Q[:ns_].conj() if not gamma else Q[:ns_].real.copy()
+        t.sinvS[iq] = U
+        V = U @ assemble_full({(I, J): v for (k, I, J), v in s.Vq.items() if k == ik}, s.nabf) @ U.conj().T
+        for I in range(na):
+            for J in range(I, na):
+                t.Vq[(ik, I, J)] = V[offs[I]:offs[I + 1], offs[J]:offs[J + 1]].copy()
+    return t
+
+
 def minimax_ref():
     return json.loads((GOLDEN / "minimax_ref.json").read_text())
 
@@ -125,4 +181,5 @@ def oracle_input(s):
     from oracle.rpa_oracle import RPAInput
     return RPAInput(n_spins=s.n_spins, n_kpts=s.n_kpts, n_bands=s.n_bands, n_ao=s.n_ao, wg=s.wg, ekb=s.ekb,
                     efermi=s.efermi, wfc=s.wfc, latvec=s.latvec, period=s.period, kvecs=s.kvecs,
-                    ibz_map=s.ibz_map, nao=s.nao, nabf=s.nabf, Cs=s.Cs, Vq=s.Vq, positions=s.positions)
+                    ibz_map=s.ibz_map, nao=s.nao, nabf=s.nabf, Cs=s.Cs, Vq=s.Vq, positions=s.positions,
+                    nabf_small=getattr(s, "nabf_small", None), sinvS=getattr(s, "sinvS", None))

@@ -45,8 +45,15 @@ Produces (all committed, so the tests need no reference tree at run time):
                      printed by the reference run (refs/exx_aims_bccHe_k_parallel_libri/librpa/
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
+  bn_shrink_dataset.tar.gz  the ABACUS BN case with an ABF shrink (2 atoms, 2x2x2 k; 60 + 59
+                     ABFs, shrunk to 17 + 17) copied unchanged
+                     (regression_tests/testcases/g0w0_band_abacus_BN_shrink_libri/input_librpa.tar.gz):
+                     Cs of the large basis, Coulomb matrix of the small one, shrink_sinvS, and the
+                     Cs_shrinked_data whose headers give the small basis; the reference prints no
+                     E_c for it
+
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_g0w0 ...].
+h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_g0w0|bn_shrink ...].
 """
 from __future__ import annotations
 
@@ -355,14 +362,21 @@ def he_exx(ref: Path):
     print("he_exx.npz written:", len(tables), "k-points")
 
 
+def bn_shrink(ref: Path):
+    import shutil
+    src = ref / "regression_tests/testcases/g0w0_band_abacus_BN_shrink_libri/input_librpa.tar.gz"
+    shutil.copyfile(src, HERE / "bn_shrink_dataset.tar.gz")
+    print("bn_shrink_dataset.tar.gz written")
+
+
 if __name__ == "__main__":
     src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LIBRPA_REFERENCE")
     if not src:
         sys.exit("usage: make_fixtures.py /path/to/reference [fixture ...] (or set LIBRPA_REFERENCE)")
     ref = Path(src)
     which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "li_dataset", "minimax", "he_bcc", "g0w0",
-                             "li_g0w0", "he_exx", "mgo_g0w0"]
+                             "li_g0w0", "he_exx", "mgo_g0w0", "bn_shrink"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
          "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset, "li_dataset": li_dataset,
-         "mgo_g0w0": mgo_g0w0}[name](ref)
+         "mgo_g0w0": mgo_g0w0, "bn_shrink": bn_shrink}[name](ref)

@@ -111,3 +111,36 @@ def test_coulomb_size_mismatch_is_refused(he_dirs):
     b, _t = he_dirs
     with pytest.raises(ValueError, match="auxiliary"):
         read_coulomb(str(b), "coulomb_mat", [13, 12])
+
+
+def test_driver_reads_the_abf_shrink_without_gpu(lib, tmp_path):
+    """use_shrink_abfs = t on the ABACUS BN shrink dataset: the driver reads the small basis from
+    Cs_shrinked_data, U(q) from shrink_sinvS and the 34 x 34 Coulomb matrix, then stops at the
+    missing GPU (without use_shrink_abfs the Coulomb size is refused with a hint)."""
+    if lib.librpa_gb300_device_count() > 0:
+        pytest.skip("a GPU is visible: the GPU test covers the full run")
+    from conftest import bn_shrink_dir
+    d = bn_shrink_dir()
+    r = _run(lib, d, "use_shrink_abfs = t\n")
+    assert r.returncode == 1 and ("CUDA" in r.stderr or "device" in r.stderr), r.stderr
+    r = _run(lib, d)
+    assert r.returncode == 1 and "use_shrink_abfs = t" in r.stderr, r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_abf_shrink_gives_the_library_ec(lib):
+    """The driver on the BN shrink dataset prints the E_c the library gives through its C API
+    for the same inputs (FP64 chi0, LU form)."""
+    import librpa_gb300 as L
+    from conftest import bn_shrink_dir, load_bn_shrink
+    d = bn_shrink_dir()
+    r = _run(lib, d, "use_shrink_abfs = t\ngb300_chi0_precision = fp64\ngb300_ec_path = lu\n")
+    assert r.returncode == 0, r.stderr
+    ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))
+    s = load_bn_shrink()
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    ref, _ = h.get_rpa_correlation_energy(L.Options(nfreq=16, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                                                    use_shrink_abfs=1), L.n_ibz(s))
+    assert abs(ec - ref) <= 1e-8, (ec, ref)
