@@ -67,8 +67,8 @@ struct T1Group
     int pair, cell;
 };
 
-// A tile: up to 128 consecutive rows of the row groups of one atom J (groups ordered by I,
-// then cell), all contracted with the same C^J operand.
+// A tile: up to 128 consecutive rows of the row groups of one atom J (groups ordered by the NAO
+// count of I, then by I, then cell), all contracted with the same C^J operand.
 struct T1Work
 {
     int J;         // atom of the B operand
@@ -78,6 +78,7 @@ struct T1Work
     int nslot;     // row groups the tile touches
     int kc0, kc1;  // chunks [kc0, kc1) of the supercell axis this CTA contracts
     int split;     // 1: one of several K parts of the tile, added atomically to the output
+    int ra;        // most NAOs of an I atom among the tile's row groups (the producers' i range)
 };
 
 constexpr int T1_MAXSPEC = 8;    // distinct (NAO, ABF) species with their own B maps
@@ -271,6 +272,9 @@ __global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid
             gp[pass] = reinterpret_cast<const float4 *>(gsm) + (static_cast<size_t>(pass) * a.maxcj + slot) * RP * gst / 4;
         const float *Xp[2] = {a.X + a.xsign, a.X};  // pass 0 contracts G(+) with X(-), pass 1 G(-) with X(+)
         // X_b^I[mu i][shift_cJ(col)] for the thread's 4 columns of chunk kc (np passes from pass p0)
+        // The tile's i range: row groups of one NAO count share tiles, so on a tile of small
+        // atoms the loops over i stop at its own count (a CTA-uniform branch), not at RA.
+        const int ira = w.ra;
         auto load_x = [&](int kc, int p0, int np, float4 (&x0)[RA], float4 (&x1)[BOTHX ? RA : 1]) {
             const long long col0 = static_cast<long long>(kc) * CW + cq * 4;
             if (a.vec4)
@@ -284,7 +288,7 @@ __global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid
                 const float *b0 = Xp[p0] + xrow * nsup + src;
 #pragma unroll
                 for (int i = 0; i < RA; ++i)
-                    x0[i] = (i < aI && src >= 0) ? __ldg(reinterpret_cast<const float4 *>(b0 + i * nsup))
+                    if (i < ira) x0[i] = (i < aI && src >= 0) ? __ldg(reinterpret_cast<const float4 *>(b0 + i * nsup))
                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
                 if constexpr (BOTHX)
                     if (np == 2)
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid
                         const float *b1 = Xp[p0 + 1] + xrow * nsup + src;
 #pragma unroll
                         for (int i = 0; i < RA; ++i)
-                            x1[i] = (i < aI && src >= 0) ? __ldg(reinterpret_cast<const float4 *>(b1 + i * nsup))
+                            if (i < ira) x1[i] = (i < aI && src >= 0) ? __ldg(reinterpret_cast<const float4 *>(b1 + i * nsup))
                                                          : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
             }
@@ -314,6 +318,7 @@ __global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid
 #pragma unroll
                     for (int i = 0; i < RA; ++i)
                     {
+                        if (i >= ira) continue;
                         const float *xr = Xb + (xrow + i) * nsup;
                         const bool ri = i < aI;
                         x[i] = make_float4(ri && src[0] >= 0 ? xr[src[0]] : 0.f, ri && src[1] >= 0 ? xr[src[1]] : 0.f,
@@ -331,6 +336,7 @@ __global__ void __launch_bounds__(T1Layout<P2>::threads, 1) k_t1_tc(const __grid
 #pragma unroll
             for (int i = 0; i < RA; ++i)
             {
+                if (i >= ira) continue;
                 // one 16-byte load gives g_ij for the JH = 4 values of j; each is paired {g, g}
                 // in registers as the broadcast operand of the packed FMAs
                 static_assert(JH == 4, "one float4 of G per (i, half stage)");
@@ -955,7 +961,7 @@ struct TcChi0::Impl
     DevBuf<T1Work> work;
     DevBuf<T1Group> groups;
     int n_work = 0, n_groups = 0;
-    std::vector<int> hI, hJ, nabf_h;
+    std::vector<int> hI, hJ, nabf_h, nao_h;
     bool all_active = false;  // the uploaded work list covers every (pair, cell)
     bool has_split = false;   // some tiles are K parts that add into chi0(R) atomically
     int n_sm = 0;
@@ -1099,6 +1105,7 @@ TcChi0::TcChi0(const Geom &g, const Pairs &pr, const double *C, cudaStream_t st)
     m.hI = hI;
     m.hJ = hJ;
     m.nabf_h = nabf;
+    m.nao_h = nao;
     {
         int dev = 0;
         GB_CUDA(cudaGetDevice(&dev));
@@ -1250,7 +1257,11 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
     for (int p = 0; p < pr.n_pairs; ++p) pairs_of[hJ[p]].push_back(p);
     for (int J = 0; J < g.n_at; ++J)
     {
-        std::sort(pairs_of[J].begin(), pairs_of[J].end(), [&](int x, int y) { return hI[x] < hI[y]; });
+        // I atoms of one NAO count next to each other, so that most tiles hold row groups of one
+        // NAO count and their producers loop over that many orbitals i, not over the largest
+        std::sort(pairs_of[J].begin(), pairs_of[J].end(), [&](int x, int y) {
+            return nao_h[hI[x]] != nao_h[hI[y]] ? nao_h[hI[x]] < nao_h[hI[y]] : hI[x] < hI[y];
+        });
         const int gbeg = static_cast<int>(grp.size());
         for (int p : pairs_of[J])
             for (int c = 0; c < g.n_c; ++c)
@@ -1265,7 +1276,9 @@ void TcChi0::Impl::build_work(const unsigned char *active, cudaStream_t st)
         for (const sched::RowTile &r : rt)
         {
             GB_REQUIRE(r.nslot <= maxcj, "chi0 tile touches more row groups than its shared-memory G slots");
-            tiles.push_back(T1Work{J, r.g0, r.r0, r.nrows, r.nslot, 0, nkc, 0});
+            int ra_t = 0;
+            for (int k = 0; k < r.nslot; ++k) ra_t = std::max(ra_t, nao_h[hI[grp[r.g0 + k].pair]]);
+            tiles.push_back(T1Work{J, r.g0, r.r0, r.nrows, r.nslot, 0, nkc, 0, ra_t});
         }
     }
     // launch order: by the I atom of a tile's first row group, so the CTAs resident at one time
