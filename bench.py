@@ -1,4 +1,5 @@
-"""Benchmark: RPA correlation energy of a synthetic cell on one GB300 (or N replicas).
+"""Benchmark: RPA correlation energy of a synthetic cell on one GB300 (or N replicas, or with
+--sharded one E_c split over N ranks by tau and q slices).
 
 One step = one librpa_get_rpa_correlation_energy evaluation of the workload
 (grids, G(R, +-tau) build, chi0 contraction, FT/CT, Pi / log-det / trace).
@@ -13,6 +14,7 @@ One step = one librpa_get_rpa_correlation_energy evaluation of the workload
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                        [--workload fcc16_k333] [--precision bf16x3|fp32|fp64] [--fp64-check auto|on|off]
+                       [--sharded]
 """
 from __future__ import annotations
 
@@ -248,11 +250,30 @@ def run_gb300(args, s, ws, rank, local, dist):
     opts = _opts(L, s)
     h = L.Handler()
     L.load_system(h, s)
-    h.set_gb300_options(L.gb300_options(chi0_precision=prec, device=local, reuse_device_inputs=1))
     nq = L.n_ibz(s)
+
+    def step(reuse):
+        """One E_c through the public API: one call, or with --sharded this rank's tau slice
+        (stage CHI0), the q-keyed reduce-scatter and its q slice's E_c (stage EC).  Returns
+        (E_c, the call's counters; the two stages' summed when sharded)."""
+        if not args.sharded:
+            h.set_gb300_options(L.gb300_options(chi0_precision=prec, device=local, reuse_device_inputs=reuse))
+            e, _ = h.get_rpa_correlation_energy(opts, nq)
+            return e, h.stats()
+        from librpa_gb300.tau_shard import sharded_correlation_energy
+        sts = []
+        e, _ = sharded_correlation_energy(h, opts, nq, stats=sts, chi0_precision=prec, device=local,
+                                          reuse_device_inputs=reuse)
+        st = dict(sts[0])
+        for k, v in sts[1].items():
+            if k.startswith("t_") or k in ("n_launches", "dt_chi0_kernel_ms", "n_chi0_kernel", "chi0_flops",
+                                           "ec_flops", "h2d_bytes", "d2h_bytes"):
+                st[k] = st[k] + v
+        return e, st
+
     ec = None
     for _ in range(max(args.warmup, 1)):
-        ec, _ = h.get_rpa_correlation_energy(opts, nq)
+        ec, _ = step(1)
     # ---- device-resident timed region
     torch.cuda.synchronize()
     _barrier(dist)
@@ -264,8 +285,7 @@ def run_gb300(args, s, ws, rank, local, dist):
         e0.record()
         for _ in range(args.steps):
             lib.librpa_gb300_clear_grid_cache()  # every step fits its minimax grids, as the reference does
-            ec, perq = h.get_rpa_correlation_energy(opts, nq)
-            st = h.stats()
+            ec, st = step(1)
             launches += st["n_launches"]
             chi0_ms += st["dt_chi0_kernel_ms"]
             chi0_n += st["n_chi0_kernel"]
@@ -276,18 +296,16 @@ def run_gb300(args, s, ws, rank, local, dist):
     ms = e0.elapsed_time(e1) / args.steps
     ms = _max_over_ranks(dist, ms)
     # ---- e2e: host buffers, re-staged every step
-    h.set_gb300_options(L.gb300_options(chi0_precision=prec, device=local, reuse_device_inputs=0))
-    h.get_rpa_correlation_energy(opts, nq)
+    step(0)
     torch.cuda.synchronize()
     _barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         lib.librpa_gb300_clear_grid_cache()
-        ec2, _ = h.get_rpa_correlation_energy(opts, nq)
+        ec2, st2 = step(0)
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     e2e_ms = _max_over_ranks(dist, e2e_ms)
-    st2 = h.stats()
     # ---- FP64 plain GPU path (the metric's denominator) and accuracy
     fp64 = None
     if args.fp64_check != "off" and prec != 0:
@@ -323,10 +341,12 @@ def run_gb300(args, s, ws, rank, local, dist):
         cpu = {"value": v, "unit": "s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
     line = {
         "metric": "rpa_ec_wall_time", "value": ms / 1e3, "unit": "s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "strong" if args.sharded else "weak",
         "vs_baseline": None, "dtype": {"bf16x3": "bf16x3/f32acc+f64", "fp32": "f32+f64", "fp64": "f64"}[args.precision],
         "data": "synthetic",
-        "precision": args.precision, "parallelism": f"replicas x{ws}",
+        "precision": args.precision,
+        "parallelism": f"tau/q shards x{ws} (one reduce-scatter of chi0(q, omega))" if args.sharded else f"replicas x{ws}",
         "config": _config(s),
         "ec": ec, "chi0_tflops": ach, "chi0_flops_per_step": chi0_flops / args.steps,
         "t1_choice": {"narrow_producers": st["t1_narrow"], "kparts": st["t1_kparts"]},
@@ -423,6 +443,9 @@ def main():
     ap.add_argument("--fp64-check", default="auto", choices=["auto", "on", "off"])
     ap.add_argument("--fp64-budget-s", type=float, default=90.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sharded", action="store_true",
+                    help="split one E_c over the ranks (tau slices, a q-keyed reduce-scatter, q slices) "
+                         "instead of running independent replicas")
     ap.add_argument("--no-north-star", dest="north_star", action="store_false",
                     help="skip the 256-atom sub-record (default path, FP64 denominator, screening)")
     args = ap.parse_args()

@@ -422,6 +422,31 @@ class Handler:
         if self.lib.librpa_gb300_load_chi0_qw(self.h, a.ctypes.data_as(C.c_void_p), a.size, 0) != 0:
             raise LibrpaError(self.last_error())
 
+    def chi0_qw_tensor(self, device):
+        """The kept chi0(q, omega) as a float64 torch tensor of (re, im) pairs on `device`; a CUDA
+        device gets a device-to-device copy (it must be the handler's GPU)."""
+        import torch
+        n = self.lib.librpa_gb300_chi0_qw_elems(self.h)
+        if n <= 0:
+            raise LibrpaError(self.last_error() or "no chi0(q, omega) kept")
+        t = torch.empty(2 * n, dtype=torch.float64, device=device)
+        if t.is_cuda:
+            torch.cuda.current_stream(t.device).synchronize()
+        if self.lib.librpa_gb300_copy_chi0_qw(self.h, C.c_void_p(t.data_ptr()), int(t.is_cuda)) != 0:
+            raise LibrpaError(self.last_error())
+        return t
+
+    def load_chi0_qw_tensor(self, t):
+        """Replace the kept chi0(q, omega) from a float64 (re, im) torch tensor (host or GPU)."""
+        import torch
+        t = t.contiguous()
+        if t.dtype != torch.float64 or t.numel() % 2:
+            raise LibrpaError("chi0(q, omega) tensor must be float64 (re, im) pairs")
+        if t.is_cuda:
+            torch.cuda.current_stream(t.device).synchronize()
+        if self.lib.librpa_gb300_load_chi0_qw(self.h, C.c_void_p(t.data_ptr()), t.numel() // 2, int(t.is_cuda)) != 0:
+            raise LibrpaError(self.last_error())
+
     def stats(self) -> dict:
         s = GB300Stats()
         self.lib.librpa_gb300_get_stats(self.h, C.byref(s))

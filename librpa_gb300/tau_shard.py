@@ -79,9 +79,41 @@ def reduce_scatter_q(part: np.ndarray, n_w: int, n_q: int, group=None) -> tuple[
     return full.reshape(-1), (b, e)
 
 
-def sharded_correlation_energy(h, opts, n_ibz: int, group=None, **gb_options):
+def reduce_scatter_q_tensor(part, n_w: int, n_q: int, group=None):
+    """reduce_scatter_q on a torch tensor: `part` holds the complex [omega][q][pair blocks]
+    partial as float64 pairs (re, im), on this rank's GPU for NCCL groups or on the host for
+    gloo.  The rank-blocked packing, the collective and the unpacking into the full layout (other
+    q zero) all run where the tensor lives, so an NCCL group never copies chi0 to the host."""
+    import torch
+    import torch.distributed as dist
+
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    a = part.reshape(n_w, n_q, -1)
+    sl = q_slices(n_q, world)
+    width = max(1, max(e - b for b, e in sl))
+    buf = torch.zeros((world, width, n_w, a.shape[2]), dtype=a.dtype, device=a.device)
+    for r, (b, e) in enumerate(sl):
+        buf[r, :e - b] = a[:, b:e, :].transpose(0, 1)
+    if dist.get_backend(group) == "nccl":
+        out = torch.empty(width * n_w * a.shape[2], dtype=a.dtype, device=a.device)
+        dist.reduce_scatter_tensor(out, buf.reshape(-1), op=dist.ReduceOp.SUM, group=group)
+    else:
+        dist.all_reduce(buf, op=dist.ReduceOp.SUM, group=group)
+        out = buf[rank]
+    mine = out.reshape(width, n_w, a.shape[2])
+    b, e = sl[rank]
+    full = torch.zeros_like(a)
+    full[:, b:e, :] = mine[:e - b].transpose(0, 1)
+    return full.reshape(-1), (b, e)
+
+
+def sharded_correlation_energy(h, opts, n_ibz: int, group=None, resident=None, stats=None, **gb_options):
     """E_c with this rank's tau slice and q slice; `h` is a Handler with the system loaded,
     `opts` the LibrpaOptions of the call, gb_options further LibrpaGB300Options fields.
+    resident (default: on for NCCL groups) exchanges chi0(q, omega) as a torch tensor copied
+    device to device out of and back into the library (librpa_gb300_copy_chi0_qw /
+    librpa_gb300_load_chi0_qw with on_device = 1); otherwise through host numpy arrays.
+    stats, a list, receives the handler's counters after each of the two stages.
     Returns (E_c, per-q contributions), identical on every rank."""
     import torch.distributed as dist
 
@@ -91,14 +123,26 @@ def sharded_correlation_energy(h, opts, n_ibz: int, group=None, **gb_options):
     b, e = tau_slices(n_w, world)[rank]
     h.set_gb300_options(gb300_options(**gb_options, tau_begin=b, tau_end=e, stage=STAGE_CHI0))
     h.get_rpa_correlation_energy(opts, n_ibz)
-    part = h.chi0_qw()
+    if stats is not None:
+        stats.append(h.stats())
+    qa, qe = 0, n_ibz
     if world > 1:
-        mine, (qa, qe) = reduce_scatter_q(part, n_w, n_ibz, group)
-    else:
-        mine, (qa, qe) = part, (0, n_ibz)
-    h.load_chi0_qw(mine)
+        nccl = dist.get_backend(group) == "nccl"
+        if resident is None:
+            resident = nccl
+        if resident:
+            import torch
+            dev = torch.device("cuda", torch.cuda.current_device()) if nccl else torch.device("cpu")
+            mine, (qa, qe) = reduce_scatter_q_tensor(h.chi0_qw_tensor(dev), n_w, n_ibz, group)
+            h.load_chi0_qw_tensor(mine)
+        else:
+            mine, (qa, qe) = reduce_scatter_q(h.chi0_qw(), n_w, n_ibz, group)
+            h.load_chi0_qw(mine)
+    # world 1: the kept chi0(q, omega) is already the full sum
     h.set_gb300_options(gb300_options(**gb_options, stage=STAGE_EC, q_begin=qa, q_end=qe))
     _, per_q = h.get_rpa_correlation_energy(opts, n_ibz)
+    if stats is not None:
+        stats.append(h.stats())
     per_q = np.asarray(per_q, np.complex128)
     if world > 1:
         per_q = allreduce_sum(per_q, group)

@@ -75,3 +75,30 @@ def test_q_sliced_ec_stages_add_up(world):
     np.testing.assert_allclose(per_q, full_q, rtol=1e-11, atol=1e-14)
     assert abs(per_q.sum().real - full) <= 1e-12 * abs(full)
 
+
+
+def test_tensor_copies_of_chi0_qw():
+    """The device-resident exchange's copies: chi0(q, omega) copied device to device into a torch
+    tensor equals the host copy bit for bit, and loading a tensor back (here the sum of two tau
+    slices' partials, added on the GPU) gives the unsharded E_c, as the host-array path does."""
+    import torch
+    s = sy.small_periodic(n_atoms=2, nao=[3, 4], nabf=[6, 8], period=(2, 1, 1), nocc=2, seed=9)
+    h = L.Handler()
+    L.load_system(h, s)
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  minimax_emin=s.minimax_emin, minimax_emax=s.minimax_emax)
+    prec = dict(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64)
+    h.set_gb300_options(L.gb300_options(**prec))
+    full, _ = h.get_rpa_correlation_energy(o, L.n_ibz(s))
+    dev = torch.device("cuda", 0)
+    total = None
+    for b, e in tau_slices(s.nfreq, 2):
+        h.set_gb300_options(L.gb300_options(**prec, tau_begin=b, tau_end=e, stage=L.STAGE_CHI0))
+        h.get_rpa_correlation_energy(o, L.n_ibz(s))
+        t = h.chi0_qw_tensor(dev)
+        assert t.is_cuda and np.array_equal(t.cpu().numpy().view(np.complex128), h.chi0_qw())
+        total = t if total is None else total + t
+    h.load_chi0_qw_tensor(total)
+    h.set_gb300_options(L.gb300_options(**prec, stage=L.STAGE_EC))
+    ec, _ = h.get_rpa_correlation_energy(o, L.n_ibz(s))
+    assert abs(ec - full) <= 1e-12 * abs(full), (ec, full)

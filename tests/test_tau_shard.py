@@ -75,8 +75,15 @@ class OracleHandler:
     def load_chi0_qw(self, a):
         self.kept = np.array(a, np.complex128)
 
+    def chi0_qw_tensor(self, device):
+        import torch
+        return torch.from_numpy(self.kept.view(np.float64).copy()).to(device)
 
-def _rank_main(rank, world, port, out_dir):
+    def load_chi0_qw_tensor(self, t):
+        self.kept = t.cpu().numpy().view(np.complex128).copy()
+
+
+def _rank_main(rank, world, port, out_dir, resident=False):
     import sys
     sys.path.insert(0, os.path.dirname(__file__))
     import torch.distributed as dist
@@ -85,7 +92,7 @@ def _rank_main(rank, world, port, out_dir):
         s = _system()
         h = OracleHandler(s)
         opts = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI)
-        ec, per_q = sharded_correlation_energy(h, opts, L.n_ibz(s))
+        ec, per_q = sharded_correlation_energy(h, opts, L.n_ibz(s), resident=resident)
         np.save(os.path.join(out_dir, f"ec{rank}.npy"), np.array([ec]))
         np.save(os.path.join(out_dir, f"perq{rank}.npy"), per_q)
     finally:
@@ -98,10 +105,13 @@ def _free_port():
         return s.getsockname()[1]
 
 
-@pytest.mark.parametrize("world", [2, 3])
-def test_gloo_ranks_sharded_ec_matches_unsharded(tmp_path, lib, world):
+@pytest.mark.parametrize("world,resident", [(2, False), (3, False), (2, True), (3, True)])
+def test_gloo_ranks_sharded_ec_matches_unsharded(tmp_path, lib, world, resident):
+    """resident: the exchange runs on torch tensors (the NCCL path's packing and unpacking, here
+    on host tensors over gloo) instead of numpy arrays."""
     import torch.multiprocessing as mp
-    mp.start_processes(_rank_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    mp.start_processes(_rank_main, args=(world, _free_port(), str(tmp_path), resident), nprocs=world,
+                       start_method="spawn")
     from conftest import oracle_input
     from oracle.rpa_oracle import Options, rpa_correlation_energy
     s = _system()
@@ -115,6 +125,42 @@ def test_gloo_ranks_sharded_ec_matches_unsharded(tmp_path, lib, world):
     assert all(np.array_equal(p, perqs[0]) for p in perqs)
     assert abs(ecs[0] - ref) <= 1e-12 * abs(ref)
     np.testing.assert_allclose(perqs[0], np.asarray(r["per_q"]), rtol=1e-11, atol=1e-15)
+
+
+def _rs_main(rank, world, port, out_dir):
+    import torch
+    import torch.distributed as dist
+    from librpa_gb300.tau_shard import reduce_scatter_q, reduce_scatter_q_tensor
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        rng = np.random.default_rng(rank)
+        part = rng.standard_normal(5 * 7 * 6) + 1j * rng.standard_normal(5 * 7 * 6)
+        a, sa = reduce_scatter_q(part, 5, 7)
+        t, st = reduce_scatter_q_tensor(torch.from_numpy(part.view(np.float64).copy()), 5, 7)
+        assert sa == st
+        np.save(os.path.join(out_dir, f"rs{rank}.npy"), np.stack([a, t.numpy().view(np.complex128)]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_tensor_reduce_scatter_equals_numpy_form(tmp_path):
+    """The tensor form of the q-keyed reduce-scatter gives each rank the numpy form's result, and
+    that result is the sum over ranks on the rank's own q slice, zero elsewhere."""
+    import torch.multiprocessing as mp
+    from librpa_gb300.tau_shard import q_slices
+    world = 3
+    mp.start_processes(_rs_main, args=(world, _free_port(), str(tmp_path)), nprocs=world, start_method="spawn")
+    total = np.zeros(210, complex)
+    for r in range(world):
+        rng = np.random.default_rng(r)
+        total += rng.standard_normal(210) + 1j * rng.standard_normal(210)
+    total = total.reshape(5, 7, 6)
+    for r, (b, e) in enumerate(q_slices(7, world)):
+        got = np.load(tmp_path / f"rs{r}.npy")
+        assert np.array_equal(got[0], got[1])
+        want = np.zeros_like(total)
+        want[:, b:e] = total[:, b:e]
+        np.testing.assert_allclose(got[1].reshape(5, 7, 6), want, rtol=1e-14, atol=1e-14)
 
 
 @pytest.mark.parametrize("n_q,world", [(2, 2), (2, 3), (27, 4), (1, 2)])
