@@ -97,6 +97,9 @@ typedef struct
     int t1_narrow;              /* tensor-core chi0 contraction: 1 = 16 producer warps of 2 columns,
                                    0 = 8 of 4 columns (the tuner's choice for this shape) */
     int t1_kparts;              /* K parts per 128-row tile of that contraction (tuner's choice) */
+    int chi0_precision_used;    /* the chi0 path that ran (LIBRPA_GB300_CHI0_*): BF16X3 requested
+                                   on atoms beyond the tensor-core tiles (more than 32 NAOs or
+                                   128 ABFs) runs the FP32 path */
 } LibrpaGB300Stats;
 
 /* Set defaults. */

@@ -110,6 +110,7 @@ class GB300Stats(C.Structure):
         ("audit_max_dropped", C.c_double), ("dt_chi0_kernel_ms", C.c_double), ("n_chi0_kernel", C.c_longlong),
         ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double), ("screen_fallbacks", C.c_longlong),
         ("ec_lu_fallback_q", C.c_longlong), ("t1_narrow", C.c_int), ("t1_kparts", C.c_int),
+        ("chi0_precision_used", C.c_int),
     ]
 
     def as_dict(self):

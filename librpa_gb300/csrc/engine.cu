@@ -319,7 +319,12 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     // ------------------------------------------------------------ tau loop
     const int nw = tf.n;
     DevBuf<double> d_s(2ull * nk * nb);
-    const int prec = go.chi0_precision;
+    // Atoms beyond the tensor-core contraction's tiles (32 NAOs and 128 ABFs per atom) run the
+    // FP32 path (SIMT contraction, no limit on the ABF count; NAOs up to its shared-memory tile)
+    const int prec = go.chi0_precision == LIBRPA_GB300_CHI0_BF16X3 && (max_nao > 32 || max_nabf > 128)
+                         ? LIBRPA_GB300_CHI0_FP32
+                         : go.chi0_precision;
+    S.chi0_precision_used = prec;
     const bool tc_path = prec == LIBRPA_GB300_CHI0_BF16X3;
     DevBuf<cuDoubleComplex> d_A(tc_path ? 0 : 2ull * nk * nao * nao);
     DevBuf<double> d_G(2ull * nc * nao * nao);

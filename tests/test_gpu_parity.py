@@ -266,3 +266,17 @@ def test_batch_call_equals_single_calls():
     got = L.rpa_correlation_energy_batch(hs, opts, n_threads=4)
     # the K parts of the contraction add into chi0 atomically, in varying order
     np.testing.assert_allclose(got, single, rtol=1e-9, atol=0)
+
+
+def test_atoms_beyond_the_tensor_core_tiles():
+    """An atom with more than 32 NAOs and 128 ABFs (36 and 140 here) is outside the tensor-core
+    contraction's tiles: the default options run the FP32 path instead (reported in the stats)
+    and stay within 0.1 meV/atom of the oracle; the FP64 path matches it to 1e-10."""
+    s = sy.small_periodic(n_atoms=2, nao=[36, 6], nabf=[140, 20], period=(2, 1, 1), nocc=3, seed=11, nfreq=8)
+    o = run_oracle(s)
+    h, ec, _ = run_gpu(s, L.CHI0_BF16X3, ec_path=L.EC_CHOL)
+    assert h.stats()["chi0_precision_used"] == L.CHI0_FP32
+    assert abs(ec - o["ec"].real) <= MEV_PER_ATOM * len(s.nao), (ec, o["ec"])
+    h64, ec64, _ = run_gpu(s, L.CHI0_FP64)
+    assert h64.stats()["chi0_precision_used"] == L.CHI0_FP64
+    assert abs(ec64 - o["ec"].real) <= 1e-10 * abs(o["ec"].real)
