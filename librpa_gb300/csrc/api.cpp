@@ -872,24 +872,9 @@ void prepare_gw(Dataset *ds)
     merge_vq_2d(ds);
 }
 
-// -<psi_n|H_x|psi_n> at Gamma for state n of spin s (exx.cpp:820-860)
-double vexx_state(const Dataset &ds, int s, int n)
-{
-    const int nao = ds.n_ao;
-    const cplx *v = ds.wfc.data() + (static_cast<size_t>(s) * ds.n_states + n) * nao;
-    const std::vector<double> &H = ds.hx[s];
-    double acc = 0.0;
-    for (int p = 0; p < nao; ++p)
-    {
-        cplx hv = 0.0;
-        for (int q = 0; q < nao; ++q) hv += H[static_cast<size_t>(p) * nao + q] * v[q];
-        acc += (std::conj(v[p]) * hv).real();
-    }
-    return -acc;
-}
 } // namespace
 
-// compute_exx.cpp: librpa_build_exx (Gamma-point inputs on the GPU; gw.cu)
+// compute_exx.cpp: librpa_build_exx (H_x(R) on the GPU, k-grids and the Gamma point; gw.cu)
 void librpa_build_exx(LibrpaHandler *h, const LibrpaOptions *p_opts)
 {
     guarded(h, [&] {
@@ -897,7 +882,7 @@ void librpa_build_exx(LibrpaHandler *h, const LibrpaOptions *p_opts)
         clear_error(ds);
         GB_REQUIRE(p_opts, "null options");
         prepare_gw(ds);
-        gb::build_exx_gamma(*ds, *p_opts);
+        gb::build_exx(*ds, *p_opts);
     });
 }
 
@@ -914,19 +899,19 @@ void librpa_get_exx_pot_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, con
         i_state_high = std::min(ds->n_states, i_state_high);
         GB_REQUIRE(n_spins == ds->n_spins, "parsed nspins is not consistent with the SCF starting point");
         if (i_state_high <= i_state_low) return;
-        if (ds->hx.empty() || ds->exx_generation != ds->generation)
+        if (ds->hx_r.empty() || ds->exx_generation != ds->generation)
         {
             prepare_gw(ds);
-            gb::build_exx_gamma(*ds, *p_opts);
+            gb::build_exx(*ds, *p_opts);
         }
         const int nc = i_state_high - i_state_low;
+        for (int k = 0; k < n_kpts_this; ++k)
+            GB_REQUIRE(iks_this[k] >= 0 && iks_this[k] < ds->n_kpts, "k-point index out of range");
         for (int isp = 0; isp < n_spins; ++isp)
             for (int k = 0; k < n_kpts_this; ++k)
-            {
-                GB_REQUIRE(iks_this[k] == 0, "the Gamma-point exchange has k-point 0 only");
                 for (int i = 0; i < nc; ++i)
-                    vexx[(static_cast<size_t>(isp) * n_kpts_this + k) * nc + i] = vexx_state(*ds, isp, i_state_low + i);
-            }
+                    vexx[(static_cast<size_t>(isp) * n_kpts_this + k) * nc + i] =
+                        gb::exx_state(*ds, isp, iks_this[k], i_state_low + i);
     });
 }
 

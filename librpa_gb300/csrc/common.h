@@ -102,6 +102,15 @@ private:
     size_t n_ = 0;
 };
 
+// A device copy of a host vector, staged on stream st.
+template <typename T>
+DevBuf<T> to_dev(const std::vector<T> &h, cudaStream_t st)
+{
+    DevBuf<T> d(h.size());
+    d.upload(h.data(), h.size(), st);
+    return d;
+}
+
 // Per-device one-time set-up (kernel attributes act on the current device only).  The
 // caller keeps one PerDeviceOnce per set-up step; run() calls f() the first time it is used
 // with a given device current, and is safe to call from several host threads.

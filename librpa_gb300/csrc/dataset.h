@@ -87,7 +87,9 @@ struct Dataset
     std::map<int, ShrinkU> shrink_u;
 
     // Gamma-point exchange and G0W0 results (gw.cu), valid while generation is unchanged
-    std::vector<std::vector<double>> hx;       // per spin: H_x, n_ao x n_ao
+    std::vector<std::vector<double>> hx;       // per spin: H_x(R = 0), n_ao x n_ao
+    std::vector<std::vector<double>> hx_r;     // per spin: H_x(R) [cell][n_ao][n_ao]
+    std::vector<std::array<int, 3>> hx_cells;  // the cells R of hx_r
     std::vector<std::vector<cplx>> sigc_ks;    // per spin: Sigma_c(i omega) on the KS states, [n][omega]
     std::vector<double> gw_omega;              // the imaginary frequencies of sigc_ks
     unsigned long long exx_generation = 0, g0w0_generation = 0;

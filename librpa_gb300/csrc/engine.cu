@@ -40,14 +40,6 @@ namespace gb {
 
 namespace {
 
-template <typename T>
-DevBuf<T> to_dev(const std::vector<T> &h, cudaStream_t st)
-{
-    DevBuf<T> d(h.size());
-    d.upload(h.data(), h.size(), st);
-    return d;
-}
-
 struct EventTimer
 {
     cudaEvent_t a = nullptr, b = nullptr;

@@ -22,13 +22,17 @@
 // this formulation to cells of a few hundred orbitals; larger cells need the atom-pair-sparse
 // form of the χ0 contraction.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
+#include <map>
 #include <vector>
 
 #include "common.h"
+#include "cs_fold.h"
 #include "dataset.h"
 #include "gw.h"
+#include "host_tables.h"
 #include "kernels.h"
 #include "minimax.h"
 
@@ -317,16 +321,53 @@ std::vector<double> coulomb_gamma(const std::vector<VqBlock> &blocks, const std:
     return V;
 }
 
+// The Born-von Karman supercell of the k-grid: atom (c, I) for cell c of the BvK list and atom
+// I, cell-major.  Every k-grid quantity of the exchange and of Sigma_c is the Gamma-point
+// quantity of this supercell, its matrices built from the cell-periodic blocks,
+//   X_s[(c, A)][(c', B)] = X(R_c' - R_c)_AB,
+// with the cell arithmetic of LibRI's periodic keys (BvK modulo, LRI_Cal_Tools.h:44-60).  With one
+// k-point the supercell is the cell itself.
 struct GammaSetup
 {
-    int n_at = 0, N = 0, nao = 0;
-    std::vector<int> abf_off, ao_off;
-    DevBuf<double> U;  // [(a, p), r]
+    int n_at = 0, N = 0, nao = 0;      // supercell ABF and NAO counts (N = nc Nc, nao = nc naoc)
+    int nc = 1, Nc = 0, naoc = 0, c0 = 0;  // cells, per-cell ABF and NAO counts, the cell R = 0
+    std::vector<int> abf_off, ao_off;  // per atom of one cell
+    std::vector<int> cdiff;            // [a][b]: cell of R_a - R_b
+    std::vector<std::array<int, 3>> cells;
+    DevBuf<double> U;                  // [(a, p), r] over the supercell
 };
 
-// U[a][p][r] = T[a][p][r] + T[a][r][p], T from the RI blocks folded to the Gamma cell (every cell
-// vector folds onto R = 0 with one k-point), blocks with max |C| <= thr dropped after folding
-// (LibRI set_tensors, RI_Tools.hpp:49-67, LRI-set.hpp:33-75).
+// U_s[a][p][r] += C, U_s[a][r][p] += C for the folded block (I, K, cell R) placed at every cell c:
+// a = (c, I, mu), p = (c, I, i), r = (c + R, K, k).  At most the two writes of one block meet on an
+// element (I = K, R = 0, i = k), so the atomic adds give the same sum in any order.
+__global__ void k_super_u(const double *__restrict__ blob, const long long *__restrict__ off,
+                          const int *__restrict__ meta, const int *__restrict__ nao_at, const int *__restrict__ nabf_at,
+                          const int *__restrict__ ao_off, const int *__restrict__ abf_off,
+                          const int *__restrict__ cadd, int nc, int Nc, int naoc, double *__restrict__ U)
+{
+    const int b = blockIdx.x, c = blockIdx.y;
+    const int I = meta[4 * b], K = meta[4 * b + 1], R = meta[4 * b + 2];
+    const int ni = nao_at[I], nk = nao_at[K], nmu = nabf_at[I];
+    const int cK = cadd[c * nc + R];
+    const long long naos = static_cast<long long>(nc) * naoc;
+    const double *f = blob + off[b];
+    const long long n = static_cast<long long>(ni) * nk * nmu;
+    for (long long t = threadIdx.x; t < n; t += blockDim.x)
+    {
+        // block layout: (i * n_k + k) * n_mu + mu  (input.cpp:525-541)
+        const int mu = static_cast<int>(t % nmu), k = static_cast<int>((t / nmu) % nk), i = static_cast<int>(t / (static_cast<long long>(nmu) * nk));
+        const double v = f[t];
+        const long long a = static_cast<long long>(c) * Nc + abf_off[I] + mu;
+        const long long p = static_cast<long long>(c) * naoc + ao_off[I] + i;
+        const long long r = static_cast<long long>(cK) * naoc + ao_off[K] + k;
+        atomicAdd(U + (a * naos + p) * naos + r, v);
+        atomicAdd(U + (a * naos + r) * naos + p, v);
+    }
+}
+
+// The supercell of the handler's k-grid and its dense U from the RI blocks, folded onto the BvK
+// cells and filtered by max |C| > thr after folding (LibRI set_tensors, RI_Tools.hpp:49-67,
+// LRI-set.hpp:33-75).
 void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
 {
     const int n_at = ds.n_atoms();
@@ -340,47 +381,148 @@ void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
         gs.abf_off[I + 1] = gs.abf_off[I] + ds.nabf_at[I];
         gs.ao_off[I + 1] = gs.ao_off[I] + ds.nao_at[I];
     }
-    gs.N = gs.abf_off[n_at];
-    gs.nao = gs.ao_off[n_at];
-    GB_REQUIRE(gs.nao == ds.n_ao, "sum of per-atom NAOs differs from the mean-field basis size");
-    const int N = gs.N, nao = gs.nao;
+    gs.Nc = gs.abf_off[n_at];
+    gs.naoc = gs.ao_off[n_at];
+    GB_REQUIRE(gs.naoc == ds.n_ao, "sum of per-atom NAOs differs from the mean-field basis size");
+    const PhaseTables pt = build_phase_tables(ds);
+    gs.nc = pt.nc;
+    gs.cells = pt.cells.R;
+    gs.cdiff = pt.cdiff;
+    gs.c0 = pt.cells.find(0, 0, 0);
+    GB_REQUIRE(gs.c0 >= 0, "the BvK cell list lacks R = 0");
+    gs.N = gs.nc * gs.Nc;
+    gs.nao = gs.nc * gs.naoc;
+    const int N = gs.N, nao = gs.nao, nc = gs.nc;
     GB_REQUIRE(static_cast<double>(N) * nao * nao <= 2.0e9,
-               "the Gamma-point G0W0/EXX path holds the dense RI tensor (N_abf n_ao^2 values): input too large");
-    // fold blocks per (I, K) and filter
-    std::vector<std::vector<double>> folded(static_cast<size_t>(n_at) * n_at);
+               "the G0W0/exchange path holds the dense RI tensor of the BvK supercell (N_abf n_ao^2 values, "
+               "times the cell count cubed on a k-grid): input too large");
     for (const CsBlock &b : ds.cs_blocks)
-    {
         GB_REQUIRE(b.ni == ds.nao_at[b.I] && b.nj == ds.nao_at[b.J] && b.nmu == ds.nabf_at[b.I],
                    "RI block dimensions inconsistent with the bases");
-        std::vector<double> &f = folded[static_cast<size_t>(b.I) * n_at + b.J];
-        const size_t n = static_cast<size_t>(b.ni) * b.nj * b.nmu;
-        if (f.empty()) f.assign(n, 0.0);
-        for (size_t t = 0; t < n; ++t) f[t] += ds.cs_blob[b.offset + t];
+    const Cells &cells = pt.cells;
+    CsFold f = fold_cs_blocks(
+        ds.cs_blocks, ds.cs_blob.data(), ds.cs_blob.size(), ds.period,
+        [&](const std::array<int, 3> &R) { return cells.find(R[0], R[1], R[2]); }, thr);
+    // cadd[c][R]: cell of R_c + R_R
+    std::vector<int> cadd(static_cast<size_t>(nc) * nc);
+    for (int c = 0; c < nc; ++c)
+        for (int r = 0; r < nc; ++r)
+            cadd[static_cast<size_t>(c) * nc + r] = cells.find(cells.R[c][0] + cells.R[r][0], cells.R[c][1] + cells.R[r][1],
+                                                               cells.R[c][2] + cells.R[r][2]);
+    gs.U.alloc(static_cast<size_t>(N) * nao * nao);
+    gs.U.zero(st);
+    const int nblk = static_cast<int>(f.off.size());
+    if (nblk > 0)
+    {
+        DevBuf<double> blob(ds.cs_blob.size() + f.extra.size());
+        blob.upload(ds.cs_blob.data(), ds.cs_blob.size(), st);
+        if (!f.extra.empty())
+            GB_CUDA(cudaMemcpyAsync(blob.get() + ds.cs_blob.size(), f.extra.data(), f.extra.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, st));
+        auto d_off = to_dev(f.off, st);
+        auto d_meta = to_dev(f.meta, st);
+        auto d_nao = to_dev(ds.nao_at, st);
+        auto d_nabf = to_dev(ds.nabf_at, st);
+        auto d_aoo = to_dev(gs.ao_off, st);
+        auto d_abo = to_dev(gs.abf_off, st);
+        auto d_cadd = to_dev(cadd, st);
+        k_super_u<<<dim3(nblk, nc), 256, 0, st>>>(blob.get(), d_off.get(), d_meta.get(), d_nao.get(), d_nabf.get(),
+                                                  d_aoo.get(), d_abo.get(), d_cadd.get(), nc, gs.Nc, gs.naoc, gs.U.get());
+        GB_LAUNCH_CHECK();
+        GB_CUDA(cudaStreamSynchronize(st));  // the staged tables go out of scope
     }
-    std::vector<double> T(static_cast<size_t>(N) * nao * nao, 0.0);
-    for (int I = 0; I < n_at; ++I)
-        for (int K = 0; K < n_at; ++K)
+}
+
+// X_s[(c a)][(c' b)] = XR[cell of R_c' - R_c][a][b] for the cell-periodic blocks XR [cell][n][n].
+std::vector<double> to_supercell(const std::vector<double> &XR, int n, const GammaSetup &gs)
+{
+    const int nc = gs.nc;
+    const size_t ns = static_cast<size_t>(nc) * n;
+    std::vector<double> Xs(ns * ns);
+    for (int c = 0; c < nc; ++c)
+        for (int d = 0; d < nc; ++d)
         {
-            const std::vector<double> &f = folded[static_cast<size_t>(I) * n_at + K];
-            if (f.empty()) continue;
-            double mx = 0.0;
-            for (double v : f) mx = std::max(mx, std::fabs(v));
-            if (thr > 0.0 && mx <= thr) continue;
-            const int ni = ds.nao_at[I], nk = ds.nao_at[K], nmu = ds.nabf_at[I];
-            // block layout: (i * n_k + k) * n_mu + mu  (input.cpp:525-541)
-            for (int i = 0; i < ni; ++i)
-                for (int k = 0; k < nk; ++k)
-                    for (int mu = 0; mu < nmu; ++mu)
-                    {
-                        const double v = f[(static_cast<size_t>(i) * nk + k) * nmu + mu];
-                        const size_t a = gs.abf_off[I] + mu, p = gs.ao_off[I] + i, r = gs.ao_off[K] + k;
-                        T[(a * nao + p) * nao + r] += v;
-                        T[(a * nao + r) * nao + p] += v;
-                    }
+            const double *src = XR.data() + static_cast<size_t>(gs.cdiff[static_cast<size_t>(d) * nc + c]) * n * n;
+            for (int a = 0; a < n; ++a)
+                std::copy(src + static_cast<size_t>(a) * n, src + static_cast<size_t>(a + 1) * n,
+                          Xs.data() + (static_cast<size_t>(c) * n + a) * ns + static_cast<size_t>(d) * n);
         }
-    gs.U.alloc(T.size());
-    gs.U.upload(T.data(), T.size(), st);
-    GB_CUDA(cudaStreamSynchronize(st));
+    return Xs;
+}
+
+// Theta[k][c] = 2 pi kfrac_k . R_c
+double k_dot_r(const Dataset &ds, int k, const std::array<int, 3> &R)
+{
+    return 2.0 * M_PI * (ds.kfrac[3 * k] * R[0] + ds.kfrac[3 * k + 1] * R[1] + ds.kfrac[3 * k + 2] * R[2]);
+}
+
+// V(R) [cell][N][N] = Re sum_k e^{-i 2 pi k.R} V(k) / n_k over the full k list, V(k) the full
+// Hermitian matrix of the IBZ representative's upper blocks, conjugated for the other members of
+// its star (FT_Vq, src/core/coulmat.cpp:7-90).
+std::vector<double> coulomb_r(const Dataset &ds, const std::vector<VqBlock> &blocks, const std::vector<cplx> &blob,
+                              const GammaSetup &gs)
+{
+    const int N = gs.Nc, nc = gs.nc, nk = ds.n_kpts;
+    std::map<int, std::vector<cplx>> Vrep;
+    for (const VqBlock &b : blocks)
+    {
+        if (b.I > b.J) continue;
+        std::vector<cplx> &M = Vrep[b.ik];
+        if (M.empty()) M.assign(static_cast<size_t>(N) * N, cplx(0, 0));
+        for (int m = 0; m < b.nmu; ++m)
+            for (int n = 0; n < b.nnu; ++n)
+            {
+                const cplx v = blob[b.offset + static_cast<size_t>(m) * b.nnu + n];
+                M[static_cast<size_t>(gs.abf_off[b.I] + m) * N + gs.abf_off[b.J] + n] = v;
+                M[static_cast<size_t>(gs.abf_off[b.J] + n) * N + gs.abf_off[b.I] + m] = std::conj(v);
+            }
+    }
+    std::vector<double> VR(static_cast<size_t>(nc) * N * N, 0.0);
+    for (int k = 0; k < nk; ++k)
+    {
+        const int rep = ds.ibz_map[k];
+        auto it = Vrep.find(rep);
+        if (it == Vrep.end()) continue;
+        const bool cj = rep != k;
+        for (int c = 0; c < nc; ++c)
+        {
+            const double th = k_dot_r(ds, k, gs.cells[c]);
+            const cplx ph = std::polar(1.0 / nk, -th);
+            double *dst = VR.data() + static_cast<size_t>(c) * N * N;
+            for (size_t e = 0; e < static_cast<size_t>(N) * N; ++e)
+                dst[e] += (ph * (cj ? std::conj(it->second[e]) : it->second[e])).real();
+        }
+    }
+    return VR;
+}
+
+// D(R) [cell][nao][nao] = Re sum_k e^{-i 2 pi k.R} D(k), D(k)_ij = sum_n w_n psi_ni conj(psi_nj)
+// with w = wg n_s / 2 (wg already divided by n_k), states up to the first below 1e-4 / n_k
+// (MeanField::get_dmat_cplx_R, src/core/meanfield.cpp:201-244).
+std::vector<double> dmat_r(const Dataset &ds, int s, const GammaSetup &gs)
+{
+    const int nao = gs.naoc, nc = gs.nc, nk = ds.n_kpts, nb = ds.n_states, ns = ds.n_spins;
+    std::vector<double> DR(static_cast<size_t>(nc) * nao * nao, 0.0);
+    std::vector<cplx> Dk(static_cast<size_t>(nao) * nao);
+    for (int k = 0; k < nk; ++k)
+    {
+        std::fill(Dk.begin(), Dk.end(), cplx(0, 0));
+        for (int n = 0; n < nb; ++n)
+        {
+            const double w = ds.wg[(static_cast<size_t>(s) * nk + k) * nb + n] * 0.5 * ns;
+            if (w < 1e-4 / nk) break;
+            const cplx *v = ds.wfc.data() + ((static_cast<size_t>(s) * nk + k) * nb + n) * nao;
+            for (int i = 0; i < nao; ++i)
+                for (int j = 0; j < nao; ++j) Dk[static_cast<size_t>(i) * nao + j] += w * v[i] * std::conj(v[j]);
+        }
+        for (int c = 0; c < nc; ++c)
+        {
+            const cplx ph = std::polar(1.0, -k_dot_r(ds, k, gs.cells[c]));
+            double *dst = DR.data() + static_cast<size_t>(c) * nao * nao;
+            for (size_t e = 0; e < Dk.size(); ++e) dst[e] += (ph * Dk[e]).real();
+        }
+    }
+    return DR;
 }
 
 // H[p][q] = sum U[a,p,r] W[a,b] U[b,q,s] D[r,s] for each of nd matrices D (nd <= 2); Z = W U is
@@ -427,9 +569,11 @@ void require_gamma(const Dataset &ds)
 
 } // namespace
 
-void build_exx_gamma(Dataset &ds, const LibrpaOptions &opts)
+void build_exx(Dataset &ds, const LibrpaOptions &opts)
 {
-    require_gamma(ds);
+    GB_REQUIRE(ds.n_spinor == 1, "spinor (SOC) wave functions are not supported");
+    GB_REQUIRE(ds.occ_set, "occupations/eigenvalues not set");
+    for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some (spin, k)");
     GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
     GB_CUDA(cudaSetDevice(ds.gbopt.device));
     cudaStream_t st;
@@ -441,37 +585,63 @@ void build_exx_gamma(Dataset &ds, const LibrpaOptions &opts)
     } guard{st};
     GammaSetup gs;
     setup_gamma(ds, opts.libri_exx_threshold_C, gs, st);
-    const int N = gs.N, nao = gs.nao, nb = ds.n_states, ns = ds.n_spins;
-    const std::vector<double> vc = coulomb_gamma(ds.vq_cut_blocks, ds.vq_cut_blob, gs.abf_off, N);
-    DevBuf<double> dV(vc.size()), dD(static_cast<size_t>(nao) * nao), dH(static_cast<size_t>(nao) * nao), ds_w(nb);
-    dV.upload(vc.data(), vc.size(), st);
-    DevBuf<cuDoubleComplex> dpsi(static_cast<size_t>(nb) * nao);
+    const int nao = gs.nao, naoc = gs.naoc, nc = gs.nc, ns = ds.n_spins;
+    const std::vector<double> vs = to_supercell(coulomb_r(ds, ds.vq_cut_blocks, ds.vq_cut_blob, gs), gs.Nc, gs);
+    const long long nn = static_cast<long long>(nao) * nao;
+    DevBuf<double> dV(vs.size()), dD(nn), dH(nn);
+    dV.upload(vs.data(), vs.size(), st);
+    std::vector<double> hs(nn);
     HsWork wk;
     ds.hx.assign(ns, {});
+    ds.hx_r.assign(ns, {});
     for (int s = 0; s < ns; ++s)
     {
-        // density-matrix weights: wg n_s/2 per state, up to the first below 1e-4/n_k
-        // (meanfield.cpp:201-228; wg is stored already divided by n_k)
-        std::vector<double> w(nb, 0.0);
-        for (int n = 0; n < nb; ++n)
-        {
-            const double v = ds.wg[static_cast<size_t>(s) * nb + n] * 0.5 * ns;
-            if (v < 1e-4 / ds.n_kpts) break;
-            w[n] = v;
-        }
-        ds_w.upload(w.data(), nb, st);
-        dpsi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()) + static_cast<size_t>(s) * nb * nao,
-                    static_cast<size_t>(nb) * nao, st);
-        k_gamma_dm<<<(nao * nao + 255) / 256, 256, 0, st>>>(dpsi.get(), ds_w.get(), nb, nao, 1.0, dD.get());
-        GB_LAUNCH_CHECK();
+        const std::vector<double> dsup = to_supercell(dmat_r(ds, s, gs), naoc, gs);
+        dD.upload(dsup.data(), dsup.size(), st);
         const double *Dp[1] = {dD.get()};
         double *Hp[1] = {dH.get()};
         hs_closed_form(gs, dV.get(), Dp, 1, Hp, wk, st);
-        ds.hx[s].resize(static_cast<size_t>(nao) * nao);
-        dH.download(ds.hx[s].data(), ds.hx[s].size(), st);
+        dH.download(hs.data(), hs.size(), st);
         GB_CUDA(cudaStreamSynchronize(st));
+        // H(R_c)_KL: the supercell row block of the cell R = 0, column block of cell c
+        std::vector<double> &hr = ds.hx_r[s];
+        hr.resize(static_cast<size_t>(nc) * naoc * naoc);
+        for (int c = 0; c < nc; ++c)
+            for (int K = 0; K < naoc; ++K)
+                std::copy(hs.data() + (static_cast<size_t>(gs.c0) * naoc + K) * nao + static_cast<size_t>(c) * naoc,
+                          hs.data() + (static_cast<size_t>(gs.c0) * naoc + K) * nao + static_cast<size_t>(c + 1) * naoc,
+                          hr.data() + (static_cast<size_t>(c) * naoc + K) * naoc);
+        ds.hx[s].assign(hr.begin() + static_cast<size_t>(gs.c0) * naoc * naoc,
+                        hr.begin() + static_cast<size_t>(gs.c0 + 1) * naoc * naoc);
     }
+    ds.hx_cells = gs.cells;
     ds.exx_generation = ds.generation;
+}
+
+double exx_state(const Dataset &ds, int s, int k, int n)
+{
+    const int nao = ds.n_ao, nk = ds.n_kpts;
+    GB_REQUIRE(s >= 0 && s < static_cast<int>(ds.hx_r.size()) && k >= 0 && k < nk && n >= 0 && n < ds.n_states,
+               "exchange state index out of range");
+    const std::vector<double> &hr = ds.hx_r[s];
+    const int nc = static_cast<int>(ds.hx_cells.size());
+    // H(k) = sum_c e^{i 2 pi k.R_c} H(R_c) (Exx::build_KS_kgrid, src/core/exx.cpp:720-860)
+    std::vector<cplx> Hk(static_cast<size_t>(nao) * nao, cplx(0, 0));
+    for (int c = 0; c < nc; ++c)
+    {
+        const cplx ph = std::polar(1.0, k_dot_r(ds, k, ds.hx_cells[c]));
+        const double *src = hr.data() + static_cast<size_t>(c) * nao * nao;
+        for (size_t e = 0; e < Hk.size(); ++e) Hk[e] += ph * src[e];
+    }
+    const cplx *v = ds.wfc.data() + ((static_cast<size_t>(s) * nk + k) * ds.n_states + n) * nao;
+    cplx acc(0, 0);
+    for (int p = 0; p < nao; ++p)
+    {
+        cplx hv(0, 0);
+        for (int q = 0; q < nao; ++q) hv += Hk[static_cast<size_t>(p) * nao + q] * v[q];
+        acc += std::conj(v[p]) * hv;
+    }
+    return -acc.real();
 }
 
 void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)

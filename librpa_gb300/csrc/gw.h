@@ -1,4 +1,4 @@
-// Exact exchange and G0W0 self-energy at the Gamma point on the GPU (gw.cu).
+// Exact exchange (k-grids) and the G0W0 self-energy (Gamma point) on the GPU (gw.cu).
 #pragma once
 
 #include "../../include/librpa_options.h"
@@ -8,9 +8,13 @@ namespace gb {
 struct Dataset;
 struct TimeFreqGrids;
 
-// H_x per spin (n_ao x n_ao, Hartree) into ds.hx: LibRI Exx::cal_Hs at Gamma with the density
-// matrix and the truncated Coulomb matrix.
-void build_exx_gamma(Dataset &ds, const LibrpaOptions &opts);
+// H_x(R) per spin into ds.hx_r ([cell][n_ao][n_ao], Hartree; the cells in ds.hx_cells) and
+// H_x(R = 0) into ds.hx: LibRI Exx::cal_Hs with the density matrix D(R) and the truncated Coulomb
+// matrix V(R) of the k-grid (one cell at the Gamma point), as the Gamma-point closed form of the
+// Born-von Karman supercell.
+void build_exx(Dataset &ds, const LibrpaOptions &opts);
+// v_exx of state n of spin s at k-point k (SCF grid), after build_exx: -<psi|H_x(k)|psi>.
+double exx_state(const Dataset &ds, int s, int k, int n);
 // Sigma_c(i omega) on the KS states per spin into ds.sigc_ks ([state][omega]) and the imaginary
 // frequencies into ds.gw_omega.
 void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);

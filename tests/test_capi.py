@@ -136,15 +136,17 @@ def test_invalid_routing_is_rejected_before_any_gpu_work(lib):
             h.get_rpa_correlation_energy(L.Options(nfreq=16, tfgrids_type=L.Minimax, parallel_routing=7), 1)
 
 
-def test_g0w0_and_exchange_reject_k_grids_before_any_gpu_work(lib):
-    """The GPU exchange and G0W0 chain covers Gamma-point inputs; a k-grid input (MgO, 3x3x3) is
-    refused with a message, as is a Gamma input without the truncated Coulomb matrix."""
+def test_g0w0_and_exchange_input_checks_before_any_gpu_work(lib):
+    """The exchange takes k-grid inputs (MgO, 3x3x3) and reaches the GPU (here: none); the G0W0
+    chain covers Gamma-point inputs and refuses the k-grid with a message, as the exchange refuses
+    an input without the truncated Coulomb matrix."""
     from conftest import load_mgo
     s = load_mgo()
     with L.Handler() as h:
         L.load_system(h, s)
-        with pytest.raises(L.LibrpaError, match="Gamma-point inputs"):
-            h.get_exx_pot_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4)
+        if lib.librpa_gb300_device_count() == 0:
+            with pytest.raises(L.LibrpaError, match="CUDA|device"):
+                h.get_exx_pot_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4)
         with pytest.raises(L.LibrpaError, match="Gamma-point inputs"):
             h.get_g0w0_sigc_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4, np.zeros(4), np.zeros(4))
     s = load_h2o()

@@ -1,12 +1,12 @@
-"""Exchange and G0W0 at the Gamma point on the GPU through the C ABI (librpa_get_exx_pot_kgrid,
-librpa_get_g0w0_sigc_kgrid), against the reference's own quasi-particle tables and the CPU
-oracle (needs a GB300)."""
+"""Exchange (k-grids and the Gamma point) and G0W0 (Gamma point) on the GPU through the C ABI
+(librpa_get_exx_pot_kgrid, librpa_get_g0w0_sigc_kgrid), against the reference's own tables and
+the CPU oracle (needs a GB300)."""
 import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_h2o_g0w0, load_li_g0w0, oracle_input
-from oracle.gw_oracle import HA2EV, g0w0_gamma
+from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
+from oracle.gw_oracle import HA2EV, exx_kgrid, g0w0_gamma
 from oracle.rpa_oracle import Options as OOpts
 
 pytestmark = pytest.mark.gpu
@@ -91,3 +91,29 @@ def test_li_spin_polarised_table():
         got = np.c_[vexx[sp] * HA2EV, sig[sp].real * HA2EV, sig[sp].imag * HA2EV]
         np.testing.assert_allclose(got, t[:, 4:7], rtol=0, atol=6e-6, err_msg=f"spin {sp}")
         np.testing.assert_allclose(e_qp[sp] * HA2EV, t[:, 7], rtol=0, atol=3e-5)
+
+
+def _vexx_kgrid(s):
+    h = L.Handler()
+    L.load_system(h, s)
+    return h.get_exx_pot_kgrid(L.Options(nfreq=16, tfgrids_type=L.Minimax), s.n_spins, list(range(s.n_kpts)), 0,
+                               s.n_bands)
+
+
+def test_periodic_exchange_bcc_he_every_k_point():
+    """BCC He (2-atom cell, 2x2x2 k-points, C blocks given on cells [0, 2) that LibRI folds): v_exx
+    of all 8 bands at all 8 k-points against the reference's table
+    (refs/exx_aims_bccHe_k_parallel_libri, 5 decimals in Hartree) and the oracle (1e-10)."""
+    s = load_he_exx()
+    got = _vexx_kgrid(s)
+    np.testing.assert_allclose(got[0], s.exx_tables[:, :, 1], rtol=0, atol=6e-6)
+    np.testing.assert_allclose(got, exx_kgrid(oracle_input(s), s.v_cut), rtol=0, atol=1e-10)
+
+
+def test_periodic_exchange_mgo_ibz_reduced():
+    """MgO (3x3x3 k-points, 14 irreducible by time reversal, the truncated Coulomb given at those
+    only): v_exx of all 17 states at all 27 k-points against the reference's G0W0 table
+    (refs/g0w0_aims_MgO_libri, 5 decimals in eV)."""
+    s = load_mgo()
+    got = _vexx_kgrid(s)
+    np.testing.assert_allclose(got[0] * HA2EV, s.qp_tables[:, :, 4], rtol=0, atol=6e-6)
