@@ -182,6 +182,7 @@ def load_library(path: str | Path | None = None):
         "librpa_set_lri_coeff": (None, [vp, i, i, i, i, i, i, _ip, _dp]),
         "librpa_set_aux_bare_coulomb_k_atom_pair": (None, [vp, i, i, i, i, i, _dp, _dp, d]),
         "librpa_set_aux_bare_coulomb_k_2d_block": (None, [vp, i, i, i, i, i, _dp, _dp]),
+        "librpa_set_dielect_func_imagfreq": (None, [vp, i, _dp, _dp]),
         "librpa_get_imaginary_frequency_grids": (None, [vp, C.POINTER(LibrpaOptions), _dp, _dp]),
         "librpa_get_rpa_correlation_energy": (d, [vp, C.POINTER(LibrpaOptions), i, _dp, _dp]),
         "librpa_build_exx": (None, [vp, C.POINTER(LibrpaOptions)]),
@@ -388,6 +389,12 @@ class Handler:
                                             i_state_high, _f64(vxc).ravel(), _f64(vexx).ravel(), re, im)
         self._check()
         return (re + 1j * im).reshape(n_spins, len(iks), nc)
+
+    def set_dielect_func_imagfreq(self, omegas, dielect_func):
+        """The macroscopic dielectric function on the imaginary axis (replace_w_head)."""
+        om = _f64(omegas).ravel()
+        self.lib.librpa_set_dielect_func_imagfreq(self.h, len(om), om, _f64(dielect_func).ravel())
+        self._check()
 
     def g0w0_sigc_iw(self, ispin, lo, hi, nfreq):
         """KS-diagonal Sigma_c(i omega) [state][omega] of the last G0W0 build."""

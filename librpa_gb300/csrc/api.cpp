@@ -921,7 +921,7 @@ void librpa_get_exx_pot_band_k(LibrpaHandler *h, const LibrpaOptions *, const in
     GB_UNSUPPORTED("librpa_get_exx_pot_band_k");
 }
 
-// compute_g0w0.cpp:22-166: chi0, W_c and Sigma_c (Gamma-point inputs on the GPU; gw.cu)
+// compute_g0w0.cpp:22-166: chi0, W_c and Sigma_c on the GPU (k-grids and the Gamma point; gw.cu)
 void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *p_opts)
 {
     guarded(h, [&] {
@@ -931,14 +931,13 @@ void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *p_opts)
         prepare_gw(ds);
         const auto g = make_grids(*ds, *p_opts);
         GB_REQUIRE(!g.tau.empty(), "time grids required for the space-time method");
-        gb::build_g0w0_gamma(*ds, *p_opts, g);
+        gb::build_g0w0(*ds, *p_opts, g);
     });
 }
 
-// compute_g0w0.cpp:168-260: Sigma_c of states [i_state_low, i_state_high) at the quasi-particle
-// energy (Pade continuation with n_params_anacon, damped fixed point); NaN where the solver failed
 // No counterpart in the reference: the KS-diagonal Sigma_c(i omega) that the quasi-particle step
-// continues, after librpa_build_g0w0_sigma; [state][omega] for states [lo, hi) of one spin.
+// continues, after librpa_build_g0w0_sigma; [state][omega] for states [lo, hi) of one spin at
+// k-point 0 (the Gamma point, or the first point of a k-grid).
 int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
                                   double *im)
 {
@@ -964,6 +963,8 @@ int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, 
     return rc;
 }
 
+// compute_g0w0.cpp:168-260: Sigma_c of states [i_state_low, i_state_high) at the quasi-particle
+// energy (Pade continuation with n_params_anacon, damped fixed point); NaN where the solver failed
 void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, const int n_spins, const int n_kpts_this,
                                 const int *iks_this, int i_state_low, int i_state_high, const double *vxc,
                                 const double *vexx, double *sigc_re, double *sigc_im)
@@ -980,22 +981,26 @@ void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, c
         {
             prepare_gw(ds);
             const auto g = make_grids(*ds, *p_opts);
-            gb::build_g0w0_gamma(*ds, *p_opts, g);
+            gb::build_g0w0(*ds, *p_opts, g);
         }
         const int nc = i_state_high - i_state_low, nw = static_cast<int>(ds->gw_omega.size());
+        const int nb = ds->n_states, nk = ds->n_kpts;
         std::vector<std::complex<double>> x(nw), f(nw);
         for (int w = 0; w < nw; ++w) x[w] = {0.0, ds->gw_omega[w]};
+        for (int k = 0; k < n_kpts_this; ++k)
+            GB_REQUIRE(iks_this[k] >= 0 && iks_this[k] < nk, "k-point index out of range");
         for (int isp = 0; isp < n_spins; ++isp)
             for (int k = 0; k < n_kpts_this; ++k)
             {
-                GB_REQUIRE(iks_this[k] == 0, "the Gamma-point G0W0 has k-point 0 only");
+                const int ik = iks_this[k];
                 for (int i = 0; i < nc; ++i)
                 {
                     const int n = i_state_low + i;
                     const size_t o = (static_cast<size_t>(isp) * n_kpts_this + k) * nc + i;
-                    for (int w = 0; w < nw; ++w) f[w] = ds->sigc_ks[isp][static_cast<size_t>(n) * nw + w];
+                    for (int w = 0; w < nw; ++w)
+                        f[w] = ds->sigc_ks[isp][(static_cast<size_t>(ik) * nb + n) * nw + w];
                     const gb::PadeContinuation pade(p_opts->n_params_anacon, x, f);
-                    const gb::QpeResult r = gb::solve_qpe(pade, ds->ekb[static_cast<size_t>(isp) * ds->n_states + n],
+                    const gb::QpeResult r = gb::solve_qpe(pade, ds->ekb[(static_cast<size_t>(isp) * nk + ik) * nb + n],
                                                           ds->efermi, vxc[o], vexx[o]);
                     sigc_re[o] = r.info == 0 ? r.sigc.real() : std::numeric_limits<double>::quiet_NaN();
                     sigc_im[o] = r.info == 0 ? r.sigc.imag() : std::numeric_limits<double>::quiet_NaN();

@@ -217,6 +217,80 @@ __global__ void k_ks_diag(const cuDoubleComplex *__restrict__ psi, const cuDoubl
     out[t] = make_cuDoubleComplex(re, im);
 }
 
+// Real embedding of complex N x N matrices, batch-strided: E = [[Re A, -Im A], [Im A, Re A]]
+// (2N x 2N).  Products, inverses and solves of embedded matrices are the embeddings of the complex
+// ones, so the complex W_c(q) runs through the real kernels.
+__global__ void k_embed(const cuDoubleComplex *__restrict__ A, long long sa, int N, int batch, double *__restrict__ E)
+{
+    const long long nn = static_cast<long long>(N) * N, n = nn * batch;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long b = t / nn, e = t % nn;
+        const int i = static_cast<int>(e / N), j = static_cast<int>(e % N);
+        const cuDoubleComplex v = A[b * sa + e];
+        double *o = E + b * 4 * nn;
+        const long long w = 2LL * N;
+        o[i * w + j] = v.x;
+        o[i * w + N + j] = -v.y;
+        o[(N + i) * w + j] = v.y;
+        o[(N + i) * w + N + j] = v.x;
+    }
+}
+
+// The complex matrices back from their embeddings: re = E[0:N, 0:N], im = E[N:2N, 0:N].
+__global__ void k_unembed(const double *__restrict__ E, int N, int batch, double *__restrict__ re, double *__restrict__ im)
+{
+    const long long nn = static_cast<long long>(N) * N, n = nn * batch;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long b = t / nn, e = t % nn;
+        const int i = static_cast<int>(e / N), j = static_cast<int>(e % N);
+        const double *o = E + b * 4 * nn;
+        re[t] = o[static_cast<long long>(i) * 2 * N + j];
+        im[t] = o[static_cast<long long>(N + i) * 2 * N + j];
+    }
+}
+
+// Supercell matrix from cell-periodic blocks: X_s[(c a)][(d b)] = src[cell of R_d - R_c][a][b],
+// src blocks cstride apart.
+__global__ void k_to_super(const double *__restrict__ src, long long cstride, int n, int nc, const int *__restrict__ cdiff,
+                           double *__restrict__ Xs)
+{
+    const long long ns = static_cast<long long>(nc) * n, tot = ns * ns;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < tot;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long r = t / ns, q = t % ns;
+        const int c = static_cast<int>(r / n), a = static_cast<int>(r % n), d = static_cast<int>(q / n), b = static_cast<int>(q % n);
+        Xs[t] = src[cdiff[d * nc + c] * cstride + static_cast<long long>(a) * n + b];
+    }
+}
+
+// Sig[w][c][K][L] += cw[w] (S+ + S-)/2 + i sw[w] (S+ - S-)/2 with S(R_c)_KL the supercell row block
+// of the cell R = 0 (row cell c0), column block c.
+__global__ void k_sigma_rows(const double *__restrict__ Sp, const double *__restrict__ Sm, int c0, int nc, int n,
+                             const double *__restrict__ cw, const double *__restrict__ sw, int nw,
+                             cuDoubleComplex *__restrict__ Sig)
+{
+    const long long per = static_cast<long long>(nc) * n * n, tot = per * nw, ns = static_cast<long long>(nc) * n;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < tot;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const int w = static_cast<int>(t / per);
+        const long long e = t % per;
+        const int c = static_cast<int>(e / (static_cast<long long>(n) * n));
+        const int K = static_cast<int>((e / n) % n), L = static_cast<int>(e % n);
+        const long long src = (static_cast<long long>(c0) * n + K) * ns + static_cast<long long>(c) * n + L;
+        const double cp = 0.5 * (Sp[src] + Sm[src]), sp = 0.5 * (Sp[src] - Sm[src]);
+        cuDoubleComplex o = Sig[t];
+        o.x += cw[w] * cp;
+        o.y += sw[w] * sp;
+        Sig[t] = o;
+    }
+}
+
 unsigned grid_for(long long n) { return static_cast<unsigned>(std::min<long long>((n + 255) / 256, 152LL * 32)); }
 
 // Cyclic Jacobi eigen-decomposition of a symmetric n x n matrix (row-major, destroyed):
@@ -300,6 +374,49 @@ std::vector<double> power_sym(const std::vector<double> &A, int n, double power,
         }
     }
     return out;
+}
+
+// A^p of a complex Hermitian n x n matrix (row-major), over the eigenvalues at or above the
+// threshold as power_sym: through its real symmetric embedding [[Re, -Im], [Im, Re]], whose
+// eigenvalues are A's, each twice (power_hemat_blacs, utils_matrix_m_mpi.h:597-720).
+std::vector<cplx> power_herm(const std::vector<cplx> &A, int n, double power, double threshold)
+{
+    const int m = 2 * n;
+    std::vector<double> E(static_cast<size_t>(m) * m);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+        {
+            const cplx v = A[static_cast<size_t>(i) * n + j];
+            E[static_cast<size_t>(i) * m + j] = v.real();
+            E[static_cast<size_t>(i) * m + n + j] = -v.imag();
+            E[static_cast<size_t>(n + i) * m + j] = v.imag();
+            E[static_cast<size_t>(n + i) * m + n + j] = v.real();
+        }
+    const std::vector<double> P = power_sym(E, m, power, threshold);
+    std::vector<cplx> out(static_cast<size_t>(n) * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            out[static_cast<size_t>(i) * n + j] = cplx(P[static_cast<size_t>(i) * m + j], P[static_cast<size_t>(n + i) * m + j]);
+    return out;
+}
+
+// Full Hermitian N x N matrix of the Coulomb blocks of k-point ik (upper pairs given).
+std::vector<cplx> coulomb_k(const std::vector<VqBlock> &blocks, const std::vector<cplx> &blob, int ik,
+                            const std::vector<int> &abf_off, int N)
+{
+    std::vector<cplx> V(static_cast<size_t>(N) * N, cplx(0, 0));
+    for (const VqBlock &b : blocks)
+    {
+        if (b.ik != ik || b.I > b.J) continue;
+        for (int m = 0; m < b.nmu; ++m)
+            for (int n = 0; n < b.nnu; ++n)
+            {
+                const cplx v = blob[b.offset + static_cast<size_t>(m) * b.nnu + n];
+                V[static_cast<size_t>(abf_off[b.I] + m) * N + abf_off[b.J] + n] = v;
+                V[static_cast<size_t>(abf_off[b.J] + n) * N + abf_off[b.I] + m] = std::conj(v);
+            }
+    }
+    return V;
 }
 
 // Full real symmetric N x N matrix of the Gamma-point Coulomb blocks (upper pairs, real part).
@@ -821,6 +938,329 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     ds.gw_omega = tf.omega;
     ds.g0w0_generation = ds.generation;
     release_kept(ds);
+}
+
+
+// G0W0 on a k-grid (task = g0w0 with k-points; epsilon.cpp:1763-2322, :2323-2660, gw.cpp:217-876,
+// :884-1240): W_c(q, omega) at every IBZ q by the real embedding of the complex matrices, with the
+// head of the dielectric matrix replaced at q = 0 when replace_w_head is on (epsilon.cpp:2030-2120);
+// W_c(R, omega) = Re sum_k e^{-i 2 pi k.R} W_c(k, omega) / n_k over the full k list (conjugated for
+// the time-reversed members of a star); W_c(R, tau) by costrans_f2t; Sigma_c(R, +-tau) as the
+// Gamma-point closed form of the BvK supercell with G(R, +-tau); Sigma_c(k, i omega) on the KS
+// states of every k-point.
+void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)
+{
+    GB_REQUIRE(ds.n_spinor == 1, "spinor (SOC) wave functions are not supported");
+    GB_REQUIRE(ds.occ_set, "occupations/eigenvalues not set");
+    for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some (spin, k)");
+    GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
+    GB_REQUIRE(!ds.vq_blocks.empty(), "the Coulomb matrix of the dielectric function is not set");
+    GB_REQUIRE(opts.use_shrink_abfs != LIBRPA_SWITCH_ON,
+               "use_shrink_abfs: the G0W0 chain has no unfolding of W to the large ABF basis");
+    const int nw = tf.n;
+    const bool head = opts.replace_w_head == LIBRPA_SWITCH_ON && !ds.dielect_eps.empty();
+    if (head)
+    {
+        // interpolate_dielec_func (src/core/dielecmodel.cpp:65-104), option 0: the given values
+        GB_REQUIRE(opts.option_dielect_func == 0,
+                   "replace_w_head: only option_dielect_func = 0 (the dielectric function given at the minimax "
+                   "frequencies) is supported");
+        GB_REQUIRE(static_cast<int>(ds.dielect_eps.size()) == nw,
+                   "replace_w_head: the dielectric function must be given at the nfreq minimax frequencies");
+    }
+    // chi0(q, omega) of every IBZ q from the RPA path, kept on the device
+    {
+        const LibrpaGB300Options saved = ds.gbopt;
+        ds.gbopt.stage = LIBRPA_GB300_STAGE_CHI0;
+        ds.gbopt.tau_begin = 0;
+        ds.gbopt.tau_end = -1;
+        try
+        {
+            run_rpa_gpu(ds, opts, tf, opts.n_bands_chi0);
+        }
+        catch (...)
+        {
+            ds.gbopt = saved;
+            throw;
+        }
+        ds.gbopt = saved;
+    }
+    GB_REQUIRE(ds.kept_chi0 && ds.kept_nfreq == nw, "chi0(q, omega) was not kept");
+    GB_CUDA(cudaSetDevice(ds.gbopt.device));
+    cudaStream_t st;
+    GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    struct Guard
+    {
+        cudaStream_t s;
+        ~Guard() { cudaStreamDestroy(s); }
+    } guard{st};
+    GammaSetup gs;
+    setup_gamma(ds, opts.libri_g0w0_threshold_C, gs, st);
+    const PhaseTables pt = build_phase_tables(ds);
+    const int Nc = gs.Nc, naoc = gs.naoc, nc = gs.nc, nq = pt.nq, nk = ds.n_kpts, nb = ds.n_states, ns = ds.n_spins;
+    const int n_at = gs.n_at, N2 = 2 * Nc;
+    GB_REQUIRE(ds.kept_nq == nq, "kept chi0 holds another IBZ");
+    const long long NN = static_cast<long long>(Nc) * Nc, M4 = 4 * NN, e_tot = static_cast<long long>(ds.kept_pair_elems);
+    const double thr = opts.sqrt_coulomb_threshold;
+
+    // layout tables of the kept chi0 (upper atom pairs of one cell)
+    std::vector<int> atom_of(Nc), pair_of(static_cast<size_t>(n_at) * n_at, -1), abf_off_n(n_at), nabf(n_at);
+    std::vector<long long> eoff;
+    {
+        long long e = 0;
+        for (int I = 0; I < n_at; ++I)
+            for (int J = I; J < n_at; ++J)
+            {
+                pair_of[static_cast<size_t>(I) * n_at + J] = static_cast<int>(eoff.size());
+                eoff.push_back(e);
+                e += static_cast<long long>(ds.nabf_at[I]) * ds.nabf_at[J];
+            }
+        GB_REQUIRE(e == e_tot, "kept chi0 layout does not match the bases");
+        for (int I = 0; I < n_at; ++I)
+        {
+            abf_off_n[I] = gs.abf_off[I];
+            nabf[I] = ds.nabf_at[I];
+            for (int a = gs.abf_off[I]; a < gs.abf_off[I + 1]; ++a) atom_of[a] = I;
+        }
+    }
+    auto d_atom = to_dev(atom_of, st);
+    auto d_pair = to_dev(pair_of, st);
+    auto d_off = to_dev(abf_off_n, st);
+    auto d_nabf = to_dev(nabf, st);
+    auto d_eoff = to_dev(eoff, st);
+
+    // ---- W_c(q, omega), [Re | Im][q][omega][N][N]
+    DevBuf<double> Wq(2ull * nq * nw * NN);
+    {
+        DevBuf<cuDoubleComplex> X(static_cast<size_t>(nw) * NN);
+        DevBuf<double> Xe(nw * M4), T(nw * M4), Ye(nw * M4), We(nw * M4), Se(M4), Sce(M4), ScSc(M4), d_ones(nw);
+        DevBuf<int> bad(1);
+        bad.zero(st);
+        std::vector<double> ones(nw, -1.0);
+        d_ones.upload(ones.data(), nw, st);
+        auto embed_h = [&](const std::vector<cplx> &A) {
+            std::vector<double> E(M4);
+            for (int i = 0; i < Nc; ++i)
+                for (int j = 0; j < Nc; ++j)
+                {
+                    const cplx v = A[static_cast<size_t>(i) * Nc + j];
+                    E[static_cast<size_t>(i) * N2 + j] = v.real();
+                    E[static_cast<size_t>(i) * N2 + Nc + j] = -v.imag();
+                    E[static_cast<size_t>(Nc + i) * N2 + j] = v.imag();
+                    E[static_cast<size_t>(Nc + i) * N2 + Nc + j] = v.real();
+                }
+            return E;
+        };
+        const size_t gj_smem = sizeof(double) * N2;
+        GB_REQUIRE(gj_smem <= 48 * 1024, "auxiliary basis too large for the W_c solve");
+        for (int q = 0; q < nq; ++q)
+        {
+            const int kq = pt.ibz_rep[q];
+            const std::vector<cplx> ve = coulomb_k(ds.vq_blocks, ds.vq_blob, kq, gs.abf_off, Nc);
+            const std::vector<cplx> vc = coulomb_k(ds.vq_cut_blocks, ds.vq_cut_blob, kq, gs.abf_off, Nc);
+            const bool gq = std::fabs(ds.kfrac[3 * kq]) < 1e-10 && std::fabs(ds.kfrac[3 * kq + 1]) < 1e-10 &&
+                            std::fabs(ds.kfrac[3 * kq + 2]) < 1e-10;
+            const bool head_q = gq && head;
+            std::vector<double> z0;
+            double w0 = 0.0;
+            std::vector<double> se_h;
+            if (head_q)
+            {
+                // power_hemat_blacs_real on Re V (utils_matrix_m_mpi.h:886-1010): S = V^1/2 over the
+                // eigenvalues at or above the threshold; z0 the eigenvector of the largest one
+                std::vector<double> rv(NN);
+                for (long long e = 0; e < NN; ++e) rv[e] = ve[e].real();
+                std::vector<double> B = rv, w, Z;
+                sym_eig(B, Nc, w, Z);
+                w0 = w[Nc - 1];
+                GB_REQUIRE(w0 >= thr, "replace_w_head: the Coulomb matrix at q = 0 has no eigenvalue above the threshold");
+                z0.resize(Nc);
+                for (int r = 0; r < Nc; ++r) z0[r] = Z[static_cast<size_t>(r) * Nc + Nc - 1];
+                const std::vector<double> S = power_sym(rv, Nc, 0.5, thr);
+                std::vector<cplx> Sc(NN);
+                for (long long e = 0; e < NN; ++e) Sc[e] = S[e];
+                se_h = embed_h(Sc);
+            }
+            else
+                se_h = embed_h(power_herm(ve, Nc, 0.5, thr));
+            const std::vector<double> sc_h = embed_h(power_herm(vc, Nc, 0.5, thr));
+            Se.upload(se_h.data(), M4, st);
+            Sce.upload(sc_h.data(), M4, st);
+            launch_dgemm(N2, N2, N2, Sce.get(), N2, 0, Sce.get(), N2, 0, ScSc.get(), N2, 0, 1, 1.0, 0.0, st);
+            launch_assemble_chi0(static_cast<const cuDoubleComplex *>(ds.kept_chi0) + static_cast<long long>(q) * e_tot,
+                                 static_cast<long long>(nq) * e_tot, nw, Nc, d_atom.get(), d_off.get(), d_nabf.get(),
+                                 d_pair.get(), n_at, d_eoff.get(), false, X.get(), nullptr, NN, st);
+            k_embed<<<grid_for(NN * nw), 256, 0, st>>>(X.get(), NN, Nc, nw, Xe.get());
+            GB_LAUNCH_CHECK();
+            // S chi0 S
+            launch_dgemm(N2, N2, N2, Se.get(), N2, 0, Xe.get(), N2, M4, T.get(), N2, M4, nw, 1.0, 0.0, st);
+            launch_dgemm(N2, N2, N2, T.get(), N2, M4, Se.get(), N2, 0, Xe.get(), N2, M4, nw, 1.0, 0.0, st);
+            if (head_q)
+            {
+                // in V's eigenbasis the (0, 0) element of S chi0 S, w0 z0^T chi0 z0, becomes
+                // 1 - eps_mac: add ((1 - eps_mac) - X00) z0 z0^T
+                std::vector<cplx> hx(static_cast<size_t>(nw) * NN);
+                X.download(reinterpret_cast<cuDoubleComplex *>(hx.data()), hx.size(), st);
+                std::vector<double> hxe(nw * M4);
+                Xe.download(hxe.data(), hxe.size(), st);
+                GB_CUDA(cudaStreamSynchronize(st));
+                for (int w = 0; w < nw; ++w)
+                {
+                    cplx x00(0, 0);
+                    for (int r = 0; r < Nc; ++r)
+                        for (int c = 0; c < Nc; ++c) x00 += z0[r] * hx[static_cast<size_t>(w) * NN + static_cast<size_t>(r) * Nc + c] * z0[c];
+                    x00 *= w0;
+                    const cplx d = (1.0 - ds.dielect_eps[w]) - x00;
+                    double *E = hxe.data() + static_cast<size_t>(w) * M4;
+                    for (int r = 0; r < Nc; ++r)
+                        for (int c = 0; c < Nc; ++c)
+                        {
+                            const double zz = z0[r] * z0[c];
+                            E[static_cast<size_t>(r) * N2 + c] += d.real() * zz;
+                            E[static_cast<size_t>(r) * N2 + Nc + c] -= d.imag() * zz;
+                            E[static_cast<size_t>(Nc + r) * N2 + c] += d.imag() * zz;
+                            E[static_cast<size_t>(Nc + r) * N2 + Nc + c] += d.real() * zz;
+                        }
+                }
+                Xe.upload(hxe.data(), hxe.size(), st);
+            }
+            // eps = 1 - S chi0 S; W_c = S_c eps^-1 S_c - S_c S_c
+            k_one_minus<<<grid_for(M4 * nw), 256, 0, st>>>(Xe.get(), N2, nw);
+            GB_LAUNCH_CHECK();
+            for (int w = 0; w < nw; ++w)
+                GB_CUDA(cudaMemcpyAsync(Ye.get() + w * M4, Sce.get(), sizeof(double) * M4, cudaMemcpyDeviceToDevice, st));
+            k_gj_solve<<<nw, 256, gj_smem, st>>>(Xe.get(), Ye.get(), N2, N2, bad.get());
+            GB_LAUNCH_CHECK();
+            launch_dgemm(N2, N2, N2, Sce.get(), N2, 0, Ye.get(), N2, M4, We.get(), N2, M4, nw, 1.0, 0.0, st);
+            launch_dgemm(nw, static_cast<int>(M4), 1, d_ones.get(), 1, 0, ScSc.get(), M4, 0, We.get(), M4, 0, 1, 1.0, 1.0, st);
+            k_unembed<<<grid_for(NN * nw), 256, 0, st>>>(We.get(), Nc, nw, Wq.get() + static_cast<long long>(q) * nw * NN,
+                                                         Wq.get() + (static_cast<long long>(nq) + q) * nw * NN);
+            GB_LAUNCH_CHECK();
+            GB_CUDA(cudaStreamSynchronize(st));  // the host matrices are rebuilt for the next q
+        }
+        int hbad = 0;
+        bad.download(&hbad, 1, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+        GB_REQUIRE(hbad == 0, "1 - S chi0 S is singular: no W_c");
+    }
+    // ---- W_c(R, omega) = sum_q [a_cq Re W_q + b_cq Im W_q], then W_c(R, tau) by costrans_f2t
+    DevBuf<double> WR(static_cast<size_t>(nc) * nw * NN), Wt(static_cast<size_t>(nc) * nw * NN);
+    {
+        std::vector<double> coef(static_cast<size_t>(nc) * 2 * nq, 0.0);
+        std::vector<int> q_of_rep(nk, -1);
+        for (int q = 0; q < nq; ++q) q_of_rep[pt.ibz_rep[q]] = q;
+        for (int k = 0; k < nk; ++k)
+        {
+            const int rep = ds.ibz_map[k], q = q_of_rep[rep];
+            GB_REQUIRE(q >= 0, "k-point outside the IBZ list");
+            const double sg = rep == k ? 1.0 : -1.0;
+            for (int c = 0; c < nc; ++c)
+            {
+                const double th = k_dot_r(ds, k, gs.cells[c]);
+                coef[static_cast<size_t>(c) * 2 * nq + q] += std::cos(th) / nk;
+                coef[static_cast<size_t>(c) * 2 * nq + nq + q] += sg * std::sin(th) / nk;
+            }
+        }
+        auto d_coef = to_dev(coef, st);
+        launch_dgemm(nc, static_cast<int>(nw * NN), 2 * nq, d_coef.get(), 2 * nq, 0, Wq.get(), nw * NN, 0, WR.get(),
+                     nw * NN, 0, 1, 1.0, 0.0, st);
+        DevBuf<double> d_f2t(static_cast<size_t>(nw) * nw);
+        d_f2t.upload(tf.cos_f2t.data(), static_cast<size_t>(nw) * nw, st);
+        launch_dgemm(nw, static_cast<int>(NN), nw, d_f2t.get(), nw, 0, WR.get(), NN, nw * NN, Wt.get(), NN, nw * NN, nc,
+                     1.0, 0.0, st);
+        GB_CUDA(cudaStreamSynchronize(st));
+    }
+    Wq.release();
+    WR.release();
+
+    // ---- Sigma_c(R, i omega) per spin from the supercell closed form at every tau, then the KS
+    // diagonal at every k
+    const int nao = naoc;
+    const long long naos = gs.nao, ns2 = naos * naos, nnc = static_cast<long long>(nao) * nao;
+    auto d_ekb = to_dev(ds.ekb, st);
+    auto d_wg = to_dev(ds.wg, st);
+    DevBuf<cuDoubleComplex> d_psi(ds.wfc.size());
+    d_psi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()), ds.wfc.size(), st);
+    auto d_gcos = to_dev(pt.gcos, st);
+    auto d_gsin = to_dev(pt.gsin, st);
+    auto d_cdiff = to_dev(gs.cdiff, st);
+    DevBuf<double> d_s(2ull * nk * nb), d_G(2ull * nc * nnc), Ws(static_cast<size_t>(gs.N) * gs.N), Gps(ns2), Gms(ns2),
+        Sp(ns2), Sm(ns2), cw(nw), sw(nw);
+    DevBuf<cuDoubleComplex> d_A(2ull * nk * nnc), Sig(static_cast<size_t>(nw) * nc * nnc);
+    HsWork wk;
+    ds.sigc_ks.assign(ns, {});
+    std::vector<cplx> hsig(static_cast<size_t>(nw) * nc * nnc);
+    for (int sp = 0; sp < ns; ++sp)
+    {
+        Sig.zero(st);
+        for (int it = 0; it < nw; ++it)
+        {
+            launch_tau_scale(d_ekb.get() + static_cast<size_t>(sp) * nk * nb, d_wg.get() + static_cast<size_t>(sp) * nk * nb,
+                             nk, nb, ds.efermi, tf.tau[it], ns, opts.n_bands_chi0, d_s.get(), st);
+            launch_gk_build(d_psi.get() + static_cast<size_t>(sp) * nk * nb * nao, d_s.get(), nk, nb, nao, d_A.get(), st);
+            launch_phase_sum(d_A.get(), d_gcos.get(), d_gsin.get(), nk, nc, nao, d_G.get(), st);
+            k_to_super<<<grid_for(ns2), 256, 0, st>>>(d_G.get(), nnc, nao, nc, d_cdiff.get(), Gps.get());
+            k_to_super<<<grid_for(ns2), 256, 0, st>>>(d_G.get() + nc * nnc, nnc, nao, nc, d_cdiff.get(), Gms.get());
+            k_to_super<<<grid_for(static_cast<long long>(gs.N) * gs.N), 256, 0, st>>>(
+                Wt.get() + static_cast<long long>(it) * NN, nw * NN, Nc, nc, d_cdiff.get(), Ws.get());
+            GB_LAUNCH_CHECK();
+            const double *Dp[2] = {Gps.get(), Gms.get()};
+            double *Hp[2] = {Sp.get(), Sm.get()};
+            hs_closed_form(gs, Ws.get(), Dp, 2, Hp, wk, st);
+            std::vector<double> c(nw), sn(nw);
+            for (int w = 0; w < nw; ++w)
+            {
+                c[w] = tf.cos_t2f[static_cast<size_t>(w) * nw + it];
+                sn[w] = tf.sin_t2f[static_cast<size_t>(w) * nw + it];
+            }
+            cw.upload(c.data(), nw, st);
+            sw.upload(sn.data(), nw, st);
+            k_sigma_rows<<<grid_for(nnc * nc * nw), 256, 0, st>>>(Sp.get(), Sm.get(), gs.c0, nc, nao, cw.get(), sw.get(),
+                                                                  nw, Sig.get());
+            GB_LAUNCH_CHECK();
+            GB_CUDA(cudaStreamSynchronize(st));  // the host weight vectors are reused
+        }
+        Sig.download(reinterpret_cast<cuDoubleComplex *>(hsig.data()), hsig.size(), st);
+        GB_CUDA(cudaStreamSynchronize(st));
+        // Sigma_c(k, i omega) = sum_c e^{i 2 pi k.R_c} Sigma_c(R_c, i omega); <psi_kn|.|psi_kn>
+        std::vector<cplx> &out = ds.sigc_ks[sp];
+        out.assign(static_cast<size_t>(nk) * nb * nw, cplx(0, 0));
+        std::vector<cplx> Sk(nnc);
+        for (int k = 0; k < nk; ++k)
+            for (int w = 0; w < nw; ++w)
+            {
+                std::fill(Sk.begin(), Sk.end(), cplx(0, 0));
+                for (int c = 0; c < nc; ++c)
+                {
+                    const cplx ph = std::polar(1.0, k_dot_r(ds, k, gs.cells[c]));
+                    const cplx *src = hsig.data() + (static_cast<size_t>(w) * nc + c) * nnc;
+                    for (long long e = 0; e < nnc; ++e) Sk[e] += ph * src[e];
+                }
+                for (int n = 0; n < nb; ++n)
+                {
+                    const cplx *v = ds.wfc.data() + ((static_cast<size_t>(sp) * nk + k) * nb + n) * nao;
+                    cplx acc(0, 0);
+                    for (int p = 0; p < nao; ++p)
+                    {
+                        cplx t(0, 0);
+                        for (int q2 = 0; q2 < nao; ++q2) t += Sk[static_cast<size_t>(p) * nao + q2] * v[q2];
+                        acc += std::conj(v[p]) * t;
+                    }
+                    out[(static_cast<size_t>(k) * nb + n) * nw + w] = acc;
+                }
+            }
+    }
+    ds.gw_omega = tf.omega;
+    ds.g0w0_generation = ds.generation;
+    release_kept(ds);
+}
+
+void build_g0w0(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)
+{
+    if (ds.n_kpts > 1)
+        build_g0w0_kgrid(ds, opts, tf);
+    else
+        build_g0w0_gamma(ds, opts, tf);
 }
 
 } // namespace gb

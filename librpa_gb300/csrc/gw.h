@@ -15,8 +15,11 @@ struct TimeFreqGrids;
 void build_exx(Dataset &ds, const LibrpaOptions &opts);
 // v_exx of state n of spin s at k-point k (SCF grid), after build_exx: -<psi|H_x(k)|psi>.
 double exx_state(const Dataset &ds, int s, int k, int n);
-// Sigma_c(i omega) on the KS states per spin into ds.sigc_ks ([state][omega]) and the imaginary
-// frequencies into ds.gw_omega.
+// Sigma_c(i omega) on the KS states of every k-point per spin into ds.sigc_ks ([k][state][omega])
+// and the imaginary frequencies into ds.gw_omega: the Gamma-point chain for one k-point, the
+// k-grid chain (W_c(q) at every IBZ q, the BvK supercell closed form for Sigma_c(R)) otherwise.
+void build_g0w0(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);
 void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);
+void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);
 
 } // namespace gb

@@ -137,9 +137,9 @@ def test_invalid_routing_is_rejected_before_any_gpu_work(lib):
 
 
 def test_g0w0_and_exchange_input_checks_before_any_gpu_work(lib):
-    """The exchange takes k-grid inputs (MgO, 3x3x3) and reaches the GPU (here: none); the G0W0
-    chain covers Gamma-point inputs and refuses the k-grid with a message, as the exchange refuses
-    an input without the truncated Coulomb matrix."""
+    """The exchange and G0W0 take k-grid inputs (MgO, 3x3x3) and reach the GPU (here: none); the
+    G0W0 head correction needs the dielectric function at the nfreq minimax frequencies, and the
+    exchange refuses an input without the truncated Coulomb matrix."""
     from conftest import load_mgo
     s = load_mgo()
     with L.Handler() as h:
@@ -147,8 +147,10 @@ def test_g0w0_and_exchange_input_checks_before_any_gpu_work(lib):
         if lib.librpa_gb300_device_count() == 0:
             with pytest.raises(L.LibrpaError, match="CUDA|device"):
                 h.get_exx_pot_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4)
-        with pytest.raises(L.LibrpaError, match="Gamma-point inputs"):
-            h.get_g0w0_sigc_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax), 1, [0], 0, 4, np.zeros(4), np.zeros(4))
+        h.set_dielect_func_imagfreq(np.arange(5.0), np.ones(5))
+        with pytest.raises(L.LibrpaError, match="nfreq minimax frequencies"):
+            h.get_g0w0_sigc_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax, replace_w_head=1), 1, [0], 0, 4,
+                                  np.zeros(4), np.zeros(4))
     s = load_h2o()
     with L.Handler() as h:
         L.load_system(h, s)

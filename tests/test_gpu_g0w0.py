@@ -1,4 +1,4 @@
-"""Exchange (k-grids and the Gamma point) and G0W0 (Gamma point) on the GPU through the C ABI
+"""Exchange and G0W0 (k-grids and the Gamma point) on the GPU through the C ABI
 (librpa_get_exx_pot_kgrid, librpa_get_g0w0_sigc_kgrid), against the reference's own tables and
 the CPU oracle (needs a GB300)."""
 import numpy as np
@@ -117,3 +117,26 @@ def test_periodic_exchange_mgo_ibz_reduced():
     s = load_mgo()
     got = _vexx_kgrid(s)
     np.testing.assert_allclose(got[0] * HA2EV, s.qp_tables[:, :, 4], rtol=0, atol=6e-6)
+
+
+def test_mgo_kgrid_g0w0_tables():
+    """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
+    replaced by the given eps_mac, 6 minimax points, all 6 in the Pade fit), FP64 chi0: v_exx,
+    Re/Im Sigma_c and e_qp of all 17 states at all 27 k-points against the reference's tables
+    (refs/g0w0_aims_MgO_libri, 5 decimals in eV)."""
+    s = load_mgo()
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  n_params_anacon=s.n_params_anacon, replace_w_head=1, option_dielect_func=0)
+    om, _ = h.get_imaginary_frequency_grids(o)
+    h.set_dielect_func_imagfreq(om, s.epsmac)
+    nb, nk = s.n_bands, s.n_kpts
+    ks = list(range(nk))
+    vexx = h.get_exx_pot_kgrid(o, s.n_spins, ks, 0, nb)
+    vxc = s.vxc.reshape(s.n_spins, nk, nb)
+    sig = h.get_g0w0_sigc_kgrid(o, s.n_spins, ks, 0, nb, vxc, vexx)
+    e_qp = s.ekb - vxc + vexx + sig.real
+    got = np.stack([vexx[0] * HA2EV, sig[0].real * HA2EV, sig[0].imag * HA2EV, e_qp[0] * HA2EV], axis=-1)
+    np.testing.assert_allclose(got, s.qp_tables[:, :, 4:8], rtol=0, atol=6e-6)
