@@ -1,9 +1,8 @@
 #pragma once
 /*
  * Compute entry points (replaces LibRPA include/librpa_compute.h:26-142).
- * The RPA calls run on one GB300 GPU.  The exchange and G0W0 calls run on the GPU for
- * Gamma-point inputs (molecules and Gamma-point cells); k-grid inputs and the band-k-point
- * variants record an error.
+ * The RPA calls run on one GB300 GPU.  The exchange and G0W0 calls run on the GPU for k-grid
+ * and Gamma-point inputs; the band-k-point variants record an error.
  */
 #include "librpa_handler.h"
 #include "librpa_options.h"

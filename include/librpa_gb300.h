@@ -197,10 +197,10 @@ void librpa_gb300_clear_screening(LibrpaHandler *h);
 int librpa_gb300_mlp_loss_grad(const float *params, const float *norm, const float *x, const float *y, int n,
                                float *grad, double *loss);
 
-/* No counterpart in the reference: after librpa_build_g0w0_sigma (Gamma-point inputs), the
- * KS-diagonal correlation self-energy on the imaginary axis that the quasi-particle step
- * continues, re/im[(state - i_state_low) * nfreq + ifreq] for states [i_state_low, i_state_high)
- * of spin ispin.  Returns 0 on success. */
+/* No counterpart in the reference: after librpa_build_g0w0_sigma, the KS-diagonal correlation
+ * self-energy on the imaginary axis that the quasi-particle step continues, at k-point 0 (the
+ * Gamma point, or the first point of a k-grid), re/im[(state - i_state_low) * nfreq + ifreq] for
+ * states [i_state_low, i_state_high) of spin ispin.  Returns 0 on success. */
 int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
                                   double *im);
 

@@ -1,6 +1,7 @@
-// Exact exchange and the G0W0 correlation self-energy at the Gamma point, on the GPU.
+// Exact exchange and the G0W0 correlation self-energy on the GPU, for k-grids and the Gamma point.
 //
-// The chain of LibRPA's task = g0w0 for Gamma-only inputs (molecules and Gamma-point cells):
+// The chain of LibRPA's task = g0w0 for Gamma-only inputs (molecules and Gamma-point cells); the
+// k-grid chain (build_g0w0_kgrid, build_exx) runs the same steps on the Born-von Karman supercell:
 //   chi0(omega)      the RPA path's chi0(q = 0, omega) (engine.cu, any chi0 precision)
 //   W_c(omega)       S_c [(1 - S chi0 S)^-1 - 1] S_c with S = V^1/2, S_c = V_cut^1/2, the square
 //                    roots by eigen-decomposition with eigenvalues below the threshold dropped
@@ -677,8 +678,7 @@ void hs_closed_form(const GammaSetup &gs, const double *W, const double *const *
 void require_gamma(const Dataset &ds)
 {
     GB_REQUIRE(ds.n_kpts == 1 && ds.period[0] == 1 && ds.period[1] == 1 && ds.period[2] == 1,
-               "the GPU G0W0 and exchange path covers Gamma-point inputs (molecules and Gamma-point cells); "
-               "k-grid inputs are not supported");
+               "the Gamma-point G0W0 chain takes one k-point (k-grids go through build_g0w0_kgrid)");
     GB_REQUIRE(ds.n_spinor == 1, "spinor (SOC) wave functions are not supported");
     GB_REQUIRE(ds.occ_set, "occupations/eigenvalues not set");
     for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some spin");
