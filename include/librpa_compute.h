@@ -2,7 +2,7 @@
 /*
  * Compute entry points (replaces LibRPA include/librpa_compute.h:26-142).
  * The RPA calls run on one GB300 GPU.  The exchange and G0W0 calls run on the GPU for k-grid
- * and Gamma-point inputs; the band-k-point variants record an error.
+ * and Gamma-point inputs; the band-k-point variants project their k-grid results.
  */
 #include "librpa_handler.h"
 #include "librpa_options.h"

@@ -183,6 +183,12 @@ def load_library(path: str | Path | None = None):
         "librpa_set_aux_bare_coulomb_k_atom_pair": (None, [vp, i, i, i, i, i, _dp, _dp, d]),
         "librpa_set_aux_bare_coulomb_k_2d_block": (None, [vp, i, i, i, i, i, _dp, _dp]),
         "librpa_set_dielect_func_imagfreq": (None, [vp, i, _dp, _dp]),
+        "librpa_set_band_kvec": (None, [vp, i, _dp]),
+        "librpa_set_band_occ_eigval": (None, [vp, i, i, i, _dp, _dp]),
+        "librpa_set_wfc_band": (None, [vp, i, i, i, i, _dp, _dp]),
+        "librpa_reset_band_data": (None, [vp]),
+        "librpa_get_exx_pot_band_k": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp]),
+        "librpa_get_g0w0_sigc_band_k": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp, _dp, _dp, _dp]),
         "librpa_get_imaginary_frequency_grids": (None, [vp, C.POINTER(LibrpaOptions), _dp, _dp]),
         "librpa_get_rpa_correlation_energy": (d, [vp, C.POINTER(LibrpaOptions), i, _dp, _dp]),
         "librpa_build_exx": (None, [vp, C.POINTER(LibrpaOptions)]),
@@ -395,6 +401,44 @@ class Handler:
         om = _f64(omegas).ravel()
         self.lib.librpa_set_dielect_func_imagfreq(self.h, len(om), om, _f64(dielect_func).ravel())
         self._check()
+
+    def set_band_points(self, kfrac, occ, eig, wfc):
+        """Band k-points off the SCF grid: fractional coordinates (n, 3), occupations and
+        eigenvalues (n_spins, n, n_states) and eigenvectors (n_spins, n, n_states, n_ao)."""
+        kf = _f64(kfrac).reshape(-1, 3)
+        occ, eig = _f64(occ), _f64(eig)
+        ns, nk, nst = eig.shape
+        self.lib.librpa_set_band_kvec(self.h, nk, kf.ravel())
+        self._check()
+        self.lib.librpa_set_band_occ_eigval(self.h, ns, nk, nst, occ.ravel(), eig.ravel())
+        self._check()
+        for sp in range(ns):
+            for k in range(nk):
+                w = np.asarray(wfc[sp, k])
+                self.lib.librpa_set_wfc_band(self.h, sp, k, w.shape[0], w.shape[1], _f64(w.real).ravel(),
+                                             _f64(w.imag).ravel())
+                self._check()
+
+    def get_exx_pot_band_k(self, opts, n_spins, iks_band, i_state_low, i_state_high):
+        """v_exx at band k-points [n_spins][len(iks_band)][states] (Hartree)."""
+        iks = np.ascontiguousarray(iks_band, np.int32)
+        nc = i_state_high - i_state_low
+        out = np.zeros(n_spins * len(iks) * max(nc, 0))
+        self.lib.librpa_get_exx_pot_band_k(self.h, C.byref(opts), n_spins, len(iks), iks, i_state_low, i_state_high,
+                                           out)
+        self._check()
+        return out.reshape(n_spins, len(iks), nc)
+
+    def get_g0w0_sigc_band_k(self, opts, n_spins, iks_band, i_state_low, i_state_high, vxc, vexx):
+        """Sigma_c at the quasi-particle energy at band k-points, complex [n_spins][len(iks_band)][states]."""
+        iks = np.ascontiguousarray(iks_band, np.int32)
+        nc = i_state_high - i_state_low
+        re = np.zeros(n_spins * len(iks) * max(nc, 0))
+        im = np.zeros_like(re)
+        self.lib.librpa_get_g0w0_sigc_band_k(self.h, C.byref(opts), n_spins, len(iks), iks, i_state_low,
+                                             i_state_high, _f64(vxc).ravel(), _f64(vexx).ravel(), re, im)
+        self._check()
+        return (re + 1j * im).reshape(n_spins, len(iks), nc)
 
     def g0w0_sigc_iw(self, ispin, lo, hi, nfreq):
         """KS-diagonal Sigma_c(i omega) [state][omega] of the last G0W0 build."""

@@ -684,68 +684,82 @@ void librpa_set_dielect_func_imagfreq(LibrpaHandler *h, int nfreq, const double 
     });
 }
 
+// Band-point inputs (input.cpp:710-820).  They do not enter the k-grid results (H_x(R),
+// Sigma_c(R)), so they leave those valid: no generation change.
 void librpa_set_band_kvec(LibrpaHandler *h, int n, const double *kf)
 {
-    guarded(h, [&] { Dataset *ds = get_ds(h); ds->generation++; ds->band_kfrac.assign(kf, kf + 3 * n); });
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(n > 0 && kf, "band k-points: count and coordinates required");
+        ds->band_kfrac.assign(kf, kf + 3 * n);
+    });
 }
 
 void librpa_set_band_occ_eigval(LibrpaHandler *h, int ns, int nk, int nst, const double *occ, const double *eig)
 {
     guarded(h, [&] {
-        Dataset *ds = get_ds(h); ds->generation++;
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ns > 0 && nk > 0 && nst > 0 && occ && eig, "band occupations: dimensions and data required");
         const size_t n = static_cast<size_t>(ns) * nk * nst;
         ds->band_occ.assign(occ, occ + n);
         ds->band_eig.assign(eig, eig + n);
+        // occupations scaled by 1 / n_kpts_band as the SCF ones (input.cpp:755)
+        for (double &o : ds->band_occ) o /= nk;
+        ds->band_ns = ns;
+        ds->band_nk = nk;
+        ds->band_nst = nst;
+        ds->band_wfc.assign(n * static_cast<size_t>(ds->n_ao), cplx(0, 0));
     });
 }
 
-void librpa_set_wfc_band(LibrpaHandler *h, int, int, int nst, int nbas, const double *re, const double *im)
+void librpa_set_wfc_band(LibrpaHandler *h, int ispin, int ik, int nst, int nbas, const double *re, const double *im)
 {
     guarded(h, [&] {
-        Dataset *ds = get_ds(h); ds->generation++;
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ds->band_nk > 0, "band eigenvectors: call librpa_set_band_occ_eigval first");
+        GB_REQUIRE(ispin >= 0 && ispin < ds->band_ns && ik >= 0 && ik < ds->band_nk && nst == ds->band_nst &&
+                       nbas == ds->n_ao && re && im,
+                   "band eigenvectors: indices or dimensions differ from librpa_set_band_occ_eigval / the SCF basis");
         const size_t n = static_cast<size_t>(nst) * nbas;
-        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(re[t], im[t]);
+        cplx *dst = ds->band_wfc.data() + (static_cast<size_t>(ispin) * ds->band_nk + ik) * n;
+        for (size_t t = 0; t < n; ++t) dst[t] = cplx(re[t], im[t]);
     });
 }
 
-void librpa_set_wfc_band_spinor(LibrpaHandler *h, int, int nst, int nbas, const double *ur, const double *ui,
-                                const double *dr, const double *di)
+void librpa_set_wfc_band_spinor(LibrpaHandler *h, int, int, int, const double *, const double *, const double *,
+                                const double *)
+{
+    guarded(h, [&] { GB_FAIL("spinor (SOC) wave functions are not supported by the GPU G0W0 and exchange path"); });
+}
+
+void librpa_set_wfc_band_packed(LibrpaHandler *h, int ispin, int ik, int nst, int nbas, const double *ri)
 {
     guarded(h, [&] {
-        Dataset *ds = get_ds(h); ds->generation++;
+        Dataset *ds = get_ds(h);
+        GB_REQUIRE(ds->band_nk > 0, "band eigenvectors: call librpa_set_band_occ_eigval first");
+        GB_REQUIRE(ispin >= 0 && ispin < ds->band_ns && ik >= 0 && ik < ds->band_nk && nst == ds->band_nst &&
+                       nbas == ds->n_ao && ri,
+                   "band eigenvectors: indices or dimensions differ from librpa_set_band_occ_eigval / the SCF basis");
         const size_t n = static_cast<size_t>(nst) * nbas;
-        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(ur[t], ui[t]);
-        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(dr[t], di[t]);
+        cplx *dst = ds->band_wfc.data() + (static_cast<size_t>(ispin) * ds->band_nk + ik) * n;
+        for (size_t t = 0; t < n; ++t) dst[t] = cplx(ri[2 * t], ri[2 * t + 1]);
     });
 }
 
-void librpa_set_wfc_band_packed(LibrpaHandler *h, int, int, int nst, int nbas, const double *ri)
+void librpa_set_wfc_band_spinor_packed(LibrpaHandler *h, int, int, int, const double *, const double *)
 {
-    guarded(h, [&] {
-        Dataset *ds = get_ds(h); ds->generation++;
-        const size_t n = static_cast<size_t>(nst) * nbas;
-        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(ri[2 * t], ri[2 * t + 1]);
-    });
-}
-
-void librpa_set_wfc_band_spinor_packed(LibrpaHandler *h, int, int nst, int nbas, const double *u, const double *d)
-{
-    guarded(h, [&] {
-        Dataset *ds = get_ds(h); ds->generation++;
-        const size_t n = static_cast<size_t>(nst) * nbas;
-        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(u[2 * t], u[2 * t + 1]);
-        for (size_t t = 0; t < n; ++t) ds->band_wfc.emplace_back(d[2 * t], d[2 * t + 1]);
-    });
+    guarded(h, [&] { GB_FAIL("spinor (SOC) wave functions are not supported by the GPU G0W0 and exchange path"); });
 }
 
 void librpa_reset_band_data(LibrpaHandler *h)
 {
     guarded(h, [&] {
-        Dataset *ds = get_ds(h); ds->generation++;
+        Dataset *ds = get_ds(h);
         ds->band_kfrac.clear();
         ds->band_occ.clear();
         ds->band_eig.clear();
         ds->band_wfc.clear();
+        ds->band_ns = ds->band_nk = ds->band_nst = 0;
     });
 }
 
@@ -855,8 +869,6 @@ int librpa_gb300_get_rpa_correlation_energy_batch(LibrpaHandler **hs, int n, con
     return failed;
 }
 
-#define GB_UNSUPPORTED(name)                                                                        \
-    guarded(h, [&] { GB_FAIL(std::string(name) + " is outside the RPA path of this GB300 build"); })
 
 namespace {
 // Set-up shared by the exchange and G0W0 calls: Gamma-only default lattice, 2D Coulomb input
@@ -915,10 +927,32 @@ void librpa_get_exx_pot_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, con
     });
 }
 
-void librpa_get_exx_pot_band_k(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
-                               double *)
+// compute_exx.cpp:115-180: v_exx at band k-points (librpa_set_band_*), from the k-grid H_x(R)
+void librpa_get_exx_pot_band_k(LibrpaHandler *h, const LibrpaOptions *p_opts, const int n_spins,
+                               const int n_kpts_band_this, const int *iks_band_this, int i_state_low, int i_state_high,
+                               double *vexx_band)
 {
-    GB_UNSUPPORTED("librpa_get_exx_pot_band_k");
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts && iks_band_this && vexx_band, "null argument");
+        GB_REQUIRE(ds->band_nk > 0, "Meanfield data for band calculation is not set");
+        i_state_low = std::max(0, i_state_low);
+        i_state_high = std::min(ds->band_nst, i_state_high);
+        GB_REQUIRE(n_spins == ds->n_spins, "parsed nspins is not consistent with the SCF starting point");
+        if (i_state_high <= i_state_low) return;
+        if (ds->hx_r.empty() || ds->exx_generation != ds->generation)
+        {
+            prepare_gw(ds);
+            gb::build_exx(*ds, *p_opts);
+        }
+        const int nc = i_state_high - i_state_low;
+        for (int isp = 0; isp < n_spins; ++isp)
+            for (int k = 0; k < n_kpts_band_this; ++k)
+                for (int i = 0; i < nc; ++i)
+                    vexx_band[(static_cast<size_t>(isp) * n_kpts_band_this + k) * nc + i] =
+                        gb::exx_band_state(*ds, isp, iks_band_this[k], i_state_low + i);
+    });
 }
 
 // compute_g0w0.cpp:22-166: chi0, W_c and Sigma_c on the GPU (k-grids and the Gamma point; gw.cu)
@@ -1009,10 +1043,49 @@ void librpa_get_g0w0_sigc_kgrid(LibrpaHandler *h, const LibrpaOptions *p_opts, c
     });
 }
 
-void librpa_get_g0w0_sigc_band_k(LibrpaHandler *h, const LibrpaOptions *, const int, const int, const int *, int, int,
-                                 const double *, const double *, double *, double *)
+// compute_g0w0.cpp:263-366: Sigma_c at band k-points from the k-grid Sigma_c(R, i omega), the
+// quasi-particle equation with the band eigenvalues and the SCF Fermi level
+void librpa_get_g0w0_sigc_band_k(LibrpaHandler *h, const LibrpaOptions *p_opts, const int n_spins,
+                                 const int n_kpts_band_this, const int *iks_band_this, int i_state_low,
+                                 int i_state_high, const double *vxc_band, const double *vexx_band, double *sigc_re,
+                                 double *sigc_im)
 {
-    GB_UNSUPPORTED("librpa_get_g0w0_sigc_band_k");
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h);
+        clear_error(ds);
+        GB_REQUIRE(p_opts && iks_band_this && vxc_band && vexx_band && sigc_re && sigc_im, "null argument");
+        GB_REQUIRE(ds->band_nk > 0, "Meanfield data for band calculation is not set");
+        i_state_low = std::max(0, i_state_low);
+        i_state_high = std::min(ds->band_nst, i_state_high);
+        GB_REQUIRE(n_spins == ds->n_spins, "parsed nspins is not consistent with the SCF starting point");
+        if (i_state_high <= i_state_low) return;
+        if (ds->sigc_r.empty() || ds->g0w0_generation != ds->generation)
+        {
+            prepare_gw(ds);
+            const auto g = make_grids(*ds, *p_opts);
+            gb::build_g0w0(*ds, *p_opts, g);
+        }
+        const int nc = i_state_high - i_state_low, nw = static_cast<int>(ds->gw_omega.size());
+        std::vector<std::complex<double>> x(nw);
+        for (int w = 0; w < nw; ++w) x[w] = {0.0, ds->gw_omega[w]};
+        for (int isp = 0; isp < n_spins; ++isp)
+            for (int k = 0; k < n_kpts_band_this; ++k)
+            {
+                const int kb = iks_band_this[k];
+                for (int i = 0; i < nc; ++i)
+                {
+                    const int n = i_state_low + i;
+                    const size_t o = (static_cast<size_t>(isp) * n_kpts_band_this + k) * nc + i;
+                    const std::vector<std::complex<double>> f = gb::sigc_band_iw(*ds, isp, kb, n);
+                    const gb::PadeContinuation pade(p_opts->n_params_anacon, x, f);
+                    const gb::QpeResult r = gb::solve_qpe(
+                        pade, ds->band_eig[(static_cast<size_t>(isp) * ds->band_nk + kb) * ds->band_nst + n], ds->efermi,
+                        vxc_band[o], vexx_band[o]);
+                    sigc_re[o] = r.info == 0 ? r.sigc.real() : std::numeric_limits<double>::quiet_NaN();
+                    sigc_im[o] = r.info == 0 ? r.sigc.imag() : std::numeric_limits<double>::quiet_NaN();
+                }
+            }
+    });
 }
 
 // ------------------------------------------------------------------ GB300 extensions

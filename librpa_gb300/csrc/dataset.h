@@ -89,15 +89,20 @@ struct Dataset
     // Gamma-point exchange and G0W0 results (gw.cu), valid while generation is unchanged
     std::vector<std::vector<double>> hx;       // per spin: H_x(R = 0), n_ao x n_ao
     std::vector<std::vector<double>> hx_r;     // per spin: H_x(R) [cell][n_ao][n_ao]
-    std::vector<std::array<int, 3>> hx_cells;  // the cells R of hx_r
+    std::vector<std::array<int, 3>> hx_cells;  // the cells R of hx_r and sigc_r
+    std::vector<std::vector<cplx>> sigc_r;     // per spin: Sigma_c(R, i omega) [omega][cell][n_ao][n_ao]
     std::vector<std::vector<cplx>> sigc_ks;    // per spin: Sigma_c(i omega) on the KS states, [n][omega]
     std::vector<double> gw_omega;              // the imaginary frequencies of sigc_ks
     unsigned long long exx_generation = 0, g0w0_generation = 0;
 
     // GW-side inputs that the RPA path does not use (kept so the setters behave)
     std::vector<double> dielect_omega, dielect_eps;
+    // band k-points off the SCF grid (task = exx_band / g0w0_band): k fractions, and per
+    // [spin][band k][state] occupations / eigenvalues and [spin][band k][state][ao] eigenvectors
+    // (dimensions from librpa_set_band_occ_eigval)
     std::vector<double> band_kfrac, band_occ, band_eig;
     std::vector<cplx> band_wfc;
+    int band_ns = 0, band_nk = 0, band_nst = 0;
 
     // GB300 extensions
     LibrpaGB300Options gbopt{};

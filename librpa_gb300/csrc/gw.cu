@@ -882,6 +882,7 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     DevBuf<double> sgn_s(2ull * nb), Gp(nn), Gm(nn), Sp(nn), Sm(nn), cw(nw), sw(nw);
     HsWork wk;
     ds.sigc_ks.assign(ns, {});
+    ds.sigc_r.assign(ns, {});
     for (int s = 0; s < ns; ++s)
     {
         Sig.zero(st);
@@ -933,8 +934,11 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         GB_LAUNCH_CHECK();
         ds.sigc_ks[s].resize(static_cast<size_t>(nb) * nw);
         sks.download(reinterpret_cast<cuDoubleComplex *>(ds.sigc_ks[s].data()), ds.sigc_ks[s].size(), st);
+        ds.sigc_r[s].resize(static_cast<size_t>(nw) * nn);  // [omega][cell R = 0][p][q]
+        Sig.download(reinterpret_cast<cuDoubleComplex *>(ds.sigc_r[s].data()), ds.sigc_r[s].size(), st);
         GB_CUDA(cudaStreamSynchronize(st));
     }
+    ds.hx_cells = gs.cells;
     ds.gw_omega = tf.omega;
     ds.g0w0_generation = ds.generation;
     release_kept(ds);
@@ -1189,6 +1193,7 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     DevBuf<cuDoubleComplex> d_A(2ull * nk * nnc), Sig(static_cast<size_t>(nw) * nc * nnc);
     HsWork wk;
     ds.sigc_ks.assign(ns, {});
+    ds.sigc_r.assign(ns, {});
     std::vector<cplx> hsig(static_cast<size_t>(nw) * nc * nnc);
     for (int sp = 0; sp < ns; ++sp)
     {
@@ -1222,6 +1227,7 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         }
         Sig.download(reinterpret_cast<cuDoubleComplex *>(hsig.data()), hsig.size(), st);
         GB_CUDA(cudaStreamSynchronize(st));
+        ds.sigc_r[sp] = hsig;
         // Sigma_c(k, i omega) = sum_c e^{i 2 pi k.R_c} Sigma_c(R_c, i omega); <psi_kn|.|psi_kn>
         std::vector<cplx> &out = ds.sigc_ks[sp];
         out.assign(static_cast<size_t>(nk) * nb * nw, cplx(0, 0));
@@ -1250,9 +1256,129 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                 }
             }
     }
+    ds.hx_cells = gs.cells;
     ds.gw_omega = tf.omega;
     ds.g0w0_generation = ds.generation;
     release_kept(ds);
+}
+
+namespace {
+// The image of cell c that the block (I, J, R_c) takes at band k-points: R_c + n period with n in
+// {-1, 0, 1}^3, the one nearest to x_I - x_J (Exx::build_KS_band, exx.cpp:683-725; applied when
+// the atom positions are set).  table[(I n_at + J) nc + c].
+std::vector<std::array<int, 3>> band_images(const Dataset &ds, int n_at, const std::vector<std::array<int, 3>> &cells)
+{
+    const int nc = static_cast<int>(cells.size());
+    std::vector<std::array<int, 3>> img(static_cast<size_t>(n_at) * n_at * nc);
+    const bool shift = static_cast<int>(ds.positions.size()) == 3 * n_at;
+    // fractional positions: x_cart = frac . latvec (rows a1, a2, a3)
+    std::vector<double> frac(3 * static_cast<size_t>(n_at), 0.0);
+    if (shift)
+    {
+        const double *L = ds.latvec;
+        const double det = L[0] * (L[4] * L[8] - L[5] * L[7]) - L[1] * (L[3] * L[8] - L[5] * L[6]) +
+                           L[2] * (L[3] * L[7] - L[4] * L[6]);
+        GB_REQUIRE(std::fabs(det) > 0.0, "singular lattice vectors");
+        const double inv[9] = {(L[4] * L[8] - L[5] * L[7]) / det, (L[2] * L[7] - L[1] * L[8]) / det,
+                               (L[1] * L[5] - L[2] * L[4]) / det, (L[5] * L[6] - L[3] * L[8]) / det,
+                               (L[0] * L[8] - L[2] * L[6]) / det, (L[2] * L[3] - L[0] * L[5]) / det,
+                               (L[3] * L[7] - L[4] * L[6]) / det, (L[1] * L[6] - L[0] * L[7]) / det,
+                               (L[0] * L[4] - L[1] * L[3]) / det};
+        for (int a = 0; a < n_at; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (int e = 0; e < 3; ++e) frac[3 * a + d] += ds.positions[3 * a + e] * inv[3 * e + d];
+    }
+    for (int I = 0; I < n_at; ++I)
+        for (int J = 0; J < n_at; ++J)
+            for (int c = 0; c < nc; ++c)
+            {
+                std::array<int, 3> best = cells[c];
+                if (shift)
+                {
+                    double bn = 1e300;
+                    for (int i = -1; i <= 1; ++i)
+                        for (int j = -1; j <= 1; ++j)
+                            for (int k = -1; k <= 1; ++k)
+                            {
+                                const int R[3] = {cells[c][0] + i * ds.period[0], cells[c][1] + j * ds.period[1],
+                                                  cells[c][2] + k * ds.period[2]};
+                                double dv[3];
+                                for (int e = 0; e < 3; ++e)
+                                {
+                                    dv[e] = 0.0;
+                                    for (int d = 0; d < 3; ++d)
+                                        dv[e] += (frac[3 * I + d] - frac[3 * J + d] - R[d]) * ds.latvec[3 * d + e];
+                                }
+                                const double n2 = dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2];
+                                if (n2 < bn)
+                                {
+                                    bn = n2;
+                                    best = {R[0], R[1], R[2]};
+                                }
+                            }
+                }
+                img[(static_cast<size_t>(I) * n_at + J) * nc + c] = best;
+            }
+    return img;
+}
+
+// <psi| sum_c e^{i 2 pi k.R'} X(R_c) |psi> over the cell blocks X [cell][n_ao][n_ao], R' the band
+// image of each atom-pair block
+template <typename T>
+cplx band_element(const Dataset &ds, const T *X, const std::vector<std::array<int, 3>> &img, const double *kb,
+                  const cplx *psi)
+{
+    const int nao = ds.n_ao, n_at = ds.n_atoms(), nc = static_cast<int>(ds.hx_cells.size());
+    std::vector<int> atom(nao);
+    for (int a = 0, o = 0; a < n_at; ++a)
+        for (int i = 0; i < ds.nao_at[a]; ++i) atom[o++] = a;
+    cplx acc(0, 0);
+    for (int c = 0; c < nc; ++c)
+    {
+        const T *Xc = X + static_cast<size_t>(c) * nao * nao;
+        for (int p = 0; p < nao; ++p)
+        {
+            cplx row(0, 0);
+            for (int q = 0; q < nao; ++q)
+            {
+                const std::array<int, 3> &R = img[(static_cast<size_t>(atom[p]) * n_at + atom[q]) * nc + c];
+                const double th = 2.0 * M_PI * (kb[0] * R[0] + kb[1] * R[1] + kb[2] * R[2]);
+                row += std::polar(1.0, th) * cplx(Xc[static_cast<size_t>(p) * nao + q]) * psi[q];
+            }
+            acc += std::conj(psi[p]) * row;
+        }
+    }
+    return acc;
+}
+
+const cplx *band_psi(const Dataset &ds, int s, int kb, int n)
+{
+    GB_REQUIRE(ds.band_nk > 0 && static_cast<int>(ds.band_kfrac.size()) == 3 * ds.band_nk,
+               "band data not set: librpa_set_band_kvec and librpa_set_band_occ_eigval with the same count");
+    GB_REQUIRE(s >= 0 && s < ds.band_ns && kb >= 0 && kb < ds.band_nk && n >= 0 && n < ds.band_nst,
+               "band state index out of range");
+    return ds.band_wfc.data() + ((static_cast<size_t>(s) * ds.band_nk + kb) * ds.band_nst + n) * ds.n_ao;
+}
+} // namespace
+
+double exx_band_state(const Dataset &ds, int s, int kb, int n)
+{
+    GB_REQUIRE(s < static_cast<int>(ds.hx_r.size()), "no exchange matrix: build the exchange first");
+    const auto img = band_images(ds, ds.n_atoms(), ds.hx_cells);
+    return -band_element(ds, ds.hx_r[s].data(), img, ds.band_kfrac.data() + 3 * kb, band_psi(ds, s, kb, n)).real();
+}
+
+std::vector<cplx> sigc_band_iw(const Dataset &ds, int s, int kb, int n)
+{
+    GB_REQUIRE(s < static_cast<int>(ds.sigc_r.size()), "no self-energy: build G0W0 first");
+    const int nw = static_cast<int>(ds.gw_omega.size()), nao = ds.n_ao, nc = static_cast<int>(ds.hx_cells.size());
+    const auto img = band_images(ds, ds.n_atoms(), ds.hx_cells);
+    const cplx *psi = band_psi(ds, s, kb, n);
+    std::vector<cplx> out(nw);
+    for (int w = 0; w < nw; ++w)
+        out[w] = band_element(ds, ds.sigc_r[s].data() + static_cast<size_t>(w) * nc * nao * nao, img,
+                              ds.band_kfrac.data() + 3 * kb, psi);
+    return out;
 }
 
 void build_g0w0(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)

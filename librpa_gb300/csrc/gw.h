@@ -1,6 +1,9 @@
 // Exact exchange (k-grids) and the G0W0 self-energy (Gamma point) on the GPU (gw.cu).
 #pragma once
 
+#include <complex>
+#include <vector>
+
 #include "../../include/librpa_options.h"
 
 namespace gb {
@@ -21,5 +24,10 @@ double exx_state(const Dataset &ds, int s, int k, int n);
 void build_g0w0(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);
 void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);
 void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf);
+// At band k-point kb (librpa_set_band_*), after build_exx / build_g0w0: v_exx of band state n,
+// and the KS-diagonal Sigma_c(i omega) of band state n, each from the R blocks moved to the image
+// nearest to the atom pair (exx.cpp:683-725) and summed with e^{i 2 pi k.R}.
+double exx_band_state(const Dataset &ds, int s, int kb, int n);
+std::vector<std::complex<double>> sigc_band_iw(const Dataset &ds, int s, int kb, int n);
 
 } // namespace gb

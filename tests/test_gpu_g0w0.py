@@ -6,7 +6,7 @@ import pytest
 
 import librpa_gb300 as L
 from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
-from oracle.gw_oracle import HA2EV, exx_kgrid, g0w0_gamma
+from oracle.gw_oracle import HA2EV, BandPoints, exx_kgrid, g0w0_gamma
 from oracle.rpa_oracle import Options as OOpts
 
 pytestmark = pytest.mark.gpu
@@ -140,3 +140,38 @@ def test_mgo_kgrid_g0w0_tables():
     e_qp = s.ekb - vxc + vexx + sig.real
     got = np.stack([vexx[0] * HA2EV, sig[0].real * HA2EV, sig[0].imag * HA2EV, e_qp[0] * HA2EV], axis=-1)
     np.testing.assert_allclose(got, s.qp_tables[:, :, 4:8], rtol=0, atol=6e-6)
+    # band k-points placed on three SCF points reproduce those points' results (task = g0w0_band)
+    kb = [0, 5, 13]
+    h.set_band_points(h_kfrac(s)[kb], s.wg[:, kb], s.ekb[:, kb], s.wfc[:, kb])
+    # (the k fractions of the input carry about 1e-11 of rounding, which the images shifted by a
+    # period turn into phase differences of about 1e-10: far below the tables' print precision)
+    vb = h.get_exx_pot_band_k(o, s.n_spins, [0, 1, 2], 0, nb)
+    np.testing.assert_allclose(vb, vexx[:, kb], rtol=0, atol=1e-9)
+    sb = h.get_g0w0_sigc_band_k(o, s.n_spins, [0, 1, 2], 0, nb, vxc[:, kb], vb)
+    np.testing.assert_allclose(sb, sig[:, kb], rtol=0, atol=1e-8)
+
+
+def h_kfrac(s):
+    """Fractional coordinates of the SCF k-points (k_cart / 2 pi times the lattice vectors)."""
+    return (np.asarray(s.kvecs) / (2 * np.pi)) @ np.asarray(s.latvec).T
+
+
+def test_periodic_exchange_at_band_points_off_the_grid():
+    """v_exx at k-points off the SCF grid (task = exx_band) for BCC He: the R blocks moved to the
+    image nearest to each atom pair (exx.cpp:683-725) and summed at k, against the oracle's
+    restatement; arbitrary orthonormal band vectors, so every matrix element counts."""
+    s = load_he_exx()
+    rng = np.random.default_rng(3)
+    kf = np.array([[0.1, 0.2, 0.3], [0.5, 0.25, 0.0], [0.37, 0.0, 0.61]])
+    nkb, nb, nao = len(kf), s.n_bands, s.n_ao
+    wfc = np.zeros((s.n_spins, nkb, nb, nao), complex)
+    for k in range(nkb):
+        q, _ = np.linalg.qr(rng.standard_normal((nao, nao)) + 1j * rng.standard_normal((nao, nao)))
+        wfc[0, k] = q[:nb]
+    ekb = np.sort(rng.uniform(-1, 1, (s.n_spins, nkb, nb)), axis=-1)
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_band_points(kf, np.zeros_like(ekb), ekb, wfc)
+    got = h.get_exx_pot_band_k(L.Options(nfreq=16, tfgrids_type=L.Minimax), s.n_spins, list(range(nkb)), 0, nb)
+    ref = exx_kgrid(oracle_input(s), s.v_cut, BandPoints(kf, wfc, ekb, s.efermi))
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10)
