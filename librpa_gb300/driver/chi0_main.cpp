@@ -1,12 +1,14 @@
-// chi0_main: the task = rpa driver of LibRPA (driver/main.cpp, driver/task/rpa.cpp) on top of
-// this library's C API.
+// chi0_main: the task = rpa / exx / g0w0 driver of LibRPA (driver/main.cpp, driver/task/rpa.cpp,
+// exx.cpp, g0w0.cpp) on top of this library's C API.
 //
 // Reads `librpa.in` (key = value lines, '#' comments, the last occurrence of a key wins, as in
 // driver/inputfile.cpp) from the working directory, reads the FHI-aims export named by
 // input_dir (formats of driver/read_data.cpp), passes it through the librpa_set_* calls and
-// prints the RPA correlation energy in the layout of driver/task/rpa.cpp.
+// prints the RPA correlation energy in the layout of driver/task/rpa.cpp (task = exx: the v_exx
+// tables of task/exx.cpp; task = g0w0: the quasi-particle tables of task/g0w0.cpp, with the
+// keys n_params_anacon, replace_w_head, option_dielect_func, sqrt_coulomb_threshold).
 //
-// Keys: task (rpa), input_dir, nfreq, tfgrids_type, parallel_routing, cs_threshold,
+// Keys: task (rpa, exx, g0w0), input_dir, nfreq, tfgrids_type, parallel_routing, cs_threshold,
 // vq_threshold, libri_chi0_threshold_C, libri_chi0_threshold_G, minimax_emin/emax, and the
 // GPU controls gb300_chi0_precision (fp64 | bf16x3 | fp32), gb300_ec_path (lu | chol |
 // chol_fp64), gb300_screen_mode (off | threshold | mlp), gb300_screen_threshold.
@@ -144,7 +146,8 @@ int main()
         const auto p = read_params("librpa.in");
         auto par = [&](const std::string &k, const std::string &d) { return p.count(k) ? p.at(k) : d; };
         const std::string task = lower(par("task", "rpa"));
-        if (task != "rpa") die("this driver runs task = rpa only (got " + task + ")");
+        if (task != "rpa" && task != "exx" && task != "g0w0")
+            die("this driver runs task = rpa, exx or g0w0 (got " + task + ")");
         std::string dir = par("input_dir", "./");
         if (dir.back() != '/') dir += '/';
         const double cs_threshold = std::stod(par("cs_threshold", "1e-6"));
@@ -162,6 +165,12 @@ int main()
         opts.libri_chi0_threshold_G = std::stod(par("libri_chi0_threshold_G", "0"));
         opts.minimax_emin = std::stod(par("minimax_emin", "-1"));
         opts.minimax_emax = std::stod(par("minimax_emax", "-1"));
+        opts.n_params_anacon = std::stoi(par("n_params_anacon", std::to_string(opts.n_params_anacon)));
+        opts.option_dielect_func = std::stoi(par("option_dielect_func", std::to_string(opts.option_dielect_func)));
+        opts.sqrt_coulomb_threshold = std::stod(par("sqrt_coulomb_threshold", std::to_string(opts.sqrt_coulomb_threshold)));
+        const std::string rwh = lower(par("replace_w_head", "f"));
+        opts.replace_w_head = (rwh == "t" || rwh == "true" || rwh == ".true." || rwh == "1") ? LIBRPA_SWITCH_ON
+                                                                                             : LIBRPA_SWITCH_OFF;
         const std::string shr = lower(par("use_shrink_abfs", "f"));
         const bool shrink = shr == "t" || shr == "true" || shr == ".true." || shr == "1";
         opts.use_shrink_abfs = shrink ? LIBRPA_SWITCH_ON : LIBRPA_SWITCH_OFF;
@@ -183,6 +192,8 @@ int main()
         librpa_gb300_set_options(h, &go);
 
         Mesh m;
+        std::vector<double> wg_h, ekb_h;  // occupations (as read) and eigenvalues [s][k][n]
+        double latv[9] = {0};            // lattice vectors, rows a1, a2, a3 (Bohr)
         // band_out (read_data.cpp:32-140): nk ns nb nao efermi, then per (k, s) block n f e e_eV
         {
             const auto t = tokens(dir + "band_out");
@@ -192,7 +203,9 @@ int main()
             m.nb = std::stoi(t.at(q++));
             m.nao = std::stoi(t.at(q++));
             const double ef = std::stod(t.at(q++));
-            std::vector<double> wg(static_cast<size_t>(m.ns) * m.nk * m.nb), ekb(wg.size());
+            std::vector<double> &wg = wg_h, &ekb = ekb_h;
+            wg.assign(static_cast<size_t>(m.ns) * m.nk * m.nb, 0.0);
+            ekb.assign(wg.size(), 0.0);
             for (int kk = 0; kk < m.nk; ++kk)
                 for (int ss = 0; ss < m.ns; ++ss)
                 {
@@ -213,6 +226,7 @@ int main()
         {
             double lat[9], G[9];
             for (int i = 0; i < 9; ++i) lat[i] = std::stod(stru.at(i));
+            std::copy(lat, lat + 9, latv);
             for (int i = 0; i < 9; ++i) G[i] = std::stod(stru.at(9 + i));
             librpa_set_latvec_and_G(h, lat, G);
             m.nat = std::stoi(stru.at(18));
@@ -516,14 +530,14 @@ int main()
                 librpa_gb300_set_shrink_sinvS(h, reps[iq], n_s, n_l, ur.data(), ui.data());
             }
         }
-        // coulomb_mat* binary (read_data.cpp:1472-1577): n_irk n_local, then per block
-        // nbasbas brow erow bcol ecol iq q_weight and the rows (complex); atom-pair blocks I <= J
-        {
+        // coulomb_mat* / coulomb_cut* binary (read_data.cpp:1472-1577): n_irk n_local, then per
+        // block nbasbas brow erow bcol ecol iq q_weight and the rows (complex); atom-pair blocks I <= J
+        auto read_coulomb = [&](const std::string &prefix, const std::vector<int> &nabf_v, bool cut) {
             std::vector<int> off_at(m.nat + 1, 0);
             for (int a = 0; a < m.nat; ++a) off_at[a + 1] = off_at[a] + nabf_v[a];
             std::map<int, std::vector<cplx>> full;
             int nbb = 0;
-            for (const auto &fn : files_with_prefix(dir, "coulomb_mat"))
+            for (const auto &fn : files_with_prefix(dir, prefix))
             {
                 if (is_text_file(fn))
                 {
@@ -589,9 +603,117 @@ int main()
                                 vr[static_cast<size_t>(a) * nn + c] = z.real();
                                 vi[static_cast<size_t>(a) * nn + c] = z.imag();
                             }
-                        librpa_set_aux_bare_coulomb_k_atom_pair(h, iq, I, J, nm, nn, vr.data(), vi.data(),
-                                                                opts.vq_threshold);
+                        if (cut)
+                            librpa_set_aux_cut_coulomb_k_atom_pair(h, iq, I, J, nm, nn, vr.data(), vi.data(),
+                                                                   opts.vq_threshold);
+                        else
+                            librpa_set_aux_bare_coulomb_k_atom_pair(h, iq, I, J, nm, nn, vr.data(), vi.data(),
+                                                                    opts.vq_threshold);
                     }
+        };
+        read_coulomb("coulomb_mat", nabf_v, false);
+
+        if (task == "exx" || task == "g0w0")
+        {
+            // k fractions: k_cart / 2 pi times the lattice vectors
+            std::vector<double> kfrac(3 * static_cast<size_t>(m.nk));
+            for (int k = 0; k < m.nk; ++k)
+                for (int d = 0; d < 3; ++d)
+                {
+                    double v = 0.0;
+                    for (int e = 0; e < 3; ++e) v += m.kvecs[3 * k + e] / (2.0 * M_PI) * latv[3 * d + e];
+                    kfrac[3 * k + d] = std::fabs(v) < 1e-12 ? 0.0 : v;
+                }
+            // driver/task/exx.cpp, driver/task/g0w0.cpp: the truncated Coulomb matrix, for G0W0 the
+            // dielectric function of the head correction (dielecfunc_out: omega, Re, Im per line;
+            // read_data.cpp:1211-1229) and v_xc (vxc_out: n_k n_s n_states, then per k and spin an
+            // "Ha eV" pair per state; read_data.cpp:142-182)
+            read_coulomb("coulomb_cut", m.nabf_at, true);
+            std::vector<int> iks(m.nk);
+            for (int k = 0; k < m.nk; ++k) iks[k] = k;
+            const int nst = m.nb;
+            std::vector<double> vexx(static_cast<size_t>(m.ns) * m.nk * nst);
+            librpa_get_exx_pot_kgrid(h, &opts, m.ns, m.nk, iks.data(), 0, nst, vexx.data());
+            if (librpa_get_last_error_code(h)) die(librpa_get_last_error(h));
+            const double ha2ev = 27.211386245988;
+            if (task == "exx")
+            {
+                for (int sp = 0; sp < m.ns; ++sp)
+                {
+                    std::printf("Spin channel %d\n", sp + 1);
+                    for (int k = 0; k < m.nk; ++k)
+                    {
+                        std::printf("k-point %d: (%.5f, %.5f, %.5f)\n", k + 1, kfrac[3 * k], kfrac[3 * k + 1],
+                                    kfrac[3 * k + 2]);
+                        std::printf("%-4s  %-10s  %-10s\n", "Band", "e_exx (Ha)", "e_exx (eV)");
+                        for (int n = 0; n < nst; ++n)
+                        {
+                            const double e = vexx[(static_cast<size_t>(sp) * m.nk + k) * nst + n];
+                            std::printf("%4d  %10.5f  %10.5f\n", n + 1, e, ha2ev * e);
+                        }
+                        std::printf("\n");
+                    }
+                }
+                librpa_destroy_handler(h);
+                return 0;
+            }
+            if (opts.replace_w_head == LIBRPA_SWITCH_ON && exists(dir + "dielecfunc_out"))
+            {
+                std::vector<double> om, df;
+                std::ifstream f(dir + "dielecfunc_out");
+                double w, re, im;
+                while (f >> w >> re >> im)
+                {
+                    om.push_back(w);
+                    df.push_back(re);
+                }
+                librpa_set_dielect_func_imagfreq(h, static_cast<int>(om.size()), om.data(), df.data());
+            }
+            const auto tv = tokens(dir + "vxc_out");
+            if (tv.size() < 3) die("cannot read vxc_out");
+            const int vk = std::stoi(tv[0]), vs = std::stoi(tv[1]), vn = std::stoi(tv[2]);
+            if (vk != m.nk || vs != m.ns || vn < nst) die("vxc_out dimensions differ from the mean field");
+            std::vector<double> vxc(static_cast<size_t>(m.ns) * m.nk * nst);
+            {
+                size_t q = 3;
+                for (int k = 0; k < vk; ++k)
+                    for (int sp = 0; sp < vs; ++sp)
+                        for (int n = 0; n < vn; ++n, q += 2)
+                            if (n < nst) vxc[(static_cast<size_t>(sp) * m.nk + k) * nst + n] = std::stod(tv.at(q));
+            }
+            std::vector<double> sre(vxc.size()), sim(vxc.size());
+            librpa_get_g0w0_sigc_kgrid(h, &opts, m.ns, m.nk, iks.data(), 0, nst, vxc.data(), vexx.data(), sre.data(),
+                                       sim.data());
+            if (librpa_get_last_error_code(h)) die(librpa_get_last_error(h));
+            for (int sp = 0; sp < m.ns; ++sp)
+                for (int k = 0; k < m.nk; ++k)
+                    for (int n = 0; n < nst; ++n)
+                        if (std::isnan(sre[(static_cast<size_t>(sp) * m.nk + k) * nst + n]))
+                            std::printf("Warning! QPE solver failed for spin %d, kpoint %d, state %d\n", sp + 1, k + 1,
+                                        n + 1);
+            const std::string banner(124, '-');
+            std::printf("Printing quasi-particle energy [unit: eV]\n\n");
+            for (int sp = 0; sp < m.ns; ++sp)
+                for (int k = 0; k < m.nk; ++k)
+                {
+                    std::printf("spin %2d, k-point %4d: (%.5f, %.5f, %.5f) \n", sp + 1, k + 1, kfrac[3 * k],
+                                kfrac[3 * k + 1], kfrac[3 * k + 2]);
+                    std::printf("%124s\n", banner.c_str());
+                    std::printf("%5s %16s %16s %16s %16s %16s %16s %16s\n", "State", "occ", "e_mf", "v_xc", "v_exx",
+                                "ReSigc", "ImSigc", "e_qp");
+                    std::printf("%124s\n", banner.c_str());
+                    for (int n = 0; n < nst; ++n)
+                    {
+                        const size_t o = (static_cast<size_t>(sp) * m.nk + k) * nst + n;
+                        const double emf = ekb_h[o], e_qp = emf - vxc[o] + vexx[o] + sre[o];
+                        std::printf("%5d %16.5f %16.5f %16.5f %16.5f %16.5f %16.5f %16.5f\n", n + 1, wg_h[o],
+                                    emf * ha2ev, vxc[o] * ha2ev, vexx[o] * ha2ev, sre[o] * ha2ev, sim[o] * ha2ev,
+                                    e_qp * ha2ev);
+                    }
+                    std::printf("\n");
+                }
+            librpa_destroy_handler(h);
+            return 0;
         }
 
         int n_ibz = 0;

@@ -45,6 +45,8 @@ Produces (all committed, so the tests need no reference tree at run time):
                      printed by the reference run (refs/exx_aims_bccHe_k_parallel_libri/librpa/
                      librpa.out, Hartree and eV; the suite checks the first to 1e-4)
 
+  h2o_g0w0_dataset.tar.gz  the H2O G0W0 regression dataset itself (copied unchanged), for the
+                     driver's task = g0w0 test
   bn_shrink_dataset.tar.gz  the ABACUS BN case with an ABF shrink (2 atoms, 2x2x2 k; 60 + 59
                      ABFs, shrunk to 17 + 17) copied unchanged
                      (regression_tests/testcases/g0w0_band_abacus_BN_shrink_libri/input_librpa.tar.gz):
@@ -53,7 +55,7 @@ Produces (all committed, so the tests need no reference tree at run time):
                      E_c for it
 
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
-h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_g0w0|bn_shrink ...].
+h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_g0w0|bn_shrink|h2o_g0w0_dataset ...].
 """
 from __future__ import annotations
 
@@ -362,6 +364,13 @@ def he_exx(ref: Path):
     print("he_exx.npz written:", len(tables), "k-points")
 
 
+def h2o_g0w0_dataset(ref: Path):
+    import shutil
+    src = ref / "regression_tests/testcases/g0w0_aims_mole_H2O_libri/dataset.tar.gz"
+    shutil.copyfile(src, HERE / "h2o_g0w0_dataset.tar.gz")
+    print("h2o_g0w0_dataset.tar.gz written")
+
+
 def bn_shrink(ref: Path):
     import shutil
     src = ref / "regression_tests/testcases/g0w0_band_abacus_BN_shrink_libri/input_librpa.tar.gz"
@@ -375,8 +384,9 @@ if __name__ == "__main__":
         sys.exit("usage: make_fixtures.py /path/to/reference [fixture ...] (or set LIBRPA_REFERENCE)")
     ref = Path(src)
     which = sys.argv[2:] or ["h2o", "h2o_dataset", "he_dataset", "li_dataset", "minimax", "he_bcc", "g0w0",
-                             "li_g0w0", "he_exx", "mgo_g0w0", "bn_shrink"]
+                             "li_g0w0", "he_exx", "mgo_g0w0", "bn_shrink", "h2o_g0w0_dataset"]
     for name in which:
         {"h2o": h2o, "h2o_dataset": h2o_dataset, "minimax": minimax, "he_bcc": he_bcc, "g0w0": g0w0,
          "li_g0w0": li_g0w0, "he_exx": he_exx, "he_dataset": he_dataset, "li_dataset": li_dataset,
-         "mgo_g0w0": mgo_g0w0, "bn_shrink": bn_shrink}[name](ref)
+         "mgo_g0w0": mgo_g0w0, "bn_shrink": bn_shrink,
+         "h2o_g0w0_dataset": h2o_g0w0_dataset}[name](ref)

@@ -98,3 +98,54 @@ def test_driver_li_spin_polarised(tmp_path, lib):
     assert r.returncode == 0, r.stderr
     ec = float(re.search(r"\| Total EcRPA:\s*([-0-9.eE+]+)", r.stdout).group(1))
     assert abs(ec - ref) <= 1e-9, (ec, ref)
+
+
+H2O_G0W0_DATASET = ROOT / "tests" / "golden" / "h2o_g0w0_dataset.tar.gz"
+
+
+def _run_task(tmp_path, lib, task, dataset, extra=""):
+    with tarfile.open(dataset) as tf:
+        tf.extractall(tmp_path, filter="data")
+    data = next(tmp_path.rglob("band_out")).parent
+    (tmp_path / "librpa.in").write_text(f"task = {task}\ninput_dir = {data}\nparallel_routing = libri\n{extra}")
+    return subprocess.run([_driver(lib)], cwd=tmp_path, capture_output=True, text=True, timeout=900)
+
+
+def test_driver_exx_and_g0w0_tasks_read_without_gpu(tmp_path, lib):
+    """task = exx (BCC He) and task = g0w0 (H2O) parse their extra files up to the GPU call."""
+    if lib.librpa_gb300_device_count() > 0:
+        pytest.skip("a GPU is visible: the GPU tests cover the full runs")
+    r = _run_task(tmp_path / "exx", lib, "exx", HE_DATASET)
+    assert r.returncode == 1 and ("CUDA" in r.stderr or "device" in r.stderr), r.stderr
+    r = _run_task(tmp_path / "g0w0", lib, "g0w0", H2O_G0W0_DATASET, "nfreq = 16\nn_params_anacon = 16\n")
+    assert r.returncode == 1 and ("CUDA" in r.stderr or "device" in r.stderr), r.stderr
+
+
+@pytest.mark.gpu
+def test_driver_exx_task_bcc_he(tmp_path, lib):
+    """task = exx on the reference's BCC He exchange dataset: the printed v_exx tables (Band,
+    e_exx in Hartree and eV, every k-point) match the reference's printed tables."""
+    import numpy as np
+    from conftest import load_he_exx
+    r = _run_task(tmp_path, lib, "exx", HE_DATASET)
+    assert r.returncode == 0, r.stderr
+    rows = [[float(x) for x in l.split()] for l in r.stdout.splitlines() if re.match(r"^\s*\d+\s+-?\d+\.\d{5}\s+-?\d+\.\d{5}\s*$", l)]
+    got = np.array(rows).reshape(8, 8, 3)
+    np.testing.assert_allclose(got, load_he_exx().exx_tables, rtol=0, atol=1.1e-5)
+
+
+@pytest.mark.gpu
+def test_driver_g0w0_task_h2o(tmp_path, lib):
+    """task = g0w0 on the reference's H2O G0W0 dataset with its own settings (16 minimax points,
+    16 Pade parameters), FP64 chi0: the printed quasi-particle table matches the reference's."""
+    import numpy as np
+    from conftest import load_h2o_g0w0
+    r = _run_task(tmp_path, lib, "g0w0", H2O_G0W0_DATASET,
+                  "nfreq = 16\nn_params_anacon = 16\ngb300_chi0_precision = fp64\n")
+    assert r.returncode == 0, r.stderr
+    rows = [[float(x) for x in l.split()] for l in r.stdout.splitlines()
+            if re.match(r"^\s*\d+(\s+-?\d+\.\d{5}){7}\s*$", l)]
+    got = np.array(rows)
+    t = load_h2o_g0w0().qp_table
+    assert got.shape == t.shape, (got.shape, t.shape)
+    np.testing.assert_allclose(got[:, 2:], t[:, 2:], rtol=0, atol=1.1e-5)
