@@ -232,28 +232,6 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         din->vblob.alloc(ds.vq_blob.size());
         din->vblob.upload(reinterpret_cast<const cuDoubleComplex *>(ds.vq_blob.data()), ds.vq_blob.size(), st);
         DevBuf<double> d_csblob(ds.cs_blob.size() + csf.extra.size());
-        // The RI blob (the bulk of the inputs) is page-locked for its copy: a pageable copy runs
-        // through the driver's bounce buffers at a fraction of the host link's bandwidth.  Memory
-        // the caller registered already, or a failed registration, is copied as it is.
-        struct Pin
-        {
-            void *p = nullptr;
-            cudaStream_t s;
-            ~Pin()
-            {
-                if (!p) return;
-                cudaStreamSynchronize(s);  // the copy has finished reading it (also on an error path)
-                cudaHostUnregister(p);
-            }
-        } pin{nullptr, st};
-        if (ds.cs_blob.size() * sizeof(double) >= (64u << 20))
-        {
-            if (cudaHostRegister(ds.cs_blob.data(), ds.cs_blob.size() * sizeof(double), cudaHostRegisterDefault) ==
-                cudaSuccess)
-                pin.p = ds.cs_blob.data();
-            else
-                cudaGetLastError();  // not an error of this call: copy from pageable memory
-        }
         d_csblob.upload(ds.cs_blob.data(), ds.cs_blob.size(), st);
         if (!csf.extra.empty())
             GB_CUDA(cudaMemcpyAsync(d_csblob.get() + ds.cs_blob.size(), csf.extra.data(),
