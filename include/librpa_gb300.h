@@ -206,7 +206,7 @@ int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, 
 
 /* No counterpart in the reference: librpa_get_rpa_correlation_energy for n independent handlers
  * (separate systems, such as a batch of small cells), opts[i] for handler i, run concurrently on
- * up to n_threads host threads (0: up to 8), each call on its own CUDA stream so that their GPU
+ * up to n_threads host threads (0: up to 4), each call on its own CUDA stream so that their GPU
  * work overlaps.  ec[i] receives handler i's E_c, NaN on error with the message on that handler.
  * The handlers must be distinct.  Returns the number of failed calls, or -1 on a bad argument
  * (null pointers, a handler listed twice) with the message in librpa_get_last_error(NULL). */

@@ -849,7 +849,7 @@ int librpa_gb300_get_rpa_correlation_energy_batch(LibrpaHandler **hs, int n, con
             nq[i] = std::max<int>(1, static_cast<int>(std::unique(reps.begin(), reps.end()) - reps.begin()));
         }
         const int hw = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
-        const int nt = std::max(1, std::min(n, n_threads > 0 ? n_threads : std::min(8, hw)));
+        const int nt = std::max(1, std::min(n, n_threads > 0 ? n_threads : std::min(4, hw)));
         std::atomic<int> next{0}, bad{0};
         auto work = [&] {
             std::vector<double> re, im;

@@ -27,6 +27,7 @@ def main(argv=None):
     ap.add_argument("--chi0", default="bf16x3", choices=list(CHI0))
     ap.add_argument("--ec", default="chol", choices=list(EC))
     ap.add_argument("--repeat", type=int, default=1)
+    ap.add_argument("--threads", type=int, default=0, help="host threads of the concurrent batch call (0: up to 4)")
     ap.add_argument("--concurrent", action="store_true",
                     help="batch workloads: one librpa_gb300_get_rpa_correlation_energy_batch call for all systems")
     a = ap.parse_args(argv)
@@ -61,7 +62,7 @@ def run_batch(a):
     for _ in range(a.repeat):
         t = time.time()
         if a.concurrent:
-            ecs = list(rpa_correlation_energy_batch([h for h, _, _ in hs], [o for _, o, _ in hs]))
+            ecs = list(rpa_correlation_energy_batch([h for h, _, _ in hs], [o for _, o, _ in hs], a.threads))
         else:
             ecs = [h.get_rpa_correlation_energy(o, n_ibz(s))[0] for h, o, s in hs]
         dt = time.time() - t
