@@ -204,6 +204,16 @@ int librpa_gb300_mlp_loss_grad(const float *params, const float *norm, const flo
 int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
                                   double *im);
 
+/* No counterpart in the reference (the internal interpolate_dielec_func,
+ * src/core/dielecmodel.cpp:65-104, exposed for checking): the macroscopic dielectric function
+ * eps(i omega) given at n_in frequencies, mapped onto n_out target frequencies as the G0W0 head
+ * correction maps it onto the minimax frequencies.  option 0: the values unchanged (n_in must
+ * equal n_out); 1: cubic spline (src/math/interpolate.cpp); 2: least-squares fit of the two-term
+ * Havriliak-Negami model (src/math/fitting.cpp).  Host work; needs no GPU.  Returns 0 on success,
+ * 1 on error (message: librpa_get_last_error(NULL)). */
+int librpa_gb300_interpolate_dielec_func(int option, int n_in, const double *omega_in, const double *eps_in,
+                                         int n_out, const double *omega_out, double *eps_out);
+
 /* No counterpart in the reference: librpa_get_rpa_correlation_energy for n independent handlers
  * (separate systems, such as a batch of small cells), opts[i] for handler i, run concurrently on
  * up to n_threads host threads (0: up to 4), each call on its own CUDA stream so that their GPU

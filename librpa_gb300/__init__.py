@@ -143,7 +143,7 @@ EXPORTS = [
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
-    "librpa_gb300_solve_qpe", "librpa_gb300_phase_tables",
+    "librpa_gb300_solve_qpe", "librpa_gb300_phase_tables", "librpa_gb300_interpolate_dielec_func",
 ]
 
 _lib = None
@@ -227,6 +227,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_mlp_loss_grad": (i, [vp, vp, vp, vp, i, vp, C.POINTER(C.c_double)]),
         "librpa_gb300_solve_qpe": (i, [i, i, _dp, _dp, _dp, i, _dp, d, _dp, _dp, _dp, _dp, _dp]),
         "librpa_gb300_phase_tables": (i, [vp, vp, vp, vp, vp, vp, vp, vp]),
+        "librpa_gb300_interpolate_dielec_func": (i, [i, i, _dp, _dp, i, _dp, _dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -562,6 +563,19 @@ def solve_qpe(omegas, sigc_iw, e_mf, e_fermi, vxc, vexx, n_params=-1):
     if rc < 0:
         raise LibrpaError(lib.librpa_get_last_error(None).decode())
     return e_qp, sr + 1j * si, rc
+
+
+def interpolate_dielec_func(option, omega_in, eps_in, omega_target):
+    """eps(i omega) mapped onto target frequencies as the G0W0 head correction maps it onto the
+    minimax ones (librpa_gb300_interpolate_dielec_func, host only): option 0 the given values,
+    1 cubic spline, 2 Havriliak-Negami fit."""
+    lib = load_library()
+    f64 = lambda a: np.ascontiguousarray(a, np.float64)
+    om, eps, tg = f64(omega_in), f64(eps_in), f64(omega_target)
+    out = np.zeros(len(tg))
+    if lib.librpa_gb300_interpolate_dielec_func(int(option), len(om), om, eps, len(tg), tg, out) != 0:
+        raise LibrpaError(lib.librpa_get_last_error(None).decode())
+    return out
 
 
 def minimax_grid(n, emin, emax, regularization=0.0):

@@ -20,6 +20,7 @@
 #include "chol.h"
 #include "common.h"
 #include "dataset.h"
+#include "dielec.h"
 #include "screen.h"
 #include "host_tables.h"
 #include "minimax.h"
@@ -1466,6 +1467,24 @@ int librpa_gb300_mlp_loss_grad(const float *params, const float *norm, const flo
         }
         cudaStreamDestroy(st);
         if (loss) *loss = l;
+        rc = 0;
+    });
+    return rc;
+}
+
+// interpolate_dielec_func (dielecmodel.cpp:65-104) on caller arrays; host work (dielec.cpp)
+int librpa_gb300_interpolate_dielec_func(int option, int n_in, const double *omega_in, const double *eps_in,
+                                         int n_out, const double *omega_out, double *eps_out)
+{
+    int rc = 1;
+    guarded(nullptr, [&] {
+        GB_REQUIRE(n_in > 0 && n_out >= 0, "need n_in > 0 and n_out >= 0");
+        GB_REQUIRE(omega_in && eps_in && (n_out == 0 || (omega_out && eps_out)), "null array");
+        const std::vector<double> out =
+            gb::interpolate_dielec_func(option, std::vector<double>(omega_in, omega_in + n_in),
+                                        std::vector<double>(eps_in, eps_in + n_in),
+                                        std::vector<double>(omega_out, omega_out + n_out));
+        std::copy(out.begin(), out.end(), eps_out);
         rc = 0;
     });
     return rc;

@@ -32,6 +32,7 @@
 #include "common.h"
 #include "cs_fold.h"
 #include "dataset.h"
+#include "dielec.h"
 #include "gw.h"
 #include "host_tables.h"
 #include "kernels.h"
@@ -766,8 +767,6 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     require_gamma(ds);
     GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
     GB_REQUIRE(!ds.vq_blocks.empty(), "the Coulomb matrix of the dielectric function is not set");
-    GB_REQUIRE(opts.replace_w_head != LIBRPA_SWITCH_ON,
-               "the head correction of W belongs to k-grid inputs; the Gamma-point path does not apply it");
     GB_REQUIRE(opts.use_shrink_abfs != LIBRPA_SWITCH_ON,
                "use_shrink_abfs: the Gamma-point G0W0 chain has no unfolding of W to the large ABF basis");
     // chi0(q = 0, omega) from the RPA path, kept on the device
@@ -963,14 +962,17 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                "use_shrink_abfs: the G0W0 chain has no unfolding of W to the large ABF basis");
     const int nw = tf.n;
     const bool head = opts.replace_w_head == LIBRPA_SWITCH_ON && !ds.dielect_eps.empty();
+    // eps_mac on the minimax frequencies (compute_g0w0.cpp:103-107, interpolate_dielec_func):
+    // option 0 the given values, 1 a cubic spline, 2 a fitted Havriliak-Negami model; the
+    // option 3 head of the reference comes from its velocity-matrix model, which its C API
+    // does not feed
+    std::vector<double> eps_head;
     if (head)
     {
-        // interpolate_dielec_func (src/core/dielecmodel.cpp:65-104), option 0: the given values
-        GB_REQUIRE(opts.option_dielect_func == 0,
-                   "replace_w_head: only option_dielect_func = 0 (the dielectric function given at the minimax "
-                   "frequencies) is supported");
-        GB_REQUIRE(static_cast<int>(ds.dielect_eps.size()) == nw,
-                   "replace_w_head: the dielectric function must be given at the nfreq minimax frequencies");
+        GB_REQUIRE(opts.option_dielect_func >= 0 && opts.option_dielect_func <= 2,
+                   "replace_w_head: option_dielect_func must be 0, 1 or 2 (3 needs the head and wings of the "
+                   "dielectric model, which the C API does not set)");
+        eps_head = interpolate_dielec_func(opts.option_dielect_func, ds.dielect_omega, ds.dielect_eps, tf.omega);
     }
     // chi0(q, omega) of every IBZ q from the RPA path, kept on the device
     {
@@ -1114,7 +1116,7 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                     for (int r = 0; r < Nc; ++r)
                         for (int c = 0; c < Nc; ++c) x00 += z0[r] * hx[static_cast<size_t>(w) * NN + static_cast<size_t>(r) * Nc + c] * z0[c];
                     x00 *= w0;
-                    const cplx d = (1.0 - ds.dielect_eps[w]) - x00;
+                    const cplx d = (1.0 - eps_head[w]) - x00;
                     double *E = hxe.data() + static_cast<size_t>(w) * M4;
                     for (int r = 0; r < Nc; ++r)
                         for (int c = 0; c < Nc; ++c)
@@ -1383,7 +1385,11 @@ std::vector<cplx> sigc_band_iw(const Dataset &ds, int s, int kb, int n)
 
 void build_g0w0(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)
 {
-    if (ds.n_kpts > 1)
+    // the head of the dielectric matrix is replaced at q = 0 whenever a dielectric function is
+    // set (compute_g0w0.cpp:103-107, epsilon.cpp:2110-2160), Gamma-only inputs included: the
+    // k-grid chain (complex W, one q-point) carries it
+    const bool head = opts.replace_w_head == LIBRPA_SWITCH_ON && !ds.dielect_eps.empty();
+    if (ds.n_kpts > 1 || head)
         build_g0w0_kgrid(ds, opts, tf);
     else
         build_g0w0_gamma(ds, opts, tf);

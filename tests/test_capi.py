@@ -141,7 +141,8 @@ def test_invalid_routing_is_rejected_before_any_gpu_work(lib):
 
 def test_g0w0_and_exchange_input_checks_before_any_gpu_work(lib):
     """The exchange and G0W0 take k-grid inputs (MgO, 3x3x3) and reach the GPU (here: none); the
-    G0W0 head correction needs the dielectric function at the nfreq minimax frequencies, and the
+    G0W0 head correction with option_dielect_func = 0 needs the dielectric function at the nfreq
+    minimax frequencies (1 and 2 interpolate it, 3 is not fed by the C API), and the
     exchange refuses an input without the truncated Coulomb matrix."""
     from conftest import load_mgo
     s = load_mgo()
@@ -154,6 +155,10 @@ def test_g0w0_and_exchange_input_checks_before_any_gpu_work(lib):
         with pytest.raises(L.LibrpaError, match="nfreq minimax frequencies"):
             h.get_g0w0_sigc_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax, replace_w_head=1), 1, [0], 0, 4,
                                   np.zeros(4), np.zeros(4))
+        # the velocity-matrix head and wings (option 3) have no setter in the C API
+        with pytest.raises(L.LibrpaError, match="option_dielect_func must be 0, 1 or 2"):
+            h.get_g0w0_sigc_kgrid(L.Options(nfreq=6, tfgrids_type=L.Minimax, replace_w_head=1, option_dielect_func=3),
+                                  1, [0], 0, 4, np.zeros(4), np.zeros(4))
     s = load_h2o()
     with L.Handler() as h:
         L.load_system(h, s)

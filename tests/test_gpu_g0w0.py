@@ -6,7 +6,8 @@ import pytest
 
 import librpa_gb300 as L
 from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
-from oracle.gw_oracle import HA2EV, BandPoints, exx_kgrid, g0w0_gamma
+from oracle.dielec import interpolate_dielec_func
+from oracle.gw_oracle import HA2EV, BandPoints, exx_kgrid, g0w0_gamma, g0w0_kgrid
 from oracle.rpa_oracle import Options as OOpts
 
 pytestmark = pytest.mark.gpu
@@ -80,6 +81,35 @@ def test_h2o_tensor_core_chi0_within_1mev(h2o):
     homo = int(np.sum(s.wg[0, 0] > 0)) - 1
     frontier = slice(homo - 2, homo + 4)
     assert np.abs(sig[0][frontier] - r["sigc"][0][frontier]).max() * HA2EV < 1e-3
+
+
+def test_gamma_point_head_correction_from_a_spline(h2o):
+    """A Gamma-only input with replace_w_head and a dielectric function given on its own 20-point
+    grid (option_dielect_func = 1): the reference replaces the head at q = 0 for any input once a
+    dielectric function is set, so the chain runs with eps_mac spline-mapped onto the 16 minimax
+    frequencies.  FP64 chi0 against the oracle's k-grid chain (one q-point) fed the oracle's
+    spline of the same data; the head moves Sigma_c well beyond that tolerance."""
+    s, r0 = h2o
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  n_params_anacon=s.n_params_anacon, replace_w_head=1, option_dielect_func=1)
+    om, _ = h.get_imaginary_frequency_grids(o)
+    grid = np.geomspace(om[0] * 0.7, om[-1] * 1.3, 20)
+    eps = 1.0 + 1.5 / (1.0 + (grid / 0.4) ** 2)
+    h.set_dielect_func_imagfreq(grid, eps)
+    nb = s.n_bands
+    vexx = h.get_exx_pot_kgrid(o, s.n_spins, [0], 0, nb)
+    vxc = s.vxc.reshape(s.n_spins, 1, nb)
+    sig = h.get_g0w0_sigc_kgrid(o, s.n_spins, [0], 0, nb, vxc, vexx)
+    iw = h.g0w0_sigc_iw(0, 0, nb, s.nfreq)
+    epsmac = interpolate_dielec_func(1, grid, eps, om)
+    r = g0w0_kgrid(oracle_input(s), s.v_cut, s.vxc, OOpts(nfreq=s.nfreq), n_params=s.n_params_anacon,
+                   epsmac=epsmac)
+    np.testing.assert_allclose(iw, np.asarray(r["sigc_iw"][0]).reshape(iw.shape), rtol=0, atol=1e-10)
+    np.testing.assert_allclose(sig[0, 0], np.asarray(r["sigc"][0]).ravel(), rtol=0, atol=1e-7)
+    assert np.abs(iw - r0["sigc_iw"][0]).max() > 1e-4
 
 
 def test_li_spin_polarised_table():
