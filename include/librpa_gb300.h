@@ -237,6 +237,13 @@ int librpa_gb300_get_rpa_correlation_energy_batch(LibrpaHandler **hs, int n, con
 void librpa_gb300_set_shrink_basis(LibrpaHandler *h, int natoms, const size_t *nbs_aux_small);
 void librpa_gb300_set_shrink_sinvS(LibrpaHandler *h, int ik, int n_small, int n_large, const double *re,
                                    const double *im);
+/* The RI coefficients in the small basis (the reference driver's Cs_shrinked_data), for the
+ * exchange and G0W0 of a shrunk input: the exchange contracts them with the truncated Coulomb
+ * matrix of the small basis, while chi0 and the correlation self-energy use those of
+ * librpa_set_lri_coeff, W_c being taken back to that basis as U^H W_c U (unfold_abfs_Wc).
+ * Arguments as librpa_set_lri_coeff, with naux_mu the small ABF count of atom I. */
+void librpa_gb300_set_shrink_lri_coeff(LibrpaHandler *h, int I, int J, int nbasis_i, int nbasis_j, int naux_mu,
+                                       const int R[3], const double *Cs_in);
 
 /* Number of CUDA devices visible (0 when there is no GPU). */
 int librpa_gb300_device_count(void);

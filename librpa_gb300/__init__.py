@@ -139,7 +139,7 @@ EXPORTS = [
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
     "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw", "librpa_gb300_get_rpa_correlation_energy_batch",
-    "librpa_gb300_set_shrink_basis", "librpa_gb300_set_shrink_sinvS",
+    "librpa_gb300_set_shrink_basis", "librpa_gb300_set_shrink_sinvS", "librpa_gb300_set_shrink_lri_coeff",
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
     "librpa_gb300_copy_chi0_qw", "librpa_gb300_load_chi0_qw", "librpa_gb300_selftest_chol_ozaki",
@@ -201,6 +201,7 @@ def load_library(path: str | Path | None = None):
         "librpa_gb300_get_rpa_correlation_energy_batch": (i, [vp, i, vp, i, _dp]),
         "librpa_gb300_set_shrink_basis": (None, [vp, i, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]),
         "librpa_gb300_set_shrink_sinvS": (None, [vp, i, i, i, _dp, _dp]),
+        "librpa_gb300_set_shrink_lri_coeff": (None, [vp, i, i, i, i, i, _ip, _dp]),
         "librpa_gb300_init_options": (None, [C.POINTER(GB300Options)]),
         "librpa_gb300_set_options": (None, [vp, C.POINTER(GB300Options)]),
         "librpa_gb300_get_stats": (None, [vp, C.POINTER(GB300Stats)]),
@@ -340,6 +341,12 @@ class Handler:
         U = np.asarray(U)
         self.lib.librpa_gb300_set_shrink_sinvS(self.h, ik, U.shape[0], U.shape[1], _f64(U.real).ravel(),
                                                _f64(U.imag).ravel())
+        self._check()
+
+    def set_shrink_lri_coeff(self, I, J, nbasis_i, nbasis_j, naux_mu_small, R, Cs):
+        """An RI block in the small ABF basis (the exchange of a shrunk input)."""
+        r = np.ascontiguousarray(R, dtype=np.int32)
+        self.lib.librpa_gb300_set_shrink_lri_coeff(self.h, I, J, nbasis_i, nbasis_j, naux_mu_small, r, _f64(Cs).ravel())
         self._check()
 
     def set_latvec_and_G(self, lat_mat, G_mat):
@@ -619,8 +626,10 @@ def load_system(h: Handler, s, routing=LIBRI):
         reps = list(dict.fromkeys(int(x) for x in s.ibz_map))
         for iq, U in s.sinvS.items():
             h.set_shrink_sinvS(reps[iq], U)
+        for (I, J, R), m in (getattr(s, "Cs_small", None) or {}).items():
+            h.set_shrink_lri_coeff(I, J, s.nao[I], s.nao[J], s.nabf_small[I], R, m)
     for (ik, I, J), v in getattr(s, "v_cut", {}).items():
-        h.set_aux_cut_coulomb_k_atom_pair(ik, I, J, s.nabf[I], s.nabf[J], v.real, v.imag, 0.0)
+        h.set_aux_cut_coulomb_k_atom_pair(ik, I, J, nbv[I], nbv[J], v.real, v.imag, 0.0)
 
 
 def rpa_correlation_energy_batch(handlers, opts, n_threads=0):

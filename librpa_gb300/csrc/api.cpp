@@ -518,7 +518,7 @@ void librpa_set_ao_basis_aux(LibrpaHandler *h, int natoms, const size_t *nbs)
 void librpa_gb300_set_shrink_basis(LibrpaHandler *h, int natoms, const size_t *nbs_aux_small)
 {
     guarded(h, [&] {
-        Dataset *ds = get_ds(h);
+        Dataset *ds = get_ds(h); ds->generation++;
         GB_REQUIRE(natoms > 0 && nbs_aux_small, "natoms must be positive and the counts given");
         ds->shrink_nabf.assign(nbs_aux_small, nbs_aux_small + natoms);
     });
@@ -528,7 +528,7 @@ void librpa_gb300_set_shrink_sinvS(LibrpaHandler *h, int ik, int n_small, int n_
                                    const double *im)
 {
     guarded(h, [&] {
-        Dataset *ds = get_ds(h);
+        Dataset *ds = get_ds(h); ds->generation++;
         GB_REQUIRE(ik >= 0 && n_small > 0 && n_large > 0 && re, "invalid shrink transform arguments");
         Dataset::ShrinkU &u = ds->shrink_u[ik];
         u.n_small = n_small;
@@ -601,6 +601,27 @@ void librpa_set_ibz_mapping(LibrpaHandler *h, int nkpts, const int *map)
     });
 }
 
+namespace {
+// One RI block (I, J, R) copied into a block store, replacing an earlier block of the same key.
+void store_cs_block(std::vector<double> &blob, std::vector<gb::CsBlock> &blocks,
+                    std::map<std::array<int, 5>, size_t> &index, int I, int J, int ni, int nj, int nmu,
+                    const int R[3], const double *Cs)
+{
+    const size_t n = static_cast<size_t>(ni) * nj * nmu;
+    std::array<int, 5> key{I, J, R[0], R[1], R[2]};
+    auto it = index.find(key);
+    if (it != index.end())
+    {
+        std::memcpy(&blob[blocks[it->second].offset], Cs, n * sizeof(double));
+        return;
+    }
+    gb::CsBlock b{I, J, {R[0], R[1], R[2]}, ni, nj, nmu, blob.size()};
+    blob.insert(blob.end(), Cs, Cs + n);
+    index[key] = blocks.size();
+    blocks.push_back(b);
+}
+} // namespace
+
 void librpa_set_lri_coeff(LibrpaHandler *h, LibrpaParallelRouting, int I, int J, int ni, int nj, int nmu,
                           const int R[3], const double *Cs)
 {
@@ -612,18 +633,24 @@ void librpa_set_lri_coeff(LibrpaHandler *h, LibrpaParallelRouting, int I, int J,
         GB_REQUIRE(I >= 0 && J >= 0 && I < static_cast<int>(ds->nao_at.size()) && J < static_cast<int>(ds->nao_at.size()),
                    "atom index out of range");
         GB_REQUIRE(ds->nabf_at[I] == nmu && ds->nao_at[I] == ni && ds->nao_at[J] == nj, "RI block dimensions inconsistent");
-        const size_t n = static_cast<size_t>(ni) * nj * nmu;
-        std::array<int, 5> key{I, J, R[0], R[1], R[2]};
-        auto it = ds->cs_index.find(key);
-        if (it != ds->cs_index.end())
-        {
-            std::memcpy(&ds->cs_blob[ds->cs_blocks[it->second].offset], Cs, n * sizeof(double));
-            return;
-        }
-        gb::CsBlock b{I, J, {R[0], R[1], R[2]}, ni, nj, nmu, ds->cs_blob.size()};
-        ds->cs_blob.insert(ds->cs_blob.end(), Cs, Cs + n);
-        ds->cs_index[key] = ds->cs_blocks.size();
-        ds->cs_blocks.push_back(b);
+        store_cs_block(ds->cs_blob, ds->cs_blocks, ds->cs_index, I, J, ni, nj, nmu, R, Cs);
+    });
+}
+
+void librpa_gb300_set_shrink_lri_coeff(LibrpaHandler *h, int I, int J, int ni, int nj, int nmu, const int R[3],
+                                       const double *Cs)
+{
+    guarded(h, [&] {
+        Dataset *ds = get_ds(h); ds->generation++;
+        GB_REQUIRE(!ds->nao_at.empty(), "wave function basis not set, call (librpa_)set_ao_basis_wfc first");
+        GB_REQUIRE(!ds->shrink_nabf.empty(), "small auxiliary basis not set, call librpa_gb300_set_shrink_basis first");
+        GB_REQUIRE(R && Cs, "null argument");
+        GB_REQUIRE(I >= 0 && J >= 0 && I < static_cast<int>(ds->nao_at.size()) && J < static_cast<int>(ds->nao_at.size()) &&
+                       I < static_cast<int>(ds->shrink_nabf.size()),
+                   "atom index out of range");
+        GB_REQUIRE(ds->shrink_nabf[I] == nmu && ds->nao_at[I] == ni && ds->nao_at[J] == nj,
+                   "RI block dimensions inconsistent with the small basis");
+        store_cs_block(ds->shrink_cs_blob, ds->shrink_cs_blocks, ds->shrink_cs_index, I, J, ni, nj, nmu, R, Cs);
     });
 }
 

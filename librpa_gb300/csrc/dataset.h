@@ -85,6 +85,11 @@ struct Dataset
     };
     std::vector<int> shrink_nabf;
     std::map<int, ShrinkU> shrink_u;
+    // the RI coefficients in the small basis (the Cs_shrinked_data files of the reference's driver):
+    // the exchange of a shrunk input contracts them with the truncated Coulomb matrix of that basis
+    std::vector<double> shrink_cs_blob;
+    std::vector<CsBlock> shrink_cs_blocks;
+    std::map<std::array<int, 5>, size_t> shrink_cs_index;
 
     // Gamma-point exchange and G0W0 results (gw.cu), valid while generation is unchanged
     std::vector<std::vector<double>> hx;       // per spin: H_x(R = 0), n_ao x n_ao

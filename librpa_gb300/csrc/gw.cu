@@ -487,17 +487,26 @@ __global__ void k_super_u(const double *__restrict__ blob, const long long *__re
 // The supercell of the handler's k-grid and its dense U from the RI blocks, folded onto the BvK
 // cells and filtered by max |C| > thr after folding (LibRI set_tensors, RI_Tools.hpp:49-67,
 // LRI-set.hpp:33-75).
-void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
+// The RI coefficients the closed form contracts: the handler's (the basis of librpa_set_ao_basis_aux)
+// or, for the exchange of a shrunk input, those of the small basis.
+struct RiSet
+{
+    const std::vector<CsBlock> &blocks;
+    const std::vector<double> &blob;
+    const std::vector<int> &nabf;
+};
+
+void setup_gamma(const Dataset &ds, const RiSet &ri, double thr, GammaSetup &gs, cudaStream_t st)
 {
     const int n_at = ds.n_atoms();
-    GB_REQUIRE(n_at > 0 && static_cast<int>(ds.nao_at.size()) == n_at && static_cast<int>(ds.nabf_at.size()) == n_at,
+    GB_REQUIRE(n_at > 0 && static_cast<int>(ds.nao_at.size()) == n_at && static_cast<int>(ri.nabf.size()) == n_at,
                "wave-function and auxiliary bases must be set for every atom");
     gs.n_at = n_at;
     gs.abf_off.assign(n_at + 1, 0);
     gs.ao_off.assign(n_at + 1, 0);
     for (int I = 0; I < n_at; ++I)
     {
-        gs.abf_off[I + 1] = gs.abf_off[I] + ds.nabf_at[I];
+        gs.abf_off[I + 1] = gs.abf_off[I] + ri.nabf[I];
         gs.ao_off[I + 1] = gs.ao_off[I] + ds.nao_at[I];
     }
     gs.Nc = gs.abf_off[n_at];
@@ -515,12 +524,12 @@ void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
     GB_REQUIRE(static_cast<double>(N) * nao * nao <= 2.0e9,
                "the G0W0/exchange path holds the dense RI tensor of the BvK supercell (N_abf n_ao^2 values, "
                "times the cell count cubed on a k-grid): input too large");
-    for (const CsBlock &b : ds.cs_blocks)
-        GB_REQUIRE(b.ni == ds.nao_at[b.I] && b.nj == ds.nao_at[b.J] && b.nmu == ds.nabf_at[b.I],
+    for (const CsBlock &b : ri.blocks)
+        GB_REQUIRE(b.ni == ds.nao_at[b.I] && b.nj == ds.nao_at[b.J] && b.nmu == ri.nabf[b.I],
                    "RI block dimensions inconsistent with the bases");
     const Cells &cells = pt.cells;
     CsFold f = fold_cs_blocks(
-        ds.cs_blocks, ds.cs_blob.data(), ds.cs_blob.size(), ds.period,
+        ri.blocks, ri.blob.data(), ri.blob.size(), ds.period,
         [&](const std::array<int, 3> &R) { return cells.find(R[0], R[1], R[2]); }, thr);
     // cadd[c][R]: cell of R_c + R_R
     std::vector<int> cadd(static_cast<size_t>(nc) * nc);
@@ -533,15 +542,15 @@ void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
     const int nblk = static_cast<int>(f.off.size());
     if (nblk > 0)
     {
-        DevBuf<double> blob(ds.cs_blob.size() + f.extra.size());
-        blob.upload(ds.cs_blob.data(), ds.cs_blob.size(), st);
+        DevBuf<double> blob(ri.blob.size() + f.extra.size());
+        blob.upload(ri.blob.data(), ri.blob.size(), st);
         if (!f.extra.empty())
-            GB_CUDA(cudaMemcpyAsync(blob.get() + ds.cs_blob.size(), f.extra.data(), f.extra.size() * sizeof(double),
+            GB_CUDA(cudaMemcpyAsync(blob.get() + ri.blob.size(), f.extra.data(), f.extra.size() * sizeof(double),
                                     cudaMemcpyHostToDevice, st));
         auto d_off = to_dev(f.off, st);
         auto d_meta = to_dev(f.meta, st);
         auto d_nao = to_dev(ds.nao_at, st);
-        auto d_nabf = to_dev(ds.nabf_at, st);
+        auto d_nabf = to_dev(ri.nabf, st);
         auto d_aoo = to_dev(gs.ao_off, st);
         auto d_abo = to_dev(gs.abf_off, st);
         auto d_cadd = to_dev(cadd, st);
@@ -550,6 +559,11 @@ void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
         GB_LAUNCH_CHECK();
         GB_CUDA(cudaStreamSynchronize(st));  // the staged tables go out of scope
     }
+}
+
+void setup_gamma(const Dataset &ds, double thr, GammaSetup &gs, cudaStream_t st)
+{
+    setup_gamma(ds, RiSet{ds.cs_blocks, ds.cs_blob, ds.nabf_at}, thr, gs, st);
 }
 
 // X_s[(c a)][(c' b)] = XR[cell of R_c' - R_c][a][b] for the cell-periodic blocks XR [cell][n][n].
@@ -701,8 +715,20 @@ void build_exx(Dataset &ds, const LibrpaOptions &opts)
         cudaStream_t s;
         ~Guard() { cudaStreamDestroy(s); }
     } guard{st};
+    // with use_shrink_abfs the exchange contracts the RI coefficients of the small basis with the
+    // truncated Coulomb matrix given there (Exx::build on Cs_shrinked_data, driver/task_gw_band.cpp:92-99)
     GammaSetup gs;
-    setup_gamma(ds, opts.libri_exx_threshold_C, gs, st);
+    if (opts.use_shrink_abfs == LIBRPA_SWITCH_ON)
+    {
+        GB_REQUIRE(static_cast<int>(ds.shrink_nabf.size()) == ds.n_atoms(),
+                   "use_shrink_abfs: the small ABF basis must be set for every atom (librpa_gb300_set_shrink_basis)");
+        GB_REQUIRE(!ds.shrink_cs_blocks.empty(),
+                   "use_shrink_abfs: the exchange needs the RI coefficients of the small basis "
+                   "(librpa_gb300_set_shrink_lri_coeff)");
+        setup_gamma(ds, RiSet{ds.shrink_cs_blocks, ds.shrink_cs_blob, ds.shrink_nabf}, opts.libri_exx_threshold_C, gs, st);
+    }
+    else
+        setup_gamma(ds, opts.libri_exx_threshold_C, gs, st);
     const int nao = gs.nao, naoc = gs.naoc, nc = gs.nc, ns = ds.n_spins;
     const std::vector<double> vs = to_supercell(coulomb_r(ds, ds.vq_cut_blocks, ds.vq_cut_blob, gs), gs.Nc, gs);
     const long long nn = static_cast<long long>(nao) * nao;
@@ -767,8 +793,6 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     require_gamma(ds);
     GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
     GB_REQUIRE(!ds.vq_blocks.empty(), "the Coulomb matrix of the dielectric function is not set");
-    GB_REQUIRE(opts.use_shrink_abfs != LIBRPA_SWITCH_ON,
-               "use_shrink_abfs: the Gamma-point G0W0 chain has no unfolding of W to the large ABF basis");
     // chi0(q = 0, omega) from the RPA path, kept on the device
     {
         const LibrpaGB300Options saved = ds.gbopt;
@@ -958,8 +982,6 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some (spin, k)");
     GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
     GB_REQUIRE(!ds.vq_blocks.empty(), "the Coulomb matrix of the dielectric function is not set");
-    GB_REQUIRE(opts.use_shrink_abfs != LIBRPA_SWITCH_ON,
-               "use_shrink_abfs: the G0W0 chain has no unfolding of W to the large ABF basis");
     const int nw = tf.n;
     const bool head = opts.replace_w_head == LIBRPA_SWITCH_ON && !ds.dielect_eps.empty();
     // eps_mac on the minimax frequencies (compute_g0w0.cpp:103-107, interpolate_dielec_func):
@@ -1036,34 +1058,63 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     auto d_eoff = to_dev(eoff, st);
 
     // ---- W_c(q, omega), [Re | Im][q][omega][N][N]
+    // With use_shrink_abfs the dielectric function and W_c live in the small ABF basis of the
+    // Coulomb matrices: chi0_s = U chi0 U^H first (shrink_abfs_chi0, chi0.cpp:711-898), and W_c is
+    // taken back to the basis of the RI coefficients as U^H W_c U (unfold_abfs_Wc, the two pgemm
+    // calls of src/gw_old.cpp:208-225) before the q -> R transform.  Both run on the real
+    // embeddings: U^H embeds as the transpose of U's embedding.
+    const bool shrink = opts.use_shrink_abfs == LIBRPA_SWITCH_ON;
+    std::vector<int> abf_off_w = gs.abf_off;
+    if (shrink)
+    {
+        GB_REQUIRE(static_cast<int>(ds.shrink_nabf.size()) == n_at,
+                   "use_shrink_abfs: the small ABF basis must be set for every atom (librpa_gb300_set_shrink_basis)");
+        for (int I = 0; I < n_at; ++I)
+        {
+            GB_REQUIRE(ds.shrink_nabf[I] > 0, "use_shrink_abfs: small ABF counts must be positive");
+            abf_off_w[I + 1] = abf_off_w[I] + ds.shrink_nabf[I];
+        }
+    }
+    const int Nw = abf_off_w[n_at], N2w = 2 * Nw;
+    const long long NNw = static_cast<long long>(Nw) * Nw, M4w = 4 * NNw;
     DevBuf<double> Wq(2ull * nq * nw * NN);
     {
         DevBuf<cuDoubleComplex> X(static_cast<size_t>(nw) * NN);
-        DevBuf<double> Xe(nw * M4), T(nw * M4), Ye(nw * M4), We(nw * M4), Se(M4), Sce(M4), ScSc(M4), d_ones(nw);
+        DevBuf<double> Xe(nw * M4w), T(nw * M4w), Ye(nw * M4w), We(nw * M4w), Se(M4w), Sce(M4w), ScSc(M4w), d_ones(nw);
+        // shrink: the embedded chi0 of the large basis, U_e (2 Nw x 2 Nc) and its transpose, and a
+        // (2 Nw x 2 Nc) / (2 Nc x 2 Nw) product per frequency
+        DevBuf<double> Xl, Ue, UeT, Tsl;
+        if (shrink)
+        {
+            Xl.alloc(nw * M4);
+            Ue.alloc(static_cast<size_t>(N2w) * N2);
+            UeT.alloc(static_cast<size_t>(N2w) * N2);
+            Tsl.alloc(static_cast<size_t>(nw) * N2w * N2);
+        }
         DevBuf<int> bad(1);
         bad.zero(st);
         std::vector<double> ones(nw, -1.0);
         d_ones.upload(ones.data(), nw, st);
         auto embed_h = [&](const std::vector<cplx> &A) {
-            std::vector<double> E(M4);
-            for (int i = 0; i < Nc; ++i)
-                for (int j = 0; j < Nc; ++j)
+            std::vector<double> E(M4w);
+            for (int i = 0; i < Nw; ++i)
+                for (int j = 0; j < Nw; ++j)
                 {
-                    const cplx v = A[static_cast<size_t>(i) * Nc + j];
-                    E[static_cast<size_t>(i) * N2 + j] = v.real();
-                    E[static_cast<size_t>(i) * N2 + Nc + j] = -v.imag();
-                    E[static_cast<size_t>(Nc + i) * N2 + j] = v.imag();
-                    E[static_cast<size_t>(Nc + i) * N2 + Nc + j] = v.real();
+                    const cplx v = A[static_cast<size_t>(i) * Nw + j];
+                    E[static_cast<size_t>(i) * N2w + j] = v.real();
+                    E[static_cast<size_t>(i) * N2w + Nw + j] = -v.imag();
+                    E[static_cast<size_t>(Nw + i) * N2w + j] = v.imag();
+                    E[static_cast<size_t>(Nw + i) * N2w + Nw + j] = v.real();
                 }
             return E;
         };
-        const size_t gj_smem = sizeof(double) * N2;
+        const size_t gj_smem = sizeof(double) * N2w;
         GB_REQUIRE(gj_smem <= 48 * 1024, "auxiliary basis too large for the W_c solve");
         for (int q = 0; q < nq; ++q)
         {
             const int kq = pt.ibz_rep[q];
-            const std::vector<cplx> ve = coulomb_k(ds.vq_blocks, ds.vq_blob, kq, gs.abf_off, Nc);
-            const std::vector<cplx> vc = coulomb_k(ds.vq_cut_blocks, ds.vq_cut_blob, kq, gs.abf_off, Nc);
+            const std::vector<cplx> ve = coulomb_k(ds.vq_blocks, ds.vq_blob, kq, abf_off_w, Nw);
+            const std::vector<cplx> vc = coulomb_k(ds.vq_cut_blocks, ds.vq_cut_blob, kq, abf_off_w, Nw);
             const bool gq = std::fabs(ds.kfrac[3 * kq]) < 1e-10 && std::fabs(ds.kfrac[3 * kq + 1]) < 1e-10 &&
                             std::fabs(ds.kfrac[3 * kq + 2]) < 1e-10;
             const bool head_q = gq && head;
@@ -1074,72 +1125,128 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             {
                 // power_hemat_blacs_real on Re V (utils_matrix_m_mpi.h:886-1010): S = V^1/2 over the
                 // eigenvalues at or above the threshold; z0 the eigenvector of the largest one
-                std::vector<double> rv(NN);
-                for (long long e = 0; e < NN; ++e) rv[e] = ve[e].real();
+                std::vector<double> rv(NNw);
+                for (long long e = 0; e < NNw; ++e) rv[e] = ve[e].real();
                 std::vector<double> B = rv, w, Z;
-                sym_eig(B, Nc, w, Z);
-                w0 = w[Nc - 1];
+                sym_eig(B, Nw, w, Z);
+                w0 = w[Nw - 1];
                 GB_REQUIRE(w0 >= thr, "replace_w_head: the Coulomb matrix at q = 0 has no eigenvalue above the threshold");
-                z0.resize(Nc);
-                for (int r = 0; r < Nc; ++r) z0[r] = Z[static_cast<size_t>(r) * Nc + Nc - 1];
-                const std::vector<double> S = power_sym(rv, Nc, 0.5, thr);
-                std::vector<cplx> Sc(NN);
-                for (long long e = 0; e < NN; ++e) Sc[e] = S[e];
+                z0.resize(Nw);
+                for (int r = 0; r < Nw; ++r) z0[r] = Z[static_cast<size_t>(r) * Nw + Nw - 1];
+                const std::vector<double> S = power_sym(rv, Nw, 0.5, thr);
+                std::vector<cplx> Sc(NNw);
+                for (long long e = 0; e < NNw; ++e) Sc[e] = S[e];
                 se_h = embed_h(Sc);
             }
             else
-                se_h = embed_h(power_herm(ve, Nc, 0.5, thr));
-            const std::vector<double> sc_h = embed_h(power_herm(vc, Nc, 0.5, thr));
-            Se.upload(se_h.data(), M4, st);
-            Sce.upload(sc_h.data(), M4, st);
-            launch_dgemm(N2, N2, N2, Sce.get(), N2, 0, Sce.get(), N2, 0, ScSc.get(), N2, 0, 1, 1.0, 0.0, st);
+                se_h = embed_h(power_herm(ve, Nw, 0.5, thr));
+            const std::vector<double> sc_h = embed_h(power_herm(vc, Nw, 0.5, thr));
+            Se.upload(se_h.data(), M4w, st);
+            Sce.upload(sc_h.data(), M4w, st);
+            launch_dgemm(N2w, N2w, N2w, Sce.get(), N2w, 0, Sce.get(), N2w, 0, ScSc.get(), N2w, 0, 1, 1.0, 0.0, st);
             launch_assemble_chi0(static_cast<const cuDoubleComplex *>(ds.kept_chi0) + static_cast<long long>(q) * e_tot,
                                  static_cast<long long>(nq) * e_tot, nw, Nc, d_atom.get(), d_off.get(), d_nabf.get(),
                                  d_pair.get(), n_at, d_eoff.get(), false, X.get(), nullptr, NN, st);
-            k_embed<<<grid_for(NN * nw), 256, 0, st>>>(X.get(), NN, Nc, nw, Xe.get());
-            GB_LAUNCH_CHECK();
-            // S chi0 S
-            launch_dgemm(N2, N2, N2, Se.get(), N2, 0, Xe.get(), N2, M4, T.get(), N2, M4, nw, 1.0, 0.0, st);
-            launch_dgemm(N2, N2, N2, T.get(), N2, M4, Se.get(), N2, 0, Xe.get(), N2, M4, nw, 1.0, 0.0, st);
+            if (shrink)
+            {
+                auto it = ds.shrink_u.find(kq);
+                GB_REQUIRE(it != ds.shrink_u.end(), "use_shrink_abfs: no shrink transform U(q) for IBZ k index " +
+                                                        std::to_string(kq) + " (librpa_gb300_set_shrink_sinvS)");
+                const Dataset::ShrinkU &u = it->second;
+                GB_REQUIRE(u.n_small == Nw && u.n_large == Nc,
+                           "use_shrink_abfs: U(q) must be (sum of small ABFs) x (sum of ABFs) = " + std::to_string(Nw) +
+                               " x " + std::to_string(Nc));
+                std::vector<double> ue(static_cast<size_t>(N2w) * N2), uet(static_cast<size_t>(N2w) * N2);
+                for (int i = 0; i < Nw; ++i)
+                    for (int j = 0; j < Nc; ++j)
+                    {
+                        const cplx v = u.u[static_cast<size_t>(i) * Nc + j];
+                        const size_t r0 = static_cast<size_t>(i) * N2, r1 = static_cast<size_t>(Nw + i) * N2;
+                        ue[r0 + j] = v.real();
+                        ue[r0 + Nc + j] = -v.imag();
+                        ue[r1 + j] = v.imag();
+                        ue[r1 + Nc + j] = v.real();
+                    }
+                for (int r = 0; r < N2w; ++r)
+                    for (int c = 0; c < N2; ++c) uet[static_cast<size_t>(c) * N2w + r] = ue[static_cast<size_t>(r) * N2 + c];
+                Ue.upload(ue.data(), ue.size(), st);
+                UeT.upload(uet.data(), uet.size(), st);
+                k_embed<<<grid_for(NN * nw), 256, 0, st>>>(X.get(), NN, Nc, nw, Xl.get());
+                GB_LAUNCH_CHECK();
+                // chi0_s = U chi0 U^H
+                launch_dgemm(N2w, N2, N2, Ue.get(), N2, 0, Xl.get(), N2, M4, Tsl.get(), N2, static_cast<long long>(N2w) * N2,
+                             nw, 1.0, 0.0, st);
+                launch_dgemm(N2w, N2w, N2, Tsl.get(), N2, static_cast<long long>(N2w) * N2, UeT.get(), N2w, 0, Xe.get(),
+                             N2w, M4w, nw, 1.0, 0.0, st);
+            }
+            else
+            {
+                k_embed<<<grid_for(NN * nw), 256, 0, st>>>(X.get(), NN, Nc, nw, Xe.get());
+                GB_LAUNCH_CHECK();
+            }
+            // the head element of chi0 in V's eigenbasis, w0 z0^T chi0 z0, from the embedded chi0
+            std::vector<cplx> x00(head_q ? nw : 0);
             if (head_q)
             {
-                // in V's eigenbasis the (0, 0) element of S chi0 S, w0 z0^T chi0 z0, becomes
-                // 1 - eps_mac: add ((1 - eps_mac) - X00) z0 z0^T
-                std::vector<cplx> hx(static_cast<size_t>(nw) * NN);
-                X.download(reinterpret_cast<cuDoubleComplex *>(hx.data()), hx.size(), st);
-                std::vector<double> hxe(nw * M4);
+                std::vector<double> hxe(nw * M4w);
                 Xe.download(hxe.data(), hxe.size(), st);
                 GB_CUDA(cudaStreamSynchronize(st));
                 for (int w = 0; w < nw; ++w)
                 {
-                    cplx x00(0, 0);
-                    for (int r = 0; r < Nc; ++r)
-                        for (int c = 0; c < Nc; ++c) x00 += z0[r] * hx[static_cast<size_t>(w) * NN + static_cast<size_t>(r) * Nc + c] * z0[c];
-                    x00 *= w0;
-                    const cplx d = (1.0 - eps_head[w]) - x00;
-                    double *E = hxe.data() + static_cast<size_t>(w) * M4;
-                    for (int r = 0; r < Nc; ++r)
-                        for (int c = 0; c < Nc; ++c)
+                    const double *E = hxe.data() + static_cast<size_t>(w) * M4w;
+                    cplx acc(0, 0);
+                    for (int r = 0; r < Nw; ++r)
+                        for (int c = 0; c < Nw; ++c)
+                            acc += z0[r] * cplx(E[static_cast<size_t>(r) * N2w + c], E[static_cast<size_t>(Nw + r) * N2w + c]) * z0[c];
+                    x00[w] = w0 * acc;
+                }
+            }
+            // S chi0 S
+            launch_dgemm(N2w, N2w, N2w, Se.get(), N2w, 0, Xe.get(), N2w, M4w, T.get(), N2w, M4w, nw, 1.0, 0.0, st);
+            launch_dgemm(N2w, N2w, N2w, T.get(), N2w, M4w, Se.get(), N2w, 0, Xe.get(), N2w, M4w, nw, 1.0, 0.0, st);
+            if (head_q)
+            {
+                // in V's eigenbasis the (0, 0) element of S chi0 S becomes 1 - eps_mac: add
+                // ((1 - eps_mac) - X00) z0 z0^T
+                std::vector<double> hxe(nw * M4w);
+                Xe.download(hxe.data(), hxe.size(), st);
+                GB_CUDA(cudaStreamSynchronize(st));
+                for (int w = 0; w < nw; ++w)
+                {
+                    const cplx d = (1.0 - eps_head[w]) - x00[w];
+                    double *E = hxe.data() + static_cast<size_t>(w) * M4w;
+                    for (int r = 0; r < Nw; ++r)
+                        for (int c = 0; c < Nw; ++c)
                         {
                             const double zz = z0[r] * z0[c];
-                            E[static_cast<size_t>(r) * N2 + c] += d.real() * zz;
-                            E[static_cast<size_t>(r) * N2 + Nc + c] -= d.imag() * zz;
-                            E[static_cast<size_t>(Nc + r) * N2 + c] += d.imag() * zz;
-                            E[static_cast<size_t>(Nc + r) * N2 + Nc + c] += d.real() * zz;
+                            E[static_cast<size_t>(r) * N2w + c] += d.real() * zz;
+                            E[static_cast<size_t>(r) * N2w + Nw + c] -= d.imag() * zz;
+                            E[static_cast<size_t>(Nw + r) * N2w + c] += d.imag() * zz;
+                            E[static_cast<size_t>(Nw + r) * N2w + Nw + c] += d.real() * zz;
                         }
                 }
                 Xe.upload(hxe.data(), hxe.size(), st);
             }
             // eps = 1 - S chi0 S; W_c = S_c eps^-1 S_c - S_c S_c
-            k_one_minus<<<grid_for(M4 * nw), 256, 0, st>>>(Xe.get(), N2, nw);
+            k_one_minus<<<grid_for(M4w * nw), 256, 0, st>>>(Xe.get(), N2w, nw);
             GB_LAUNCH_CHECK();
             for (int w = 0; w < nw; ++w)
-                GB_CUDA(cudaMemcpyAsync(Ye.get() + w * M4, Sce.get(), sizeof(double) * M4, cudaMemcpyDeviceToDevice, st));
-            k_gj_solve<<<nw, 256, gj_smem, st>>>(Xe.get(), Ye.get(), N2, N2, bad.get());
+                GB_CUDA(cudaMemcpyAsync(Ye.get() + w * M4w, Sce.get(), sizeof(double) * M4w, cudaMemcpyDeviceToDevice, st));
+            k_gj_solve<<<nw, 256, gj_smem, st>>>(Xe.get(), Ye.get(), N2w, N2w, bad.get());
             GB_LAUNCH_CHECK();
-            launch_dgemm(N2, N2, N2, Sce.get(), N2, 0, Ye.get(), N2, M4, We.get(), N2, M4, nw, 1.0, 0.0, st);
-            launch_dgemm(nw, static_cast<int>(M4), 1, d_ones.get(), 1, 0, ScSc.get(), M4, 0, We.get(), M4, 0, 1, 1.0, 1.0, st);
-            k_unembed<<<grid_for(NN * nw), 256, 0, st>>>(We.get(), Nc, nw, Wq.get() + static_cast<long long>(q) * nw * NN,
+            launch_dgemm(N2w, N2w, N2w, Sce.get(), N2w, 0, Ye.get(), N2w, M4w, We.get(), N2w, M4w, nw, 1.0, 0.0, st);
+            launch_dgemm(nw, static_cast<int>(M4w), 1, d_ones.get(), 1, 0, ScSc.get(), M4w, 0, We.get(), M4w, 0, 1, 1.0, 1.0, st);
+            const double *Wout = We.get();
+            if (shrink)
+            {
+                // W_c of the large basis: U^H W_c U
+                launch_dgemm(N2w, N2, N2w, We.get(), N2w, M4w, Ue.get(), N2, 0, Tsl.get(), N2,
+                             static_cast<long long>(N2w) * N2, nw, 1.0, 0.0, st);
+                launch_dgemm(N2, N2, N2w, UeT.get(), N2w, 0, Tsl.get(), N2, static_cast<long long>(N2w) * N2, Xl.get(), N2,
+                             M4, nw, 1.0, 0.0, st);
+                Wout = Xl.get();
+            }
+            k_unembed<<<grid_for(NN * nw), 256, 0, st>>>(Wout, Nc, nw, Wq.get() + static_cast<long long>(q) * nw * NN,
                                                          Wq.get() + (static_cast<long long>(nq) + q) * nw * NN);
             GB_LAUNCH_CHECK();
             GB_CUDA(cudaStreamSynchronize(st));  // the host matrices are rebuilt for the next q
@@ -1387,9 +1494,9 @@ void build_g0w0(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrids &tf)
 {
     // the head of the dielectric matrix is replaced at q = 0 whenever a dielectric function is
     // set (compute_g0w0.cpp:103-107, epsilon.cpp:2110-2160), Gamma-only inputs included: the
-    // k-grid chain (complex W, one q-point) carries it
+    // k-grid chain (complex W, one q-point) carries it, and the ABF shrink
     const bool head = opts.replace_w_head == LIBRPA_SWITCH_ON && !ds.dielect_eps.empty();
-    if (ds.n_kpts > 1 || head)
+    if (ds.n_kpts > 1 || head || opts.use_shrink_abfs == LIBRPA_SWITCH_ON)
         build_g0w0_kgrid(ds, opts, tf);
     else
         build_g0w0_gamma(ds, opts, tf);

@@ -16,6 +16,7 @@
 // count per atom from the Cs_shrinked_data headers, U(q) from shrink_sinvS_*, and the Coulomb
 // matrix in the small basis.
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <cmath>
 #include <complex>
@@ -145,9 +146,13 @@ int main()
     {
         const auto p = read_params("librpa.in");
         auto par = [&](const std::string &k, const std::string &d) { return p.count(k) ? p.at(k) : d; };
-        const std::string task = lower(par("task", "rpa"));
+        // task = g0w0_band runs the k-grid part of driver/task/g0w0_band.cpp; the band path along
+        // band_kpath_info is skipped, as the reference skips it when that file is absent
+        const std::string task_in = lower(par("task", "rpa"));
+        const bool band_task = task_in == "g0w0_band";
+        const std::string task = band_task ? "g0w0" : task_in;
         if (task != "rpa" && task != "exx" && task != "g0w0")
-            die("this driver runs task = rpa, exx or g0w0 (got " + task + ")");
+            die("this driver runs task = rpa, exx, g0w0 or g0w0_band (got " + task_in + ")");
         std::string dir = par("input_dir", "./");
         if (dir.back() != '/') dir += '/';
         const double cs_threshold = std::stod(par("cs_threshold", "1e-6"));
@@ -385,43 +390,46 @@ int main()
             librpa_set_lri_coeff(h, static_cast<LibrpaParallelRouting>(opts.parallel_routing), v[0] - 1, v[1] - 1,
                                  v[5], v[6], v[7], R, c.data());
         };
-        for (const auto &fn : files_with_prefix(dir, "Cs_data"))
-        {
-            if (is_text_file(fn))
+        auto for_each_cs_block = [&](const std::string &prefix, const auto &fn_block) {
+            for (const auto &fn : files_with_prefix(dir, prefix))
             {
-                const auto t = tokens(fn);
-                size_t q = 2;  // natom, ncell
-                while (q + 8 <= t.size())
+                if (is_text_file(fn))
+                {
+                    const auto t = tokens(fn);
+                    size_t q = 2;  // natom, ncell
+                    while (q + 8 <= t.size())
+                    {
+                        int v[8];
+                        for (int i = 0; i < 8; ++i) v[i] = std::stoi(t[q + i]);
+                        q += 8;
+                        const size_t cnt = static_cast<size_t>(v[5]) * v[6] * v[7];
+                        if (q + cnt > t.size()) die("truncated RI file " + fn);
+                        std::vector<double> c(cnt);
+                        for (size_t i = 0; i < cnt; ++i) c[i] = std::stod(t[q + i]);
+                        q += cnt;
+                        fn_block(v, c);
+                    }
+                    continue;
+                }
+                const auto raw = slurp(fn);
+                size_t off = 0;
+                get<int>(raw, off);
+                get<int>(raw, off);
+                const int nblk = get<int>(raw, off);
+                for (int b = 0; b < nblk; ++b)
                 {
                     int v[8];
-                    for (int i = 0; i < 8; ++i) v[i] = std::stoi(t[q + i]);
-                    q += 8;
+                    for (auto &x : v) x = get<int>(raw, off);
                     const size_t cnt = static_cast<size_t>(v[5]) * v[6] * v[7];
-                    if (q + cnt > t.size()) die("truncated RI file " + fn);
+                    if (off + 8 * cnt > raw.size()) die("truncated RI file " + fn);
                     std::vector<double> c(cnt);
-                    for (size_t i = 0; i < cnt; ++i) c[i] = std::stod(t[q + i]);
-                    q += cnt;
-                    set_cs(v, c);
+                    std::memcpy(c.data(), raw.data() + off, 8 * cnt);
+                    off += 8 * cnt;
+                    fn_block(v, c);
                 }
-                continue;
             }
-            const auto raw = slurp(fn);
-            size_t off = 0;
-            get<int>(raw, off);
-            get<int>(raw, off);
-            const int nblk = get<int>(raw, off);
-            for (int b = 0; b < nblk; ++b)
-            {
-                int v[8];
-                for (auto &x : v) x = get<int>(raw, off);
-                const size_t cnt = static_cast<size_t>(v[5]) * v[6] * v[7];
-                if (off + 8 * cnt > raw.size()) die("truncated RI file " + fn);
-                std::vector<double> c(cnt);
-                std::memcpy(c.data(), raw.data() + off, 8 * cnt);
-                off += 8 * cnt;
-                set_cs(v, c);
-            }
-        }
+        };
+        for_each_cs_block("Cs_data", set_cs);
         // ABF shrink: small basis from the n_mu of the Cs_shrinked_data blocks (first atom of a
         // block), U(q) from shrink_sinvS_* (handle_sinvS_file, read_data.cpp:2455-2568: n_irk, then
         // blocks n_small n_large brow erow bcol ecol iq q_weight and the (re, im) of the rows; iq
@@ -429,33 +437,19 @@ int main()
         std::vector<int> nabf_v = m.nabf_at;  // the basis of the Coulomb matrix
         if (shrink)
         {
+            // the blocks also carry the RI coefficients of the small basis (the exchange of a
+            // shrunk input, driver/task_gw_band.cpp:92-99), read with the same threshold
             std::map<int, int> aa;
-            for (const auto &fn : files_with_prefix(dir, "Cs_shrinked_data"))
-            {
-                if (is_text_file(fn))
-                {
-                    const auto t = tokens(fn);
-                    size_t q = 2;
-                    while (q + 8 <= t.size())
-                    {
-                        int v[8];
-                        for (int i = 0; i < 8; ++i) v[i] = std::stoi(t[q + i]);
-                        aa[v[0] - 1] = v[7];
-                        q += 8 + static_cast<size_t>(v[5]) * v[6] * v[7];
-                    }
-                    continue;
-                }
-                const auto raw = slurp(fn);
-                size_t off = 8;
-                const int nblk = get<int>(raw, off);
-                for (int b = 0; b < nblk; ++b)
-                {
-                    int v[8];
-                    for (auto &x : v) x = get<int>(raw, off);
-                    aa[v[0] - 1] = v[7];
-                    off += 8 * static_cast<size_t>(v[5]) * v[6] * v[7];
-                }
-            }
+            std::vector<std::pair<std::array<int, 8>, std::vector<double>>> small_cs;
+            for_each_cs_block("Cs_shrinked_data", [&](const int *v, std::vector<double> &c) {
+                aa[v[0] - 1] = v[7];
+                double mx = 0.0;
+                for (double x : c) mx = std::max(mx, std::fabs(x));
+                if (mx < cs_threshold) return;
+                std::array<int, 8> key;
+                std::copy(v, v + 8, key.begin());
+                small_cs.emplace_back(key, std::move(c));
+            });
             std::vector<size_t> ns(m.nat);
             for (int a = 0; a < m.nat; ++a)
             {
@@ -465,6 +459,12 @@ int main()
                 nabf_v[a] = aa[a];
             }
             librpa_gb300_set_shrink_basis(h, m.nat, ns.data());
+            for (const auto &kb : small_cs)
+            {
+                const int *v = kb.first.data();
+                const int R[3] = {v[2], v[3], v[4]};
+                librpa_gb300_set_shrink_lri_coeff(h, v[0] - 1, v[1] - 1, v[5], v[6], v[7], R, kb.second.data());
+            }
             std::vector<int> reps;  // IBZ representatives in order of appearance
             for (int k : m.ibz)
                 if (std::find(reps.begin(), reps.end(), k) == reps.end()) reps.push_back(k);
@@ -628,7 +628,7 @@ int main()
             // dielectric function of the head correction (dielecfunc_out: omega, Re, Im per line;
             // read_data.cpp:1211-1229) and v_xc (vxc_out: n_k n_s n_states, then per k and spin an
             // "Ha eV" pair per state; read_data.cpp:142-182)
-            read_coulomb("coulomb_cut", m.nabf_at, true);
+            read_coulomb("coulomb_cut", nabf_v, true);
             std::vector<int> iks(m.nk);
             for (int k = 0; k < m.nk; ++k) iks[k] = k;
             const int nst = m.nb;

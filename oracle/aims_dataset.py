@@ -157,8 +157,28 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
                         wfc[s, ik, ib, iw] = complex(float(t[p]), float(t[p + 1]))
                         p += 2
 
+    Cs = read_cs(d, "Cs_data", cs_threshold)
+
+    nabf_small = sinvS = Cs_small = None
+    if glob.glob(d + "shrink_sinvS*"):
+        # ABF shrink (use_shrink_abfs): the Coulomb matrices are given in the small basis, the
+        # exchange takes the RI coefficients of that basis (Cs_shrinked_data)
+        nabf_small = _basis_from_cs(d, nat, "Cs_shrinked_data")[1]
+        sinvS = read_sinvS(d, "shrink_sinvS")
+        Cs_small = read_cs(d, "Cs_shrinked_data", cs_threshold)
+    Vq = read_coulomb(d, "coulomb_mat", nabf_small if nabf_small is not None else nabf_at)
+
+    return RPAInput(n_spins=ns, n_kpts=nk, n_bands=nb, n_ao=nao, wg=wg, ekb=ekb, efermi=efermi,
+                    wfc=wfc, latvec=lat, period=period, kvecs=kv, ibz_map=ibz,
+                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos, nabf_small=nabf_small,
+                    sinvS=sinvS, Cs_small=Cs_small)
+
+
+def read_cs(d: str, prefix: str, cs_threshold: float) -> dict:
+    """RI blocks {(I, J, R): (n_i n_j, n_mu)} of the Cs files with the given prefix, text or binary
+    (handle_Cs_file, read_data.cpp:690-747), blocks whose max |C| is below cs_threshold dropped."""
     Cs = {}
-    for fn in sorted(glob.glob(d + "Cs_data*")):
+    for fn in sorted(glob.glob(d + prefix + "*")):
         if is_text_file(fn):
             t = _tokens(fn)
             p = 2  # natom, ncell
@@ -182,18 +202,7 @@ def read_dataset(d: str, cs_threshold: float = 1e-6) -> RPAInput:
             off += 8 * cnt
             if np.abs(m).max() >= cs_threshold:
                 Cs[(I - 1, J - 1, (r1, r2, r3))] = m
-
-    nabf_small = sinvS = None
-    if glob.glob(d + "shrink_sinvS*"):
-        # ABF shrink (use_shrink_abfs): the Coulomb matrix is given in the small basis
-        nabf_small = _basis_from_cs(d, nat, "Cs_shrinked_data")[1]
-        sinvS = read_sinvS(d, "shrink_sinvS")
-    Vq = read_coulomb(d, "coulomb_mat", nabf_small if nabf_small is not None else nabf_at)
-
-    return RPAInput(n_spins=ns, n_kpts=nk, n_bands=nb, n_ao=nao, wg=wg, ekb=ekb, efermi=efermi,
-                    wfc=wfc, latvec=lat, period=period, kvecs=kv, ibz_map=ibz,
-                    nao=nao_at, nabf=nabf_at, Cs=Cs, Vq=Vq, positions=pos, nabf_small=nabf_small,
-                    sinvS=sinvS)
+    return Cs
 
 
 def read_coulomb(d: str, prefix: str, nabf_at) -> dict:

@@ -37,12 +37,13 @@ run on a 3x3x3 k-grid with 14 IBZ points and the head correction (mgo_g0w0.npz).
 from __future__ import annotations
 
 import math
+import dataclasses
 from dataclasses import dataclass
 
 import numpy as np
 
 from .rpa_oracle import (TWO_PI, Options, RPAInput, assemble_full, blocks_of, build_gf, centred_mod,
-                         chi0q_partial, cs_tensors, grids_for, k_lists, r_grid, upper_pairs)
+                         chi0q_partial, cs_tensors, grids_for, k_lists, r_grid, shrink_chi0q, upper_pairs)
 
 HA2EV = 27.211386245988  # src/utils/constants.cpp:13 (the driver's default "internal" choice)
 
@@ -411,9 +412,20 @@ class BandPoints:
     vxc: np.ndarray | None = None  # (n_spins, n, n_bands) Hartree
 
 
+def small_basis_view(inp: RPAInput) -> RPAInput:
+    """A shrunk input as its exchange sees it: the RI coefficients and ABF counts of the small
+    basis (Exx::build on Cs_shrinked_data, driver/task_gw_band.cpp:92-99)."""
+    if inp.Cs_small is None:
+        raise ValueError("use_shrink_abfs: the exchange needs the RI coefficients of the small basis")
+    return dataclasses.replace(inp, Cs=inp.Cs_small, nabf=list(inp.nabf_small))
+
+
 def exx_kgrid(inp: RPAInput, v_cut: dict, band: BandPoints | None = None):
     """v_exx[s, k, n] (Hartree) on the SCF k-grid (task = exx; exx.cpp:213-500, :720-860), or at
-    the band points: H(R) summed with e^{i 2 pi k.R} at any k (Exx::build_KS_band)."""
+    the band points: H(R) summed with e^{i 2 pi k.R} at any k (Exx::build_KS_band).  A shrunk
+    input (inp.sinvS set) takes the small basis, where v_cut is then given."""
+    if inp.sinvS is not None:
+        inp = small_basis_view(inp)
     _, kfrac, _, _ = k_lists(inp)
     kpts, wfc = (kfrac, inp.wfc) if band is None else (band.kfrac, band.wfc)
     rlist = r_grid(inp.period)
@@ -569,22 +581,34 @@ def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
     pairs = upper_pairs(inp.n_atoms)
     nbt = int(sum(nb))
     chi0q = chi0q_partial(inp, opts, 0, nf)
+    # ABF shrink: chi0 and W_c in the small basis of the Coulomb matrices (shrink_abfs_chi0,
+    # chi0.cpp:711-898), W_c taken back to the RI basis as U^H W_c U (unfold_abfs_Wc,
+    # src/gw_old.cpp:208-225) for the self-energy
+    shrink = inp.sinvS is not None
+    nbw = list(inp.nabf_small) if shrink else nb
+    if shrink:
+        chi0q = shrink_chi0q(chi0q, inp.sinvS, nb, nbw)
+    nbwt = int(sum(nbw))
 
     # Wc(q, omega) at the IBZ points
     Wq = {}
     for iq, kq in enumerate(ibz_order):
-        v_e = assemble_full({p: inp.Vq[(kq, *p)] for p in pairs if (kq, *p) in inp.Vq}, nb)
-        v_c = assemble_full({p: v_cut[(kq, *p)] for p in pairs if (kq, *p) in v_cut}, nb)
+        v_e = assemble_full({p: inp.Vq[(kq, *p)] for p in pairs if (kq, *p) in inp.Vq}, nbw)
+        v_c = assemble_full({p: v_cut[(kq, *p)] for p in pairs if (kq, *p) in v_cut}, nbw)
         gamma = bool(np.all(np.abs(klist[kq]) < 1e-10))
         for iw in range(nf):
-            X = assemble_full(chi0q[iw][iq], nb)
+            X = assemble_full(chi0q[iw][iq], nbw)
             if gamma and epsmac is not None:
-                Wq[(iq, iw)] = wc_freq_head(X, v_e, v_c, epsmac[iw], sqrt_threshold)
+                W = wc_freq_head(X, v_e, v_c, epsmac[iw], sqrt_threshold)
             else:
                 s_e = power_hemat(v_e, 0.5, sqrt_threshold)
                 s_c = power_hemat(v_c, 0.5, sqrt_threshold)
-                eps = np.eye(nbt) - s_e @ X @ s_e
-                Wq[(iq, iw)] = s_c @ (np.linalg.solve(eps, s_c) - s_c)
+                eps = np.eye(nbwt) - s_e @ X @ s_e
+                W = s_c @ (np.linalg.solve(eps, s_c) - s_c)
+            if shrink:
+                U = inp.sinvS[iq]
+                W = U.conj().T @ W @ U
+            Wq[(iq, iw)] = W
 
     # Wc(R, omega) (FT_Wc_freq_q: the BZ from the IBZ with W(-q) = W(q)^*, 1/n_k), real part,
     # then Wc(R, tau) = sum_omega f2t(tau, omega) Wc(R, omega)

@@ -63,6 +63,7 @@ class RPAInput:
     # ABF shrink (use_shrink_abfs): small ABFs per atom (the basis of Vq then) and U(q) per IBZ q
     nabf_small: list | None = None
     sinvS: dict | None = None             # iq_ibz -> (sum nabf_small, sum nabf) complex
+    Cs_small: dict | None = None          # RI blocks of the small basis (exchange of a shrunk input)
 
     @property
     def n_atoms(self):

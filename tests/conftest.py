@@ -142,6 +142,24 @@ def load_bn_shrink():
                            types=np.zeros(len(inp.nao), int), nfreq=16, minimax_emin=-1.0, minimax_emax=-1.0)
 
 
+def load_bn_shrink_g0w0():
+    """The BN shrink case as its G0W0 run reads it: load_bn_shrink plus the truncated Coulomb
+    matrix and v_xc (small basis / Hartree) and the reference's quasi-particle tables
+    ([k][state][column], eV)."""
+    from oracle.aims_dataset import read_coulomb, read_vxc
+    s = load_bn_shrink()
+    d = str(bn_shrink_dir()).rstrip("/") + "/"
+    z = np.load(GOLDEN / "bn_shrink_g0w0.npz")
+    s.name = "bn_shrink_g0w0"
+    s.v_cut = read_coulomb(d, "coulomb_cut", s.nabf_small)
+    s.vxc = read_vxc(d + "vxc_out")
+    s.qp_tables = z["tables"]
+    s.nfreq = int(z["nfreq"])
+    s.n_params_anacon = int(z["n_params_anacon"])
+    s.sqrt_coulomb_threshold = float(z["sqrt_coulomb_threshold"])
+    return s
+
+
 def shrunk_copy(s, nabf_small, seed=5, unitary=False):
     """s with an ABF shrink added: per IBZ point a U(q) of orthonormal rows (a complex unitary
     when unitary=True and the sizes agree; real at the Gamma point) and the Coulomb matrix taken to
@@ -182,4 +200,5 @@ def oracle_input(s):
     return RPAInput(n_spins=s.n_spins, n_kpts=s.n_kpts, n_bands=s.n_bands, n_ao=s.n_ao, wg=s.wg, ekb=s.ekb,
                     efermi=s.efermi, wfc=s.wfc, latvec=s.latvec, period=s.period, kvecs=s.kvecs,
                     ibz_map=s.ibz_map, nao=s.nao, nabf=s.nabf, Cs=s.Cs, Vq=s.Vq, positions=s.positions,
-                    nabf_small=getattr(s, "nabf_small", None), sinvS=getattr(s, "sinvS", None))
+                    nabf_small=getattr(s, "nabf_small", None), sinvS=getattr(s, "sinvS", None),
+                    Cs_small=getattr(s, "Cs_small", None))

@@ -51,8 +51,12 @@ Produces (all committed, so the tests need no reference tree at run time):
                      ABFs, shrunk to 17 + 17) copied unchanged
                      (regression_tests/testcases/g0w0_band_abacus_BN_shrink_libri/input_librpa.tar.gz):
                      Cs of the large basis, Coulomb matrix of the small one, shrink_sinvS, and the
-                     Cs_shrinked_data whose headers give the small basis; the reference prints no
-                     E_c for it
+                     Cs_shrinked_data (the RI coefficients of the small basis); the reference prints
+                     no E_c for it
+  bn_shrink_g0w0.npz the quasi-particle tables of the same case's G0W0 run on its 2x2x2 k-grid
+                     (refs/g0w0_band_abacus_BN_shrink_libri/librpa.out: 8 k-points x 26 states, eV;
+                     16 minimax points, 16 Pade parameters, sqrt_coulomb_threshold 1e-8 from its
+                     librpa.in; the suite checks the first table to 1e-4 eV)
 
 Fixtures can be regenerated one at a time: make_fixtures.py <reference> [h2o|minimax|he_bcc|
 h2o_dataset|he_dataset|li_dataset|g0w0|li_g0w0|he_exx|mgo_g0w0|bn_shrink|h2o_g0w0_dataset ...].
@@ -376,6 +380,13 @@ def bn_shrink(ref: Path):
     src = ref / "regression_tests/testcases/g0w0_band_abacus_BN_shrink_libri/input_librpa.tar.gz"
     shutil.copyfile(src, HERE / "bn_shrink_dataset.tar.gz")
     print("bn_shrink_dataset.tar.gz written")
+    # the quasi-particle tables its G0W0 run printed on the 2x2x2 k-grid (the band path was skipped)
+    log = (ref / "regression_tests/refs/g0w0_band_abacus_BN_shrink_libri/librpa.out").read_text().splitlines()
+    tables = np.array(_qp_tables(log))
+    assert tables.shape == (8, 26, 8), tables.shape
+    np.savez_compressed(HERE / "bn_shrink_g0w0.npz", tables=tables, nfreq=16, n_params_anacon=16,
+                        sqrt_coulomb_threshold=1e-8)
+    print("bn_shrink_g0w0.npz written")
 
 
 if __name__ == "__main__":

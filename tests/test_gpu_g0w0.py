@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import librpa_gb300 as L
-from conftest import load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
+from conftest import load_bn_shrink_g0w0, load_h2o_g0w0, load_he_exx, load_li_g0w0, load_mgo, oracle_input
 from oracle.dielec import interpolate_dielec_func
 from oracle.gw_oracle import HA2EV, BandPoints, exx_kgrid, g0w0_gamma, g0w0_kgrid
 from oracle.rpa_oracle import Options as OOpts
@@ -205,3 +205,55 @@ def test_periodic_exchange_at_band_points_off_the_grid():
     got = h.get_exx_pot_band_k(L.Options(nfreq=16, tfgrids_type=L.Minimax), s.n_spins, list(range(nkb)), 0, nb)
     ref = exx_kgrid(oracle_input(s), s.v_cut, BandPoints(kf, wfc, ekb, s.efermi))
     np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10)
+
+
+@pytest.fixture(scope="module")
+def bn_shrink():
+    s = load_bn_shrink_g0w0()
+    r = g0w0_kgrid(oracle_input(s), s.v_cut, s.vxc, OOpts(nfreq=s.nfreq), n_params=s.n_params_anacon,
+                   sqrt_threshold=s.sqrt_coulomb_threshold)
+    return s, r
+
+
+def _bn_run(s, prec):
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=prec, ec_path=L.EC_LU_FP64))
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  n_params_anacon=s.n_params_anacon, use_shrink_abfs=1,
+                  sqrt_coulomb_threshold=s.sqrt_coulomb_threshold)
+    nb, nk = s.n_bands, s.n_kpts
+    ks = list(range(nk))
+    vexx = h.get_exx_pot_kgrid(o, s.n_spins, ks, 0, nb)
+    vxc = s.vxc.reshape(s.n_spins, nk, nb)
+    sig = h.get_g0w0_sigc_kgrid(o, s.n_spins, ks, 0, nb, vxc, vexx)
+    return h, vexx, vxc, sig
+
+
+def test_bn_shrink_g0w0_tables(bn_shrink):
+    """G0W0 with the ABF shrink (the reference's ABACUS BN case, 2x2x2 k-points, 60 + 59 ABFs
+    shrunk to 17 + 17), FP64 chi0: chi0 shrunk by U chi0 U^H and W_c unfolded by U^H W_c U on the
+    GPU, the exchange on the RI coefficients of the small basis.  Against the oracle (v_exx 1e-10,
+    Sigma_c(i omega) 1e-9, Sigma_c(e_qp) 1e-7 Ha) and the reference's 8 tables: v_exx at print
+    precision, Sigma_c to 2e-4 eV and e_qp to 4e-4 eV (the bounds of the oracle's own agreement:
+    an ill-conditioned 16-point cosine fit and the solver's 1e-5 Ha stopping threshold)."""
+    s, r = bn_shrink
+    h, vexx, vxc, sig = _bn_run(s, L.CHI0_FP64)
+    np.testing.assert_allclose(vexx[0], r["vexx"][0], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq), r["sigc_iw"][0][0], rtol=0, atol=1e-9)
+    np.testing.assert_allclose(sig[0], r["sigc"][0], rtol=0, atol=1e-7)
+    t = s.qp_tables
+    e_qp = s.ekb - vxc + vexx + sig.real
+    np.testing.assert_allclose(vexx[0] * HA2EV, t[:, :, 4], rtol=0, atol=6e-6)
+    np.testing.assert_allclose(sig[0].real * HA2EV, t[:, :, 5], rtol=0, atol=2e-4)
+    np.testing.assert_allclose(sig[0].imag * HA2EV, t[:, :, 6], rtol=0, atol=2e-4)
+    np.testing.assert_allclose(e_qp[0] * HA2EV, t[:, :, 7], rtol=0, atol=4e-4)
+
+
+def test_bn_shrink_g0w0_tensor_core_chi0_within_1mev(bn_shrink):
+    """The default tensor-core chi0 through the same shrunk chain: Sigma_c(i omega) of every
+    state at k-point 0 within 1 meV of the FP64 oracle."""
+    s, r = bn_shrink
+    h, _, _, _ = _bn_run(s, L.CHI0_BF16X3)
+    iw = h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq)
+    assert np.abs(iw - r["sigc_iw"][0][0]).max() * HA2EV < 1e-3
