@@ -27,6 +27,7 @@ TFGRID_UNSET, GaussLegendre, GaussChebyshevI, GaussChebyshevII, Minimax, EvenSpa
     -101, 0, 1, 2, 3, 4, 5)
 CHI0_FP64, CHI0_BF16X3, CHI0_FP32 = 0, 1, 2
 EC_LU_FP64, EC_CHOL, EC_CHOL_FP64 = 0, 1, 2
+SIGMA_FP64, SIGMA_BF16X3 = 0, 1
 SCREEN_OFF, SCREEN_THRESHOLD, SCREEN_MLP = 0, 1, 2
 MLP_IN = 9
 MLP_NPARAM, MLP_NNORM = 64 * MLP_IN + 64 + 64 * 64 + 64 + 64 + 1, 2 * MLP_IN + 3
@@ -96,7 +97,7 @@ class GB300Options(C.Structure):
         ("keep_chi0", C.c_int),
         ("device", C.c_int),
         ("reuse_device_inputs", C.c_int), ("tau_begin", C.c_int), ("tau_end", C.c_int), ("stage", C.c_int),
-        ("q_begin", C.c_int), ("q_end", C.c_int),
+        ("q_begin", C.c_int), ("q_end", C.c_int), ("sigma_precision", C.c_int),
     ]
 
 

@@ -1133,6 +1133,7 @@ void librpa_gb300_init_options(LibrpaGB300Options *o)
     o->tau_end = -1;
     o->q_begin = 0;
     o->q_end = -1;
+    o->sigma_precision = LIBRPA_GB300_SIGMA_FP64;
     o->stage = LIBRPA_GB300_STAGE_FULL;
     o->device = 0;
     o->reuse_device_inputs = 1;
@@ -1142,7 +1143,11 @@ void librpa_gb300_set_options(LibrpaHandler *h, const LibrpaGB300Options *o)
 {
     guarded(h, [&] {
         GB_REQUIRE(o, "null options");
-        get_ds(h)->gbopt = *o;
+        Dataset *ds = get_ds(h);
+        // the kept self-energy depends on the precisions it was built with
+        if (o->chi0_precision != ds->gbopt.chi0_precision || o->sigma_precision != ds->gbopt.sigma_precision)
+            ds->g0w0_generation = 0;
+        ds->gbopt = *o;
     });
 }
 

@@ -37,6 +37,7 @@
 #include "host_tables.h"
 #include "kernels.h"
 #include "minimax.h"
+#include "tc_gemm.h"
 
 namespace gb {
 
@@ -690,6 +691,147 @@ void hs_closed_form(const GammaSetup &gs, const double *W, const double *const *
     }
 }
 
+// ---- the closed form on the tensor cores (3-piece BF16 splits, FP32 accumulation): the three
+// products of hs_closed_form as split GEMMs.  The last one has a short output (n_ao x n_ao) and
+// a long K (N n_ao), so K is cut into chunks of kChunkAbf supercell ABFs, each chunk a batch
+// entry of the split GEMM, and the chunk partials are summed in FP64.
+constexpr int kChunkAbf = 64;
+
+// Zc[c][q][(al, s)] = Z[c kChunkAbf + al][(q, s)] (zero past N): the B operand of the last product
+__global__ void k_chunk_z(const float *__restrict__ Z, int N, int nao, int nch, float *__restrict__ Zc)
+{
+    const long long kc = static_cast<long long>(kChunkAbf) * nao, n = static_cast<long long>(nch) * nao * kc;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long c = t / (static_cast<long long>(nao) * kc);
+        const int q = static_cast<int>((t / kc) % nao);
+        const long long k = t % kc;
+        const long long a = c * kChunkAbf + k / nao;
+        const int s = static_cast<int>(k % nao);
+        Zc[t] = a < N ? Z[(a * nao + q) * nao + s] : 0.0f;
+    }
+}
+
+// Yc[c][p][(al, s)] = Y[(c kChunkAbf + al, p)][s] (zero past N): the A operand of the last product
+__global__ void k_chunk_y(const float *__restrict__ Y, int N, int nao, int nch, float *__restrict__ Yc)
+{
+    const long long kc = static_cast<long long>(kChunkAbf) * nao, n = static_cast<long long>(nch) * nao * kc;
+    for (long long t = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; t < n;
+         t += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        const long long c = t / (static_cast<long long>(nao) * kc);
+        const int p = static_cast<int>((t / kc) % nao);
+        const long long k = t % kc;
+        const long long a = c * kChunkAbf + k / nao;
+        const int s = static_cast<int>(k % nao);
+        Yc[t] = a < N ? Y[(a * nao + p) * nao + s] : 0.0f;
+    }
+}
+
+// H[e] = sum_c Hp[c][e] in FP64
+__global__ void k_sum_chunks(const float *__restrict__ Hp, long long nn, int nch, double *__restrict__ H)
+{
+    for (long long e = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x; e < nn;
+         e += static_cast<long long>(gridDim.x) * blockDim.x)
+    {
+        double acc = 0.0;
+        for (int c = 0; c < nch; ++c) acc += static_cast<double>(Hp[static_cast<long long>(c) * nn + e]);
+        H[e] = acc;
+    }
+}
+
+struct HsSplitWork
+{
+    const GammaSetup *gs = nullptr;  // the setup whose U the cached splits hold
+    SplitStore Ut, Ur, Wsp, Dsp, Zs, Ys;
+    DevBuf<float> Zf, Yf, Zc, Yc, Hp;
+    DevBuf<int> err;
+};
+
+int pad64(long long n) { return static_cast<int>((n + 63) / 64 * 64); }
+
+void hs_closed_form_split(const GammaSetup &gs, const double *W, const double *const *D, int nd, double *const *H,
+                          HsSplitWork &wk, cudaStream_t st)
+{
+    const int N = gs.N, nao = gs.nao;
+    const long long nn = static_cast<long long>(nao) * nao, big = static_cast<long long>(N) * nn;
+    const int kpN = pad64(N), kpA = pad64(nao);
+    const int nch = (N + kChunkAbf - 1) / kChunkAbf;
+    const long long kc = static_cast<long long>(kChunkAbf) * nao, chunked = static_cast<long long>(nch) * nao * kc;
+    GB_REQUIRE(kc <= 0x7fffffffLL && big <= 0x7fffffffLL * 64LL, "supercell too large for the split closed form");
+    if (wk.gs != &gs)
+    {
+        // U is fixed for the setup: its two operand layouts are split once
+        wk.Ut.alloc(3, static_cast<size_t>(nn) * kpN);
+        wk.Ur.alloc(3, static_cast<size_t>(N) * nao * kpA);
+        split_transpose_f64(gs.U.get(), nn, N, static_cast<int>(nn), kpN, wk.Ut.bufs(), st);  // [(p, r)][a]
+        split_rows_f64(gs.U.get(), nao, static_cast<long long>(N) * nao, nao, kpA, wk.Ur.bufs(), st);  // [(a, p)][r]
+        wk.Wsp.alloc(3, static_cast<size_t>(N) * kpN);
+        wk.Dsp.alloc(3, static_cast<size_t>(nao) * kpA);
+        wk.Zf.alloc(big);
+        wk.Yf.alloc(big);
+        wk.Zc.alloc(chunked);
+        wk.Yc.alloc(chunked);
+        wk.Zs.alloc(3, chunked);
+        wk.Ys.alloc(3, chunked);
+        wk.Hp.alloc(static_cast<size_t>(nch) * nn);
+        wk.err.alloc(1);
+        wk.err.zero(st);
+        wk.gs = &gs;
+    }
+    // Z = W U: Z[a][(q, s)]
+    split_rows_f64(W, N, N, N, kpN, wk.Wsp.bufs(), st);
+    tc_gemm_split(wk.Wsp.mat(N, kpN, 0), wk.Ut.mat(nn, kpN, 0), N, static_cast<int>(nn), N, 1, wk.Zf.get(), nn, 0,
+                  false, wk.err.get(), st);
+    k_chunk_z<<<grid_for(chunked), 256, 0, st>>>(wk.Zf.get(), N, nao, nch, wk.Zc.get());
+    GB_LAUNCH_CHECK();
+    split_rows_f32(wk.Zc.get(), kc, static_cast<long long>(nch) * nao, static_cast<int>(kc), static_cast<int>(kc),
+                   wk.Zs.bufs(), st);
+    for (int d = 0; d < nd; ++d)
+    {
+        // Y = U D: Y[(a, p)][s]
+        split_transpose_f64(D[d], nao, nao, nao, kpA, wk.Dsp.bufs(), st);
+        tc_gemm_split(wk.Ur.mat(static_cast<long long>(N) * nao, kpA, 0), wk.Dsp.mat(nao, kpA, 0), N * nao, nao, nao, 1,
+                      wk.Yf.get(), nao, 0, false, wk.err.get(), st);
+        k_chunk_y<<<grid_for(chunked), 256, 0, st>>>(wk.Yf.get(), N, nao, nch, wk.Yc.get());
+        GB_LAUNCH_CHECK();
+        split_rows_f32(wk.Yc.get(), kc, static_cast<long long>(nch) * nao, static_cast<int>(kc), static_cast<int>(kc),
+                       wk.Ys.bufs(), st);
+        // H = sum over chunks of Yc[c] Zc[c]^T
+        tc_gemm_split(wk.Ys.mat(nao, kc, static_cast<long long>(nao) * kc), wk.Zs.mat(nao, kc, static_cast<long long>(nao) * kc),
+                      nao, nao, static_cast<int>(kc), nch, wk.Hp.get(), nao, nn, false, wk.err.get(), st);
+        k_sum_chunks<<<grid_for(nn), 256, 0, st>>>(wk.Hp.get(), nn, nch, H[d]);
+        GB_LAUNCH_CHECK();
+    }
+    int herr = 0;
+    wk.err.download(&herr, 1, st);
+    GB_CUDA(cudaStreamSynchronize(st));
+    GB_REQUIRE(herr == 0, "split GEMM of the self-energy closed form timed out");
+}
+
+// The self-energy's closed form in the precision LibrpaGB300Options.sigma_precision asks for:
+// FP64 GEMMs (the default), or the 3-piece split GEMMs where the split transpose of U fits its
+// launch grid.
+struct SigmaClosedForm
+{
+    bool split = false;
+    HsWork fp64;
+    HsSplitWork tc;
+    SigmaClosedForm(const Dataset &ds, const GammaSetup &gs)
+    {
+        const long long nn = static_cast<long long>(gs.nao) * gs.nao;
+        split = ds.gbopt.sigma_precision == LIBRPA_GB300_SIGMA_BF16X3 && (nn + 31) / 32 <= 65535;
+    }
+    void run(const GammaSetup &gs, const double *W, const double *const *D, int nd, double *const *H, cudaStream_t st)
+    {
+        if (split)
+            hs_closed_form_split(gs, W, D, nd, H, tc, st);
+        else
+            hs_closed_form(gs, W, D, nd, H, fp64, st);
+    }
+};
+
 void require_gamma(const Dataset &ds)
 {
     GB_REQUIRE(ds.n_kpts == 1 && ds.period[0] == 1 && ds.period[1] == 1 && ds.period[2] == 1,
@@ -903,7 +1045,7 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     // Sigma_c(i omega) = sum_tau [cos_t2f (S+ + S-)/2 + i sin_t2f (S+ - S-)/2] per spin, then the KS diagonal
     DevBuf<cuDoubleComplex> Sig(nn * nw), dpsi(static_cast<size_t>(nb) * nao), sks(static_cast<size_t>(nb) * nw);
     DevBuf<double> sgn_s(2ull * nb), Gp(nn), Gm(nn), Sp(nn), Sm(nn), cw(nw), sw(nw);
-    HsWork wk;
+    SigmaClosedForm cf(ds, gs);
     ds.sigc_ks.assign(ns, {});
     ds.sigc_r.assign(ns, {});
     for (int s = 0; s < ns; ++s)
@@ -939,7 +1081,7 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             GB_LAUNCH_CHECK();
             const double *Dp[2] = {Gp.get(), Gm.get()};
             double *Hp[2] = {Sp.get(), Sm.get()};
-            hs_closed_form(gs, Wt.get() + it * NN, Dp, 2, Hp, wk, st);
+            cf.run(gs, Wt.get() + it * NN, Dp, 2, Hp, st);
             std::vector<double> c(nw), sn(nw);
             for (int w = 0; w < nw; ++w)
             {
@@ -1300,7 +1442,7 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     DevBuf<double> d_s(2ull * nk * nb), d_G(2ull * nc * nnc), Ws(static_cast<size_t>(gs.N) * gs.N), Gps(ns2), Gms(ns2),
         Sp(ns2), Sm(ns2), cw(nw), sw(nw);
     DevBuf<cuDoubleComplex> d_A(2ull * nk * nnc), Sig(static_cast<size_t>(nw) * nc * nnc);
-    HsWork wk;
+    SigmaClosedForm cf(ds, gs);
     ds.sigc_ks.assign(ns, {});
     ds.sigc_r.assign(ns, {});
     std::vector<cplx> hsig(static_cast<size_t>(nw) * nc * nnc);
@@ -1320,7 +1462,7 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             GB_LAUNCH_CHECK();
             const double *Dp[2] = {Gps.get(), Gms.get()};
             double *Hp[2] = {Sp.get(), Sm.get()};
-            hs_closed_form(gs, Ws.get(), Dp, 2, Hp, wk, st);
+            cf.run(gs, Ws.get(), Dp, 2, Hp, st);
             std::vector<double> c(nw), sn(nw);
             for (int w = 0; w < nw; ++w)
             {

@@ -11,7 +11,8 @@
 // Keys: task (rpa, exx, g0w0), input_dir, nfreq, tfgrids_type, parallel_routing, cs_threshold,
 // vq_threshold, libri_chi0_threshold_C, libri_chi0_threshold_G, minimax_emin/emax, and the
 // GPU controls gb300_chi0_precision (fp64 | bf16x3 | fp32), gb300_ec_path (lu | chol |
-// chol_fp64), gb300_screen_mode (off | threshold | mlp), gb300_screen_threshold.
+// chol_fp64), gb300_screen_mode (off | threshold | mlp), gb300_screen_threshold,
+// gb300_sigma_precision (fp64 | bf16x3: the G0W0 self-energy's contraction).
 // use_shrink_abfs = t reads the ABF shrink as driver/read_data.cpp:2455-2622 does: the small ABF
 // count per atom from the Cs_shrinked_data headers, U(q) from shrink_sinvS_*, and the Coulomb
 // matrix in the small basis.
@@ -194,6 +195,8 @@ int main()
         go.screen_mode = sm == "threshold" ? LIBRPA_GB300_SCREEN_THRESHOLD : sm == "mlp" ? LIBRPA_GB300_SCREEN_MLP
                                                                                          : LIBRPA_GB300_SCREEN_OFF;
         go.screen_threshold = std::stod(par("gb300_screen_threshold", "1e-6"));
+        go.sigma_precision = lower(par("gb300_sigma_precision", "fp64")) == "bf16x3" ? LIBRPA_GB300_SIGMA_BF16X3
+                                                                                    : LIBRPA_GB300_SIGMA_FP64;
         librpa_gb300_set_options(h, &go);
 
         Mesh m;

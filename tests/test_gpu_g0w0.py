@@ -24,14 +24,14 @@ def _opts(s):
                      n_params_anacon=s.n_params_anacon)
 
 
-def _run(s, prec, keep=None):
+def _run(s, prec, keep=None, sigma=L.SIGMA_FP64):
     """v_exx and Sigma_c(e_qp) of every state, per spin, through the library; e_qp from them.
     keep (a list) receives the handler."""
     h = L.Handler()
     if keep is not None:
         keep.append(h)
     L.load_system(h, s)
-    h.set_gb300_options(L.gb300_options(chi0_precision=prec, ec_path=L.EC_LU_FP64))
+    h.set_gb300_options(L.gb300_options(chi0_precision=prec, ec_path=L.EC_LU_FP64, sigma_precision=sigma))
     o = _opts(s)
     nb = s.n_bands
     vexx = h.get_exx_pot_kgrid(o, s.n_spins, [0], 0, nb)
@@ -66,8 +66,10 @@ def test_h2o_table_fp64(h2o):
     np.testing.assert_allclose(h[0].g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq), r["sigc_iw"][0], rtol=0, atol=1e-10)
 
 
-def test_h2o_tensor_core_chi0_within_1mev(h2o):
-    """The default 3-piece BF16 tensor-core chi0 feeding the same chain: the KS-diagonal
+@pytest.mark.parametrize("sigma", [L.SIGMA_FP64, L.SIGMA_BF16X3])
+def test_h2o_tensor_core_chi0_within_1mev(h2o, sigma):
+    """The default 3-piece BF16 tensor-core chi0 feeding the same chain, with the self-energy's
+    contraction in FP64 and as 3-piece BF16 split GEMMs: the KS-diagonal
     Sigma_c(i omega) of every state and frequency within 1 meV of the FP64 oracle (the G0W0 bar).
     The analytic continuation to the real axis with 16 Pade parameters is ill-conditioned for the
     high virtual states (measured: up to 0.15 eV at the quasi-particle energy for the highest
@@ -75,7 +77,7 @@ def test_h2o_tensor_core_chi0_within_1mev(h2o):
     states around the gap: the top three occupied and the first three empty ones."""
     s, r = h2o
     hs = []
-    _, sig, _ = _run(s, L.CHI0_BF16X3, hs)
+    _, sig, _ = _run(s, L.CHI0_BF16X3, hs, sigma)
     iw = hs[0].g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq)
     assert np.abs(iw - r["sigc_iw"][0]).max() * HA2EV < 1e-3, np.abs(iw - r["sigc_iw"][0]).max() * HA2EV
     homo = int(np.sum(s.wg[0, 0] > 0)) - 1
@@ -149,15 +151,10 @@ def test_periodic_exchange_mgo_ibz_reduced():
     np.testing.assert_allclose(got[0] * HA2EV, s.qp_tables[:, :, 4], rtol=0, atol=6e-6)
 
 
-def test_mgo_kgrid_g0w0_tables():
-    """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
-    replaced by the given eps_mac, 6 minimax points, all 6 in the Pade fit), FP64 chi0: v_exx,
-    Re/Im Sigma_c and e_qp of all 17 states at all 27 k-points against the reference's tables
-    (refs/g0w0_aims_MgO_libri, 5 decimals in eV)."""
-    s = load_mgo()
+def _mgo_run(s, prec, sigma=L.SIGMA_FP64):
     h = L.Handler()
     L.load_system(h, s)
-    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    h.set_gb300_options(L.gb300_options(chi0_precision=prec, ec_path=L.EC_LU_FP64, sigma_precision=sigma))
     o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
                   n_params_anacon=s.n_params_anacon, replace_w_head=1, option_dielect_func=0)
     om, _ = h.get_imaginary_frequency_grids(o)
@@ -167,6 +164,22 @@ def test_mgo_kgrid_g0w0_tables():
     vexx = h.get_exx_pot_kgrid(o, s.n_spins, ks, 0, nb)
     vxc = s.vxc.reshape(s.n_spins, nk, nb)
     sig = h.get_g0w0_sigc_kgrid(o, s.n_spins, ks, 0, nb, vxc, vexx)
+    return h, o, vexx, vxc, sig
+
+
+@pytest.fixture(scope="module")
+def mgo_fp64():
+    s = load_mgo()
+    return (s,) + _mgo_run(s, L.CHI0_FP64)
+
+
+def test_mgo_kgrid_g0w0_tables(mgo_fp64):
+    """Periodic G0W0 (MgO, 3x3x3 k-points from 14 IBZ points, head of the dielectric matrix
+    replaced by the given eps_mac, 6 minimax points, all 6 in the Pade fit), FP64 chi0 and FP64
+    self-energy products: v_exx, Re/Im Sigma_c and e_qp of all 17 states at all 27 k-points
+    against the reference's tables (refs/g0w0_aims_MgO_libri, 5 decimals in eV)."""
+    s, h, o, vexx, vxc, sig = mgo_fp64
+    nb = s.n_bands
     e_qp = s.ekb - vxc + vexx + sig.real
     got = np.stack([vexx[0] * HA2EV, sig[0].real * HA2EV, sig[0].imag * HA2EV, e_qp[0] * HA2EV], axis=-1)
     np.testing.assert_allclose(got, s.qp_tables[:, :, 4:8], rtol=0, atol=6e-6)
@@ -179,6 +192,23 @@ def test_mgo_kgrid_g0w0_tables():
     np.testing.assert_allclose(vb, vexx[:, kb], rtol=0, atol=1e-9)
     sb = h.get_g0w0_sigc_band_k(o, s.n_spins, [0, 1, 2], 0, nb, vxc[:, kb], vb)
     np.testing.assert_allclose(sb, sig[:, kb], rtol=0, atol=1e-8)
+
+
+def test_mgo_tensor_core_self_energy_within_1mev(mgo_fp64):
+    """Tensor-core chi0 and the self-energy's closed form as 3-piece BF16 split GEMMs
+    (sigma_precision = BF16X3: FP32 accumulation, the long contraction cut into ABF chunks summed
+    in FP64) on MgO.
+    Sigma_c(i omega) of every state at k-point 0 within 1 meV of the all-FP64 run, and Sigma_c at
+    the quasi-particle energy of the states around the gap at every k-point within 1 meV."""
+    s, h64, _, _, _, sig64 = mgo_fp64
+    h, _, _, _, sig = _mgo_run(s, L.CHI0_BF16X3, L.SIGMA_BF16X3)
+    nb = s.n_bands
+    d_iw = np.abs(h.g0w0_sigc_iw(0, 0, nb, s.nfreq) - h64.g0w0_sigc_iw(0, 0, nb, s.nfreq)).max() * HA2EV
+    assert d_iw < 1e-3, d_iw
+    homo = int(np.sum(s.wg[0, 0] > 0)) - 1
+    frontier = slice(homo - 2, homo + 4)
+    d_qp = np.abs(sig[0][:, frontier] - sig64[0][:, frontier]).max() * HA2EV
+    assert d_qp < 1e-3, d_qp
 
 
 def h_kfrac(s):
