@@ -57,11 +57,11 @@ typedef struct
      * scattered chi0(q, omega) and the per-q sums are all-reduced) */
     int q_begin;             /* first IBZ q point (default 0) */
     int q_end;               /* one past the last; -1 = all (default -1) */
-    int sigma_precision;     /* LIBRPA_GB300_SIGMA_*: the G0W0 self-energy's contraction
-                                (default FP64) */
+    int sigma_precision;     /* LIBRPA_GB300_SIGMA_*: the contraction of the G0W0 correlation
+                                self-energy (default FP64; the exchange is always FP64) */
 } LibrpaGB300Options;
 
-/* G0W0 self-energy contraction precision */
+/* G0W0 correlation self-energy contraction precision */
 #define LIBRPA_GB300_SIGMA_FP64 0     /* FP64 GEMMs */
 #define LIBRPA_GB300_SIGMA_BF16X3 1   /* 3-term BF16 split GEMMs on tcgen05, FP32 accumulate, the
                                          long contraction cut into chunks summed in FP64 */

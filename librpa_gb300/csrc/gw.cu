@@ -810,9 +810,10 @@ void hs_closed_form_split(const GammaSetup &gs, const double *W, const double *c
     GB_REQUIRE(herr == 0, "split GEMM of the self-energy closed form timed out");
 }
 
-// The self-energy's closed form in the precision LibrpaGB300Options.sigma_precision asks for:
-// FP64 GEMMs (the default), or the 3-piece split GEMMs where the split transpose of U fits its
-// launch grid.
+// The correlation self-energy's closed form in the precision LibrpaGB300Options.sigma_precision
+// asks for: FP64 GEMMs (the default), or the 3-piece split GEMMs where the split transpose of U
+// fits its launch grid.  (The exchange stays FP64: through the split products its v_exx moved by
+// up to 1 meV on MgO, far above the reference's print precision.)
 struct SigmaClosedForm
 {
     bool split = false;
@@ -877,7 +878,7 @@ void build_exx(Dataset &ds, const LibrpaOptions &opts)
     DevBuf<double> dV(vs.size()), dD(nn), dH(nn);
     dV.upload(vs.data(), vs.size(), st);
     std::vector<double> hs(nn);
-    HsWork wk;
+    HsWork wk;  // FP64: v_exx is held to the reference's print precision
     ds.hx.assign(ns, {});
     ds.hx_r.assign(ns, {});
     for (int s = 0; s < ns; ++s)

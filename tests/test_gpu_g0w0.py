@@ -195,14 +195,16 @@ def test_mgo_kgrid_g0w0_tables(mgo_fp64):
 
 
 def test_mgo_tensor_core_self_energy_within_1mev(mgo_fp64):
-    """Tensor-core chi0 and the self-energy's closed form as 3-piece BF16 split GEMMs
+    """Tensor-core chi0 and the self-energies' closed form as 3-piece BF16 split GEMMs
     (sigma_precision = BF16X3: FP32 accumulation, the long contraction cut into ABF chunks summed
     in FP64) on MgO.
     Sigma_c(i omega) of every state at k-point 0 within 1 meV of the all-FP64 run, and Sigma_c at
     the quasi-particle energy of the states around the gap at every k-point within 1 meV."""
-    s, h64, _, _, _, sig64 = mgo_fp64
-    h, _, _, _, sig = _mgo_run(s, L.CHI0_BF16X3, L.SIGMA_BF16X3)
+    s, h64, _, vexx64, _, sig64 = mgo_fp64
+    h, _, vexx, _, sig = _mgo_run(s, L.CHI0_BF16X3, L.SIGMA_BF16X3)
     nb = s.n_bands
+    # the exchange stays FP64 whatever sigma_precision says
+    np.testing.assert_allclose(vexx, vexx64, rtol=0, atol=1e-10)
     d_iw = np.abs(h.g0w0_sigc_iw(0, 0, nb, s.nfreq) - h64.g0w0_sigc_iw(0, 0, nb, s.nfreq)).max() * HA2EV
     assert d_iw < 1e-3, d_iw
     homo = int(np.sum(s.wg[0, 0] > 0)) - 1
