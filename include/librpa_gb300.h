@@ -46,7 +46,8 @@ typedef struct
     int keep_chi0;           /* keep chi0(q, omega) on the device for librpa_gb300_get_chi0_block */
     int device;              /* CUDA device ordinal (default 0) */
     int reuse_device_inputs; /* keep the staged inputs on the device between calls while no
-                                librpa_set_* call changed them (default 1); 0 re-uploads every call */
+                                librpa_set_* call changed them (default 1); 0 re-uploads every call
+                                (into the device buffers the handler keeps while sizes agree) */
     /* tau sharding (one slice of the minimax tau points per rank; the chi0(q, omega) partial
      * sums are reduced over ranks before E_c): */
     int tau_begin;           /* first tau point of this call (default 0) */

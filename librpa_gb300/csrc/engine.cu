@@ -203,35 +203,49 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     auto d_atom_of = to_dev(atom_of, st);
     std::vector<int> abf_off_n(abf_off.begin(), abf_off.end() - 1);
     auto d_abf_off = to_dev(abf_off_n, st);
-    // Inputs staged once per input generation (reused while no setter ran).
+    // Inputs staged once per input generation (reused while no setter ran).  Their device buffers
+    // are kept with the handler: a call that re-stages (a setter ran, or reuse_device_inputs = 0)
+    // copies into them again when the sizes still fit, instead of freeing and allocating ~1 GB.
     struct DeviceInputs
     {
         unsigned long long generation = 0;
-        int precision = -1;
-        DevBuf<double> ekb, wg, C;
+        int device = -1;
+        DevBuf<double> ekb, wg, C, csblob;
         DevBuf<cuDoubleComplex> psi, vblob;
         long long rows_c = 0, n_sup = 0;
     };
     std::shared_ptr<DeviceInputs> din = std::static_pointer_cast<DeviceInputs>(ds.dev_cache);
     const bool reuse = go.reuse_device_inputs && din && din->generation == ds.generation &&
-                       din->rows_c == rows_c && din->n_sup == n_sup;
+                       din->device == go.device && din->rows_c == rows_c && din->n_sup == n_sup;
     double h2d = 0.0;
     if (!reuse)
     {
-        ds.dev_cache.reset();
-        din = std::make_shared<DeviceInputs>();
+        const size_t n_cs = ds.cs_blob.size() + csf.extra.size();
+        const bool fits = din && din->device == go.device && din->rows_c == rows_c && din->n_sup == n_sup &&
+                          din->ekb.size() == ds.ekb.size() &&
+                          din->wg.size() == ds.wg.size() && din->psi.size() == ds.wfc.size() &&
+                          din->vblob.size() == ds.vq_blob.size() && din->csblob.size() == n_cs;
+        if (!fits)
+        {
+            ds.dev_cache.reset();
+            din.reset();
+            din = std::make_shared<DeviceInputs>();
+            din->device = go.device;
+            din->rows_c = rows_c;
+            din->n_sup = n_sup;
+            din->ekb.alloc(ds.ekb.size());
+            din->wg.alloc(ds.wg.size());
+            din->psi.alloc(ds.wfc.size());
+            din->vblob.alloc(ds.vq_blob.size());
+            din->csblob.alloc(n_cs);
+            din->C.alloc(static_cast<size_t>(rows_c) * n_sup);
+        }
         din->generation = ds.generation;
-        din->rows_c = rows_c;
-        din->n_sup = n_sup;
-        din->ekb.alloc(ds.ekb.size());
-        din->wg.alloc(ds.wg.size());
         din->ekb.upload(ds.ekb.data(), ds.ekb.size(), st);
         din->wg.upload(ds.wg.data(), ds.wg.size(), st);
-        din->psi.alloc(ds.wfc.size());
         din->psi.upload(reinterpret_cast<const cuDoubleComplex *>(ds.wfc.data()), ds.wfc.size(), st);
-        din->vblob.alloc(ds.vq_blob.size());
         din->vblob.upload(reinterpret_cast<const cuDoubleComplex *>(ds.vq_blob.data()), ds.vq_blob.size(), st);
-        DevBuf<double> d_csblob(ds.cs_blob.size() + csf.extra.size());
+        DevBuf<double> &d_csblob = din->csblob;
         d_csblob.upload(ds.cs_blob.data(), ds.cs_blob.size(), st);
         if (!csf.extra.empty())
             GB_CUDA(cudaMemcpyAsync(d_csblob.get() + ds.cs_blob.size(), csf.extra.data(),
@@ -239,7 +253,6 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
         auto d_csoff = to_dev(cs_off, st);
         auto d_csmeta = to_dev(cs_meta, st);
         h2d = 8.0 * (ds.ekb.size() + ds.wg.size() + ds.cs_blob.size()) + 16.0 * (ds.wfc.size() + ds.vq_blob.size());
-        din->C.alloc(static_cast<size_t>(rows_c) * n_sup);
         din->C.zero(st);
         Geom gs;
         gs.n_at = n_at;
@@ -254,7 +267,7 @@ RpaResult run_rpa_gpu(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                           din->C.get(), st);
         ++launches;
         GB_CUDA(cudaStreamSynchronize(st));
-        if (go.reuse_device_inputs) ds.dev_cache = din;
+        ds.dev_cache = din;
     }
     S.h2d_bytes = h2d;
     DevBuf<double> &d_ekb = din->ekb, &d_wg = din->wg;
