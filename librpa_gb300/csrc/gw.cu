@@ -850,6 +850,17 @@ void build_exx(Dataset &ds, const LibrpaOptions &opts)
     GB_REQUIRE(ds.occ_set, "occupations/eigenvalues not set");
     for (size_t i = 0; i < ds.wfc_set.size(); ++i) GB_REQUIRE(ds.wfc_set[i], "wave function missing for some (spin, k)");
     GB_REQUIRE(!ds.vq_cut_blocks.empty(), "the truncated Coulomb matrix is not set (librpa_set_aux_cut_coulomb_*)");
+    // with use_shrink_abfs the exchange contracts the RI coefficients of the small basis with the
+    // truncated Coulomb matrix given there (Exx::build on Cs_shrinked_data, driver/task_gw_band.cpp:92-99)
+    const bool shrink = opts.use_shrink_abfs == LIBRPA_SWITCH_ON;
+    if (shrink)
+    {
+        GB_REQUIRE(static_cast<int>(ds.shrink_nabf.size()) == ds.n_atoms(),
+                   "use_shrink_abfs: the small ABF basis must be set for every atom (librpa_gb300_set_shrink_basis)");
+        GB_REQUIRE(!ds.shrink_cs_blocks.empty(),
+                   "use_shrink_abfs: the exchange needs the RI coefficients of the small basis "
+                   "(librpa_gb300_set_shrink_lri_coeff)");
+    }
     GB_CUDA(cudaSetDevice(ds.gbopt.device));
     cudaStream_t st;
     GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
@@ -858,16 +869,9 @@ void build_exx(Dataset &ds, const LibrpaOptions &opts)
         cudaStream_t s;
         ~Guard() { cudaStreamDestroy(s); }
     } guard{st};
-    // with use_shrink_abfs the exchange contracts the RI coefficients of the small basis with the
-    // truncated Coulomb matrix given there (Exx::build on Cs_shrinked_data, driver/task_gw_band.cpp:92-99)
     GammaSetup gs;
-    if (opts.use_shrink_abfs == LIBRPA_SWITCH_ON)
+    if (shrink)
     {
-        GB_REQUIRE(static_cast<int>(ds.shrink_nabf.size()) == ds.n_atoms(),
-                   "use_shrink_abfs: the small ABF basis must be set for every atom (librpa_gb300_set_shrink_basis)");
-        GB_REQUIRE(!ds.shrink_cs_blocks.empty(),
-                   "use_shrink_abfs: the exchange needs the RI coefficients of the small basis "
-                   "(librpa_gb300_set_shrink_lri_coeff)");
         setup_gamma(ds, RiSet{ds.shrink_cs_blocks, ds.shrink_cs_blob, ds.shrink_nabf}, opts.libri_exx_threshold_C, gs, st);
     }
     else

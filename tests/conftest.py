@@ -132,12 +132,19 @@ def bn_shrink_dir():
     return _BN_DIR
 
 
+_BN_INPUT = None
+
+
 def load_bn_shrink():
     """The ABACUS BN case with an ABF shrink, read as the reference's driver reads it: Cs in the
     large ABF basis (60 + 59), the Coulomb matrix in the small basis (17 + 17) and U(q) = sinvS(q)
-    per IBZ point."""
+    per IBZ point.  The text files are parsed once per session; each call returns a fresh record
+    (the arrays are shared: tests must not change them in place)."""
+    global _BN_INPUT
     from oracle.aims_dataset import read_dataset
-    inp = read_dataset(str(bn_shrink_dir()))
+    if _BN_INPUT is None:
+        _BN_INPUT = read_dataset(str(bn_shrink_dir()))
+    inp = _BN_INPUT
     return SimpleNamespace(**{k: getattr(inp, k) for k in inp.__dataclass_fields__}, name="bn_shrink",
                            types=np.zeros(len(inp.nao), int), nfreq=16, minimax_emin=-1.0, minimax_emax=-1.0)
 

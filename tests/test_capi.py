@@ -227,3 +227,28 @@ def test_rank_cut_grid_gives_the_oracle_ec_on_an_ill_conditioned_window(lib):
     finally:
         R.grids_for = saved
     assert abs(ec - ref) <= 1e-10 * abs(ref), (ec, ref)
+
+
+def test_shrink_lri_coeff_setter_checks_its_inputs(lib):
+    """librpa_gb300_set_shrink_lri_coeff needs the small basis first and blocks sized for it; the
+    exchange of a shrunk input refuses to run without those blocks (before any GPU work)."""
+    from conftest import load_bn_shrink_g0w0
+    s = load_bn_shrink_g0w0()
+    with L.Handler() as h:
+        h.set_scf_dimension(s.n_spins, s.n_kpts, s.n_bands, s.n_ao)
+        h.set_ao_basis_wfc(s.nao)
+        h.set_ao_basis_aux(s.nabf)
+        c = np.zeros((s.nao[0] * s.nao[1], s.nabf_small[0]))
+        with pytest.raises(L.LibrpaError, match="small auxiliary basis not set"):
+            h.set_shrink_lri_coeff(0, 1, s.nao[0], s.nao[1], s.nabf_small[0], (0, 0, 0), c)
+        h.set_shrink_basis(s.nabf_small)
+        with pytest.raises(L.LibrpaError, match="inconsistent with the small basis"):
+            h.set_shrink_lri_coeff(0, 1, s.nao[0], s.nao[1], s.nabf[0], (0, 0, 0),
+                                   np.zeros((s.nao[0] * s.nao[1], s.nabf[0])))
+        h.set_shrink_lri_coeff(0, 1, s.nao[0], s.nao[1], s.nabf_small[0], (0, 0, 0), c)
+    s.Cs_small = None
+    with L.Handler() as h:
+        L.load_system(h, s)
+        o = L.Options(nfreq=16, tfgrids_type=L.Minimax, use_shrink_abfs=1)
+        with pytest.raises(L.LibrpaError, match="RI coefficients of the small basis"):
+            h.get_exx_pot_kgrid(o, 1, [0], 0, 4)
