@@ -441,6 +441,59 @@ std::vector<double> coulomb_gamma(const std::vector<VqBlock> &blocks, const std:
     return V;
 }
 
+// LibRI's filter of set_Ws / set_Gs / set_Vs / set_Ds (threshold_filter, RI_Tools.hpp:16-27, applied
+// after the period folding of LRI-set.hpp:33-75): an atom-pair block of a cell-periodic matrix is
+// dropped unless its largest |x| exceeds the threshold.  Block (I, J) of cell blockIdx.y and slice
+// blockIdx.z of X, the cells cstride and the slices zstride elements apart, each cell n x n.
+__global__ void k_block_filter(double *__restrict__ X, long long cstride, long long zstride, int n,
+                               const int *__restrict__ off, int n_at, double thr)
+{
+    __shared__ double red[128];
+    const int I = blockIdx.x / n_at, J = blockIdx.x % n_at;
+    double *B = X + static_cast<long long>(blockIdx.y) * cstride + static_cast<long long>(blockIdx.z) * zstride;
+    const int r0 = off[I], c0 = off[J], nr = off[I + 1] - r0, nc = off[J + 1] - c0;
+    double m = 0.0;
+    for (int t = threadIdx.x; t < nr * nc; t += blockDim.x)
+        m = fmax(m, fabs(B[static_cast<long long>(r0 + t / nc) * n + c0 + t % nc]));
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1)
+    {
+        if (threadIdx.x < h) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+        __syncthreads();
+    }
+    if (red[0] > thr) return;
+    for (int t = threadIdx.x; t < nr * nc; t += blockDim.x) B[static_cast<long long>(r0 + t / nc) * n + c0 + t % nc] = 0.0;
+}
+
+void block_filter_dev(double *X, long long cstride, int ncell, long long zstride, int nz, int n, const int *d_off,
+                      int n_at, double thr, cudaStream_t st)
+{
+    if (thr <= 0.0) return;
+    k_block_filter<<<dim3(n_at * n_at, ncell, nz), 128, 0, st>>>(X, cstride, zstride, n, d_off, n_at, thr);
+    GB_LAUNCH_CHECK();
+}
+
+// The same filter on host cell-periodic blocks XR [cell][n][n] (the exchange's V(R) and D(R)).
+void block_filter_host(std::vector<double> &XR, int n, const std::vector<int> &off, double thr)
+{
+    if (thr <= 0.0) return;
+    const int n_at = static_cast<int>(off.size()) - 1;
+    const size_t ncell = XR.size() / (static_cast<size_t>(n) * n);
+    for (size_t c = 0; c < ncell; ++c)
+        for (int I = 0; I < n_at; ++I)
+            for (int J = 0; J < n_at; ++J)
+            {
+                double *B = XR.data() + c * n * n;
+                double m = 0.0;
+                for (int r = off[I]; r < off[I + 1]; ++r)
+                    for (int q = off[J]; q < off[J + 1]; ++q) m = std::max(m, std::fabs(B[static_cast<size_t>(r) * n + q]));
+                if (m > thr) continue;
+                for (int r = off[I]; r < off[I + 1]; ++r)
+                    for (int q = off[J]; q < off[J + 1]; ++q) B[static_cast<size_t>(r) * n + q] = 0.0;
+            }
+}
+
 // The Born-von Karman supercell of the k-grid: atom (c, I) for cell c of the BvK list and atom
 // I, cell-major.  Every k-grid quantity of the exchange and of Sigma_c is the Gamma-point
 // quantity of this supercell, its matrices built from the cell-periodic blocks,
@@ -877,7 +930,10 @@ void build_exx(Dataset &ds, const LibrpaOptions &opts)
     else
         setup_gamma(ds, opts.libri_exx_threshold_C, gs, st);
     const int nao = gs.nao, naoc = gs.naoc, nc = gs.nc, ns = ds.n_spins;
-    const std::vector<double> vs = to_supercell(coulomb_r(ds, ds.vq_cut_blocks, ds.vq_cut_blob, gs), gs.Nc, gs);
+    // V(R) and D(R) pass LibRI's block filters (libri_exx_threshold_V / _D; exx.cpp:365-418)
+    std::vector<double> vr = coulomb_r(ds, ds.vq_cut_blocks, ds.vq_cut_blob, gs);
+    block_filter_host(vr, gs.Nc, gs.abf_off, opts.libri_exx_threshold_V);
+    const std::vector<double> vs = to_supercell(vr, gs.Nc, gs);
     const long long nn = static_cast<long long>(nao) * nao;
     DevBuf<double> dV(vs.size()), dD(nn), dH(nn);
     dV.upload(vs.data(), vs.size(), st);
@@ -887,7 +943,9 @@ void build_exx(Dataset &ds, const LibrpaOptions &opts)
     ds.hx_r.assign(ns, {});
     for (int s = 0; s < ns; ++s)
     {
-        const std::vector<double> dsup = to_supercell(dmat_r(ds, s, gs), naoc, gs);
+        std::vector<double> dr = dmat_r(ds, s, gs);
+        block_filter_host(dr, naoc, gs.ao_off, opts.libri_exx_threshold_D);
+        const std::vector<double> dsup = to_supercell(dr, naoc, gs);
         dD.upload(dsup.data(), dsup.size(), st);
         const double *Dp[1] = {dD.get()};
         double *Hp[1] = {dH.get()};
@@ -1051,6 +1109,10 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     DevBuf<cuDoubleComplex> Sig(nn * nw), dpsi(static_cast<size_t>(nb) * nao), sks(static_cast<size_t>(nb) * nw);
     DevBuf<double> sgn_s(2ull * nb), Gp(nn), Gm(nn), Sp(nn), Sm(nn), cw(nw), sw(nw);
     SigmaClosedForm cf(ds, gs);
+    // LibRI's set_Ws filter on every W(tau) (libri_g0w0_threshold_Wc; gw.cpp:459-470)
+    auto d_aoo_f = to_dev(gs.ao_off, st);
+    auto d_abo_f = to_dev(gs.abf_off, st);
+    block_filter_dev(Wt.get(), 0, 1, NN, nw, N, d_abo_f.get(), gs.n_at, opts.libri_g0w0_threshold_Wc, st);
     ds.sigc_ks.assign(ns, {});
     ds.sigc_r.assign(ns, {});
     for (int s = 0; s < ns; ++s)
@@ -1084,6 +1146,9 @@ void build_g0w0_gamma(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
             sgn_s.upload(sm.data(), nb, st);
             k_gamma_dm<<<(nao * nao + 255) / 256, 256, 0, st>>>(dpsi.get(), sgn_s.get(), nb, nao, -1.0, Gm.get());
             GB_LAUNCH_CHECK();
+            // LibRI's set_Gs filter (libri_g0w0_threshold_G; gw.cpp:546-616)
+            block_filter_dev(Gp.get(), 0, 1, 0, 1, nao, d_aoo_f.get(), gs.n_at, opts.libri_g0w0_threshold_G, st);
+            block_filter_dev(Gm.get(), 0, 1, 0, 1, nao, d_aoo_f.get(), gs.n_at, opts.libri_g0w0_threshold_G, st);
             const double *Dp[2] = {Gp.get(), Gm.get()};
             double *Hp[2] = {Sp.get(), Sm.get()};
             cf.run(gs, Wt.get() + it * NN, Dp, 2, Hp, st);
@@ -1432,6 +1497,11 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
     }
     Wq.release();
     WR.release();
+    // LibRI's set_Ws filter on every W(R, tau) block (libri_g0w0_threshold_Wc; gw.cpp:459-470)
+    auto d_abo_f = to_dev(gs.abf_off, st);
+    auto d_aoo_f = to_dev(gs.ao_off, st);
+    block_filter_dev(Wt.get(), static_cast<long long>(nw) * NN, nc, NN, nw, Nc, d_abo_f.get(), n_at,
+                     opts.libri_g0w0_threshold_Wc, st);
 
     // ---- Sigma_c(R, i omega) per spin from the supercell closed form at every tau, then the KS
     // diagonal at every k
@@ -1460,6 +1530,8 @@ void build_g0w0_kgrid(Dataset &ds, const LibrpaOptions &opts, const TimeFreqGrid
                              nk, nb, ds.efermi, tf.tau[it], ns, opts.n_bands_chi0, d_s.get(), st);
             launch_gk_build(d_psi.get() + static_cast<size_t>(sp) * nk * nb * nao, d_s.get(), nk, nb, nao, d_A.get(), st);
             launch_phase_sum(d_A.get(), d_gcos.get(), d_gsin.get(), nk, nc, nao, d_G.get(), st);
+            // LibRI's set_Gs filter on G(R, +-tau) (libri_g0w0_threshold_G; gw.cpp:546-616)
+            block_filter_dev(d_G.get(), nnc, 2 * nc, 0, 1, nao, d_aoo_f.get(), n_at, opts.libri_g0w0_threshold_G, st);
             k_to_super<<<grid_for(ns2), 256, 0, st>>>(d_G.get(), nnc, nao, nc, d_cdiff.get(), Gps.get());
             k_to_super<<<grid_for(ns2), 256, 0, st>>>(d_G.get() + nc * nnc, nnc, nao, nc, d_cdiff.get(), Gms.get());
             k_to_super<<<grid_for(static_cast<long long>(gs.N) * gs.N), 256, 0, st>>>(

@@ -239,8 +239,8 @@ def ordered_blocks(full: np.ndarray, nb) -> dict:
 
 def full_from_blocks(blocks: dict, nb) -> np.ndarray:
     off = np.concatenate([[0], np.cumsum(nb)]).astype(int)
-    first = next(iter(blocks.values()))
-    M = np.zeros((off[-1], off[-1]), first.dtype)
+    dtype = next(iter(blocks.values())).dtype if blocks else float  # no blocks: every one filtered out
+    M = np.zeros((off[-1], off[-1]), dtype)
     for (I, J, _R), b in blocks.items():
         M[off[I]:off[I + 1], off[J]:off[J + 1]] += b
     return M
@@ -412,6 +412,14 @@ class BandPoints:
     vxc: np.ndarray | None = None  # (n_spins, n, n_bands) Hartree
 
 
+def drop_small(blocks: dict, threshold: float) -> dict:
+    """LibRI's set_tensors filter (threshold_filter, RI_Tools.hpp:16-27): an atom-pair block is kept
+    only if its largest |x| exceeds the threshold (0: every block)."""
+    if threshold <= 0:
+        return blocks
+    return {k: v for k, v in blocks.items() if np.abs(v).max() > threshold}
+
+
 def small_basis_view(inp: RPAInput) -> RPAInput:
     """A shrunk input as its exchange sees it: the RI coefficients and ABF counts of the small
     basis (Exx::build on Cs_shrinked_data, driver/task_gw_band.cpp:92-99)."""
@@ -420,21 +428,22 @@ def small_basis_view(inp: RPAInput) -> RPAInput:
     return dataclasses.replace(inp, Cs=inp.Cs_small, nabf=list(inp.nabf_small))
 
 
-def exx_kgrid(inp: RPAInput, v_cut: dict, band: BandPoints | None = None):
+def exx_kgrid(inp: RPAInput, v_cut: dict, band: BandPoints | None = None, thr_v: float = 0.0, thr_d: float = 0.0):
     """v_exx[s, k, n] (Hartree) on the SCF k-grid (task = exx; exx.cpp:213-500, :720-860), or at
     the band points: H(R) summed with e^{i 2 pi k.R} at any k (Exx::build_KS_band).  A shrunk
-    input (inp.sinvS set) takes the small basis, where v_cut is then given."""
+    input (inp.sinvS set) takes the small basis, where v_cut is then given.  thr_v / thr_d: LibRI's
+    block filters of V(R) and D(R)."""
     if inp.sinvS is not None:
         inp = small_basis_view(inp)
     _, kfrac, _, _ = k_lists(inp)
     kpts, wfc = (kfrac, inp.wfc) if band is None else (band.kfrac, band.wfc)
     rlist = r_grid(inp.period)
     C = cs_tensors(inp, 0.0)
-    VR = coulomb_r(inp, v_cut, rlist)
+    VR = drop_small(coulomb_r(inp, v_cut, rlist), thr_v)   # libri_exx_threshold_V / _D (exx.cpp:365-418)
     out = np.zeros((inp.n_spins, len(kpts), inp.n_bands))
     off = np.concatenate([[0], np.cumsum(inp.nao)]).astype(int)
     for s in range(inp.n_spins):
-        H = cal_hs_cells(C, VR, dmat_r(inp, s, rlist), inp.nao, inp.nabf, inp.period)
+        H = cal_hs_cells(C, VR, drop_small(dmat_r(inp, s, rlist), thr_d), inp.nao, inp.nabf, inp.period)
         H = shift_bvk(H, inp)
         for k in range(len(kpts)):
             Hk = np.zeros((inp.n_ao, inp.n_ao), complex)
@@ -463,7 +472,7 @@ def dmat(inp: RPAInput, ispin: int) -> np.ndarray:
 
 
 def g0w0_gamma(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None = None,
-               n_params: int = -1, sqrt_threshold: float = 0.0):
+               n_params: int = -1, sqrt_threshold: float = 0.0, thr_w: float = 0.0, thr_g: float = 0.0):
     """G0W0 at the Gamma point.  inp.Vq holds the Coulomb matrix of the dielectric function,
     v_cut the truncated Coulomb (W and exchange); vxc (n_spins, 1, n_states) in Hartree.
     Returns per spin arrays (Hartree): vexx, sigc (complex, at e_qp), e_qp, sigc_iw (KS
@@ -503,9 +512,10 @@ def g0w0_gamma(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
     for s in range(inp.n_spins):
         sig_w = np.zeros((nf, inp.n_ao, inp.n_ao), complex)
         for it, tau in enumerate(grid["tau"]):
-            Wb = ordered_blocks(Wt[it], nb)
-            Gp = blocks_of(build_gf(inp, s, tau, kfrac, [z]), nao)
-            Gn = blocks_of(build_gf(inp, s, -tau, kfrac, [z]), nao)
+            # libri_g0w0_threshold_Wc / _G (gw.cpp:459-616)
+            Wb = drop_small(ordered_blocks(Wt[it], nb), thr_w)
+            Gp = drop_small(blocks_of(build_gf(inp, s, tau, kfrac, [z]), nao), thr_g)
+            Gn = drop_small(blocks_of(build_gf(inp, s, -tau, kfrac, [z]), nao), thr_g)
             Sp = full_from_blocks(cal_hs_loops(C, Wb, Gp, inp.n_atoms, (1, 1, 1)), nao)
             Sn = full_from_blocks(cal_hs_loops(C, Wb, Gn, inp.n_atoms, (1, 1, 1)), nao)
             cos_part, sin_part = 0.5 * (Sp + Sn), 0.5 * (Sp - Sn)
@@ -563,7 +573,8 @@ def wc_freq_head(chi0, v_eps, v_cut, epsmac, sqrt_threshold=0.0):
 
 
 def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None = None, n_params: int = -1,
-               epsmac=None, sqrt_threshold: float = 0.0, band: BandPoints | None = None):
+               epsmac=None, sqrt_threshold: float = 0.0, band: BandPoints | None = None, thr_w: float = 0.0,
+               thr_g: float = 0.0):
     """G0W0 on the SCF k-grid (task = g0w0 with k-points; epsilon.cpp:1763-2322, :2323-2660,
     gw.cpp:217-876, :884-1240).  inp.Vq: Coulomb matrix of the dielectric function at the IBZ
     q-points, v_cut: truncated Coulomb there; epsmac: the macroscopic dielectric function at the
@@ -634,7 +645,7 @@ def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
             for I in range(inp.n_atoms):
                 for J in range(inp.n_atoms):
                     blocks[(I, J, tuple(R))] = full[off[I]:off[I + 1], off[J]:off[J + 1]].copy()
-        Wt.append(blocks)
+        Wt.append(drop_small(blocks, thr_w))   # libri_g0w0_threshold_Wc (gw.cpp:459-470)
 
     out = {"grid": grid, "vexx": exx_kgrid(inp, v_cut, band), "sigc": [], "e_qp": [], "sigc_iw": []}
     if band is None:
@@ -645,8 +656,8 @@ def g0w0_kgrid(inp: RPAInput, v_cut: dict, vxc: np.ndarray, opts: Options | None
     for s in range(inp.n_spins):
         sig_R = {}  # (I, J, R) -> (nf, n_I, n_J) complex
         for it, tau in enumerate(grid["tau"]):
-            Gp = blocks_of(build_gf(inp, s, tau, kfrac, rl), nao)
-            Gn = blocks_of(build_gf(inp, s, -tau, kfrac, rl), nao)
+            Gp = drop_small(blocks_of(build_gf(inp, s, tau, kfrac, rl), nao), thr_g)
+            Gn = drop_small(blocks_of(build_gf(inp, s, -tau, kfrac, rl), nao), thr_g)
             Sp = cal_hs_cells(C, Wt[it], Gp, nao, nb, inp.period)
             Sn = cal_hs_cells(C, Wt[it], Gn, nao, nb, inp.period)
             for key in Sp:

@@ -289,3 +289,70 @@ def test_bn_shrink_g0w0_tensor_core_chi0_within_1mev(bn_shrink):
     h, _, _, _ = _bn_run(s, L.CHI0_BF16X3)
     iw = h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq)
     assert np.abs(iw - r["sigc_iw"][0][0]).max() * HA2EV < 1e-3
+
+
+def _threshold_between(blocks):
+    """A threshold halfway (geometrically) between two distinct middle block max-norms: about half
+    of the blocks fall under it and none is near it (blocks related by symmetry share a max-norm)."""
+    m = np.sort([np.abs(v).max() for v in blocks.values() if np.abs(v).max() > 0])
+    u = [m[0]]
+    for x in m[1:]:
+        if x > u[-1] * (1 + 1e-6):
+            u.append(x)
+    i = max(1, len(u) // 2)
+    return float(np.sqrt(u[i - 1] * u[i]))
+
+
+def test_exchange_block_filters_match_the_oracle():
+    """libri_exx_threshold_V / _D drop the V(R) and D(R) blocks LibRI's set_Vs / set_Ds filters drop
+    (exx.cpp:365-418): BCC He with thresholds that remove about half of each, against the oracle
+    with the same filters (1e-10 Ha), and visibly different from the unfiltered exchange."""
+    from oracle.gw_oracle import coulomb_r, dmat_r
+    from oracle.rpa_oracle import r_grid
+    s = load_he_exx()
+    inp = oracle_input(s)
+    rl = r_grid(inp.period)
+    tv = _threshold_between(coulomb_r(inp, s.v_cut, rl))
+    td = _threshold_between(dmat_r(inp, 0, rl))
+    h = L.Handler()
+    L.load_system(h, s)
+    o = L.Options(nfreq=16, tfgrids_type=L.Minimax, libri_exx_threshold_V=tv, libri_exx_threshold_D=td)
+    got = h.get_exx_pot_kgrid(o, s.n_spins, list(range(s.n_kpts)), 0, s.n_bands)
+    ref = exx_kgrid(inp, s.v_cut, thr_v=tv, thr_d=td)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-10)
+    assert np.abs(ref - exx_kgrid(inp, s.v_cut)).max() > 1e-4
+
+
+def test_self_energy_block_filters_match_the_oracle(h2o, bn_shrink):
+    """libri_g0w0_threshold_G / _Wc drop the G(R, +-tau) and W(R, tau) blocks LibRI's set_Gs /
+    set_Ws filters drop (gw.cpp:459-616), on the Gamma-point chain (H2O) and the k-grid chain (BN
+    with the shrink): FP64, against the oracle with the same filters (Sigma_c(i omega) to 1e-9),
+    and different from the unfiltered result."""
+    s, r0 = h2o
+    thr = dict(libri_g0w0_threshold_G=2e-3, libri_g0w0_threshold_Wc=2e-3)
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  n_params_anacon=s.n_params_anacon, **thr)
+    h.get_g0w0_sigc_kgrid(o, s.n_spins, [0], 0, s.n_bands, s.vxc.reshape(s.n_spins, 1, -1),
+                          h.get_exx_pot_kgrid(o, s.n_spins, [0], 0, s.n_bands))
+    r = g0w0_gamma(oracle_input(s), s.v_cut, s.vxc, OOpts(nfreq=s.nfreq), n_params=s.n_params_anacon,
+                   thr_w=2e-3, thr_g=2e-3)
+    iw = h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq)
+    np.testing.assert_allclose(iw, r["sigc_iw"][0], rtol=0, atol=1e-9)
+    assert np.abs(iw - r0["sigc_iw"][0]).max() > 1e-6
+
+    b, _ = bn_shrink
+    h = L.Handler()
+    L.load_system(h, b)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    o = L.Options(nfreq=b.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  n_params_anacon=b.n_params_anacon, use_shrink_abfs=1,
+                  sqrt_coulomb_threshold=b.sqrt_coulomb_threshold, **thr)
+    ks = list(range(b.n_kpts))
+    h.get_g0w0_sigc_kgrid(o, b.n_spins, ks, 0, b.n_bands, b.vxc.reshape(b.n_spins, b.n_kpts, -1),
+                          h.get_exx_pot_kgrid(o, b.n_spins, ks, 0, b.n_bands))
+    rb = g0w0_kgrid(oracle_input(b), b.v_cut, b.vxc, OOpts(nfreq=b.nfreq), n_params=b.n_params_anacon,
+                    sqrt_threshold=b.sqrt_coulomb_threshold, thr_w=2e-3, thr_g=2e-3)
+    np.testing.assert_allclose(h.g0w0_sigc_iw(0, 0, b.n_bands, b.nfreq), rb["sigc_iw"][0][0], rtol=0, atol=1e-9)
