@@ -205,7 +205,38 @@ std::vector<double> fit_weights(int n, const std::vector<double> &tau, const std
                 psi[i] = 2.0 * omega[ip] / (x[i] * x[i] + omega[ip] * omega[ip]);
         }
         std::vector<double> Ain = A;
-        jacobi_svd(A, num_x, n, S, V);
+        // Householder QR first (A = Q R, psi <- Q^T psi), then the one-sided Jacobi SVD of the
+        // n x n factor R = U_r S V^T: the same singular triplets as A's (U = Q U_r) at a sweep cost
+        // of n^3 instead of n^2 num_x.
+        for (int k = 0; k < n; ++k)
+        {
+            double *ak = &A[static_cast<size_t>(k) * num_x];
+            double nrm = 0.0;
+            for (int i = k; i < num_x; ++i) nrm += ak[i] * ak[i];
+            nrm = std::sqrt(nrm);
+            if (nrm == 0.0) continue;
+            const double alpha = ak[k] > 0 ? -nrm : nrm;
+            // v = a_k(k:) - alpha e_k, H = I - 2 v v^T / (v^T v)
+            const double v0 = ak[k] - alpha;
+            const double vtv = nrm * nrm - ak[k] * ak[k] + v0 * v0;
+            ak[k] = v0;
+            if (vtv > 0.0)
+            {
+                auto reflect = [&](double *y) {
+                    double d = 0.0;
+                    for (int i = k; i < num_x; ++i) d += ak[i] * y[i];
+                    const double f = 2.0 * d / vtv;
+                    for (int i = k; i < num_x; ++i) y[i] -= f * ak[i];
+                };
+                for (int j = k + 1; j < n; ++j) reflect(&A[static_cast<size_t>(j) * num_x]);
+                reflect(psi.data());
+            }
+            ak[k] = alpha;
+        }
+        std::vector<double> R(static_cast<size_t>(n) * n, 0.0);
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i <= j; ++i) R[static_cast<size_t>(j) * n + i] = A[static_cast<size_t>(j) * num_x + i];
+        jacobi_svd(R, n, n, S, V);
         // w = sum_j V[:, j] * S_j/(reg^2+S_j^2) * (u_j . psi),  u_j = A_j / S_j, over the
         // numerical rank: singular values below num_x * eps * S_max are dropped, the rank rule
         // of a least-squares solver.  GreenX keeps them all, which only matters for fits that are
@@ -220,9 +251,10 @@ std::vector<double> fit_weights(int n, const std::vector<double> &tau, const std
         for (int j = 0; j < n; ++j)
         {
             if (!(S[j] > s_floor)) continue;
+            // u_j . psi = (U_r)_j . (Q^T psi)(0:n)
             double ut = 0.0;
-            const double *a = &A[static_cast<size_t>(j) * num_x];
-            for (int i = 0; i < num_x; ++i) ut += a[i] * psi[i];
+            const double *a = &R[static_cast<size_t>(j) * n];
+            for (int i = 0; i < n; ++i) ut += a[i] * psi[i];
             ut /= S[j];
             const double f = S[j] / (reg * reg + S[j] * S[j]) * ut;
             for (int k = 0; k < n; ++k) w[k] += V[static_cast<size_t>(j) * n + k] * f;
