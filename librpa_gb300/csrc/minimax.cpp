@@ -180,21 +180,23 @@ std::vector<double> fit_weights(int n, const std::vector<double> &tau, const std
     for (int i = 0; i < num_x; ++i) x[i] = emin * std::pow(x_factor, i);
     std::vector<double> W(static_cast<size_t>(n) * n, 0.0);
     std::vector<double> errs(n, 0.0);
+    // the x-dependent factor of the basis functions is the same for every point: exp(-x tau_j)
+    // (types 1, 3) or 2 x / (x^2 + omega_j^2) (type 2), [j][i]
+    std::vector<double> base(static_cast<size_t>(num_x) * n);
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < num_x; ++i)
+            base[static_cast<size_t>(j) * num_x + i] =
+                ttype == 2 ? 2.0 * x[i] / (x[i] * x[i] + omega[j] * omega[j]) : std::exp(-x[i] * tau[j]);
     // one least-squares fit per point ip, independent of the others: spread over host threads
     auto fit_point = [&](int ip) {
         std::vector<double> A(static_cast<size_t>(num_x) * n), psi(num_x), S, V;
         for (int j = 0; j < n; ++j)
+        {
+            const double f = ttype == 1 ? std::cos(omega[ip] * tau[j])
+                                        : ttype == 2 ? std::cos(tau[ip] * omega[j]) : std::sin(omega[ip] * tau[j]);
             for (int i = 0; i < num_x; ++i)
-            {
-                double a;
-                if (ttype == 1)
-                    a = std::cos(omega[ip] * tau[j]) * std::exp(-x[i] * tau[j]);
-                else if (ttype == 2)
-                    a = std::cos(tau[ip] * omega[j]) * 2.0 * x[i] / (x[i] * x[i] + omega[j] * omega[j]);
-                else
-                    a = std::sin(omega[ip] * tau[j]) * std::exp(-x[i] * tau[j]);
-                A[static_cast<size_t>(j) * num_x + i] = a;
-            }
+                A[static_cast<size_t>(j) * num_x + i] = f * base[static_cast<size_t>(j) * num_x + i];
+        }
         for (int i = 0; i < num_x; ++i)
         {
             if (ttype == 1)
