@@ -308,7 +308,8 @@ std::string minimax_table_path()
 static TimeFreqGrids minimax_grids_uncached(int n, double emin, double emax, double reg);
 
 // The grids are a pure function of (n, e_min, e_max, regularisation): repeated E_c calls on the
-// same system reuse the last few results instead of refitting (the fit costs tens of ms).
+// same systems reuse the results of up to 256 windows (a few MB) instead of refitting (the fit
+// costs milliseconds to tens of ms); the cache is emptied when it is full.
 namespace {
 using GridKey = std::tuple<int, double, double, double>;
 std::mutex g_grid_mu;
@@ -333,7 +334,7 @@ TimeFreqGrids minimax_grids(int n, double emin, double emax, double reg)
     }
     TimeFreqGrids g = minimax_grids_uncached(n, emin, emax, reg);
     std::lock_guard<std::mutex> lk(mu);
-    if (cache.size() >= 16) cache.clear();
+    if (cache.size() >= 256) cache.clear();
     cache.emplace(key, g);
     return g;
 }
