@@ -356,3 +356,29 @@ def test_self_energy_block_filters_match_the_oracle(h2o, bn_shrink):
     rb = g0w0_kgrid(oracle_input(b), b.v_cut, b.vxc, OOpts(nfreq=b.nfreq), n_params=b.n_params_anacon,
                     sqrt_threshold=b.sqrt_coulomb_threshold, thr_w=2e-3, thr_g=2e-3)
     np.testing.assert_allclose(h.g0w0_sigc_iw(0, 0, b.n_bands, b.nfreq), rb["sigc_iw"][0][0], rtol=0, atol=1e-9)
+
+
+def test_precision_change_rebuilds_the_self_energy(h2o):
+    """The kept self-energy belongs to the precisions it was built with: switching
+    sigma_precision on the handler rebuilds it (and gives what a fresh handler gives)."""
+    s, _ = h2o
+    h = L.Handler()
+    L.load_system(h, s)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64))
+    o = _opts(s)
+    nb = s.n_bands
+    vexx = h.get_exx_pot_kgrid(o, s.n_spins, [0], 0, nb)
+    vxc = s.vxc.reshape(s.n_spins, 1, nb)
+    h.get_g0w0_sigc_kgrid(o, s.n_spins, [0], 0, nb, vxc, vexx)
+    iw64 = h.g0w0_sigc_iw(0, 0, nb, s.nfreq)
+    h.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64,
+                                        sigma_precision=L.SIGMA_BF16X3))
+    h.get_g0w0_sigc_kgrid(o, s.n_spins, [0], 0, nb, vxc, vexx)
+    iw_split = h.g0w0_sigc_iw(0, 0, nb, s.nfreq)
+    assert 0 < np.abs(iw_split - iw64).max() * HA2EV < 1e-3
+    h2 = L.Handler()
+    L.load_system(h2, s)
+    h2.set_gb300_options(L.gb300_options(chi0_precision=L.CHI0_FP64, ec_path=L.EC_LU_FP64,
+                                         sigma_precision=L.SIGMA_BF16X3))
+    h2.get_g0w0_sigc_kgrid(o, s.n_spins, [0], 0, nb, vxc, h2.get_exx_pot_kgrid(o, s.n_spins, [0], 0, nb))
+    np.testing.assert_allclose(h2.g0w0_sigc_iw(0, 0, nb, s.nfreq), iw_split, rtol=0, atol=1e-12)
