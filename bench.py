@@ -360,12 +360,12 @@ def run_gb300(args, s, ws, rank, local, dist):
         "clocks": clk.summary(),
     }
     del h
-    if ws == 1 and args.north_star:
-        line["north_star_256"] = run_north_star(L, lib, torch, local, args)
+    if ws == 1 and args.sc256:
+        line["sc256_g"] = run_sc256(L, lib, torch, local, args)
     print(json.dumps(line), flush=True)
 
 
-def run_north_star(L, lib, torch, local, args):
+def run_sc256(L, lib, torch, local, args):
     """The 256-atom Gamma cell (13 NAO / 40 ABF per atom, C decay 1.5 A, 16 minimax points): the
     default path over 3 timed steps (grids fitted every step), the plain FP64 GPU path once (the
     denominator of the wall-time target), and the block-screened paths: the plain threshold
@@ -446,7 +446,7 @@ def main():
     ap.add_argument("--sharded", action="store_true",
                     help="split one E_c over the ranks (tau slices, a q-keyed reduce-scatter, q slices) "
                          "instead of running independent replicas")
-    ap.add_argument("--no-north-star", dest="north_star", action="store_false",
+    ap.add_argument("--no-sc256", dest="sc256", action="store_false",
                     help="skip the 256-atom sub-record (default path, FP64 denominator, screening)")
     args = ap.parse_args()
     ws, rank, local, dist = _dist()

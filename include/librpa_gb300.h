@@ -32,7 +32,7 @@ extern "C" {
                                              rule); log block features and norms for training */
 #define LIBRPA_GB300_SCREEN_MLP 2         /* contract only blocks a trained MLP predicts above the
                                              threshold, plus a random audit share of the others;
-                                             the threshold rule stays the judge and the fallback */
+                                             the threshold rule still decides and is the fallback */
 
 typedef struct
 {
