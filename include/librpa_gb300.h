@@ -211,6 +211,9 @@ int librpa_gb300_mlp_loss_grad(const float *params, const float *norm, const flo
  * states [i_state_low, i_state_high) of spin ispin.  Returns 0 on success. */
 int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
                                   double *im);
+/* The same at k-point ik of the SCF grid. */
+int librpa_gb300_get_g0w0_sigc_iw_k(LibrpaHandler *h, int ispin, int ik, int i_state_low, int i_state_high, double *re,
+                                    double *im);
 
 /* No counterpart in the reference (the internal interpolate_dielec_func,
  * src/core/dielecmodel.cpp:65-104, exposed for checking): the macroscopic dielectric function

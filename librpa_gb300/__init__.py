@@ -139,7 +139,7 @@ EXPORTS = [
     "librpa_gb300_get_chi0_block", "librpa_gb300_device_count", "librpa_gb300_selftest_tc_gemm",
     "librpa_gb300_tc_gemm_noalloc", "librpa_gb300_train_screening", "librpa_gb300_screening_samples",
     "librpa_gb300_get_screening_samples", "librpa_gb300_add_screening_samples", "librpa_gb300_get_screening_model",
-    "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw", "librpa_gb300_get_rpa_correlation_energy_batch",
+    "librpa_gb300_clear_grid_cache", "librpa_gb300_get_g0w0_sigc_iw", "librpa_gb300_get_g0w0_sigc_iw_k", "librpa_gb300_get_rpa_correlation_energy_batch",
     "librpa_gb300_set_shrink_basis", "librpa_gb300_set_shrink_sinvS", "librpa_gb300_set_shrink_lri_coeff",
     "librpa_gb300_set_screening_model",
     "librpa_gb300_clear_screening", "librpa_gb300_mlp_loss_grad", "librpa_gb300_chi0_qw_elems",
@@ -199,6 +199,7 @@ def load_library(path: str | Path | None = None):
         "librpa_build_g0w0_sigma": (None, [vp, C.POINTER(LibrpaOptions)]),
         "librpa_get_g0w0_sigc_kgrid": (None, [vp, C.POINTER(LibrpaOptions), i, i, _ip, i, i, _dp, _dp, _dp, _dp]),
         "librpa_gb300_get_g0w0_sigc_iw": (i, [vp, i, i, i, _dp, _dp]),
+        "librpa_gb300_get_g0w0_sigc_iw_k": (i, [vp, i, i, i, i, _dp, _dp]),
         "librpa_gb300_get_rpa_correlation_energy_batch": (i, [vp, i, vp, i, _dp]),
         "librpa_gb300_set_shrink_basis": (None, [vp, i, np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]),
         "librpa_gb300_set_shrink_sinvS": (None, [vp, i, i, i, _dp, _dp]),
@@ -449,11 +450,11 @@ class Handler:
         self._check()
         return (re + 1j * im).reshape(n_spins, len(iks), nc)
 
-    def g0w0_sigc_iw(self, ispin, lo, hi, nfreq):
-        """KS-diagonal Sigma_c(i omega) [state][omega] of the last G0W0 build."""
+    def g0w0_sigc_iw(self, ispin, lo, hi, nfreq, ik=0):
+        """KS-diagonal Sigma_c(i omega) [state][omega] of the last G0W0 build at SCF k-point ik."""
         re = np.zeros((hi - lo) * nfreq)
         im = np.zeros_like(re)
-        if self.lib.librpa_gb300_get_g0w0_sigc_iw(self.h, ispin, lo, hi, re, im) != 0:
+        if self.lib.librpa_gb300_get_g0w0_sigc_iw_k(self.h, ispin, ik, lo, hi, re, im) != 0:
             raise LibrpaError(self.last_error())
         return (re + 1j * im).reshape(hi - lo, nfreq)
 

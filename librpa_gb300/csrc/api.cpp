@@ -999,9 +999,9 @@ void librpa_build_g0w0_sigma(LibrpaHandler *h, const LibrpaOptions *p_opts)
 
 // No counterpart in the reference: the KS-diagonal Sigma_c(i omega) that the quasi-particle step
 // continues, after librpa_build_g0w0_sigma; [state][omega] for states [lo, hi) of one spin at
-// k-point 0 (the Gamma point, or the first point of a k-grid).
-int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
-                                  double *im)
+// k-point ik of the SCF grid (k-point 0 without the _k suffix).
+int librpa_gb300_get_g0w0_sigc_iw_k(LibrpaHandler *h, int ispin, int ik, int i_state_low, int i_state_high, double *re,
+                                    double *im)
 {
     int rc = 1;
     guarded(h, [&] {
@@ -1009,20 +1009,28 @@ int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, 
         GB_REQUIRE(!ds->sigc_ks.empty() && ds->g0w0_generation == ds->generation,
                    "no self-energy: call librpa_build_g0w0_sigma first");
         GB_REQUIRE(ispin >= 0 && ispin < static_cast<int>(ds->sigc_ks.size()), "spin index out of range");
-        GB_REQUIRE(0 <= i_state_low && i_state_low <= i_state_high && i_state_high <= ds->n_states,
-                   "state range out of range");
+        const int nw = static_cast<int>(ds->gw_omega.size()), nb = ds->n_states;
+        const int nk = static_cast<int>(ds->sigc_ks[ispin].size() / (static_cast<size_t>(nb) * nw));
+        GB_REQUIRE(ik >= 0 && ik < nk, "k-point index out of range");
+        GB_REQUIRE(0 <= i_state_low && i_state_low <= i_state_high && i_state_high <= nb, "state range out of range");
         GB_REQUIRE(re && im, "null array");
-        const int nw = static_cast<int>(ds->gw_omega.size());
+        const cplx *src = ds->sigc_ks[ispin].data() + static_cast<size_t>(ik) * nb * nw;
         for (int n = i_state_low; n < i_state_high; ++n)
             for (int w = 0; w < nw; ++w)
             {
-                const cplx v = ds->sigc_ks[ispin][static_cast<size_t>(n) * nw + w];
+                const cplx v = src[static_cast<size_t>(n) * nw + w];
                 re[static_cast<size_t>(n - i_state_low) * nw + w] = v.real();
                 im[static_cast<size_t>(n - i_state_low) * nw + w] = v.imag();
             }
         rc = 0;
     });
     return rc;
+}
+
+int librpa_gb300_get_g0w0_sigc_iw(LibrpaHandler *h, int ispin, int i_state_low, int i_state_high, double *re,
+                                  double *im)
+{
+    return librpa_gb300_get_g0w0_sigc_iw_k(h, ispin, 0, i_state_low, i_state_high, re, im);
 }
 
 // compute_g0w0.cpp:168-260: Sigma_c of states [i_state_low, i_state_high) at the quasi-particle

@@ -272,7 +272,10 @@ def test_bn_shrink_g0w0_tables(bn_shrink):
     s, r = bn_shrink
     h, vexx, vxc, sig = _bn_run(s, L.CHI0_FP64)
     np.testing.assert_allclose(vexx[0], r["vexx"][0], rtol=0, atol=1e-10)
-    np.testing.assert_allclose(h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq), r["sigc_iw"][0][0], rtol=0, atol=1e-9)
+    for ik in range(s.n_kpts):  # librpa_gb300_get_g0w0_sigc_iw_k at every SCF k-point
+        np.testing.assert_allclose(h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq, ik), r["sigc_iw"][0][ik], rtol=0, atol=1e-9)
+    with pytest.raises(L.LibrpaError, match="k-point index out of range"):
+        h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq, s.n_kpts)
     np.testing.assert_allclose(sig[0], r["sigc"][0], rtol=0, atol=1e-7)
     t = s.qp_tables
     e_qp = s.ekb - vxc + vexx + sig.real
