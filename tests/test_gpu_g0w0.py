@@ -276,6 +276,16 @@ def test_bn_shrink_g0w0_tables(bn_shrink):
         np.testing.assert_allclose(h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq, ik), r["sigc_iw"][0][ik], rtol=0, atol=1e-9)
     with pytest.raises(L.LibrpaError, match="k-point index out of range"):
         h.g0w0_sigc_iw(0, 0, s.n_bands, s.nfreq, s.n_kpts)
+    # band k-points on three SCF points (task = g0w0_band with the shrink) reproduce their results
+    o = L.Options(nfreq=s.nfreq, tfgrids_type=L.Minimax, parallel_routing=L.LIBRI,
+                  n_params_anacon=s.n_params_anacon, use_shrink_abfs=1,
+                  sqrt_coulomb_threshold=s.sqrt_coulomb_threshold)
+    kb = [0, 3, 7]
+    h.set_band_points(h_kfrac(s)[kb], s.wg[:, kb], s.ekb[:, kb], s.wfc[:, kb])
+    vb = h.get_exx_pot_band_k(o, s.n_spins, [0, 1, 2], 0, s.n_bands)
+    np.testing.assert_allclose(vb, vexx[:, kb], rtol=0, atol=1e-9)
+    sb = h.get_g0w0_sigc_band_k(o, s.n_spins, [0, 1, 2], 0, s.n_bands, vxc[:, kb], vb)
+    np.testing.assert_allclose(sb, sig[:, kb], rtol=0, atol=1e-8)
     np.testing.assert_allclose(sig[0], r["sigc"][0], rtol=0, atol=1e-7)
     t = s.qp_tables
     e_qp = s.ekb - vxc + vexx + sig.real
