@@ -27,7 +27,10 @@ oracle's chi0(q, omega):
 g0w0_kgrid extends the chain to k-grids: W_c at the IBZ q-points (with the head of the
 dielectric matrix replaced by eps_mac at Gamma when asked), the q -> R transform with the
 time-reversed partners (FT_Wc_freq_q, epsilon.cpp:2323-2488), Sigma_c(R) shifted to the nearest
-BvK image and summed into Sigma_c(k) (gw.cpp:1010-1140).
+BvK image and summed into Sigma_c(k) (gw.cpp:1010-1140).  A shrunk input (inp.sinvS) forms chi0
+and W_c in the small ABF basis and unfolds W_c as U^H W_c U for the self-energy
+(src/gw_old.cpp:55-280), its exchange on the small basis's RI coefficients; LibRI's block
+filters (thr_v / thr_d, thr_w / thr_g) drop the blocks set_Vs / set_Ds / set_Ws / set_Gs drop.
 
 Pinned by the reference's own regression outputs: the H2O molecule (24 states, 16 minimax
 points, 16 Pade parameters; tests/golden/h2o_g0w0.npz), the spin-polarised Li atom

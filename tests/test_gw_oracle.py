@@ -229,3 +229,18 @@ def test_wc_is_vcut_half_epsinv_minus_one_vcut_half():
     chi = -0.01 * (B @ B.T)
     W = wc_freq(chi, V, V)
     np.testing.assert_allclose(W, np.linalg.solve(np.eye(8) - V @ chi, V) - V, atol=1e-10)
+
+
+def test_block_filters_are_identity_at_zero_and_empty_above_every_block():
+    """LibRI's block filter restated (drop_small): threshold 0 keeps every block; a threshold above
+    every block's max-norm drops them all, and the exchange built from no density matrix blocks is
+    zero."""
+    import numpy as np
+    from conftest import load_he_exx, oracle_input
+    from oracle.gw_oracle import drop_small, exx_kgrid
+    blocks = {(0, 0, (0, 0, 0)): np.array([[1.0, -2.0]]), (0, 1, (0, 0, 0)): np.array([[0.5]])}
+    assert drop_small(blocks, 0.0) is blocks
+    assert list(drop_small(blocks, 1.0)) == [(0, 0, (0, 0, 0))]
+    assert drop_small(blocks, 2.0) == {}
+    s = load_he_exx()
+    assert np.abs(exx_kgrid(oracle_input(s), s.v_cut, thr_d=1e9)).max() == 0.0
